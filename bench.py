@@ -1,0 +1,444 @@
+"""Benchmark of the DBSR_MAT3 Hamiltonian-block assembly on GB300.
+
+One step = one assembled channel-pair matrix: hch zeroed, the R^k/S^k
+tables rebuilt, and every coefficient list of the workload passed through
+Gen_matrix (R^k direct/exchange for k=0..10, S^k structures 6 and 8 for
+both PQ types).  Default workload: 400 B-splines (ks=9, P order 8, Q order
+9), r_max=40, Z=26, 20 bound orbitals, 120 channels (7260 blocks of
+800x800 FP64 = 37.2 GB), about 1.8e6 unique angular coefficients over 5%
+of the (channel pair, k) slots -- seeded synthetic data, no public dataset
+(see dbsr_gb300/synth.py).
+
+Output: one JSON line (rank 0).  value = algorithmic GFLOP/s of the
+reference's own loop counts (2 x multiply-adds of convol + density) per
+assembled matrix, with the lists and orbitals resident in device memory;
+e2e = the same with the lists copied from pinned host memory inside the
+timed region and the assembled matrix copied back to pinned host memory.
+``--impl reference`` times the CPU restatement of the reference
+(oracle/, the reference itself needs a Fortran compiler and an external
+library that this image lacks) on a bounded sample of the same workload
+with all host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+if HERE not in sys.path:
+    sys.path.insert(0, HERE)
+
+METRIC = "H-block assembly s and GFLOP/s: mixed-prec vs FP64 on GPU at ≤1e-10 rel err"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=3)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--precision", default="plain", choices=["plain", "split"])
+    p.add_argument("--scale", type=float, default=1.0, help="fraction of the 2e6 entries")
+    p.add_argument("--nch", type=int, default=120)
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU sample")
+    return p.parse_args()
+
+
+# ---------------------------------------------------------------------------
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self) -> dict:
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        self.f.flush()
+        self.f.seek(0)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f.read().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        os.unlink(self.f.name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(HERE, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d, "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+def fp64_peak_tflops(torch, dev) -> float:
+    """Measured FP64 dense-matmul throughput (cuBLAS DGEMM 8192^3), the
+    denominator of the FP64 contraction kernels."""
+    n = 8192
+    a = torch.randn(n, n, dtype=torch.float64, device=dev)
+    b = torch.randn(n, n, dtype=torch.float64, device=dev)
+    for _ in range(2):
+        torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 1e9
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1) / 1e3)
+    del a, b
+    torch.cuda.empty_cache()
+    return 2 * n ** 3 / best / 1e12
+
+
+# ---------------------------------------------------------------------------
+def cpu_sample(w, budget_s: float, threads: int = 1):
+    """Time the CPU restatement on a bounded sample of the workload: the
+    first segments of one direct, one exchange and two S^k lists at k=2
+    (with the tables they need), and extrapolate per algorithmic FLOP.
+    Returns (GFLOP/s, seconds per full matrix, description)."""
+    from dbsr_gb300 import synth
+    from oracle import oracle as O
+
+    ns, ks = w.ns, w.ks
+    Ts = ks * ns - ks * (ks - 1) // 2
+    Tn = (2 * ks - 1) * ns - ks * (ks - 1)
+    g = O.Grid(w.t, w.ks, w.ksp, w.ksq)
+    m = O.Matrix(g, w.pq, w.ipbs, w.nch, w.icc, w.mk)
+    want = {(2, 3, 2): 6, (2, 4, 2): 1, (3, 6, 2): 1, (3, 8, 2): 1}
+    t_tab = 0.0
+    t0 = time.perf_counter()
+    # tables first (timed separately; the reference builds each once per run)
+    for typ in range(4):
+        m_t = time.perf_counter()
+        g.mrk(typ, 2)
+        t_tab += time.perf_counter() - m_t
+    n_tab_built = 4
+    for typ in range(2):
+        m_t = time.perf_counter()
+        g.msk(typ, 2)
+        t_tab += time.perf_counter() - m_t
+    n_tab_built += 2
+    flops, t_seg, desc = 0.0, 0.0, []
+    for L in w.lists:
+        key = (L.icase, L.itype, L.kpol)
+        if key not in want or L.n == 0:
+            continue
+        segs = np.flatnonzero(np.r_[True, L.k1[1:] != L.k1[:-1]])
+        nseg = min(want[key], segs.size)
+        end = segs[nseg] if nseg < segs.size else L.n
+        sub = slice(0, end)
+        # warm the table cache of the Matrix (not timed)
+        m.gen_matrix(L.icase, L.itype, L.kpol, L.k1[:1], L.k2[:1], L.k3[:1], L.k4[:1], L.c[:1])
+        ts = time.perf_counter()
+        m.gen_matrix(L.icase, L.itype, L.kpol, L.k1[sub], L.k2[sub], L.k3[sub], L.k4[sub],
+                     L.c[sub])
+        t_seg += time.perf_counter() - ts
+        if L.icase == 2:
+            flops += 4 * nseg * 2 * (Ts * Ts if L.itype == 3 else Tn * Tn)
+            flops += 4 * end * 2 * ns * (ks if L.itype == 3 else ns)
+        else:
+            flops += nseg * 2 * Tn * Tn + end * 2 * ns * ((2 * ks - 1) if L.itype % 10 <= 7 else ns)
+        desc.append(f"{key}:{nseg}seg")
+        if time.perf_counter() - t0 > budget_s:
+            break
+    rate = flops / t_seg
+    fl = synth.algorithmic_flops(w)
+    n_tables = 4 * (w.mk + 1) + 2 * (w.mk + 2)
+    full_s = fl["total"] / rate + t_tab / n_tab_built * n_tables
+    return rate / 1e9, full_s, (
+        f"oracle (CPU restatement, -O2, 1 thread) on {', '.join(desc)} at k=2 "
+        f"({t_seg:.1f} s) plus 6 table builds ({t_tab:.1f} s); extrapolated per algorithmic "
+        f"FLOP to the full matrix ({fl['total'] / 1e12:.2f} TFLOP) and {n_tables} tables")
+
+
+def _ref_worker(args):
+    """One reference-arm worker: the oracle on a slice of segments."""
+    ws, key, lo, hi = args
+    from oracle import oracle as O
+
+    w = ws
+    g = O.Grid(w.t, w.ks, w.ksp, w.ksq)
+    m = O.Matrix(g, w.pq, w.ipbs, w.nch, w.icc, w.mk)
+    for L in w.lists:
+        if (L.icase, L.itype, L.kpol) == key:
+            sub = slice(lo, hi)
+            m.gen_matrix(L.icase, L.itype, L.kpol, L.k1[sub], L.k2[sub], L.k3[sub], L.k4[sub],
+                         L.c[sub])
+    return 0
+
+
+def reference_arm(args, w):
+    """The reference's CPU path (its restatement: the Fortran reference
+    cannot be built here) on all host cores, each step a bounded sample:
+    the first segments of the k=2 direct and exchange R^k lists, split
+    over worker processes (tables built inside each worker, as a serial
+    reference run does)."""
+    import multiprocessing as mp
+
+    from dbsr_gb300 import synth
+
+    ns, ks = w.ns, w.ks
+    Ts = ks * ns - ks * (ks - 1) // 2
+    Tn = (2 * ks - 1) * ns - ks * (ks - 1)
+    cores = os.cpu_count() or 1
+    # work items: one exchange segment or four direct segments per worker
+    items, flops = [], 0.0
+    for L in w.lists:
+        key = (L.icase, L.itype, L.kpol)
+        if key not in ((2, 3, 2), (2, 4, 2)):
+            continue
+        segs = list(np.flatnonzero(np.r_[True, L.k1[1:] != L.k1[:-1]])) + [L.n]
+        per = 4 if L.itype == 3 else 1
+        take = cores // 2
+        for i in range(take):
+            a, b = i * per, (i + 1) * per
+            if b >= len(segs):
+                break
+            items.append((w, key, int(segs[a]), int(segs[b])))
+            nseg = per
+            ne = int(segs[b] - segs[a])
+            flops += 4 * nseg * 2 * (Ts * Ts if L.itype == 3 else Tn * Tn)
+            flops += 4 * ne * 2 * ns * (ks if L.itype == 3 else ns)
+    ctx = mp.get_context("spawn")
+    times = []
+    with ctx.Pool(min(cores, len(items))) as pool:
+        for s in range(args.warmup + args.steps):
+            t0 = time.perf_counter()
+            pool.map(_ref_worker, items)
+            dt = time.perf_counter() - t0
+            if s >= args.warmup:
+                times.append(dt)
+    dt = max(times)
+    v = flops / dt / 1e9
+    sample = (f"oracle restatement, {len(items)} worker processes on {cores} cores: first "
+              f"segments of the k=2 R^k direct and exchange lists incl. their table builds, "
+              f"{flops / 1e9:.1f} GFLOP algorithmic per step")
+    return {
+        "metric": METRIC, "value": v, "unit": "GFLOP/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "impl": "reference",
+        "config": {"workload": w.name, "sample": "k=2 R^k direct+exchange segments"},
+        "cpu_baseline": {"value": v, "unit": "GFLOP/s", "cores": min(cores, len(items)),
+                         "kind": "port", "sample": sample},
+        "e2e": {"value": v, "unit": "GFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+# ---------------------------------------------------------------------------
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+
+    from dbsr_gb300 import synth
+
+    w = synth.config1(scale=args.scale, nch=args.nch)
+
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps(reference_arm(args, w)), flush=True)
+        return
+
+    import torch
+
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=dev)
+        pg = dist
+
+    from dbsr_gb300 import PLAIN_FP64, SPLIT_BF16, Assembler
+
+    a = Assembler(w.t, w.ks, w.ksp, w.ksq, device=local)
+    a.set_orbitals(w.pq, w.ipbs)
+    a.alloc_matrix(w.nch, w.icc, w.iicc, w.mk)
+    a.set_precision(SPLIT_BF16 if args.precision == "split" else PLAIN_FP64)
+    # device-resident lists
+    dl = []
+    for L in w.lists:
+        t = [torch.from_numpy(np.ascontiguousarray(x)).to(dev) for x in (L.k1, L.k2, L.k3, L.k4)]
+        c = torch.from_numpy(np.ascontiguousarray(L.c)).to(dev)
+        dl.append((L.icase, L.itype, L.kpol, *t, c))
+    torch.cuda.synchronize()
+
+    def step(lists):
+        a.zero_matrix()
+        a.release_tables()
+        for (ic, it, kp, k1, k2, k3, k4, c) in lists:
+            a.gen_matrix(ic, it, kp, k1, k2, k3, k4, c)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if pg is not None:
+            pg.barrier()
+
+    def timed(fn, n):
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(n):
+            fn()
+        e1.record()
+        barrier()
+        dt = e0.elapsed_time(e1) / 1e3 / n
+        if pg is not None:
+            t = torch.tensor([dt], device=dev)
+            pg.all_reduce(t, op=pg.ReduceOp.MAX)
+            dt = float(t.item())
+        return dt
+
+    for _ in range(args.warmup):
+        step(dl)
+    l0 = a.launches
+    clk = Clocks(local)
+    clk.start()
+    dt = timed(lambda: step(dl), args.steps)
+    clocks = clk.stop()
+    launches = (a.launches - l0) // max(1, args.steps)
+
+    fl = synth.algorithmic_flops(w)
+    value = world * fl["total"] / dt / 1e9
+
+    # per-kernel device time of one instrumented step (outside the timed region)
+    a.timing(True)
+    step(dl)
+    rep = a.timing_report()
+    a.timing(False)
+    top = max(rep.items(), key=lambda kv: kv[1][1])
+    tot_ms = sum(v[1] for v in rep.values())
+
+    peaks, peak_kind = measured_peaks()
+    if args.precision == "plain":
+        p64 = fp64_peak_tflops(torch, dev)
+        # algorithmic FLOPs of the contraction kernels (convol) over their time
+        conv_ms = sum(rep.get(k, (0, 0.0))[1] for k in ("k_exchange", "k_band_contract"))
+        n_top = top[1][0]
+        if top[0] in ("k_exchange", "k_band_contract"):
+            share = rep[top[0]][1] / max(conv_ms, 1e-9)
+            per_launch = fl["convol"] * share / max(n_top, 1)
+            achieved = per_launch / (top[1][1] / n_top / 1e3) / 1e12
+        else:
+            achieved = float("nan")
+        roofline = {"bound": "fp64", "kernel": top[0], "achieved": achieved, "peak": p64,
+                    "unit": "TFLOP/s", "frac": achieved / p64,
+                    "peak_source": "measured cuBLAS DGEMM 8192^3 on this GPU",
+                    "traffic": None, "launches": n_top, "avg_launch_ms": top[1][1] / n_top,
+                    "share_of_step": top[1][1] / tot_ms}
+    else:
+        roofline = {}
+
+    # e2e: lists from pinned host memory, matrix back to pinned host memory
+    e2e = None
+    if not args.no_e2e:
+        hl = []
+        h2d = 0
+        for L in w.lists:
+            t = [torch.from_numpy(np.ascontiguousarray(x)).pin_memory() for x in
+                 (L.k1, L.k2, L.k3, L.k4)]
+            c = torch.from_numpy(np.ascontiguousarray(L.c)).pin_memory()
+            h2d += sum(x.numel() * 4 for x in t[:3]) + c.numel() * 8
+            hl.append((L.icase, L.itype, L.kpol, *[x.numpy() for x in t], c.numpy()))
+        hout = torch.empty(w.iicc * a.ms * a.ms, dtype=torch.float64).pin_memory()
+        hout_np = hout.numpy()
+
+        def e2e_step():
+            step(hl)
+            a.get_matrix(out=hout_np)
+
+        e2e_step()
+        dte = timed(e2e_step, 1)
+        e2e = {"value": world * fl["total"] / dte / 1e9, "unit": "GFLOP/s",
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(hout.numel() * 8),
+               "s_per_matrix": dte}
+        del hout
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        gf, full_s, desc = cpu_sample(w, args.cpu_budget)
+        cpu = {"value": gf, "unit": "GFLOP/s", "cores": 1, "kind": "port", "sample": desc,
+               "s_per_matrix_extrapolated": full_s}
+
+    if rank == 0:
+        out = {
+            "metric": METRIC, "value": value, "unit": "GFLOP/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if args.precision == "plain" else "bf16-split/f32-acc/f64",
+            "data": "synthetic",
+            "config": {"workload": w.name, "precision": args.precision, "ns": w.ns,
+                       "nch": w.nch, "blocks": w.iicc, "lists": len(w.lists),
+                       "entries": int(sum(L.n for L in w.lists)),
+                       "matrix_gb": w.iicc * a.ms * a.ms * 8 / 1e9,
+                       "algorithmic_tflop": fl["total"] / 1e12,
+                       "l2": "inputs and output larger than L2 (hch 37 GB)",
+                       "parallelism": f"replicas x{world}"},
+            "s_per_matrix": dt,
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "clocks": clocks,
+            "gpu_launches": int(launches),
+            "kernel_ms": {k: round(v[1], 3) for k, v in sorted(rep.items(), key=lambda kv: -kv[1][1])},
+            "peaks": {"source": peak_kind, "bf16_tflops": peaks.get("bf16_tflops"),
+                      "hbm_gbs": peaks.get("hbm_gbs")},
+        }
+        print(json.dumps(out), flush=True)
+    a.close()
+    if pg is not None:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,201 @@
+"""Host-side mirror of the reference's Gen_matrix interface.
+
+``Assembler`` owns one library context: the B-spline grid of one partial
+wave, the orbitals (module DBS_orbitals_pq), the channel-pair matrix
+(hch/icc/acf of module dbsr_mat) and the cached R^k/S^k tables.  Its
+methods carry the reference's names and argument meaning:
+
+* ``gen_matrix(icase, itype, kpol, k1, k2, k3, k4, cdata, ipt=None)`` --
+  Gen_matrix (DBSR_MAT3/gen_matrix.f90:2-17) for a list laid out as
+  Add_matrix leaves it (MOD_c_data.f90:318-368);
+* ``update_hx(ich, jch, d, c)`` -- UPDATE_HX (updates.f90:79-106);
+* ``get_block(ich, jch)`` -- block icc(ich,jch) of hch(ms,ms,:).
+
+Arrays may be numpy arrays (host; the library copies them) or torch CUDA
+tensors (device; used in place).  Errors raise ``DbsrgError`` where the
+reference would stop.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import check, load
+
+PLAIN_FP64 = 0
+SPLIT_BF16 = 1
+RK = 0
+SK = 1
+
+
+def _ptr(a, dtype):
+    """(pointer, keepalive) for a numpy array or a torch tensor."""
+    if a is None:
+        return None, None
+    if hasattr(a, "data_ptr") and hasattr(a, "is_cuda"):
+        if not a.is_contiguous():
+            raise ValueError("torch tensor arguments must be contiguous")
+        want = {np.float64: "float64", np.int32: "int32"}[dtype]
+        if str(a.dtype).split(".")[-1] != want:
+            raise TypeError(f"expected torch.{want}, got {a.dtype}")
+        return C.c_void_p(a.data_ptr()), a
+    arr = np.asarray(a)
+    if arr.dtype != dtype or not (arr.flags.c_contiguous or arr.flags.f_contiguous):
+        arr = np.array(arr, dtype=dtype, order="F")
+    return C.c_void_p(arr.ctypes.data), arr
+
+
+class Assembler:
+    def __init__(self, t, ks: int = 9, ksp: int = 8, ksq: int = 9, device: int = 0):
+        L = load()
+        t = np.ascontiguousarray(t, dtype=np.float64)
+        self.ks, self.ksp, self.ksq = ks, ksp, ksq
+        self.ns = t.size - ks
+        self.nv = self.ns - ks + 1
+        self.ms = 2 * self.ns
+        d = _lib.GridDesc(self.ns, ks, ksp, ksq, C.c_void_p(t.ctypes.data), device)
+        h = C.c_void_p()
+        rc = L.dbsrg_create(C.byref(h), C.byref(d))
+        check(None, rc, "dbsrg_create")
+        self._h = h
+        self._L = L
+        self.nch = 0
+        self.iicc = 0
+        self.mk = -1
+        self.nbf = 0
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.dbsrg_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # -- state ------------------------------------------------------------
+    def set_orbitals(self, pq, ipbs):
+        """pq(ns,2,nbf) in Fortran order; ipbs(nbf) channel of each orbital."""
+        if not hasattr(pq, "data_ptr"):
+            pq = np.asfortranarray(pq, dtype=np.float64)
+        nbf = int(pq.shape[-1]) if pq.ndim == 3 else int(pq.size // (2 * self.ns))
+        p, k1 = _ptr(pq, np.float64)
+        q, k2 = _ptr(np.ascontiguousarray(ipbs, dtype=np.int32), np.int32)
+        check(self._h, self._L.dbsrg_set_orbitals(self._h, nbf, p, q), "set_orbitals")
+        self.nbf = nbf
+
+    def alloc_matrix(self, nch: int, icc, iicc: int, mk: int):
+        icc = np.asfortranarray(icc, dtype=np.int32)
+        p, keep = _ptr(icc, np.int32)
+        check(self._h, self._L.dbsrg_alloc_matrix(self._h, nch, p, iicc, mk), "alloc_matrix")
+        self.nch, self.iicc, self.mk = nch, iicc, mk
+        self.icc = icc
+
+    def zero_matrix(self):
+        check(self._h, self._L.dbsrg_zero_matrix(self._h), "zero_matrix")
+
+    def set_precision(self, mode: int):
+        check(self._h, self._L.dbsrg_set_precision(self._h, mode), "set_precision")
+
+    # -- the drop-in ----------------------------------------------------------
+    def gen_matrix(self, icase, itype, kpol, k1, k2, k3, k4, cdata, ipt=None):
+        n = int(len(k1))
+        ptrs, keep = [], []
+        for a, dt in ((ipt, np.int32), (k1, np.int32), (k2, np.int32), (k3, np.int32),
+                      (k4, np.int32), (cdata, np.float64)):
+            p, kk = _ptr(a, dt)
+            ptrs.append(p)
+            keep.append(kk)
+        rc = self._L.dbsrg_gen_matrix(self._h, icase, itype, kpol, n, *ptrs)
+        check(self._h, rc, f"gen_matrix(icase={icase},itype={itype},kpol={kpol})")
+
+    def update_hx(self, ich, jch, d, c):
+        p, keep = _ptr(np.asfortranarray(d, dtype=np.float64) if not hasattr(d, "data_ptr") else d,
+                       np.float64)
+        check(self._h, self._L.dbsrg_update_hx(self._h, ich, jch, p, float(c)), "update_hx")
+
+    # -- results --------------------------------------------------------------
+    def get_block(self, ich, jch):
+        out = np.zeros((self.ms, self.ms), order="F")
+        check(self._h, self._L.dbsrg_get_block(self._h, ich, jch, C.c_void_p(out.ctypes.data)),
+              "get_block")
+        return out
+
+    def get_matrix(self, out=None):
+        if out is None:
+            out = np.zeros((self.ms, self.ms, self.iicc), order="F")
+        p, keep = _ptr(out, np.float64)
+        check(self._h, self._L.dbsrg_get_matrix(self._h, p), "get_matrix")
+        return out
+
+    def get_acf(self):
+        out = np.zeros((self.iicc, self.mk + 1), order="F")
+        check(self._h, self._L.dbsrg_get_acf(self._h, C.c_void_p(out.ctypes.data)), "get_acf")
+        return out
+
+    def matrix_device_ptr(self) -> int:
+        p = C.c_void_p()
+        check(self._h, self._L.dbsrg_matrix_device_ptr(self._h, C.byref(p)), "matrix_device_ptr")
+        return int(p.value)
+
+    def get_table(self, family: int, typ: int, k: int):
+        kb = self.ks if family == RK else 2 * self.ks - 1
+        out = np.zeros((self.ns, self.ns, kb, kb), order="F")
+        rc = self._L.dbsrg_get_table(self._h, family, typ, k, C.c_void_p(out.ctypes.data))
+        check(self._h, rc, "get_table")
+        return out
+
+    def get_moments(self, which: int, k: int):
+        kk = self.ks * self.ks
+        out = np.zeros((kk, self.nv), order="F")
+        check(self._h, self._L.dbsrg_get_moments(self._h, which, k, C.c_void_p(out.ctypes.data)),
+              "get_moments")
+        return out
+
+    def get_diag_cells(self, typ: int, k: int):
+        kk = self.ks * self.ks
+        out = np.zeros((kk, kk, self.nv), order="F")
+        rc = self._L.dbsrg_get_diag_cells(self._h, typ, k, C.c_void_p(out.ctypes.data))
+        check(self._h, rc, "get_diag_cells")
+        return out
+
+    def grid_array(self, name: str):
+        nv, ks, ns, ms = self.nv, self.ks, self.ns, self.ms
+        shapes = {"gr": (nv, ks), "grw": (nv, ks), "grm": (nv, ks), "gx": (ks,), "gw": (ks,),
+                  "pbsp": (nv + 1, ks, self.ksp), "qbsp": (nv + 1, ks, self.ksq),
+                  "fpbs": (ns, ns), "fqbs": (ns, ns), "fppqq": (ms, ms)}
+        out = np.zeros(shapes[name], order="F")
+        rc = self._L.dbsrg_get_grid_array(self._h, name.encode(), C.c_void_p(out.ctypes.data))
+        check(self._h, rc, "grid_array")
+        return out
+
+    def release_tables(self):
+        check(self._h, self._L.dbsrg_release_tables(self._h), "release_tables")
+
+    def timing(self, enable: bool = True):
+        check(self._h, self._L.dbsrg_timing(self._h, int(enable)), "timing")
+
+    def timing_report(self) -> dict:
+        """{kernel: (launches, total ms)} of the launches since timing(True)."""
+        import json
+
+        buf = C.create_string_buffer(1 << 16)
+        check(self._h, self._L.dbsrg_timing_report(self._h, buf, len(buf)), "timing_report")
+        return {k: (int(v[0]), float(v[1])) for k, v in json.loads(buf.value.decode()).items()}
+
+    @property
+    def launches(self) -> int:
+        return int(self._L.dbsrg_kernel_launches(self._h))
+
+    def sync(self):
+        check(self._h, self._L.dbsrg_sync(self._h), "sync")

@@ -1,0 +1,811 @@
+// assemble.cu -- the plain-FP64 Gen_matrix path: density accumulation per
+// channel-pair segment, contraction with the R^k/S^k tables and the ordered
+// scatter into the channel-pair blocks, following
+//   R_data itype 3/4  DBSR_MAT3/R_data.f90:56-86, 214-277
+//   S_data itype 6-9  DBSR_MAT3/S_data.f90:67-113, 240-274
+//   O_data itype 3    DBSR_MAT3/O_data.f90:50-61
+//   UPDATE_HS/HW/HX   DBSR_MAT3/updates.f90:79-216
+//
+// Work decomposition (one Gen_matrix call):
+//   1. the list is copied to the device in Add_matrix (IPT) order;
+//   2. k_segments marks the runs of equal K1 (one channel pair each) --
+//      the reference flushes a segment when the next K1 differs;
+//   3. k_density_acc forms xx = sum_e c_e * density(e) for every segment
+//      and atype, entries in list order;
+//   4. the contraction: band products (convol cases 1/2) as a tiled FP64
+//      product over all segments sharing one table, exchange (cases 3/4)
+//      as a gather per output element batched over segments;
+//   5. k_scatter adds the results into hch.  One thread owns one hch
+//      element and applies the contributions in the reference's order
+//      (atype-major, then list order), so no atomics are needed and the
+//      result is deterministic.
+#include "internal.cuh"
+
+#include <algorithm>
+
+namespace {
+
+constexpr int kSegChunk = 256;  // segments per contraction/scatter pass
+
+struct SegInfo {
+  int start, end;  // entry range [start,end)
+  int ich, jch;    // channel pair decoded from K1
+  int blk;         // 1-based block from icc, 0 if invalid
+  int partner;     // other segment of this list mapping to the same block, or -1
+  int owner;       // 1 if this segment applies the block's contributions
+};
+
+// ---------------------------------------------------------------------------
+// list gather into IPT order
+__global__ void k_gather(int n, const int *ipt, const int *k1, const int *k2, const int *k3,
+                         const double *c, int *o1, int *o2, int *o3, double *oc) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  int i = ipt ? ipt[e] - 1 : e;
+  o1[e] = k1[i];
+  o2[e] = k2[i];
+  o3[e] = k3[i];
+  oc[e] = c[i];
+}
+
+// segment starts: positions where K1 differs from the previous entry.
+// Single thread block; counts per thread chunk, block scan, then writes.
+__global__ void k_segments(int n, const int *k1, int *seg_start, int *nseg_out) {
+  __shared__ int cnt[1024];
+  int tid = threadIdx.x, nt = blockDim.x;
+  int chunk = (n + nt - 1) / nt;
+  int lo = tid * chunk, hi = min(n, lo + chunk);
+  int c = 0;
+  for (int p = lo; p < hi; p++)
+    if (p == 0 || k1[p] != k1[p - 1]) c++;
+  cnt[tid] = c;
+  __syncthreads();
+  // inclusive scan (Hillis-Steele)
+  for (int off = 1; off < nt; off <<= 1) {
+    int v = tid >= off ? cnt[tid - off] : 0;
+    __syncthreads();
+    cnt[tid] += v;
+    __syncthreads();
+  }
+  int base = cnt[tid] - c;
+  for (int p = lo; p < hi; p++)
+    if (p == 0 || k1[p] != k1[p - 1]) seg_start[base++] = p;
+  if (tid == nt - 1) {
+    seg_start[cnt[tid]] = n;
+    *nseg_out = cnt[tid];
+  }
+}
+
+// bound-orbital indices of every entry must address pq(:,:,1:nbf)
+__global__ void k_check_orbitals(int n, const int *k2, const int *k3, int nbf, int *err) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  if (k2[e] < 1 || k2[e] > nbf || k3[e] < 1 || k3[e] > nbf) atomicExch(err, 1);
+}
+
+// decode segments, look up blocks, pair up segments of the same block
+__global__ void k_seg_info(int nseg, const int *seg_start, const int *k1, int nch, int iicc,
+                           const int *icc, SegInfo *info, int *err) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nseg) return;
+  SegInfo si;
+  si.start = seg_start[s];
+  si.end = seg_start[s + 1];
+  int key = k1[si.start];
+  si.ich = key / DBSRG_IBO;
+  si.jch = key % DBSRG_IBO;
+  si.blk = 0;
+  si.partner = -1;
+  si.owner = 1;
+  if (si.ich < 1 || si.jch < 1 || si.ich > nch || si.jch > nch) {
+    atomicExch(err, 1);
+  } else {
+    int b = icc[(si.ich - 1) + (size_t)nch * (si.jch - 1)];
+    if (b < 1 || b > iicc)
+      atomicExch(err, 2);
+    else
+      si.blk = b;
+    if (si.ich != si.jch) {
+      // the swapped pair maps to the same block; binary search its K1
+      int want = si.jch * DBSRG_IBO + si.ich;
+      int lo = 0, hi = nseg - 1;
+      while (lo <= hi) {
+        int mid = (lo + hi) >> 1;
+        int v = k1[seg_start[mid]];
+        if (v == want) {
+          si.partner = mid;
+          break;
+        }
+        if (v < want)
+          lo = mid + 1;
+        else
+          hi = mid - 1;
+      }
+      if (si.partner >= 0 && si.partner < s) si.owner = 0;
+    }
+  }
+  info[s] = si;
+}
+
+// ---------------------------------------------------------------------------
+// density accumulation (density, dbsr_lib_dbs.f90:2834-2891; the
+// xx = xx + cdata*dd loops of R_data.f90:217-220 / S_data.f90:244-246).
+// xx layout: [atype][segment][ns*ncol], column-major per segment.
+struct DensSpec {
+  int jp1[4], jp2[4];  // components (1 P, 2 Q) of the two bound orbitals
+};
+
+__global__ void k_density_acc(int ns, int ks, char sym, int ncol, int na, DensSpec spec,
+                              int nm, const int *members, const SegInfo *info, const int *k2,
+                              const int *k3, const double *cd, const double *pq,
+                              double *xx) {
+  size_t per = (size_t)ns * ncol;
+  size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= per) return;
+  const int slot = blockIdx.y;
+  int s = members[slot];
+  int a = blockIdx.z;
+  int i = (int)(q % ns) + 1, j = (int)(q / ns) + 1;  // 1-based (i,j) of d(i,j)
+  const SegInfo si = info[s];
+  const double *P1base = pq + (size_t)ns * (spec.jp1[a] - 1);
+  const double *P2base = pq + (size_t)ns * (spec.jp2[a] - 1);
+  double acc = 0.0;
+  for (int e = si.start; e < si.end; e++) {
+    const double *p1 = P1base + (size_t)2 * ns * (k2[e] - 1) - 1;  // 1-based view
+    const double *p2 = P2base + (size_t)2 * ns * (k3[e] - 1) - 1;
+    double d;
+    if (sym == 's') {
+      if (j == 1)
+        d = p1[i] * p2[i];
+      else if (i <= ns - j + 1)
+        d = p1[i] * p2[i + j - 1] + p1[i + j - 1] * p2[i];
+      else
+        d = 0.0;
+    } else if (sym == 'n') {
+      int imin = max(1, 1 + ks - j), imax = min(ns, ns + ks - j);
+      d = (i >= imin && i <= imax) ? p1[i] * p2[i + j - ks] : 0.0;
+    } else {
+      d = p1[i] * p2[j];
+    }
+    acc = acc + cd[e] * d;
+  }
+  xx[((size_t)a * nm + slot) * per + q] = acc;
+}
+
+// ---------------------------------------------------------------------------
+// band contraction, convol cases 1 and 2 (dbsr_lib_dbs.f90:2243-2338 and
+// :2517-2608): for every segment n of the chunk
+//   case 1: a(i,ip) = sum_{j,jp} d(j,jp) rkb(i,j,ip,jp)
+//   case 2: a(j,jp) = sum_{i,ip} d(i,ip) rkb(i,j,ip,jp)
+// as one product over all segments that share the table: rows r=(i,ip),
+// columns n, contraction over (j,jp).  Tiles: 64 rows x 64 segments x 16,
+// 256 threads with 4x4 outputs each.
+constexpr int GBM = 64, GBN = 64, GBK = 16;
+
+__global__ void __launch_bounds__(256) k_band_contract(int ns, int kb, int icase,
+                                                      const double *__restrict__ rkb,
+                                                      int nsg, const double *__restrict__ X,
+                                                      double *__restrict__ A) {
+  __shared__ double Rs[GBK][GBM + 1];
+  __shared__ double Xs[GBK][GBN + 1];
+  const int nrt = (ns + GBM - 1) / GBM;  // row tiles per band column
+  const int rt = blockIdx.x % nrt;
+  const int obp = blockIdx.x / nrt;  // output band column (ip for case 1)
+  const int n0 = blockIdx.y * GBN;
+  const int r0 = rt * GBM;
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  const size_t per = (size_t)ns * kb;
+  const size_t ns2 = (size_t)ns * ns;
+  double acc[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; a++)
+#pragma unroll
+    for (int b = 0; b < 4; b++) acc[a][b] = 0.0;
+  for (int cbp = 0; cbp < kb; cbp++) {  // contracted band column
+    for (int c0 = 0; c0 < ns; c0 += GBK) {
+      // table tile: rows r0..r0+63 (output index), cols c0..c0+15
+      for (int q = threadIdx.x; q < GBK * GBM; q += 256) {
+        int rr = q % GBM, cc = q / GBM;
+        int r = r0 + rr, cidx = c0 + cc;
+        double v = 0.0;
+        if (r < ns && cidx < ns) {
+          size_t off;
+          if (icase == 1)  // rkb(r, cidx, obp, cbp)
+            off = (size_t)r + (size_t)ns * cidx + ns2 * ((size_t)obp + (size_t)kb * cbp);
+          else  // rkb(cidx, r, cbp, obp)
+            off = (size_t)cidx + (size_t)ns * r + ns2 * ((size_t)cbp + (size_t)kb * obp);
+          v = rkb[off];
+        }
+        Rs[cc][rr] = v;
+      }
+      for (int q = threadIdx.x; q < GBK * GBN; q += 256) {
+        int cc = q % GBK, nn = q / GBK;
+        int cidx = c0 + cc, n = n0 + nn;
+        double v = 0.0;
+        if (cidx < ns && n < nsg) v = X[(size_t)n * per + cidx + (size_t)ns * cbp];
+        Xs[cc][nn] = v;
+      }
+      __syncthreads();
+#pragma unroll
+      for (int kk = 0; kk < GBK; kk++) {
+        double rv[4], xv[4];
+#pragma unroll
+        for (int a = 0; a < 4; a++) rv[a] = Rs[kk][ty * 4 + a];
+#pragma unroll
+        for (int b = 0; b < 4; b++) xv[b] = Xs[kk][tx * 4 + b];
+#pragma unroll
+        for (int a = 0; a < 4; a++)
+#pragma unroll
+          for (int b = 0; b < 4; b++) acc[a][b] = fma(rv[a], xv[b], acc[a][b]);
+      }
+      __syncthreads();
+    }
+  }
+#pragma unroll
+  for (int a = 0; a < 4; a++) {
+    int r = r0 + ty * 4 + a;
+    if (r >= ns) continue;
+#pragma unroll
+    for (int b = 0; b < 4; b++) {
+      int n = n0 + tx * 4 + b;
+      if (n < nsg) A[(size_t)n * per + r + (size_t)ns * obp] = acc[a][b];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// exchange contraction, convol case 3 with 's','s' storage
+// (dbsr_lib_dbs.f90:2344-2356) and cases 3/4 with 'n','n' storage
+// (:2370-2378, :2418-2426; convol_sk :2632-2640, :2690-2698), written as a
+// gather: one thread owns output a(x,y) of NB segments and sums the table
+// entries that the reference scatters into it.
+constexpr int XNB = 4;
+
+__global__ void __launch_bounds__(256) k_exchange(int ns, int ks, int mode, int nsg,
+                                                 const double *__restrict__ rkb,
+                                                 const double *__restrict__ D,
+                                                 double *__restrict__ A) {
+  size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const size_t nn = (size_t)ns * ns;
+  if (q >= nn) return;
+  const int x = (int)(q % ns) + 1, y = (int)(q / ns) + 1;  // 1-based output (x,y)
+  const int sb = blockIdx.y * XNB;
+  const int nb = min(XNB, nsg - sb);
+  const double *Db = D + (size_t)sb * nn;
+  double acc[XNB];
+#pragma unroll
+  for (int b = 0; b < XNB; b++) acc[b] = 0.0;
+  auto TB = [&](int i, int j, int ip, int jp, int kb) -> double {
+    return __ldg(&rkb[(size_t)(i - 1) + (size_t)ns * ((size_t)(j - 1) +
+                       (size_t)ns * ((size_t)(ip - 1) + (size_t)kb * (size_t)(jp - 1)))]);
+  };
+  auto DV = [&](int b, int i, int j) -> double {
+    return __ldg(&Db[(size_t)b * nn + (size_t)(i - 1) + (size_t)ns * (size_t)(j - 1)]);
+  };
+  if (mode == 0) {  // R table, 's','s', case 3: four symmetric terms
+    for (int jp = 1; jp <= ks; jp++) {
+      for (int ip = 1; ip <= ks; ip++) {
+        // T1: a(i,jj) += c*d(ii,j), i=x, jj=y -> j=y-jp+1, ii=x+ip-1
+        if (y - jp + 1 >= 1 && x + ip - 1 <= ns) {
+          double c = TB(x, y - jp + 1, ip, jp, ks);
+#pragma unroll
+          for (int b = 0; b < XNB; b++)
+            if (b < nb) acc[b] = fma(c, DV(b, x + ip - 1, y - jp + 1), acc[b]);
+        }
+        // T2 (ip>1): a(ii,jj) += c*d(i,j): ii=x -> i=x-ip+1, jj=y -> j=y-jp+1
+        if (ip > 1 && x - ip + 1 >= 1 && y - jp + 1 >= 1) {
+          double c = TB(x - ip + 1, y - jp + 1, ip, jp, ks);
+#pragma unroll
+          for (int b = 0; b < XNB; b++)
+            if (b < nb) acc[b] = fma(c, DV(b, x - ip + 1, y - jp + 1), acc[b]);
+        }
+        // T3 (jp>1): a(i,j) += c*d(ii,jj): i=x, j=y
+        if (jp > 1 && x + ip - 1 <= ns && y + jp - 1 <= ns) {
+          double c = TB(x, y, ip, jp, ks);
+#pragma unroll
+          for (int b = 0; b < XNB; b++)
+            if (b < nb) acc[b] = fma(c, DV(b, x + ip - 1, y + jp - 1), acc[b]);
+        }
+        // T4 (ip>1,jp>1): a(ii,j) += c*d(i,jj): ii=x -> i=x-ip+1, j=y
+        if (ip > 1 && jp > 1 && x - ip + 1 >= 1 && y + jp - 1 <= ns) {
+          double c = TB(x - ip + 1, y, ip, jp, ks);
+#pragma unroll
+          for (int b = 0; b < XNB; b++)
+            if (b < nb) acc[b] = fma(c, DV(b, x - ip + 1, y + jp - 1), acc[b]);
+        }
+      }
+    }
+  } else {  // S table 'n','n' (kb = 2ks-1)
+    const int kb = 2 * ks - 1;
+    for (int jp = 1; jp <= kb; jp++) {
+      for (int ip = 1; ip <= kb; ip++) {
+        if (mode == 1) {
+          // case 3: a(i,jj) += c*d(ii,j), i=x, jj=y -> j=y-jp+ks, ii=x+ip-ks
+          int j = y - jp + ks, ii = x + ip - ks;
+          if (j < max(1, 1 + ks - jp) || j > min(ns, ns + ks - jp)) continue;
+          if (x < max(1, 1 + ks - ip) || x > min(ns, ns + ks - ip)) continue;
+          double c = TB(x, j, ip, jp, kb);
+#pragma unroll
+          for (int b = 0; b < XNB; b++)
+            if (b < nb) acc[b] = fma(c, DV(b, ii, j), acc[b]);
+        } else {
+          // case 4: a(ii,j) += c*d(i,jj), ii=x -> i=x-ip+ks, j=y, jj=y+jp-ks
+          int i = x - ip + ks, jj = y + jp - ks;
+          if (y < max(1, 1 + ks - jp) || y > min(ns, ns + ks - jp)) continue;
+          if (i < max(1, 1 + ks - ip) || i > min(ns, ns + ks - ip)) continue;
+          double c = TB(i, y, ip, jp, kb);
+#pragma unroll
+          for (int b = 0; b < XNB; b++)
+            if (b < nb) acc[b] = fma(c, DV(b, i, jj), acc[b]);
+        }
+      }
+    }
+  }
+  for (int b = 0; b < nb; b++) A[(size_t)(sb + b) * nn + q] = acc[b];
+}
+
+// ---------------------------------------------------------------------------
+// ordered scatter into hch (UPDATE_HS, updates.f90:110-179).
+struct ScatterSpec {
+  int na;           // number of contribution sets (atypes) in order
+  int ii[4], jj[4]; // target quadrant of each set
+  char sym;         // storage of the results: 's', 'n' or 'x'
+  int ncol;         // columns of one result
+};
+
+__device__ __forceinline__ double yval(const double *d, int ns, int ks, char sym, int i, int j) {
+  // element (i,j) (1-based) of the ns x ns matrix y built from d
+  if (sym == 'x') return d[(size_t)(i - 1) + (size_t)ns * (j - 1)];
+  if (sym == 's') {
+    int lo = min(i, j), dlt = abs(i - j);
+    if (dlt >= ks) return 0.0;
+    return d[(size_t)(lo - 1) + (size_t)ns * dlt];
+  }
+  int jp = j - i + ks;  // 'n'
+  if (jp < 1 || jp > 2 * ks - 1) return 0.0;
+  return d[(size_t)(i - 1) + (size_t)ns * (jp - 1)];
+}
+
+// index space: mode 0 (full): the ms x ms block; mode 1 (band): the four
+// quadrants x ns rows x (2ks-1) diagonals.
+__global__ void k_scatter(int ns, int ks, int mode, ScatterSpec sp, int nm, const int *members,
+                          const int *own_slots, const SegInfo *info, const double *Y,
+                          double *hch) {
+  const int ms = 2 * ns;
+  const int oslot = own_slots[blockIdx.y];
+  const int s = members[oslot];
+  const SegInfo si = info[s];
+  if (si.blk < 1) return;
+  // the partner, if any, is stored in the next member slot
+  const int pslot = (si.partner >= 0) ? oslot + 1 : -1;
+  size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int r, c;  // 0-based position in the ms x ms block
+  if (mode == 0) {
+    if (q >= (size_t)ms * ms) return;
+    r = (int)(q % ms);
+    c = (int)(q / ms);
+  } else {
+    const int nd = 2 * ks - 1;
+    if (q >= (size_t)4 * ns * nd) return;
+    int quad = (int)(q / ((size_t)ns * nd));
+    int rem = (int)(q % ((size_t)ns * nd));
+    int lr = rem % ns, off = rem / ns - (ks - 1);
+    int lc = lr + off;
+    if (lc < 0 || lc >= ns) return;
+    r = (quad & 1) * ns + lr;
+    c = (quad >> 1) * ns + lc;
+  }
+  const int qr = r / ns + 1, qc = c / ns + 1;
+  const int lr = r % ns + 1, lc = c % ns + 1;
+  const size_t per = (size_t)ns * sp.ncol;
+  bool touched = false;
+  double val = 0.0;
+  double *h = hch + (size_t)(si.blk - 1) * ms * ms + (size_t)r + (size_t)ms * c;
+  for (int a = 0; a < sp.na; a++) {
+    for (int pass = 0; pass < 2; pass++) {
+      int slot = pass == 0 ? oslot : pslot;
+      if (slot < 0) break;
+      const SegInfo sj = info[members[slot]];
+      const double *d = Y + ((size_t)a * nm + slot) * per;
+      const int ii = sp.ii[a], jj = sp.jj[a];
+      if (sj.ich > sj.jch) {
+        if (qr == ii && qc == jj) {
+          if (!touched) { val = *h; touched = true; }
+          val = val + yval(d, ns, ks, sp.sym, lr, lc);
+        }
+      } else if (sj.jch > sj.ich) {
+        if (qr == ii && qc == jj) {
+          if (!touched) { val = *h; touched = true; }
+          val = val + yval(d, ns, ks, sp.sym, lc, lr);
+        }
+      } else {
+        if (qr == ii && qc == jj) {
+          if (!touched) { val = *h; touched = true; }
+          val = val + yval(d, ns, ks, sp.sym, lr, lc) / 2.0;
+        }
+        if (qr == jj && qc == ii) {
+          if (!touched) { val = *h; touched = true; }
+          val = val + yval(d, ns, ks, sp.sym, lc, lr) / 2.0;
+        }
+      }
+    }
+  }
+  if (touched) *h = val;
+}
+
+// asymptotic coefficients (UPDATE_ACF, R_data.f90:223-240): one thread per
+// owner segment, atypes 0 and 1, list order.
+__global__ void k_acf(int nseg_owner, const int *owners, const SegInfo *info, int kpol,
+                      int nbf, const int *k2, const int *k3, const double *cd,
+                      const double *quad, double *acf, int iicc) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nseg_owner) return;
+  int s = owners[t];
+  SegInfo si = info[s];
+  if (si.blk < 1) return;
+  double *dst = acf + (size_t)(si.blk - 1) + (size_t)iicc * kpol;
+  for (int a = 0; a < 2; a++) {
+    for (int pass = 0; pass < 2; pass++) {
+      int ss = pass == 0 ? s : si.partner;
+      if (pass == 1 && ss < 0) break;
+      SegInfo sj = info[ss];
+      double CA = 0.0;
+      for (int e = sj.start; e < sj.end; e++) {
+        double S = quad[(size_t)(k2[e] - 1) + (size_t)nbf * ((k3[e] - 1) + (size_t)nbf * a)];
+        CA = CA + cd[e] * S;
+      }
+      *dst = *dst + CA;
+    }
+  }
+}
+
+__global__ void k_owner_list(int nseg, const SegInfo *info, int *owners, int *nown) {
+  // single thread: compact the owner segments in list order
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  int c = 0;
+  for (int s = 0; s < nseg; s++)
+    if (info[s].owner) owners[c++] = s;
+  *nown = c;
+}
+
+// ---------------------------------------------------------------------------
+// O_data itype 3 (<i|.><.|j>, O_data.f90:50-61) with UPDATE_HW
+// (updates.f90:183-216).  V_ch is restated as the B-spline overlap vector
+// of the bound orbital: v(1:ns) = fpbs*P, v(ns+1:ms) = fqbs*Q.
+__global__ void k_vch(int ns, int nbf, const double *fpbs, const double *fqbs,
+                      const double *pq, double *vch) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= 2 * ns * nbf) return;
+  int i = q % (2 * ns), b = q / (2 * ns);
+  int comp = i / ns, ii = i % ns;
+  const double *F = comp == 0 ? fpbs : fqbs;
+  const double *p = pq + (size_t)2 * ns * b + (size_t)ns * comp;
+  double s = 0.0;
+  for (int j = 0; j < ns; j++) s += F[(size_t)ii + (size_t)ns * j] * p[j];
+  vch[q] = s;
+}
+
+// group entries by block, keeping list order (single thread, counting sort)
+__global__ void k_group_entries(int n, const int *k1, const int *k2, const double *cd,
+                                const int *ipbs, int nbf, const int *icc, int nch, int iicc,
+                                int *bcount, int *bstart, int *order, int *eblk, int *err) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  for (int b = 0; b <= iicc; b++) bcount[b] = 0;
+  for (int e = 0; e < n; e++) {
+    eblk[e] = 0;
+    if (fabs(cd[e]) < 1.0e-10) continue;  // eps_c, mod_dbsr_mat.f90:56
+    int i1 = k1[e] / DBSRG_IBO, j1 = k2[e] / DBSRG_IBO;
+    if (i1 < 1 || i1 > nbf || j1 < 1 || j1 > nbf) { *err = 1; continue; }
+    int ich = ipbs[i1 - 1], jch = ipbs[j1 - 1];
+    if (ich < 1 || jch < 1 || ich > nch || jch > nch) { *err = 1; continue; }
+    int b = icc[(ich - 1) + (size_t)nch * (jch - 1)];
+    if (b < 1 || b > iicc) { *err = 2; continue; }
+    eblk[e] = b;
+    bcount[b]++;
+  }
+  int acc = 0;
+  for (int b = 0; b <= iicc; b++) {
+    bstart[b] = acc;
+    acc += bcount[b];
+    bcount[b] = 0;
+  }
+  bstart[iicc + 1] = acc;
+  for (int e = 0; e < n; e++) {
+    int b = eblk[e];
+    if (b) order[bstart[b] + bcount[b]++] = e;
+  }
+}
+
+__global__ void k_overlap_update(int ns, int iicc, const int *bstart, const int *order,
+                                 const int *k1, const int *k2, const double *cd,
+                                 const int *ipbs, const double *vch, double *hch) {
+  const int ms = 2 * ns;
+  int b = blockIdx.y + 1;
+  int e0 = bstart[b], e1 = bstart[b + 1];
+  if (e0 == e1) return;
+  size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= (size_t)ms * ms) return;
+  int r = (int)(q % ms), c = (int)(q / ms);
+  double *h = hch + (size_t)(b - 1) * ms * ms + q;
+  double val = *h;
+  for (int t = e0; t < e1; t++) {
+    int e = order[t];
+    int i1 = k1[e] / DBSRG_IBO, i2 = k1[e] % DBSRG_IBO;
+    int j1 = k2[e] / DBSRG_IBO, j2 = k2[e] % DBSRG_IBO;
+    int ich = ipbs[i1 - 1], jch = ipbs[j1 - 1];
+    const double *v = vch + (size_t)ms * (i2 - 1);
+    const double *w = vch + (size_t)ms * (j2 - 1);
+    double C = cd[e], xx;
+    if (ich > jch)
+      xx = C * (v[r] * w[c]);
+    else if (jch > ich)
+      xx = C * (v[c] * w[r]);
+    else
+      xx = (C / 2.0) * (v[r] * w[c] + v[c] * w[r]);
+    val = val + xx;
+  }
+  *h = val;
+}
+
+// UPDATE_HX (updates.f90:79-106)
+__global__ void k_update_hx(int ms, int ich, int jch, const double *d, double cc, double *blk) {
+  size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= (size_t)ms * ms) return;
+  int r = (int)(q % ms), c = (int)(q / ms);
+  double x = ich >= jch ? cc * d[q] : cc * d[(size_t)c + (size_t)ms * r];
+  blk[q] = blk[q] + x;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+static int rd_err(dbsrg_ctx *c, int *derr) {
+  int h = 0;
+  DBSRG_TRY(c, cudaMemcpyAsync(&h, derr, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  DBSRG_TRY(c, cudaStreamSynchronize(c->stream));
+  if (h == 1) return set_err(c, DBSRG_ERANGE, "channel or orbital index out of range in list");
+  if (h == 2) return set_err(c, DBSRG_ERANGE, "channel pair has no block in icc");
+  return DBSRG_OK;
+}
+
+int update_hx(dbsrg_ctx *c, int ich, int jch, const double *d, double cc) {
+  const int ms = c->g.ms;
+  if (!c->hch) return set_err(c, DBSRG_ESTATE, "no matrix allocated");
+  if (ich < 1 || jch < 1 || ich > c->nch || jch > c->nch)
+    return set_err(c, DBSRG_ERANGE, "UPDATE_HX: channel out of range");
+  int b = c->h_icc[(ich - 1) + (size_t)c->nch * (jch - 1)];
+  if (b < 1 || b > c->iicc) return set_err(c, DBSRG_ERANGE, "UPDATE_HX: i out of range");
+  const double *dd = d;
+  size_t bytes = sizeof(double) * (size_t)ms * ms;
+  if (!is_device_ptr(d)) {
+    int rc = ensure_scratch2(c, bytes);
+    if (rc) return rc;
+    rc = copy_in(c, c->scratch2, d, bytes);
+    if (rc) return rc;
+    dd = (const double *)c->scratch2;
+  }
+  size_t n = (size_t)ms * ms;
+  DBSRG_RUN(c, "k_update_hx", k_update_hx<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(
+      ms, ich, jch, dd, cc, c->hch + (size_t)(b - 1) * ms * ms));
+  DBSRG_TRY(c, cudaStreamSynchronize(c->stream));
+  return DBSRG_OK;
+}
+
+int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const int *ipt,
+                     const int *k1, const int *k2, const int *k3, const int *k4,
+                     const double *cdata) {
+  (void)k4;
+  if (n <= 0) return DBSRG_OK;
+  if (!c->hch) return set_err(c, DBSRG_ESTATE, "no matrix allocated");
+  if (!c->pq) return set_err(c, DBSRG_ESTATE, "no orbitals set");
+  const DeviceGrid &g = c->g;
+  const int ns = g.ns, ks = g.ks, ms = g.ms;
+  cudaStream_t st = c->stream;
+  int rc;
+
+  // ---- 1. list in IPT order on the device (scratch2 holds the list state)
+  const size_t ibytes = sizeof(int) * (size_t)n, dbytes = sizeof(double) * (size_t)n;
+  auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  size_t tot = 7 * al(ibytes) + 2 * al(dbytes) + al(sizeof(int) * (n + 2)) + al(64) +
+               al(sizeof(SegInfo) * (size_t)(n + 1)) + 3 * al(sizeof(int) * (size_t)(n + 1));
+  if ((rc = ensure_scratch2(c, tot))) return rc;
+  char *base = (char *)c->scratch2;
+  auto take = [&](size_t bytes) {
+    char *p = base;
+    base += al(bytes);
+    return (void *)p;
+  };
+  int *dk1 = (int *)take(ibytes), *dk2 = (int *)take(ibytes), *dk3 = (int *)take(ibytes);
+  double *dcd = (double *)take(dbytes);
+  int *dipt = (int *)take(ibytes);
+  int *lk1 = (int *)take(ibytes), *lk2 = (int *)take(ibytes), *lk3 = (int *)take(ibytes);
+  double *lcd = (double *)take(dbytes);
+  int *seg_start = (int *)take(sizeof(int) * (size_t)(n + 2));
+  int *dscal = (int *)take(64);  // [0]=nseg [1]=err [2]=nown
+  SegInfo *info = (SegInfo *)take(sizeof(SegInfo) * (size_t)(n + 1));
+  int *owners = (int *)take(sizeof(int) * (size_t)(n + 1));
+  int *members = (int *)take(sizeof(int) * (size_t)(2 * (n + 1)));  // members + owner slots
+  if ((rc = copy_in(c, dk1, k1, ibytes))) return rc;
+  if ((rc = copy_in(c, dk2, k2, ibytes))) return rc;
+  if ((rc = copy_in(c, dk3, k3, ibytes))) return rc;
+  if ((rc = copy_in(c, dcd, cdata, dbytes))) return rc;
+  if (ipt && (rc = copy_in(c, dipt, ipt, ibytes))) return rc;
+  DBSRG_TRY(c, cudaMemsetAsync(dscal, 0, 64, st));
+  DBSRG_RUN(c, "k_gather", k_gather<<<(n + 255) / 256, 256, 0, st>>>(n, ipt ? dipt : nullptr, dk1, dk2, dk3, dcd, lk1,
+                                            lk2, lk3, lcd));
+
+  // ---- overlaps
+  if (icase == 0) {
+    if (itype != 3) return set_err(c, DBSRG_EINVAL, "O_data: only itype 3 is supported");
+    size_t vbytes = sizeof(double) * (size_t)ms * c->nbf;
+    rc = ensure_scratch(c, vbytes + sizeof(int) * ((size_t)2 * n + 2 * (c->iicc + 2)) + 1024);
+    if (rc) return rc;
+    double *vch = (double *)c->scratch;
+    int *bcount = (int *)(vch + (size_t)ms * c->nbf);
+    int *bstart = bcount + (c->iicc + 2);
+    int *order = bstart + (c->iicc + 2);
+    int *eblk = order + n;
+    DBSRG_RUN(c, "k_vch", k_vch<<<(2 * ns * c->nbf + 255) / 256, 256, 0, st>>>(ns, c->nbf, g.fpbs, g.fqbs, c->pq, vch));
+    DBSRG_RUN(c, "k_group_entries", k_group_entries<<<1, 1, 0, st>>>(n, lk1, lk2, lcd, c->ipbs, c->nbf, c->icc, c->nch,
+                                     c->iicc, bcount, bstart, order, eblk, dscal + 1));
+    dim3 grid((unsigned)(((size_t)ms * ms + 255) / 256), (unsigned)c->iicc);
+    DBSRG_RUN(c, "k_overlap_update", k_overlap_update<<<grid, 256, 0, st>>>(ns, c->iicc, bstart, order, lk1, lk2, lcd, c->ipbs,
+                                           vch, c->hch));
+    return rd_err(c, dscal + 1);
+  }
+
+  // ---- 2. segments
+  DBSRG_RUN(c, "k_check_orbitals", k_check_orbitals<<<(n + 255) / 256, 256, 0, st>>>(n, lk2, lk3, c->nbf, dscal + 1));
+  if ((rc = rd_err(c, dscal + 1))) return rc;
+  DBSRG_RUN(c, "k_segments", k_segments<<<1, 1024, 0, st>>>(n, lk1, seg_start, dscal));
+  int nseg = 0;
+  DBSRG_TRY(c, cudaMemcpyAsync(&nseg, dscal, sizeof(int), cudaMemcpyDeviceToHost, st));
+  DBSRG_TRY(c, cudaStreamSynchronize(st));
+  DBSRG_RUN(c, "k_seg_info", k_seg_info<<<(nseg + 127) / 128, 128, 0, st>>>(nseg, seg_start, lk1, c->nch, c->iicc, c->icc,
+                                                 info, dscal + 1));
+  DBSRG_RUN(c, "k_owner_list", k_owner_list<<<1, 1, 0, st>>>(nseg, info, owners, dscal + 2));
+  if ((rc = rd_err(c, dscal + 1))) return rc;
+
+  // ---- 3. contraction set-up per case
+  DensSpec dsp{};
+  ScatterSpec ssp{};
+  int na, icv, tabfam;
+  char sym_d;
+  const double *tabs[4] = {nullptr, nullptr, nullptr, nullptr};
+  if (icase == 2) {
+    if (itype != 3 && itype != 4)
+      return set_err(c, DBSRG_EINVAL, "R_data: only itypes 3 and 4 are supported");
+    if (kpol < 0 || kpol > c->mk) return set_err(c, DBSRG_ERANGE, "R_data: kpol out of range");
+    na = 4;
+    tabfam = 0;
+    icv = itype == 3 ? 1 : 3;
+    sym_d = itype == 3 ? 's' : 'x';
+    for (int a = 0; a < 4; a++) {
+      int ip1, ip2, jp1, jp2;
+      switch (a) {  // R_data.f90:73-86
+        case 0: ip1 = 1; ip2 = 1; jp1 = 1; jp2 = 1; break;
+        case 1: ip1 = 2; ip2 = 2; jp1 = 2; jp2 = 2; break;
+        case 2: ip1 = 1; ip2 = 1; jp1 = 2; jp2 = 2;
+          if (itype == 4) { ip1 = 1; ip2 = 2; jp1 = 1; jp2 = 2; }
+          break;
+        default: ip1 = 2; ip2 = 2; jp1 = 1; jp2 = 1;
+          if (itype == 4) { ip1 = 2; ip2 = 1; jp1 = 2; jp2 = 1; }
+          break;
+      }
+      dsp.jp1[a] = jp1; dsp.jp2[a] = jp2;
+      ssp.ii[a] = ip1; ssp.jj[a] = ip2;
+      if ((rc = get_rtable(c, a, kpol, &tabs[a]))) return rc;
+    }
+  } else if (icase == 3) {
+    int atype = itype / 10, it = itype % 10;
+    if (atype < 0 || atype > 1 || it < 6 || it > 9)
+      return set_err(c, DBSRG_EINVAL, "S_data: only ktypes 6-9 and 16-19 are supported");
+    if (kpol < 0 || kpol > c->mk + 1) return set_err(c, DBSRG_ERANGE, "S_data: kpol out of range");
+    int ip1, ip2, jp1, jp2, in;  // S_data.f90:74-97
+    if (atype == 0) {
+      switch (it) {
+        case 6: ip1 = 1; ip2 = 2; jp1 = 1; jp2 = 2; in = 1; break;
+        case 7: ip1 = 1; ip2 = 2; jp1 = 1; jp2 = 2; in = 2; break;
+        case 8: ip1 = 1; ip2 = 2; jp1 = 2; jp2 = 1; in = 3; break;
+        default: ip1 = 2; ip2 = 1; jp1 = 1; jp2 = 2; in = 4; break;
+      }
+    } else {
+      switch (it) {
+        case 6: ip1 = 1; ip2 = 2; jp1 = 2; jp2 = 1; in = 1; break;
+        case 7: ip1 = 2; ip2 = 1; jp1 = 1; jp2 = 2; in = 2; break;
+        case 8: ip1 = 1; ip2 = 1; jp1 = 2; jp2 = 2; in = 3; break;
+        default: ip1 = 2; ip2 = 2; jp1 = 1; jp2 = 1; in = 4; break;
+      }
+    }
+    na = 1;
+    tabfam = 1;
+    icv = in;
+    sym_d = in <= 2 ? 'n' : 'x';
+    dsp.jp1[0] = jp1; dsp.jp2[0] = jp2;
+    ssp.ii[0] = ip1; ssp.jj[0] = ip2;
+    if ((rc = get_stable(c, atype, kpol, &tabs[0]))) return rc;
+  } else {
+    return set_err(c, DBSRG_EINVAL, "unsupported icase");
+  }
+  ssp.na = na;
+  ssp.sym = sym_d;
+  const int ncol = sym_d == 's' ? ks : (sym_d == 'n' ? 2 * ks - 1 : ns);
+  ssp.ncol = ncol;
+  const int kb = tabfam == 0 ? ks : 2 * ks - 1;
+
+  // ---- chunks of owner segments, each with its partner (a channel pair
+  // listed in both orders maps to one block; both lists contribute to that
+  // block in list order within every atype, so they stay in one chunk)
+  std::vector<SegInfo> hinfo(nseg);
+  DBSRG_TRY(c, cudaMemcpyAsync(hinfo.data(), info, sizeof(SegInfo) * nseg,
+                               cudaMemcpyDeviceToHost, st));
+  DBSRG_TRY(c, cudaStreamSynchronize(st));
+  for (int s = 0; s < nseg; s++) {
+    const SegInfo &si = hinfo[s];
+    if (si.start < 0 || si.end > n || si.start >= si.end || si.blk < 1 || si.blk > c->iicc ||
+        si.partner < -1 || si.partner >= nseg)
+      return set_err(c, DBSRG_ECUDA, "inconsistent segment table");
+  }
+  const size_t per = (size_t)ns * ncol;
+  std::vector<int> mem, own;  // member segment ids; owner slot positions
+  auto flush = [&]() -> int {
+    int nm = (int)mem.size();
+    if (nm == 0) return DBSRG_OK;
+    // device copy of member ids and of the owner slots
+    std::vector<int> h(nm + own.size());
+    std::copy(mem.begin(), mem.end(), h.begin());
+    std::copy(own.begin(), own.end(), h.begin() + nm);
+    int rc2;
+    if ((rc2 = copy_in(c, members, h.data(), sizeof(int) * h.size()))) return rc2;
+    size_t need2 = 2 * sizeof(double) * per * na * nm;
+    if ((rc2 = ensure_scratch(c, need2))) return rc2;
+    double *X = (double *)c->scratch;
+    double *Y = X + per * na * nm;
+    dim3 gd((unsigned)((per + 255) / 256), (unsigned)nm, (unsigned)na);
+    DBSRG_RUN(c, "k_density_acc", k_density_acc<<<gd, 256, 0, st>>>(ns, ks, sym_d, ncol, na, dsp, nm, members, info, lk2,
+                                      lk3, lcd, c->pq, X));
+    for (int a = 0; a < na; a++) {
+      const double *Xa = X + (size_t)a * nm * per;
+      double *Ya = Y + (size_t)a * nm * per;
+      if (icv <= 2) {
+        int nrt = (ns + GBM - 1) / GBM;
+        dim3 gg((unsigned)(nrt * kb), (unsigned)((nm + GBN - 1) / GBN));
+        DBSRG_RUN(c, "k_band_contract",
+                  k_band_contract<<<gg, 256, 0, st>>>(ns, kb, icv, tabs[a], nm, Xa, Ya));
+      } else {
+        int mode = tabfam == 0 ? 0 : (icv == 3 ? 1 : 2);
+        dim3 gx((unsigned)(((size_t)ns * ns + 255) / 256), (unsigned)((nm + XNB - 1) / XNB));
+        DBSRG_RUN(c, "k_exchange",
+                  k_exchange<<<gx, 256, 0, st>>>(ns, ks, mode, nm, tabs[a], Xa, Ya));
+      }
+    }
+    int mode = sym_d == 'x' ? 0 : 1;
+    size_t space = mode == 0 ? (size_t)ms * ms : (size_t)4 * ns * (2 * ks - 1);
+    dim3 gs((unsigned)((space + 255) / 256), (unsigned)own.size());
+    DBSRG_RUN(c, "k_scatter",
+              k_scatter<<<gs, 256, 0, st>>>(ns, ks, mode, ssp, nm, members, members + nm, info,
+                                            Y, c->hch));
+    mem.clear();
+    own.clear();
+    return DBSRG_OK;
+  };
+  for (int s = 0; s < nseg; s++) {
+    if (!hinfo[s].owner) continue;
+    own.push_back((int)mem.size());
+    mem.push_back(s);
+    if (hinfo[s].partner >= 0) mem.push_back(hinfo[s].partner);
+    if ((int)mem.size() >= kSegChunk - 1)
+      if ((rc = flush())) return rc;
+  }
+  if ((rc = flush())) return rc;
+  int nown = 0;
+  for (int s = 0; s < nseg; s++) nown += hinfo[s].owner;
+  if (icase == 2 && itype == 3 && nown > 0) {
+    const double *quad;
+    if ((rc = get_quad(c, kpol, &quad))) return rc;
+    DBSRG_RUN(c, "k_acf", k_acf<<<(nown + 127) / 128, 128, 0, st>>>(nown, owners, info, kpol, c->nbf, lk2, lk3, lcd,
+                                             quad, c->acf, c->iicc));
+  }
+  DBSRG_TRY(c, cudaStreamSynchronize(st));
+  return DBSRG_OK;
+}

@@ -1,0 +1,445 @@
+// capi.cu -- the extern "C" entry points declared in include/dbsrg.h.
+#include <cstdlib>
+#include <cstring>
+#include <new>
+
+#include "internal.cuh"
+
+int set_err(dbsrg_ctx *c, int code, const std::string &msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+int cuda_check(dbsrg_ctx *c, cudaError_t e, const char *what) {
+  if (e == cudaSuccess) return DBSRG_OK;
+  std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+  if (e == cudaErrorMemoryAllocation) return set_err(c, DBSRG_ENOMEM, m);
+  return set_err(c, DBSRG_ECUDA, m);
+}
+
+bool is_device_ptr(const void *p) {
+  if (!p) return false;
+  cudaPointerAttributes a;
+  cudaError_t e = cudaPointerGetAttributes(&a, p);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+int copy_in(dbsrg_ctx *c, void *dst, const void *src, size_t n) {
+  if (n == 0) return DBSRG_OK;
+  if (!src) return set_err(c, DBSRG_EINVAL, "null input pointer");
+  cudaMemcpyKind k = is_device_ptr(src) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  DBSRG_TRY(c, cudaMemcpyAsync(dst, src, n, k, c->stream));
+  return DBSRG_OK;
+}
+
+int copy_out(dbsrg_ctx *c, void *dst, const void *src, size_t n) {
+  if (n == 0) return DBSRG_OK;
+  if (!dst) return set_err(c, DBSRG_EINVAL, "null output pointer");
+  cudaMemcpyKind k = is_device_ptr(dst) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  DBSRG_TRY(c, cudaMemcpyAsync(dst, src, n, k, c->stream));
+  DBSRG_TRY(c, cudaStreamSynchronize(c->stream));
+  return DBSRG_OK;
+}
+
+static int grow(dbsrg_ctx *c, void **p, size_t *have, size_t bytes) {
+  if (*have >= bytes) return DBSRG_OK;
+  if (*p) {
+    cudaStreamSynchronize(c->stream);
+    cudaFree(*p);
+    *p = nullptr;
+    *have = 0;
+  }
+  size_t want = bytes + bytes / 4;
+  cudaError_t e = cudaMalloc(p, want);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+      *p = nullptr;
+      return cuda_check(c, e, "scratch allocation");
+    }
+    want = bytes;
+  }
+  *have = want;
+  return DBSRG_OK;
+}
+
+int ensure_scratch(dbsrg_ctx *c, size_t bytes) {
+  return grow(c, &c->scratch, &c->scratch_bytes, bytes);
+}
+int ensure_scratch2(dbsrg_ctx *c, size_t bytes) {
+  return grow(c, &c->scratch2, &c->scratch2_bytes, bytes);
+}
+int ensure_tscratch(dbsrg_ctx *c, size_t bytes) {
+  return grow(c, &c->tscratch, &c->tscratch_bytes, bytes);
+}
+bool sync_check_enabled() {
+  static int v = -1;
+  if (v < 0) {
+    const char *e = getenv("DBSRG_SYNC_CHECK");
+    v = (e && e[0] == '1') ? 1 : 0;
+  }
+  return v == 1;
+}
+int ensure_pinned(dbsrg_ctx *c, size_t bytes) {
+  if (c->pinned_bytes >= bytes) return DBSRG_OK;
+  if (c->pinned) cudaFreeHost(c->pinned);
+  c->pinned = nullptr;
+  c->pinned_bytes = 0;
+  DBSRG_TRY(c, cudaMallocHost(&c->pinned, bytes));
+  c->pinned_bytes = bytes;
+  return DBSRG_OK;
+}
+
+cudaEvent_t event_get(dbsrg_ctx *c) {
+  cudaEvent_t e = nullptr;
+  if (!c->evpool.empty()) {
+    e = c->evpool.back();
+    c->evpool.pop_back();
+    return e;
+  }
+  cudaEventCreate(&e);
+  return e;
+}
+
+static void timing_clear(dbsrg_ctx *c) {
+  for (auto &t : c->tev) {
+    c->evpool.push_back(t.a);
+    c->evpool.push_back(t.b);
+  }
+  c->tev.clear();
+}
+
+static void free_tables(dbsrg_ctx *c) {
+  for (double *p : c->rtab)
+    if (p) cudaFree(p);
+  for (double *p : c->stab)
+    if (p) cudaFree(p);
+  for (double *p : c->quad)
+    if (p) cudaFree(p);
+  c->rtab.clear();
+  c->stab.clear();
+  c->quad.clear();
+}
+
+extern "C" {
+
+int dbsrg_create(dbsrg_ctx **out, const dbsrg_grid_desc *d) {
+  if (!out || !d) return DBSRG_EINVAL;
+  *out = nullptr;
+  if (d->ns < 2 || d->ks < 2 || d->ks > DBSRG_MAXK || d->ksp < 2 || d->ksp > d->ks ||
+      d->ksq < 2 || d->ksq > d->ks || d->ns < d->ks || !d->t)
+    return DBSRG_EINVAL;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= d->device || d->device < 0) {
+    cudaGetLastError();
+    return DBSRG_ECUDA;
+  }
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, d->device) != cudaSuccess) return DBSRG_ECUDA;
+  if (prop.major * 10 + prop.minor < 100) return DBSRG_ECUDA;  // built for sm_103a only
+  dbsrg_ctx *c = new (std::nothrow) dbsrg_ctx();
+  if (!c) return DBSRG_ENOMEM;
+  c->device = d->device;
+  if (cudaSetDevice(d->device) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete c;
+    return DBSRG_ECUDA;
+  }
+  DeviceGrid &g = c->g;
+  g.ns = d->ns;
+  g.ks = d->ks;
+  g.ksp = d->ksp;
+  g.ksq = d->ksq;
+  g.nv = g.ns - g.ks + 1;
+  g.nsp = g.nv + g.ksp - 1;
+  g.nsq = g.nv + g.ksq - 1;
+  g.ms = 2 * g.ns;
+  int rc = build_grid(c, d->t);
+  if (rc) {
+    dbsrg_destroy(c);
+    return rc;
+  }
+  *out = c;
+  return DBSRG_OK;
+}
+
+int dbsrg_destroy(dbsrg_ctx *c) {
+  if (!c) return DBSRG_OK;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  free_tables(c);
+  DeviceGrid &g = c->g;
+  double *arrs[] = {g.t, g.tp, g.tq, g.gx, g.gw, g.gr, g.grw, g.grm,
+                    g.pbsp, g.qbsp, g.fpbs, g.fqbs, g.fppqq};
+  for (double *p : arrs)
+    if (p) cudaFree(p);
+  if (c->pq) cudaFree(c->pq);
+  if (c->ipbs) cudaFree(c->ipbs);
+  if (c->icc) cudaFree(c->icc);
+  if (c->hch) cudaFree(c->hch);
+  if (c->acf) cudaFree(c->acf);
+  if (c->scratch) cudaFree(c->scratch);
+  if (c->scratch2) cudaFree(c->scratch2);
+  if (c->tscratch) cudaFree(c->tscratch);
+  if (c->pinned) cudaFreeHost(c->pinned);
+  timing_clear(c);
+  for (cudaEvent_t e : c->evpool) cudaEventDestroy(e);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return DBSRG_OK;
+}
+
+int dbsrg_release_tables(dbsrg_ctx *c) {
+  if (!c) return DBSRG_EINVAL;
+  cudaSetDevice(c->device);
+  DBSRG_TRY(c, cudaStreamSynchronize(c->stream));
+  free_tables(c);
+  return DBSRG_OK;
+}
+
+int dbsrg_timing(dbsrg_ctx *c, int enable) {
+  if (!c) return DBSRG_EINVAL;
+  DBSRG_TRY(c, cudaStreamSynchronize(c->stream));
+  timing_clear(c);
+  c->timing = enable != 0;
+  return DBSRG_OK;
+}
+
+int dbsrg_timing_report(dbsrg_ctx *c, char *buf, size_t len) {
+  if (!c || !buf || len < 3) return DBSRG_EINVAL;
+  DBSRG_TRY(c, cudaStreamSynchronize(c->stream));
+  std::vector<std::string> names;
+  std::vector<long long> cnt;
+  std::vector<double> ms;
+  for (auto &t : c->tev) {
+    float m = 0.f;
+    if (cudaEventElapsedTime(&m, t.a, t.b) != cudaSuccess) {
+      cudaGetLastError();
+      m = 0.f;
+    }
+    size_t i = 0;
+    while (i < names.size() && names[i] != t.name) i++;
+    if (i == names.size()) {
+      names.push_back(t.name);
+      cnt.push_back(0);
+      ms.push_back(0.0);
+    }
+    cnt[i]++;
+    ms[i] += m;
+  }
+  std::string s = "{";
+  for (size_t i = 0; i < names.size(); i++) {
+    char tmp[256];
+    snprintf(tmp, sizeof tmp, "%s\"%s\": [%lld, %.6f]", i ? ", " : "", names[i].c_str(), cnt[i],
+             ms[i]);
+    s += tmp;
+  }
+  s += "}";
+  if (s.size() + 1 > len) return set_err(c, DBSRG_EINVAL, "timing report buffer too small");
+  memcpy(buf, s.c_str(), s.size() + 1);
+  return DBSRG_OK;
+}
+
+const char *dbsrg_last_error(const dbsrg_ctx *c) { return c ? c->err.c_str() : "no context"; }
+
+long long dbsrg_kernel_launches(const dbsrg_ctx *c) { return c ? c->launches : 0; }
+
+int dbsrg_sync(dbsrg_ctx *c) {
+  if (!c) return DBSRG_EINVAL;
+  DBSRG_TRY(c, cudaStreamSynchronize(c->stream));
+  return DBSRG_OK;
+}
+
+int dbsrg_set_orbitals(dbsrg_ctx *c, int nbf, const double *pq, const int *ipbs) {
+  if (!c || nbf < 1 || !pq || !ipbs) return set_err(c, DBSRG_EINVAL, "bad orbital arguments");
+  cudaSetDevice(c->device);
+  if (c->pq) cudaFree(c->pq);
+  if (c->ipbs) cudaFree(c->ipbs);
+  c->pq = nullptr;
+  c->ipbs = nullptr;
+  for (double *p : c->quad)
+    if (p) cudaFree(p);
+  c->quad.clear();
+  size_t n = (size_t)2 * c->g.ns * nbf;
+  DBSRG_TRY(c, cudaMalloc((void **)&c->pq, n * sizeof(double)));
+  DBSRG_TRY(c, cudaMalloc((void **)&c->ipbs, nbf * sizeof(int)));
+  int rc = copy_in(c, c->pq, pq, n * sizeof(double));
+  if (rc) return rc;
+  c->h_ipbs.assign(nbf, 0);
+  if (is_device_ptr(ipbs)) {
+    DBSRG_TRY(c, cudaMemcpy(c->h_ipbs.data(), ipbs, nbf * sizeof(int), cudaMemcpyDeviceToHost));
+  } else {
+    std::memcpy(c->h_ipbs.data(), ipbs, nbf * sizeof(int));
+  }
+  rc = copy_in(c, c->ipbs, c->h_ipbs.data(), nbf * sizeof(int));
+  if (rc) return rc;
+  c->nbf = nbf;
+  DBSRG_TRY(c, cudaStreamSynchronize(c->stream));
+  return DBSRG_OK;
+}
+
+int dbsrg_alloc_matrix(dbsrg_ctx *c, int nch, const int *icc, int iicc, int mk) {
+  if (!c || nch < 1 || !icc || iicc < 1 || mk < 0)
+    return set_err(c, DBSRG_EINVAL, "bad matrix arguments");
+  cudaSetDevice(c->device);
+  if (c->icc) cudaFree(c->icc);
+  if (c->hch) cudaFree(c->hch);
+  if (c->acf) cudaFree(c->acf);
+  c->icc = nullptr;
+  c->hch = nullptr;
+  c->acf = nullptr;
+  c->h_icc.assign((size_t)nch * nch, 0);
+  if (is_device_ptr(icc)) {
+    DBSRG_TRY(c, cudaMemcpy(c->h_icc.data(), icc, sizeof(int) * nch * nch, cudaMemcpyDeviceToHost));
+  } else {
+    std::memcpy(c->h_icc.data(), icc, sizeof(int) * (size_t)nch * nch);
+  }
+  for (int v : c->h_icc)
+    if (v < 0 || v > iicc) return set_err(c, DBSRG_ERANGE, "icc entry out of range");
+  const size_t ms = c->g.ms;
+  DBSRG_TRY(c, cudaMalloc((void **)&c->icc, sizeof(int) * (size_t)nch * nch));
+  DBSRG_TRY(c, cudaMalloc((void **)&c->hch, sizeof(double) * ms * ms * iicc));
+  DBSRG_TRY(c, cudaMalloc((void **)&c->acf, sizeof(double) * (size_t)iicc * (mk + 1)));
+  int rc = copy_in(c, c->icc, c->h_icc.data(), sizeof(int) * (size_t)nch * nch);
+  if (rc) return rc;
+  c->nch = nch;
+  c->iicc = iicc;
+  c->mk = mk;
+  return dbsrg_zero_matrix(c);
+}
+
+int dbsrg_zero_matrix(dbsrg_ctx *c) {
+  if (!c || !c->hch) return set_err(c, DBSRG_ESTATE, "no matrix allocated");
+  const size_t ms = c->g.ms;
+  DBSRG_TRY(c, cudaMemsetAsync(c->hch, 0, sizeof(double) * ms * ms * c->iicc, c->stream));
+  DBSRG_TRY(c, cudaMemsetAsync(c->acf, 0, sizeof(double) * (size_t)c->iicc * (c->mk + 1), c->stream));
+  DBSRG_TRY(c, cudaStreamSynchronize(c->stream));
+  return DBSRG_OK;
+}
+
+int dbsrg_set_precision(dbsrg_ctx *c, int p) {
+  if (!c) return DBSRG_EINVAL;
+  if (p != DBSRG_PLAIN_FP64 && p != DBSRG_SPLIT_BF16) return set_err(c, DBSRG_EINVAL, "unknown precision");
+  c->precision = p;
+  return DBSRG_OK;
+}
+
+int dbsrg_gen_matrix(dbsrg_ctx *c, int icase, int itype, int kpol, int ncdata, const int *ipt,
+                     const int *k1, const int *k2, const int *k3, const int *k4,
+                     const double *cdata) {
+  if (!c) return DBSRG_EINVAL;
+  if (ncdata < 0) return set_err(c, DBSRG_EINVAL, "ncdata < 0");
+  if (ncdata == 0) return DBSRG_OK;
+  if (!k1 || !k2 || !k3 || !cdata) return set_err(c, DBSRG_EINVAL, "null list pointer");
+  cudaSetDevice(c->device);
+  return gen_matrix_plain(c, icase, itype, kpol, ncdata, ipt, k1, k2, k3, k4, cdata);
+}
+
+int dbsrg_update_hx(dbsrg_ctx *c, int ich, int jch, const double *d, double cc) {
+  if (!c || !d) return set_err(c, DBSRG_EINVAL, "bad UPDATE_HX arguments");
+  cudaSetDevice(c->device);
+  return update_hx(c, ich, jch, d, cc);
+}
+
+int dbsrg_get_block(dbsrg_ctx *c, int ich, int jch, double *out) {
+  if (!c || !out) return DBSRG_EINVAL;
+  if (!c->hch) return set_err(c, DBSRG_ESTATE, "no matrix allocated");
+  if (ich < 1 || jch < 1 || ich > c->nch || jch > c->nch)
+    return set_err(c, DBSRG_ERANGE, "channel out of range");
+  int b = c->h_icc[(ich - 1) + (size_t)c->nch * (jch - 1)];
+  if (b < 1) return set_err(c, DBSRG_ERANGE, "channel pair has no block");
+  const size_t ms = c->g.ms;
+  return copy_out(c, out, c->hch + (size_t)(b - 1) * ms * ms, sizeof(double) * ms * ms);
+}
+
+int dbsrg_get_matrix(dbsrg_ctx *c, double *out) {
+  if (!c || !out) return DBSRG_EINVAL;
+  if (!c->hch) return set_err(c, DBSRG_ESTATE, "no matrix allocated");
+  const size_t ms = c->g.ms;
+  return copy_out(c, out, c->hch, sizeof(double) * ms * ms * c->iicc);
+}
+
+int dbsrg_get_acf(dbsrg_ctx *c, double *out) {
+  if (!c || !out) return DBSRG_EINVAL;
+  if (!c->acf) return set_err(c, DBSRG_ESTATE, "no matrix allocated");
+  return copy_out(c, out, c->acf, sizeof(double) * (size_t)c->iicc * (c->mk + 1));
+}
+
+int dbsrg_matrix_device_ptr(dbsrg_ctx *c, double **p) {
+  if (!c || !p) return DBSRG_EINVAL;
+  if (!c->hch) return set_err(c, DBSRG_ESTATE, "no matrix allocated");
+  *p = c->hch;
+  return DBSRG_OK;
+}
+
+int dbsrg_get_table(dbsrg_ctx *c, int family, int type, int k, double *out) {
+  if (!c || !out || k < 0 || k > 64) return set_err(c, DBSRG_EINVAL, "bad table request");
+  cudaSetDevice(c->device);
+  const double *tab = nullptr;
+  int rc;
+  size_t n;
+  const size_t ns = c->g.ns, ks = c->g.ks;
+  if (family == DBSRG_RK) {
+    if (type < 0 || type > 3) return set_err(c, DBSRG_EINVAL, "R table type 0..3");
+    rc = get_rtable(c, type, k, &tab);
+    n = ns * ns * ks * ks;
+  } else if (family == DBSRG_SK) {
+    if (type < 0 || type > 1) return set_err(c, DBSRG_EINVAL, "S table type 0..1");
+    rc = get_stable(c, type, k, &tab);
+    n = ns * ns * (2 * ks - 1) * (2 * ks - 1);
+  } else {
+    return set_err(c, DBSRG_EINVAL, "unknown table family");
+  }
+  if (rc) return rc;
+  return copy_out(c, out, tab, n * sizeof(double));
+}
+
+int dbsrg_get_moments(dbsrg_ctx *c, int which, int k, double *out) {
+  if (!c || !out || which < 0 || which > 3) return set_err(c, DBSRG_EINVAL, "bad moments request");
+  cudaSetDevice(c->device);
+  const DeviceGrid &g = c->g;
+  size_t n = (size_t)g.ks * g.ks * g.nv;
+  int rc = ensure_scratch(c, n * sizeof(double));
+  if (rc) return rc;
+  if ((rc = compute_moments(c, which, k, (double *)c->scratch))) return rc;
+  return copy_out(c, out, c->scratch, n * sizeof(double));
+}
+
+int dbsrg_get_diag_cells(dbsrg_ctx *c, int type, int k, double *out) {
+  if (!c || !out || type < 0 || type > 5) return set_err(c, DBSRG_EINVAL, "bad diag-cell request");
+  cudaSetDevice(c->device);
+  const DeviceGrid &g = c->g;
+  size_t kk = (size_t)g.ks * g.ks;
+  size_t n = kk * kk * g.nv;
+  int rc = ensure_scratch(c, n * sizeof(double));
+  if (rc) return rc;
+  if ((rc = compute_diag_cells(c, type, k, (double *)c->scratch))) return rc;
+  return copy_out(c, out, c->scratch, n * sizeof(double));
+}
+
+int dbsrg_get_grid_array(dbsrg_ctx *c, const char *name, double *out) {
+  if (!c || !name || !out) return DBSRG_EINVAL;
+  const DeviceGrid &g = c->g;
+  const size_t nv = g.nv, ks = g.ks, ns = g.ns, ms = g.ms;
+  const double *src = nullptr;
+  size_t n = 0;
+  if (!strcmp(name, "gr")) { src = g.gr; n = nv * ks; }
+  else if (!strcmp(name, "grw")) { src = g.grw; n = nv * ks; }
+  else if (!strcmp(name, "grm")) { src = g.grm; n = nv * ks; }
+  else if (!strcmp(name, "pbsp")) { src = g.pbsp; n = (nv + 1) * ks * g.ksp; }
+  else if (!strcmp(name, "qbsp")) { src = g.qbsp; n = (nv + 1) * ks * g.ksq; }
+  else if (!strcmp(name, "fpbs")) { src = g.fpbs; n = ns * ns; }
+  else if (!strcmp(name, "fqbs")) { src = g.fqbs; n = ns * ns; }
+  else if (!strcmp(name, "fppqq")) { src = g.fppqq; n = ms * ms; }
+  else if (!strcmp(name, "gx")) { src = g.gx; n = ks; }
+  else if (!strcmp(name, "gw")) { src = g.gw; n = ks; }
+  else return set_err(c, DBSRG_EINVAL, "unknown grid array");
+  return copy_out(c, out, src, n * sizeof(double));
+}
+
+}  // extern "C"

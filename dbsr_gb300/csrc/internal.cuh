@@ -1,0 +1,179 @@
+// internal.cuh -- shared declarations of the sm_103a assembly library.
+//
+// Device memory layout (all FP64 arrays keep the reference's Fortran
+// column-major order so results can be compared element by element and
+// handed back to a Fortran caller without reshuffling):
+//   grid:     t(ns+ks), tp, tq, gx/gw(ks), gr/grw/grm(nv,ks),
+//             pbsp(nv+1,ks,ksp), qbsp(nv+1,ks,ksq), fpbs/fqbs(ns,ns),
+//             fppqq(ms,ms)
+//   tables:   R: rkb(ns,ns,ks,ks) per (k,type); S: rkb(ns,ns,2ks-1,2ks-1)
+//             per (k,type), built on first use (the irka cache of
+//             dbsr_lib_dbs.f90:2919-2925) and kept resident in HBM
+//   orbitals: pq(ns,2,nbf)
+//   matrix:   hch(ms,ms,iicc), acf(iicc,0:mk), icc(nch,nch)
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/dbsrg.h"
+
+#define DBSRG_IBO 32768  // packing basis for orbitals, mod_dbsr_mat.f90:61
+#define DBSRG_MAXK 16    // largest supported spline order
+
+struct DeviceGrid {
+  int ns = 0, ks = 0, ksp = 0, ksq = 0, nv = 0, nsp = 0, nsq = 0, ms = 0;
+  double *t = nullptr, *tp = nullptr, *tq = nullptr;
+  double *gx = nullptr, *gw = nullptr;
+  double *gr = nullptr, *grw = nullptr, *grm = nullptr;
+  double *pbsp = nullptr, *qbsp = nullptr;
+  double *fpbs = nullptr, *fqbs = nullptr, *fppqq = nullptr;
+};
+
+struct dbsrg_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  DeviceGrid g;
+  std::string err;
+  long long launches = 0;
+  int precision = DBSRG_PLAIN_FP64;
+  // orbitals
+  int nbf = 0;
+  double *pq = nullptr;
+  int *ipbs = nullptr;
+  std::vector<int> h_ipbs;
+  // matrix
+  int nch = 0, iicc = 0, mk = -1;
+  int *icc = nullptr;
+  std::vector<int> h_icc;
+  double *hch = nullptr;
+  double *acf = nullptr;
+  // table caches, indexed [k*4+type] (R) and [k*2+type] (S)
+  std::vector<double *> rtab, stab;
+  // <a|r^k|b> per component for the asymptotic coefficients, [k]
+  std::vector<double *> quad;
+  // scratch arena (grown on demand, reused across calls)
+  void *scratch = nullptr;
+  size_t scratch_bytes = 0;
+  void *scratch2 = nullptr;   // list state of one Gen_matrix call
+  size_t scratch2_bytes = 0;
+  void *tscratch = nullptr;   // table construction (moments, diagonal cells)
+  size_t tscratch_bytes = 0;
+  // pinned staging for host lists
+  void *pinned = nullptr;
+  size_t pinned_bytes = 0;
+  // per-kernel CUDA-event timing (dbsrg_timing): event pairs recorded on
+  // the context stream around each named launch, resolved on report
+  bool timing = false;
+  struct TimedLaunch {
+    const char *name;
+    cudaEvent_t a, b;
+  };
+  std::vector<TimedLaunch> tev;
+  std::vector<cudaEvent_t> evpool;
+};
+
+cudaEvent_t event_get(dbsrg_ctx *c);
+
+// ---- error helpers -------------------------------------------------------
+int set_err(dbsrg_ctx *c, int code, const std::string &msg);
+int cuda_check(dbsrg_ctx *c, cudaError_t e, const char *what);
+#define DBSRG_TRY(ctx, call)                                \
+  do {                                                      \
+    cudaError_t _e = (call);                                \
+    if (_e != cudaSuccess) return cuda_check(ctx, _e, #call); \
+  } while (0)
+// After every launch: count it, check the launch, and with the environment
+// variable DBSRG_SYNC_CHECK=1 also synchronise so a failing kernel is
+// reported by name at its own launch.
+bool sync_check_enabled();
+#define DBSRG_LAUNCHED(ctx)                                                  \
+  do {                                                                       \
+    (ctx)->launches++;                                                       \
+    cudaError_t _e = cudaGetLastError();                                     \
+    if (_e != cudaSuccess) return cuda_check(ctx, _e, "kernel launch");      \
+    if (sync_check_enabled()) {                                              \
+      _e = cudaStreamSynchronize((ctx)->stream);                             \
+      if (_e != cudaSuccess) return cuda_check(ctx, _e, __func__);           \
+    }                                                                        \
+  } while (0)
+
+// Launch a named kernel on the context stream; with timing enabled the
+// launch is bracketed by events (resolved by dbsrg_timing_report).
+#define DBSRG_RUN(ctx, name, ...)                                 \
+  do {                                                            \
+    cudaEvent_t _ea = nullptr;                                    \
+    if ((ctx)->timing) {                                          \
+      _ea = event_get(ctx);                                       \
+      cudaEventRecord(_ea, (ctx)->stream);                        \
+    }                                                             \
+    __VA_ARGS__;                                                  \
+    if ((ctx)->timing) {                                          \
+      cudaEvent_t _eb = event_get(ctx);                           \
+      cudaEventRecord(_eb, (ctx)->stream);                        \
+      (ctx)->tev.push_back({name, _ea, _eb});                     \
+    }                                                             \
+    DBSRG_LAUNCHED(ctx);                                          \
+  } while (0)
+
+bool is_device_ptr(const void *p);
+// copies n bytes from a host-or-device pointer into device memory dst
+int copy_in(dbsrg_ctx *c, void *dst, const void *src, size_t n);
+int copy_out(dbsrg_ctx *c, void *dst, const void *src, size_t n);
+// scratch arenas (device)
+int ensure_scratch(dbsrg_ctx *c, size_t bytes);
+int ensure_scratch2(dbsrg_ctx *c, size_t bytes);
+int ensure_tscratch(dbsrg_ctx *c, size_t bytes);
+int ensure_pinned(dbsrg_ctx *c, size_t bytes);
+
+// ---- tables.cu ------------------------------------------------------------
+int build_grid(dbsrg_ctx *c, const double *t_host_or_dev);
+int compute_moments(dbsrg_ctx *c, int which, int k, double *rkm_dev);
+int compute_diag_cells(dbsrg_ctx *c, int type, int k, double *rkd_dev);
+// returns device pointer of the cached table (building it if needed)
+int get_rtable(dbsrg_ctx *c, int type, int k, const double **out);
+int get_stable(dbsrg_ctx *c, int type, int k, const double **out);
+int get_quad(dbsrg_ctx *c, int k, const double **out);
+
+// ---- assemble.cu ----------------------------------------------------------
+int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n,
+                     const int *ipt, const int *k1, const int *k2,
+                     const int *k3, const int *k4, const double *cdata);
+int update_hx(dbsrg_ctx *c, int ich, int jch, const double *d, double cc);
+
+// ---- device helpers ---------------------------------------------------------
+// Values of the kx B-splines that are nonzero on the interval starting at
+// knot tx(kg) (1-based), at point x: the ni=1, nderiv=1 path of zbsplvd /
+// zbsplvb (dbsr_lib_dbs.f90:4197-4468).  Explicit round-to-nearest
+// intrinsics keep the reference's operation order (no contraction).
+__device__ __forceinline__ void bspline_values(const double *tx, int kx,
+                                               int kg, double x,
+                                               double *biatx) {
+  double dr[DBSRG_MAXK], dl[DBSRG_MAXK];
+  biatx[0] = 1.0;
+  for (int j = 1; j < kx; j++) {
+    const int jp1 = j + 1;
+    double saved = 0.0;
+    dr[j - 1] = __dsub_rn(tx[kg + j - 1], x);
+    dl[j - 1] = __dsub_rn(x, tx[kg - j]);
+    for (int m = 1; m <= j; m++) {
+      double term = __ddiv_rn(biatx[m - 1], __dadd_rn(dr[m - 1], dl[jp1 - m - 1]));
+      biatx[m - 1] = __dadd_rn(saved, __dmul_rn(dr[m - 1], term));
+      saved = __dmul_rn(dl[jp1 - m - 1], term);
+    }
+    biatx[jp1 - 1] = saved;
+  }
+}
+
+// real**integer by binary exponentiation (same method as libgcc's powi)
+__device__ __forceinline__ double ipow_d(double x, int m) {
+  unsigned int n = m < 0 ? (unsigned)(-m) : (unsigned)m;
+  double y = (n % 2) ? x : 1.0;
+  while (n >>= 1) {
+    x = __dmul_rn(x, x);
+    if (n % 2) y = __dmul_rn(y, x);
+  }
+  return m < 0 ? __ddiv_rn(1.0, y) : y;
+}

@@ -1,0 +1,596 @@
+// tables.cu -- B-spline grid, cell moments, diagonal-cell integrals and the
+// assembled R^k / S^k tables, all computed on the device in FP64.
+//
+// Operation order follows the reference routines (cited per kernel) and
+// uses explicit round-to-nearest intrinsics where the reference forms a
+// product and then a sum, so the tables reproduce the reference's loop
+// arithmetic instead of a contracted variant.
+#include "internal.cuh"
+
+#include <cmath>
+
+#define IDX2(i, j, n1) ((size_t)(i) + (size_t)(n1) * (size_t)(j))
+#define IDX3(i, j, k, n1, n2) ((size_t)(i) + (size_t)(n1) * ((size_t)(j) + (size_t)(n2) * (size_t)(k)))
+
+// ----------------------------------------------------------------------------
+// gauleg on [0,1]: dbsr_lib_zcom.f90:1990-2039 (Newton on the Legendre
+// recurrence).  One thread; n is the spline order.
+__global__ void k_gauleg(int n, double *x, double *w) {
+  const double EPS = 1.0e-14;
+  int m = (n + 1) / 2;
+  double xm = 0.5, xl = 0.5;
+  for (int i = 1; i <= m; i++) {
+    double z = cos(__ddiv_rn(__dmul_rn(3.141592654, (i - 0.25)), (n + 0.5)));
+    double z1, pp, p1, p2, p3;
+    do {
+      p1 = 1.0;
+      p2 = 0.0;
+      for (int j = 1; j <= n; j++) {
+        p3 = p2;
+        p2 = p1;
+        p1 = __ddiv_rn(__dsub_rn(__dmul_rn(__dmul_rn(2.0 * j - 1.0, z), p2),
+                                 __dmul_rn(j - 1.0, p3)),
+                       (double)j);
+      }
+      pp = __ddiv_rn(__dmul_rn((double)n, __dsub_rn(__dmul_rn(z, p1), p2)),
+                     __dsub_rn(__dmul_rn(z, z), 1.0));
+      z1 = z;
+      z = __dsub_rn(z1, __ddiv_rn(p1, pp));
+    } while (fabs(z - z1) > EPS);
+    x[i - 1] = __dsub_rn(xm, __dmul_rn(xl, z));
+    x[n - i] = __dadd_rn(xm, __dmul_rn(xl, z));
+    w[i - 1] = __ddiv_rn(2.0 * xl, __dmul_rn(__dmul_rn(__dsub_rn(1.0, __dmul_rn(z, z)), pp), pp));
+    w[n - i] = w[i - 1];
+  }
+}
+
+// Gauss points per interval: alloc_DBS_gauss, dbsr_lib_dbs.f90:929-936.
+__global__ void k_gauss_points(int nv, int ks, const double *t, const double *gx,
+                               const double *gw, double *gr, double *grm, double *grw) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nv * ks) return;
+  int iv = q % nv, m = q / nv;  // 0-based
+  double tl = t[ks + iv - 1], tr = t[ks + iv];
+  double h = __dsub_rn(tr, tl);
+  double r = __dadd_rn(__dmul_rn(h, gx[m]), tl);
+  gr[q] = r;
+  grm[q] = __ddiv_rn(1.0, r);
+  grw[q] = __dmul_rn(h, gw[m]);
+}
+
+// Knots of a component basis: Def_pbsp / Def_qbsp, dbsr_lib_dbs.f90:997-999.
+__global__ void k_sub_knots(int ns, int ks, int kx, int nsx, const double *t, double *tx) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x + 1;  // 1-based
+  if (i > nsx + kx) return;
+  double v;
+  if (i <= kx)
+    v = t[0];
+  else if (i <= nsx)
+    v = t[ks + (i - kx) - 1];
+  else
+    v = t[ns + (i - nsx) - 1];
+  tx[i - 1] = v;
+}
+
+// B-spline values at the Gauss points, bsp(nv+1,ks,kx): Def_pbsp /
+// Def_qbsp (dbsr_lib_dbs.f90:1003-1020); row nv+1 holds the values at the
+// last knot in its first column.
+__global__ void k_bsp_values(int nv, int ks, int kx, int nsx, const double *tx,
+                             const double *gr, double *bsp) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nw = nv + 1;
+  if (q >= nw * ks) return;
+  int iv = q % nw, m = q / nw;
+  double v[DBSRG_MAXK];
+  if (iv < nv) {
+    bspline_values(tx, kx, kx + iv, gr[IDX2(iv, m, nv)], v);
+  } else if (m == 0) {
+    bspline_values(tx, kx, nsx, tx[nsx], v);
+  } else {
+    for (int j = 0; j < kx; j++) v[j] = 0.0;
+  }
+  for (int j = 0; j < kx; j++) bsp[IDX3(iv, m, j, nw, ks)] = v[j];
+}
+
+// Banded Gram matrix ym(i,j) = <B1_i|y|B2_j>: ZINTYM, dbsr_lib_dbs.f90:4472-4497.
+// ym has leading dimension ld and is written at offset (off,off).
+__global__ void k_gram(int ns, int nv, int ks, int kx, const double *b, const double *ygr,
+                       double *ym, int ld, int off) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= ns * ns) return;
+  int i = q % ns + 1, j = q / ns + 1;  // 1-based
+  const int nw = nv + 1;
+  double acc = 0.0;
+  int lo = max(max(1, i - kx + 1), j - kx + 1), hi = min(min(nv, i), j);
+  for (int iv = lo; iv <= hi; iv++) {
+    int ith = i - iv + 1, jth = j - iv + 1;
+    double s = 0.0;
+    for (int m = 0; m < ks; m++) {
+      double p = __dmul_rn(__dmul_rn(ygr[IDX2(iv - 1, m, nv)], b[IDX3(iv - 1, m, ith - 1, nw, ks)]),
+                           b[IDX3(iv - 1, m, jth - 1, nw, ks)]);
+      s = __dadd_rn(s, p);
+    }
+    acc = __dadd_rn(acc, s);
+  }
+  ym[IDX2(off + i - 1, off + j - 1, ld)] = acc;
+}
+
+int build_grid(dbsrg_ctx *c, const double *t_in) {
+  DeviceGrid &g = c->g;
+  const int ns = g.ns, ks = g.ks, nv = g.nv, nw = nv + 1, ms = g.ms;
+  auto alloc = [&](double **p, size_t n) -> cudaError_t {
+    return cudaMalloc((void **)p, sizeof(double) * (n > 0 ? n : 1));
+  };
+  DBSRG_TRY(c, alloc(&g.t, ns + ks));
+  DBSRG_TRY(c, alloc(&g.tp, g.nsp + g.ksp));
+  DBSRG_TRY(c, alloc(&g.tq, g.nsq + g.ksq));
+  DBSRG_TRY(c, alloc(&g.gx, ks));
+  DBSRG_TRY(c, alloc(&g.gw, ks));
+  DBSRG_TRY(c, alloc(&g.gr, (size_t)nv * ks));
+  DBSRG_TRY(c, alloc(&g.grw, (size_t)nv * ks));
+  DBSRG_TRY(c, alloc(&g.grm, (size_t)nv * ks));
+  DBSRG_TRY(c, alloc(&g.pbsp, (size_t)nw * ks * g.ksp));
+  DBSRG_TRY(c, alloc(&g.qbsp, (size_t)nw * ks * g.ksq));
+  DBSRG_TRY(c, alloc(&g.fpbs, (size_t)ns * ns));
+  DBSRG_TRY(c, alloc(&g.fqbs, (size_t)ns * ns));
+  DBSRG_TRY(c, alloc(&g.fppqq, (size_t)ms * ms));
+  int rc = copy_in(c, g.t, t_in, sizeof(double) * (ns + ks));
+  if (rc) return rc;
+  cudaStream_t s = c->stream;
+  DBSRG_RUN(c, "k_gauleg", k_gauleg<<<1, 1, 0, s>>>(ks, g.gx, g.gw));
+  int nt = nv * ks;
+  DBSRG_RUN(c, "k_gauss_points", k_gauss_points<<<(nt + 127) / 128, 128, 0, s>>>(nv, ks, g.t, g.gx, g.gw, g.gr, g.grm, g.grw));
+  DBSRG_RUN(c, "k_sub_knots", k_sub_knots<<<(g.nsp + g.ksp + 127) / 128, 128, 0, s>>>(ns, ks, g.ksp, g.nsp, g.t, g.tp));
+  DBSRG_RUN(c, "k_sub_knots", k_sub_knots<<<(g.nsq + g.ksq + 127) / 128, 128, 0, s>>>(ns, ks, g.ksq, g.nsq, g.t, g.tq));
+  int nb = nw * ks;
+  DBSRG_RUN(c, "k_bsp_values", k_bsp_values<<<(nb + 127) / 128, 128, 0, s>>>(nv, ks, g.ksp, g.nsp, g.tp, g.gr, g.pbsp));
+  DBSRG_RUN(c, "k_bsp_values", k_bsp_values<<<(nb + 127) / 128, 128, 0, s>>>(nv, ks, g.ksq, g.nsq, g.tq, g.gr, g.qbsp));
+  int nn = ns * ns;
+  DBSRG_RUN(c, "k_gram", k_gram<<<(nn + 255) / 256, 256, 0, s>>>(ns, nv, ks, g.ksp, g.pbsp, g.grw, g.fpbs, ns, 0));
+  DBSRG_RUN(c, "k_gram", k_gram<<<(nn + 255) / 256, 256, 0, s>>>(ns, nv, ks, g.ksq, g.qbsp, g.grw, g.fqbs, ns, 0));
+  DBSRG_TRY(c, cudaMemsetAsync(g.fppqq, 0, sizeof(double) * (size_t)ms * ms, s));
+  DBSRG_RUN(c, "k_gram", k_gram<<<(nn + 255) / 256, 256, 0, s>>>(ns, nv, ks, g.ksp, g.pbsp, g.grw, g.fppqq, ms, 0));
+  DBSRG_RUN(c, "k_gram", k_gram<<<(nn + 255) / 256, 256, 0, s>>>(ns, nv, ks, g.ksq, g.qbsp, g.grw, g.fppqq, ms, ns));
+  DBSRG_TRY(c, cudaStreamSynchronize(s));
+  return DBSRG_OK;
+}
+
+// ----------------------------------------------------------------------------
+// Cell moments <B_i|r^k|B_j> per interval: moment_pp/qq/pq/qp,
+// dbsr_lib_dbs.f90:1401-1564.  rkm(ks*ks,nv); pp/qq packed i<=j.
+__global__ void k_moments(int nv, int ks, int k1, int k2, int sym, int k, const double *b1s,
+                          const double *b2s, const double *gr, const double *grm,
+                          const double *grw, double *rkm) {
+  int kk = ks * ks;
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= kk * nv) return;
+  int ii = q % kk, iv = q / kk;
+  int npair = sym ? k1 * (k1 + 1) / 2 : k1 * k2;
+  if (ii >= npair) {
+    rkm[q] = 0.0;
+    return;
+  }
+  int i, j;
+  if (sym) {  // invert the packed upper-triangular index
+    int r = ii, row = 0;
+    while (r >= k1 - row) {
+      r -= k1 - row;
+      row++;
+    }
+    i = row;
+    j = row + r;
+  } else {
+    i = ii / k2;
+    j = ii % k2;
+  }
+  const int nw = nv + 1;
+  double s = 0.0;
+  for (int m = 0; m < ks; m++) {
+    double w = grw[IDX2(iv, m, nv)];
+    if (k > 0) w = __dmul_rn(grw[IDX2(iv, m, nv)], ipow_d(gr[IDX2(iv, m, nv)], k));
+    if (k < 0) w = __dmul_rn(grw[IDX2(iv, m, nv)], ipow_d(grm[IDX2(iv, m, nv)], -k));
+    double b2 = __dmul_rn(b2s[IDX3(iv, m, j, nw, ks)], w);
+    s = __dadd_rn(s, __dmul_rn(b1s[IDX3(iv, m, i, nw, ks)], b2));
+  }
+  rkm[q] = s;
+}
+
+static void basis_of(const DeviceGrid &g, int which, const double **b1, const double **b2,
+                     int *k1, int *k2, int *sym) {
+  switch (which) {
+    case 0: *b1 = g.pbsp; *b2 = g.pbsp; *k1 = g.ksp; *k2 = g.ksp; *sym = 1; break;
+    case 1: *b1 = g.qbsp; *b2 = g.qbsp; *k1 = g.ksq; *k2 = g.ksq; *sym = 1; break;
+    case 2: *b1 = g.pbsp; *b2 = g.qbsp; *k1 = g.ksp; *k2 = g.ksq; *sym = 0; break;
+    default: *b1 = g.qbsp; *b2 = g.pbsp; *k1 = g.ksq; *k2 = g.ksp; *sym = 0; break;
+  }
+}
+
+int compute_moments(dbsrg_ctx *c, int which, int k, double *rkm) {
+  const DeviceGrid &g = c->g;
+  const double *b1, *b2;
+  int k1, k2, sym;
+  basis_of(g, which, &b1, &b2, &k1, &k2, &sym);
+  int n = g.ks * g.ks * g.nv;
+  DBSRG_RUN(c, "k_moments", k_moments<<<(n + 127) / 128, 128, 0, c->stream>>>(g.nv, g.ks, k1, k2, sym, k, b1, b2, g.gr,
+                                                   g.grm, g.grw, rkm));
+  return DBSRG_OK;
+}
+
+// ----------------------------------------------------------------------------
+// Diagonal-cell integrals triang_*: dbsr_lib_dbs.f90:2979-3063 (pppp),
+// 3151-3245 (pqpq), 3333-3427 (qpqp), 3512-3597 (qqqq), 3682-3767 (ppqq),
+// 3852-3936 (pqqp).  One thread block per interval iv.  For each outer
+// Gauss point r2 = gr(iv,m) the inner integral of B_j B_jp r^k over
+// [t_iv, r2] uses ks Gauss points; B-splines at the inner points come from
+// the same de Boor recursion as zbsplvd.
+//   type 0 pppp, 1 qqqq: rkd = a + a^T, a(outer pair, inner pair)
+//   type 2 pqpq: rkd(P pair, Q pair) = sum bp*INTQ + sum bq*INTP
+//   type 3 qpqp: rkd(Q pair, P pair) = the same two sums
+//   type 4 ppqq: rkd(inner (P,Q), outer (P,Q))
+//   type 5 pqqp: rkd(inner (P,Q), outer (Q,P))
+__global__ void k_triang(int nv, int ks, int ksp, int ksq, int type, int k, const double *t,
+                         const double *tp, const double *tq, const double *gx,
+                         const double *gw, const double *gr, const double *grm,
+                         const double *grw, const double *pbsp, const double *qbsp,
+                         double *rkd) {
+  extern __shared__ double sm[];
+  const int iv = blockIdx.x;  // 0-based interval
+  const int nw = nv + 1, kk = ks * ks;
+  const int KS2 = ks * ks;
+  double *wk = sm;                 // (m,i) inner weight * r^k       [ks*ks]
+  double *BP = wk + KS2;           // (m,i,j) P values at inner pts  [ks*ks*ksp]
+  double *BQ = BP + KS2 * ksp;     // (m,i,j) Q values               [ks*ks*ksq]
+  double *INTP = BQ + KS2 * ksq;   // (j,jp,m) over P x P            [ksp*ksp*ks]
+  double *INTQ = INTP + ksp * ksp * ks;  // Q x Q                    [ksq*ksq*ks]
+  double *INTPQ = INTQ + ksq * ksq * ks; // P x Q                    [ksp*ksq*ks]
+  double *gxo = INTPQ + ksp * ksq * ks;  // outer weights            [ks]
+  double *A = gxo + ks;                  // a(ii,jj) for pppp/qqqq   [kk*kk]
+
+  const bool needP = true, needQ = (type != 0);
+  const double xbase = t[iv + ks - 1];
+  // phase 1: inner points, weights and B-spline values
+  for (int q = threadIdx.x; q < KS2; q += blockDim.x) {
+    int m = q / ks, i = q % ks;
+    double r2 = gr[IDX2(iv, m, nv)];
+    double d = __dsub_rn(r2, xbase);
+    double x = __dadd_rn(__dmul_rn(d, gx[i]), xbase);
+    double w = __dmul_rn(d, gw[i]);
+    wk[q] = __dmul_rn(w, ipow_d(x, k));
+    double v[DBSRG_MAXK];
+    if (needP) {
+      bspline_values(tp, ksp, iv + ksp, x, v);
+      for (int j = 0; j < ksp; j++) BP[(size_t)q * ksp + j] = v[j];
+    }
+    if (needQ || type == 1) {
+      bspline_values(tq, ksq, iv + ksq, x, v);
+      for (int j = 0; j < ksq; j++) BQ[(size_t)q * ksq + j] = v[j];
+    }
+  }
+  for (int m = threadIdx.x; m < ks; m += blockDim.x)
+    gxo[m] = __dmul_rn(grw[IDX2(iv, m, nv)], ipow_d(grm[IDX2(iv, m, nv)], k + 1));
+  __syncthreads();
+  // phase 2: INT(j,jp,m) = sum_i (wk*Ba_j)*Bb_jp
+  auto inner = [&](const double *Ba, int ka, const double *Bb, int kb, double *INT) {
+    for (int q = threadIdx.x; q < ka * kb * ks; q += blockDim.x) {
+      int j = q % ka, jp = (q / ka) % kb, m = q / (ka * kb);
+      double s = 0.0;
+      for (int i = 0; i < ks; i++) {
+        int p = m * ks + i;
+        double gwl = __dmul_rn(wk[p], Ba[(size_t)p * ka + j]);
+        s = __dadd_rn(s, __dmul_rn(gwl, Bb[(size_t)p * kb + jp]));
+      }
+      INT[j + ka * (jp + kb * m)] = s;
+    }
+  };
+  if (type == 0) inner(BP, ksp, BP, ksp, INTP);
+  if (type == 1) inner(BQ, ksq, BQ, ksq, INTQ);
+  if (type == 2 || type == 3) {
+    inner(BP, ksp, BP, ksp, INTP);
+    inner(BQ, ksq, BQ, ksq, INTQ);
+  }
+  if (type == 4 || type == 5) inner(BP, ksp, BQ, ksq, INTPQ);
+  __syncthreads();
+
+  double *out = rkd + (size_t)kk * kk * iv;
+  auto ob = [&](const double *b1, int i, const double *b2, int ip, int m) -> double {
+    return __dmul_rn(__dmul_rn(b1[IDX3(iv, m, i, nw, ks)], b2[IDX3(iv, m, ip, nw, ks)]), gxo[m]);
+  };
+  auto pair_of = [](int ii, int kx, int *i, int *ip) {
+    int r = ii, row = 0;
+    while (r >= kx - row) {
+      r -= kx - row;
+      row++;
+    }
+    *i = row;
+    *ip = row + r;
+  };
+  if (type == 0 || type == 1) {
+    const int kx = type == 0 ? ksp : ksq;
+    const double *bs = type == 0 ? pbsp : qbsp;
+    const double *INT = type == 0 ? INTP : INTQ;
+    const int ik = kx * (kx + 1) / 2;
+    for (int q = threadIdx.x; q < ik * ik; q += blockDim.x) {
+      int ii = q % ik, jj = q / ik;
+      int i, ip, j, jp;
+      pair_of(ii, kx, &i, &ip);
+      pair_of(jj, kx, &j, &jp);
+      double s = 0.0;
+      for (int m = 0; m < ks; m++)
+        s = __dadd_rn(s, __dmul_rn(ob(bs, i, bs, ip, m), INT[j + kx * (jp + kx * m)]));
+      A[q] = s;
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < kk * kk; q += blockDim.x) {
+      int ii = q % kk, jj = q / kk;
+      out[q] = (ii < ik && jj < ik) ? __dadd_rn(A[ii + ik * jj], A[jj + ik * ii]) : 0.0;
+    }
+  } else if (type == 2 || type == 3) {
+    const int ikp = ksp * (ksp + 1) / 2, ikq = ksq * (ksq + 1) / 2;
+    for (int q = threadIdx.x; q < kk * kk; q += blockDim.x) {
+      int r = q % kk, cc = q / kk;
+      int pp_ = type == 2 ? r : cc, qq_ = type == 2 ? cc : r;  // P pair, Q pair
+      double v = 0.0;
+      if (pp_ < ikp && qq_ < ikq) {
+        int i, ip, j, jp;
+        pair_of(pp_, ksp, &i, &ip);
+        pair_of(qq_, ksq, &j, &jp);
+        double s1 = 0.0, s2 = 0.0;
+        for (int m = 0; m < ks; m++)
+          s1 = __dadd_rn(s1, __dmul_rn(ob(pbsp, i, pbsp, ip, m), INTQ[j + ksq * (jp + ksq * m)]));
+        for (int m = 0; m < ks; m++)
+          s2 = __dadd_rn(s2, __dmul_rn(ob(qbsp, j, qbsp, jp, m), INTP[i + ksp * (ip + ksp * m)]));
+        v = __dadd_rn(s1, s2);
+      }
+      out[q] = v;
+    }
+  } else {
+    const int np = ksp * ksq;
+    for (int q = threadIdx.x; q < kk * kk; q += blockDim.x) {
+      int jj = q % kk, ii = q / kk;  // rkd(jj,ii): jj inner (P,Q), ii outer
+      double v = 0.0;
+      if (jj < np && ii < np) {
+        int j = jj / ksq, jp = jj % ksq;
+        int i, ip;
+        const double *b1, *b2;
+        if (type == 4) {
+          i = ii / ksq; ip = ii % ksq; b1 = pbsp; b2 = qbsp;
+        } else {
+          i = ii / ksp; ip = ii % ksp; b1 = qbsp; b2 = pbsp;
+        }
+        double s = 0.0;
+        for (int m = 0; m < ks; m++)
+          s = __dadd_rn(s, __dmul_rn(ob(b1, i, b2, ip, m), INTPQ[j + ksp * (jp + ksq * m)]));
+        v = s;
+      }
+      out[q] = v;
+    }
+  }
+}
+
+int compute_diag_cells(dbsrg_ctx *c, int type, int k, double *rkd) {
+  const DeviceGrid &g = c->g;
+  const int ks = g.ks, kk = ks * ks;
+  size_t nsm = (size_t)ks * ks + (size_t)ks * ks * g.ksp + (size_t)ks * ks * g.ksq +
+               (size_t)g.ksp * g.ksp * ks + (size_t)g.ksq * g.ksq * ks +
+               (size_t)g.ksp * g.ksq * ks + ks + (size_t)kk * kk;
+  size_t bytes = nsm * sizeof(double);
+  if (bytes > 48 * 1024)
+    DBSRG_TRY(c, cudaFuncSetAttribute(k_triang, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)bytes));
+  DBSRG_RUN(c, "k_triang", k_triang<<<g.nv, 256, bytes, c->stream>>>(g.nv, ks, g.ksp, g.ksq, type, k, g.t, g.tp, g.tq,
+                                            g.gx, g.gw, g.gr, g.grm, g.grw, g.pbsp, g.qbsp, rkd));
+  return DBSRG_OK;
+}
+
+// ----------------------------------------------------------------------------
+// R^k table fill: mrk_pppp/qqqq/pqpq/qpqp, dbsr_lib_dbs.f90:2898-2959,
+// 3431-3492, 3067-3131, 3249-3313.  One thread per table element
+// rkb(i,j,ip,jp); the element gathers its cell contributions in the
+// reference's accumulation order (jv ascending, then iv ascending).
+__device__ __forceinline__ int tri_index(int h, int hp, int kx) {  // 1-based
+  return (h - 1) * kx - ((h - 1) * (h - 2)) / 2 + (hp - h + 1);
+}
+
+__global__ void k_fill_r(int ns, int ks, int nv, int ka, int kb, const double *lowA,
+                         const double *highA, const double *lowB, const double *highB,
+                         const double *rkd, double *rkb) {
+  size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  size_t total = (size_t)ns * ns * ks * ks;
+  if (q >= total) return;
+  const int kk = ks * ks;
+  int i = (int)(q % ns) + 1;
+  size_t r = q / ns;
+  int j = (int)(r % ns) + 1;
+  r /= ns;
+  int ip = (int)(r % ks) + 1;
+  int jp = (int)(r / ks) + 1;
+  double acc = 0.0;
+  if (ip <= ka && jp <= kb) {
+    int ivlo = max(1, i - ka + ip), ivhi = min(nv, i);
+    int jvlo = max(1, j - kb + jp), jvhi = min(nv, j);
+    for (int jv = jvlo; jv <= jvhi; jv++) {
+      int jh = j - jv + 1;
+      int jj = tri_index(jh, jh + jp - 1, kb);
+      for (int iv = ivlo; iv <= ivhi; iv++) {
+        int ih = i - iv + 1;
+        int ii = tri_index(ih, ih + ip - 1, ka);
+        double cc;
+        if (iv < jv)
+          cc = __dmul_rn(lowA[(ii - 1) + (size_t)kk * (iv - 1)], highB[(jj - 1) + (size_t)kk * (jv - 1)]);
+        else if (iv > jv)
+          cc = __dmul_rn(lowB[(jj - 1) + (size_t)kk * (jv - 1)], highA[(ii - 1) + (size_t)kk * (iv - 1)]);
+        else
+          cc = rkd[(ii - 1) + (size_t)kk * ((jj - 1) + (size_t)kk * (iv - 1))];
+        acc = __dadd_rn(acc, cc);
+      }
+    }
+  }
+  rkb[q] = acc;
+}
+
+// S^k table fill: msk_ppqq / msk_pqqp, dbsr_lib_dbs.f90:3601-3662,
+// 3771-3833.  Only cells iv <= jv; band offsets ip = ihp-ih+ks.
+__global__ void k_fill_s(int ns, int ks, int nv, int ksp, int ksq, int kj1, int kj2,
+                         const double *r1, const double *r2, const double *rkd, double *rkb) {
+  const int kb2 = 2 * ks - 1, kk = ks * ks;
+  size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  size_t total = (size_t)ns * ns * kb2 * kb2;
+  if (q >= total) return;
+  int i = (int)(q % ns) + 1;
+  size_t r = q / ns;
+  int j = (int)(r % ns) + 1;
+  r /= ns;
+  int ip = (int)(r % kb2) + 1;
+  int jp = (int)(r / kb2) + 1;
+  double acc = 0.0;
+  // electron 1: ih in [1,ksp], ihp = ip+ih-ks in [1,ksq], iv = i-ih+1
+  int ihlo = max(1, ks - ip + 1), ihhi = min(ksp, ks - ip + ksq);
+  // electron 2: jh in [1,kj1], jhp = jp+jh-ks in [1,kj2], jv = j-jh+1
+  int jhlo = max(1, ks - jp + 1), jhhi = min(kj1, ks - jp + kj2);
+  // jv ascending <=> jh descending
+  for (int jh = jhhi; jh >= jhlo; jh--) {
+    int jv = j - jh + 1;
+    if (jv < 1 || jv > nv) continue;
+    int jhp = jp + jh - ks;
+    int jj = (jh - 1) * kj2 + jhp;
+    for (int ih = ihhi; ih >= ihlo; ih--) {
+      int iv = i - ih + 1;
+      if (iv < 1 || iv > jv) continue;
+      int ihp = ip + ih - ks;
+      int ii = (ih - 1) * ksq + ihp;
+      double cc;
+      if (iv == jv)
+        cc = rkd[(ii - 1) + (size_t)kk * ((jj - 1) + (size_t)kk * (iv - 1))];
+      else
+        cc = __dmul_rn(r1[(ii - 1) + (size_t)kk * (iv - 1)], r2[(jj - 1) + (size_t)kk * (jv - 1)]);
+      acc = __dadd_rn(acc, cc);
+    }
+  }
+  rkb[q] = acc;
+}
+
+static int ensure_slot(dbsrg_ctx *c, std::vector<double *> &v, size_t idx) {
+  if (v.size() <= idx) v.resize(idx + 1, nullptr);
+  return 0;
+}
+
+int get_rtable(dbsrg_ctx *c, int type, int k, const double **out) {
+  const DeviceGrid &g = c->g;
+  size_t idx = (size_t)k * 4 + type;
+  ensure_slot(c, c->rtab, idx);
+  if (c->rtab[idx]) {
+    *out = c->rtab[idx];
+    return DBSRG_OK;
+  }
+  const int ns = g.ns, ks = g.ks, nv = g.nv, kk = ks * ks;
+  size_t nt = (size_t)ns * ns * ks * ks;
+  double *tab = nullptr;
+  cudaError_t e = cudaMalloc((void **)&tab, nt * sizeof(double));
+  if (e != cudaSuccess) return set_err(c, DBSRG_ENOMEM, "R table allocation failed");
+  int wa = (type == 0 || type == 2) ? 0 : 1, wb = (type == 0 || type == 3) ? 0 : 1;
+  int ka = wa ? g.ksq : g.ksp, kb = wb ? g.ksq : g.ksp;
+  size_t mbytes = (size_t)kk * nv * sizeof(double);
+  size_t dbytes = (size_t)kk * kk * nv * sizeof(double);
+  int rc = ensure_tscratch(c, 4 * mbytes + dbytes);
+  if (rc) return rc;
+  double *lowA = (double *)c->tscratch;
+  double *highA = lowA + (size_t)kk * nv;
+  double *lowB = highA + (size_t)kk * nv;
+  double *highB = lowB + (size_t)kk * nv;
+  double *rkd = highB + (size_t)kk * nv;
+  if ((rc = compute_moments(c, wa, k, lowA))) return rc;
+  if ((rc = compute_moments(c, wa, -(k + 1), highA))) return rc;
+  if ((rc = compute_moments(c, wb, k, lowB))) return rc;
+  if ((rc = compute_moments(c, wb, -(k + 1), highB))) return rc;
+  if ((rc = compute_diag_cells(c, type, k, rkd))) return rc;
+  unsigned nb = (unsigned)((nt + 255) / 256);
+  DBSRG_RUN(c, "k_fill_r", k_fill_r<<<nb, 256, 0, c->stream>>>(ns, ks, nv, ka, kb, lowA, highA, lowB, highB, rkd, tab));
+  c->rtab[idx] = tab;
+  *out = tab;
+  return DBSRG_OK;
+}
+
+int get_stable(dbsrg_ctx *c, int type, int k, const double **out) {
+  const DeviceGrid &g = c->g;
+  size_t idx = (size_t)k * 2 + type;
+  ensure_slot(c, c->stab, idx);
+  if (c->stab[idx]) {
+    *out = c->stab[idx];
+    return DBSRG_OK;
+  }
+  const int ns = g.ns, ks = g.ks, nv = g.nv, kk = ks * ks, kb2 = 2 * ks - 1;
+  size_t nt = (size_t)ns * ns * kb2 * kb2;
+  double *tab = nullptr;
+  cudaError_t e = cudaMalloc((void **)&tab, nt * sizeof(double));
+  if (e != cudaSuccess) return set_err(c, DBSRG_ENOMEM, "S table allocation failed");
+  size_t mbytes = (size_t)kk * nv * sizeof(double);
+  size_t dbytes = (size_t)kk * kk * nv * sizeof(double);
+  int rc = ensure_tscratch(c, 2 * mbytes + dbytes);
+  if (rc) return rc;
+  double *r1 = (double *)c->tscratch;
+  double *r2 = r1 + (size_t)kk * nv;
+  double *rkd = r2 + (size_t)kk * nv;
+  if ((rc = compute_moments(c, 2, k, r1))) return rc;
+  if ((rc = compute_moments(c, type == 0 ? 2 : 3, -(k + 1), r2))) return rc;
+  if ((rc = compute_diag_cells(c, type == 0 ? 4 : 5, k, rkd))) return rc;
+  int kj1 = type == 0 ? g.ksp : g.ksq, kj2 = type == 0 ? g.ksq : g.ksp;
+  unsigned nb = (unsigned)((nt + 255) / 256);
+  DBSRG_RUN(c, "k_fill_s", k_fill_s<<<nb, 256, 0, c->stream>>>(ns, ks, nv, g.ksp, g.ksq, kj1, kj2, r1, r2, rkd, tab));
+  c->stab[idx] = tab;
+  *out = tab;
+  return DBSRG_OK;
+}
+
+// ----------------------------------------------------------------------------
+// <a|r^k|b> split by component for all orbital pairs: quadr
+// (dbsr_lib_dbs.f90:3940-3976), used for the asymptotic coefficients
+// (QUADR_PQ at R_data.f90:224, which selects the component by atype).
+// quad(a,b,comp) with a,b 0-based orbital indices.
+__global__ void k_quad(int nbf, int ns, int nv, int ks, int ksp, int ksq, int k,
+                       const double *pq, const double *gr, const double *grw,
+                       const double *pbsp, const double *qbsp, double *quad) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nbf * nbf * 2) return;
+  int a = q % nbf, b = (q / nbf) % nbf, comp = q / (nbf * nbf);
+  const int nw = nv + 1;
+  const int kx = comp == 0 ? ksp : ksq;
+  const double *bs = comp == 0 ? pbsp : qbsp;
+  const double *Fi = pq + (size_t)ns * comp + (size_t)2 * ns * a;
+  const double *Fj = pq + (size_t)ns * comp + (size_t)2 * ns * b;
+  double acc = 0.0, gxl[DBSRG_MAXK];
+  for (int iv = 0; iv < nv; iv++) {
+    for (int m = 0; m < ks; m++)
+      gxl[m] = __dmul_rn(ipow_d(gr[IDX2(iv, m, nv)], k), grw[IDX2(iv, m, nv)]);
+    for (int ith = 0; ith < kx; ith++) {
+      double pi = Fi[iv + ith];
+      for (int jth = 0; jth < kx; jth++) {
+        double pj = Fj[iv + jth], s = 0.0;
+        for (int m = 0; m < ks; m++) {
+          double gwl = __dmul_rn(gxl[m], bs[IDX3(iv, m, ith, nw, ks)]);
+          s = __dadd_rn(s, __dmul_rn(bs[IDX3(iv, m, jth, nw, ks)], gwl));
+        }
+        acc = __dadd_rn(acc, __dmul_rn(__dmul_rn(s, pi), pj));
+      }
+    }
+  }
+  quad[q] = acc;
+}
+
+int get_quad(dbsrg_ctx *c, int k, const double **out) {
+  if ((int)c->quad.size() <= k) c->quad.resize(k + 1, nullptr);
+  if (c->quad[k]) {
+    *out = c->quad[k];
+    return DBSRG_OK;
+  }
+  const DeviceGrid &g = c->g;
+  double *q = nullptr;
+  size_t n = (size_t)c->nbf * c->nbf * 2;
+  if (cudaMalloc((void **)&q, n * sizeof(double)) != cudaSuccess)
+    return set_err(c, DBSRG_ENOMEM, "quad allocation failed");
+  DBSRG_RUN(c, "k_quad", k_quad<<<(unsigned)((n + 127) / 128), 128, 0, c->stream>>>(c->nbf, g.ns, g.nv, g.ks, g.ksp,
+                                                             g.ksq, k, c->pq, g.gr, g.grw,
+                                                             g.pbsp, g.qbsp, q));
+  c->quad[k] = q;
+  *out = q;
+  return DBSRG_OK;
+}

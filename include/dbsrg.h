@@ -1,0 +1,156 @@
+/*
+ * dbsrg.h -- C ABI of the GB300 (sm_103a) Hamiltonian-block assembly
+ * library (libdbsrgpu.so) for DBSR_MAT3.
+ *
+ * The library replaces the assembly step that DBSR_MAT3 enters through
+ *     Subroutine Gen_matrix(itype,kpol)      DBSR_MAT3/gen_matrix.f90:2-17
+ * and everything below it:
+ *   - B-spline grid and Gauss tables      dbsr_lib_dbs.f90:911-1102
+ *   - cell moments and R^k/S^k tables    dbsr_lib_dbs.f90:1234-1720,2898-3936
+ *   - density / convol / convol_sk       dbsr_lib_dbs.f90:2208-2891
+ *   - R_data / S_data / O_data dispatch  DBSR_MAT3/R_data.f90, S_data.f90,
+ *                                        O_data.f90
+ *   - UPDATE_HS / UPDATE_HW / UPDATE_HX  DBSR_MAT3/updates.f90:79-292
+ * The Fortran caller keeps its module data; these entry points receive
+ * that data explicitly (plain pointers and sizes, Fortran column-major
+ * layout, 1-based orbital/channel/block numbers exactly as in the
+ * reference), so an iso_c_binding interface block can bind them one to
+ * one.  Conventions:
+ *   - every entry point returns a dbsrg_status; nonzero means failure and
+ *     dbsrg_last_error() gives a message.  The library never aborts; the
+ *     Fortran shim stops on nonzero status as the reference does.
+ *   - one context per process and thread; calls are serialised on the
+ *     context's CUDA stream and return after the work is complete unless
+ *     stated otherwise.
+ *   - host arrays passed in stay owned by the caller; the library copies
+ *     them.  Pointers may also be device pointers (CUDA unified
+ *     addressing tells them apart); then no copy is made.
+ *   - there is no CPU fallback: without a usable sm_103a device every
+ *     call that needs one returns DBSRG_ECUDA.
+ */
+#ifndef DBSRG_H
+#define DBSRG_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct dbsrg_ctx dbsrg_ctx;
+
+enum dbsrg_status {
+  DBSRG_OK = 0,
+  DBSRG_EINVAL = -1,   /* bad argument (the reference would Stop)        */
+  DBSRG_ECUDA = -2,    /* CUDA error or no usable device                  */
+  DBSRG_ENOMEM = -3,   /* device allocation failed                        */
+  DBSRG_ERANGE = -4,   /* index out of range in a list (UPDATE_* checks)  */
+  DBSRG_ESTATE = -5,   /* call order violated (e.g. no matrix allocated)  */
+  DBSRG_ETIMEOUT = -6  /* a device-side bounded wait ran out              */
+};
+
+/* precision / algorithm of the contraction */
+enum dbsrg_precision {
+  DBSRG_PLAIN_FP64 = 0, /* reference loop structure, FP64 throughout      */
+  DBSRG_SPLIT_BF16 = 1  /* split-precision tensor-core contraction        */
+};
+
+/* table families for dbsrg_get_table */
+enum dbsrg_family { DBSRG_RK = 0, DBSRG_SK = 1 };
+
+typedef struct dbsrg_grid_desc {
+  int ns;          /* number of order-ks B-splines                         */
+  int ks;          /* order of the knot sequence (9)                       */
+  int ksp;         /* order for P (large) components (8)                   */
+  int ksq;         /* order for Q (small) components (9)                   */
+  const double *t; /* knots t(1:ns+ks), host or device                     */
+  int device;      /* CUDA device ordinal                                  */
+} dbsrg_grid_desc;
+
+/* Context with the B-spline grid: knots -> Gauss points, B-spline values
+ * (pbsp/qbsp), overlap matrices fpbs/fqbs/fppqq, all built on the device.
+ * Replaces read_knot_dat/def_grid (grid_type -1, dbsr_lib_dbs.f90:611)
+ * + alloc_DBS_gauss (:911) + Def_pbsp/Def_qbsp/Def_pq_arrays (:987-1102). */
+int dbsrg_create(dbsrg_ctx **ctx, const dbsrg_grid_desc *desc);
+int dbsrg_destroy(dbsrg_ctx *ctx);
+const char *dbsrg_last_error(const dbsrg_ctx *ctx);
+
+/* Orbitals pq(ns,2,nbf) (Fortran order, P then Q) and ipbs(nbf), the
+ * channel number of a channel orbital or 0 for a bound orbital: the
+ * DBS_orbitals_pq module data read by R_data/S_data (R_data.f90:226,255). */
+int dbsrg_set_orbitals(dbsrg_ctx *ctx, int nbf, const double *pq,
+                       const int *ipbs);
+
+/* Channel-pair matrix in the reference layout hch(ms,ms,iicc), ms=2*ns,
+ * with icc(nch,nch) giving the 1-based block of a channel pair (0: not
+ * held), and acf(iicc,0:mk).  Replaces Alloc_dbsr_matrix
+ * (updates.f90:2-76); the matrix is zeroed. */
+int dbsrg_alloc_matrix(dbsrg_ctx *ctx, int nch, const int *icc, int iicc,
+                       int mk);
+int dbsrg_zero_matrix(dbsrg_ctx *ctx);
+
+int dbsrg_set_precision(dbsrg_ctx *ctx, int precision);
+
+/* Drop-in for Gen_matrix(itype,kpol) (gen_matrix.f90:2-17): processes one
+ * coefficient list exactly as Add_matrix leaves it (MOD_c_data.f90:318-
+ * 368): entries ipt(1:ncdata) index the arrays k1..k4, cdata, sorted by
+ * (K1,K2,K3,K4).  ipt may be NULL for the identity order.
+ *   icase 0: overlaps, itype 3 (O_data.f90:50-61)
+ *   icase 2: R^k, itype 3 direct / 4 exchange, all four atypes
+ *            (R_data.f90:214-277)
+ *   icase 3: S^k, ktype = 10*atype + itype, itype 6..9 (S_data.f90:240-274)
+ * Adds into hch and acf. */
+int dbsrg_gen_matrix(dbsrg_ctx *ctx, int icase, int itype, int kpol,
+                     int ncdata, const int *ipt, const int *k1,
+                     const int *k2, const int *k3, const int *k4,
+                     const double *cdata);
+
+/* UPDATE_HX(ich,jch,d,C) (updates.f90:79-106): add C*d (d is ms x ms,
+ * host or device) to the block of channel pair (ich,jch). */
+int dbsrg_update_hx(dbsrg_ctx *ctx, int ich, int jch, const double *d,
+                    double c);
+
+/* Copies of results (host or device destination). */
+int dbsrg_get_block(dbsrg_ctx *ctx, int ich, int jch, double *out);
+int dbsrg_get_matrix(dbsrg_ctx *ctx, double *hch);
+int dbsrg_get_acf(dbsrg_ctx *ctx, double *acf);
+/* Device pointer to hch (valid until the next alloc/destroy). */
+int dbsrg_matrix_device_ptr(dbsrg_ctx *ctx, double **hch_dev);
+
+/* One assembled B-spline integral table, in the reference layout
+ * rkb(ns,ns,ks,ks) for R (type 0 pppp,1 qqqq,2 pqpq,3 qpqp; mrk_*,
+ * dbsr_lib_dbs.f90:2898-3492) or rkb(ns,ns,2ks-1,2ks-1) for S (type 0
+ * ppqq, 1 pqqp; msk_*, :3601-3833). */
+int dbsrg_get_table(dbsrg_ctx *ctx, int family, int type, int k,
+                    double *out);
+/* Cell moments (moment_pp/qq/pq/qp, :1401-1564) as rkm(ks*ks,nv) and
+ * diagonal-cell integrals (triang_*, :2979-3936) as rkd(ks*ks,ks*ks,nv). */
+int dbsrg_get_moments(dbsrg_ctx *ctx, int which, int k, double *out);
+int dbsrg_get_diag_cells(dbsrg_ctx *ctx, int type, int k, double *out);
+/* Grid arrays: name is one of "gr","grw","grm","pbsp","qbsp","pbsd",
+ * "qbsd","fpbs","fqbs","fppqq" (reference shapes). */
+int dbsrg_get_grid_array(dbsrg_ctx *ctx, const char *name, double *out);
+
+/* Free the cached R^k/S^k tables (the reference keeps them for the whole
+ * run, dbsr_lib_dbs.f90:1595-1624; a caller that wants each assembly to
+ * rebuild them, or to reclaim the memory, releases them here). */
+int dbsrg_release_tables(dbsrg_ctx *ctx);
+
+/* Number of this library's kernels launched by the context so far. */
+long long dbsrg_kernel_launches(const dbsrg_ctx *ctx);
+/* Synchronise the context's stream. */
+int dbsrg_sync(dbsrg_ctx *ctx);
+
+/* Per-kernel device timing (no reference counterpart; it replaces the
+ * CPU_time counters time_convol/time_density of dbsr_lib_dbs.f90:1106-1116
+ * and t_rdata/t_sdata of mod_dbsr_mat.f90:114).  enable=1 clears the record
+ * and brackets every kernel launch with CUDA events on the context stream;
+ * dbsrg_timing_report writes a JSON object {"kernel": [launches, ms], ...}
+ * into buf (synchronising the stream first). */
+int dbsrg_timing(dbsrg_ctx *ctx, int enable);
+int dbsrg_timing_report(dbsrg_ctx *ctx, char *buf, size_t len);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,1411 @@
+/*
+ * dbsr_oracle.c -- CPU restatement (test infrastructure only) of the
+ * DBSR_MAT3 Hamiltonian-block assembly path.  See dbsr_oracle.h for the
+ * role of this file and how it is pinned.
+ *
+ * Layout: all arrays are Fortran column-major with the reference's own
+ * dimensions; the macros below translate 1-based Fortran subscripts to
+ * 0-based offsets so that every loop reads like the routine it follows.
+ * Build with -ffp-contract=off so x86-64 and aarch64 hosts give the same
+ * bits (no fused multiply-add contraction).
+ */
+#include "dbsr_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define A2(a, i, j, n1) (a)[((size_t)(i)-1) + (size_t)(n1) * ((size_t)(j)-1)]
+#define A3(a, i, j, m, n1, n2)                                               \
+  (a)[((size_t)(i)-1) +                                                      \
+      (size_t)(n1) * (((size_t)(j)-1) + (size_t)(n2) * ((size_t)(m)-1))]
+#define A4(a, i, j, k, l, n1, n2, n3)                                        \
+  (a)[((size_t)(i)-1) +                                                      \
+      (size_t)(n1) *                                                         \
+          (((size_t)(j)-1) +                                                 \
+           (size_t)(n2) * (((size_t)(k)-1) + (size_t)(n3) * ((size_t)(l)-1)))]
+
+static int imax(int a, int b) { return a > b ? a : b; }
+static int imin(int a, int b) { return a < b ? a : b; }
+
+/* Integer power by binary exponentiation (the libgcc __powidf2 method
+ * that gfortran uses for real**integer). */
+static double ipow(double x, int m) {
+  unsigned int n = m < 0 ? (unsigned)(-m) : (unsigned)m;
+  double y = (n % 2) ? x : 1.0;
+  while (n >>= 1) {
+    x = x * x;
+    if (n % 2) y = y * x;
+  }
+  return m < 0 ? 1.0 / y : y;
+}
+
+/* ------------------------------------------------------------------ */
+/* gauleg: dbsr_lib_zcom.f90:1990-2039 (Numerical-Recipes Newton).     */
+void orc_gauleg(double x1, double x2, double *x, double *w, int n) {
+  const double EPS = 1.0e-14;
+  int m = (n + 1) / 2;
+  double xm = 0.5 * (x2 + x1), xl = 0.5 * (x2 - x1);
+  for (int i = 1; i <= m; i++) {
+    double z = cos(3.141592654 * (i - 0.25) / (n + 0.5));
+    double z1, pp, p1, p2, p3;
+    do {
+      p1 = 1.0;
+      p2 = 0.0;
+      for (int j = 1; j <= n; j++) {
+        p3 = p2;
+        p2 = p1;
+        p1 = ((2.0 * j - 1.0) * z * p2 - (j - 1.0) * p3) / j;
+      }
+      pp = n * (z * p1 - p2) / (z * z - 1.0);
+      z1 = z;
+      z = z1 - p1 / pp;
+    } while (fabs(z - z1) > EPS);
+    x[i - 1] = xm - xl * z;
+    x[n - i] = xm + xl * z;
+    w[i - 1] = 2.0 * xl / ((1.0 - z * z) * pp * pp);
+    w[n - i] = w[i - 1];
+  }
+}
+
+/* ------------------------------------------------------------------ */
+/* mkgrid_01: dbsr_lib_dbs.f90:724-783.  hs is the first step (hi/Z for a
+ * point nucleus, 4 ln3 a_fermi * hi for a Fermi nucleus, :738-747).
+ * Writes t(1:ns+ks) into t_out and returns ns (or -1 if max_t is too
+ * small). */
+int orc_mkgrid_01(int ks, int ml, double hs, double hi_unused, double he,
+                  double hmax, double rmax, double *t_out, int max_t) {
+  (void)hi_unused;
+  double ti = hs * ml;
+  int ns = ks + ml;
+  double ht = 1.0 + he;
+  int ne = ns;
+  for (;;) {
+    double tj = ti * ht;
+    if (tj - ti > hmax) break;
+    ns = ns + 1;
+    ti = tj;
+    ne = ns;
+    if (ti > rmax) {
+      ns = ns - 1;
+      break;
+    }
+  }
+  if (ti < rmax) {
+    for (;;) {
+      ti = ti + hmax;
+      if (ti >= rmax) break;
+      ns = ns + 1;
+    }
+  }
+  if (ns + ks > max_t) return -1;
+  double *t = t_out - 1; /* 1-based view */
+  for (int i = 1; i <= ns + ks; i++) t[i] = 0.0;
+  for (int i = ks + 1; i <= ks + ml; i++) t[i] = hs * (i - ks);
+  for (int i = ks + ml + 1; i <= ne; i++) t[i] = t[i - 1] * ht;
+  if (t[ne] < rmax)
+    for (int i = ne + 1; i <= ns + 1; i++) t[i] = t[i - 1] + hmax;
+  for (int i = ns + 2; i <= ns + ks; i++) t[i] = t[ns + 1];
+  return ns;
+}
+
+/* ------------------------------------------------------------------ */
+/* zbsplvd / zbsplvb: dbsr_lib_dbs.f90:4197-4468 (vector form of de
+ * Boor's bsplvd/bsplvb).  dbiatx has the declared shape (nv,ks,ks). */
+typedef struct {
+  const double *t; /* 1-based view */
+  int ks, nv, ni;
+  double *deltar, *deltal; /* (ni,ks) */
+  double *saved;           /* (ni) */
+  int j;                   /* the SAVEd order counter of zbsplvb */
+} bspl_ws;
+
+static void zbsplvb(bspl_ws *s, int kg, const double *x, int jhigh, int index,
+                    double *biatx) {
+  const int ni = s->ni, nv = s->nv;
+  const double *t = s->t;
+  double *saved = s->saved, term;
+  if (index == 1) {
+    s->j = 1;
+    for (int i = 1; i <= ni; i++) A2(biatx, i, 1, nv) = 1.0;
+    if (s->j >= jhigh) return;
+  }
+  for (;;) {
+    int j = s->j, jp1 = j + 1;
+    for (int i = 1; i <= ni; i++) saved[i - 1] = 0.0;
+    for (int i = 1; i <= ni; i++) {
+      A2(s->deltar, i, j, ni) = t[i + kg - 1 + j] - x[i - 1];
+      A2(s->deltal, i, j, ni) = x[i - 1] - t[i + kg - j];
+    }
+    for (int m = 1; m <= j; m++) {
+      for (int i = 1; i <= ni; i++) {
+        term = A2(biatx, i, m, nv) /
+               (A2(s->deltar, i, m, ni) + A2(s->deltal, i, jp1 - m, ni));
+        A2(biatx, i, m, nv) = saved[i - 1] + A2(s->deltar, i, m, ni) * term;
+        saved[i - 1] = A2(s->deltal, i, jp1 - m, ni) * term;
+      }
+    }
+    for (int i = 1; i <= ni; i++) A2(biatx, i, jp1, nv) = saved[i - 1];
+    s->j = jp1;
+    if (s->j >= jhigh) break;
+  }
+}
+
+void orc_zbsplvd(int ns, int ks, int nv, const double *t, int kg, int ni,
+                 const double *x, int nderiv, double *dbiatx) {
+  (void)ns;
+  /* per-point work arrays; ni is at most nv */
+  double *deltar = (double *)calloc((size_t)ni * ks, sizeof(double));
+  double *deltal = (double *)calloc((size_t)ni * ks, sizeof(double));
+  double *savedv = (double *)calloc((size_t)ni, sizeof(double));
+  bspl_ws s = {t - 1, ks, nv, ni, deltar, deltal, savedv, 1};
+  int mhigh = imax(imin(nderiv, ks), 1);
+  int kp1 = ks + 1;
+  int jhigh = kp1 - mhigh;
+  zbsplvb(&s, kg, x, jhigh, 1, dbiatx);
+  if (mhigh == 1) {
+    free(deltar);
+    free(deltal);
+    free(savedv);
+    return;
+  }
+  int ideriv = mhigh;
+  for (int m = 2; m <= mhigh; m++) {
+    int jpimid = 1;
+    for (int j = ideriv; j <= ks; j++) {
+      for (int i = 1; i <= ni; i++)
+        A3(dbiatx, i, j, ideriv, nv, ks) = A3(dbiatx, i, jpimid, 1, nv, ks);
+      jpimid++;
+    }
+    ideriv--;
+    jhigh = kp1 - ideriv;
+    zbsplvb(&s, kg, x, jhigh, 2, dbiatx);
+  }
+  double *w31 = (double *)calloc((size_t)ni * ks * ks, sizeof(double));
+  double *w1 = (double *)calloc((size_t)ni, sizeof(double));
+  double *w2 = (double *)calloc((size_t)ni, sizeof(double));
+  const double *tt = t - 1;
+  int jlow = 1;
+  for (int i = 1; i <= ks; i++) {
+    for (int j = jlow; j <= ks; j++)
+      for (int q = 1; q <= ni; q++) A3(w31, q, j, i, ni, ks) = 0.0;
+    jlow = i;
+    for (int q = 1; q <= ni; q++) A3(w31, q, i, i, ni, ks) = 1.0;
+  }
+  for (int m = 2; m <= mhigh; m++) {
+    int kpimm = kp1 - m;
+    double fkpimm = kpimm;
+    int i = ks, il = 0;
+    for (int ld = 1; ld <= kpimm; ld++) {
+      for (int n = kg - il; n <= ni + kg - il - 1; n++)
+        w1[n - kg + il] = fkpimm / (tt[n + kpimm] - tt[n]);
+      for (int j = 1; j <= i; j++)
+        for (int q = 1; q <= ni; q++)
+          A3(w31, q, i, j, ni, ks) =
+              (A3(w31, q, i, j, ni, ks) - A3(w31, q, i - 1, j, ni, ks)) *
+              w1[q - 1];
+      il++;
+      i--;
+    }
+    for (int ii = 1; ii <= ks; ii++) {
+      for (int q = 0; q < ni; q++) w2[q] = 0.0;
+      int jl = imax(ii, m);
+      for (int j = jl; j <= ks; j++)
+        for (int q = 1; q <= ni; q++)
+          w2[q - 1] = w2[q - 1] +
+                      A3(w31, q, j, ii, ni, ks) * A3(dbiatx, q, j, m, nv, ks);
+      for (int q = 1; q <= ni; q++) A3(dbiatx, q, ii, m, nv, ks) = w2[q - 1];
+    }
+  }
+  free(w31);
+  free(w1);
+  free(w2);
+  free(deltar);
+  free(deltal);
+  free(savedv);
+}
+
+/* ZINTYM: dbsr_lib_dbs.f90:4472-4497 */
+static void zintym(int nv, int ks, int ks1, int ks2, const double *b1,
+                   const double *b2, const double *ygr, int mm, double *ym) {
+  memset(ym, 0, sizeof(double) * (size_t)mm * mm);
+  for (int iv = 1; iv <= nv; iv++)
+    for (int ith = 1; ith <= ks1; ith++) {
+      int i = iv + ith - 1;
+      for (int jth = 1; jth <= ks2; jth++) {
+        int j = iv + jth - 1;
+        double s = 0.0;
+        for (int m = 1; m <= ks; m++)
+          s += A2(ygr, iv, m, nv) * A3(b1, iv, m, ith, nv + 1, ks) *
+               A3(b2, iv, m, jth, nv + 1, ks);
+        A2(ym, i, j, mm) = A2(ym, i, j, mm) + s;
+      }
+    }
+}
+
+/* Def_pbsp / Def_qbsp: dbsr_lib_dbs.f90:987-1074 */
+static void def_xbsp(orc_grid *g, int kx, double *tx, double *bsp,
+                     double *bsd) {
+  const int nv = g->nv, ks = g->ks, ns = g->ns;
+  const int nsx = nv + kx - 1, nw = nv + 1;
+  for (int i = 1; i <= kx; i++) tx[i - 1] = g->t[0];
+  for (int i = kx + 1; i <= nsx; i++) tx[i - 1] = g->t[ks + (i - kx) - 1];
+  for (int i = nsx + 1; i <= nsx + kx; i++)
+    tx[i - 1] = g->t[ns + (i - nsx) - 1];
+  double *dbi = (double *)calloc((size_t)nv * kx * kx, sizeof(double));
+  for (int m = 1; m <= ks; m++) {
+    orc_zbsplvd(nsx, kx, nv, tx, kx, nv, &A2(g->gr, 1, m, nv), 2, dbi);
+    for (int ith = 1; ith <= kx; ith++)
+      for (int i = 1; i <= nv; i++) {
+        A3(bsp, i, m, ith, nw, ks) = A3(dbi, i, ith, 1, nv, kx);
+        A3(bsd, i, m, ith, nw, ks) = A3(dbi, i, ith, 2, nv, kx);
+      }
+  }
+  for (int m = 1; m <= ks; m++)
+    for (int ith = 1; ith <= kx; ith++) {
+      A3(bsp, nw, m, ith, nw, ks) = 0.0;
+      A3(bsd, nw, m, ith, nw, ks) = 0.0;
+    }
+  orc_zbsplvd(nsx, kx, nv, tx, nsx, 1, &tx[nsx], 2, dbi);
+  for (int ith = 1; ith <= kx; ith++) {
+    A3(bsp, nw, 1, ith, nw, ks) = A3(dbi, 1, ith, 1, nv, kx);
+    A3(bsd, nw, 1, ith, nw, ks) = A3(dbi, 1, ith, 2, nv, kx);
+  }
+  free(dbi);
+}
+
+/* alloc_DBS_gauss + Def_pbsp + Def_qbsp + Def_pq_arrays:
+ * dbsr_lib_dbs.f90:911-983, 987-1102 (order-ks bsp arrays are not built:
+ * nothing on the assembly path reads them). */
+orc_grid *orc_grid_new(int ns, int ks, int ksp, int ksq, const double *t) {
+  orc_grid *g = (orc_grid *)calloc(1, sizeof(orc_grid));
+  g->ns = ns;
+  g->ks = ks;
+  g->ksp = ksp;
+  g->ksq = ksq;
+  g->nv = ns - ks + 1;
+  g->nsp = g->nv + ksp - 1;
+  g->nsq = g->nv + ksq - 1;
+  g->ms = 2 * ns;
+  const int nv = g->nv, nw = nv + 1, ms = g->ms;
+  g->t = (double *)malloc(sizeof(double) * (ns + ks));
+  memcpy(g->t, t, sizeof(double) * (ns + ks));
+  g->tp = (double *)calloc(g->nsp + ksp, sizeof(double));
+  g->tq = (double *)calloc(g->nsq + ksq, sizeof(double));
+  g->gx = (double *)calloc(ks, sizeof(double));
+  g->gw = (double *)calloc(ks, sizeof(double));
+  g->gr = (double *)calloc((size_t)nv * ks, sizeof(double));
+  g->grw = (double *)calloc((size_t)nv * ks, sizeof(double));
+  g->grm = (double *)calloc((size_t)nv * ks, sizeof(double));
+  g->pbsp = (double *)calloc((size_t)nw * ks * ksp, sizeof(double));
+  g->pbsd = (double *)calloc((size_t)nw * ks * ksp, sizeof(double));
+  g->qbsp = (double *)calloc((size_t)nw * ks * ksq, sizeof(double));
+  g->qbsd = (double *)calloc((size_t)nw * ks * ksq, sizeof(double));
+  size_t nn = (size_t)ns * ns;
+  g->fpbs = (double *)calloc(nn, sizeof(double));
+  g->fqbs = (double *)calloc(nn, sizeof(double));
+  g->fpqbs = (double *)calloc(nn, sizeof(double));
+  g->fqpbs = (double *)calloc(nn, sizeof(double));
+  g->fpqbsd = (double *)calloc(nn, sizeof(double));
+  g->fqpbsd = (double *)calloc(nn, sizeof(double));
+  g->fppqq = (double *)calloc((size_t)ms * ms, sizeof(double));
+
+  orc_gauleg(0.0, 1.0, g->gx, g->gw, ks);
+  const double *tt = g->t - 1;
+  for (int m = 1; m <= ks; m++)
+    for (int i = 1; i <= nv; i++) {
+      double h = tt[ks + i] - tt[ks + i - 1];
+      A2(g->gr, i, m, nv) = h * g->gx[m - 1] + tt[ks + i - 1];
+      A2(g->grm, i, m, nv) = 1.0 / A2(g->gr, i, m, nv);
+      A2(g->grw, i, m, nv) = h * g->gw[m - 1];
+    }
+  def_xbsp(g, ksp, g->tp, g->pbsp, g->pbsd);
+  zintym(nv, ks, ksp, ksp, g->pbsp, g->pbsp, g->grw, ns, g->fpbs);
+  def_xbsp(g, ksq, g->tq, g->qbsp, g->qbsd);
+  zintym(nv, ks, ksq, ksq, g->qbsp, g->qbsp, g->grw, ns, g->fqbs);
+  double *ygw = (double *)calloc((size_t)nv * ks, sizeof(double));
+  for (size_t q = 0; q < (size_t)nv * ks; q++) ygw[q] = g->grm[q] * g->grw[q];
+  zintym(nv, ks, ksp, ksq, g->pbsp, g->qbsp, ygw, ns, g->fpqbs);
+  zintym(nv, ks, ksq, ksp, g->qbsp, g->pbsp, ygw, ns, g->fqpbs);
+  zintym(nv, ks, ksp, ksq, g->pbsp, g->qbsd, g->grw, ns, g->fpqbsd);
+  zintym(nv, ks, ksq, ksp, g->qbsp, g->pbsd, g->grw, ns, g->fqpbsd);
+  free(ygw);
+  for (int j = 1; j <= ns; j++)
+    for (int i = 1; i <= ns; i++) {
+      A2(g->fppqq, i, j, ms) = A2(g->fpbs, i, j, ns);
+      A2(g->fppqq, ns + i, ns + j, ms) = A2(g->fqbs, i, j, ns);
+    }
+  return g;
+}
+
+void orc_grid_free(orc_grid *g) {
+  if (!g) return;
+  free(g->t); free(g->tp); free(g->tq); free(g->gx); free(g->gw);
+  free(g->gr); free(g->grw); free(g->grm); free(g->pbsp); free(g->pbsd);
+  free(g->qbsp); free(g->qbsd); free(g->fpbs); free(g->fqbs);
+  free(g->fpqbs); free(g->fqpbs); free(g->fpqbsd); free(g->fqpbsd);
+  free(g->fppqq);
+  free(g);
+}
+
+/* ------------------------------------------------------------------ */
+/* moment_pp/qq/pq/qp: dbsr_lib_dbs.f90:1401-1564.  rkm(ks*ks,nv);
+ * pp/qq are packed upper-triangular (i<=j), pq/qp full (i outer). */
+void orc_moments(const orc_grid *g, int which, int k, double *rkm) {
+  const int nv = g->nv, ks = g->ks, kk = ks * ks, nw = nv + 1;
+  const double *b1s, *b2s;
+  int k1, k2, sym;
+  switch (which) {
+    case 0: b1s = g->pbsp; b2s = g->pbsp; k1 = g->ksp; k2 = g->ksp; sym = 1; break;
+    case 1: b1s = g->qbsp; b2s = g->qbsp; k1 = g->ksq; k2 = g->ksq; sym = 1; break;
+    case 2: b1s = g->pbsp; b2s = g->qbsp; k1 = g->ksp; k2 = g->ksq; sym = 0; break;
+    default: b1s = g->qbsp; b2s = g->pbsp; k1 = g->ksq; k2 = g->ksp; sym = 0; break;
+  }
+  memset(rkm, 0, sizeof(double) * (size_t)kk * nv);
+  double gwv[64], b2[64 * 16];
+  for (int iv = 1; iv <= nv; iv++) {
+    for (int m = 1; m <= ks; m++) {
+      double w = A2(g->grw, iv, m, nv);
+      if (k > 0) w = A2(g->grw, iv, m, nv) * ipow(A2(g->gr, iv, m, nv), k);
+      if (k < 0) w = A2(g->grw, iv, m, nv) * ipow(A2(g->grm, iv, m, nv), -k);
+      gwv[m - 1] = w;
+    }
+    for (int j = 1; j <= k2; j++)
+      for (int m = 1; m <= ks; m++)
+        b2[(m - 1) + ks * (j - 1)] = A3(b2s, iv, m, j, nw, ks) * gwv[m - 1];
+    int ii = 0;
+    for (int i = 1; i <= k1; i++) {
+      int j0 = sym ? i : 1;
+      for (int j = j0; j <= k2; j++) {
+        ii++;
+        double s = 0.0;
+        for (int m = 1; m <= ks; m++)
+          s += A3(b1s, iv, m, i, nw, ks) * b2[(m - 1) + ks * (j - 1)];
+        A2(rkm, ii, iv, kk) = s;
+      }
+    }
+  }
+}
+
+/* ------------------------------------------------------------------ */
+/* Diagonal-cell integrals triang_*: dbsr_lib_dbs.f90:2979-3063 (pppp),
+ * 3151-3245 (pqpq), 3333-3427 (qpqp), 3512-3597 (qqqq), 3682-3767 (ppqq),
+ * 3852-3936 (pqqp).  Inner integral over [t_iv, r] with ks Gauss points,
+ * B-splines at the inner points from zbsplvd (order ksp or ksq). */
+
+/* values of the kx B-splines nonzero on interval iv at point x */
+static void bvals(const orc_grid *g, int kx, int iv, double x, double *out) {
+  const double *tx = (kx == g->ksp) ? g->tp : g->tq;
+  int nsx = g->nv + kx - 1;
+  /* with ni=1 only dbiatx(1,:,1) is touched, so a leading dimension of 1
+   * addresses the same elements as the reference's (nv,kx,kx) array */
+  double buf[32 * 32];
+  orc_zbsplvd(nsx, kx, 1, tx, iv + kx - 1, 1, &x, 1, buf);
+  for (int j = 1; j <= kx; j++) out[j - 1] = buf[j - 1];
+}
+
+/* INT(j,jp,m) tables for one interval: for each outer point m, the inner
+ * quadrature of B_j B_jp r^k over [t_iv, gr(iv,m)].  full=1 gives all
+ * (j,jp) pairs of bases (ka,kb), full=0 only jp>=j (same basis). */
+static void inner_table(const orc_grid *g, int iv, int k, int ka, int kb,
+                        int full, double *INT /* (ka,kb,ks) */) {
+  const int ks = g->ks, nv = g->nv;
+  double x[32], w[32], gxl[32], gwl[32], ba[32 * 32], bb[32 * 32], v[32];
+  orc_gauleg(0.0, 1.0, x, w, ks);
+  double xbase = g->t[(iv + ks - 1) - 1];
+  for (int m = 1; m <= ks; m++) {
+    double r2 = A2(g->gr, iv, m, nv);
+    for (int i = 0; i < ks; i++) gxl[i] = (r2 - xbase) * x[i] + xbase;
+    for (int i = 0; i < ks; i++) {
+      bvals(g, ka, iv, gxl[i], v);
+      for (int j = 0; j < ka; j++) ba[i + ks * j] = v[j];
+      bvals(g, kb, iv, gxl[i], v);
+      for (int j = 0; j < kb; j++) bb[i + ks * j] = v[j];
+    }
+    for (int i = 0; i < ks; i++) gwl[i] = (r2 - xbase) * w[i];
+    for (int i = 0; i < ks; i++) gxl[i] = gwl[i] * ipow(gxl[i], k);
+    for (int j = 1; j <= ka; j++) {
+      for (int i = 0; i < ks; i++) gwl[i] = gxl[i] * ba[i + ks * (j - 1)];
+      int jp0 = full ? 1 : j;
+      for (int jp = jp0; jp <= kb; jp++) {
+        double s = 0.0;
+        for (int i = 0; i < ks; i++) s += gwl[i] * bb[i + ks * (jp - 1)];
+        A3(INT, j, jp, m, ka, kb) = s;
+      }
+    }
+  }
+}
+
+void orc_triang(const orc_grid *g, int type, int k, double *rkd) {
+  const int ks = g->ks, nv = g->nv, kk = ks * ks, nw = nv + 1;
+  const int ksp = g->ksp, ksq = g->ksq;
+  memset(rkd, 0, sizeof(double) * (size_t)kk * kk * nv);
+  double *INTA = (double *)calloc((size_t)ks * ks * ks, sizeof(double));
+  double *INTB = (double *)calloc((size_t)ks * ks * ks, sizeof(double));
+  double *a = (double *)calloc((size_t)kk * kk, sizeof(double));
+  double gxo[32], bi[32];
+  for (int iv = 1; iv <= nv; iv++) {
+    for (int m = 1; m <= ks; m++)
+      gxo[m - 1] = A2(g->grw, iv, m, nv) * ipow(A2(g->grm, iv, m, nv), k + 1);
+    if (type == 0 || type == 1) { /* pppp / qqqq: a + a^T */
+      int kx = type == 0 ? ksp : ksq;
+      const double *bs = type == 0 ? g->pbsp : g->qbsp;
+      inner_table(g, iv, k, kx, kx, 0, INTA);
+      int ik = kx * (kx + 1) / 2;
+      int ii = 0;
+      for (int i = 1; i <= kx; i++)
+        for (int ip = i; ip <= kx; ip++) {
+          ii++;
+          for (int m = 1; m <= ks; m++)
+            bi[m - 1] = A3(bs, iv, m, i, nw, ks) * A3(bs, iv, m, ip, nw, ks) *
+                        gxo[m - 1];
+          int jj = 0;
+          for (int j = 1; j <= kx; j++)
+            for (int jp = j; jp <= kx; jp++) {
+              jj++;
+              double s = 0.0;
+              for (int m = 1; m <= ks; m++)
+                s += bi[m - 1] * A3(INTA, j, jp, m, kx, kx);
+              A2(a, ii, jj, ik) = s;
+            }
+        }
+      for (int jj = 1; jj <= ik; jj++)
+        for (int ii2 = 1; ii2 <= ik; ii2++)
+          A3(rkd, ii2, jj, iv, kk, kk) = A2(a, ii2, jj, ik) + A2(a, jj, ii2, ik);
+    } else if (type == 2 || type == 3) { /* pqpq / qpqp */
+      inner_table(g, iv, k, ksp, ksp, 0, INTA); /* INTP */
+      inner_table(g, iv, k, ksq, ksq, 0, INTB); /* INTQ */
+      int ii = 0;
+      for (int i = 1; i <= ksp; i++)
+        for (int ip = i; ip <= ksp; ip++) {
+          ii++;
+          for (int m = 1; m <= ks; m++)
+            bi[m - 1] = A3(g->pbsp, iv, m, i, nw, ks) *
+                        A3(g->pbsp, iv, m, ip, nw, ks) * gxo[m - 1];
+          int jj = 0;
+          for (int j = 1; j <= ksq; j++)
+            for (int jp = j; jp <= ksq; jp++) {
+              jj++;
+              double s = 0.0;
+              for (int m = 1; m <= ks; m++)
+                s += bi[m - 1] * A3(INTB, j, jp, m, ksq, ksq);
+              if (type == 2)
+                A3(rkd, ii, jj, iv, kk, kk) = A3(rkd, ii, jj, iv, kk, kk) + s;
+              else
+                A3(rkd, jj, ii, iv, kk, kk) = A3(rkd, jj, ii, iv, kk, kk) + s;
+            }
+        }
+      ii = 0;
+      for (int i = 1; i <= ksq; i++)
+        for (int ip = i; ip <= ksq; ip++) {
+          ii++;
+          for (int m = 1; m <= ks; m++)
+            bi[m - 1] = A3(g->qbsp, iv, m, i, nw, ks) *
+                        A3(g->qbsp, iv, m, ip, nw, ks) * gxo[m - 1];
+          int jj = 0;
+          for (int j = 1; j <= ksp; j++)
+            for (int jp = j; jp <= ksp; jp++) {
+              jj++;
+              double s = 0.0;
+              for (int m = 1; m <= ks; m++)
+                s += bi[m - 1] * A3(INTA, j, jp, m, ksp, ksp);
+              if (type == 2)
+                A3(rkd, jj, ii, iv, kk, kk) = A3(rkd, jj, ii, iv, kk, kk) + s;
+              else
+                A3(rkd, ii, jj, iv, kk, kk) = A3(rkd, ii, jj, iv, kk, kk) + s;
+            }
+        }
+    } else { /* 4 ppqq: outer (P_i,Q_ip), inner (P_j,Q_jp);
+                5 pqqp: outer (Q_i,P_ip), inner (P_j,Q_jp) */
+      inner_table(g, iv, k, ksp, ksq, 1, INTA); /* INTPQ */
+      const double *b1 = type == 4 ? g->pbsp : g->qbsp;
+      const double *b2 = type == 4 ? g->qbsp : g->pbsp;
+      int k1 = type == 4 ? ksp : ksq, k2 = type == 4 ? ksq : ksp;
+      int ii = 0;
+      for (int i = 1; i <= k1; i++)
+        for (int ip = 1; ip <= k2; ip++) {
+          ii++;
+          for (int m = 1; m <= ks; m++)
+            bi[m - 1] = A3(b1, iv, m, i, nw, ks) * A3(b2, iv, m, ip, nw, ks) *
+                        gxo[m - 1];
+          int jj = 0;
+          for (int j = 1; j <= ksp; j++)
+            for (int jp = 1; jp <= ksq; jp++) {
+              jj++;
+              double s = 0.0;
+              for (int m = 1; m <= ks; m++)
+                s += bi[m - 1] * A3(INTA, j, jp, m, ksp, ksq);
+              A3(rkd, jj, ii, iv, kk, kk) = s;
+            }
+        }
+    }
+  }
+  free(INTA);
+  free(INTB);
+  free(a);
+}
+
+/* ------------------------------------------------------------------ */
+/* R^k table fill: mrk_pppp/qqqq/pqpq/qpqp, dbsr_lib_dbs.f90:2898-2959,
+ * 3431-3492, 3067-3131, 3249-3313.  Electron 1 (i,i') in basis A, electron
+ * 2 (j,j') in basis B; off-diagonal cells are products of the 1-D moments,
+ * diagonal cells come from triang_*. */
+void orc_mrk(const orc_grid *g, int type, int k, double *rkb) {
+  const int ns = g->ns, ks = g->ks, nv = g->nv, kk = ks * ks;
+  int wa = (type == 0 || type == 2) ? 0 : 1; /* 0 = P, 1 = Q */
+  int wb = (type == 0 || type == 3) ? 0 : 1;
+  int ka = wa ? g->ksq : g->ksp, kb = wb ? g->ksq : g->ksp;
+  double *lowA = (double *)malloc(sizeof(double) * kk * nv);
+  double *highA = (double *)malloc(sizeof(double) * kk * nv);
+  double *lowB = (double *)malloc(sizeof(double) * kk * nv);
+  double *highB = (double *)malloc(sizeof(double) * kk * nv);
+  double *rkd = (double *)malloc(sizeof(double) * (size_t)kk * kk * nv);
+  orc_moments(g, wa, k, lowA);
+  orc_moments(g, wa, -(k + 1), highA);
+  orc_moments(g, wb, k, lowB);
+  orc_moments(g, wb, -(k + 1), highB);
+  orc_triang(g, type, k, rkd);
+  memset(rkb, 0, sizeof(double) * (size_t)ns * ns * ks * ks);
+  for (int jv = 1; jv <= nv; jv++) {
+    int jj = 0;
+    for (int jh = 1; jh <= kb; jh++) {
+      int j = jv + jh - 1;
+      for (int jhp = jh; jhp <= kb; jhp++) {
+        int jp = jhp - jh + 1;
+        jj++;
+        for (int iv = 1; iv <= nv; iv++) {
+          int ii = 0;
+          for (int ih = 1; ih <= ka; ih++) {
+            int i = iv + ih - 1;
+            for (int ihp = ih; ihp <= ka; ihp++) {
+              int ip = ihp - ih + 1;
+              ii++;
+              double c;
+              if (iv < jv)
+                c = A2(lowA, ii, iv, kk) * A2(highB, jj, jv, kk);
+              else if (iv > jv)
+                c = A2(lowB, jj, jv, kk) * A2(highA, ii, iv, kk);
+              else
+                c = A3(rkd, ii, jj, iv, kk, kk);
+              A4(rkb, i, j, ip, jp, ns, ns, ks) =
+                  A4(rkb, i, j, ip, jp, ns, ns, ks) + c;
+            }
+          }
+        }
+      }
+    }
+  }
+  free(lowA); free(highA); free(lowB); free(highB); free(rkd);
+}
+
+/* S^k table fill: msk_ppqq / msk_pqqp, dbsr_lib_dbs.f90:3601-3662,
+ * 3771-3833.  Only cells iv<=jv; band offsets ip = ihp-ih+ks. */
+void orc_msk(const orc_grid *g, int type, int k, double *rkb) {
+  const int ns = g->ns, ks = g->ks, nv = g->nv, kk = ks * ks, kb2 = 2 * ks - 1;
+  const int ksp = g->ksp, ksq = g->ksq;
+  double *r1 = (double *)malloc(sizeof(double) * kk * nv);
+  double *r2 = (double *)malloc(sizeof(double) * kk * nv);
+  double *rkd = (double *)malloc(sizeof(double) * (size_t)kk * kk * nv);
+  orc_moments(g, 2, k, r1);                       /* pq(k)      */
+  orc_moments(g, type == 0 ? 2 : 3, -(k + 1), r2); /* pq or qp   */
+  orc_triang(g, type == 0 ? 4 : 5, k, rkd);
+  memset(rkb, 0, sizeof(double) * (size_t)ns * ns * kb2 * kb2);
+  int kj1 = type == 0 ? ksp : ksq, kj2 = type == 0 ? ksq : ksp;
+  for (int jv = 1; jv <= nv; jv++) {
+    int jj = 0;
+    for (int jh = 1; jh <= kj1; jh++) {
+      int j = jv + jh - 1;
+      for (int jhp = 1; jhp <= kj2; jhp++) {
+        int jp = jhp - jh + ks;
+        jj++;
+        for (int iv = 1; iv <= jv; iv++) {
+          int ii = 0;
+          for (int ih = 1; ih <= ksp; ih++) {
+            int i = iv + ih - 1;
+            for (int ihp = 1; ihp <= ksq; ihp++) {
+              int ip = ihp - ih + ks;
+              ii++;
+              double c;
+              if (iv == jv)
+                c = A3(rkd, ii, jj, iv, kk, kk);
+              else
+                c = A2(r1, ii, iv, kk) * A2(r2, jj, jv, kk);
+              A4(rkb, i, j, ip, jp, ns, ns, kb2) =
+                  A4(rkb, i, j, ip, jp, ns, ns, kb2) + c;
+            }
+          }
+        }
+      }
+    }
+  }
+  free(r1); free(r2); free(rkd);
+}
+
+/* ------------------------------------------------------------------ */
+/* density: dbsr_lib_dbs.f90:2834-2891 */
+void orc_density(int ns, int ks, double *d, const double *p1,
+                 const double *p2, char type) {
+  const double *P1 = p1 - 1, *P2 = p2 - 1;
+  if (type == 's' || type == 'u') {
+    for (int j = 1; j <= ks; j++)
+      for (int i = 1; i <= ns; i++) A2(d, i, j, ns) = 0.0;
+    for (int i = 1; i <= ns; i++) A2(d, i, 1, ns) = P1[i] * P2[i];
+    for (int j = 2; j <= ks; j++)
+      for (int i = 1; i <= ns - j + 1; i++)
+        A2(d, i, j, ns) = P1[i] * P2[i + j - 1] + P1[i + j - 1] * P2[i];
+  } else if (type == 'l') {
+    for (int j = 1; j <= ks; j++)
+      for (int i = 1; i <= ns; i++) A2(d, i, j, ns) = 0.0;
+    for (int i = 1; i <= ns; i++) A2(d, i, ks, ns) = P1[i] * P2[i];
+    for (int j = 1; j <= ks - 1; j++)
+      for (int i = ks + 1 - j; i <= ns; i++)
+        A2(d, i, j, ns) = P1[i] * P2[i + j - ks] + P1[i + j - ks] * P2[i];
+  } else if (type == 'n') {
+    for (int j = 1; j <= 2 * ks - 1; j++)
+      for (int i = 1; i <= ns; i++) A2(d, i, j, ns) = 0.0;
+    for (int j = 1; j <= 2 * ks - 1; j++) {
+      int i0 = imax(1, 1 + ks - j), i1 = imin(ns, ns + ks - j);
+      for (int i = i0; i <= i1; i++) A2(d, i, j, ns) = P1[i] * P2[i + j - ks];
+    }
+  } else {
+    for (int j = 1; j <= ns; j++)
+      for (int i = 1; i <= ns; i++) A2(d, i, j, ns) = P1[i] * P2[j];
+  }
+}
+
+/* ------------------------------------------------------------------ */
+/* convol / convol_sk: dbsr_lib_dbs.f90:2208-2478, 2482-2752.  The table
+ * is passed explicitly; kb is its declared band extent (ks or 2ks-1). */
+#define RKB(i, j, ip, jp) A4(rkb, i, j, ip, jp, ns, ns, kb)
+#define AA(i, j) A2(a, i, j, ns)
+#define DD(i, j) A2(d, i, j, ns)
+void orc_convol(int ns, int ks, int kb, const double *rkb, double *a,
+                const double *d, int icase, char sym_i, char sym_j) {
+  int ii, jj;
+  double c;
+  if (icase <= 2)
+    for (int j = 1; j <= ks; j++)
+      for (int i = 1; i <= ns; i++) AA(i, j) = 0.0;
+  if (icase > 2)
+    for (int j = 1; j <= ns; j++)
+      for (int i = 1; i <= ns; i++) AA(i, j) = 0.0;
+  const int k2 = ks + ks - 1;
+  switch (icase) {
+    case 1:
+      if (sym_i == 's' && sym_j == 's') {
+        for (int ip = 1; ip <= ks; ip++)
+          for (int i = 1; i <= ns - ip + 1; i++) {
+            c = 0.0;
+            for (int jp = 1; jp <= ks; jp++)
+              for (int j = 1; j <= ns - jp + 1; j++) c = c + DD(j, jp) * RKB(i, j, ip, jp);
+            AA(i, ip) = c;
+          }
+      } else if (sym_i == 'n' && sym_j == 'n') {
+        for (int ip = 1; ip <= k2; ip++) {
+          int i0 = imax(1, 1 + ks - ip), i1 = imin(ns, ns + ks - ip);
+          for (int i = i0; i <= i1; i++) {
+            c = 0.0;
+            for (int jp = 1; jp <= k2; jp++) {
+              int j0 = imax(1, 1 + ks - jp), j1 = imin(ns, ns + ks - jp);
+              for (int j = j0; j <= j1; j++) c = c + DD(j, jp) * RKB(i, j, ip, jp);
+            }
+            AA(i, ip) = c;
+          }
+        }
+      } else if (sym_i == 'l' && sym_j == 'l') {
+        for (int ip = 1; ip <= ks; ip++)
+          for (int i = ks + 1 - ip; i <= ns; i++) {
+            c = 0.0;
+            for (int jp = 1; jp <= ks; jp++)
+              for (int j = ks + 1 - jp; j <= ns; j++) c = c + DD(j, jp) * RKB(i, j, ip, jp);
+            AA(i, ip) = c;
+          }
+      } else if (sym_i == 'l' && sym_j == 'n') {
+        for (int ip = 1; ip <= ks; ip++)
+          for (int i = ks + 1 - ip; i <= ns; i++) {
+            c = 0.0;
+            for (int jp = 1; jp <= k2; jp++) {
+              int j0 = imax(1, 1 + ks - jp), j1 = imin(ns, ns + ks - jp);
+              for (int j = j0; j <= j1; j++) c = c + DD(j, jp) * RKB(i, j, ip, jp);
+            }
+            AA(i, ip) = c;
+          }
+      } else if (sym_i == 'n' && sym_j == 'l') {
+        for (int ip = 1; ip <= k2; ip++) {
+          int i0 = imax(1, 1 + ks - ip), i1 = imin(ns, ns + ks - ip);
+          for (int i = i0; i <= i1; i++) {
+            c = 0.0;
+            for (int jp = 1; jp <= ks; jp++)
+              for (int j = ks + 1 - jp; j <= ns; j++) c = c + DD(j, jp) * RKB(i, j, ip, jp);
+            AA(i, ip) = c;
+          }
+        }
+      }
+      break;
+    case 2:
+      if (sym_i == 's' && sym_j == 's') {
+        for (int jp = 1; jp <= ks; jp++)
+          for (int j = 1; j <= ns - jp + 1; j++) {
+            c = 0.0;
+            for (int ip = 1; ip <= ks; ip++)
+              for (int i = 1; i <= ns - ip + 1; i++) c = c + DD(i, ip) * RKB(i, j, ip, jp);
+            AA(j, jp) = c;
+          }
+      } else if (sym_i == 'n' && sym_j == 'n') {
+        for (int jp = 1; jp <= k2; jp++) {
+          int j0 = imax(1, 1 + ks - jp), j1 = imin(ns, ns + ks - jp);
+          for (int j = j0; j <= j1; j++) {
+            c = 0.0;
+            for (int ip = 1; ip <= k2; ip++) {
+              int i0 = imax(1, 1 + ks - ip), i1 = imin(ns, ns + ks - ip);
+              for (int i = i0; i <= i1; i++) c = c + DD(i, ip) * RKB(i, j, ip, jp);
+            }
+            AA(j, jp) = c;
+          }
+        }
+      } else if (sym_i == 'l' && sym_j == 'l') {
+        for (int jp = 1; jp <= ks; jp++)
+          for (int j = ks + 1 - jp; j <= ns; j++) {
+            c = 0.0;
+            for (int ip = 1; ip <= ks; ip++)
+              for (int i = ks + 1 - ip; i <= ns; i++) c = c + DD(i, ip) * RKB(i, j, ip, jp);
+            AA(j, jp) = c;
+          }
+      } else if (sym_i == 'l' && sym_j == 'n') {
+        for (int jp = 1; jp <= k2; jp++) {
+          int j0 = imax(1, 1 + ks - jp), j1 = imin(ns, ns + ks - jp);
+          for (int j = j0; j <= j1; j++) {
+            c = 0.0;
+            for (int ip = 1; ip <= ks; ip++)
+              for (int i = ks + 1 - ip; i <= ns; i++) c = c + DD(i, ip) * RKB(i, j, ip, jp);
+            AA(j, jp) = c;
+          }
+        }
+      } else if (sym_i == 'n' && sym_j == 'l') {
+        for (int jp = 1; jp <= ks; jp++)
+          for (int j = ks + 1 - jp; j <= ns; j++) {
+            c = 0.0;
+            for (int ip = 1; ip <= k2; ip++) {
+              int i0 = imax(1, 1 + ks - ip), i1 = imin(ns, ns + ks - ip);
+              for (int i = i0; i <= i1; i++) c = c + DD(i, ip) * RKB(i, j, ip, jp);
+            }
+            AA(j, jp) = c;
+          }
+      }
+      break;
+    case 3:
+      if (sym_i == 's' && sym_j == 's') {
+        for (int jp = 1; jp <= ks; jp++)
+          for (int j = 1; j <= ns - jp + 1; j++) {
+            jj = j + jp - 1;
+            for (int ip = 1; ip <= ks; ip++)
+              for (int i = 1; i <= ns - ip + 1; i++) {
+                ii = i + ip - 1;
+                c = RKB(i, j, ip, jp);
+                AA(i, jj) = AA(i, jj) + c * DD(ii, j);
+                if (ip > 1) AA(ii, jj) = AA(ii, jj) + c * DD(i, j);
+                if (jp > 1) AA(i, j) = AA(i, j) + c * DD(ii, jj);
+                if (ip > 1 && jp > 1) AA(ii, j) = AA(ii, j) + c * DD(i, jj);
+              }
+          }
+      } else if (sym_i == 'l' && sym_j == 'l') {
+        for (int jp = 1; jp <= ks; jp++)
+          for (int j = ks + 1 - jp; j <= ns; j++) {
+            jj = j + jp - ks;
+            for (int ip = 1; ip <= ks; ip++)
+              for (int i = ks + 1 - ip; i <= ns; i++) {
+                ii = i + ip - ks;
+                c = RKB(i, j, ip, jp);
+                AA(i, jj) = AA(i, jj) + c * DD(ii, j);
+                if (ip != ks) AA(ii, jj) = AA(ii, jj) + c * DD(i, j);
+                if (jp != ks) AA(i, j) = AA(i, j) + c * DD(ii, jj);
+                if (ip != ks && jp != ks) AA(ii, j) = AA(ii, j) + c * DD(i, jj);
+              }
+          }
+      } else if (sym_i == 'n' && sym_j == 'n') {
+        for (int jp = 1; jp <= k2; jp++) {
+          int j0 = imax(1, 1 + ks - jp), j1 = imin(ns, ns + ks - jp);
+          for (int j = j0; j <= j1; j++) {
+            jj = j + jp - ks;
+            for (int ip = 1; ip <= k2; ip++) {
+              int i0 = imax(1, 1 + ks - ip), i1 = imin(ns, ns + ks - ip);
+              for (int i = i0; i <= i1; i++) {
+                ii = i + ip - ks;
+                c = RKB(i, j, ip, jp);
+                AA(i, jj) = AA(i, jj) + c * DD(ii, j);
+              }
+            }
+          }
+        }
+      } else if (sym_i == 'n' && sym_j == 'l') {
+        for (int jp = 1; jp <= ks; jp++)
+          for (int j = ks + 1 - jp; j <= ns; j++) {
+            jj = j + jp - ks;
+            for (int ip = 1; ip <= k2; ip++) {
+              int i0 = imax(1, 1 + ks - ip), i1 = imin(ns, ns + ks - ip);
+              for (int i = i0; i <= i1; i++) {
+                ii = i + ip - ks;
+                c = RKB(i, j, ip, jp);
+                AA(i, jj) = AA(i, jj) + c * DD(ii, j);
+                if (jp != ks) AA(i, j) = AA(i, j) + c * DD(ii, jj);
+              }
+            }
+          }
+      } else if (sym_i == 'l' && sym_j == 'n') {
+        for (int jp = 1; jp <= k2; jp++) {
+          int j0 = imax(1, 1 + ks - jp), j1 = imin(ns, ns + ks - jp);
+          for (int j = j0; j <= j1; j++) {
+            jj = j + jp - ks;
+            for (int ip = 1; ip <= ks; ip++)
+              for (int i = ks + 1 - ip; i <= ns; i++) {
+                ii = i + ip - ks;
+                c = RKB(i, j, ip, jp);
+                AA(i, jj) = AA(i, jj) + c * DD(ii, j);
+                if (ip != ks) AA(ii, jj) = AA(ii, jj) + c * DD(i, j);
+              }
+          }
+        }
+      }
+      break;
+    case 4:
+      if (sym_i == 's' && sym_j == 's') {
+        for (int jp = 1; jp <= ks; jp++)
+          for (int j = 1; j <= ns - jp + 1; j++) {
+            jj = j + jp - 1;
+            for (int ip = 1; ip <= ks; ip++)
+              for (int i = 1; i <= ns - ip + 1; i++) {
+                ii = i + ip - 1;
+                c = RKB(i, j, ip, jp);
+                AA(ii, j) = AA(ii, j) + c * DD(i, jj);
+                if (ip > 1) AA(i, j) = AA(i, j) + c * DD(ii, jj);
+                if (jp > 1) AA(ii, jj) = AA(ii, jj) + c * DD(i, j);
+                if (ip > 1 && jp > 1) AA(i, jj) = AA(i, jj) + c * DD(ii, j);
+              }
+          }
+      } else if (sym_i == 'n' && sym_j == 'n') {
+        for (int jp = 1; jp <= k2; jp++) {
+          int j0 = imax(1, 1 + ks - jp), j1 = imin(ns, ns + ks - jp);
+          for (int j = j0; j <= j1; j++) {
+            jj = j + jp - ks;
+            for (int ip = 1; ip <= k2; ip++) {
+              int i0 = imax(1, 1 + ks - ip), i1 = imin(ns, ns + ks - ip);
+              for (int i = i0; i <= i1; i++) {
+                ii = i + ip - ks;
+                c = RKB(i, j, ip, jp);
+                AA(ii, j) = AA(ii, j) + c * DD(i, jj);
+              }
+            }
+          }
+        }
+      } else if (sym_i == 'l' && sym_j == 'l') {
+        for (int jp = 1; jp <= ks; jp++)
+          for (int j = ks + 1 - jp; j <= ns; j++) {
+            jj = j + jp - ks;
+            for (int ip = 1; ip <= ks; ip++)
+              for (int i = ks + 1 - ip; i <= ns; i++) {
+                ii = i + ip - ks;
+                c = RKB(i, j, ip, jp);
+                AA(ii, j) = AA(ii, j) + c * DD(i, jj);
+                if (ip != ks) AA(i, j) = AA(i, j) + c * DD(ii, jj);
+                if (jp != ks) AA(ii, jj) = AA(ii, jj) + c * DD(i, j);
+                if (ip != ks && jp != ks) AA(i, jj) = AA(i, jj) + c * DD(ii, j);
+              }
+          }
+      } else if (sym_i == 'n' && sym_j == 'l') {
+        for (int jp = 1; jp <= ks; jp++)
+          for (int j = ks + 1 - jp; j <= ns; j++) {
+            jj = j + jp - ks;
+            for (int ip = 1; ip <= k2; ip++) {
+              int i0 = imax(1, 1 + ks - ip), i1 = imin(ns, ns + ks - ip);
+              for (int i = i0; i <= i1; i++) {
+                ii = i + ip - ks;
+                c = RKB(i, j, ip, jp);
+                AA(ii, j) = AA(ii, j) + c * DD(i, jj);
+                if (jp != ks) AA(ii, jj) = AA(ii, jj) + c * DD(i, j);
+              }
+            }
+          }
+      } else if (sym_i == 'l' && sym_j == 'n') {
+        for (int jp = 1; jp <= k2; jp++) {
+          int j0 = imax(1, 1 + ks - jp), j1 = imin(ns, ns + ks - jp);
+          for (int j = j0; j <= j1; j++) {
+            jj = j + jp - ks;
+            for (int ip = 1; ip <= ks; ip++)
+              for (int i = ks + 1 - ip; i <= ns; i++) {
+                ii = i + ip - ks;
+                c = RKB(i, j, ip, jp);
+                AA(ii, j) = AA(ii, j) + c * DD(i, jj);
+                if (ip != ks) AA(i, j) = AA(i, j) + c * DD(ii, jj);
+              }
+          }
+        }
+      }
+      break;
+    default:
+      break;
+  }
+}
+#undef RKB
+#undef AA
+#undef DD
+
+/* SUM_AmB: dbsr_lib_dbs.f90:4027-4080 */
+double orc_sum_amb(int ns, int ks, const double *a, const double *b,
+                   char sym) {
+  double x = 0.0;
+  if (sym == 'x') {
+    for (int i = 1; i <= ns; i++)
+      for (int j = 1; j <= ns; j++) x = x + A2(a, i, j, ns) * A2(b, i, j, ns);
+  } else if (sym == 's') {
+    for (int j = 1; j <= ks; j++)
+      for (int i = 1; i <= ns - j + 1; i++) x = x + A2(a, i, j, ns) * A2(b, i, j, ns);
+  } else if (sym == 'l') {
+    for (int j = 1; j <= ks; j++)
+      for (int i = ks + 1 - j; i <= ns; i++) x = x + A2(a, i, j, ns) * A2(b, i, j, ns);
+  } else if (sym == 'n') {
+    for (int j = 1; j <= 2 * ks - 1; j++) {
+      int i0 = imax(1, 1 + ks - j), i1 = imin(ns, ns + ks - j);
+      for (int i = i0; i <= i1; i++) x = x + A2(a, i, j, ns) * A2(b, i, j, ns);
+    }
+  }
+  return x;
+}
+
+/* quadr: dbsr_lib_dbs.f90:3940-3976; fi,fj are (ns,2) */
+static double quadr_part(const orc_grid *g, const double *fi, const double *fj,
+                         int m, int comp) {
+  const int nv = g->nv, ks = g->ks, ns = g->ns, nw = nv + 1;
+  const int kx = comp == 0 ? g->ksp : g->ksq;
+  const double *bs = comp == 0 ? g->pbsp : g->qbsp;
+  const double *Fi = fi + (size_t)ns * comp - 1, *Fj = fj + (size_t)ns * comp - 1;
+  double q = 0.0, gxl[64], gwl[64];
+  for (int iv = 1; iv <= nv; iv++) {
+    for (int mm = 1; mm <= ks; mm++)
+      gxl[mm - 1] = ipow(A2(g->gr, iv, mm, nv), m) * A2(g->grw, iv, mm, nv);
+    for (int ith = 1; ith <= kx; ith++) {
+      int i = iv + ith - 1;
+      double pi = Fi[i];
+      for (int mm = 1; mm <= ks; mm++)
+        gwl[mm - 1] = gxl[mm - 1] * A3(bs, iv, mm, ith, nw, ks);
+      for (int jth = 1; jth <= kx; jth++) {
+        int j = iv + jth - 1;
+        double pj = Fj[j], s = 0.0;
+        for (int mm = 1; mm <= ks; mm++) s += A3(bs, iv, mm, jth, nw, ks) * gwl[mm - 1];
+        q = q + s * pi * pj;
+      }
+    }
+  }
+  return q;
+}
+
+double orc_quadr(const orc_grid *g, const double *fi, const double *fj,
+                 int m) {
+  /* the reference accumulates the Q part onto the running P sum */
+  const int nv = g->nv, ks = g->ks, ns = g->ns, nw = nv + 1;
+  double q = quadr_part(g, fi, fj, m, 0);
+  const double *Fi = fi + ns - 1, *Fj = fj + ns - 1;
+  double gxl[64], gwl[64];
+  for (int iv = 1; iv <= nv; iv++) {
+    for (int mm = 1; mm <= ks; mm++)
+      gxl[mm - 1] = ipow(A2(g->gr, iv, mm, nv), m) * A2(g->grw, iv, mm, nv);
+    for (int ith = 1; ith <= g->ksq; ith++) {
+      int i = iv + ith - 1;
+      double qi = Fi[i];
+      for (int mm = 1; mm <= ks; mm++)
+        gwl[mm - 1] = gxl[mm - 1] * A3(g->qbsp, iv, mm, ith, nw, ks);
+      for (int jth = 1; jth <= g->ksq; jth++) {
+        int j = iv + jth - 1;
+        double qj = Fj[j], s = 0.0;
+        for (int mm = 1; mm <= ks; mm++)
+          s += A3(g->qbsp, iv, mm, jth, nw, ks) * gwl[mm - 1];
+        q = q + s * qi * qj;
+      }
+    }
+  }
+  return q;
+}
+
+/* rk: dbsr_lib_dbs.f90:3981-4022 */
+double orc_rk(const orc_grid *g, const double *f1, const double *f2,
+              const double *f3, const double *f4, int k) {
+  const int ns = g->ns, ks = g->ks;
+  size_t nb = (size_t)ns * ks;
+  double *d1 = (double *)malloc(sizeof(double) * nb);
+  double *d2 = (double *)malloc(sizeof(double) * nb);
+  double *d3 = (double *)malloc(sizeof(double) * nb);
+  double *d4 = (double *)malloc(sizeof(double) * nb);
+  double *cv = (double *)malloc(sizeof(double) * nb);
+  double *rkb = (double *)malloc(sizeof(double) * (size_t)ns * ns * ks * ks);
+  orc_density(ns, ks, d1, f1, f3, 's');
+  orc_density(ns, ks, d2, f2, f4, 's');
+  orc_density(ns, ks, d3, f1 + ns, f3 + ns, 's');
+  orc_density(ns, ks, d4, f2 + ns, f4 + ns, 's');
+  double r = 0.0;
+  orc_mrk(g, 0, k, rkb);
+  orc_convol(ns, ks, ks, rkb, cv, d1, 2, 's', 's');
+  r = r + orc_sum_amb(ns, ks, cv, d2, 's');
+  orc_mrk(g, 1, k, rkb);
+  orc_convol(ns, ks, ks, rkb, cv, d3, 2, 's', 's');
+  r = r + orc_sum_amb(ns, ks, cv, d4, 's');
+  orc_mrk(g, 3, k, rkb);
+  orc_convol(ns, ks, ks, rkb, cv, d3, 2, 's', 's');
+  r = r + orc_sum_amb(ns, ks, cv, d2, 's');
+  orc_mrk(g, 2, k, rkb);
+  orc_convol(ns, ks, ks, rkb, cv, d1, 2, 's', 's');
+  r = r + orc_sum_amb(ns, ks, cv, d4, 's');
+  free(d1); free(d2); free(d3); free(d4); free(cv); free(rkb);
+  return r;
+}
+
+/* ------------------------------------------------------------------ */
+/* DBSR_MAT3 matrix structures */
+orc_mat *orc_mat_new(const orc_grid *g, int nbf, const double *pq,
+                     const int *ipbs, int nch, const int *icc, int iicc,
+                     double *hch, int mk, double *acf) {
+  orc_mat *m = (orc_mat *)calloc(1, sizeof(orc_mat));
+  m->g = g;
+  m->nbf = nbf;
+  m->pq = pq;
+  m->ipbs = ipbs;
+  m->nch = nch;
+  m->icc = icc;
+  m->iicc = iicc;
+  m->hch = hch;
+  m->mk = mk;
+  m->acf = acf;
+  m->kmax_cache = mk + 2;
+  m->rcache = (double **)calloc((size_t)(m->kmax_cache + 1) * 4, sizeof(double *));
+  m->scache = (double **)calloc((size_t)(m->kmax_cache + 1) * 2, sizeof(double *));
+  return m;
+}
+
+void orc_mat_free(orc_mat *m) {
+  if (!m) return;
+  for (int i = 0; i < (m->kmax_cache + 1) * 4; i++) free(m->rcache[i]);
+  for (int i = 0; i < (m->kmax_cache + 1) * 2; i++) free(m->scache[i]);
+  free(m->rcache);
+  free(m->scache);
+  free(m);
+}
+
+/* cached table lookup (the irka flag, dbsr_lib_dbs.f90:2919-2925) */
+static const double *rtable(orc_mat *m, int type, int k) {
+  double **slot = &m->rcache[k * 4 + type];
+  if (!*slot) {
+    const orc_grid *g = m->g;
+    *slot = (double *)malloc(sizeof(double) * (size_t)g->ns * g->ns * g->ks * g->ks);
+    orc_mrk(g, type, k, *slot);
+  }
+  return *slot;
+}
+static const double *stable(orc_mat *m, int type, int k) {
+  double **slot = &m->scache[k * 2 + type];
+  if (!*slot) {
+    const orc_grid *g = m->g;
+    size_t kb = 2 * g->ks - 1;
+    *slot = (double *)malloc(sizeof(double) * (size_t)g->ns * g->ns * kb * kb);
+    orc_msk(g, type, k, *slot);
+  }
+  return *slot;
+}
+
+#define ICC(i, j) A2(m->icc, i, j, m->nch)
+#define HCH(i, j, b) A3(m->hch, i, j, b, ms, ms)
+
+/* UPDATE_HS: DBSR_MAT3/updates.f90:110-179 */
+void orc_update_hs(orc_mat *m, int ich, int jch, const double *d, char sym,
+                   int ii, int jj) {
+  const int ns = m->g->ns, ks = m->g->ks, ms = m->g->ms;
+  double *y = (double *)calloc((size_t)ns * ns, sizeof(double));
+  if (sym == 's') {
+    for (int jp = 1; jp <= ks; jp++)
+      for (int i = 1; i <= ns - jp + 1; i++) {
+        int j = i + jp - 1;
+        A2(y, i, j, ns) = A2(d, i, jp, ns);
+        A2(y, j, i, ns) = A2(d, i, jp, ns);
+      }
+  } else if (sym == 'n') {
+    for (int jp = 1; jp <= ks + ks - 1; jp++) {
+      int i0 = imax(1, 1 + ks - jp), i1 = imin(ns, ns + ks - jp);
+      for (int i = i0; i <= i1; i++) A2(y, i, i + jp - ks, ns) = A2(d, i, jp, ns);
+    }
+  } else {
+    memcpy(y, d, sizeof(double) * (size_t)ns * ns);
+  }
+  int b = ICC(ich, jch);
+  int i1 = 1 + (ii - 1) * ns, j1 = 1 + (jj - 1) * ns;
+  if (ich > jch) {
+    for (int j = 1; j <= ns; j++)
+      for (int i = 1; i <= ns; i++)
+        HCH(i1 + i - 1, j1 + j - 1, b) = HCH(i1 + i - 1, j1 + j - 1, b) + A2(y, i, j, ns);
+  } else if (jch > ich) {
+    for (int j = 1; j <= ns; j++)
+      for (int i = 1; i <= ns; i++)
+        HCH(i1 + i - 1, j1 + j - 1, b) = HCH(i1 + i - 1, j1 + j - 1, b) + A2(y, j, i, ns);
+  } else {
+    for (size_t q = 0; q < (size_t)ns * ns; q++) y[q] = y[q] / 2.0;
+    for (int j = 1; j <= ns; j++)
+      for (int i = 1; i <= ns; i++)
+        HCH(i1 + i - 1, j1 + j - 1, b) = HCH(i1 + i - 1, j1 + j - 1, b) + A2(y, i, j, ns);
+    for (int j = 1; j <= ns; j++)
+      for (int i = 1; i <= ns; i++)
+        HCH(j1 + i - 1, i1 + j - 1, b) = HCH(j1 + i - 1, i1 + j - 1, b) + A2(y, j, i, ns);
+  }
+  free(y);
+}
+
+/* UPDATE_HX: updates.f90:79-106 */
+void orc_update_hx(orc_mat *m, int ich, int jch, const double *d, double c) {
+  const int ms = m->g->ms;
+  int b = ICC(ich, jch);
+  for (int j = 1; j <= ms; j++)
+    for (int i = 1; i <= ms; i++) {
+      double x = ich >= jch ? c * A2(d, i, j, ms) : c * A2(d, j, i, ms);
+      HCH(i, j, b) = HCH(i, j, b) + x;
+    }
+}
+
+/* UPDATE_HW: updates.f90:183-216 */
+void orc_update_hw(orc_mat *m, int ich, int jch, const double *v,
+                   const double *w, double c) {
+  const int ms = m->g->ms;
+  int b = ICC(ich, jch);
+  for (int j = 1; j <= ms; j++)
+    for (int i = 1; i <= ms; i++) {
+      double xx;
+      if (ich > jch)
+        xx = c * (v[i - 1] * w[j - 1]);
+      else if (jch > ich)
+        xx = c * (v[j - 1] * w[i - 1]);
+      else
+        xx = (c / 2.0) * (v[i - 1] * w[j - 1] + v[j - 1] * w[i - 1]);
+      HCH(i, j, b) = HCH(i, j, b) + xx;
+    }
+}
+
+/* UPDATE_ACF: updates.f90:268-292 */
+static void update_acf(orc_mat *m, int k, int ich, int jch, double c) {
+  int b = ICC(ich, jch);
+  A2(m->acf, b, k + 1, m->iicc) = A2(m->acf, b, k + 1, m->iicc) + c;
+}
+
+/* V_ch restatement (Get_v_ch is not in the reference snapshot): the
+ * B-spline overlap vector of a bound orbital, <B_i|P_b> and <B_i|Q_b>. */
+void orc_v_ch(const orc_grid *g, const double *pq_b, double *v) {
+  const int ns = g->ns;
+  for (int i = 1; i <= ns; i++) {
+    double sp = 0.0, sq = 0.0;
+    for (int j = 1; j <= ns; j++) {
+      sp += A2(g->fpbs, i, j, ns) * pq_b[j - 1];
+      sq += A2(g->fqbs, i, j, ns) * pq_b[ns + j - 1];
+    }
+    v[i - 1] = sp;
+    v[ns + i - 1] = sq;
+  }
+}
+
+#define PQ(orb, comp) (m->pq + (size_t)ns * ((comp)-1) + (size_t)2 * ns * ((orb)-1))
+
+/* R_data itype 3 (direct) and 4 (exchange): DBSR_MAT3/R_data.f90:56-86,
+ * 214-277.  QUADR_PQ (not in the reference snapshot) is restated as the
+ * component of quadr selected by atype (P for atype 0, Q for atype 1). */
+static int r_data(orc_mat *m, int itype, int kpol, int btype, int ncdata,
+                  const int *ipt, const int *k1, const int *k2, const int *k3,
+                  const double *cdata) {
+  const orc_grid *g = m->g;
+  const int ns = g->ns, ks = g->ks;
+  int ip1, ip2, jp1, jp2, in;
+  char sym_d, sym_r;
+  if (itype == 3) { in = 1; sym_d = 's'; sym_r = 's'; }
+  else if (itype == 4) { in = 3; sym_d = 'x'; sym_r = 'x'; }
+  else return -2;
+  int atype = btype;
+  switch (atype) {
+    case 0: ip1 = 1; ip2 = 1; jp1 = 1; jp2 = 1; break;
+    case 1: ip1 = 2; ip2 = 2; jp1 = 2; jp2 = 2; break;
+    case 2: ip1 = 1; ip2 = 1; jp1 = 2; jp2 = 2;
+      if (itype == 4) { ip1 = 1; ip2 = 2; jp1 = 1; jp2 = 2; }
+      break;
+    default: ip1 = 2; ip2 = 2; jp1 = 1; jp2 = 1;
+      if (itype == 4) { ip1 = 2; ip2 = 1; jp1 = 2; jp2 = 1; }
+      break;
+  }
+  const double *rkb = rtable(m, atype, kpol);
+  size_t nn = (size_t)ns * ns;
+  double *xx = (double *)calloc(nn, sizeof(double));
+  double *dd = (double *)calloc(nn, sizeof(double));
+  double CA = 0.0;
+  for (int j = 1; j <= ncdata; j++) {
+    int i = ipt[j - 1];
+    int j1 = k2[i - 1], j2 = k3[i - 1];
+    orc_density(ns, ks, dd, PQ(j1, jp1), PQ(j2, jp2), sym_d);
+    int ncol = sym_d == 's' ? ks : ns;
+    for (size_t q = 0; q < (size_t)ns * ncol; q++) xx[q] = xx[q] + cdata[i - 1] * dd[q];
+    if (itype == 3 && atype <= 1) {
+      double S = quadr_part(g, PQ(j1, 1), PQ(j2, 1), kpol, atype);
+      CA = CA + cdata[i - 1] * S;
+    }
+    int last = 1;
+    if (j < ncdata && k1[i - 1] == k1[ipt[j] - 1]) last = 0;
+    if (!last) continue;
+    orc_convol(ns, ks, ks, rkb, dd, xx, in, 's', 's');
+    int ich = k1[i - 1] / ORC_IBO, jch = k1[i - 1] % ORC_IBO;
+    orc_update_hs(m, ich, jch, dd, sym_r, ip1, ip2);
+    if (itype == 3 && atype <= 1) update_acf(m, kpol, ich, jch, CA);
+    memset(xx, 0, nn * sizeof(double));
+    CA = 0.0;
+  }
+  free(xx);
+  free(dd);
+  return 0;
+}
+
+/* S_data itypes 6-9: DBSR_MAT3/S_data.f90:67-113, 240-274, with the
+ * contraction taken with convol_sk semantics (the S^k table). */
+static int s_data(orc_mat *m, int ktype, int kpol, int ncdata, const int *ipt,
+                  const int *k1, const int *k2, const int *k3,
+                  const double *cdata) {
+  const orc_grid *g = m->g;
+  const int ns = g->ns, ks = g->ks;
+  int atype = ktype / 10, itype = ktype % 10;
+  int ip1, ip2, jp1, jp2, in;
+  if (itype < 6 || itype > 9 || atype < 0 || atype > 1) return -2;
+  if (atype == 0) {
+    switch (itype) {
+      case 6: ip1 = 1; ip2 = 2; jp1 = 1; jp2 = 2; in = 1; break;
+      case 7: ip1 = 1; ip2 = 2; jp1 = 1; jp2 = 2; in = 2; break;
+      case 8: ip1 = 1; ip2 = 2; jp1 = 2; jp2 = 1; in = 3; break;
+      default: ip1 = 2; ip2 = 1; jp1 = 1; jp2 = 2; in = 4; break;
+    }
+  } else {
+    switch (itype) {
+      case 6: ip1 = 1; ip2 = 2; jp1 = 2; jp2 = 1; in = 1; break;
+      case 7: ip1 = 2; ip2 = 1; jp1 = 1; jp2 = 2; in = 2; break;
+      case 8: ip1 = 1; ip2 = 1; jp1 = 2; jp2 = 2; in = 3; break;
+      default: ip1 = 2; ip2 = 2; jp1 = 1; jp2 = 1; in = 4; break;
+    }
+  }
+  char sym_d = in <= 2 ? 'n' : 'x', sym_r = sym_d;
+  const double *rkb = stable(m, atype, kpol);
+  size_t nn = (size_t)ns * ns;
+  double *xx = (double *)calloc(nn, sizeof(double));
+  double *dd = (double *)calloc(nn, sizeof(double));
+  for (int j = 1; j <= ncdata; j++) {
+    int i = ipt[j - 1];
+    int i1 = k2[i - 1], j1 = k3[i - 1];
+    orc_density(ns, ks, dd, PQ(i1, jp1), PQ(j1, jp2), sym_d);
+    int ncol = sym_d == 'n' ? 2 * ks - 1 : ns;
+    for (size_t q = 0; q < (size_t)ns * ncol; q++) xx[q] = xx[q] + cdata[i - 1] * dd[q];
+    int last = 1;
+    if (j < ncdata && k1[i - 1] == k1[ipt[j] - 1]) last = 0;
+    if (!last) continue;
+    orc_convol(ns, ks, 2 * ks - 1, rkb, dd, xx, in, 'n', 'n');
+    int ich = k1[i - 1] / ORC_IBO, jch = k1[i - 1] % ORC_IBO;
+    orc_update_hs(m, ich, jch, dd, sym_r, ip1, ip2);
+    memset(xx, 0, nn * sizeof(double));
+  }
+  free(xx);
+  free(dd);
+  return 0;
+}
+
+/* O_data itype 3 (<i|.><.|j> rank-1 overlaps): O_data.f90:50-61 */
+static int o_data(orc_mat *m, int itype, int ncdata, const int *ipt,
+                  const int *k1, const int *k2, const double *cdata) {
+  const orc_grid *g = m->g;
+  const int ns = g->ns, ms = g->ms;
+  if (itype != 3) return -2;
+  double *v = (double *)malloc(sizeof(double) * ms);
+  double *w = (double *)malloc(sizeof(double) * ms);
+  for (int j = 1; j <= ncdata; j++) {
+    int i = ipt[j - 1];
+    double C = cdata[i - 1];
+    if (fabs(C) < 1.0e-10) continue; /* eps_c, mod_dbsr_mat.f90:56 */
+    int io = k1[i - 1], jo = k2[i - 1];
+    int i1 = io / ORC_IBO, i2 = io % ORC_IBO;
+    int j1 = jo / ORC_IBO, j2 = jo % ORC_IBO;
+    orc_v_ch(g, PQ(i2, 1), v);
+    orc_v_ch(g, PQ(j2, 1), w);
+    orc_update_hw(m, m->ipbs[i1 - 1], m->ipbs[j1 - 1], v, w, C);
+  }
+  free(v);
+  free(w);
+  (void)ns;
+  return 0;
+}
+
+/* Gen_matrix: DBSR_MAT3/gen_matrix.f90:2-17 */
+int orc_gen_matrix(orc_mat *m, int icase, int itype, int kpol, int ncdata,
+                   const int *ipt, const int *k1, const int *k2,
+                   const int *k3, const int *k4, const double *cdata) {
+  (void)k4;
+  if (ncdata == 0) return 0;
+  if (kpol < 0 || kpol > m->kmax_cache) return -3;
+  switch (icase) {
+    case 0:
+      return o_data(m, itype, ncdata, ipt, k1, k2, cdata);
+    case 2:
+      for (int bt = 0; bt <= 3; bt++) {
+        int rc = r_data(m, itype, kpol, bt, ncdata, ipt, k1, k2, k3, cdata);
+        if (rc) return rc;
+      }
+      return 0;
+    case 3:
+      return s_data(m, itype, kpol, ncdata, ipt, k1, k2, k3, cdata);
+    default:
+      return -1;
+  }
+}
+
+/* ------------------------------------------------------------------ */
+/* Add_cdata semantics (MOD_c_data.f90:177-236) for a whole raw list:
+ * entries are ordered by (K1,K2,K3,K4) and equal keys are summed in the
+ * order they arrive.  A stable merge sort keeps arrival order among equal
+ * keys, so the sequential sum below adds the coefficients exactly as the
+ * insertion routine does. */
+typedef struct {
+  int k1, k2, k3, k4, pos;
+} key5;
+static int keycmp(const key5 *a, const key5 *b) {
+  if (a->k1 != b->k1) return a->k1 < b->k1 ? -1 : 1;
+  if (a->k2 != b->k2) return a->k2 < b->k2 ? -1 : 1;
+  if (a->k3 != b->k3) return a->k3 < b->k3 ? -1 : 1;
+  if (a->k4 != b->k4) return a->k4 < b->k4 ? -1 : 1;
+  return 0;
+}
+static void msort(key5 *a, key5 *tmp, int n) {
+  if (n < 2) return;
+  int h = n / 2;
+  msort(a, tmp, h);
+  msort(a + h, tmp, n - h);
+  int i = 0, j = h, o = 0;
+  while (i < h && j < n) tmp[o++] = (keycmp(&a[j], &a[i]) < 0) ? a[j++] : a[i++];
+  while (i < h) tmp[o++] = a[i++];
+  while (j < n) tmp[o++] = a[j++];
+  memcpy(a, tmp, sizeof(key5) * n);
+}
+int orc_sort_merge(int n, const int *k1, const int *k2, const int *k3,
+                   const int *k4, const double *c, int *o1, int *o2,
+                   int *o3, int *o4, double *oc) {
+  key5 *a = (key5 *)malloc(sizeof(key5) * (n > 0 ? n : 1));
+  key5 *tmp = (key5 *)malloc(sizeof(key5) * (n > 0 ? n : 1));
+  for (int i = 0; i < n; i++) {
+    a[i].k1 = k1[i]; a[i].k2 = k2[i]; a[i].k3 = k3[i]; a[i].k4 = k4[i];
+    a[i].pos = i;
+  }
+  msort(a, tmp, n);
+  int u = -1;
+  for (int i = 0; i < n; i++) {
+    if (u >= 0 && a[i].k1 == o1[u] && a[i].k2 == o2[u] && a[i].k3 == o3[u] &&
+        a[i].k4 == o4[u]) {
+      oc[u] = oc[u] + c[a[i].pos];
+    } else {
+      u++;
+      o1[u] = a[i].k1; o2[u] = a[i].k2; o3[u] = a[i].k3; o4[u] = a[i].k4;
+      oc[u] = c[a[i].pos];
+    }
+  }
+  free(a);
+  free(tmp);
+  return u + 1;
+}

@@ -1,0 +1,132 @@
+/*
+ * dbsr_oracle.h -- CPU restatement of the DBSR_MAT3 Hamiltonian-block
+ * assembly path, used ONLY as test infrastructure (the checker).
+ *
+ * Nothing in the product (the CUDA library under dbsr_gb300/) links,
+ * loads or calls this code.  Tests, the package smoke check and the
+ * bench's CPU-baseline leg load it through ctypes to produce the
+ * expected results.
+ *
+ * Every routine follows one reference routine loop by loop, keeps the
+ * Fortran column-major layout and 1-based index arithmetic (translated
+ * to 0-based storage offsets), and keeps the reference's summation
+ * order.  File:line citations are relative to the reference project
+ * root (zatsaroi/DBSR3).
+ *
+ * Pinning: the knot generator is checked against the knot files the
+ * reference ships (Rb_bound_example/dbsr_cc27/knot.dat,
+ * DBSR_HF/examples/<name>.knot), the table sizes against the memory lines of
+ * the reference logs, and the whole R^k chain (Gauss grid, B-splines,
+ * moments, diagonal cells, rkb tables, density, convol, SUM_AmB) against
+ * the Dirac-Fock Coulomb energies printed in DBSR_HF/examples/<name>.log for
+ * the orbitals stored in the matching <name>.bsw files.  The matrix-level
+ * routines (R_data/S_data/UPDATE_*) have no reference output to compare
+ * with: the reference ships no dbsr_mat.nnn; their parity is "unpinned"
+ * beyond the restatement itself.
+ */
+#ifndef DBSR_ORACLE_H
+#define DBSR_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ORC_IBO 32768 /* packing basis for orbitals, mod_dbsr_mat.f90:61 */
+
+typedef struct orc_grid {
+  int ns, ks, ksp, ksq, nv, nsp, nsq, ms;
+  double *t;            /* t(ns+ks)                                  */
+  double *tp, *tq;      /* tp(nsp+ksp), tq(nsq+ksq)                  */
+  double *gx, *gw;      /* gauss points/weights on [0,1], (ks)       */
+  double *gr, *grw, *grm; /* (nv,ks)                                 */
+  double *pbsp, *pbsd;  /* (nv+1,ks,ksp)                             */
+  double *qbsp, *qbsd;  /* (nv+1,ks,ksq)                             */
+  double *fpbs, *fqbs;  /* (ns,ns)                                   */
+  double *fpqbs, *fqpbs, *fpqbsd, *fqpbsd; /* (ns,ns)                */
+  double *fppqq;        /* (ms,ms)                                   */
+} orc_grid;
+
+/* ---- level 0: knots, gauss, B-splines (dbsr_lib_dbs.f90, zcom) ---- */
+void orc_gauleg(double x1, double x2, double *x, double *w, int n);
+int orc_mkgrid_01(int ks, int ml, double hs, double hi_unused, double he,
+                  double hmax, double rmax, double *t_out, int max_t);
+void orc_zbsplvd(int ns, int ks, int nv, const double *t, int kg, int ni,
+                 const double *x, int nderiv, double *dbiatx);
+orc_grid *orc_grid_new(int ns, int ks, int ksp, int ksq, const double *t);
+void orc_grid_free(orc_grid *g);
+
+/* ---- level 1: moments and diagonal cells ---- */
+/* which: 0 pp, 1 qq, 2 pq, 3 qp; rkm is (ks*ks, nv) */
+void orc_moments(const orc_grid *g, int which, int k, double *rkm);
+/* type: 0 pppp, 1 qqqq, 2 pqpq, 3 qpqp, 4 ppqq, 5 pqqp; rkd (ks*ks,ks*ks,nv) */
+void orc_triang(const orc_grid *g, int type, int k, double *rkd);
+
+/* ---- level 1b: assembled tables ---- */
+/* R tables, type 0 pppp,1 qqqq,2 pqpq,3 qpqp: rkb(ns,ns,ks,ks)          */
+void orc_mrk(const orc_grid *g, int type, int k, double *rkb);
+/* S tables, type 0 ppqq,1 pqqp: rkb(ns,ns,2ks-1,2ks-1)                   */
+void orc_msk(const orc_grid *g, int type, int k, double *rkb);
+
+/* ---- level 2: density, convol, traces ---- */
+void orc_density(int ns, int ks, double *d, const double *p1,
+                 const double *p2, char type);
+/* kb = band extent of the table: ks for R tables, 2ks-1 for S tables.  */
+void orc_convol(int ns, int ks, int kb, const double *rkb, double *a,
+                const double *d, int icase, char sym_i, char sym_j);
+double orc_sum_amb(int ns, int ks, const double *a, const double *b,
+                   char sym);
+double orc_quadr(const orc_grid *g, const double *fi, const double *fj,
+                 int m);
+double orc_rk(const orc_grid *g, const double *f1, const double *f2,
+              const double *f3, const double *f4, int k);
+
+/* ---- level 3: matrix structures and dispatch (DBSR_MAT3) ---- */
+typedef struct orc_mat {
+  const orc_grid *g;
+  int nbf;            /* number of orbitals (bound + channel)            */
+  const double *pq;   /* pq(ns,2,nbf)                                    */
+  const int *ipbs;    /* ipbs(nbf): channel index of an orbital, or 0    */
+  int nch;            /* number of channels                              */
+  const int *icc;     /* icc(nch,nch), 1-based block index or 0          */
+  int iicc;           /* number of blocks                                */
+  double *hch;        /* hch(ms,ms,iicc)                                 */
+  int mk;             /* max multipole                                   */
+  double *acf;        /* acf(iicc,0:mk)                                  */
+  /* table caches (allocated lazily): R[k*4+type], S[k*2+type]          */
+  int kmax_cache;
+  double **rcache;
+  double **scache;
+} orc_mat;
+
+orc_mat *orc_mat_new(const orc_grid *g, int nbf, const double *pq,
+                     const int *ipbs, int nch, const int *icc, int iicc,
+                     double *hch, int mk, double *acf);
+void orc_mat_free(orc_mat *m);
+
+void orc_update_hs(orc_mat *m, int ich, int jch, const double *d, char sym,
+                   int ii, int jj);
+void orc_update_hx(orc_mat *m, int ich, int jch, const double *d, double c);
+void orc_update_hw(orc_mat *m, int ich, int jch, const double *v,
+                   const double *w, double c);
+
+/* icase 0 O, 2 R, 3 S; lists in Add_matrix order (ipt 1-based). Returns 0
+ * or a negative error code. */
+int orc_gen_matrix(orc_mat *m, int icase, int itype, int kpol, int ncdata,
+                   const int *ipt, const int *k1, const int *k2,
+                   const int *k3, const int *k4, const double *cdata);
+
+/* channel-orbital overlap vector used by O_data (V_ch restatement):
+ * v(1:ns) = fpbs*P_b, v(ns+1:ms) = fqbs*Q_b.                            */
+void orc_v_ch(const orc_grid *g, const double *pq_b, double *v);
+
+/* sorted insertion with merging of equal keys (Add_cdata semantics) for a
+ * whole raw list: returns the number of unique entries written to the
+ * output arrays (sorted by K1,K2,K3,K4). */
+int orc_sort_merge(int n, const int *k1, const int *k2, const int *k3,
+                   const int *k4, const double *c, int *o1, int *o2,
+                   int *o3, int *o4, double *oc);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

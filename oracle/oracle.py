@@ -1,0 +1,251 @@
+"""ctypes front end of the CPU oracle (test infrastructure only).
+
+The oracle is a C restatement of the reference's DBSR_MAT3 assembly path
+(dbsr_oracle.c).  Only tests, ``__graft_entry__.smoke()`` and the
+CPU-baseline leg of ``bench.py`` import this module; the product library
+never does.  ``build()`` compiles the C file into ``oracle/_build``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+IBO = 32768
+
+_lib = None
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+
+
+class _Grid(C.Structure):
+    _fields_ = [(n, C.c_int) for n in ("ns", "ks", "ksp", "ksq", "nv", "nsp", "nsq", "ms")] + [
+        (n, _dp)
+        for n in (
+            "t", "tp", "tq", "gx", "gw", "gr", "grw", "grm", "pbsp", "pbsd", "qbsp", "qbsd",
+            "fpbs", "fqbs", "fpqbs", "fqpbs", "fpqbsd", "fqpbsd", "fppqq",
+        )
+    ]
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle shared library (make in oracle/)."""
+    src = os.path.join(HERE, "dbsr_oracle.c")
+    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(src):
+        subprocess.run(["make", "-s", "-C", HERE], check=True)
+    return LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(LIB_PATH)
+        L.orc_grid_new.restype = C.POINTER(_Grid)
+        L.orc_grid_new.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, _dp]
+        L.orc_grid_free.argtypes = [C.POINTER(_Grid)]
+        L.orc_gauleg.argtypes = [C.c_double, C.c_double, _dp, _dp, C.c_int]
+        L.orc_mkgrid_01.restype = C.c_int
+        L.orc_mkgrid_01.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
+                                    C.c_double, C.c_double, _dp, C.c_int]
+        L.orc_moments.argtypes = [C.POINTER(_Grid), C.c_int, C.c_int, _dp]
+        L.orc_triang.argtypes = [C.POINTER(_Grid), C.c_int, C.c_int, _dp]
+        L.orc_mrk.argtypes = [C.POINTER(_Grid), C.c_int, C.c_int, _dp]
+        L.orc_msk.argtypes = [C.POINTER(_Grid), C.c_int, C.c_int, _dp]
+        L.orc_density.argtypes = [C.c_int, C.c_int, _dp, _dp, _dp, C.c_char]
+        L.orc_convol.argtypes = [C.c_int, C.c_int, C.c_int, _dp, _dp, _dp, C.c_int, C.c_char, C.c_char]
+        L.orc_sum_amb.restype = C.c_double
+        L.orc_sum_amb.argtypes = [C.c_int, C.c_int, _dp, _dp, C.c_char]
+        L.orc_quadr.restype = C.c_double
+        L.orc_quadr.argtypes = [C.POINTER(_Grid), _dp, _dp, C.c_int]
+        L.orc_rk.restype = C.c_double
+        L.orc_rk.argtypes = [C.POINTER(_Grid), _dp, _dp, _dp, _dp, C.c_int]
+        L.orc_mat_new.restype = C.c_void_p
+        L.orc_mat_new.argtypes = [C.POINTER(_Grid), C.c_int, _dp, _ip, C.c_int, _ip, C.c_int,
+                                  _dp, C.c_int, _dp]
+        L.orc_mat_free.argtypes = [C.c_void_p]
+        L.orc_gen_matrix.restype = C.c_int
+        L.orc_gen_matrix.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int,
+                                     _ip, _ip, _ip, _ip, _ip, _dp]
+        L.orc_v_ch.argtypes = [C.POINTER(_Grid), _dp, _dp]
+        L.orc_sort_merge.restype = C.c_int
+        L.orc_sort_merge.argtypes = [C.c_int, _ip, _ip, _ip, _ip, _dp, _ip, _ip, _ip, _ip, _dp]
+        _lib = L
+    return _lib
+
+
+def _d(a):
+    return a.ctypes.data_as(_dp)
+
+
+def _i(a):
+    return a.ctypes.data_as(_ip)
+
+
+def f64(a):
+    """Fortran-ordered float64 copy/view (the oracle uses column-major)."""
+    return np.asfortranarray(a, dtype=np.float64)
+
+
+def i32(a):
+    return np.asfortranarray(a, dtype=np.int32)
+
+
+def gauleg(n: int, x1: float = 0.0, x2: float = 1.0):
+    x = np.zeros(n)
+    w = np.zeros(n)
+    lib().orc_gauleg(x1, x2, _d(x), _d(w), n)
+    return x, w
+
+
+def mkgrid_01(ks: int, ml: int, hs: float, he: float, hmax: float, rmax: float):
+    """Knots of the semi-exponential grid (mkgrid_01); returns (ns, t)."""
+    buf = np.zeros(100000)
+    ns = lib().orc_mkgrid_01(ks, ml, hs, 0.0, he, hmax, rmax, _d(buf), buf.size)
+    if ns < 0:
+        raise ValueError("grid too large")
+    return ns, buf[: ns + ks].copy()
+
+
+class Grid:
+    """B-spline grid (alloc_DBS_gauss + Def_pbsp/qbsp + Def_pq_arrays)."""
+
+    def __init__(self, t, ks: int = 9, ksp: int = 8, ksq: int = 9):
+        t = f64(t)
+        self.ks = ks
+        self.ns = t.size - ks
+        self._t = t
+        self._p = lib().orc_grid_new(self.ns, ks, ksp, ksq, _d(t))
+        g = self._p.contents
+        self.ksp, self.ksq, self.nv, self.nsp, self.nsq, self.ms = g.ksp, g.ksq, g.nv, g.nsp, g.nsq, g.ms
+
+    def __del__(self):
+        try:
+            if getattr(self, "_p", None) is not None:
+                lib().orc_grid_free(self._p)
+                self._p = None
+        except Exception:
+            pass
+
+    def array(self, name: str) -> np.ndarray:
+        """Copy of a grid array in Fortran order with its reference shape."""
+        g = self._p.contents
+        ns, ks, nv, ms = self.ns, self.ks, self.nv, self.ms
+        shapes = {
+            "t": (ns + ks,), "tp": (self.nsp + self.ksp,), "tq": (self.nsq + self.ksq,),
+            "gx": (ks,), "gw": (ks,), "gr": (nv, ks), "grw": (nv, ks), "grm": (nv, ks),
+            "pbsp": (nv + 1, ks, self.ksp), "pbsd": (nv + 1, ks, self.ksp),
+            "qbsp": (nv + 1, ks, self.ksq), "qbsd": (nv + 1, ks, self.ksq),
+            "fpbs": (ns, ns), "fqbs": (ns, ns), "fpqbs": (ns, ns), "fqpbs": (ns, ns),
+            "fpqbsd": (ns, ns), "fqpbsd": (ns, ns), "fppqq": (ms, ms),
+        }
+        shp = shapes[name]
+        n = int(np.prod(shp))
+        flat = np.ctypeslib.as_array(getattr(g, name), shape=(n,)).copy()
+        return flat.reshape(shp, order="F")
+
+    # ---- level 1
+    def moments(self, which: int, k: int) -> np.ndarray:
+        kk = self.ks * self.ks
+        out = np.zeros(kk * self.nv)
+        lib().orc_moments(self._p, which, k, _d(out))
+        return out.reshape((kk, self.nv), order="F")
+
+    def triang(self, typ: int, k: int) -> np.ndarray:
+        kk = self.ks * self.ks
+        out = np.zeros(kk * kk * self.nv)
+        lib().orc_triang(self._p, typ, k, _d(out))
+        return out.reshape((kk, kk, self.nv), order="F")
+
+    def mrk(self, typ: int, k: int) -> np.ndarray:
+        out = np.zeros(self.ns * self.ns * self.ks * self.ks)
+        lib().orc_mrk(self._p, typ, k, _d(out))
+        return out.reshape((self.ns, self.ns, self.ks, self.ks), order="F")
+
+    def msk(self, typ: int, k: int) -> np.ndarray:
+        kb = 2 * self.ks - 1
+        out = np.zeros(self.ns * self.ns * kb * kb)
+        lib().orc_msk(self._p, typ, k, _d(out))
+        return out.reshape((self.ns, self.ns, kb, kb), order="F")
+
+    def quadr(self, fi, fj, m: int) -> float:
+        return lib().orc_quadr(self._p, _d(f64(fi)), _d(f64(fj)), m)
+
+    def rk(self, f1, f2, f3, f4, k: int) -> float:
+        return lib().orc_rk(self._p, _d(f64(f1)), _d(f64(f2)), _d(f64(f3)), _d(f64(f4)), k)
+
+    def v_ch(self, pq_b) -> np.ndarray:
+        v = np.zeros(self.ms)
+        lib().orc_v_ch(self._p, _d(f64(pq_b)), _d(v))
+        return v
+
+
+def density(ns, ks, p1, p2, typ: str) -> np.ndarray:
+    ncol = {"s": ks, "u": ks, "l": ks, "n": 2 * ks - 1}.get(typ, ns)
+    d = np.zeros(ns * max(ncol, ns))
+    lib().orc_density(ns, ks, _d(d), _d(f64(p1)), _d(f64(p2)), typ.encode())
+    return d.reshape((ns, max(ncol, ns)), order="F")[:, :ncol].copy(order="F")
+
+
+def convol(ns, ks, rkb, d, icase: int, sym_i: str, sym_j: str) -> np.ndarray:
+    rkb = np.asfortranarray(rkb, dtype=np.float64)
+    kb = rkb.shape[2]
+    dd = np.zeros((ns, ns), order="F")
+    dd[:, : d.shape[1]] = d
+    a = np.zeros((ns, ns), order="F")
+    lib().orc_convol(ns, ks, kb, rkb.ctypes.data_as(_dp), a.ctypes.data_as(_dp),
+                     dd.ctypes.data_as(_dp), icase, sym_i.encode(), sym_j.encode())
+    return a
+
+
+def sort_merge(k1, k2, k3, k4, c):
+    """Add_cdata list semantics: sorted unique keys with summed coefficients."""
+    k1, k2, k3, k4, c = i32(k1), i32(k2), i32(k3), i32(k4), f64(c)
+    n = k1.size
+    o = [np.zeros(max(n, 1), np.int32) for _ in range(4)]
+    oc = np.zeros(max(n, 1))
+    u = lib().orc_sort_merge(n, _i(k1), _i(k2), _i(k3), _i(k4), _d(c), _i(o[0]), _i(o[1]),
+                             _i(o[2]), _i(o[3]), _d(oc))
+    return o[0][:u].copy(), o[1][:u].copy(), o[2][:u].copy(), o[3][:u].copy(), oc[:u].copy()
+
+
+class Matrix:
+    """hch/acf state plus Gen_matrix dispatch (DBSR_MAT3)."""
+
+    def __init__(self, grid: Grid, pq, ipbs, nch: int, icc, mk: int):
+        self.grid = grid
+        self.pq = np.asfortranarray(pq, dtype=np.float64)  # (ns,2,nbf)
+        self.ipbs = i32(ipbs)
+        self.nch = nch
+        self.icc = np.asfortranarray(icc, dtype=np.int32)
+        self.iicc = int(self.icc.max())
+        ms = grid.ms
+        self.hch = np.zeros((ms, ms, self.iicc), order="F")
+        self.mk = mk
+        self.acf = np.zeros((self.iicc, mk + 1), order="F")
+        self._m = lib().orc_mat_new(
+            grid._p, self.pq.shape[2], self.pq.ctypes.data_as(_dp), _i(self.ipbs), nch,
+            self.icc.ctypes.data_as(_ip), self.iicc, self.hch.ctypes.data_as(_dp), mk,
+            self.acf.ctypes.data_as(_dp))
+
+    def __del__(self):
+        try:
+            if getattr(self, "_m", None):
+                lib().orc_mat_free(self._m)
+                self._m = None
+        except Exception:
+            pass
+
+    def gen_matrix(self, icase, itype, kpol, k1, k2, k3, k4, cdata, ipt=None):
+        k1, k2, k3, k4, cdata = i32(k1), i32(k2), i32(k3), i32(k4), f64(cdata)
+        n = k1.size
+        ipt = i32(np.arange(1, n + 1) if ipt is None else ipt)
+        rc = lib().orc_gen_matrix(self._m, icase, itype, kpol, n, _i(ipt), _i(k1), _i(k2),
+                                  _i(k3), _i(k4), _d(cdata))
+        if rc != 0:
+            raise RuntimeError(f"orc_gen_matrix failed: {rc}")
