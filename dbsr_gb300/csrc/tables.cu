@@ -545,35 +545,53 @@ int get_stable(dbsrg_ctx *c, int type, int k, const double **out) {
 // <a|r^k|b> split by component for all orbital pairs: quadr
 // (dbsr_lib_dbs.f90:3940-3976), used for the asymptotic coefficients
 // (QUADR_PQ at R_data.f90:224, which selects the component by atype).
-// quad(a,b,comp) with a,b 0-based orbital indices.
-__global__ void k_quad(int nbf, int ns, int nv, int ks, int ksp, int ksq, int k,
-                       const double *pq, const double *gr, const double *grw,
-                       const double *pbsp, const double *qbsp, double *quad) {
+// First the banded matrix G(i,i+d) = sum over intervals and Gauss points of
+// r^k w B_i B_{i+d} (d = 0..kx-1) per component, then quad(a,b,comp) =
+// sum_{i,j} G(i,j) p_a(i) p_b(j) with one warp per (a,b,comp).
+__global__ void k_rk_gram(int ns, int nv, int ks, int kx, int k, const double *bs,
+                          const double *gr, const double *grw, double *G) {
   int q = blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= nbf * nbf * 2) return;
-  int a = q % nbf, b = (q / nbf) % nbf, comp = q / (nbf * nbf);
+  if (q >= ns * kx) return;
+  int i = q % ns + 1, d = q / ns, j = i + d;  // 1-based i, j = i + d
   const int nw = nv + 1;
-  const int kx = comp == 0 ? ksp : ksq;
-  const double *bs = comp == 0 ? pbsp : qbsp;
-  const double *Fi = pq + (size_t)ns * comp + (size_t)2 * ns * a;
-  const double *Fj = pq + (size_t)ns * comp + (size_t)2 * ns * b;
-  double acc = 0.0, gxl[DBSRG_MAXK];
-  for (int iv = 0; iv < nv; iv++) {
-    for (int m = 0; m < ks; m++)
-      gxl[m] = __dmul_rn(ipow_d(gr[IDX2(iv, m, nv)], k), grw[IDX2(iv, m, nv)]);
-    for (int ith = 0; ith < kx; ith++) {
-      double pi = Fi[iv + ith];
-      for (int jth = 0; jth < kx; jth++) {
-        double pj = Fj[iv + jth], s = 0.0;
-        for (int m = 0; m < ks; m++) {
-          double gwl = __dmul_rn(gxl[m], bs[IDX3(iv, m, ith, nw, ks)]);
-          s = __dadd_rn(s, __dmul_rn(bs[IDX3(iv, m, jth, nw, ks)], gwl));
-        }
-        acc = __dadd_rn(acc, __dmul_rn(__dmul_rn(s, pi), pj));
+  double acc = 0.0;
+  if (j <= ns) {
+    int lo = max(1, j - kx + 1), hi = min(nv, i);
+    for (int iv = lo; iv <= hi; iv++) {
+      int ith = i - iv, jth = j - iv;
+      double s = 0.0;
+      for (int m = 0; m < ks; m++) {
+        double wk = __dmul_rn(ipow_d(gr[IDX2(iv - 1, m, nv)], k), grw[IDX2(iv - 1, m, nv)]);
+        s = __dadd_rn(s, __dmul_rn(bs[IDX3(iv - 1, m, jth, nw, ks)],
+                                   __dmul_rn(wk, bs[IDX3(iv - 1, m, ith, nw, ks)])));
       }
+      acc = __dadd_rn(acc, s);
     }
   }
-  quad[q] = acc;
+  G[q] = acc;
+}
+
+__global__ void k_quad(int nbf, int ns, int ksp, int ksq, const double *pq, const double *GP,
+                       const double *GQ, double *quad) {
+  int warp = (blockIdx.x * blockDim.x + threadIdx.x) / 32, lane = threadIdx.x % 32;
+  if (warp >= nbf * nbf * 2) return;
+  int a = warp % nbf, b = (warp / nbf) % nbf, comp = warp / (nbf * nbf);
+  const int kx = comp == 0 ? ksp : ksq;
+  const double *G = comp == 0 ? GP : GQ;
+  const double *pa = pq + (size_t)ns * comp + (size_t)2 * ns * a;
+  const double *pb = pq + (size_t)ns * comp + (size_t)2 * ns * b;
+  double acc = 0.0;
+  for (int i = lane; i < ns; i += 32) {
+    double s = G[i] * pb[i];  // d = 0
+    for (int d = 1; d < kx && i + d < ns; d++) {
+      double g = G[(size_t)i + (size_t)ns * d];
+      s += g * pb[i + d];
+      acc += g * pb[i] * pa[i + d];
+    }
+    acc += pa[i] * s;
+  }
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if (lane == 0) quad[warp] = acc;
 }
 
 int get_quad(dbsrg_ctx *c, int k, const double **out) {
@@ -585,11 +603,16 @@ int get_quad(dbsrg_ctx *c, int k, const double **out) {
   const DeviceGrid &g = c->g;
   double *q = nullptr;
   size_t n = (size_t)c->nbf * c->nbf * 2;
-  if (cudaMalloc((void **)&q, n * sizeof(double)) != cudaSuccess)
+  size_t gp = (size_t)g.ns * g.ksp, gq = (size_t)g.ns * g.ksq;
+  if (cudaMalloc((void **)&q, (n + gp + gq) * sizeof(double)) != cudaSuccess)
     return set_err(c, DBSRG_ENOMEM, "quad allocation failed");
-  DBSRG_RUN(c, "k_quad", k_quad<<<(unsigned)((n + 127) / 128), 128, 0, c->stream>>>(c->nbf, g.ns, g.nv, g.ks, g.ksp,
-                                                             g.ksq, k, c->pq, g.gr, g.grw,
-                                                             g.pbsp, g.qbsp, q));
+  double *GP = q + n, *GQ = GP + gp;
+  DBSRG_RUN(c, "k_rk_gram", k_rk_gram<<<(unsigned)((gp + 127) / 128), 128, 0, c->stream>>>(
+                                g.ns, g.nv, g.ks, g.ksp, k, g.pbsp, g.gr, g.grw, GP));
+  DBSRG_RUN(c, "k_rk_gram", k_rk_gram<<<(unsigned)((gq + 127) / 128), 128, 0, c->stream>>>(
+                                g.ns, g.nv, g.ks, g.ksq, k, g.qbsp, g.gr, g.grw, GQ));
+  DBSRG_RUN(c, "k_quad", k_quad<<<(unsigned)((n * 32 + 255) / 256), 256, 0, c->stream>>>(
+                             c->nbf, g.ns, g.ksp, g.ksq, c->pq, GP, GQ, q));
   c->quad[k] = q;
   *out = q;
   return DBSRG_OK;

@@ -150,6 +150,7 @@ int dbsrg_sync(dbsrg_ctx *ctx);
 int dbsrg_timing(dbsrg_ctx *ctx, int enable);
 int dbsrg_timing_report(dbsrg_ctx *ctx, char *buf, size_t len);
 
+
 #ifdef __cplusplus
 }
 #endif
