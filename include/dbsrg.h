@@ -150,6 +150,28 @@ int dbsrg_sync(dbsrg_ctx *ctx);
 int dbsrg_timing(dbsrg_ctx *ctx, int enable);
 int dbsrg_timing_report(dbsrg_ctx *ctx, char *buf, size_t len);
 
+/* Allocation-free exchange contraction of one channel-pair segment.  This
+ * entry point has no counterpart in the reference; it exists for callers
+ * that cannot call cudaMalloc: code recorded into a CUDA graph (allocation
+ * is not allowed during stream capture) and programs that must fix their
+ * device memory when the library is loaded.  It needs no context.
+ *
+ * For the n list entries (k2,k3,cdata) of one segment it forms the 'x'
+ * density xx = sum_e cdata(e)*pq(:,jp1,k2(e)) pq(:,jp2,k3(e))^T and writes
+ * out(ns,ns) = convol(xx, case 3, 's','s') with the R^k table rkb
+ * (ns,ns,ks,ks) -- the block R_data adds for itype 4 (R_data.f90:250-262).
+ * All pointers are device pointers owned by the caller; stream may be NULL.
+ * The density lives in a fixed static device array: ns is limited to 512
+ * (larger ns returns DBSRG_ERANGE, as do orbital indices outside 1..nbf).
+ * The array is shared by all calls on a device: calls that overlap on the
+ * GPU race and must be ordered by the caller.  The first call on a device
+ * sets up the array's address (cudaGetSymbolAddress) and must come before
+ * any stream capture.  The call waits for its own work to finish. */
+int dbsrg_exchange_segment_noalloc(int ns, int ks, const double *rkb,
+                                   const double *pq, int nbf, int jp1,
+                                   int jp2, int n, const int *k2,
+                                   const int *k3, const double *cdata,
+                                   double *out, void *stream);
 
 #ifdef __cplusplus
 }

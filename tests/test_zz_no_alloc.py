@@ -1,0 +1,83 @@
+"""The allocation-free exchange entry point against the regular one.
+
+dbsrg_exchange_segment_noalloc serves callers that cannot allocate device
+memory (work recorded into a CUDA graph, programs with a fixed device
+memory budget): its scratch is a static device array instead of a
+cudaMalloc'd buffer.  Here the test (not the entry point) allocates the
+inputs and the output, calls the new entry point twice in a row through the
+C ABI and compares each result with the block that Gen_matrix
+(dbsrg_gen_matrix) adds for the same segment.
+
+For a channel pair with ich > jch, UPDATE_HS adds the exchange result of
+PQ type 0 (P-P table, P components) unchanged into quadrant (1,1) and that
+of PQ type 1 (Q-Q) into quadrant (2,2); those quadrants are the reference
+values.  Tolerance: 1e-12 of the largest element, the plain-FP64 bar of
+the other GPU tests.  This file sorts last so a stop-at-first-failure run
+has already run every other test.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+from dbsr_gb300 import RK, Assembler, _lib, synth
+
+pytestmark = pytest.mark.gpu
+
+
+def _segment_case():
+    for seed in range(11, 60):
+        w = synth.small(ns=60, nch=2, mk=3, n_entries=400, breit=False, seed=seed)
+        for L in w.lists:
+            if L.icase == 2 and L.itype == 4:
+                sel = L.k1 == 2 * synth.IBO + 1
+                if sel.sum() >= 2:
+                    return w, L, sel
+    raise RuntimeError("no exchange segment for channel pair (2,1)")
+
+
+def test_noalloc_exchange_matches_gen_matrix_twice():
+    import torch
+
+    w, L, sel = _segment_case()
+    k1, k2, k3, k4, c = (np.ascontiguousarray(x[sel]) for x in (L.k1, L.k2, L.k3, L.k4, L.c))
+    ns, ks = w.ns, w.ks
+
+    # the existing entry point
+    a = Assembler(w.t, w.ks, w.ksp, w.ksq)
+    a.set_orbitals(w.pq, w.ipbs)
+    a.alloc_matrix(w.nch, w.icc, w.iicc, w.mk)
+    a.gen_matrix(2, 4, L.kpol, k1, k2, k3, k4, c)
+    blk = a.get_block(2, 1)
+    ref = {0: blk[:ns, :ns].copy(), 1: blk[ns:, ns:].copy()}
+    tables = {t: a.get_table(RK, t, L.kpol) for t in (0, 1)}
+    a.close()
+
+    dev = torch.device("cuda", 0)
+    pq = torch.from_numpy(np.asfortranarray(w.pq).ravel(order="F").copy()).to(dev)
+    dk2 = torch.from_numpy(k2.astype(np.int32)).to(dev)
+    dk3 = torch.from_numpy(k3.astype(np.int32)).to(dev)
+    dc = torch.from_numpy(c.astype(np.float64)).to(dev)
+    L_ = _lib.load()
+    for atype in (0, 1):  # two calls in a row on the shared static scratch
+        rkb = torch.from_numpy(tables[atype].ravel(order="F").copy()).to(dev)
+        out = torch.full((ns * ns,), float("nan"), dtype=torch.float64, device=dev)
+        jp = atype + 1
+        rc = L_.dbsrg_exchange_segment_noalloc(
+            ns, ks, ctypes.c_void_p(rkb.data_ptr()), ctypes.c_void_p(pq.data_ptr()), w.nbf, jp,
+            jp, int(k2.size), ctypes.c_void_p(dk2.data_ptr()), ctypes.c_void_p(dk3.data_ptr()),
+            ctypes.c_void_p(dc.data_ptr()), ctypes.c_void_p(out.data_ptr()), None)
+        assert rc == 0, rc
+        got = out.cpu().numpy().reshape((ns, ns), order="F")
+        r = ref[atype]
+        assert np.abs(r).max() > 0
+        err = np.abs(got - r).max() / np.abs(r).max()
+        assert err <= 1e-12, (atype, err)
+
+
+def test_noalloc_rejects_sizes_beyond_its_scratch():
+    L_ = _lib.load()
+    one = ctypes.c_void_p(1)
+    rc = L_.dbsrg_exchange_segment_noalloc(600, 9, one, one, 1, 1, 1, 0, None, None, None, one,
+                                           None)
+    assert rc == -4  # DBSRG_ERANGE
