@@ -46,7 +46,7 @@ def parse():
     p.add_argument("--steps", type=int, default=3)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--precision", default="plain", choices=["plain", "split"])
+    p.add_argument("--precision", default="plain", choices=["plain", "split", "factor"])
     p.add_argument("--scale", type=float, default=1.0, help="fraction of the 2e6 entries")
     p.add_argument("--nch", type=int, default=120)
     p.add_argument("--no-e2e", action="store_true")
@@ -299,12 +299,12 @@ def main():
         dist.init_process_group("nccl", device_id=dev)
         pg = dist
 
-    from dbsr_gb300 import PLAIN_FP64, SPLIT_BF16, Assembler
+    from dbsr_gb300 import FACTOR_FP64, PLAIN_FP64, SPLIT_BF16, Assembler
 
     a = Assembler(w.t, w.ks, w.ksp, w.ksq, device=local)
     a.set_orbitals(w.pq, w.ipbs)
     a.alloc_matrix(w.nch, w.icc, w.iicc, w.mk)
-    a.set_precision(SPLIT_BF16 if args.precision == "split" else PLAIN_FP64)
+    a.set_precision({"plain": PLAIN_FP64, "split": SPLIT_BF16, "factor": FACTOR_FP64}[args.precision])
     # device-resident lists
     dl = []
     for L in w.lists:

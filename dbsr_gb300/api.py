@@ -24,8 +24,9 @@ import numpy as np
 from . import _lib
 from ._lib import check, load
 
-PLAIN_FP64 = 0
-SPLIT_BF16 = 1
+PLAIN_FP64 = 0   # the reference's loop structure over assembled tables
+SPLIT_BF16 = 1   # cell-factored contraction, far field on the tensor cores
+FACTOR_FP64 = 2  # cell-factored contraction, all FP64
 RK = 0
 SK = 1
 

@@ -27,13 +27,6 @@ namespace {
 
 constexpr int kSegChunk = 256;  // segments per contraction/scatter pass
 
-struct SegInfo {
-  int start, end;  // entry range [start,end)
-  int ich, jch;    // channel pair decoded from K1
-  int blk;         // 1-based block from icc, 0 if invalid
-  int partner;     // other segment of this list mapping to the same block, or -1
-  int owner;       // 1 if this segment applies the block's contributions
-};
 
 // ---------------------------------------------------------------------------
 // list gather into IPT order
@@ -672,6 +665,8 @@ int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const 
   int na, icv, tabfam;
   char sym_d;
   const double *tabs[4] = {nullptr, nullptr, nullptr, nullptr};
+  int ttype[4] = {0, 1, 2, 3};  // table type of each atype (R: the atype itself)
+  const bool factored = c->precision != DBSRG_PLAIN_FP64;
   if (icase == 2) {
     if (itype != 3 && itype != 4)
       return set_err(c, DBSRG_EINVAL, "R_data: only itypes 3 and 4 are supported");
@@ -724,6 +719,7 @@ int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const 
     dsp.jp1[0] = jp1; dsp.jp2[0] = jp2;
     ssp.ii[0] = ip1; ssp.jj[0] = ip2;
     if ((rc = get_stable(c, atype, kpol, &tabs[0]))) return rc;
+    ttype[0] = atype;
   } else {
     return set_err(c, DBSRG_EINVAL, "unsupported icase");
   }
@@ -736,6 +732,14 @@ int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const 
   // ---- chunks of owner segments, each with its partner (a channel pair
   // listed in both orders maps to one block; both lists contribute to that
   // block in list order within every atype, so they stay in one chunk)
+  if (factored && icv >= 3) {
+    if (c->nbound < 1) return set_err(c, DBSRG_ESTATE, "no bound orbitals (ipbs = 0)");
+    if ((rc = check_bound_orbitals(c, n, lk2, lk3, dscal + 1))) return rc;
+    int h = 0;
+    DBSRG_TRY(c, cudaMemcpyAsync(&h, dscal + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+    DBSRG_TRY(c, cudaStreamSynchronize(st));
+    if (h) return set_err(c, DBSRG_EINVAL, "factored exchange: K2/K3 must be bound orbitals");
+  }
   std::vector<SegInfo> hinfo(nseg);
   DBSRG_TRY(c, cudaMemcpyAsync(hinfo.data(), info, sizeof(SegInfo) * nseg,
                                cudaMemcpyDeviceToHost, st));
@@ -757,14 +761,44 @@ int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const 
     std::copy(own.begin(), own.end(), h.begin() + nm);
     int rc2;
     if ((rc2 = copy_in(c, members, h.data(), sizeof(int) * h.size()))) return rc2;
-    size_t need2 = 2 * sizeof(double) * per * na * nm;
+    // the factored exchange forms its own band-limited densities: no X
+    const bool no_x = factored && icv >= 3;
+    size_t need2 = (no_x ? 1 : 2) * sizeof(double) * per * na * nm;
     if ((rc2 = ensure_scratch(c, need2))) return rc2;
     double *X = (double *)c->scratch;
-    double *Y = X + per * na * nm;
-    dim3 gd((unsigned)((per + 255) / 256), (unsigned)nm, (unsigned)na);
-    DBSRG_RUN(c, "k_density_acc", k_density_acc<<<gd, 256, 0, st>>>(ns, ks, sym_d, ncol, na, dsp, nm, members, info, lk2,
-                                      lk3, lcd, c->pq, X));
-    for (int a = 0; a < na; a++) {
+    double *Y = no_x ? X : X + per * na * nm;
+    if (!no_x) {
+      dim3 gd((unsigned)((per + 255) / 256), (unsigned)nm, (unsigned)na);
+      DBSRG_RUN(c, "k_density_acc",
+                k_density_acc<<<gd, 256, 0, st>>>(ns, ks, sym_d, ncol, na, dsp, nm, members, info,
+                                                  lk2, lk3, lcd, c->pq, X));
+    }
+    if (factored) {
+      FactorJob job{};
+      job.family = tabfam;
+      job.kpol = kpol;
+      job.icv = icv;
+      job.sym = sym_d;
+      job.na = na;
+      for (int a = 0; a < na; a++) {
+        job.types[a] = ttype[a];
+        job.jp1[a] = dsp.jp1[a];
+        job.jp2[a] = dsp.jp2[a];
+        job.tabs[a] = tabs[a];
+      }
+      job.nm = nm;
+      job.members = members;
+      job.info = info;
+      job.k2 = lk2;
+      job.k3 = lk3;
+      job.cd = lcd;
+      job.X = no_x ? nullptr : X;
+      job.Y = Y;
+      job.per = per;
+      job.split = c->precision == DBSRG_SPLIT_BF16;
+      if ((rc2 = factored_contract(c, job))) return rc2;
+    }
+    for (int a = 0; a < na && !factored; a++) {
       const double *Xa = X + (size_t)a * nm * per;
       double *Ya = Y + (size_t)a * nm * per;
       if (icv <= 2) {

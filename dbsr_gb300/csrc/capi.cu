@@ -114,6 +114,15 @@ static void timing_clear(dbsrg_ctx *c) {
   c->tev.clear();
 }
 
+static void free_farfield(dbsrg_ctx *c) {
+  for (auto &f : c->rfar)
+    if (f.U) cudaFree(f.U);
+  for (auto &f : c->sfar)
+    if (f.U) cudaFree(f.U);
+  c->rfar.clear();
+  c->sfar.clear();
+}
+
 static void free_tables(dbsrg_ctx *c) {
   for (double *p : c->rtab)
     if (p) cudaFree(p);
@@ -121,9 +130,16 @@ static void free_tables(dbsrg_ctx *c) {
     if (p) cudaFree(p);
   for (double *p : c->quad)
     if (p) cudaFree(p);
+  for (auto &cd : c->rcell)
+    if (cd.lo1) cudaFree(cd.lo1);
+  for (auto &cd : c->scell)
+    if (cd.lo1) cudaFree(cd.lo1);
+  free_farfield(c);
   c->rtab.clear();
   c->stab.clear();
   c->quad.clear();
+  c->rcell.clear();
+  c->scell.clear();
 }
 
 extern "C" {
@@ -186,6 +202,9 @@ int dbsrg_destroy(dbsrg_ctx *c) {
   if (c->scratch) cudaFree(c->scratch);
   if (c->scratch2) cudaFree(c->scratch2);
   if (c->tscratch) cudaFree(c->tscratch);
+  if (c->fscratch) cudaFree(c->fscratch);
+  if (c->bmap) cudaFree(c->bmap);
+  if (c->b2o) cudaFree(c->b2o);
   if (c->pinned) cudaFreeHost(c->pinned);
   timing_clear(c);
   for (cudaEvent_t e : c->evpool) cudaEventDestroy(e);
@@ -278,6 +297,24 @@ int dbsrg_set_orbitals(dbsrg_ctx *c, int nbf, const double *pq, const int *ipbs)
   }
   rc = copy_in(c, c->ipbs, c->h_ipbs.data(), nbf * sizeof(int));
   if (rc) return rc;
+  // dense numbering of the bound orbitals (ipbs = 0) for the factored path
+  free_farfield(c);
+  if (c->bmap) cudaFree(c->bmap);
+  if (c->b2o) cudaFree(c->b2o);
+  c->bmap = nullptr;
+  c->b2o = nullptr;
+  c->h_bmap.assign(nbf, -1);
+  std::vector<int> b2o;
+  for (int o = 0; o < nbf; o++)
+    if (c->h_ipbs[o] == 0) {
+      c->h_bmap[o] = (int)b2o.size();
+      b2o.push_back(o + 1);
+    }
+  c->nbound = (int)b2o.size();
+  DBSRG_TRY(c, cudaMalloc((void **)&c->bmap, nbf * sizeof(int)));
+  DBSRG_TRY(c, cudaMalloc((void **)&c->b2o, (b2o.size() + 1) * sizeof(int)));
+  if ((rc = copy_in(c, c->bmap, c->h_bmap.data(), nbf * sizeof(int)))) return rc;
+  if (!b2o.empty() && (rc = copy_in(c, c->b2o, b2o.data(), b2o.size() * sizeof(int)))) return rc;
   c->nbf = nbf;
   DBSRG_TRY(c, cudaStreamSynchronize(c->stream));
   return DBSRG_OK;
@@ -324,7 +361,8 @@ int dbsrg_zero_matrix(dbsrg_ctx *c) {
 
 int dbsrg_set_precision(dbsrg_ctx *c, int p) {
   if (!c) return DBSRG_EINVAL;
-  if (p != DBSRG_PLAIN_FP64 && p != DBSRG_SPLIT_BF16) return set_err(c, DBSRG_EINVAL, "unknown precision");
+  if (p != DBSRG_PLAIN_FP64 && p != DBSRG_SPLIT_BF16 && p != DBSRG_FACTOR_FP64)
+    return set_err(c, DBSRG_EINVAL, "unknown precision");
   c->precision = p;
   return DBSRG_OK;
 }

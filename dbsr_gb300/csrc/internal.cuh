@@ -32,6 +32,26 @@ struct DeviceGrid {
   double *fpbs = nullptr, *fqbs = nullptr, *fppqq = nullptr;
 };
 
+// resident cell moments and diagonal-cell integrals of one table
+struct CellData {
+  double *lo1 = nullptr, *hi1 = nullptr, *lo2 = nullptr, *hi2 = nullptr, *rkd = nullptr;
+};
+
+// far-field orbital vectors of one exchange table and contraction case:
+// U, V (upper field) and Ul, Vl (lower field, R^k only), each (ns, nbound)
+struct FarField {
+  double *U = nullptr, *V = nullptr, *Ul = nullptr, *Vl = nullptr;
+};
+
+// one channel-pair segment of a coefficient list (a run of equal K1)
+struct SegInfo {
+  int start, end;  // entry range [start,end) in IPT order
+  int ich, jch;    // channel pair decoded from K1
+  int blk;         // 1-based block from icc, 0 if invalid
+  int partner;     // other segment of this list mapping to the same block, or -1
+  int owner;       // 1 if this segment applies the block's contributions
+};
+
 struct dbsrg_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -52,6 +72,14 @@ struct dbsrg_ctx {
   double *acf = nullptr;
   // table caches, indexed [k*4+type] (R) and [k*2+type] (S)
   std::vector<double *> rtab, stab;
+  std::vector<CellData> rcell, scell;
+  // far-field vectors, indexed [(k*4+type)*2+case34] (R) / [(k*2+type)*2+case34] (S)
+  std::vector<FarField> rfar, sfar;
+  // bound-orbital map: bmap[orb-1] = dense bound index or -1; nbound
+  int nbound = 0;
+  int *bmap = nullptr;  // (nbf)
+  int *b2o = nullptr;   // (nbound): 1-based orbital of each bound index
+  std::vector<int> h_bmap;
   // <a|r^k|b> per component for the asymptotic coefficients, [k]
   std::vector<double *> quad;
   // scratch arena (grown on demand, reused across calls)
@@ -61,6 +89,8 @@ struct dbsrg_ctx {
   size_t scratch2_bytes = 0;
   void *tscratch = nullptr;   // table construction (moments, diagonal cells)
   size_t tscratch_bytes = 0;
+  void *fscratch = nullptr;   // factored contraction (band densities, Z vectors)
+  size_t fscratch_bytes = 0;
   // pinned staging for host lists
   void *pinned = nullptr;
   size_t pinned_bytes = 0;
@@ -136,12 +166,38 @@ int compute_diag_cells(dbsrg_ctx *c, int type, int k, double *rkd_dev);
 int get_rtable(dbsrg_ctx *c, int type, int k, const double **out);
 int get_stable(dbsrg_ctx *c, int type, int k, const double **out);
 int get_quad(dbsrg_ctx *c, int k, const double **out);
+int get_celldata(dbsrg_ctx *c, int family, int type, int k, const CellData **out);
 
 // ---- assemble.cu ----------------------------------------------------------
 int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n,
                      const int *ipt, const int *k1, const int *k2,
                      const int *k3, const int *k4, const double *cdata);
 int update_hx(dbsrg_ctx *c, int ich, int jch, const double *d, double cc);
+
+// ---- factor.cu ------------------------------------------------------------
+int ensure_fscratch(dbsrg_ctx *c, size_t bytes);
+// One chunk of segments of one list through the factored contraction.
+struct FactorJob {
+  int family;        // 0 R^k, 1 S^k
+  int kpol;
+  int icv;           // convol case 1..4
+  char sym;          // storage of densities/results: 's', 'n', 'x'
+  int na;            // PQ types (atypes) processed, in order
+  int types[4];      // table type of each atype
+  int jp1[4], jp2[4];
+  const double *tabs[4];
+  int nm;            // member segments of the chunk
+  const int *members;
+  const SegInfo *info;
+  const int *k2, *k3;
+  const double *cd;
+  const double *X;   // direct cases: accumulated densities [a][slot][per]
+  double *Y;         // results [a][slot][per]
+  size_t per;        // ns * ncol
+  bool split;        // far field on the tensor cores (split BF16)
+};
+int factored_contract(dbsrg_ctx *c, const FactorJob &job);
+int check_bound_orbitals(dbsrg_ctx *c, int n, const int *k2, const int *k3, int *derr);
 
 // ---- device helpers ---------------------------------------------------------
 // Values of the kx B-splines that are nonzero on the interval starting at

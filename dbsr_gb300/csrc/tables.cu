@@ -474,6 +474,52 @@ static int ensure_slot(dbsrg_ctx *c, std::vector<double *> &v, size_t idx) {
   return 0;
 }
 
+// Cell moments and diagonal-cell integrals of one table (family, type, k),
+// kept resident: the table fill and the factored contraction both read
+// them.  R: lo1/hi1 = moments of the electron-1 basis at r^k / r^-(k+1),
+// lo2/hi2 the same for electron 2 (mrk_*: rkd1..rkd4).  S: lo1 =
+// moments_pq(k) of electron 1, hi2 = moments_pq or moments_qp(-(k+1)) of
+// electron 2 (msk_*: rkd1, rkd2); hi1 = lo2 = null (no r1 > r2 cells).
+int get_celldata(dbsrg_ctx *c, int family, int type, int k, const CellData **out) {
+  const DeviceGrid &g = c->g;
+  std::vector<CellData> &v = family == 0 ? c->rcell : c->scell;
+  size_t idx = (size_t)k * (family == 0 ? 4 : 2) + type;
+  if (v.size() <= idx) v.resize(idx + 1);
+  if (v[idx].rkd) {
+    *out = &v[idx];
+    return DBSRG_OK;
+  }
+  const int nv = g.nv, kk = g.ks * g.ks;
+  size_t m = (size_t)kk * nv, d = (size_t)kk * kk * nv;
+  double *base = nullptr;
+  if (cudaMalloc((void **)&base, (4 * m + d) * sizeof(double)) != cudaSuccess)
+    return set_err(c, DBSRG_ENOMEM, "cell data allocation failed");
+  CellData cd;
+  cd.lo1 = base;
+  cd.hi1 = base + m;
+  cd.lo2 = base + 2 * m;
+  cd.hi2 = base + 3 * m;
+  cd.rkd = base + 4 * m;
+  int rc;
+  if (family == 0) {
+    int wa = (type == 0 || type == 2) ? 0 : 1, wb = (type == 0 || type == 3) ? 0 : 1;
+    if ((rc = compute_moments(c, wa, k, cd.lo1))) return rc;
+    if ((rc = compute_moments(c, wa, -(k + 1), cd.hi1))) return rc;
+    if ((rc = compute_moments(c, wb, k, cd.lo2))) return rc;
+    if ((rc = compute_moments(c, wb, -(k + 1), cd.hi2))) return rc;
+    if ((rc = compute_diag_cells(c, type, k, cd.rkd))) return rc;
+  } else {
+    if ((rc = compute_moments(c, 2, k, cd.lo1))) return rc;
+    if ((rc = compute_moments(c, type == 0 ? 2 : 3, -(k + 1), cd.hi2))) return rc;
+    if ((rc = compute_diag_cells(c, type == 0 ? 4 : 5, k, cd.rkd))) return rc;
+    cd.hi1 = nullptr;
+    cd.lo2 = nullptr;
+  }
+  v[idx] = cd;
+  *out = &v[idx];
+  return DBSRG_OK;
+}
+
 int get_rtable(dbsrg_ctx *c, int type, int k, const double **out) {
   const DeviceGrid &g = c->g;
   size_t idx = (size_t)k * 4 + type;
@@ -482,29 +528,19 @@ int get_rtable(dbsrg_ctx *c, int type, int k, const double **out) {
     *out = c->rtab[idx];
     return DBSRG_OK;
   }
-  const int ns = g.ns, ks = g.ks, nv = g.nv, kk = ks * ks;
+  const int ns = g.ns, ks = g.ks, nv = g.nv;
   size_t nt = (size_t)ns * ns * ks * ks;
+  const CellData *cd;
+  int rc = get_celldata(c, 0, type, k, &cd);
+  if (rc) return rc;
   double *tab = nullptr;
   cudaError_t e = cudaMalloc((void **)&tab, nt * sizeof(double));
   if (e != cudaSuccess) return set_err(c, DBSRG_ENOMEM, "R table allocation failed");
   int wa = (type == 0 || type == 2) ? 0 : 1, wb = (type == 0 || type == 3) ? 0 : 1;
   int ka = wa ? g.ksq : g.ksp, kb = wb ? g.ksq : g.ksp;
-  size_t mbytes = (size_t)kk * nv * sizeof(double);
-  size_t dbytes = (size_t)kk * kk * nv * sizeof(double);
-  int rc = ensure_tscratch(c, 4 * mbytes + dbytes);
-  if (rc) return rc;
-  double *lowA = (double *)c->tscratch;
-  double *highA = lowA + (size_t)kk * nv;
-  double *lowB = highA + (size_t)kk * nv;
-  double *highB = lowB + (size_t)kk * nv;
-  double *rkd = highB + (size_t)kk * nv;
-  if ((rc = compute_moments(c, wa, k, lowA))) return rc;
-  if ((rc = compute_moments(c, wa, -(k + 1), highA))) return rc;
-  if ((rc = compute_moments(c, wb, k, lowB))) return rc;
-  if ((rc = compute_moments(c, wb, -(k + 1), highB))) return rc;
-  if ((rc = compute_diag_cells(c, type, k, rkd))) return rc;
   unsigned nb = (unsigned)((nt + 255) / 256);
-  DBSRG_RUN(c, "k_fill_r", k_fill_r<<<nb, 256, 0, c->stream>>>(ns, ks, nv, ka, kb, lowA, highA, lowB, highB, rkd, tab));
+  DBSRG_RUN(c, "k_fill_r", k_fill_r<<<nb, 256, 0, c->stream>>>(ns, ks, nv, ka, kb, cd->lo1, cd->hi1,
+                                                               cd->lo2, cd->hi2, cd->rkd, tab));
   c->rtab[idx] = tab;
   *out = tab;
   return DBSRG_OK;
@@ -518,24 +554,18 @@ int get_stable(dbsrg_ctx *c, int type, int k, const double **out) {
     *out = c->stab[idx];
     return DBSRG_OK;
   }
-  const int ns = g.ns, ks = g.ks, nv = g.nv, kk = ks * ks, kb2 = 2 * ks - 1;
+  const int ns = g.ns, ks = g.ks, nv = g.nv, kb2 = 2 * ks - 1;
   size_t nt = (size_t)ns * ns * kb2 * kb2;
+  const CellData *cd;
+  int rc = get_celldata(c, 1, type, k, &cd);
+  if (rc) return rc;
   double *tab = nullptr;
   cudaError_t e = cudaMalloc((void **)&tab, nt * sizeof(double));
   if (e != cudaSuccess) return set_err(c, DBSRG_ENOMEM, "S table allocation failed");
-  size_t mbytes = (size_t)kk * nv * sizeof(double);
-  size_t dbytes = (size_t)kk * kk * nv * sizeof(double);
-  int rc = ensure_tscratch(c, 2 * mbytes + dbytes);
-  if (rc) return rc;
-  double *r1 = (double *)c->tscratch;
-  double *r2 = r1 + (size_t)kk * nv;
-  double *rkd = r2 + (size_t)kk * nv;
-  if ((rc = compute_moments(c, 2, k, r1))) return rc;
-  if ((rc = compute_moments(c, type == 0 ? 2 : 3, -(k + 1), r2))) return rc;
-  if ((rc = compute_diag_cells(c, type == 0 ? 4 : 5, k, rkd))) return rc;
   int kj1 = type == 0 ? g.ksp : g.ksq, kj2 = type == 0 ? g.ksq : g.ksp;
   unsigned nb = (unsigned)((nt + 255) / 256);
-  DBSRG_RUN(c, "k_fill_s", k_fill_s<<<nb, 256, 0, c->stream>>>(ns, ks, nv, g.ksp, g.ksq, kj1, kj2, r1, r2, rkd, tab));
+  DBSRG_RUN(c, "k_fill_s", k_fill_s<<<nb, 256, 0, c->stream>>>(ns, ks, nv, g.ksp, g.ksq, kj1, kj2,
+                                                               cd->lo1, cd->hi2, cd->rkd, tab));
   c->stab[idx] = tab;
   *out = tab;
   return DBSRG_OK;

@@ -51,8 +51,13 @@ enum dbsrg_status {
 
 /* precision / algorithm of the contraction */
 enum dbsrg_precision {
-  DBSRG_PLAIN_FP64 = 0, /* reference loop structure, FP64 throughout      */
-  DBSRG_SPLIT_BF16 = 1  /* split-precision tensor-core contraction        */
+  DBSRG_PLAIN_FP64 = 0,  /* the reference's loop structure over the
+                            assembled tables, FP64 throughout           */
+  DBSRG_SPLIT_BF16 = 1,  /* cell-factored contraction; far field as
+                            split-BF16 tensor-core products, FP32
+                            accumulation, FP64 recombination; band,
+                            diagonal cells and block sums in FP64       */
+  DBSRG_FACTOR_FP64 = 2  /* the same factored contraction, all FP64      */
 };
 
 /* table families for dbsrg_get_table */
