@@ -689,7 +689,13 @@ int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const 
       }
       dsp.jp1[a] = jp1; dsp.jp2[a] = jp2;
       ssp.ii[a] = ip1; ssp.jj[a] = ip2;
-      if ((rc = get_rtable(c, a, kpol, &tabs[a]))) return rc;
+      // the factored path reads only the band |j-i| <= 16 of exchange tables
+      // and no table at all for the direct contraction
+      if (!factored)
+        rc = get_rtable(c, a, kpol, &tabs[a]);
+      else if (itype == 4)
+        rc = get_band_table(c, 0, a, kpol, &tabs[a]);
+      if (rc) return rc;
     }
   } else if (icase == 3) {
     int atype = itype / 10, it = itype % 10;
@@ -718,7 +724,11 @@ int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const 
     sym_d = in <= 2 ? 'n' : 'x';
     dsp.jp1[0] = jp1; dsp.jp2[0] = jp2;
     ssp.ii[0] = ip1; ssp.jj[0] = ip2;
-    if ((rc = get_stable(c, atype, kpol, &tabs[0]))) return rc;
+    if (!factored)
+      rc = get_stable(c, atype, kpol, &tabs[0]);
+    else if (in >= 3)
+      rc = get_band_table(c, 1, atype, kpol, &tabs[0]);
+    if (rc) return rc;
     ttype[0] = atype;
   } else {
     return set_err(c, DBSRG_EINVAL, "unsupported icase");

@@ -77,6 +77,9 @@ int ensure_scratch2(dbsrg_ctx *c, size_t bytes) {
 int ensure_tscratch(dbsrg_ctx *c, size_t bytes) {
   return grow(c, &c->tscratch, &c->tscratch_bytes, bytes);
 }
+int ensure_tcscratch(dbsrg_ctx *c, size_t bytes) {
+  return grow(c, &c->tcscratch, &c->tcscratch_bytes, bytes);
+}
 bool sync_check_enabled() {
   static int v = -1;
   if (v < 0) {
@@ -130,6 +133,12 @@ static void free_tables(dbsrg_ctx *c) {
     if (p) cudaFree(p);
   for (double *p : c->quad)
     if (p) cudaFree(p);
+  for (double *p : c->rbtab)
+    if (p) cudaFree(p);
+  for (double *p : c->sbtab)
+    if (p) cudaFree(p);
+  c->rbtab.clear();
+  c->sbtab.clear();
   for (auto &cd : c->rcell)
     if (cd.lo1) cudaFree(cd.lo1);
   for (auto &cd : c->scell)
@@ -203,6 +212,7 @@ int dbsrg_destroy(dbsrg_ctx *c) {
   if (c->scratch2) cudaFree(c->scratch2);
   if (c->tscratch) cudaFree(c->tscratch);
   if (c->fscratch) cudaFree(c->fscratch);
+  if (c->tcscratch) cudaFree(c->tcscratch);
   if (c->bmap) cudaFree(c->bmap);
   if (c->b2o) cudaFree(c->b2o);
   if (c->pinned) cudaFreeHost(c->pinned);

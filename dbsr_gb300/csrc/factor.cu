@@ -216,10 +216,13 @@ __global__ void __launch_bounds__(256) k_band_exchange(int ns, int ks, int mode,
     return __ldg(&D[(size_t)(i - 1) + (size_t)ns * (j - i + XB_HALF)]);
   };
   double acc = 0.0;
+  // band table: rkb(i, j-i+BW+1, ip, jp), |j - i| <= BW (= 16) is all that
+  // the band outputs read
+  constexpr int BW = DBSRG_TABLE_BAND, NJ = 2 * DBSRG_TABLE_BAND + 1;
   if (mode == 0) {
     auto TB = [&](int i, int j, int ip, int jp) -> double {
-      return __ldg(&rkb[(size_t)(i - 1) + (size_t)ns * ((size_t)(j - 1) +
-                        (size_t)ns * ((size_t)(ip - 1) + (size_t)ks * (size_t)(jp - 1)))]);
+      return __ldg(&rkb[(size_t)(i - 1) + (size_t)ns * ((size_t)(j - i + BW) +
+                        (size_t)NJ * ((size_t)(ip - 1) + (size_t)ks * (size_t)(jp - 1)))]);
     };
     for (int jp = 1; jp <= ks; jp++)
       for (int ip = 1; ip <= ks; ip++) {
@@ -235,8 +238,8 @@ __global__ void __launch_bounds__(256) k_band_exchange(int ns, int ks, int mode,
   } else {
     const int kb = 2 * ks - 1;
     auto TB = [&](int i, int j, int ip, int jp) -> double {
-      return __ldg(&rkb[(size_t)(i - 1) + (size_t)ns * ((size_t)(j - 1) +
-                        (size_t)ns * ((size_t)(ip - 1) + (size_t)kb * (size_t)(jp - 1)))]);
+      return __ldg(&rkb[(size_t)(i - 1) + (size_t)ns * ((size_t)(j - i + BW) +
+                        (size_t)NJ * ((size_t)(ip - 1) + (size_t)kb * (size_t)(jp - 1)))]);
     };
     for (int jp = 1; jp <= kb; jp++)
       for (int ip = 1; ip <= kb; ip++) {
@@ -331,8 +334,11 @@ __global__ void __launch_bounds__(256) k_direct(int ns, int ks, int nv, int kk, 
     }
   }
   __syncthreads();
-  // phase 3: output band
+  // phase 3a: the separable (off-diagonal cell) terms into the output band,
+  // kept in shared memory
   PairSpec eo = icv == 1 ? e1 : e2;
+  double *out = sh + 2 * nv;               // ns * ncol
+  double *rho_w = out + (size_t)ns * ncol; // 81 values per warp
   for (int q = threadIdx.x; q < ns * ncol; q += blockDim.x) {
     int f = q % ns + 1, col = q / ns + 1;
     int s2 = sym == 's' ? f + col - 1 : f + col - ks;
@@ -340,29 +346,77 @@ __global__ void __launch_bounds__(256) k_direct(int ns, int ks, int nv, int kk, 
     if (s2 >= 1 && s2 <= ns) {
       int lo = max(max(1, f - eo.k1 + 1), s2 - eo.k2 + 1), hi = min(min(nv, f), s2);
       for (int cv = lo; cv <= hi; cv++) {
-        int h1 = f - cv + 1, h2 = s2 - cv + 1;
-        int po = pidx(eo, h1, h2);
-        size_t o = (size_t)po + (size_t)kk * (cv - 1);
+        size_t o = (size_t)pidx(eo, f - cv + 1, s2 - cv + 1) + (size_t)kk * (cv - 1);
         if (icv == 1) {
           acc = fma(lo1[o], s_a[cv - 1], acc);
           if (hi1) acc = fma(hi1[o], s_b[cv - 1], acc);
         } else {
           acc = fma(hi2[o], s_a[cv - 1], acc);
         }
-        // diagonal cell
-        for (int g1 = 1; g1 <= ed.k1; g1++)
-          for (int g2 = ed.sym ? g1 : 1; g2 <= ed.k2; g2++) {
-            double r = rho(cv + g1 - 1, cv + g2 - 1);
-            if (r == 0.0) continue;
-            int pd = pidx(ed, g1, g2);
-            size_t od = icv == 1 ? (size_t)po + (size_t)kk * ((size_t)pd + (size_t)kk * (cv - 1))
-                                 : (size_t)pd + (size_t)kk * ((size_t)po + (size_t)kk * (cv - 1));
-            acc = fma(rkd[od], r, acc);
-          }
       }
     }
-    Y[(size_t)slot * per + q] = acc;
+    out[q] = acc;
   }
+  __syncthreads();
+  // phase 3b: diagonal cells, one warp per cell.  Cell cv touches outputs
+  // with first index in [cv, cv+8], so cells 9 apart never share an output:
+  // nine phases of disjoint cells give every output one writer at a time.
+  const int lane = threadIdx.x % 32, warp = threadIdx.x / 32, nwarp = blockDim.x / 32;
+  const int npo = eo.sym ? eo.k1 * (eo.k1 + 1) / 2 : eo.k1 * eo.k2;
+  double *rw = rho_w + 81 * warp;
+  for (int ph = 0; ph < 9; ph++) {
+    for (int cv = ph + 1 + 9 * warp; cv <= nv; cv += 9 * nwarp) {
+      // stage the cell's density pairs, one pair per lane
+      const int npd = ed.sym ? ed.k1 * (ed.k1 + 1) / 2 : ed.k1 * ed.k2;
+      for (int pd = lane; pd < npd; pd += 32) {
+        int g1, g2;
+        if (ed.sym) {
+          int r = pd, row = 0;
+          while (r >= ed.k1 - row) {
+            r -= ed.k1 - row;
+            row++;
+          }
+          g1 = row + 1;
+          g2 = row + 1 + r;
+        } else {
+          g1 = pd / ed.k2 + 1;
+          g2 = pd % ed.k2 + 1;
+        }
+        rw[pd] = rho(cv + g1 - 1, cv + g2 - 1);
+      }
+      __syncwarp();
+      for (int po = lane; po < npo; po += 32) {
+        int h1, h2;
+        if (eo.sym) {
+          int r = po, row = 0;
+          while (r >= eo.k1 - row) {
+            r -= eo.k1 - row;
+            row++;
+          }
+          h1 = row + 1;
+          h2 = row + 1 + r;
+        } else {
+          h1 = po / eo.k2 + 1;
+          h2 = po % eo.k2 + 1;
+        }
+        int f = cv + h1 - 1, s2 = cv + h2 - 1;
+        if (f > ns || s2 > ns) continue;
+        double acc = 0.0;
+        if (icv == 1) {
+          const double *rk = rkd + (size_t)po + (size_t)kk * (size_t)kk * (cv - 1);
+          for (int pd = 0; pd < npd; pd++) acc = fma(rk[(size_t)kk * pd], rw[pd], acc);
+        } else {
+          const double *rk = rkd + (size_t)kk * ((size_t)po + (size_t)kk * (cv - 1));
+          for (int pd = 0; pd < npd; pd++) acc = fma(rk[pd], rw[pd], acc);
+        }
+        int q = sym == 's' ? (f - 1) + ns * (s2 - f) : (f - 1) + ns * (s2 - f + ks - 1);
+        out[q] += acc;
+      }
+      __syncwarp();
+    }
+    __syncthreads();
+  }
+  for (int q = threadIdx.x; q < ns * ncol; q += blockDim.x) Y[(size_t)slot * per + q] = out[q];
 }
 
 __global__ void k_check_bound(int n, const int *k2, const int *k3, const int *bmap, int *err) {
@@ -501,7 +555,9 @@ int factored_contract(dbsrg_ctx *c, const FactorJob &j) {
     TableBases tb = table_bases(g, j.family, j.types[a]);
     const double *Xa = j.X + (size_t)a * j.nm * j.per;
     double *Ya = j.Y + (size_t)a * j.nm * j.per;
-    size_t smem = 2 * (size_t)nv * sizeof(double);
+    const int ncol = j.sym == 's' ? ks : 2 * ks - 1;
+    size_t smem = (2 * (size_t)nv + (size_t)ns * ncol + 81 * 8) * sizeof(double);
+    if (smem > 200 * 1024) return set_err(c, DBSRG_EINVAL, "direct contraction: ns too large");
     if (smem > 48 * 1024)
       DBSRG_TRY(c, cudaFuncSetAttribute(k_direct, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)smem));
@@ -511,14 +567,5 @@ int factored_contract(dbsrg_ctx *c, const FactorJob &j) {
                                                 j.family == 0 ? cd->lo2 : nullptr, cd->hi2,
                                                 cd->rkd, Xa, Ya, j.per));
   }
-  return DBSRG_OK;
-}
-
-// placeholder until the tensor-core far field is built: FP64 path
-int farfield_tc(dbsrg_ctx *c, int ns, int nb, int nm, const double *U, const double *Ul,
-                const double *Z, const double *Zl, double *Y, size_t per) {
-  dim3 gf((unsigned)((ns + 31) / 32), (unsigned)((ns + 31) / 32), (unsigned)nm);
-  DBSRG_RUN(c, "k_far_field",
-            k_far_field<<<gf, 256, 0, c->stream>>>(ns, nb, U, Ul, Z, Zl, Y, per));
   return DBSRG_OK;
 }

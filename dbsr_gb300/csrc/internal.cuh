@@ -72,6 +72,8 @@ struct dbsrg_ctx {
   double *acf = nullptr;
   // table caches, indexed [k*4+type] (R) and [k*2+type] (S)
   std::vector<double *> rtab, stab;
+  // band-limited tables (|j-i| <= DBSRG_TABLE_BAND) for the factored path
+  std::vector<double *> rbtab, sbtab;
   std::vector<CellData> rcell, scell;
   // far-field vectors, indexed [(k*4+type)*2+case34] (R) / [(k*2+type)*2+case34] (S)
   std::vector<FarField> rfar, sfar;
@@ -91,6 +93,8 @@ struct dbsrg_ctx {
   size_t tscratch_bytes = 0;
   void *fscratch = nullptr;   // factored contraction (band densities, Z vectors)
   size_t fscratch_bytes = 0;
+  void *tcscratch = nullptr;  // tensor-core far field (digit slices, scales)
+  size_t tcscratch_bytes = 0;
   // pinned staging for host lists
   void *pinned = nullptr;
   size_t pinned_bytes = 0;
@@ -156,6 +160,7 @@ int copy_out(dbsrg_ctx *c, void *dst, const void *src, size_t n);
 int ensure_scratch(dbsrg_ctx *c, size_t bytes);
 int ensure_scratch2(dbsrg_ctx *c, size_t bytes);
 int ensure_tscratch(dbsrg_ctx *c, size_t bytes);
+int ensure_tcscratch(dbsrg_ctx *c, size_t bytes);
 int ensure_pinned(dbsrg_ctx *c, size_t bytes);
 
 // ---- tables.cu ------------------------------------------------------------
@@ -167,6 +172,9 @@ int get_rtable(dbsrg_ctx *c, int type, int k, const double **out);
 int get_stable(dbsrg_ctx *c, int type, int k, const double **out);
 int get_quad(dbsrg_ctx *c, int k, const double **out);
 int get_celldata(dbsrg_ctx *c, int family, int type, int k, const CellData **out);
+// (ns, 2*DBSRG_TABLE_BAND+1, kb, kb): rkb(i, j-i+DBSRG_TABLE_BAND+1, ip, jp)
+#define DBSRG_TABLE_BAND 16
+int get_band_table(dbsrg_ctx *c, int family, int type, int k, const double **out);
 
 // ---- assemble.cu ----------------------------------------------------------
 int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n,

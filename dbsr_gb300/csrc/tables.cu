@@ -391,21 +391,26 @@ __device__ __forceinline__ int tri_index(int h, int hp, int kx) {  // 1-based
   return (h - 1) * kx - ((h - 1) * (h - 2)) / 2 + (hp - h + 1);
 }
 
+// band > 0: only the elements with |j - i| <= band, stored as
+// rkb(i, j-i+band+1, ip, jp) of shape (ns, 2*band+1, ks, ks) -- all that the
+// band part of the factored exchange reads.
 __global__ void k_fill_r(int ns, int ks, int nv, int ka, int kb, const double *lowA,
                          const double *highA, const double *lowB, const double *highB,
-                         const double *rkd, double *rkb) {
+                         const double *rkd, double *rkb, int band) {
   size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  size_t total = (size_t)ns * ns * ks * ks;
+  const int nj = band > 0 ? 2 * band + 1 : ns;
+  size_t total = (size_t)ns * nj * ks * ks;
   if (q >= total) return;
   const int kk = ks * ks;
   int i = (int)(q % ns) + 1;
   size_t r = q / ns;
-  int j = (int)(r % ns) + 1;
-  r /= ns;
+  int j = (int)(r % nj) + 1;
+  if (band > 0) j = i + (j - 1) - band;
+  r /= nj;
   int ip = (int)(r % ks) + 1;
   int jp = (int)(r / ks) + 1;
   double acc = 0.0;
-  if (ip <= ka && jp <= kb) {
+  if (ip <= ka && jp <= kb && j >= 1 && j <= ns) {
     int ivlo = max(1, i - ka + ip), ivhi = min(nv, i);
     int jvlo = max(1, j - kb + jp), jvhi = min(nv, j);
     for (int jv = jvlo; jv <= jvhi; jv++) {
@@ -431,18 +436,25 @@ __global__ void k_fill_r(int ns, int ks, int nv, int ka, int kb, const double *l
 // S^k table fill: msk_ppqq / msk_pqqp, dbsr_lib_dbs.f90:3601-3662,
 // 3771-3833.  Only cells iv <= jv; band offsets ip = ihp-ih+ks.
 __global__ void k_fill_s(int ns, int ks, int nv, int ksp, int ksq, int kj1, int kj2,
-                         const double *r1, const double *r2, const double *rkd, double *rkb) {
+                         const double *r1, const double *r2, const double *rkd, double *rkb,
+                         int band) {
   const int kb2 = 2 * ks - 1, kk = ks * ks;
   size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  size_t total = (size_t)ns * ns * kb2 * kb2;
+  const int nj = band > 0 ? 2 * band + 1 : ns;
+  size_t total = (size_t)ns * nj * kb2 * kb2;
   if (q >= total) return;
   int i = (int)(q % ns) + 1;
   size_t r = q / ns;
-  int j = (int)(r % ns) + 1;
-  r /= ns;
+  int j = (int)(r % nj) + 1;
+  if (band > 0) j = i + (j - 1) - band;
+  r /= nj;
   int ip = (int)(r % kb2) + 1;
   int jp = (int)(r / kb2) + 1;
   double acc = 0.0;
+  if (j < 1 || j > ns) {
+    rkb[q] = 0.0;
+    return;
+  }
   // electron 1: ih in [1,ksp], ihp = ip+ih-ks in [1,ksq], iv = i-ih+1
   int ihlo = max(1, ks - ip + 1), ihhi = min(ksp, ks - ip + ksq);
   // electron 2: jh in [1,kj1], jhp = jp+jh-ks in [1,kj2], jv = j-jh+1
@@ -520,55 +532,52 @@ int get_celldata(dbsrg_ctx *c, int family, int type, int k, const CellData **out
   return DBSRG_OK;
 }
 
-int get_rtable(dbsrg_ctx *c, int type, int k, const double **out) {
+// full (band == 0) or band-limited table of (family, type, k), cached
+static int get_table_any(dbsrg_ctx *c, int family, int type, int k, int band,
+                         const double **out) {
   const DeviceGrid &g = c->g;
-  size_t idx = (size_t)k * 4 + type;
-  ensure_slot(c, c->rtab, idx);
-  if (c->rtab[idx]) {
-    *out = c->rtab[idx];
+  std::vector<double *> &v = family == 0 ? (band ? c->rbtab : c->rtab) : (band ? c->sbtab : c->stab);
+  size_t idx = (size_t)k * (family == 0 ? 4 : 2) + type;
+  ensure_slot(c, v, idx);
+  if (v[idx]) {
+    *out = v[idx];
     return DBSRG_OK;
   }
-  const int ns = g.ns, ks = g.ks, nv = g.nv;
-  size_t nt = (size_t)ns * ns * ks * ks;
+  const int ns = g.ns, ks = g.ks, nv = g.nv, kb = family == 0 ? ks : 2 * ks - 1;
+  const int nj = band ? 2 * band + 1 : ns;
+  size_t nt = (size_t)ns * nj * kb * kb;
   const CellData *cd;
-  int rc = get_celldata(c, 0, type, k, &cd);
+  int rc = get_celldata(c, family, type, k, &cd);
   if (rc) return rc;
   double *tab = nullptr;
-  cudaError_t e = cudaMalloc((void **)&tab, nt * sizeof(double));
-  if (e != cudaSuccess) return set_err(c, DBSRG_ENOMEM, "R table allocation failed");
-  int wa = (type == 0 || type == 2) ? 0 : 1, wb = (type == 0 || type == 3) ? 0 : 1;
-  int ka = wa ? g.ksq : g.ksp, kb = wb ? g.ksq : g.ksp;
+  if (cudaMalloc((void **)&tab, nt * sizeof(double)) != cudaSuccess)
+    return set_err(c, DBSRG_ENOMEM, "table allocation failed");
   unsigned nb = (unsigned)((nt + 255) / 256);
-  DBSRG_RUN(c, "k_fill_r", k_fill_r<<<nb, 256, 0, c->stream>>>(ns, ks, nv, ka, kb, cd->lo1, cd->hi1,
-                                                               cd->lo2, cd->hi2, cd->rkd, tab));
-  c->rtab[idx] = tab;
+  if (family == 0) {
+    int wa = (type == 0 || type == 2) ? 0 : 1, wb = (type == 0 || type == 3) ? 0 : 1;
+    int ka = wa ? g.ksq : g.ksp, kbb = wb ? g.ksq : g.ksp;
+    DBSRG_RUN(c, "k_fill_r",
+              k_fill_r<<<nb, 256, 0, c->stream>>>(ns, ks, nv, ka, kbb, cd->lo1, cd->hi1, cd->lo2,
+                                                  cd->hi2, cd->rkd, tab, band));
+  } else {
+    int kj1 = type == 0 ? g.ksp : g.ksq, kj2 = type == 0 ? g.ksq : g.ksp;
+    DBSRG_RUN(c, "k_fill_s",
+              k_fill_s<<<nb, 256, 0, c->stream>>>(ns, ks, nv, g.ksp, g.ksq, kj1, kj2, cd->lo1,
+                                                  cd->hi2, cd->rkd, tab, band));
+  }
+  v[idx] = tab;
   *out = tab;
   return DBSRG_OK;
 }
 
+int get_rtable(dbsrg_ctx *c, int type, int k, const double **out) {
+  return get_table_any(c, 0, type, k, 0, out);
+}
 int get_stable(dbsrg_ctx *c, int type, int k, const double **out) {
-  const DeviceGrid &g = c->g;
-  size_t idx = (size_t)k * 2 + type;
-  ensure_slot(c, c->stab, idx);
-  if (c->stab[idx]) {
-    *out = c->stab[idx];
-    return DBSRG_OK;
-  }
-  const int ns = g.ns, ks = g.ks, nv = g.nv, kb2 = 2 * ks - 1;
-  size_t nt = (size_t)ns * ns * kb2 * kb2;
-  const CellData *cd;
-  int rc = get_celldata(c, 1, type, k, &cd);
-  if (rc) return rc;
-  double *tab = nullptr;
-  cudaError_t e = cudaMalloc((void **)&tab, nt * sizeof(double));
-  if (e != cudaSuccess) return set_err(c, DBSRG_ENOMEM, "S table allocation failed");
-  int kj1 = type == 0 ? g.ksp : g.ksq, kj2 = type == 0 ? g.ksq : g.ksp;
-  unsigned nb = (unsigned)((nt + 255) / 256);
-  DBSRG_RUN(c, "k_fill_s", k_fill_s<<<nb, 256, 0, c->stream>>>(ns, ks, nv, g.ksp, g.ksq, kj1, kj2,
-                                                               cd->lo1, cd->hi2, cd->rkd, tab));
-  c->stab[idx] = tab;
-  *out = tab;
-  return DBSRG_OK;
+  return get_table_any(c, 1, type, k, 0, out);
+}
+int get_band_table(dbsrg_ctx *c, int family, int type, int k, const double **out) {
+  return get_table_any(c, family, type, k, DBSRG_TABLE_BAND, out);
 }
 
 // ----------------------------------------------------------------------------
