@@ -46,7 +46,11 @@ def parse():
     p.add_argument("--steps", type=int, default=3)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--precision", default="plain", choices=["plain", "split", "factor"])
+    p.add_argument("--precision", default="split", choices=["plain", "split", "factor"])
+    p.add_argument("--no-compare", action="store_true",
+                   help="skip the FP64 comparison runs (plain and factored FP64 assemblies)")
+    p.add_argument("--block-errors", default=None,
+                   help="write the per-block max/RMS relative errors to this CSV file")
     p.add_argument("--scale", type=float, default=1.0, help="fraction of the 2e6 entries")
     p.add_argument("--nch", type=int, default=120)
     p.add_argument("--no-e2e", action="store_true")
@@ -272,6 +276,65 @@ def reference_arm(args, w):
     }
 
 
+def block_errors(torch, hs, hp, nblk, ms, chunk=64):
+    """Per-block max and RMS relative errors of hs against hp, both
+    (ms, ms, nblk) column-major on the device: max|hs-hp| / max|hp| and
+    ||hs-hp||_2 / ||hp||_2 over each ms x ms block."""
+    emax, erms = [], []
+    hs3 = hs.view(nblk, ms * ms)
+    hp3 = hp.view(nblk, ms * ms)
+    for b0 in range(0, nblk, chunk):
+        s, p = hs3[b0:b0 + chunk], hp3[b0:b0 + chunk]
+        d = s - p
+        dm = d.abs().amax(dim=1)
+        pm = p.abs().amax(dim=1)
+        dr = d.square().sum(dim=1).sqrt()
+        pr = p.square().sum(dim=1).sqrt()
+        emax.append(torch.where(pm > 0, dm / pm.clamp_min(1e-300), dm))
+        erms.append(torch.where(pr > 0, dr / pr.clamp_min(1e-300), dr))
+    return torch.cat(emax).cpu().numpy(), torch.cat(erms).cpu().numpy()
+
+
+def fp64_compare(args, a, w, step, dl, timed, torch, dev, world):
+    from dbsr_gb300 import FACTOR_FP64, PLAIN_FP64, SPLIT_BF16, synth
+
+    ms, nblk = a.ms, w.iicc
+    fl = synth.algorithmic_flops(w)["total"]
+    hs = torch.empty(nblk * ms * ms, dtype=torch.float64, device=dev)
+    a.get_matrix(out=hs)
+    out = {}
+    if args.precision == "split":
+        a.set_precision(FACTOR_FP64)
+        step(dl)
+        t = timed(lambda: step(dl), 1)
+        out["factor_fp64_s_per_matrix"] = t
+    a.set_precision(PLAIN_FP64)
+    step(dl)
+    t = timed(lambda: step(dl), 1)
+    out["plain_fp64_s_per_matrix"] = t
+    out["plain_fp64_gflops"] = world * fl / t / 1e9
+    hp = torch.empty_like(hs)
+    a.get_matrix(out=hp)
+    a.set_precision({"split": SPLIT_BF16, "factor": FACTOR_FP64}[args.precision])
+    emax, erms = block_errors(torch, hs, hp, nblk, ms)
+    del hs, hp
+    torch.cuda.empty_cache()
+    if args.block_errors:
+        with open(args.block_errors, "w") as f:
+            f.write("block,max_rel,rms_rel\n")
+            for b in range(nblk):
+                f.write(f"{b + 1},{emax[b]:.3e},{erms[b]:.3e}\n")
+    out["reference"] = ("plain FP64 GPU assembly of the same inputs (held to the CPU oracle at "
+                        "1e-12 per block by the parity tests)")
+    out["blocks"] = int(nblk)
+    out["max_rel_err"] = {"max": float(emax.max()), "p99": float(np.percentile(emax, 99)),
+                          "median": float(np.median(emax))}
+    out["rms_rel_err"] = {"max": float(erms.max()), "p99": float(np.percentile(erms, 99)),
+                          "median": float(np.median(erms))}
+    out["blocks_within_1e-10"] = int((emax <= 1e-10).sum())
+    return out
+
+
 # ---------------------------------------------------------------------------
 def main():
     args = parse()
@@ -379,6 +442,13 @@ def main():
     else:
         roofline = {}
 
+    # FP64 comparison: the same matrix by the factored FP64 and the plain FP64
+    # assemblies (the plain one is held to the CPU oracle at 1e-12 by the
+    # parity tests), per-block errors of the headline form against plain FP64
+    compare = None
+    if args.precision != "plain" and not args.no_compare:
+        compare = fp64_compare(args, a, w, step, dl, timed, torch, dev, world)
+
     # e2e: lists from pinned host memory, matrix back to pinned host memory
     e2e = None
     if not args.no_e2e:
@@ -425,6 +495,7 @@ def main():
                        "l2": "inputs and output larger than L2 (hch 37 GB)",
                        "parallelism": f"replicas x{world}"},
             "s_per_matrix": dt,
+            "fp64_comparison": compare,
             "roofline": roofline,
             "cpu_baseline": cpu,
             "e2e": e2e,

@@ -599,7 +599,7 @@ int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const 
   // ---- 1. list in IPT order on the device (scratch2 holds the list state)
   const size_t ibytes = sizeof(int) * (size_t)n, dbytes = sizeof(double) * (size_t)n;
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
-  size_t tot = 7 * al(ibytes) + 2 * al(dbytes) + al(sizeof(int) * (n + 2)) + al(64) +
+  size_t tot = 8 * al(ibytes) + 2 * al(dbytes) + al(sizeof(int) * (n + 2)) + al(64) +
                al(sizeof(SegInfo) * (size_t)(n + 1)) + 3 * al(sizeof(int) * (size_t)(n + 1));
   if ((rc = ensure_scratch2(c, tot))) return rc;
   char *base = (char *)c->scratch2;
@@ -613,6 +613,7 @@ int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const 
   int *dipt = (int *)take(ibytes);
   int *lk1 = (int *)take(ibytes), *lk2 = (int *)take(ibytes), *lk3 = (int *)take(ibytes);
   double *lcd = (double *)take(dbytes);
+  int *lpair = (int *)take(ibytes);  // factored path: bound-orbital pair of each entry
   int *seg_start = (int *)take(sizeof(int) * (size_t)(n + 2));
   int *dscal = (int *)take(64);  // [0]=nseg [1]=err [2]=nown
   SegInfo *info = (SegInfo *)take(sizeof(SegInfo) * (size_t)(n + 1));
@@ -742,13 +743,14 @@ int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const 
   // ---- chunks of owner segments, each with its partner (a channel pair
   // listed in both orders maps to one block; both lists contribute to that
   // block in list order within every atype, so they stay in one chunk)
-  if (factored && icv >= 3) {
+  if (factored) {
+    // the factored contraction works with ordered pairs of bound orbitals
     if (c->nbound < 1) return set_err(c, DBSRG_ESTATE, "no bound orbitals (ipbs = 0)");
-    if ((rc = check_bound_orbitals(c, n, lk2, lk3, dscal + 1))) return rc;
+    if ((rc = pair_index(c, n, lk2, lk3, lpair, dscal + 1))) return rc;
     int h = 0;
     DBSRG_TRY(c, cudaMemcpyAsync(&h, dscal + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
     DBSRG_TRY(c, cudaStreamSynchronize(st));
-    if (h) return set_err(c, DBSRG_EINVAL, "factored exchange: K2/K3 must be bound orbitals");
+    if (h) return set_err(c, DBSRG_EINVAL, "factored contraction: K2/K3 must be bound orbitals");
   }
   std::vector<SegInfo> hinfo(nseg);
   DBSRG_TRY(c, cudaMemcpyAsync(hinfo.data(), info, sizeof(SegInfo) * nseg,
@@ -762,6 +764,8 @@ int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const 
   }
   const size_t per = (size_t)ns * ncol;
   std::vector<int> mem, own;  // member segment ids; owner slot positions
+  // the factored direct cases keep no per-segment results: larger chunks
+  const int chunk = (factored && icv <= 2) ? 16 * kSegChunk : kSegChunk;
   auto flush = [&]() -> int {
     int nm = (int)mem.size();
     if (nm == 0) return DBSRG_OK;
@@ -771,19 +775,12 @@ int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const 
     std::copy(own.begin(), own.end(), h.begin() + nm);
     int rc2;
     if ((rc2 = copy_in(c, members, h.data(), sizeof(int) * h.size()))) return rc2;
-    // the factored exchange forms its own band-limited densities: no X
-    const bool no_x = factored && icv >= 3;
-    size_t need2 = (no_x ? 1 : 2) * sizeof(double) * per * na * nm;
-    if ((rc2 = ensure_scratch(c, need2))) return rc2;
-    double *X = (double *)c->scratch;
-    double *Y = no_x ? X : X + per * na * nm;
-    if (!no_x) {
-      dim3 gd((unsigned)((per + 255) / 256), (unsigned)nm, (unsigned)na);
-      DBSRG_RUN(c, "k_density_acc",
-                k_density_acc<<<gd, 256, 0, st>>>(ns, ks, sym_d, ncol, na, dsp, nm, members, info,
-                                                  lk2, lk3, lcd, c->pq, X));
-    }
     if (factored) {
+      double *Y = nullptr;
+      if (icv >= 3) {
+        if ((rc2 = ensure_scratch(c, sizeof(double) * per * na * nm))) return rc2;
+        Y = (double *)c->scratch;
+      }
       FactorJob job{};
       job.family = tabfam;
       job.kpol = kpol;
@@ -794,21 +791,36 @@ int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const 
         job.types[a] = ttype[a];
         job.jp1[a] = dsp.jp1[a];
         job.jp2[a] = dsp.jp2[a];
+        job.ii[a] = ssp.ii[a];
+        job.jj[a] = ssp.jj[a];
         job.tabs[a] = tabs[a];
       }
       job.nm = nm;
       job.members = members;
+      job.nown = (int)own.size();
+      job.own = members + nm;
       job.info = info;
       job.k2 = lk2;
       job.k3 = lk3;
+      job.pairs = lpair;
       job.cd = lcd;
-      job.X = no_x ? nullptr : X;
       job.Y = Y;
-      job.per = per;
       job.split = c->precision == DBSRG_SPLIT_BF16;
-      if ((rc2 = factored_contract(c, job))) return rc2;
+      rc2 = factored_contract(c, job);
+      mem.clear();
+      own.clear();
+      return rc2;
     }
-    for (int a = 0; a < na && !factored; a++) {
+    if ((rc2 = ensure_scratch(c, 2 * sizeof(double) * per * na * nm))) return rc2;
+    double *X = (double *)c->scratch;
+    double *Y = X + per * na * nm;
+    {
+      dim3 gd((unsigned)((per + 255) / 256), (unsigned)nm, (unsigned)na);
+      DBSRG_RUN(c, "k_density_acc",
+                k_density_acc<<<gd, 256, 0, st>>>(ns, ks, sym_d, ncol, na, dsp, nm, members, info,
+                                                  lk2, lk3, lcd, c->pq, X));
+    }
+    for (int a = 0; a < na; a++) {
       const double *Xa = X + (size_t)a * nm * per;
       double *Ya = Y + (size_t)a * nm * per;
       if (icv <= 2) {
@@ -838,7 +850,7 @@ int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const 
     own.push_back((int)mem.size());
     mem.push_back(s);
     if (hinfo[s].partner >= 0) mem.push_back(hinfo[s].partner);
-    if ((int)mem.size() >= kSegChunk - 1)
+    if ((int)mem.size() >= chunk - 1)
       if ((rc = flush())) return rc;
   }
   if ((rc = flush())) return rc;

@@ -80,6 +80,9 @@ int ensure_tscratch(dbsrg_ctx *c, size_t bytes) {
 int ensure_tcscratch(dbsrg_ctx *c, size_t bytes) {
   return grow(c, &c->tcscratch, &c->tcscratch_bytes, bytes);
 }
+int ensure_pscratch(dbsrg_ctx *c, size_t bytes) {
+  return grow(c, &c->pscratch, &c->pscratch_bytes, bytes);
+}
 bool sync_check_enabled() {
   static int v = -1;
   if (v < 0) {
@@ -117,15 +120,6 @@ static void timing_clear(dbsrg_ctx *c) {
   c->tev.clear();
 }
 
-static void free_farfield(dbsrg_ctx *c) {
-  for (auto &f : c->rfar)
-    if (f.U) cudaFree(f.U);
-  for (auto &f : c->sfar)
-    if (f.U) cudaFree(f.U);
-  c->rfar.clear();
-  c->sfar.clear();
-}
-
 static void free_tables(dbsrg_ctx *c) {
   for (double *p : c->rtab)
     if (p) cudaFree(p);
@@ -143,7 +137,7 @@ static void free_tables(dbsrg_ctx *c) {
     if (cd.lo1) cudaFree(cd.lo1);
   for (auto &cd : c->scell)
     if (cd.lo1) cudaFree(cd.lo1);
-  free_farfield(c);
+  free_orbital_products(c);
   c->rtab.clear();
   c->stab.clear();
   c->quad.clear();
@@ -213,6 +207,7 @@ int dbsrg_destroy(dbsrg_ctx *c) {
   if (c->tscratch) cudaFree(c->tscratch);
   if (c->fscratch) cudaFree(c->fscratch);
   if (c->tcscratch) cudaFree(c->tcscratch);
+  if (c->pscratch) cudaFree(c->pscratch);
   if (c->bmap) cudaFree(c->bmap);
   if (c->b2o) cudaFree(c->b2o);
   if (c->pinned) cudaFreeHost(c->pinned);
@@ -308,7 +303,7 @@ int dbsrg_set_orbitals(dbsrg_ctx *c, int nbf, const double *pq, const int *ipbs)
   rc = copy_in(c, c->ipbs, c->h_ipbs.data(), nbf * sizeof(int));
   if (rc) return rc;
   // dense numbering of the bound orbitals (ipbs = 0) for the factored path
-  free_farfield(c);
+  free_orbital_products(c);
   if (c->bmap) cudaFree(c->bmap);
   if (c->b2o) cudaFree(c->b2o);
   c->bmap = nullptr;

@@ -5,39 +5,47 @@
 // electron-2 functions on interval jv, a cell with iv < jv is the product of
 // two 1-D moments, lo1(pair1,iv)*hi2(pair2,jv); iv > jv gives
 // lo2(pair2,jv)*hi1(pair1,iv) (R^k only); iv == jv the diagonal-cell integral
-// rkd.  The contraction of a table with a segment's density uses that
-// structure instead of the assembled table:
+// rkd.  A segment's density is a sum over its entries of orbital products,
+// rho = sum_e c_e p1_{a_e} (x) p2_{b_e} with a_e, b_e the bound orbitals of
+// K2, K3, so every contraction is linear in the ordered bound-orbital pairs
+// (a,b).  The factored path therefore works per table with those pairs and
+// per segment only with its coefficients:
 //
-// exchange (convol cases 3/4, the full ns x ns block of R_data itype 4 and
-// S_data itypes 8/9):  out(x,y) = sum_e c_e K_{a_e b_e}(x,y), where x, y are
-// the output functions of electrons 1 and 2 and a_e, b_e the bound orbitals
-// of the entry.  When y - x >= 9 every contributing cell has iv < jv and
-//     K_ab(x,y) = U_a(x) V_b(y),  U_a(x) = sum_iv sum_x' lo1(x,x';iv) p_a(x'),
-//                                 V_b(y) = sum_jv sum_y' hi2(y',y;jv) p_b(y'),
-// so out = U C V^T on that far field (C = the segment's coefficients over
-// bound-orbital pairs); likewise x - y >= 9 gives Ul C Vl^T (R^k).  The band
-// |y - x| <= 8 is gathered from the table itself with a band-limited
-// density (|x' - y'| <= 24 is all the band needs).
+// exchange (convol cases 3/4: R_data itype 4, S_data itypes 8/9), result
+// out(x,y) over the output functions x, y of electrons 1 and 2:
+//   far field |y-x| >= 9: every contributing cell has iv < jv, so
+//     out = U C V^T with U_a(x) = sum_iv sum_x' lo1(x,x';iv) p_a(x'),
+//     V_b(y) = sum_jv sum_y' hi2(y',y;jv) p_b(y') and C the segment's
+//     coefficients over pairs (x-y >= 9: Ul C Vl^T, R^k only; zero for S^k);
+//   near band |y-x| <= 8: out = sum_e c_e Kb_{a_e b_e}, where the band pair
+//     potential Kb_ab(x,y) = sum_(i,j) W_xy(i,j) p1_a(i) p2_b(j) holds the
+//     band-table element W_xy(i,j) that the exchange gather pairs with
+//     density element (i,j) (built once per table, in two separable stages).
 //
-// direct (convol cases 1/2, the band results of R_data itype 3 and S_data
-// itypes 6/7): the output band of one electron's pair is
-//     sum_iv [lo1(pair;iv) Suf_hi(iv) + hi1(pair;iv) Pre_lo(iv) + sum_pair2 rkd(pair,pair2;iv) rho(pair2)]
-// with Suf/Pre the suffix/prefix sums over cells of the other electron's
-// moment-weighted density -- the diagonal cells are the only non-separable
-// part.
+// direct (convol cases 1/2: R_data itype 3, S_data itypes 6/7): the band
+// result is sum_e c_e Kd_{a_e b_e}, with the direct pair potential
+//   Kd_ab(pair1) = sum_iv [lo1(pair1;iv) Suf_ab(iv) + hi1(pair1;iv) Pre_ab(iv)]
+//                + sum_{pair2} rkd(pair1,pair2;iv) rho_ab(pair2)   (iv = jv)
+// Suf/Pre the suffix/prefix sums over cells of the moment-weighted density of
+// the pair, and rho_ab the pair density in the reference's storage (the
+// symmetric 's' storage sums both orders, p1(f)p2(s)+p1(s)p2(f)).
 //
-// All of this is FP64; with job.split the far-field product runs as
-// split-precision products on the tensor cores (farfield_tc.cu).
+// The per-segment work is then a sum of a few dozen potential rows per
+// output element, fused into the scatter for the direct cases.  All of this
+// is FP64; with job.split the far-field product runs as split-precision
+// products on the tensor cores (farfield_tc.cu).
 #include "internal.cuh"
 
 #include <algorithm>
 
 namespace {
 
-constexpr int NB_MAX = 64;   // bound orbitals handled by the far-field kernels
-constexpr int XB_HALF = 24;  // half width of the band-limited density
-constexpr int XB_W = 2 * XB_HALF + 1;
-constexpr int FAR = 9;       // |y - x| >= FAR is far field (spline orders <= 9)
+constexpr int NB_MAX = 64;        // bound orbitals handled by the factored path
+constexpr int FAR = 9;            // |y - x| >= FAR is far field (spline orders <= 9)
+constexpr int BAND = FAR - 1;     // near band |y - x| <= 8
+constexpr int NDB = 2 * BAND + 1; // band diagonals
+constexpr int PXC = 8;            // output rows per block of the band pair potentials
+constexpr int PBC = 4;            // second-orbital chunk of the diagonal-cell stage
 
 struct PairSpec {
   int k1, k2, sym;  // orders of the first / second function; packed symmetric
@@ -77,6 +85,41 @@ TableBases table_bases(const DeviceGrid &g, int family, int type) {
   return t;
 }
 
+// target quadrants of the atypes of one list (UPDATE_HS)
+struct QuadSpec {
+  int na;
+  int ii[4], jj[4];
+};
+
+// direct pair potentials of the atypes of one list
+struct KdSet {
+  const double *K[4];
+};
+
+// ---------------------------------------------------------------------------
+// bound-orbital rows of one component: P[a*ns + x] = pq(x+1, comp, b2o[a])
+__global__ void k_bound_rows(int ns, int nb, const int *b2o, const double *pq, int comp,
+                             double *P) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= ns * nb) return;
+  int x = q % ns, a = q / ns;
+  P[q] = pq[(size_t)x + (size_t)ns * (comp - 1) + (size_t)2 * ns * (b2o[a] - 1)];
+}
+
+// ordered bound-orbital pair of every entry
+__global__ void k_pair_index(int n, const int *k2, const int *k3, const int *bmap, int nb,
+                             int *pairs, int *err) {
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  int a = bmap[k2[e] - 1], b = bmap[k3[e] - 1];
+  if (a < 0 || b < 0) {
+    atomicExch(err, 3);
+    pairs[e] = 0;
+    return;
+  }
+  pairs[e] = a * nb + b;
+}
+
 // ---------------------------------------------------------------------------
 // far-field vectors of one electron: Ulo(x,a) = sum_iv sum_xc mlo(pair;iv) p_a(xc)
 // (and Uhi with mhi), x the output function, xc the contracted one.
@@ -103,10 +146,10 @@ __global__ void k_far_vectors(int ns, int nv, int kk, int nb, const int *b2o, co
   if (Uhi) Uhi[q] = shi;
 }
 
-// Z(a,y) = sum_{e in segment, bound(K2)=a} c_e V(y, bound(K3)), also Zl with Vl
-__global__ void k_far_z(int ns, int nb, int nm, const int *members, const SegInfo *info,
-                        const int *k2, const int *k3, const double *cd, const int *bmap,
-                        const double *V, const double *Vl, double *Z, double *Zl) {
+// Z(a,y) = sum_{e in segment, first orbital a} c_e V(y, second orbital), also Zl with Vl
+__global__ void k_far_z(int ns, int nb, const int *members, const SegInfo *info,
+                        const int *pairs, const double *cd, const double *V, const double *Vl,
+                        double *Z, double *Zl) {
   int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= ns * nb) return;
   int a = q % nb, y = q / nb;
@@ -114,35 +157,15 @@ __global__ void k_far_z(int ns, int nb, int nm, const int *members, const SegInf
   SegInfo si = info[members[slot]];
   double z = 0.0, zl = 0.0;
   for (int e = si.start; e < si.end; e++) {
-    if (bmap[k2[e] - 1] != a) continue;
-    int b = bmap[k3[e] - 1];
+    const int pr = pairs[e];
+    if (pr / nb != a) continue;
+    const int b = pr - a * nb;
     z = fma(cd[e], V[(size_t)y + (size_t)ns * b], z);
     if (Vl) zl = fma(cd[e], Vl[(size_t)y + (size_t)ns * b], zl);
   }
   size_t o = (size_t)slot * nb * ns + q;  // Z[slot][a + nb*y]
   Z[o] = z;
   if (Zl) Zl[o] = zl;
-}
-
-// band-limited exchange density: Xb(xc, d) = sum_e c_e p1(xc) p2(xc+d-24)
-__global__ void k_density_band(int ns, int nm, const int *members, const SegInfo *info,
-                               const int *k2, const int *k3, const double *cd, const double *pq,
-                               int jp1, int jp2, double *Xb) {
-  int q = blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= ns * XB_W) return;
-  int xc = q % ns, d = q / ns;
-  int yc = xc + d - XB_HALF;
-  int slot = blockIdx.y;
-  SegInfo si = info[members[slot]];
-  double acc = 0.0;
-  if (yc >= 0 && yc < ns) {
-    for (int e = si.start; e < si.end; e++) {
-      double p1 = pq[(size_t)xc + (size_t)ns * (jp1 - 1) + (size_t)2 * ns * (k2[e] - 1)];
-      double p2 = pq[(size_t)yc + (size_t)ns * (jp2 - 1) + (size_t)2 * ns * (k3[e] - 1)];
-      acc = acc + cd[e] * (p1 * p2);
-    }
-  }
-  Xb[(size_t)slot * ns * XB_W + q] = acc;
 }
 
 // far field out(x,y) = U(x,:) Z(:,y) for y-x >= FAR, Ul(x,:) Zl(:,y) for
@@ -156,9 +179,9 @@ __global__ void __launch_bounds__(256) k_far_field(int ns, int nb, const double 
   __shared__ double sul[32][FK + 1], szl[FK][33];
   const int slot = blockIdx.z;
   const int x0 = blockIdx.x * 32, y0 = blockIdx.y * 32;
-  const bool any_up = (y0 + 31) - x0 >= FAR, lo_region = (x0 + 31) - y0 >= FAR;
-  const bool any_lo = Ul && lo_region;  // S^k tables have no lower field: zeros there
-  if (!any_up && !lo_region) return;
+  const bool any_up = (y0 + 31) - x0 >= FAR;
+  const bool any_lo = Ul && (x0 + 31) - y0 >= FAR;
+  if (!any_up && !any_lo) return;
   const double *Zs = Z + (size_t)slot * nb * ns;
   const double *Zls = Zl ? Zl + (size_t)slot * nb * ns : nullptr;
   double acc[4] = {0.0, 0.0, 0.0, 0.0};
@@ -194,235 +217,432 @@ __global__ void __launch_bounds__(256) k_far_field(int ns, int nb, const double 
     int x = x0 + r, y = y0 + cc;
     if (x >= ns || y >= ns) continue;
     int d = y - x;
-    if (d >= FAR || d <= -FAR) Ys[(size_t)x + (size_t)ns * y] = acc[t];
+    if (d >= FAR || (Ul && d <= -FAR)) Ys[(size_t)x + (size_t)ns * y] = acc[t];
   }
-}
-
-// band |y-x| <= 8 of the exchange result from the table and the band density
-// (the gather of k_exchange in assemble.cu restricted to the band).
-// mode 0: R table 's','s' case 3; 1: S 'n','n' case 3; 2: S 'n','n' case 4.
-__global__ void __launch_bounds__(256) k_band_exchange(int ns, int ks, int mode,
-                                                       const double *__restrict__ rkb,
-                                                       const double *__restrict__ Xb,
-                                                       double *__restrict__ Y, size_t per) {
-  int q = blockIdx.x * blockDim.x + threadIdx.x;
-  const int nd = 2 * (FAR - 1) + 1;
-  if (q >= ns * nd) return;
-  const int slot = blockIdx.y;
-  const int x = q % ns + 1, y = x + q / ns - (FAR - 1);
-  if (y < 1 || y > ns) return;
-  const double *D = Xb + (size_t)slot * ns * XB_W;
-  auto DV = [&](int i, int j) -> double {
-    return __ldg(&D[(size_t)(i - 1) + (size_t)ns * (j - i + XB_HALF)]);
-  };
-  double acc = 0.0;
-  // band table: rkb(i, j-i+BW+1, ip, jp), |j - i| <= BW (= 16) is all that
-  // the band outputs read
-  constexpr int BW = DBSRG_TABLE_BAND, NJ = 2 * DBSRG_TABLE_BAND + 1;
-  if (mode == 0) {
-    auto TB = [&](int i, int j, int ip, int jp) -> double {
-      return __ldg(&rkb[(size_t)(i - 1) + (size_t)ns * ((size_t)(j - i + BW) +
-                        (size_t)NJ * ((size_t)(ip - 1) + (size_t)ks * (size_t)(jp - 1)))]);
-    };
-    for (int jp = 1; jp <= ks; jp++)
-      for (int ip = 1; ip <= ks; ip++) {
-        if (y - jp + 1 >= 1 && x + ip - 1 <= ns)
-          acc = fma(TB(x, y - jp + 1, ip, jp), DV(x + ip - 1, y - jp + 1), acc);
-        if (ip > 1 && x - ip + 1 >= 1 && y - jp + 1 >= 1)
-          acc = fma(TB(x - ip + 1, y - jp + 1, ip, jp), DV(x - ip + 1, y - jp + 1), acc);
-        if (jp > 1 && x + ip - 1 <= ns && y + jp - 1 <= ns)
-          acc = fma(TB(x, y, ip, jp), DV(x + ip - 1, y + jp - 1), acc);
-        if (ip > 1 && jp > 1 && x - ip + 1 >= 1 && y + jp - 1 <= ns)
-          acc = fma(TB(x - ip + 1, y, ip, jp), DV(x - ip + 1, y + jp - 1), acc);
-      }
-  } else {
-    const int kb = 2 * ks - 1;
-    auto TB = [&](int i, int j, int ip, int jp) -> double {
-      return __ldg(&rkb[(size_t)(i - 1) + (size_t)ns * ((size_t)(j - i + BW) +
-                        (size_t)NJ * ((size_t)(ip - 1) + (size_t)kb * (size_t)(jp - 1)))]);
-    };
-    for (int jp = 1; jp <= kb; jp++)
-      for (int ip = 1; ip <= kb; ip++) {
-        if (mode == 1) {
-          int j = y - jp + ks, ii = x + ip - ks;
-          if (j < max(1, 1 + ks - jp) || j > min(ns, ns + ks - jp)) continue;
-          if (x < max(1, 1 + ks - ip) || x > min(ns, ns + ks - ip)) continue;
-          acc = fma(TB(x, j, ip, jp), DV(ii, j), acc);
-        } else {
-          int i = x - ip + ks, jj = y + jp - ks;
-          if (y < max(1, 1 + ks - jp) || y > min(ns, ns + ks - jp)) continue;
-          if (i < max(1, 1 + ks - ip) || i > min(ns, ns + ks - ip)) continue;
-          acc = fma(TB(i, y, ip, jp), DV(i, jj), acc);
-        }
-      }
-  }
-  Y[(size_t)slot * per + (size_t)(x - 1) + (size_t)ns * (y - 1)] = acc;
 }
 
 // ---------------------------------------------------------------------------
-// direct contraction, one thread block per (segment slot): cell sums of the
-// density electron, prefix/suffix sums over cells, then the output band.
-//   icv 1: output electron-1 pair band, density over electron-2 pairs
-//   icv 2: output electron-2 pair band, density over electron-1 pairs (S^k)
-// storage: 's' Y(x,ip) x'=x+ip-1 (R^k), 'n' Y(x,ip) x'=x+ip-ks (S^k)
-__global__ void __launch_bounds__(256) k_direct(int ns, int ks, int nv, int kk, int icv,
-                                                char sym, PairSpec e1, PairSpec e2,
-                                                const double *lo1, const double *hi1,
-                                                const double *lo2, const double *hi2,
-                                                const double *rkd, const double *X, double *Y,
-                                                size_t per) {
-  extern __shared__ double sh[];
-  double *s_a = sh;        // cell sums (hi for icv1 upper, lo1 for icv2)
-  double *s_b = sh + nv;   // icv1 lower (R^k)
-  const int slot = blockIdx.x;
-  const double *Xs = X + (size_t)slot * per;
-  const int ncol = sym == 's' ? ks : 2 * ks - 1;
-  // density value of a pair of absolute indices (first, second) or 0
-  auto rho = [&](int f, int s2) -> double {
-    if (f < 1 || s2 < 1 || f > ns || s2 > ns) return 0.0;
-    if (sym == 's') {
-      int lo = min(f, s2), dd = abs(f - s2);
-      if (dd >= ks) return 0.0;
-      return Xs[(size_t)(lo - 1) + (size_t)ns * dd];
-    }
-    int c = s2 - f + ks;
-    if (c < 1 || c > 2 * ks - 1) return 0.0;
-    return Xs[(size_t)(f - 1) + (size_t)ns * (c - 1)];
+// band pair potentials of an exchange table, one block per PXC output rows
+// and one band diagonal d = y - x:
+//   W(x; i, j)  the table element the exchange gather of output (x, y) pairs
+//               with density element (i, j) (the gather of k_exchange in
+//               assemble.cu, restricted to the band; every (i, j) meets one
+//               element, so W needs no sums)
+//   H(x; i, b)  = sum_j W(x; i, j) P2(b, j)
+//   Kb(ab; x, y) = sum_i P1(a, i) H(x; i, b)
+// mode 0: R table 's','s' case 3; 1: S 'n','n' case 3; 2: S 'n','n' case 4.
+// Band table layout: rkb(i, j-i+BW+1, ip, jp) for |j - i| <= BW.
+__global__ void __launch_bounds__(256) k_pair_band(int ns, int ks, int nb, int mode,
+                                                   const double *__restrict__ rkb,
+                                                   const double *__restrict__ P1,
+                                                   const double *__restrict__ P2,
+                                                   double *__restrict__ Kb) {
+  extern __shared__ double sm[];
+  const int W = 2 * ks - 1;            // offsets -(ks-1) .. ks-1
+  const int WL = PXC + W - 1;          // window of the row vectors
+  const int x0 = blockIdx.x * PXC + 1; // first output row (1-based)
+  const int d = (int)blockIdx.y - BAND;
+  double *Wm = sm;                     // [PXC][W][W]
+  double *p1w = Wm + PXC * W * W;      // [nb][WL]: P1(a, x0-(ks-1)+t)
+  double *p2w = p1w + nb * WL;         // [nb][WL]: P2(b, x0+d-(ks-1)+t)
+  double *H = p2w + nb * WL;           // [PXC][W][nb]
+  const int kb = mode == 0 ? ks : 2 * ks - 1;
+  constexpr int BW = DBSRG_TABLE_BAND, NJ = 2 * DBSRG_TABLE_BAND + 1;
+  auto TB = [&](int i, int j, int ip, int jp) -> double {
+    return rkb[(size_t)(i - 1) + (size_t)ns * ((size_t)(j - i + BW) +
+               (size_t)NJ * ((size_t)(ip - 1) + (size_t)kb * (size_t)(jp - 1)))];
   };
-  PairSpec ed = icv == 1 ? e2 : e1;  // electron whose pairs carry the density
-  // phase 1: moment-weighted density per cell of the density electron
-  for (int cv = threadIdx.x + 1; cv <= nv; cv += blockDim.x) {
-    double sa = 0.0, sb = 0.0;
-    for (int h1 = 1; h1 <= ed.k1; h1++)
-      for (int h2 = ed.sym ? h1 : 1; h2 <= ed.k2; h2++) {
-        double r = rho(cv + h1 - 1, cv + h2 - 1);
-        size_t o = (size_t)pidx(ed, h1, h2) + (size_t)kk * (cv - 1);
-        if (icv == 1) {
-          sa = fma(hi2[o], r, sa);
-          if (lo2) sb = fma(lo2[o], r, sb);
-        } else {
-          sa = fma(lo1[o], r, sa);
-        }
-      }
-    s_a[cv - 1] = sa;
-    s_b[cv - 1] = sb;
+  for (int q = threadIdx.x; q < PXC * W * W; q += blockDim.x) Wm[q] = 0.0;
+  for (int q = threadIdx.x; q < nb * WL; q += blockDim.x) {
+    const int a = q / WL, t = q % WL;
+    const int xi = x0 - (ks - 1) + t, yi = x0 + d - (ks - 1) + t;
+    p1w[q] = (xi >= 1 && xi <= ns) ? P1[(size_t)a * ns + xi - 1] : 0.0;
+    p2w[q] = (yi >= 1 && yi <= ns) ? P2[(size_t)a * ns + yi - 1] : 0.0;
   }
   __syncthreads();
-  // phase 2: icv1 -> s_a := suffix sums sum_{jv>iv}, s_b := prefix sums
-  // sum_{jv<iv}; icv2 -> s_a := prefix sums sum_{iv<jv}
-  if (threadIdx.x == 0) {
-    if (icv == 1) {
-      double acc = 0.0;
-      for (int iv = nv; iv >= 1; iv--) {
-        double v = s_a[iv - 1];
-        s_a[iv - 1] = acc;
-        acc += v;
-      }
-      acc = 0.0;
-      for (int iv = 1; iv <= nv; iv++) {
-        double v = s_b[iv - 1];
-        s_b[iv - 1] = acc;
-        acc += v;
-      }
+  for (int q = threadIdx.x; q < PXC * kb * kb; q += blockDim.x) {
+    const int xl = q / (kb * kb), r = q % (kb * kb), ip = r % kb + 1, jp = r / kb + 1;
+    const int x = x0 + xl, y = x + d;
+    if (x > ns || y < 1 || y > ns) continue;
+    double *w = Wm + (size_t)xl * W * W;
+    auto put = [&](int i, int j, double v) { w[(i - x + ks - 1) * W + (j - y + ks - 1)] = v; };
+    if (mode == 0) {
+      if (y - jp + 1 >= 1 && x + ip - 1 <= ns)
+        put(x + ip - 1, y - jp + 1, TB(x, y - jp + 1, ip, jp));
+      if (ip > 1 && x - ip + 1 >= 1 && y - jp + 1 >= 1)
+        put(x - ip + 1, y - jp + 1, TB(x - ip + 1, y - jp + 1, ip, jp));
+      if (jp > 1 && x + ip - 1 <= ns && y + jp - 1 <= ns)
+        put(x + ip - 1, y + jp - 1, TB(x, y, ip, jp));
+      if (ip > 1 && jp > 1 && x - ip + 1 >= 1 && y + jp - 1 <= ns)
+        put(x - ip + 1, y + jp - 1, TB(x - ip + 1, y, ip, jp));
+    } else if (mode == 1) {
+      const int j = y - jp + ks, ii = x + ip - ks;
+      if (j < max(1, 1 + ks - jp) || j > min(ns, ns + ks - jp)) continue;
+      if (x < max(1, 1 + ks - ip) || x > min(ns, ns + ks - ip)) continue;
+      put(ii, j, TB(x, j, ip, jp));
     } else {
-      double acc = 0.0;
-      for (int iv = 1; iv <= nv; iv++) {
-        double v = s_a[iv - 1];
-        s_a[iv - 1] = acc;
-        acc += v;
-      }
+      const int i = x - ip + ks, jj = y + jp - ks;
+      if (y < max(1, 1 + ks - jp) || y > min(ns, ns + ks - jp)) continue;
+      if (i < max(1, 1 + ks - ip) || i > min(ns, ns + ks - ip)) continue;
+      put(i, jj, TB(i, y, ip, jp));
     }
   }
   __syncthreads();
-  // phase 3a: the separable (off-diagonal cell) terms into the output band,
-  // kept in shared memory
-  PairSpec eo = icv == 1 ? e1 : e2;
-  double *out = sh + 2 * nv;               // ns * ncol
-  double *rho_w = out + (size_t)ns * ncol; // 81 values per warp
-  for (int q = threadIdx.x; q < ns * ncol; q += blockDim.x) {
-    int f = q % ns + 1, col = q / ns + 1;
-    int s2 = sym == 's' ? f + col - 1 : f + col - ks;
-    double acc = 0.0;
-    if (s2 >= 1 && s2 <= ns) {
-      int lo = max(max(1, f - eo.k1 + 1), s2 - eo.k2 + 1), hi = min(min(nv, f), s2);
-      for (int cv = lo; cv <= hi; cv++) {
-        size_t o = (size_t)pidx(eo, f - cv + 1, s2 - cv + 1) + (size_t)kk * (cv - 1);
-        if (icv == 1) {
-          acc = fma(lo1[o], s_a[cv - 1], acc);
-          if (hi1) acc = fma(hi1[o], s_b[cv - 1], acc);
-        } else {
-          acc = fma(hi2[o], s_a[cv - 1], acc);
-        }
-      }
-    }
-    out[q] = acc;
+  for (int q = threadIdx.x; q < PXC * W * nb; q += blockDim.x) {
+    const int b = q % nb, r = q / nb, u = r % W, xl = r / W;
+    const double *w = Wm + ((size_t)xl * W + u) * W;
+    const double *p = p2w + (size_t)b * WL + xl;
+    double s = 0.0;
+    for (int v = 0; v < W; v++) s = fma(w[v], p[v], s);
+    H[q] = s;
   }
   __syncthreads();
-  // phase 3b: diagonal cells, one warp per cell.  Cell cv touches outputs
-  // with first index in [cv, cv+8], so cells 9 apart never share an output:
-  // nine phases of disjoint cells give every output one writer at a time.
-  const int lane = threadIdx.x % 32, warp = threadIdx.x / 32, nwarp = blockDim.x / 32;
+  const size_t per = (size_t)ns * NDB;
+  for (int q = threadIdx.x; q < PXC * nb * nb; q += blockDim.x) {
+    const int xl = q % PXC, pr = q / PXC, b = pr % nb, a = pr / nb;
+    const int x = x0 + xl, y = x + d;
+    if (x > ns || y < 1 || y > ns) continue;
+    const double *p = p1w + (size_t)a * WL + xl;
+    const double *h = H + (size_t)xl * W * nb + b;
+    double s = 0.0;
+    for (int u = 0; u < W; u++) s = fma(p[u], h[(size_t)u * nb], s);
+    Kb[(size_t)pr * per + (size_t)(x - 1) + (size_t)ns * (d + BAND)] = s;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// direct pair potentials.  ed: pairs of the density electron, eo: of the
+// output electron.  Pair densities of a symmetric storage give every ordered
+// (h1, h2) the moment of the unordered pair (pidx orders them).
+//
+// (1) cell sums, one block per cell cv:
+//   S1(ab, cv) = sum_{h1,h2} M1(h1,h2;cv) P1(a, cv+h1-1) P2(b, cv+h2-1), S2 with M2
+__global__ void k_pair_cellsum(int ns, int nv, int kk, int nb, PairSpec ed, const double *M1,
+                               const double *M2, const double *P1, const double *P2, double *S1,
+                               double *S2) {
+  extern __shared__ double sm[];
+  const int cv = blockIdx.x + 1, k1 = ed.k1, k2 = ed.k2;
+  double *w1 = sm, *w2 = w1 + nb * k1, *t1 = w2 + nb * k2, *t2 = t1 + nb * k1;
+  for (int q = threadIdx.x; q < nb * k1; q += blockDim.x) {
+    const int a = q / k1, x = cv + q % k1;
+    w1[q] = x <= ns ? P1[(size_t)a * ns + x - 1] : 0.0;
+  }
+  for (int q = threadIdx.x; q < nb * k2; q += blockDim.x) {
+    const int b = q / k2, x = cv + q % k2;
+    w2[q] = x <= ns ? P2[(size_t)b * ns + x - 1] : 0.0;
+  }
+  __syncthreads();
+  for (int q = threadIdx.x; q < nb * k1; q += blockDim.x) {
+    const int b = q / k1, h1 = q % k1 + 1;
+    double s1 = 0.0, s2 = 0.0;
+    for (int h2 = 1; h2 <= k2; h2++) {
+      const size_t o = (size_t)pidx(ed, h1, h2) + (size_t)kk * (cv - 1);
+      const double p = w2[b * k2 + h2 - 1];
+      s1 = fma(M1[o], p, s1);
+      if (M2) s2 = fma(M2[o], p, s2);
+    }
+    t1[q] = s1;
+    t2[q] = s2;
+  }
+  __syncthreads();
+  for (int q = threadIdx.x; q < nb * nb; q += blockDim.x) {
+    const int a = q / nb, b = q % nb;
+    double s1 = 0.0, s2 = 0.0;
+    for (int h = 0; h < k1; h++) {
+      const double p = w1[a * k1 + h];
+      s1 = fma(p, t1[b * k1 + h], s1);
+      s2 = fma(p, t2[b * k1 + h], s2);
+    }
+    S1[(size_t)q * nv + cv - 1] = s1;
+    if (S2) S2[(size_t)q * nv + cv - 1] = s2;
+  }
+}
+
+// (2) exclusive suffix (sum over later cells) or prefix sums per pair
+__global__ void k_pair_scan(int nv, int npair, double *S, int suffix) {
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= npair) return;
+  double *s = S + (size_t)p * nv;
+  double acc = 0.0;
+  if (suffix) {
+    for (int iv = nv - 1; iv >= 0; iv--) {
+      double v = s[iv];
+      s[iv] = acc;
+      acc += v;
+    }
+  } else {
+    for (int iv = 0; iv < nv; iv++) {
+      double v = s[iv];
+      s[iv] = acc;
+      acc += v;
+    }
+  }
+}
+
+// (3) diagonal cells, one block per cell cv:
+//   Dq[ph][ab][q(po)] = sum_{g1,g2} R(po; g1,g2; cv) P1(a, cv+g1-1) P2(b, cv+g2-1)
+// with po an output pair of the cell, q its position in the ns x ncol result
+// and ph = (cv-1) mod 9: a cell touches outputs with first index in
+// [cv, cv+8], so cells of one phase never share an output.  Two stages:
+// H(po, g1, b) = sum_g2 R P2, then sum_g1 P1 H.
+__global__ void __launch_bounds__(256) k_pair_diag(int ns, int ks, int kk, int nb, int icv,
+                                                   char sym, PairSpec eo, PairSpec ed,
+                                                   const double *__restrict__ rkd,
+                                                   const double *__restrict__ P1,
+                                                   const double *__restrict__ P2,
+                                                   double *__restrict__ Dq, size_t per) {
+  extern __shared__ double sm[];
+  const int cv = blockIdx.x + 1, k1 = ed.k1, k2 = ed.k2, kd = k1 * k2;
   const int npo = eo.sym ? eo.k1 * (eo.k1 + 1) / 2 : eo.k1 * eo.k2;
-  double *rw = rho_w + 81 * warp;
-  for (int ph = 0; ph < 9; ph++) {
-    for (int cv = ph + 1 + 9 * warp; cv <= nv; cv += 9 * nwarp) {
-      // stage the cell's density pairs, one pair per lane
-      const int npd = ed.sym ? ed.k1 * (ed.k1 + 1) / 2 : ed.k1 * ed.k2;
-      for (int pd = lane; pd < npd; pd += 32) {
-        int g1, g2;
-        if (ed.sym) {
-          int r = pd, row = 0;
-          while (r >= ed.k1 - row) {
-            r -= ed.k1 - row;
-            row++;
-          }
-          g1 = row + 1;
-          g2 = row + 1 + r;
-        } else {
-          g1 = pd / ed.k2 + 1;
-          g2 = pd % ed.k2 + 1;
-        }
-        rw[pd] = rho(cv + g1 - 1, cv + g2 - 1);
+  const size_t npair = (size_t)nb * nb;
+  double *w1 = sm, *w2 = w1 + nb * k1, *Rt = w2 + nb * k2;
+  double *H = Rt + (size_t)npo * kd;
+  int *poq = (int *)(H + (size_t)npo * k1 * PBC);
+  for (int q = threadIdx.x; q < nb * k1; q += blockDim.x) {
+    const int a = q / k1, x = cv + q % k1;
+    w1[q] = x <= ns ? P1[(size_t)a * ns + x - 1] : 0.0;
+  }
+  for (int q = threadIdx.x; q < nb * k2; q += blockDim.x) {
+    const int b = q / k2, x = cv + q % k2;
+    w2[q] = x <= ns ? P2[(size_t)b * ns + x - 1] : 0.0;
+  }
+  for (int po = threadIdx.x; po < npo; po += blockDim.x) {
+    int h1, h2;
+    if (eo.sym) {
+      int r = po, row = 0;
+      while (r >= eo.k1 - row) {
+        r -= eo.k1 - row;
+        row++;
       }
-      __syncwarp();
-      for (int po = lane; po < npo; po += 32) {
-        int h1, h2;
-        if (eo.sym) {
-          int r = po, row = 0;
-          while (r >= eo.k1 - row) {
-            r -= eo.k1 - row;
-            row++;
-          }
-          h1 = row + 1;
-          h2 = row + 1 + r;
-        } else {
-          h1 = po / eo.k2 + 1;
-          h2 = po % eo.k2 + 1;
-        }
-        int f = cv + h1 - 1, s2 = cv + h2 - 1;
-        if (f > ns || s2 > ns) continue;
-        double acc = 0.0;
-        if (icv == 1) {
-          const double *rk = rkd + (size_t)po + (size_t)kk * (size_t)kk * (cv - 1);
-          for (int pd = 0; pd < npd; pd++) acc = fma(rk[(size_t)kk * pd], rw[pd], acc);
-        } else {
-          const double *rk = rkd + (size_t)kk * ((size_t)po + (size_t)kk * (cv - 1));
-          for (int pd = 0; pd < npd; pd++) acc = fma(rk[pd], rw[pd], acc);
-        }
-        int q = sym == 's' ? (f - 1) + ns * (s2 - f) : (f - 1) + ns * (s2 - f + ks - 1);
-        out[q] += acc;
-      }
-      __syncwarp();
+      h1 = row + 1;
+      h2 = row + 1 + r;
+    } else {
+      h1 = po / eo.k2 + 1;
+      h2 = po % eo.k2 + 1;
+    }
+    const int f = cv + h1 - 1, s2 = cv + h2 - 1;
+    poq[po] = (f > ns || s2 > ns) ? -1
+              : (sym == 's' ? (f - 1) + ns * (s2 - f) : (f - 1) + ns * (s2 - f + ks - 1));
+  }
+  const double *rc = rkd + (size_t)kk * kk * (cv - 1);  // rkd(e1 pair, e2 pair; cv)
+  for (int q = threadIdx.x; q < npo * kd; q += blockDim.x) {
+    const int po = q / kd, r = q % kd, g1 = r / k2 + 1, g2 = r % k2 + 1;
+    const int pd = pidx(ed, g1, g2);
+    Rt[q] = icv == 1 ? rc[(size_t)po + (size_t)kk * pd] : rc[(size_t)pd + (size_t)kk * po];
+  }
+  __syncthreads();
+  const int ph = (cv - 1) % FAR;
+  for (int b0 = 0; b0 < nb; b0 += PBC) {
+    const int bc = min(PBC, nb - b0);
+    for (int q = threadIdx.x; q < npo * k1 * bc; q += blockDim.x) {
+      const int bb = q % bc, r = q / bc, g1 = r % k1, po = r / k1;
+      const double *rt = Rt + (size_t)po * kd + (size_t)g1 * k2;
+      const double *p = w2 + (size_t)(b0 + bb) * k2;
+      double s = 0.0;
+      for (int g2 = 0; g2 < k2; g2++) s = fma(rt[g2], p[g2], s);
+      H[((size_t)po * k1 + g1) * PBC + bb] = s;
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < npo * nb * bc; q += blockDim.x) {
+      const int bb = q % bc, r = q / bc, a = r % nb, po = r / nb;
+      const int qp = poq[po];
+      if (qp < 0) continue;
+      const double *p = w1 + (size_t)a * k1;
+      const double *h = H + (size_t)po * k1 * PBC + bb;
+      double s = 0.0;
+      for (int g1 = 0; g1 < k1; g1++) s = fma(p[g1], h[(size_t)g1 * PBC], s);
+      Dq[((size_t)ph * npair + (size_t)a * nb + b0 + bb) * per + qp] = s;
     }
     __syncthreads();
   }
-  for (int q = threadIdx.x; q < ns * ncol; q += blockDim.x) Y[(size_t)slot * per + q] = out[q];
 }
 
-__global__ void k_check_bound(int n, const int *k2, const int *k3, const int *bmap, int *err) {
-  int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= n) return;
-  if (bmap[k2[e] - 1] < 0 || bmap[k3[e] - 1] < 0) atomicExch(err, 3);
+// (4) the pair potential: separable terms from the scanned cell sums plus the
+// diagonal-cell parts, cells in order (the output loop of k_direct)
+__global__ void k_pair_direct_final(int ns, int ks, int nv, int kk, int nb, int icv, char sym,
+                                    PairSpec eo, const double *lo1, const double *hi1,
+                                    const double *hi2, const double *SA, const double *SB,
+                                    const double *Dq, double *K, size_t per) {
+  const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= per) return;
+  const int pair = blockIdx.y;
+  const size_t npair = (size_t)nb * nb;
+  const int f = (int)(t % ns) + 1, col = (int)(t / ns) + 1;
+  const int s2 = sym == 's' ? f + col - 1 : f + col - ks;
+  double acc = 0.0;
+  if (s2 >= 1 && s2 <= ns) {
+    const int lo = max(max(1, f - eo.k1 + 1), s2 - eo.k2 + 1), hi = min(min(nv, f), s2);
+    const double *sa = SA + (size_t)pair * nv;
+    const double *sb = SB ? SB + (size_t)pair * nv : nullptr;
+    for (int cv = lo; cv <= hi; cv++) {
+      const size_t o = (size_t)pidx(eo, f - cv + 1, s2 - cv + 1) + (size_t)kk * (cv - 1);
+      if (icv == 1) {
+        acc = fma(lo1[o], sa[cv - 1], acc);
+        if (sb) acc = fma(hi1[o], sb[cv - 1], acc);
+      } else {
+        acc = fma(hi2[o], sa[cv - 1], acc);
+      }
+      acc += Dq[((size_t)((cv - 1) % FAR) * npair + pair) * per + t];
+    }
+  }
+  K[(size_t)pair * per + t] = acc;
+}
+
+// ---------------------------------------------------------------------------
+// near band of the exchange results: Y(x, x+d) = sum_e c_e Kb(pair_e; x, d)
+__global__ void k_band_sum(int ns, const int *members, const SegInfo *info, const int *pairs,
+                           const double *cd, const double *Kb, double *Y, size_t per) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ns * NDB) return;
+  const int slot = blockIdx.y;
+  const int x = t % ns + 1, y = x + t / ns - BAND;
+  if (y < 1 || y > ns) return;
+  const SegInfo si = info[members[slot]];
+  const size_t kper = (size_t)ns * NDB;
+  double acc = 0.0;
+  for (int e = si.start; e < si.end; e++) acc = fma(cd[e], Kb[(size_t)pairs[e] * kper + t], acc);
+  Y[(size_t)slot * per + (size_t)(x - 1) + (size_t)ns * (y - 1)] = acc;
+}
+
+// Exchange scatter (UPDATE_HS, updates.f90:110-179): one 32x32 tile of one
+// quadrant of an owner's block; contributions in the reference's order
+// (atype-major, owner then partner), transposed reads staged through shared
+// memory so that every global access is coalesced.  Without a lower far
+// field (S^k) the region x - y >= 9 of every result is zero.
+__global__ void __launch_bounds__(256) k_scatter_x(int ns, QuadSpec sp, int nm,
+                                                   const int *members, const int *own_slots,
+                                                   const SegInfo *info, const double *Y,
+                                                   int lower, double *hch) {
+  __shared__ double tt[32][33];
+  const int ms = 2 * ns, nt = (ns + 31) / 32;
+  const int quad = blockIdx.x / (nt * nt), tile = blockIdx.x % (nt * nt);
+  const int qr = quad % 2 + 1, qc = quad / 2 + 1;
+  const int r0 = (tile % nt) * 32, c0 = (tile / nt) * 32;
+  const int oslot = own_slots[blockIdx.y];
+  const SegInfo si = info[members[oslot]];
+  if (si.blk < 1) return;
+  const int pslot = si.partner >= 0 ? oslot + 1 : -1;
+  const int tx = threadIdx.x % 32, ty = threadIdx.x / 32;
+  const size_t per = (size_t)ns * ns;
+  double *hb = hch + (size_t)(si.blk - 1) * ms * ms + (size_t)(qr - 1) * ns + (size_t)ms * (qc - 1) * ns;
+  double v[4] = {0.0, 0.0, 0.0, 0.0};
+  bool touched = false;
+  for (int a = 0; a < sp.na; a++) {
+    for (int pass = 0; pass < 2; pass++) {
+      const int slot = pass == 0 ? oslot : pslot;
+      if (slot < 0) break;
+      const SegInfo sj = info[members[slot]];
+      const double *d = Y + ((size_t)a * nm + slot) * per;
+      const int ii = sp.ii[a], jj = sp.jj[a];
+      const bool eq = sj.ich == sj.jch;
+      const bool dir = (sj.ich > sj.jch || eq) && qr == ii && qc == jj;
+      const bool tra = (sj.ich < sj.jch && qr == ii && qc == jj) || (eq && qr == jj && qc == ii);
+      if (!dir && !tra) continue;
+      if (!touched) {
+        touched = true;
+        for (int k = 0; k < 4; k++) {
+          const int lr = r0 + tx, lc = c0 + ty + 8 * k;
+          if (lr < ns && lc < ns) v[k] = hb[(size_t)lr + (size_t)ms * lc];
+        }
+      }
+      if (dir) {
+        for (int k = 0; k < 4; k++) {
+          const int lr = r0 + tx, lc = c0 + ty + 8 * k;
+          if (lr >= ns || lc >= ns) continue;
+          const double y = (lower || lr - lc < FAR) ? d[(size_t)lr + (size_t)ns * lc] : 0.0;
+          v[k] = v[k] + (eq ? y / 2.0 : y);
+        }
+      }
+      if (tra) {
+        __syncthreads();
+        for (int k = 0; k < 4; k++) {
+          const int x = c0 + tx, y = r0 + ty + 8 * k;  // y(x, y) = element (lc, lr)
+          tt[ty + 8 * k][tx] =
+              (x < ns && y < ns && (lower || x - y < FAR)) ? d[(size_t)x + (size_t)ns * y] : 0.0;
+        }
+        __syncthreads();
+        for (int k = 0; k < 4; k++) {
+          const int lr = r0 + tx, lc = c0 + ty + 8 * k;
+          if (lr >= ns || lc >= ns) continue;
+          const double y = tt[tx][ty + 8 * k];
+          v[k] = v[k] + (eq ? y / 2.0 : y);
+        }
+      }
+    }
+  }
+  if (!touched) return;
+  for (int k = 0; k < 4; k++) {
+    const int lr = r0 + tx, lc = c0 + ty + 8 * k;
+    if (lr < ns && lc < ns) hb[(size_t)lr + (size_t)ms * lc] = v[k];
+  }
+}
+
+// position of element (i, j) (1-based) of the band result y in its ns x ncol
+// storage, or -1 where the storage holds no element (yval of assemble.cu)
+__device__ __forceinline__ int band_pos(int ns, int ks, char sym, int i, int j) {
+  if (sym == 's') {
+    const int lo = min(i, j), dl = abs(i - j);
+    return dl >= ks ? -1 : (lo - 1) + ns * dl;
+  }
+  const int jp = j - i + ks;
+  return (jp < 1 || jp > 2 * ks - 1) ? -1 : (i - 1) + ns * (jp - 1);
+}
+
+// Direct scatter: every band element of the four quadrants of an owner's
+// block; each contribution is formed from the pair potentials and the
+// segment's coefficients where it is added.
+__global__ void k_scatter_dp(int ns, int ks, char sym, QuadSpec sp, KdSet kd,
+                             const int *members, const int *own_slots, const SegInfo *info,
+                             const int *pairs, const double *cd, double *hch) {
+  const int ms = 2 * ns, nd = 2 * ks - 1;
+  const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= (size_t)4 * ns * nd) return;
+  const int oslot = own_slots[blockIdx.y];
+  const SegInfo si = info[members[oslot]];
+  if (si.blk < 1) return;
+  const int pslot = si.partner >= 0 ? oslot + 1 : -1;
+  const int quad = (int)(q / ((size_t)ns * nd));
+  const int rem = (int)(q % ((size_t)ns * nd));
+  const int lr = rem % ns, lc = lr + rem / ns - (ks - 1);
+  if (lc < 0 || lc >= ns) return;
+  const int qr = (quad & 1) + 1, qc = (quad >> 1) + 1;
+  const size_t per = (size_t)ns * (sym == 's' ? ks : nd);
+  double *h = hch + (size_t)(si.blk - 1) * ms * ms + (size_t)((qr - 1) * ns + lr) +
+              (size_t)ms * ((qc - 1) * ns + lc);
+  bool touched = false;
+  double val = 0.0;
+  auto ysum = [&](const double *K, const SegInfo &sj, int i, int j) -> double {
+    const int p = band_pos(ns, ks, sym, i, j);
+    if (p < 0) return 0.0;
+    double acc = 0.0;
+    for (int e = sj.start; e < sj.end; e++) acc = fma(cd[e], K[(size_t)pairs[e] * per + p], acc);
+    return acc;
+  };
+  for (int a = 0; a < sp.na; a++) {
+    for (int pass = 0; pass < 2; pass++) {
+      const int slot = pass == 0 ? oslot : pslot;
+      if (slot < 0) break;
+      const SegInfo sj = info[members[slot]];
+      const int ii = sp.ii[a], jj = sp.jj[a];
+      if (sj.ich != sj.jch) {
+        if (qr == ii && qc == jj) {
+          if (!touched) { val = *h; touched = true; }
+          val = val + (sj.ich > sj.jch ? ysum(kd.K[a], sj, lr + 1, lc + 1)
+                                       : ysum(kd.K[a], sj, lc + 1, lr + 1));
+        }
+      } else {
+        if (qr == ii && qc == jj) {
+          if (!touched) { val = *h; touched = true; }
+          val = val + ysum(kd.K[a], sj, lr + 1, lc + 1) / 2.0;
+        }
+        if (qr == jj && qc == ii) {
+          if (!touched) { val = *h; touched = true; }
+          val = val + ysum(kd.K[a], sj, lc + 1, lr + 1) / 2.0;
+        }
+      }
+    }
+  }
+  if (touched) *h = val;
 }
 
 }  // namespace
@@ -448,10 +668,13 @@ int ensure_fscratch(dbsrg_ctx *c, size_t bytes) {
   return DBSRG_OK;
 }
 
-int check_bound_orbitals(dbsrg_ctx *c, int n, const int *k2, const int *k3, int *derr) {
+int pair_index(dbsrg_ctx *c, int n, const int *k2, const int *k3, int *pairs, int *derr) {
   if (n <= 0) return DBSRG_OK;
-  DBSRG_RUN(c, "k_check_bound",
-            k_check_bound<<<(n + 255) / 256, 256, 0, c->stream>>>(n, k2, k3, c->bmap, derr));
+  if (c->nbound < 1 || c->nbound > NB_MAX)
+    return set_err(c, DBSRG_EINVAL, "factored contraction: 1..64 bound orbitals (ipbs = 0)");
+  DBSRG_RUN(c, "k_pair_index",
+            k_pair_index<<<(n + 255) / 256, 256, 0, c->stream>>>(n, k2, k3, c->bmap, c->nbound,
+                                                                 pairs, derr));
   return DBSRG_OK;
 }
 
@@ -502,19 +725,166 @@ static int get_farfield(dbsrg_ctx *c, int family, int type, int k, int cs, const
   return DBSRG_OK;
 }
 
+// bound-orbital rows of both components, built once per orbital set
+static int ensure_brows(dbsrg_ctx *c) {
+  if (c->brows) return DBSRG_OK;
+  const int ns = c->g.ns, nb = c->nbound;
+  const size_t m = (size_t)ns * nb;
+  DBSRG_TRY(c, cudaMalloc((void **)&c->brows, 2 * m * sizeof(double)));
+  for (int comp = 1; comp <= 2; comp++)
+    DBSRG_RUN(c, "k_bound_rows",
+              k_bound_rows<<<(unsigned)((m + 255) / 256), 256, 0, c->stream>>>(
+                  ns, nb, c->b2o, c->pq, comp, c->brows + (size_t)(comp - 1) * m));
+  return DBSRG_OK;
+}
+
+static long long pairpot_key(int kind, int family, int type, int k, int icv, int jp1, int jp2) {
+  return (long long)kind | (long long)family << 1 | (long long)type << 2 | (long long)icv << 5 |
+         (long long)jp1 << 8 | (long long)jp2 << 10 | (long long)k << 12;
+}
+
+static int set_smem(dbsrg_ctx *c, const void *fn, size_t smem) {
+  if (smem > 220 * 1024) return set_err(c, DBSRG_EINVAL, "pair potentials: too many bound orbitals");
+  if (smem > 48 * 1024)
+    DBSRG_TRY(c, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  return DBSRG_OK;
+}
+
+// direct pair potentials of (family, type, k, case icv) with density
+// components jp1/jp2: Kd[pair][ns*ncol], cached
+static int get_pairpot_direct(dbsrg_ctx *c, int family, int type, int k, int icv, int jp1,
+                              int jp2, const double **out) {
+  const long long key = pairpot_key(0, family, type, k, icv, jp1, jp2);
+  auto it = c->ppot.find(key);
+  if (it != c->ppot.end()) {
+    *out = it->second;
+    return DBSRG_OK;
+  }
+  const DeviceGrid &g = c->g;
+  const int ns = g.ns, ks = g.ks, nv = g.nv, kk = ks * ks, nb = c->nbound;
+  const size_t npair = (size_t)nb * nb;
+  const char sym = family == 0 ? 's' : 'n';
+  const size_t per = (size_t)ns * (sym == 's' ? ks : 2 * ks - 1);
+  int rc;
+  const CellData *cd;
+  if ((rc = get_celldata(c, family, type, k, &cd))) return rc;
+  if ((rc = ensure_brows(c))) return rc;
+  TableBases tb = table_bases(g, family, type);
+  const PairSpec eo = icv == 1 ? tb.e1 : tb.e2, ed = icv == 1 ? tb.e2 : tb.e1;
+  const double *P1 = c->brows + (size_t)(jp1 - 1) * nb * ns;
+  const double *P2 = c->brows + (size_t)(jp2 - 1) * nb * ns;
+  const double *M1 = icv == 1 ? cd->hi2 : cd->lo1;
+  const double *M2 = (icv == 1 && family == 0) ? cd->lo2 : nullptr;
+  // scratch: SA, SB (npair x nv), Dq (9 x npair x per)
+  const size_t sbytes = (2 * npair * nv + (size_t)FAR * npair * per) * sizeof(double);
+  if ((rc = ensure_pscratch(c, sbytes))) return rc;
+  double *SA = (double *)c->pscratch, *SB = SA + npair * nv, *Dq = SB + npair * nv;
+  double *K = nullptr;
+  if (cudaMalloc((void **)&K, npair * per * sizeof(double)) != cudaSuccess) {
+    cudaGetLastError();
+    return set_err(c, DBSRG_ENOMEM, "pair potential allocation failed");
+  }
+  c->ppot[key] = K;
+  cudaStream_t st = c->stream;
+  const size_t sm1 = (size_t)nb * (3 * ed.k1 + ed.k2) * sizeof(double);
+  if ((rc = set_smem(c, (const void *)k_pair_cellsum, sm1))) return rc;
+  DBSRG_RUN(c, "k_pair_cellsum",
+            k_pair_cellsum<<<nv, 256, sm1, st>>>(ns, nv, kk, nb, ed, M1, M2, P1, P2, SA,
+                                                 M2 ? SB : nullptr));
+  const unsigned gp = (unsigned)((npair + 127) / 128);
+  DBSRG_RUN(c, "k_pair_scan", k_pair_scan<<<gp, 128, 0, st>>>(nv, (int)npair, SA, icv == 1));
+  if (M2) DBSRG_RUN(c, "k_pair_scan", k_pair_scan<<<gp, 128, 0, st>>>(nv, (int)npair, SB, 0));
+  const int npo = eo.sym ? eo.k1 * (eo.k1 + 1) / 2 : eo.k1 * eo.k2;
+  const size_t sm3 = ((size_t)nb * (ed.k1 + ed.k2) + (size_t)npo * ed.k1 * ed.k2 +
+                      (size_t)npo * ed.k1 * PBC) * sizeof(double) + (size_t)npo * sizeof(int);
+  if ((rc = set_smem(c, (const void *)k_pair_diag, sm3))) return rc;
+  DBSRG_RUN(c, "k_pair_diag",
+            k_pair_diag<<<nv, 256, sm3, st>>>(ns, ks, kk, nb, icv, sym, eo, ed, cd->rkd, P1, P2,
+                                              Dq, per));
+  dim3 gf((unsigned)((per + 255) / 256), (unsigned)npair);
+  DBSRG_RUN(c, "k_pair_direct_final",
+            k_pair_direct_final<<<gf, 256, 0, st>>>(
+                ns, ks, nv, kk, nb, icv, sym, eo, icv == 1 ? cd->lo1 : nullptr,
+                (icv == 1 && family == 0) ? cd->hi1 : nullptr, cd->hi2, SA, M2 ? SB : nullptr, Dq,
+                K, per));
+  *out = K;
+  return DBSRG_OK;
+}
+
+// exchange band pair potentials of (family, type, k, case) with density
+// components jp1/jp2: Kb[pair][ns*17], cached
+static int get_pairpot_band(dbsrg_ctx *c, int family, int type, int k, int cs, int jp1, int jp2,
+                            const double *tab, const double **out) {
+  const long long key = pairpot_key(1, family, type, k, cs, jp1, jp2);
+  auto it = c->ppot.find(key);
+  if (it != c->ppot.end()) {
+    *out = it->second;
+    return DBSRG_OK;
+  }
+  const DeviceGrid &g = c->g;
+  const int ns = g.ns, ks = g.ks, nb = c->nbound;
+  const size_t npair = (size_t)nb * nb, per = (size_t)ns * NDB;
+  int rc;
+  if ((rc = ensure_brows(c))) return rc;
+  double *K = nullptr;
+  if (cudaMalloc((void **)&K, npair * per * sizeof(double)) != cudaSuccess) {
+    cudaGetLastError();
+    return set_err(c, DBSRG_ENOMEM, "pair potential allocation failed");
+  }
+  c->ppot[key] = K;
+  const double *P1 = c->brows + (size_t)(jp1 - 1) * nb * ns;
+  const double *P2 = c->brows + (size_t)(jp2 - 1) * nb * ns;
+  const int W = 2 * ks - 1, WL = PXC + W - 1;
+  const size_t smem = ((size_t)PXC * W * W + 2 * (size_t)nb * WL + (size_t)PXC * W * nb) *
+                      sizeof(double);
+  if ((rc = set_smem(c, (const void *)k_pair_band, smem))) return rc;
+  const int mode = family == 0 ? 0 : (cs == 3 ? 1 : 2);
+  dim3 gb((unsigned)((ns + PXC - 1) / PXC), (unsigned)NDB);
+  DBSRG_RUN(c, "k_pair_band",
+            k_pair_band<<<gb, 256, smem, c->stream>>>(ns, ks, nb, mode, tab, P1, P2, K));
+  *out = K;
+  return DBSRG_OK;
+}
+
+void free_orbital_products(dbsrg_ctx *c) {
+  if (!c->rfar.empty() || !c->sfar.empty() || !c->ppot.empty() || c->brows)
+    cudaStreamSynchronize(c->stream);
+  for (auto &f : c->rfar)
+    if (f.U) cudaFree(f.U);
+  for (auto &f : c->sfar)
+    if (f.U) cudaFree(f.U);
+  c->rfar.clear();
+  c->sfar.clear();
+  for (auto &kv : c->ppot)
+    if (kv.second) cudaFree(kv.second);
+  c->ppot.clear();
+  if (c->brows) cudaFree(c->brows);
+  c->brows = nullptr;
+}
+
 int farfield_tc(dbsrg_ctx *c, int ns, int nb, int nm, const double *U, const double *Ul,
                 const double *Z, const double *Zl, double *Y, size_t per);
 
 int factored_contract(dbsrg_ctx *c, const FactorJob &j) {
   const DeviceGrid &g = c->g;
-  const int ns = g.ns, ks = g.ks, nv = g.nv, kk = ks * ks, nb = c->nbound;
+  const int ns = g.ns, ks = g.ks, nb = c->nbound;
   cudaStream_t st = c->stream;
   int rc;
+  if (nb < 1 || nb > NB_MAX)
+    return set_err(c, DBSRG_EINVAL, "factored contraction: 1..64 bound orbitals (ipbs = 0)");
+  if (ks > FAR) return set_err(c, DBSRG_EINVAL, "factored contraction: spline order above 9");
+  if (j.nown < 1) return DBSRG_OK;
+  QuadSpec qs{};
+  qs.na = j.na;
+  for (int a = 0; a < j.na; a++) {
+    qs.ii[a] = j.ii[a];
+    qs.jj[a] = j.jj[a];
+  }
   if (j.icv >= 3) {
-    if (nb < 1 || nb > NB_MAX) return set_err(c, DBSRG_EINVAL, "factored exchange: 1..64 bound orbitals");
-    size_t xb = (size_t)j.nm * ns * XB_W, zs = (size_t)j.nm * nb * ns;
-    if ((rc = ensure_fscratch(c, (xb + 2 * zs) * sizeof(double)))) return rc;
-    double *Xb = (double *)c->fscratch, *Z = Xb + xb, *Zl = Z + zs;
+    const size_t per = (size_t)ns * ns;
+    size_t zs = (size_t)j.nm * nb * ns;
+    if ((rc = ensure_fscratch(c, 2 * zs * sizeof(double)))) return rc;
+    double *Z = (double *)c->fscratch, *Zl = Z + zs;
     for (int a = 0; a < j.na; a++) {
       const int cs = j.icv;
       const FarField *f;
@@ -523,49 +893,46 @@ int factored_contract(dbsrg_ctx *c, const FactorJob &j) {
       int c1 = cs == 3 ? tb.a2 : tb.a1, c2 = cs == 3 ? tb.b1 : tb.b2;
       if (c1 != j.jp1[a] || c2 != j.jp2[a])
         return set_err(c, DBSRG_EINVAL, "factored exchange: component mismatch");
-      double *Ya = j.Y + (size_t)a * j.nm * j.per;
+      const double *Kb;
+      if ((rc = get_pairpot_band(c, j.family, j.types[a], j.kpol, cs, j.jp1[a], j.jp2[a],
+                                 j.tabs[a], &Kb)))
+        return rc;
+      double *Ya = j.Y + (size_t)a * j.nm * per;
       dim3 gz((unsigned)((ns * nb + 127) / 128), (unsigned)j.nm);
       DBSRG_RUN(c, "k_far_z",
-                k_far_z<<<gz, 128, 0, st>>>(ns, nb, j.nm, j.members, j.info, j.k2, j.k3, j.cd,
-                                            c->bmap, f->V, f->Vl, Z, f->Vl ? Zl : nullptr));
+                k_far_z<<<gz, 128, 0, st>>>(ns, nb, j.members, j.info, j.pairs, j.cd, f->V,
+                                            f->Vl, Z, f->Vl ? Zl : nullptr));
       if (j.split) {
-        if ((rc = farfield_tc(c, ns, nb, j.nm, f->U, f->Ul, Z, f->Vl ? Zl : nullptr, Ya, j.per)))
+        if ((rc = farfield_tc(c, ns, nb, j.nm, f->U, f->Ul, Z, f->Vl ? Zl : nullptr, Ya, per)))
           return rc;
       } else {
         dim3 gf((unsigned)((ns + 31) / 32), (unsigned)((ns + 31) / 32), (unsigned)j.nm);
         DBSRG_RUN(c, "k_far_field",
                   k_far_field<<<gf, 256, 0, st>>>(ns, nb, f->U, f->Ul, Z, f->Vl ? Zl : nullptr, Ya,
-                                                  j.per));
+                                                  per));
       }
-      dim3 gb((unsigned)((ns * XB_W + 255) / 256), (unsigned)j.nm);
-      DBSRG_RUN(c, "k_density_band",
-                k_density_band<<<gb, 256, 0, st>>>(ns, j.nm, j.members, j.info, j.k2, j.k3, j.cd,
-                                                   c->pq, j.jp1[a], j.jp2[a], Xb));
-      int mode = j.family == 0 ? 0 : (cs == 3 ? 1 : 2);
-      dim3 gx((unsigned)((ns * (2 * FAR - 1) + 255) / 256), (unsigned)j.nm);
-      DBSRG_RUN(c, "k_band_exchange",
-                k_band_exchange<<<gx, 256, 0, st>>>(ns, ks, mode, j.tabs[a], Xb, Ya, j.per));
+      dim3 gb((unsigned)((ns * NDB + 255) / 256), (unsigned)j.nm);
+      DBSRG_RUN(c, "k_band_sum",
+                k_band_sum<<<gb, 256, 0, st>>>(ns, j.members, j.info, j.pairs, j.cd, Kb, Ya, per));
     }
+    const int nt = (ns + 31) / 32;
+    dim3 gs((unsigned)(4 * nt * nt), (unsigned)j.nown);
+    DBSRG_RUN(c, "k_scatter_x",
+              k_scatter_x<<<gs, 256, 0, st>>>(ns, qs, j.nm, j.members, j.own, j.info, j.Y,
+                                              j.family == 0 ? 1 : 0, c->hch));
     return DBSRG_OK;
   }
   // direct
+  KdSet kd{};
   for (int a = 0; a < j.na; a++) {
-    const CellData *cd;
-    if ((rc = get_celldata(c, j.family, j.types[a], j.kpol, &cd))) return rc;
-    TableBases tb = table_bases(g, j.family, j.types[a]);
-    const double *Xa = j.X + (size_t)a * j.nm * j.per;
-    double *Ya = j.Y + (size_t)a * j.nm * j.per;
-    const int ncol = j.sym == 's' ? ks : 2 * ks - 1;
-    size_t smem = (2 * (size_t)nv + (size_t)ns * ncol + 81 * 8) * sizeof(double);
-    if (smem > 200 * 1024) return set_err(c, DBSRG_EINVAL, "direct contraction: ns too large");
-    if (smem > 48 * 1024)
-      DBSRG_TRY(c, cudaFuncSetAttribute(k_direct, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)smem));
-    DBSRG_RUN(c, "k_direct",
-              k_direct<<<j.nm, 256, smem, st>>>(ns, ks, nv, kk, j.icv, j.sym, tb.e1, tb.e2,
-                                                cd->lo1, j.family == 0 ? cd->hi1 : nullptr,
-                                                j.family == 0 ? cd->lo2 : nullptr, cd->hi2,
-                                                cd->rkd, Xa, Ya, j.per));
+    if ((rc = get_pairpot_direct(c, j.family, j.types[a], j.kpol, j.icv, j.jp1[a], j.jp2[a],
+                                 &kd.K[a])))
+      return rc;
   }
+  const size_t space = (size_t)4 * ns * (2 * ks - 1);
+  dim3 gs((unsigned)((space + 255) / 256), (unsigned)j.nown);
+  DBSRG_RUN(c, "k_scatter_dp",
+            k_scatter_dp<<<gs, 256, 0, st>>>(ns, ks, j.sym, qs, kd, j.members, j.own, j.info,
+                                             j.pairs, j.cd, c->hch));
   return DBSRG_OK;
 }

@@ -301,12 +301,6 @@ __global__ void __launch_bounds__(128) k_far_tc(int ns, int nm, int mode,
                  "r"(TMEM_COLS));
 }
 
-__global__ void k_zero_lower(int ns, double *Y, size_t per) {
-  int x = blockIdx.x * 16 + threadIdx.x, y = blockIdx.y * 16 + threadIdx.y;
-  if (x >= ns || y >= ns || x - y < FARD) return;
-  Y[(size_t)blockIdx.z * per + (size_t)x + (size_t)ns * y] = 0.0;
-}
-
 }  // namespace
 
 // Far field of one chunk of segments on the tensor cores.  U/Ul are shared
@@ -334,10 +328,6 @@ int farfield_tc(dbsrg_ctx *c, int ns, int nb, int nm, const double *U, const dou
   const size_t smem = (size_t)TS * (A_SLICE + B_SLICE) * sizeof(__nv_bfloat16);
   DBSRG_TRY(c, cudaFuncSetAttribute(k_far_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)smem));
-  if (!Ul) {  // S^k tables: the lower far field is zero
-    dim3 gz((unsigned)((ns + 15) / 16), (unsigned)((ns + 15) / 16), (unsigned)nm);
-    DBSRG_RUN(c, "k_zero_lower", k_zero_lower<<<gz, dim3(16, 16), 0, st>>>(ns, Y, per));
-  }
   for (int mode = 0; mode < (Ul ? 2 : 1); mode++) {
     const double *Um = mode == 0 ? U : Ul;
     const double *Zm = mode == 0 ? Z : Zl;

@@ -15,6 +15,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -77,6 +78,12 @@ struct dbsrg_ctx {
   std::vector<CellData> rcell, scell;
   // far-field vectors, indexed [(k*4+type)*2+case34] (R) / [(k*2+type)*2+case34] (S)
   std::vector<FarField> rfar, sfar;
+  // orbital-pair potentials of the factored contraction (direct band results
+  // and exchange band results per ordered bound-orbital pair), keyed by
+  // pairpot_key(); they depend on the tables and the orbitals
+  std::map<long long, double *> ppot;
+  // bound-orbital rows brows[(comp-1)*nbound*ns + a*ns + x] = pq(x+1, comp, b2o[a])
+  double *brows = nullptr;
   // bound-orbital map: bmap[orb-1] = dense bound index or -1; nbound
   int nbound = 0;
   int *bmap = nullptr;  // (nbf)
@@ -95,6 +102,8 @@ struct dbsrg_ctx {
   size_t fscratch_bytes = 0;
   void *tcscratch = nullptr;  // tensor-core far field (digit slices, scales)
   size_t tcscratch_bytes = 0;
+  void *pscratch = nullptr;   // pair-potential construction (cell sums, cell parts)
+  size_t pscratch_bytes = 0;
   // pinned staging for host lists
   void *pinned = nullptr;
   size_t pinned_bytes = 0;
@@ -161,7 +170,11 @@ int ensure_scratch(dbsrg_ctx *c, size_t bytes);
 int ensure_scratch2(dbsrg_ctx *c, size_t bytes);
 int ensure_tscratch(dbsrg_ctx *c, size_t bytes);
 int ensure_tcscratch(dbsrg_ctx *c, size_t bytes);
+int ensure_pscratch(dbsrg_ctx *c, size_t bytes);
 int ensure_pinned(dbsrg_ctx *c, size_t bytes);
+// frees the far-field vectors, pair potentials and bound rows (they depend
+// on the orbitals and the tables)
+void free_orbital_products(dbsrg_ctx *c);
 
 // ---- tables.cu ------------------------------------------------------------
 int build_grid(dbsrg_ctx *c, const double *t_host_or_dev);
@@ -184,28 +197,32 @@ int update_hx(dbsrg_ctx *c, int ich, int jch, const double *d, double cc);
 
 // ---- factor.cu ------------------------------------------------------------
 int ensure_fscratch(dbsrg_ctx *c, size_t bytes);
-// One chunk of segments of one list through the factored contraction.
+// One chunk of segments of one list through the factored contraction,
+// including its scatter into hch.
 struct FactorJob {
   int family;        // 0 R^k, 1 S^k
   int kpol;
   int icv;           // convol case 1..4
-  char sym;          // storage of densities/results: 's', 'n', 'x'
+  char sym;          // storage of the results: 's', 'n' (band) or 'x' (full)
   int na;            // PQ types (atypes) processed, in order
   int types[4];      // table type of each atype
   int jp1[4], jp2[4];
-  const double *tabs[4];
+  int ii[4], jj[4];  // target quadrant of each atype (UPDATE_HS)
+  const double *tabs[4];  // band tables of the exchange cases
   int nm;            // member segments of the chunk
   const int *members;
+  int nown;          // owner segments of the chunk
+  const int *own;    // member slot of each owner
   const SegInfo *info;
   const int *k2, *k3;
+  const int *pairs;  // ordered bound-orbital pair index of every entry
   const double *cd;
-  const double *X;   // direct cases: accumulated densities [a][slot][per]
-  double *Y;         // results [a][slot][per]
-  size_t per;        // ns * ncol
+  double *Y;         // exchange results [a][slot][ns*ns]
   bool split;        // far field on the tensor cores (split BF16)
 };
 int factored_contract(dbsrg_ctx *c, const FactorJob &job);
-int check_bound_orbitals(dbsrg_ctx *c, int n, const int *k2, const int *k3, int *derr);
+// pairs[e] = bmap[K2]*nbound + bmap[K3]; sets *derr when an orbital is not bound
+int pair_index(dbsrg_ctx *c, int n, const int *k2, const int *k3, int *pairs, int *derr);
 
 // ---- device helpers ---------------------------------------------------------
 // Values of the kx B-splines that are nonzero on the interval starting at
