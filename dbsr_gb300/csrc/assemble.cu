@@ -452,14 +452,6 @@ __global__ void k_acf(int nseg_owner, const int *owners, const SegInfo *info, in
   }
 }
 
-__global__ void k_owner_list(int nseg, const SegInfo *info, int *owners, int *nown) {
-  // single thread: compact the owner segments in list order
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  int c = 0;
-  for (int s = 0; s < nseg; s++)
-    if (info[s].owner) owners[c++] = s;
-  *nown = c;
-}
 
 // ---------------------------------------------------------------------------
 // O_data itype 3 (<i|.><.|j>, O_data.f90:50-61) with UPDATE_HW
@@ -481,7 +473,8 @@ __global__ void k_vch(int ns, int nbf, const double *fpbs, const double *fqbs,
 // group entries by block, keeping list order (single thread, counting sort)
 __global__ void k_group_entries(int n, const int *k1, const int *k2, const double *cd,
                                 const int *ipbs, int nbf, const int *icc, int nch, int iicc,
-                                int *bcount, int *bstart, int *order, int *eblk, int *err) {
+                                int *bcount, int *bstart, int *order, int *eblk, int *tlist,
+                                int *ntouched, int *err) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   for (int b = 0; b <= iicc; b++) bcount[b] = 0;
   for (int e = 0; e < n; e++) {
@@ -496,12 +489,14 @@ __global__ void k_group_entries(int n, const int *k1, const int *k2, const doubl
     eblk[e] = b;
     bcount[b]++;
   }
-  int acc = 0;
+  int acc = 0, nt = 0;
   for (int b = 0; b <= iicc; b++) {
     bstart[b] = acc;
     acc += bcount[b];
+    if (b > 0 && bcount[b] > 0) tlist[nt++] = b;
     bcount[b] = 0;
   }
+  *ntouched = nt;
   bstart[iicc + 1] = acc;
   for (int e = 0; e < n; e++) {
     int b = eblk[e];
@@ -509,11 +504,11 @@ __global__ void k_group_entries(int n, const int *k1, const int *k2, const doubl
   }
 }
 
-__global__ void k_overlap_update(int ns, int iicc, const int *bstart, const int *order,
+__global__ void k_overlap_update(int ns, const int *tlist, const int *bstart, const int *order,
                                  const int *k1, const int *k2, const double *cd,
                                  const int *ipbs, const double *vch, double *hch) {
   const int ms = 2 * ns;
-  int b = blockIdx.y + 1;
+  int b = tlist[blockIdx.y];
   int e0 = bstart[b], e1 = bstart[b + 1];
   if (e0 == e1) return;
   size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -600,7 +595,8 @@ int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const 
   const size_t ibytes = sizeof(int) * (size_t)n, dbytes = sizeof(double) * (size_t)n;
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
   size_t tot = 8 * al(ibytes) + 2 * al(dbytes) + al(sizeof(int) * (n + 2)) + al(64) +
-               al(sizeof(SegInfo) * (size_t)(n + 1)) + 3 * al(sizeof(int) * (size_t)(n + 1));
+               al(sizeof(SegInfo) * (size_t)(n + 1)) + al(sizeof(int) * (size_t)(n + 1)) +
+               al(sizeof(int) * (size_t)(6 * (n + 1)));
   if ((rc = ensure_scratch2(c, tot))) return rc;
   char *base = (char *)c->scratch2;
   auto take = [&](size_t bytes) {
@@ -615,10 +611,12 @@ int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const 
   double *lcd = (double *)take(dbytes);
   int *lpair = (int *)take(ibytes);  // factored path: bound-orbital pair of each entry
   int *seg_start = (int *)take(sizeof(int) * (size_t)(n + 2));
-  int *dscal = (int *)take(64);  // [0]=nseg [1]=err [2]=nown
+  int *dscal = (int *)take(64);  // [0]=nseg [1]=err
   SegInfo *info = (SegInfo *)take(sizeof(SegInfo) * (size_t)(n + 1));
   int *owners = (int *)take(sizeof(int) * (size_t)(n + 1));
-  int *members = (int *)take(sizeof(int) * (size_t)(2 * (n + 1)));  // members + owner slots
+  // per chunk: member segment ids, owner slots and (split exchange) the
+  // (owner slot, quadrant) codes -- at most 6 ints per segment
+  int *members = (int *)take(sizeof(int) * (size_t)(6 * (n + 1)));
   if ((rc = copy_in(c, dk1, k1, ibytes))) return rc;
   if ((rc = copy_in(c, dk2, k2, ibytes))) return rc;
   if ((rc = copy_in(c, dk3, k3, ibytes))) return rc;
@@ -632,20 +630,32 @@ int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const 
   if (icase == 0) {
     if (itype != 3) return set_err(c, DBSRG_EINVAL, "O_data: only itype 3 is supported");
     size_t vbytes = sizeof(double) * (size_t)ms * c->nbf;
-    rc = ensure_scratch(c, vbytes + sizeof(int) * ((size_t)2 * n + 2 * (c->iicc + 2)) + 1024);
+    rc = ensure_scratch(c, vbytes + sizeof(int) * ((size_t)2 * n + 3 * (c->iicc + 2)) + 1024);
     if (rc) return rc;
     double *vch = (double *)c->scratch;
     int *bcount = (int *)(vch + (size_t)ms * c->nbf);
     int *bstart = bcount + (c->iicc + 2);
-    int *order = bstart + (c->iicc + 2);
+    int *tlist = bstart + (c->iicc + 2);  // blocks with entries
+    int *order = tlist + (c->iicc + 2);
     int *eblk = order + n;
     DBSRG_RUN(c, "k_vch", k_vch<<<(2 * ns * c->nbf + 255) / 256, 256, 0, st>>>(ns, c->nbf, g.fpbs, g.fqbs, c->pq, vch));
-    DBSRG_RUN(c, "k_group_entries", k_group_entries<<<1, 1, 0, st>>>(n, lk1, lk2, lcd, c->ipbs, c->nbf, c->icc, c->nch,
-                                     c->iicc, bcount, bstart, order, eblk, dscal + 1));
-    dim3 grid((unsigned)(((size_t)ms * ms + 255) / 256), (unsigned)c->iicc);
-    DBSRG_RUN(c, "k_overlap_update", k_overlap_update<<<grid, 256, 0, st>>>(ns, c->iicc, bstart, order, lk1, lk2, lcd, c->ipbs,
-                                           vch, c->hch));
-    return rd_err(c, dscal + 1);
+    DBSRG_RUN(c, "k_group_entries",
+              k_group_entries<<<1, 1, 0, st>>>(n, lk1, lk2, lcd, c->ipbs, c->nbf, c->icc, c->nch,
+                                               c->iicc, bcount, bstart, order, eblk, tlist,
+                                               dscal + 2, dscal + 1));
+    if ((rc = rd_err(c, dscal + 1))) return rc;
+    int ntouched = 0;
+    DBSRG_TRY(c, cudaMemcpyAsync(&ntouched, dscal + 2, sizeof(int), cudaMemcpyDeviceToHost, st));
+    DBSRG_TRY(c, cudaStreamSynchronize(st));
+    if (ntouched < 0 || ntouched > c->iicc) return set_err(c, DBSRG_ECUDA, "inconsistent block list");
+    if (ntouched > 0) {
+      dim3 grid((unsigned)(((size_t)ms * ms + 255) / 256), (unsigned)ntouched);
+      DBSRG_RUN(c, "k_overlap_update",
+                k_overlap_update<<<grid, 256, 0, st>>>(ns, tlist, bstart, order, lk1, lk2, lcd,
+                                                       c->ipbs, vch, c->hch));
+    }
+    DBSRG_TRY(c, cudaStreamSynchronize(st));
+    return DBSRG_OK;
   }
 
   // ---- 2. segments
@@ -657,7 +667,6 @@ int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const 
   DBSRG_TRY(c, cudaStreamSynchronize(st));
   DBSRG_RUN(c, "k_seg_info", k_seg_info<<<(nseg + 127) / 128, 128, 0, st>>>(nseg, seg_start, lk1, c->nch, c->iicc, c->icc,
                                                  info, dscal + 1));
-  DBSRG_RUN(c, "k_owner_list", k_owner_list<<<1, 1, 0, st>>>(nseg, info, owners, dscal + 2));
   if ((rc = rd_err(c, dscal + 1))) return rc;
 
   // ---- 3. contraction set-up per case
@@ -763,21 +772,55 @@ int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const 
       return set_err(c, DBSRG_ECUDA, "inconsistent segment table");
   }
   const size_t per = (size_t)ns * ncol;
-  std::vector<int> mem, own;  // member segment ids; owner slot positions
-  // the factored direct cases keep no per-segment results: larger chunks
+  // chunks of owner segments, each with its partner; the member ids and owner
+  // slots of all chunks go to the device in one copy
   const int chunk = (factored && icv <= 2) ? 16 * kSegChunk : kSegChunk;
-  auto flush = [&]() -> int {
-    int nm = (int)mem.size();
-    if (nm == 0) return DBSRG_OK;
-    // device copy of member ids and of the owner slots
-    std::vector<int> h(nm + own.size());
-    std::copy(mem.begin(), mem.end(), h.begin());
-    std::copy(own.begin(), own.end(), h.begin() + nm);
+  const bool split_x = factored && icv >= 3 && c->precision == DBSRG_SPLIT_BF16;
+  struct Chunk {
+    int moff, nm, nown, npq;
+  };
+  std::vector<Chunk> chunks;
+  std::vector<int> hbuf;
+  {
+    std::vector<int> mem, own;  // member segment ids; owner slot positions
+    auto close = [&]() {
+      if (mem.empty()) return;
+      Chunk ch{(int)hbuf.size(), (int)mem.size(), (int)own.size(), 0};
+      hbuf.insert(hbuf.end(), mem.begin(), mem.end());
+      hbuf.insert(hbuf.end(), own.begin(), own.end());
+      if (split_x) {
+        // quadrants of every owner's block that receive terms
+        for (int os : own) {
+          const SegInfo &si = hinfo[mem[os]];
+          for (int q = 0; q < 4; q++)
+            if (quadrant_has_terms(q % 2 + 1, q / 2 + 1, na, ssp.ii, ssp.jj, si.ich, si.jch,
+                                   si.partner >= 0)) {
+              hbuf.push_back(os * 4 + q);
+              ch.npq++;
+            }
+        }
+      }
+      chunks.push_back(ch);
+      mem.clear();
+      own.clear();
+    };
+    for (int s = 0; s < nseg; s++) {
+      if (!hinfo[s].owner) continue;
+      own.push_back((int)mem.size());
+      mem.push_back(s);
+      if (hinfo[s].partner >= 0) mem.push_back(hinfo[s].partner);
+      if ((int)mem.size() >= chunk - 1) close();
+    }
+    close();
+  }
+  if (!hbuf.empty() && (rc = copy_in(c, members, hbuf.data(), sizeof(int) * hbuf.size())))
+    return rc;
+  auto run_chunk = [&](const int *mb, int nm, const int *ob, int nown, const int *pq,
+                       int npq) -> int {
     int rc2;
-    if ((rc2 = copy_in(c, members, h.data(), sizeof(int) * h.size()))) return rc2;
     if (factored) {
       double *Y = nullptr;
-      if (icv >= 3) {
+      if (icv >= 3 && !split_x) {
         if ((rc2 = ensure_scratch(c, sizeof(double) * per * na * nm))) return rc2;
         Y = (double *)c->scratch;
       }
@@ -796,9 +839,9 @@ int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const 
         job.tabs[a] = tabs[a];
       }
       job.nm = nm;
-      job.members = members;
-      job.nown = (int)own.size();
-      job.own = members + nm;
+      job.members = mb;
+      job.nown = nown;
+      job.own = ob;
       job.info = info;
       job.k2 = lk2;
       job.k3 = lk3;
@@ -806,10 +849,9 @@ int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const 
       job.cd = lcd;
       job.Y = Y;
       job.split = c->precision == DBSRG_SPLIT_BF16;
-      rc2 = factored_contract(c, job);
-      mem.clear();
-      own.clear();
-      return rc2;
+      job.pqlist = pq;
+      job.npq = npq;
+      return factored_contract(c, job);
     }
     if ((rc2 = ensure_scratch(c, 2 * sizeof(double) * per * na * nm))) return rc2;
     double *X = (double *)c->scratch;
@@ -817,7 +859,7 @@ int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const 
     {
       dim3 gd((unsigned)((per + 255) / 256), (unsigned)nm, (unsigned)na);
       DBSRG_RUN(c, "k_density_acc",
-                k_density_acc<<<gd, 256, 0, st>>>(ns, ks, sym_d, ncol, na, dsp, nm, members, info,
+                k_density_acc<<<gd, 256, 0, st>>>(ns, ks, sym_d, ncol, na, dsp, nm, mb, info,
                                                   lk2, lk3, lcd, c->pq, X));
     }
     for (int a = 0; a < na; a++) {
@@ -837,30 +879,30 @@ int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const 
     }
     int mode = sym_d == 'x' ? 0 : 1;
     size_t space = mode == 0 ? (size_t)ms * ms : (size_t)4 * ns * (2 * ks - 1);
-    dim3 gs((unsigned)((space + 255) / 256), (unsigned)own.size());
+    dim3 gs((unsigned)((space + 255) / 256), (unsigned)nown);
     DBSRG_RUN(c, "k_scatter",
-              k_scatter<<<gs, 256, 0, st>>>(ns, ks, mode, ssp, nm, members, members + nm, info,
+              k_scatter<<<gs, 256, 0, st>>>(ns, ks, mode, ssp, nm, mb, ob, info,
                                             Y, c->hch));
-    mem.clear();
-    own.clear();
     return DBSRG_OK;
   };
-  for (int s = 0; s < nseg; s++) {
-    if (!hinfo[s].owner) continue;
-    own.push_back((int)mem.size());
-    mem.push_back(s);
-    if (hinfo[s].partner >= 0) mem.push_back(hinfo[s].partner);
-    if ((int)mem.size() >= chunk - 1)
-      if ((rc = flush())) return rc;
-  }
-  if ((rc = flush())) return rc;
-  int nown = 0;
-  for (int s = 0; s < nseg; s++) nown += hinfo[s].owner;
-  if (icase == 2 && itype == 3 && nown > 0) {
-    const double *quad;
-    if ((rc = get_quad(c, kpol, &quad))) return rc;
-    DBSRG_RUN(c, "k_acf", k_acf<<<(nown + 127) / 128, 128, 0, st>>>(nown, owners, info, kpol, c->nbf, lk2, lk3, lcd,
-                                             quad, c->acf, c->iicc));
+  for (const Chunk &ch : chunks)
+    if ((rc = run_chunk(members + ch.moff, ch.nm, members + ch.moff + ch.nm, ch.nown,
+                        members + ch.moff + ch.nm + ch.nown, ch.npq)))
+      return rc;
+  if (icase == 2 && itype == 3) {
+    // owner segments in list order
+    std::vector<int> hown;
+    for (int s = 0; s < nseg; s++)
+      if (hinfo[s].owner) hown.push_back(s);
+    const int nown = (int)hown.size();
+    if (nown > 0) {
+      if ((rc = copy_in(c, owners, hown.data(), sizeof(int) * hown.size()))) return rc;
+      const double *quad;
+      if ((rc = get_quad(c, kpol, &quad))) return rc;
+      DBSRG_RUN(c, "k_acf", k_acf<<<(nown + 127) / 128, 128, 0, st>>>(nown, owners, info, kpol,
+                                                                    c->nbf, lk2, lk3, lcd, quad,
+                                                                    c->acf, c->iicc));
+    }
   }
   DBSRG_TRY(c, cudaStreamSynchronize(st));
   return DBSRG_OK;

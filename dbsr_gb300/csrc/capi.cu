@@ -164,6 +164,7 @@ int dbsrg_create(dbsrg_ctx **out, const dbsrg_grid_desc *d) {
   dbsrg_ctx *c = new (std::nothrow) dbsrg_ctx();
   if (!c) return DBSRG_ENOMEM;
   c->device = d->device;
+  c->nsm = prop.multiProcessorCount;
   if (cudaSetDevice(d->device) != cudaSuccess ||
       cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
     delete c;

@@ -32,8 +32,9 @@
 //
 // The per-segment work is then a sum of a few dozen potential rows per
 // output element, fused into the scatter for the direct cases.  All of this
-// is FP64; with job.split the far-field product runs as split-precision
-// products on the tensor cores (farfield_tc.cu).
+// is FP64; with job.split the exchange far field runs as split-precision
+// products on the tensor cores, fused with the near band and the scatter
+// (exchange_tc.cu).
 #include "internal.cuh"
 
 #include <algorithm>
@@ -358,22 +359,36 @@ __global__ void k_pair_cellsum(int ns, int nv, int kk, int nb, PairSpec ed, cons
   }
 }
 
-// (2) exclusive suffix (sum over later cells) or prefix sums per pair
+// (2) exclusive suffix (sum over later cells) or prefix sums per pair, one
+// warp per pair: every lane scans a run of cells, the run totals are
+// scanned across the warp by shuffles
 __global__ void k_pair_scan(int nv, int npair, double *S, int suffix) {
-  int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= npair) return;
-  double *s = S + (size_t)p * nv;
-  double acc = 0.0;
+  const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) / 32), lane = threadIdx.x % 32;
+  if (warp >= npair) return;
+  double *s = S + (size_t)warp * nv;
+  const int run = (nv + 31) / 32;
+  const int lo = min(nv, lane * run), hi = min(nv, lo + run);
+  double tot = 0.0;
+  for (int i = lo; i < hi; i++) tot += s[i];
+  double incl = tot;
+  for (int off = 1; off < 32; off <<= 1) {
+    const double v = suffix ? __shfl_down_sync(0xffffffffu, incl, off)
+                            : __shfl_up_sync(0xffffffffu, incl, off);
+    if (suffix ? lane + off < 32 : lane >= off) incl += v;
+  }
+  const double nb1 = suffix ? __shfl_down_sync(0xffffffffu, incl, 1)
+                            : __shfl_up_sync(0xffffffffu, incl, 1);
+  double acc = suffix ? (lane == 31 ? 0.0 : nb1) : (lane == 0 ? 0.0 : nb1);
   if (suffix) {
-    for (int iv = nv - 1; iv >= 0; iv--) {
-      double v = s[iv];
-      s[iv] = acc;
+    for (int i = hi - 1; i >= lo; i--) {
+      const double v = s[i];
+      s[i] = acc;
       acc += v;
     }
   } else {
-    for (int iv = 0; iv < nv; iv++) {
-      double v = s[iv];
-      s[iv] = acc;
+    for (int i = lo; i < hi; i++) {
+      const double v = s[i];
+      s[i] = acc;
       acc += v;
     }
   }
@@ -680,11 +695,11 @@ int pair_index(dbsrg_ctx *c, int n, const int *k2, const int *k3, int *pairs, in
 
 // far-field vectors of (family, type, k, exchange case), cached
 static int get_farfield(dbsrg_ctx *c, int family, int type, int k, int cs, const FarField **out) {
-  std::vector<FarField> &v = family == 0 ? c->rfar : c->sfar;
-  size_t idx = ((size_t)k * (family == 0 ? 4 : 2) + type) * 2 + (cs == 4 ? 1 : 0);
-  if (v.size() <= idx) v.resize(idx + 1);
-  if (v[idx].U) {
-    *out = &v[idx];
+  std::map<size_t, FarField> &v = family == 0 ? c->rfar : c->sfar;
+  const size_t idx = ((size_t)k * (family == 0 ? 4 : 2) + type) * 2 + (cs == 4 ? 1 : 0);
+  auto it = v.find(idx);
+  if (it != v.end() && it->second.U) {
+    *out = &it->second;
     return DBSRG_OK;
   }
   const DeviceGrid &g = c->g;
@@ -721,7 +736,7 @@ static int get_farfield(dbsrg_ctx *c, int family, int type, int k, int cs, const
                                                       ko2, kc2, cc2, cd->hi2,
                                                       family == 0 ? cd->lo2 : nullptr, f.V, f.Vl));
   v[idx] = f;
-  *out = &v[idx];
+  *out = &v.at(idx);
   return DBSRG_OK;
 }
 
@@ -791,9 +806,9 @@ static int get_pairpot_direct(dbsrg_ctx *c, int family, int type, int k, int icv
   DBSRG_RUN(c, "k_pair_cellsum",
             k_pair_cellsum<<<nv, 256, sm1, st>>>(ns, nv, kk, nb, ed, M1, M2, P1, P2, SA,
                                                  M2 ? SB : nullptr));
-  const unsigned gp = (unsigned)((npair + 127) / 128);
-  DBSRG_RUN(c, "k_pair_scan", k_pair_scan<<<gp, 128, 0, st>>>(nv, (int)npair, SA, icv == 1));
-  if (M2) DBSRG_RUN(c, "k_pair_scan", k_pair_scan<<<gp, 128, 0, st>>>(nv, (int)npair, SB, 0));
+  const unsigned gp = (unsigned)((npair * 32 + 255) / 256);
+  DBSRG_RUN(c, "k_pair_scan", k_pair_scan<<<gp, 256, 0, st>>>(nv, (int)npair, SA, icv == 1));
+  if (M2) DBSRG_RUN(c, "k_pair_scan", k_pair_scan<<<gp, 256, 0, st>>>(nv, (int)npair, SB, 0));
   const int npo = eo.sym ? eo.k1 * (eo.k1 + 1) / 2 : eo.k1 * eo.k2;
   const size_t sm3 = ((size_t)nb * (ed.k1 + ed.k2) + (size_t)npo * ed.k1 * ed.k2 +
                       (size_t)npo * ed.k1 * PBC) * sizeof(double) + (size_t)npo * sizeof(int);
@@ -832,6 +847,8 @@ static int get_pairpot_band(dbsrg_ctx *c, int family, int type, int k, int cs, i
     return set_err(c, DBSRG_ENOMEM, "pair potential allocation failed");
   }
   c->ppot[key] = K;
+  // positions past the ends of the band are never written by k_pair_band
+  DBSRG_TRY(c, cudaMemsetAsync(K, 0, npair * per * sizeof(double), c->stream));
   const double *P1 = c->brows + (size_t)(jp1 - 1) * nb * ns;
   const double *P2 = c->brows + (size_t)(jp2 - 1) * nb * ns;
   const int W = 2 * ks - 1, WL = PXC + W - 1;
@@ -849,10 +866,11 @@ static int get_pairpot_band(dbsrg_ctx *c, int family, int type, int k, int cs, i
 void free_orbital_products(dbsrg_ctx *c) {
   if (!c->rfar.empty() || !c->sfar.empty() || !c->ppot.empty() || c->brows)
     cudaStreamSynchronize(c->stream);
-  for (auto &f : c->rfar)
-    if (f.U) cudaFree(f.U);
-  for (auto &f : c->sfar)
-    if (f.U) cudaFree(f.U);
+  for (auto *v : {&c->rfar, &c->sfar})
+    for (auto &kv : *v) {
+      if (kv.second.U) cudaFree(kv.second.U);
+      if (kv.second.Ud) cudaFree(kv.second.Ud);
+    }
   c->rfar.clear();
   c->sfar.clear();
   for (auto &kv : c->ppot)
@@ -861,9 +879,6 @@ void free_orbital_products(dbsrg_ctx *c) {
   if (c->brows) cudaFree(c->brows);
   c->brows = nullptr;
 }
-
-int farfield_tc(dbsrg_ctx *c, int ns, int nb, int nm, const double *U, const double *Ul,
-                const double *Z, const double *Zl, double *Y, size_t per);
 
 int factored_contract(dbsrg_ctx *c, const FactorJob &j) {
   const DeviceGrid &g = c->g;
@@ -879,6 +894,34 @@ int factored_contract(dbsrg_ctx *c, const FactorJob &j) {
   for (int a = 0; a < j.na; a++) {
     qs.ii[a] = j.ii[a];
     qs.jj[a] = j.jj[a];
+  }
+  if (j.icv >= 3 && j.split) {
+    SplitExchange x{};
+    x.na = j.na;
+    x.nm = j.nm;
+    x.nown = j.nown;
+    x.lower = j.family == 0 ? 1 : 0;
+    for (int a = 0; a < j.na; a++) {
+      const int cs = j.icv;
+      if ((rc = get_farfield(c, j.family, j.types[a], j.kpol, cs, &x.far[a]))) return rc;
+      TableBases tb = table_bases(g, j.family, j.types[a]);
+      int c1 = cs == 3 ? tb.a2 : tb.a1, c2 = cs == 3 ? tb.b1 : tb.b2;
+      if (c1 != j.jp1[a] || c2 != j.jp2[a])
+        return set_err(c, DBSRG_EINVAL, "factored exchange: component mismatch");
+      if ((rc = get_pairpot_band(c, j.family, j.types[a], j.kpol, cs, j.jp1[a], j.jp2[a],
+                                 j.tabs[a], &x.Kb[a])))
+        return rc;
+      x.ii[a] = j.ii[a];
+      x.jj[a] = j.jj[a];
+    }
+    x.members = j.members;
+    x.own = j.own;
+    x.pqlist = j.pqlist;
+    x.npq = j.npq;
+    x.info = j.info;
+    x.pairs = j.pairs;
+    x.cd = j.cd;
+    return split_exchange(c, x);
   }
   if (j.icv >= 3) {
     const size_t per = (size_t)ns * ns;
@@ -902,15 +945,10 @@ int factored_contract(dbsrg_ctx *c, const FactorJob &j) {
       DBSRG_RUN(c, "k_far_z",
                 k_far_z<<<gz, 128, 0, st>>>(ns, nb, j.members, j.info, j.pairs, j.cd, f->V,
                                             f->Vl, Z, f->Vl ? Zl : nullptr));
-      if (j.split) {
-        if ((rc = farfield_tc(c, ns, nb, j.nm, f->U, f->Ul, Z, f->Vl ? Zl : nullptr, Ya, per)))
-          return rc;
-      } else {
-        dim3 gf((unsigned)((ns + 31) / 32), (unsigned)((ns + 31) / 32), (unsigned)j.nm);
-        DBSRG_RUN(c, "k_far_field",
-                  k_far_field<<<gf, 256, 0, st>>>(ns, nb, f->U, f->Ul, Z, f->Vl ? Zl : nullptr, Ya,
-                                                  per));
-      }
+      dim3 gf((unsigned)((ns + 31) / 32), (unsigned)((ns + 31) / 32), (unsigned)j.nm);
+      DBSRG_RUN(c, "k_far_field",
+                k_far_field<<<gf, 256, 0, st>>>(ns, nb, f->U, f->Ul, Z, f->Vl ? Zl : nullptr, Ya,
+                                                per));
       dim3 gb((unsigned)((ns * NDB + 255) / 256), (unsigned)j.nm);
       DBSRG_RUN(c, "k_band_sum",
                 k_band_sum<<<gb, 256, 0, st>>>(ns, j.members, j.info, j.pairs, j.cd, Kb, Ya, per));

@@ -42,6 +42,10 @@ struct CellData {
 // U, V (upper field) and Ul, Vl (lower field, R^k only), each (ns, nbound)
 struct FarField {
   double *U = nullptr, *V = nullptr, *Ul = nullptr, *Vl = nullptr;
+  // split-BF16 digit tiles of U (mode 0) and Ul (mode 1) and their row
+  // exponents, built on first use by the tensor-core exchange
+  void *Ud = nullptr;
+  int *eu = nullptr;
 };
 
 // one channel-pair segment of a coefficient list (a run of equal K1)
@@ -55,6 +59,7 @@ struct SegInfo {
 
 struct dbsrg_ctx {
   int device = 0;
+  int nsm = 0;  // streaming multiprocessors of the device
   cudaStream_t stream = nullptr;
   DeviceGrid g;
   std::string err;
@@ -76,8 +81,9 @@ struct dbsrg_ctx {
   // band-limited tables (|j-i| <= DBSRG_TABLE_BAND) for the factored path
   std::vector<double *> rbtab, sbtab;
   std::vector<CellData> rcell, scell;
-  // far-field vectors, indexed [(k*4+type)*2+case34] (R) / [(k*2+type)*2+case34] (S)
-  std::vector<FarField> rfar, sfar;
+  // far-field vectors, keyed (k*4+type)*2+case34 (R) / (k*2+type)*2+case34 (S);
+  // map nodes keep their addresses while other entries are added
+  std::map<size_t, FarField> rfar, sfar;
   // orbital-pair potentials of the factored contraction (direct band results
   // and exchange band results per ordered bound-orbital pair), keyed by
   // pairpot_key(); they depend on the tables and the orbitals
@@ -217,10 +223,36 @@ struct FactorJob {
   const int *k2, *k3;
   const int *pairs;  // ordered bound-orbital pair index of every entry
   const double *cd;
-  double *Y;         // exchange results [a][slot][ns*ns]
-  bool split;        // far field on the tensor cores (split BF16)
+  double *Y;         // exchange results [a][slot][ns*ns] (FP64 far field)
+  bool split;        // exchange on the tensor cores (split BF16), fused scatter
+  int npq;           // split exchange: (owner slot, quadrant) pairs receiving terms
+  const int *pqlist; //   their codes, owner slot * 4 + quadrant (0..3)
 };
 int factored_contract(dbsrg_ctx *c, const FactorJob &job);
+// exchange.cu-side entry of the split form (exchange_tc.cu)
+struct SplitExchange {
+  int na, nm, nown, lower;
+  const FarField *far[4];  // far-field vectors (and digit caches) per atype
+  const double *Kb[4];     // band pair potentials per atype
+  int ii[4], jj[4];
+  const int *members, *own, *pqlist;
+  int npq;
+  const SegInfo *info;
+  const int *pairs;
+  const double *cd;
+};
+int split_exchange(dbsrg_ctx *c, const SplitExchange &x);
+// quadrant (qr, qc) of an owner's block receives at least one term of the
+// list (UPDATE_HS): atype quadrants (ii, jj), the owner's channel pair
+// (ich, jch) and its partner's, if any
+inline bool quadrant_has_terms(int qr, int qc, int na, const int *ii, const int *jj, int ich,
+                               int jch, bool partner) {
+  for (int a = 0; a < na; a++) {
+    if (qr == ii[a] && qc == jj[a]) return true;
+    if (ich == jch && !partner && qr == jj[a] && qc == ii[a]) return true;
+  }
+  return false;
+}
 // pairs[e] = bmap[K2]*nbound + bmap[K3]; sets *derr when an orbital is not bound
 int pair_index(dbsrg_ctx *c, int n, const int *k2, const int *k3, int *pairs, int *derr);
 
