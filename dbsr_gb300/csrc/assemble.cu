@@ -777,28 +777,22 @@ int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const 
   const int chunk = (factored && icv <= 2) ? 16 * kSegChunk : kSegChunk;
   const bool split_x = factored && icv >= 3 && c->precision == DBSRG_SPLIT_BF16;
   struct Chunk {
-    int moff, nm, nown, npq;
+    int moff, nm, nown, xoff, nxq;
   };
   std::vector<Chunk> chunks;
   std::vector<int> hbuf;
+  std::vector<XQuad> hxq;  // split exchange: quadrant records of all chunks
+  bool xq_ok = true;
   {
     std::vector<int> mem, own;  // member segment ids; owner slot positions
     auto close = [&]() {
       if (mem.empty()) return;
-      Chunk ch{(int)hbuf.size(), (int)mem.size(), (int)own.size(), 0};
+      Chunk ch{(int)hbuf.size(), (int)mem.size(), (int)own.size(), (int)hxq.size(), 0};
       hbuf.insert(hbuf.end(), mem.begin(), mem.end());
       hbuf.insert(hbuf.end(), own.begin(), own.end());
       if (split_x) {
-        // quadrants of every owner's block that receive terms
-        for (int os : own) {
-          const SegInfo &si = hinfo[mem[os]];
-          for (int q = 0; q < 4; q++)
-            if (quadrant_has_terms(q % 2 + 1, q / 2 + 1, na, ssp.ii, ssp.jj, si.ich, si.jch,
-                                   si.partner >= 0)) {
-              hbuf.push_back(os * 4 + q);
-              ch.npq++;
-            }
-        }
+        xq_ok = xq_ok && build_xquads(na, ssp.ii, ssp.jj, mem, own, hinfo, hxq);
+        ch.nxq = (int)hxq.size() - ch.xoff;
       }
       chunks.push_back(ch);
       mem.clear();
@@ -815,8 +809,15 @@ int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const 
   }
   if (!hbuf.empty() && (rc = copy_in(c, members, hbuf.data(), sizeof(int) * hbuf.size())))
     return rc;
-  auto run_chunk = [&](const int *mb, int nm, const int *ob, int nown, const int *pq,
-                       int npq) -> int {
+  if (!xq_ok) return set_err(c, DBSRG_ECUDA, "split exchange: a quadrant with more than 4 terms");
+  XQuad *dxq = nullptr;
+  if (!hxq.empty()) {
+    if ((rc = ensure_lscratch(c, sizeof(XQuad) * hxq.size()))) return rc;
+    dxq = (XQuad *)c->lscratch;
+    if ((rc = copy_in(c, dxq, hxq.data(), sizeof(XQuad) * hxq.size()))) return rc;
+  }
+  auto run_chunk = [&](const int *mb, int nm, const int *ob, int nown, const XQuad *xq,
+                       int nxq) -> int {
     int rc2;
     if (factored) {
       double *Y = nullptr;
@@ -849,8 +850,8 @@ int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const 
       job.cd = lcd;
       job.Y = Y;
       job.split = c->precision == DBSRG_SPLIT_BF16;
-      job.pqlist = pq;
-      job.npq = npq;
+      job.xq = xq;
+      job.nxq = nxq;
       return factored_contract(c, job);
     }
     if ((rc2 = ensure_scratch(c, 2 * sizeof(double) * per * na * nm))) return rc2;
@@ -887,7 +888,7 @@ int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const 
   };
   for (const Chunk &ch : chunks)
     if ((rc = run_chunk(members + ch.moff, ch.nm, members + ch.moff + ch.nm, ch.nown,
-                        members + ch.moff + ch.nm + ch.nown, ch.npq)))
+                        dxq ? dxq + ch.xoff : nullptr, ch.nxq)))
       return rc;
   if (icase == 2 && itype == 3) {
     // owner segments in list order

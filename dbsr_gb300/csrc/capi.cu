@@ -83,6 +83,9 @@ int ensure_tcscratch(dbsrg_ctx *c, size_t bytes) {
 int ensure_pscratch(dbsrg_ctx *c, size_t bytes) {
   return grow(c, &c->pscratch, &c->pscratch_bytes, bytes);
 }
+int ensure_lscratch(dbsrg_ctx *c, size_t bytes) {
+  return grow(c, &c->lscratch, &c->lscratch_bytes, bytes);
+}
 bool sync_check_enabled() {
   static int v = -1;
   if (v < 0) {
@@ -209,6 +212,7 @@ int dbsrg_destroy(dbsrg_ctx *c) {
   if (c->fscratch) cudaFree(c->fscratch);
   if (c->tcscratch) cudaFree(c->tcscratch);
   if (c->pscratch) cudaFree(c->pscratch);
+  if (c->lscratch) cudaFree(c->lscratch);
   if (c->bmap) cudaFree(c->bmap);
   if (c->b2o) cudaFree(c->b2o);
   if (c->pinned) cudaFreeHost(c->pinned);

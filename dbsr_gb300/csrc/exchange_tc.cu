@@ -64,7 +64,11 @@ __device__ __forceinline__ void write_digit_row(__nv_bfloat16 *D, int NR, int ro
   }
 }
 
-// U (ns x nb, column-major) -> digit operand [slice][NR][TILE] and row exponents
+// exponents of one digit operand: NR*32 row exponents, then the NR maxima
+// over its 32-row tiles
+constexpr int EXP_PER_ROWTILE = 33;
+
+// U (ns x nb, column-major) -> digit operand [slice][NR][TILE] and exponents
 __global__ void k_udigits(int ns, int nb, int NR, const double *U, __nv_bfloat16 *D, int *eu) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   if (x >= NR * 32) return;
@@ -77,6 +81,8 @@ __global__ void k_udigits(int ns, int nb, int NR, const double *U, __nv_bfloat16
   }
   const int e = scale_exp(m);
   eu[x] = e;
+  const int et = __reduce_max_sync(0xffffffffu, e);  // a warp is one 32-row tile
+  if ((threadIdx.x & 31) == 0) eu[NR * 32 + x / 32] = et;
   write_digit_row(D, NR, x, vals, e);
 }
 
@@ -88,7 +94,7 @@ struct ZArgs {
   const int *pairs;
   const double *cd;
   __nv_bfloat16 *Zd;  // [a][mode][slot][slice][NR][TILE]
-  int *ez;            // [a][mode][slot][NR*32]
+  int *ez;            // [a][mode][slot][NR*33]
   double *Yb;         // [a][slot][ns*17]
 };
 
@@ -137,107 +143,125 @@ __global__ void __launch_bounds__(128) k_zdigits(const ZArgs z) {
     }
     const int e = scale_exp(m);
     const size_t op = (size_t)(a * 2 + mode) * z.nm + slot;
-    z.ez[op * z.NR * 32 + y] = e;
+    z.ez[op * z.NR * EXP_PER_ROWTILE + y] = e;
+    const int et = __reduce_max_sync(0xffffffffu, e);  // a warp is one 32-row tile
+    if ((t & 31) == 0) z.ez[op * z.NR * EXP_PER_ROWTILE + z.NR * 32 + y / 32] = et;
     write_digit_row(z.Zd + op * TS * sl, z.NR, y, vals, e);
   }
 }
 
 struct XArgs {
   int ns, NR, ntx, nty, nm, na, lower;
-  long long nitems;
+  int nrows;                   // (quadrant record, x tile) rows of 128 x ns
   const __nv_bfloat16 *Ud[4];  // per atype: [mode][slice][NR][TILE]
-  const int *eu[4];            // per atype: [mode][NR*32]
+  const int *eu[4];            // per atype: [mode][NR*33]
   const __nv_bfloat16 *Zd;     // [a][mode][slot][slice][NR][TILE]
-  const int *ez;               // [a][mode][slot][NR*32]
+  const int *ez;               // [a][mode][slot][NR*33]
   const double *Yb;            // [a][slot][ns*17]
-  int ii[4], jj[4];
-  const int *members;
-  const int *pqlist;           // owner slot * 4 + quadrant
-  const SegInfo *info;
+  const XQuad *xq;
   double *hch;
   int *err;
 };
 
-struct Plan {
-  int ok, tx, ty, qr, qc, blk, nt, half, np, band;
-  int ta[MAXT], tslot[MAXT], ttra[MAXT];
-  int pt[2 * MAXT], pm[2 * MAXT];
+// one row (quadrant record, x tile): the quadrant's terms, term code
+// t = atype | transposed << 2 | member slot << 3
+struct Row {
+  int blk, qr, qc, nt, half, tx;
+  int tc[MAXT];
 };
 
-// terms and products of one tile (the term order of k_scatter_x: atype-major,
-// owner then partner)
-__device__ void make_plan(const XArgs &p, long long item, Plan &pl) {
-  pl.ok = 0;
-  pl.nt = 0;
-  pl.np = 0;
-  if (item >= p.nitems) return;
-  const long long per = (long long)p.ntx * p.nty;
-  const int pqi = (int)(item / per), rem = (int)(item % per);
-  pl.tx = rem / p.nty;
-  pl.ty = rem % p.nty;
-  const int code = p.pqlist[pqi], oslot = code >> 2, quad = code & 3;
-  pl.qr = quad % 2 + 1;
-  pl.qc = quad / 2 + 1;
-  const SegInfo si = p.info[p.members[oslot]];
-  pl.blk = si.blk;
-  const int pslot = si.partner >= 0 ? oslot + 1 : -1;
-  pl.half = 0;
-  for (int a = 0; a < p.na; a++)
-    for (int pass = 0; pass < 2; pass++) {
-      const int slot = pass == 0 ? oslot : pslot;
-      if (slot < 0) break;
-      const SegInfo sj = p.info[p.members[slot]];
-      const bool eq = sj.ich == sj.jch;
-      const bool dir = (sj.ich > sj.jch || eq) && pl.qr == p.ii[a] && pl.qc == p.jj[a];
-      const bool tra = (sj.ich < sj.jch && pl.qr == p.ii[a] && pl.qc == p.jj[a]) ||
-                       (eq && pl.qr == p.jj[a] && pl.qc == p.ii[a]);
-      if (eq) pl.half = 1;
-      for (int k = 0; k < 2; k++) {
-        if (!(k == 0 ? dir : tra)) continue;
-        if (pl.nt == MAXT) {
-          atomicExch(p.err, 2);
-          continue;
-        }
-        pl.ta[pl.nt] = a;
-        pl.tslot[pl.nt] = slot;
-        pl.ttra[pl.nt] = k;
-        pl.nt++;
-      }
-    }
-  const int x0 = pl.tx * 128, y0 = pl.ty * 32;
-  const bool up = (y0 + 31) - x0 >= FAR, lo = (x0 + 127) - y0 >= FAR;
-  for (int t = 0; t < pl.nt; t++) {
-    const bool r0 = pl.ttra[t] ? lo : up;  // upper field of the term's result
-    const bool r1 = p.lower && (pl.ttra[t] ? up : lo);
-    if (r0) {
-      pl.pt[pl.np] = t;
-      pl.pm[pl.np++] = 0;
-    }
-    if (r1) {
-      pl.pt[pl.np] = t;
-      pl.pm[pl.np++] = 1;
-    }
-  }
-  pl.band = (y0 + 31) - x0 >= -BAND && y0 - (x0 + 127) <= BAND;
-  pl.ok = 1;
+__device__ __forceinline__ void load_row(const XArgs &p, int row, Row &r) {
+  const int4 *q = reinterpret_cast<const int4 *>(p.xq + row / p.ntx);
+  const int4 v0 = q[0], v1 = q[1], v2 = q[2];  // blk qr qc nt | half t0 t1 t2 | t3 . . .
+  r.tx = row % p.ntx;
+  r.blk = v0.x;
+  r.qr = v0.y;
+  r.qc = v0.z;
+  r.nt = min(v0.w, MAXT);
+  r.half = v1.x;
+  r.tc[0] = v1.y;
+  r.tc[1] = v1.z;
+  r.tc[2] = v1.w;
+  r.tc[3] = v2.x;
 }
 
-__global__ void __launch_bounds__(256, 1) k_xfused(const XArgs p) {
+// term code of term t (a select chain keeps the codes in registers)
+__device__ __forceinline__ int term_code(const Row &r, int t) {
+  return t == 0 ? r.tc[0] : t == 1 ? r.tc[1] : t == 2 ? r.tc[2] : r.tc[3];
+}
+
+// products of tile (tx, ty), packed 3 bits each (term | mode << 2): per term
+// the upper field of its result and, for R^k, the lower one, where the tile
+// meets them.  *band: the tile meets the near band |y - x| <= 8.
+__device__ __forceinline__ uint32_t tile_products(const XArgs &p, const Row &r, int ty, int &np,
+                                                  bool &band) {
+  const int x0 = r.tx * 128, y0 = ty * 32;
+  const bool up = (y0 + 31) - x0 >= FAR, lo = (x0 + 127) - y0 >= FAR;
+  uint32_t codes = 0;
+  np = 0;
+#pragma unroll
+  for (int t = 0; t < MAXT; t++) {
+    if (t >= r.nt) break;
+    const bool tra = (term_code(r, t) >> 2) & 1;
+    if (tra ? lo : up) codes |= (uint32_t)t << (3 * np++);
+    if (p.lower && (tra ? up : lo)) codes |= (uint32_t)(t | 4) << (3 * np++);
+  }
+  band = (y0 + 31) - x0 >= -BAND && y0 - (x0 + 127) <= BAND;
+  return codes;
+}
+
+constexpr int NCW = 8;                // consumer (epilogue) warps
+constexpr int WPROD = NCW;            // producer warp
+constexpr int WSTAGE = NCW + 1;       // stager warp
+constexpr int NTHR = 32 * (NCW + 2);
+
+__device__ __forceinline__ void consumers_sync() {
+  asm volatile("bar.sync 1, %0;\n" ::"n"(32 * NCW) : "memory");
+}
+
+// 8-byte asynchronous copy global -> shared; zero fill when !valid
+__device__ __forceinline__ void cp_async8(uint32_t dst, const void *src, bool valid) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(dst), "l"(src),
+               "r"(valid ? 8 : 0)
+               : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t mbar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(mbar) : "memory");
+}
+
+// Warp-specialised, one CTA per SM walking rows (quadrant record, x tile)
+// of 128 x ns; every role walks the same tile sequence.
+//  * producer (warp NCW, one lane): per product waits until its operand
+//    stage is free (the MMAs two products back completed), bulk-loads the
+//    operands (the 128-row A operand only when the stage does not hold it
+//    already -- along a row it repeats), waits until the consumers have read
+//    the TMEM set two products back, issues the MMAs and commits them;
+//  * stager (warp NCW+1, even ns): per tile waits until the consumers are
+//    done with the staging buffers, then bulk-loads the tile's hch columns
+//    and the band rows of its terms (one copy per lane);
+//  * consumers (warps 0..NCW-1): per product read the TMEM set, release it
+//    and add the product into int64 accumulators; per tile convert, add the
+//    band, add hch, store, and release the staging buffers.
+// 10 warps: one SM sub-partition holds 3 of them, so at most 168 registers.
+__global__ void __maxnreg__(168) k_xfused(const XArgs p) {
   extern __shared__ __align__(1024) unsigned char smraw[];
   unsigned char *sA = smraw;                          // [2][TS][A_BYTES]
   unsigned char *sB = sA + 2 * TS * A_BYTES;          // [2][TS][B_BYTES]
   double *sband = (double *)(sB + 2 * TS * B_BYTES);  // [MAXT][NDB][128]
-  __shared__ __align__(8) uint64_t bar_ld[2], bar_mma[2];
+  double *shch = sband + (size_t)MAXT * NDB * 128;    // [32 columns][128 rows]
+  __shared__ __align__(8) uint64_t bar_ld[2], bar_mma[2], bar_free[2], bar_tile, bar_sfree;
   __shared__ uint32_t tmem_base;
-  __shared__ Plan sp[2];
   __shared__ int s_abort;
   const int tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
-  const int lg = warp & 3, hf = warp >> 2;
   if (tid == 0) {
     for (int b = 0; b < 2; b++) {
       mbar_init(smem_u32(&bar_ld[b]), 1);
       mbar_init(smem_u32(&bar_mma[b]), 1);
+      mbar_init(smem_u32(&bar_free[b]), NCW);
     }
+    mbar_init(smem_u32(&bar_tile), 1);
+    mbar_init(smem_u32(&bar_sfree), NCW);
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     s_abort = 0;
   }
@@ -252,173 +276,332 @@ __global__ void __launch_bounds__(256, 1) k_xfused(const XArgs p) {
   fence_after();
   const uint32_t tbase = tmem_base;
   const size_t sl = (size_t)p.NR * TILE;  // elements per slice of a digit operand
+  const size_t ms = 2 * (size_t)p.ns;
+  const int EX = p.NR * EXP_PER_ROWTILE;  // exponents per digit operand
+  // even ns: every hch column and band row of a tile starts on a 16-byte
+  // boundary and is staged by 1-D bulk copies; odd ns: 8-byte cp.async
+  const bool bulk = (p.ns % 2) == 0;
+  volatile int *abort_flag = &s_abort;
 
-  // thread 0 state of the asynchronous work in flight
-  long long ld_pending = -1, mma_pending = -1;  // product index of an unfinished load / commit
-
-  auto issue = [&](const Plan &pl, int pc, uint32_t P) -> bool {
-    const int b = P & 1;
-    const uint32_t par = (P >> 1) & 1;
-    const int t = pl.pt[pc], m = pl.pm[pc], a = pl.ta[t], slot = pl.tslot[t];
-    const __nv_bfloat16 *Ub = p.Ud[a] + (size_t)m * TS * sl;
-    const __nv_bfloat16 *Zb = p.Zd + ((size_t)(a * 2 + m) * p.nm + slot) * TS * sl;
-    const __nv_bfloat16 *As = (pl.ttra[t] ? Zb : Ub) + (size_t)4 * pl.tx * TILE;
-    const __nv_bfloat16 *Bs = (pl.ttra[t] ? Ub : Zb) + (size_t)pl.ty * TILE;
-    const uint32_t la = smem_u32(&bar_ld[b]);
-    mbar_expect_tx(la, TS * (A_BYTES + B_BYTES));
-    for (int i = 0; i < TS; i++) {
-      bulk_g2s(smem_u32(sA + (size_t)(b * TS + i) * A_BYTES), As + (size_t)i * sl, A_BYTES, la);
-      bulk_g2s(smem_u32(sB + (size_t)(b * TS + i) * B_BYTES), Bs + (size_t)i * sl, B_BYTES, la);
-    }
-    ld_pending = P;
-    if (!mbar_wait(la, par, WAIT_NS)) return false;
-    ld_pending = -1;
-    const uint32_t idesc = make_idesc(128, 32);
-    const uint32_t a0 = smem_u32(sA + (size_t)b * TS * A_BYTES);
-    const uint32_t b0 = smem_u32(sB + (size_t)b * TS * B_BYTES);
-    for (int g = 0; g < TS; g++) {
-      const uint32_t dt = tbase + (uint32_t)(b * 256 + g * 32);
-      uint32_t acc = 0;
-      for (int i = 0; i <= g; i++)
-        for (int kk = 0; kk < 2; kk++) {
-          const uint64_t ad = make_desc(a0 + (uint32_t)(i * A_BYTES + kk * 256), 128, 512);
-          const uint64_t bd = make_desc(b0 + (uint32_t)((g - i) * B_BYTES + kk * 256), 128, 512);
-          mma_bf16(dt, ad, bd, idesc, acc);
-          acc = 1;
-        }
-    }
-    mma_commit(smem_u32(&bar_mma[b]));
-    mma_pending = P;
-    return true;
-  };
-
-  double tacc[16];
+  if (warp == WPROD) {
+    // ------------------------------------------------------------ producer
+    if (lane == 0) {
+      uint32_t q = 0;
+      long long ld_pend = -1, mma_last = -1;
+      long long keyA[2] = {-1, -1};  // (row, term, mode) of the A operand held by each stage
+      bool fail = false;
+      Row r;
+      for (int row = blockIdx.x; row < p.nrows && !fail; row += gridDim.x) {
+        load_row(p, row, r);
+        for (int ty = 0; ty < p.nty && !fail; ty++) {
+          int np;
+          bool band;
+          const uint32_t codes = tile_products(p, r, ty, np, band);
+          for (int pc = 0; pc < np; pc++, q++) {
+            if (*abort_flag) {
+              fail = true;
+              break;
+            }
+            const int b = q & 1;
+            const uint32_t n = q >> 1;
+            if (q >= 2 && !mbar_wait(smem_u32(&bar_mma[b]), (n - 1) & 1, WAIT_NS)) {
+              fail = true;
+              break;
+            }
+            const int pcode = (codes >> (3 * pc)) & 7, t = pcode & 3, m = pcode >> 2;
+            const int tc = term_code(r, t), a = tc & 3, tra = (tc >> 2) & 1, slot = tc >> 3;
+            const __nv_bfloat16 *Ub = p.Ud[a] + (size_t)m * TS * sl;
+            const __nv_bfloat16 *Zb = p.Zd + ((size_t)(a * 2 + m) * p.nm + slot) * TS * sl;
+            const __nv_bfloat16 *As = (tra ? Zb : Ub) + (size_t)4 * r.tx * TILE;
+            const __nv_bfloat16 *Bs = (tra ? Ub : Zb) + (size_t)ty * TILE;
+            const long long akey = ((long long)row * MAXT + t) * 2 + m;
+            const bool needA = keyA[b] != akey;
+            const uint32_t la = smem_u32(&bar_ld[b]);
+            mbar_expect_tx(la, TS * (B_BYTES + (needA ? A_BYTES : 0)));
+            for (int i = 0; i < TS; i++) {
+              if (needA)
+                bulk_g2s(smem_u32(sA + (size_t)(b * TS + i) * A_BYTES), As + (size_t)i * sl,
+                         A_BYTES, la);
+              bulk_g2s(smem_u32(sB + (size_t)(b * TS + i) * B_BYTES), Bs + (size_t)i * sl,
+                       B_BYTES, la);
+            }
+            keyA[b] = akey;
+            ld_pend = q;
+            if (!mbar_wait(la, n & 1, WAIT_NS)) {
+              fail = true;
+              break;
+            }
+            ld_pend = -1;
+            if (q >= 2 && !mbar_wait(smem_u32(&bar_free[b]), (n - 1) & 1, WAIT_NS)) {
+              fail = true;
+              break;
+            }
+            fence_after();
+            constexpr uint32_t idesc = make_idesc(128, 32);
+            // descriptors of the stage; operand offsets added to the address
+            // field (shared addresses stay below 2^18 bytes: no carry)
+            const uint64_t ad0 = make_desc(smem_u32(sA + (size_t)b * TS * A_BYTES), 128, 512);
+            const uint64_t bd0 = make_desc(smem_u32(sB + (size_t)b * TS * B_BYTES), 128, 512);
 #pragma unroll
-  for (int c = 0; c < 16; c++) tacc[c] = 0.0;
-
-  auto epilogue = [&](const Plan &pl, int pc, uint32_t P) -> bool {
-    const int b = P & 1;
-    const uint32_t par = (P >> 1) & 1;
-    const bool ok = mbar_wait(smem_u32(&bar_mma[b]), par, WAIT_NS);
-    // tcgen05.ld is warp-collective: a warp reads only when all its lanes saw completion
-    if (!__all_sync(0xffffffffu, ok)) return false;
-    fence_after();
-    uint32_t v[TS][16];
+            for (int g = 0; g < TS; g++) {
+              const uint32_t dt = tbase + (uint32_t)(b * 256 + g * 32);
 #pragma unroll
-    for (int g = 0; g < TS; g++)
-      tmem_ld16(tbase + ((uint32_t)(lg * 32) << 16) + (uint32_t)(b * 256 + g * 32 + hf * 16), v[g]);
-    tmem_wait_ld();
-    const int t = pl.pt[pc], m = pl.pm[pc], a = pl.ta[t], slot = pl.tslot[t], tra = pl.ttra[t];
-    const int x = pl.tx * 128 + lg * 32 + lane;
-    const int *eua = p.eu[a] + (size_t)m * p.NR * 32;
-    const int *ezs = p.ez + ((size_t)(a * 2 + m) * p.nm + slot) * p.NR * 32;
-    const int erow = (tra ? ezs[x] : eua[x]) - 8 * (TS + 1);
-    const int y0 = pl.ty * 32 + hf * 16;
-    const int *ecol = tra ? eua : ezs;
+              for (int i = 0; i <= g; i++)
 #pragma unroll
-    for (int c = 0; c < 16; c++) {
-      const int y = y0 + c, d = y - x;
-      const bool in = tra ? (m == 0 ? d <= -FAR : d >= FAR) : (m == 0 ? d >= FAR : d <= -FAR);
-      if (in && x < p.ns && y < p.ns) {
-        long long I = 0;
-#pragma unroll
-        for (int g = 0; g < TS; g++) I = I * 256 + (long long)f2i_exact(__uint_as_float(v[g][c]));
-        tacc[c] += i64_scaled(I, erow + ecol[y]);
-      }
-    }
-    return true;
-  };
-
-  auto finish = [&](const Plan &pl) {
-    const int x0 = pl.tx * 128, y0 = pl.ty * 32, xl = lg * 32 + lane, x = x0 + xl;
-    const int ns = p.ns;
-    if (pl.band) {
-      for (int t = 0; t < pl.nt; t++) {
-        const double *yb = p.Yb + ((size_t)pl.ta[t] * p.nm + pl.tslot[t]) * (size_t)ns * NDB;
-        double *sb = sband + (size_t)t * NDB * 128;
-        if (!pl.ttra[t]) {  // rows x of y, diagonals y - x
-          for (int q = tid; q < NDB * 128; q += 256) {
-            const int dd = q / 128, r = x0 + q % 128, yy = r + dd - BAND;
-            sb[q] = (r < ns && yy >= 0 && yy < ns) ? yb[r + (size_t)ns * dd] : 0.0;
-          }
-        } else {  // rows y of y, diagonals x - y
-          for (int q = tid; q < NDB * 32; q += 256) {
-            const int dd = q / 32, r = y0 + q % 32, xx = r + dd - BAND;
-            sb[q] = (r < ns && xx >= 0 && xx < ns) ? yb[r + (size_t)ns * dd] : 0.0;
+                for (int kk = 0; kk < 2; kk++)
+                  mma_bf16(dt, ad0 + ((i * A_BYTES + kk * 256) >> 4),
+                           bd0 + (((g - i) * B_BYTES + kk * 256) >> 4), idesc,
+                           (i == 0 && kk == 0) ? 0u : 1u);
+            }
+            mma_commit(smem_u32(&bar_mma[b]));
+            mma_last = q;
           }
         }
       }
-      __syncthreads();
+      if (fail) {
+        *abort_flag = 1;
+        atomicExch(p.err, 1);
+        if (ld_pend >= 0)
+          mbar_wait(smem_u32(&bar_ld[ld_pend & 1]), (uint32_t)((ld_pend >> 1) & 1), WAIT_NS);
+      }
+      // every MMA of this CTA completes before its TMEM is freed
+      if (mma_last >= 0)
+        mbar_wait(smem_u32(&bar_mma[mma_last & 1]), (uint32_t)((mma_last >> 1) & 1), WAIT_NS);
+    }
+  } else if (warp == WSTAGE) {
+    // ------------------------------------------------------------ stager
+    if (bulk) {
+      uint32_t nst = 0;  // tiles staged
+      long long last_tx = -1;
+      bool fail = false;
+      Row r;
+      for (int row = blockIdx.x; row < p.nrows && !fail; row += gridDim.x) {
+        load_row(p, row, r);
+        const int x0 = r.tx * 128, nrow = min(128, p.ns - x0);
+        const double *hq = p.hch + (size_t)(r.blk - 1) * ms * ms + (size_t)(r.qr - 1) * p.ns +
+                           ms * (size_t)(r.qc - 1) * p.ns;
+        for (int ty = 0; ty < p.nty; ty++) {
+          int np;
+          bool band;
+          tile_products(p, r, ty, np, band);
+          if (np == 0 && !band) continue;
+          const int ty0 = ty * 32, ncol = min(32, p.ns - ty0);
+          // the consumers release the buffers of the previous tile
+          bool ok = *abort_flag == 0 &&
+                    (nst == 0 || mbar_wait(smem_u32(&bar_sfree), (nst - 1) & 1, WAIT_NS));
+          ok = __all_sync(0xffffffffu, ok);
+          if (!ok) {
+            fail = true;
+            break;
+          }
+          const uint32_t tb = smem_u32(&bar_tile);
+          if (lane == 0) {
+            uint32_t bytes = (uint32_t)(ncol * nrow * 8);
+            if (band)
+              for (int t = 0; t < r.nt; t++)
+                bytes += NDB * 8 * (((term_code(r, t) >> 2) & 1) ? ncol : nrow);
+            asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+            mbar_expect_tx(tb, bytes);
+          }
+          __syncwarp();
+          if (lane < ncol)
+            bulk_g2s(smem_u32(shch + (size_t)lane * 128), hq + ms * (size_t)(ty0 + lane) + x0,
+                     (uint32_t)nrow * 8, tb);
+          if (band)
+            for (int k = lane; k < NDB * r.nt; k += 32) {
+              const int t = k / NDB, dd = k % NDB, tc = term_code(r, t);
+              const bool tra = (tc >> 2) & 1;
+              const double *yb =
+                  p.Yb + ((size_t)(tc & 3) * p.nm + (tc >> 3)) * (size_t)p.ns * NDB;
+              bulk_g2s(smem_u32(sband + (size_t)t * NDB * 128 + dd * (tra ? 32 : 128)),
+                       yb + (tra ? ty0 : x0) + (size_t)p.ns * dd,
+                       (uint32_t)(tra ? ncol : nrow) * 8, tb);
+            }
+          last_tx = nst;
+          nst++;
+        }
+      }
+      if (fail && lane == 0) {
+        *abort_flag = 1;
+        atomicExch(p.err, 1);
+      }
+      // the copies of the last staged tile land before the CTA exits
+      if (last_tx >= 0 && lane == 0)
+        mbar_wait(smem_u32(&bar_tile), (uint32_t)(last_tx & 1), WAIT_NS);
+    }
+  } else {
+    // ------------------------------------------------------------ consumers
+    // Thread (lane group lg, column half hf) owns row x of the tile and 16
+    // columns.  Product p scales element (x, y) by 2^(er_p(x) + ec_p(y)); the
+    // thread sums its products exactly in int64 aligned to one exponent, the
+    // largest row + tile-column exponent of the tile's products (right
+    // shifts drop bits below 2^-56 of the largest scale), and converts each
+    // sum to FP64 once.
+    const int lg = warp & 3, hf = warp >> 2, xl = lg * 32 + lane;
+    constexpr uint32_t MAGIC = 0x4B400000u;  // bits of 1.5 * 2^23 (tc::f2i_exact)
+    bool dead = false;
+    uint32_t q = 0, ntile = 0;
+    Row r;
+    long long Iacc[16];
+    for (int row = blockIdx.x; row < p.nrows; row += gridDim.x) {
+      load_row(p, row, r);
+      const int x = r.tx * 128 + xl, x0 = r.tx * 128;
+      const bool row_ok = x < p.ns;
+      const double *hq = p.hch + (size_t)(r.blk - 1) * ms * ms + (size_t)(r.qr - 1) * p.ns +
+                         ms * (size_t)(r.qc - 1) * p.ns;
+      for (int ty = 0; ty < p.nty; ty++) {
+        int np;
+        bool band;
+        const uint32_t codes = tile_products(p, r, ty, np, band);
+        if (np == 0 && !band) continue;
+        const int y0 = ty * 32 + hf * 16, ty0 = ty * 32;
+        double *h = const_cast<double *>(hq) + ms * (size_t)y0 + x;
 #pragma unroll
-      for (int c = 0; c < 16; c++) {
-        const int y = y0 + hf * 16 + c, d = y - x;
-        if (d < -BAND || d > BAND || x >= ns || y >= ns) continue;
-        for (int t = 0; t < pl.nt; t++) {
-          const double *sb = sband + (size_t)t * NDB * 128;
-          tacc[c] += pl.ttra[t] ? sb[(BAND - d) * 32 + (y - y0)] : sb[(d + BAND) * 128 + xl];
+        for (int c = 0; c < 16; c++) Iacc[c] = 0;
+        if (!bulk) {  // odd ns: the consumers stage hch and the band themselves
+#pragma unroll
+          for (int c = 0; c < 16; c++) {
+            const bool ok = row_ok && y0 + c < p.ns;
+            cp_async8(smem_u32(shch + (size_t)(hf * 16 + c) * 128 + xl), ok ? h + ms * c : p.hch,
+                      ok);
+          }
+          if (band) {
+            for (int t = 0; t < r.nt; t++) {
+              const int tc = term_code(r, t);
+              const double *yb =
+                  p.Yb + ((size_t)(tc & 3) * p.nm + (tc >> 3)) * (size_t)p.ns * NDB;
+              double *sb = sband + (size_t)t * NDB * 128;
+              if (!((tc >> 2) & 1)) {  // rows x of y, diagonals y - x
+                for (int e = tid; e < NDB * 128; e += 32 * NCW) {
+                  const int dd = e / 128, rr = x0 + e % 128, yy = rr + dd - BAND;
+                  const bool ok = rr < p.ns && yy >= 0 && yy < p.ns;
+                  cp_async8(smem_u32(sb + e), ok ? yb + rr + (size_t)p.ns * dd : yb, ok);
+                }
+              } else {  // rows y of y, diagonals x - y
+                for (int e = tid; e < NDB * 32; e += 32 * NCW) {
+                  const int dd = e / 32, rr = ty0 + e % 32, xx = rr + dd - BAND;
+                  const bool ok = rr < p.ns && xx >= 0 && xx < p.ns;
+                  cp_async8(smem_u32(sb + e), ok ? yb + rr + (size_t)p.ns * dd : yb, ok);
+                }
+              }
+            }
+          }
+          asm volatile("cp.async.commit_group;\n" ::: "memory");
+        }
+        // per element the exponent the int64 sum is kept at: the largest
+        // row + column exponent of the products added so far
+        int cur[16];
+#pragma unroll
+        for (int c = 0; c < 16; c++) cur[c] = -100000;
+        for (int pc = 0; pc < np; pc++, q++) {
+          const int b = q & 1;
+          const uint32_t n = q >> 1;
+          const int pcode = (codes >> (3 * pc)) & 7, m = pcode >> 2;
+          const int tc = term_code(r, pcode & 3), a = tc & 3, tra = (tc >> 2) & 1;
+          const int *eua = p.eu[a] + (size_t)m * EX;
+          const int *ezs = p.ez + ((size_t)(a * 2 + m) * p.nm + (tc >> 3)) * EX;
+          const int er = tra ? ezs[x] : eua[x];
+          const int *ecol = (tra ? eua : ezs) + y0;
+          if (!dead && *abort_flag) dead = true;
+          bool ok = !dead && mbar_wait(smem_u32(&bar_mma[b]), n & 1, WAIT_NS);
+          ok = __all_sync(0xffffffffu, ok);
+          if (!ok) {
+            if (!dead) {
+              dead = true;
+              *abort_flag = 1;
+              if (lane == 0) atomicExch(p.err, 1);
+            }
+            continue;
+          }
+          fence_after();
+          // I = sum_g D_g 256^(TS-1-g): pairs of orders combined in int32
+          // (|D_2k 256 + D_2k+1| < 2^31), then I = (P0 2^16 + P1) 2^16 + P2
+          long long I[16];
+#pragma unroll
+          for (int c = 0; c < 16; c++) I[c] = 0;
+#pragma unroll
+          for (int k = 0; k < TS / 2; k++) {
+            uint32_t v0[16], v1[16];
+            const uint32_t col = tbase + ((uint32_t)(lg * 32) << 16) +
+                                 (uint32_t)(b * 256 + 2 * k * 32 + hf * 16);
+            tmem_ld16(col, v0);
+            tmem_ld16(col + 32, v1);
+            tmem_wait_ld();
+#pragma unroll
+            for (int c = 0; c < 16; c++) {
+              // bits(D + 1.5 2^23) = D + MAGIC exactly for |D| < 2^22; wrap-around
+              // unsigned arithmetic leaves 256 D_2k + D_2k+1
+              const uint32_t pu =
+                  ((uint32_t)__float_as_uint(__uint_as_float(v0[c]) + 12582912.0f) << 8) +
+                  (uint32_t)__float_as_uint(__uint_as_float(v1[c]) + 12582912.0f) -
+                  257u * MAGIC;
+              I[c] = I[c] * 65536 + (long long)(int)pu;
+            }
+          }
+          fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(smem_u32(&bar_free[b]));
+#pragma unroll
+          for (int c = 0; c < 16; c++) {
+            const int d = (y0 + c) - x, se = er + ecol[c];
+            const bool in =
+                tra ? (m == 0 ? d <= -FAR : d >= FAR) : (m == 0 ? d >= FAR : d <= -FAR);
+            if (in) {
+              if (se > cur[c]) {  // raise the sum to the new exponent
+                const int up = se - cur[c];
+                Iacc[c] = up < 63 ? Iacc[c] >> up : 0;
+                cur[c] = se;
+              }
+              const int sh = cur[c] - se;
+              if (sh < 63) Iacc[c] += I[c] >> sh;
+            }
+          }
+        }
+        // to FP64 (the factor 1/2 of ich == jch in the exponent), near band,
+        // and the write of the tile: one FP64 add per element
+        double val[16];
+#pragma unroll
+        for (int c = 0; c < 16; c++)
+          val[c] = cur[c] > -100000 ? i64_to_f64(Iacc[c], cur[c] - 8 * (TS + 1) - r.half) : 0.0;
+        if (bulk) {
+          const bool ok = dead || mbar_wait(smem_u32(&bar_tile), ntile & 1, WAIT_NS);
+          if (!ok) {
+            dead = true;
+            *abort_flag = 1;
+            atomicExch(p.err, 1);
+          }
+        } else {
+          asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+          if (band) consumers_sync();
+        }
+        if (band) {
+#pragma unroll
+          for (int c = 0; c < 16; c++) {
+            const int y = y0 + c, d = y - x;
+            if (d < -BAND || d > BAND || !row_ok || y >= p.ns) continue;
+            for (int t = 0; t < r.nt; t++) {
+              const double *sb = sband + (size_t)t * NDB * 128;
+              const double bv = ((term_code(r, t) >> 2) & 1) ? sb[(BAND - d) * 32 + (y - ty0)]
+                                                             : sb[(d + BAND) * 128 + xl];
+              val[c] += r.half ? half_f64(bv) : bv;
+            }
+          }
+        }
+        if (row_ok && !dead) {
+#pragma unroll
+          for (int c = 0; c < 16; c++)
+            if (y0 + c < p.ns) h[ms * c] = shch[(size_t)(hf * 16 + c) * 128 + xl] + val[c];
+        }
+        // release the staging buffers
+        if (bulk) {
+          __syncwarp();
+          if (lane == 0) mbar_arrive(smem_u32(&bar_sfree));
+          ntile++;
+        } else if (band) {
+          consumers_sync();
         }
       }
     }
-    if ((pl.np > 0 || pl.band) && x < ns) {
-      const int ms = 2 * ns;
-      double *hb = p.hch + (size_t)(pl.blk - 1) * ms * ms + (size_t)(pl.qr - 1) * ns +
-                   (size_t)ms * (pl.qc - 1) * ns + x;
-#pragma unroll
-      for (int c = 0; c < 16; c++) {
-        const int y = y0 + hf * 16 + c;
-        if (y < ns) {
-          double *h = hb + (size_t)ms * y;
-          *h = *h + (pl.half ? 0.5 * tacc[c] : tacc[c]);
-        }
-      }
-    }
-#pragma unroll
-    for (int c = 0; c < 16; c++) tacc[c] = 0.0;
-  };
-
-  long long item = blockIdx.x;
-  int ci = 0, pc = 0;
-  uint32_t P = 0;
-  if (tid == 0) {
-    make_plan(p, item, sp[0]);
-    if (sp[0].ok && sp[0].np > 0 && !issue(sp[0], 0, 0)) s_abort = 1;
-  }
-  fence_before();
-  __syncthreads();
-  fence_after();
-  while (!s_abort && sp[ci].ok) {
-    const Plan &cur = sp[ci];
-    const bool last = cur.np == 0 || pc == cur.np - 1;
-    if (tid == 0) {
-      if (!last) {
-        if (!issue(cur, pc + 1, P + 1)) s_abort = 1;
-      } else {
-        Plan &nx = sp[ci ^ 1];
-        make_plan(p, item + gridDim.x, nx);
-        if (nx.ok && nx.np > 0 && !issue(nx, 0, P + (cur.np > 0 ? 1u : 0u))) s_abort = 1;
-      }
-    }
-    if (cur.np > 0 && !epilogue(cur, pc, P)) s_abort = 1;
-    if (last) finish(cur);
-    fence_before();
-    __syncthreads();
-    fence_after();
-    if (cur.np > 0) P++;
-    if (last) {
-      ci ^= 1;
-      item += gridDim.x;
-      pc = 0;
-    } else {
-      pc++;
-    }
-  }
-  if (s_abort && tid == 0) {
-    atomicExch(p.err, 1);
-    // bounded waits for this CTA's own copies and MMAs still in flight
-    if (ld_pending >= 0)
-      mbar_wait(smem_u32(&bar_ld[ld_pending & 1]), (uint32_t)((ld_pending >> 1) & 1), WAIT_NS);
-    if (mma_pending >= 0)
-      mbar_wait(smem_u32(&bar_mma[mma_pending & 1]), (uint32_t)((mma_pending >> 1) & 1), WAIT_NS);
   }
   fence_before();
   __syncthreads();
@@ -428,10 +611,43 @@ __global__ void __launch_bounds__(256, 1) k_xfused(const XArgs p) {
 
 }  // namespace
 
+bool build_xquads(int na, const int *ii, const int *jj, const std::vector<int> &mem,
+                  const std::vector<int> &own, const std::vector<SegInfo> &hinfo,
+                  std::vector<XQuad> &out) {
+  for (int os : own) {
+    const SegInfo &si = hinfo[mem[os]];
+    const int ps = si.partner >= 0 ? os + 1 : -1;
+    for (int q = 0; q < 4; q++) {
+      XQuad r{};
+      r.blk = si.blk;
+      r.qr = q % 2 + 1;
+      r.qc = q / 2 + 1;
+      for (int a = 0; a < na; a++)
+        for (int pass = 0; pass < 2; pass++) {
+          const int slot = pass == 0 ? os : ps;
+          if (slot < 0) break;
+          const SegInfo &sj = hinfo[mem[slot]];
+          const bool eq = sj.ich == sj.jch;
+          const bool dir = (sj.ich > sj.jch || eq) && r.qr == ii[a] && r.qc == jj[a];
+          const bool tra = (sj.ich < sj.jch && r.qr == ii[a] && r.qc == jj[a]) ||
+                           (eq && r.qr == jj[a] && r.qc == ii[a]);
+          if (eq) r.half = 1;
+          for (int k = 0; k < 2; k++) {
+            if (!(k == 0 ? dir : tra)) continue;
+            if (r.nt == MAXT) return false;
+            r.term[r.nt++] = a | k << 2 | slot << 3;
+          }
+        }
+      if (r.nt > 0) out.push_back(r);
+    }
+  }
+  return true;
+}
+
 int split_exchange(dbsrg_ctx *c, const SplitExchange &x) {
   const int ns = c->g.ns, nb = c->nbound;
   if (nb < 1 || nb > 32) return set_err(c, DBSRG_EINVAL, "split exchange: 1..32 bound orbitals");
-  if (x.na < 1 || x.na > 4 || x.nm < 1 || x.npq < 1) return DBSRG_OK;
+  if (x.na < 1 || x.na > 4 || x.nm < 1 || x.nxq < 1) return DBSRG_OK;
   cudaStream_t st = c->stream;
   const int ntx = (ns + 127) / 128, NR = 4 * ntx, nty = (ns + 31) / 32;
   const size_t sl = (size_t)NR * TILE;
@@ -440,7 +656,8 @@ int split_exchange(dbsrg_ctx *c, const SplitExchange &x) {
     FarField *f = const_cast<FarField *>(x.far[a]);
     if (f->Ud) continue;
     void *d = nullptr;
-    const size_t bytes = 2 * TS * sl * sizeof(__nv_bfloat16) + 2 * (size_t)NR * 32 * sizeof(int);
+    const size_t bytes =
+        2 * TS * sl * sizeof(__nv_bfloat16) + 2 * (size_t)NR * EXP_PER_ROWTILE * sizeof(int);
     if (cudaMalloc(&d, bytes) != cudaSuccess) {
       cudaGetLastError();
       return set_err(c, DBSRG_ENOMEM, "digit allocation failed");
@@ -451,11 +668,11 @@ int split_exchange(dbsrg_ctx *c, const SplitExchange &x) {
       DBSRG_RUN(c, "k_udigits",
                 k_udigits<<<(unsigned)((NR * 32 + 127) / 128), 128, 0, st>>>(
                     ns, nb, NR, m ? f->Ul : f->U, (__nv_bfloat16 *)f->Ud + (size_t)m * TS * sl,
-                    f->eu + (size_t)m * NR * 32));
+                    f->eu + (size_t)m * NR * EXP_PER_ROWTILE));
   }
   // per chunk: Z digits, exponents, band rows, error word
   const size_t zel = (size_t)x.na * 2 * x.nm * TS * sl;
-  const size_t zex = (size_t)x.na * 2 * x.nm * NR * 32;
+  const size_t zex = (size_t)x.na * 2 * x.nm * NR * EXP_PER_ROWTILE;
   const size_t ybn = (size_t)x.na * x.nm * ns * NDB;
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
   const size_t bytes = al(zel * 2) + al(zex * 4) + al(ybn * 8) + 256;
@@ -499,26 +716,23 @@ int split_exchange(dbsrg_ctx *c, const SplitExchange &x) {
   p.nm = x.nm;
   p.na = x.na;
   p.lower = x.lower;
-  p.nitems = (long long)x.npq * ntx * nty;
+  p.nrows = x.nxq * ntx;
   for (int a = 0; a < x.na; a++) {
     p.Ud[a] = (const __nv_bfloat16 *)x.far[a]->Ud;
     p.eu[a] = x.far[a]->eu;
-    p.ii[a] = x.ii[a];
-    p.jj[a] = x.jj[a];
   }
   p.Zd = Zd;
   p.ez = ez;
   p.Yb = Yb;
-  p.members = x.members;
-  p.pqlist = x.pqlist;
-  p.info = x.info;
+  p.xq = x.xq;
   p.hch = c->hch;
   p.err = err;
-  const size_t smem = 2 * TS * (size_t)(A_BYTES + B_BYTES) + (size_t)MAXT * NDB * 128 * sizeof(double);
+  const size_t smem = 2 * TS * (size_t)(A_BYTES + B_BYTES) +
+                      ((size_t)MAXT * NDB * 128 + 32 * 128) * sizeof(double);
   DBSRG_TRY(c, cudaFuncSetAttribute(k_xfused, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)smem));
-  const long long nblk = std::min<long long>(p.nitems, (long long)std::max(1, c->nsm));
-  DBSRG_RUN(c, "k_xfused", k_xfused<<<(unsigned)nblk, 256, smem, st>>>(p));
+  const int nblk = std::min(p.nrows, std::max(1, c->nsm));
+  DBSRG_RUN(c, "k_xfused", k_xfused<<<(unsigned)nblk, NTHR, smem, st>>>(p));
   int h = 0;
   DBSRG_TRY(c, cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, st));
   DBSRG_TRY(c, cudaStreamSynchronize(st));

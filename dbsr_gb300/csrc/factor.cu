@@ -899,7 +899,6 @@ int factored_contract(dbsrg_ctx *c, const FactorJob &j) {
     SplitExchange x{};
     x.na = j.na;
     x.nm = j.nm;
-    x.nown = j.nown;
     x.lower = j.family == 0 ? 1 : 0;
     for (int a = 0; a < j.na; a++) {
       const int cs = j.icv;
@@ -911,13 +910,10 @@ int factored_contract(dbsrg_ctx *c, const FactorJob &j) {
       if ((rc = get_pairpot_band(c, j.family, j.types[a], j.kpol, cs, j.jp1[a], j.jp2[a],
                                  j.tabs[a], &x.Kb[a])))
         return rc;
-      x.ii[a] = j.ii[a];
-      x.jj[a] = j.jj[a];
     }
     x.members = j.members;
-    x.own = j.own;
-    x.pqlist = j.pqlist;
-    x.npq = j.npq;
+    x.xq = j.xq;
+    x.nxq = j.nxq;
     x.info = j.info;
     x.pairs = j.pairs;
     x.cd = j.cd;

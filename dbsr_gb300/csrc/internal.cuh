@@ -110,6 +110,8 @@ struct dbsrg_ctx {
   size_t tcscratch_bytes = 0;
   void *pscratch = nullptr;   // pair-potential construction (cell sums, cell parts)
   size_t pscratch_bytes = 0;
+  void *lscratch = nullptr;   // work records derived from one list (split exchange)
+  size_t lscratch_bytes = 0;
   // pinned staging for host lists
   void *pinned = nullptr;
   size_t pinned_bytes = 0;
@@ -177,6 +179,7 @@ int ensure_scratch2(dbsrg_ctx *c, size_t bytes);
 int ensure_tscratch(dbsrg_ctx *c, size_t bytes);
 int ensure_tcscratch(dbsrg_ctx *c, size_t bytes);
 int ensure_pscratch(dbsrg_ctx *c, size_t bytes);
+int ensure_lscratch(dbsrg_ctx *c, size_t bytes);
 int ensure_pinned(dbsrg_ctx *c, size_t bytes);
 // frees the far-field vectors, pair potentials and bound rows (they depend
 // on the orbitals and the tables)
@@ -225,34 +228,38 @@ struct FactorJob {
   const double *cd;
   double *Y;         // exchange results [a][slot][ns*ns] (FP64 far field)
   bool split;        // exchange on the tensor cores (split BF16), fused scatter
-  int npq;           // split exchange: (owner slot, quadrant) pairs receiving terms
-  const int *pqlist; //   their codes, owner slot * 4 + quadrant (0..3)
+  int nxq;           // split exchange: (owner block, quadrant) records of the chunk
+  const struct XQuad *xq;
 };
 int factored_contract(dbsrg_ctx *c, const FactorJob &job);
-// exchange.cu-side entry of the split form (exchange_tc.cu)
+// One quadrant of one owner's block in the split exchange and the terms it
+// receives (UPDATE_HS, updates.f90:110-179), in the order of k_scatter_x
+// (atype-major, owner then partner, direct before transposed).  Term code:
+// atype | transposed << 2 | member slot << 3.
+struct XQuad {
+  int blk, qr, qc, nt, half;
+  int term[4];
+  int pad[3];
+};
+static_assert(sizeof(XQuad) == 48, "XQuad is read as three 16-byte vectors");
+// records of every quadrant of the owners of one chunk that receives terms;
+// false if a quadrant would receive more than four
+bool build_xquads(int na, const int *ii, const int *jj, const std::vector<int> &mem,
+                  const std::vector<int> &own, const std::vector<SegInfo> &hinfo,
+                  std::vector<XQuad> &out);
+// exchange_tc.cu entry of the split form
 struct SplitExchange {
-  int na, nm, nown, lower;
+  int na, nm, lower;
   const FarField *far[4];  // far-field vectors (and digit caches) per atype
   const double *Kb[4];     // band pair potentials per atype
-  int ii[4], jj[4];
-  const int *members, *own, *pqlist;
-  int npq;
+  const int *members;
+  const XQuad *xq;
+  int nxq;
   const SegInfo *info;
   const int *pairs;
   const double *cd;
 };
 int split_exchange(dbsrg_ctx *c, const SplitExchange &x);
-// quadrant (qr, qc) of an owner's block receives at least one term of the
-// list (UPDATE_HS): atype quadrants (ii, jj), the owner's channel pair
-// (ich, jch) and its partner's, if any
-inline bool quadrant_has_terms(int qr, int qc, int na, const int *ii, const int *jj, int ich,
-                               int jch, bool partner) {
-  for (int a = 0; a < na; a++) {
-    if (qr == ii[a] && qc == jj[a]) return true;
-    if (ich == jch && !partner && qr == jj[a] && qc == ii[a]) return true;
-  }
-  return false;
-}
 // pairs[e] = bmap[K2]*nbound + bmap[K3]; sets *derr when an orbital is not bound
 int pair_index(dbsrg_ctx *c, int n, const int *k2, const int *k3, int *pairs, int *derr);
 

@@ -70,15 +70,29 @@ __device__ __forceinline__ int f2i_exact(float f) {
   return __float_as_int(f + 12582912.0f) - 0x4B400000;
 }
 
-// exact int64 -> FP64 times 2^sh (far inside the normal range)
-__device__ __forceinline__ double i64_scaled(long long I, int sh) {
+// FP64 of I * 2^sh assembled with integer instructions (the FP64 pipe of
+// this GPU is narrow): normalise |I|, keep its leading 53 bits (truncation,
+// relative error below 2^-52) and set sign and exponent.  Results outside
+// the normal range, which the scales here never produce, go through ldexp.
+__device__ __forceinline__ double i64_to_f64(long long I, int sh) {
   if (I == 0) return 0.0;
-  double d = __ll2double_rn(I);
-  long long b = __double_as_longlong(d);
-  int ex = (int)((b >> 52) & 0x7FF) + sh;
-  if (ex <= 0 || ex >= 0x7FF) return ldexp(d, sh);
-  b = (b & ~(0x7FFLL << 52)) | ((long long)ex << 52);
-  return __longlong_as_double(b);
+  const unsigned long long sgn = (unsigned long long)I & 0x8000000000000000ULL;
+  unsigned long long u = sgn ? 0ULL - (unsigned long long)I : (unsigned long long)I;
+  const int lz = __clzll((long long)u);
+  u <<= lz;                                  // leading bit at position 63
+  const int ex = 63 - lz + sh + 1023;        // biased exponent of the leading bit
+  if (ex <= 0 || ex >= 0x7FF) return ldexp(sgn ? -(double)(u >> 11) : (double)(u >> 11), sh + 11 - lz);
+  const unsigned long long bits =
+      sgn | ((unsigned long long)ex << 52) | ((u >> 11) & 0x000FFFFFFFFFFFFFULL);
+  return __longlong_as_double((long long)bits);
+}
+
+// v / 2 by the exponent field (normal v; zero stays zero)
+__device__ __forceinline__ double half_f64(double v) {
+  const long long b = __double_as_longlong(v);
+  const int ex = (int)((b >> 52) & 0x7FF);
+  if (ex <= 1) return v * 0.5;  // zero and the bottom of the range
+  return __longlong_as_double(b - (1LL << 52));
 }
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
