@@ -187,12 +187,15 @@ class Assembler:
         check(self._h, self._L.dbsrg_timing(self._h, int(enable)), "timing")
 
     def timing_report(self) -> dict:
-        """{kernel: (launches, total ms)} of the launches since timing(True)."""
+        """{kernel: (launches, total ms, algorithmic bytes, algorithmic FLOPs)} of
+        the launches since timing(True); bytes/FLOPs are 0 where a launch
+        states none."""
         import json
 
         buf = C.create_string_buffer(1 << 16)
         check(self._h, self._L.dbsrg_timing_report(self._h, buf, len(buf)), "timing_report")
-        return {k: (int(v[0]), float(v[1])) for k, v in json.loads(buf.value.decode()).items()}
+        return {k: (int(v[0]), float(v[1]), float(v[2]), float(v[3]))
+                for k, v in json.loads(buf.value.decode()).items()}
 
     @property
     def launches(self) -> int:

@@ -817,7 +817,7 @@ int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const 
     if ((rc = copy_in(c, dxq, hxq.data(), sizeof(XQuad) * hxq.size()))) return rc;
   }
   auto run_chunk = [&](const int *mb, int nm, const int *ob, int nown, const XQuad *xq,
-                       int nxq) -> int {
+                       const XQuad *hxq_chunk, int nxq) -> int {
     int rc2;
     if (factored) {
       double *Y = nullptr;
@@ -851,6 +851,7 @@ int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const 
       job.Y = Y;
       job.split = c->precision == DBSRG_SPLIT_BF16;
       job.xq = xq;
+      job.hxq = hxq_chunk;
       job.nxq = nxq;
       return factored_contract(c, job);
     }
@@ -888,7 +889,8 @@ int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const 
   };
   for (const Chunk &ch : chunks)
     if ((rc = run_chunk(members + ch.moff, ch.nm, members + ch.moff + ch.nm, ch.nown,
-                        dxq ? dxq + ch.xoff : nullptr, ch.nxq)))
+                        dxq ? dxq + ch.xoff : nullptr, dxq ? hxq.data() + ch.xoff : nullptr,
+                        ch.nxq)))
       return rc;
   if (icase == 2 && itype == 3) {
     // owner segments in list order

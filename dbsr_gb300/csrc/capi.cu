@@ -244,7 +244,7 @@ int dbsrg_timing_report(dbsrg_ctx *c, char *buf, size_t len) {
   DBSRG_TRY(c, cudaStreamSynchronize(c->stream));
   std::vector<std::string> names;
   std::vector<long long> cnt;
-  std::vector<double> ms;
+  std::vector<double> ms, by, fl;
   for (auto &t : c->tev) {
     float m = 0.f;
     if (cudaEventElapsedTime(&m, t.a, t.b) != cudaSuccess) {
@@ -257,15 +257,19 @@ int dbsrg_timing_report(dbsrg_ctx *c, char *buf, size_t len) {
       names.push_back(t.name);
       cnt.push_back(0);
       ms.push_back(0.0);
+      by.push_back(0.0);
+      fl.push_back(0.0);
     }
     cnt[i]++;
     ms[i] += m;
+    by[i] += t.bytes;
+    fl[i] += t.flops;
   }
   std::string s = "{";
   for (size_t i = 0; i < names.size(); i++) {
-    char tmp[256];
-    snprintf(tmp, sizeof tmp, "%s\"%s\": [%lld, %.6f]", i ? ", " : "", names[i].c_str(), cnt[i],
-             ms[i]);
+    char tmp[320];
+    snprintf(tmp, sizeof tmp, "%s\"%s\": [%lld, %.6f, %.6e, %.6e]", i ? ", " : "",
+             names[i].c_str(), cnt[i], ms[i], by[i], fl[i]);
     s += tmp;
   }
   s += "}";

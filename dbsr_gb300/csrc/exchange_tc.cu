@@ -644,6 +644,33 @@ bool build_xquads(int na, const int *ii, const int *jj, const std::vector<int> &
   return true;
 }
 
+// algorithmic work of one k_xfused launch: the read-modify-write of hch over
+// every tile that receives a product or a band term (16 bytes per element),
+// and the tensor-core FLOPs of its products (42 MMAs of 128 x 32 x 16)
+static void xfused_work(const XQuad *hxq, int nxq, int ns, int lower, double &bytes,
+                        double &flops) {
+  bytes = flops = 0.0;
+  if (!hxq) return;
+  const int ntx = (ns + 127) / 128, nty = (ns + 31) / 32;
+  for (int i = 0; i < nxq; i++) {
+    const XQuad &r = hxq[i];
+    for (int tx = 0; tx < ntx; tx++)
+      for (int ty = 0; ty < nty; ty++) {
+        const int x0 = tx * 128, y0 = ty * 32;
+        const bool up = (y0 + 31) - x0 >= FAR, lo = (x0 + 127) - y0 >= FAR;
+        int np = 0;
+        for (int t = 0; t < r.nt && t < MAXT; t++) {
+          const bool tra = (r.term[t] >> 2) & 1;
+          np += (tra ? lo : up) + (lower && (tra ? up : lo));
+        }
+        const bool band = (y0 + 31) - x0 >= -BAND && y0 - (x0 + 127) <= BAND;
+        if (np == 0 && !band) continue;
+        bytes += 16.0 * std::min(128, ns - x0) * std::min(32, ns - y0);
+        flops += np * (TS * (TS + 1)) * 2.0 * 128 * 32 * 16;
+      }
+  }
+}
+
 int split_exchange(dbsrg_ctx *c, const SplitExchange &x) {
   const int ns = c->g.ns, nb = c->nbound;
   if (nb < 1 || nb > 32) return set_err(c, DBSRG_EINVAL, "split exchange: 1..32 bound orbitals");
@@ -732,7 +759,9 @@ int split_exchange(dbsrg_ctx *c, const SplitExchange &x) {
   DBSRG_TRY(c, cudaFuncSetAttribute(k_xfused, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)smem));
   const int nblk = std::min(p.nrows, std::max(1, c->nsm));
-  DBSRG_RUN(c, "k_xfused", k_xfused<<<(unsigned)nblk, NTHR, smem, st>>>(p));
+  double wbytes = 0.0, wflops = 0.0;
+  if (c->timing) xfused_work(x.hxq, x.nxq, ns, x.lower, wbytes, wflops);
+  DBSRG_RUN_W(c, "k_xfused", wbytes, wflops, k_xfused<<<(unsigned)nblk, NTHR, smem, st>>>(p));
   int h = 0;
   DBSRG_TRY(c, cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, st));
   DBSRG_TRY(c, cudaStreamSynchronize(st));

@@ -913,6 +913,7 @@ int factored_contract(dbsrg_ctx *c, const FactorJob &j) {
     }
     x.members = j.members;
     x.xq = j.xq;
+    x.hxq = j.hxq;
     x.nxq = j.nxq;
     x.info = j.info;
     x.pairs = j.pairs;

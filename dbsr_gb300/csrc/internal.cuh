@@ -121,6 +121,7 @@ struct dbsrg_ctx {
   struct TimedLaunch {
     const char *name;
     cudaEvent_t a, b;
+    double bytes, flops;  // algorithmic work of the launch (0: not stated)
   };
   std::vector<TimedLaunch> tev;
   std::vector<cudaEvent_t> evpool;
@@ -152,8 +153,9 @@ bool sync_check_enabled();
   } while (0)
 
 // Launch a named kernel on the context stream; with timing enabled the
-// launch is bracketed by events (resolved by dbsrg_timing_report).
-#define DBSRG_RUN(ctx, name, ...)                                 \
+// launch is bracketed by events (resolved by dbsrg_timing_report) and its
+// algorithmic bytes and FLOPs, where stated, are recorded with it.
+#define DBSRG_RUN_W(ctx, name, wbytes, wflops, ...)               \
   do {                                                            \
     cudaEvent_t _ea = nullptr;                                    \
     if ((ctx)->timing) {                                          \
@@ -164,10 +166,11 @@ bool sync_check_enabled();
     if ((ctx)->timing) {                                          \
       cudaEvent_t _eb = event_get(ctx);                           \
       cudaEventRecord(_eb, (ctx)->stream);                        \
-      (ctx)->tev.push_back({name, _ea, _eb});                     \
+      (ctx)->tev.push_back({name, _ea, _eb, (double)(wbytes), (double)(wflops)}); \
     }                                                             \
     DBSRG_LAUNCHED(ctx);                                          \
   } while (0)
+#define DBSRG_RUN(ctx, name, ...) DBSRG_RUN_W(ctx, name, 0, 0, __VA_ARGS__)
 
 bool is_device_ptr(const void *p);
 // copies n bytes from a host-or-device pointer into device memory dst
@@ -230,6 +233,7 @@ struct FactorJob {
   bool split;        // exchange on the tensor cores (split BF16), fused scatter
   int nxq;           // split exchange: (owner block, quadrant) records of the chunk
   const struct XQuad *xq;
+  const struct XQuad *hxq;  // host copy of the records (work accounting)
 };
 int factored_contract(dbsrg_ctx *c, const FactorJob &job);
 // One quadrant of one owner's block in the split exchange and the terms it
@@ -253,7 +257,7 @@ struct SplitExchange {
   const FarField *far[4];  // far-field vectors (and digit caches) per atype
   const double *Kb[4];     // band pair potentials per atype
   const int *members;
-  const XQuad *xq;
+  const XQuad *xq, *hxq;  // device records and their host copy
   int nxq;
   const SegInfo *info;
   const int *pairs;

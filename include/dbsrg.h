@@ -53,10 +53,11 @@ enum dbsrg_status {
 enum dbsrg_precision {
   DBSRG_PLAIN_FP64 = 0,  /* the reference's loop structure over the
                             assembled tables, FP64 throughout           */
-  DBSRG_SPLIT_BF16 = 1,  /* cell-factored contraction; far field as
-                            split-BF16 tensor-core products, FP32
-                            accumulation, FP64 recombination; band,
-                            diagonal cells and block sums in FP64       */
+  DBSRG_SPLIT_BF16 = 1,  /* cell-factored contraction; the exchange far
+                            field as split-BF16 tcgen05 products (exact
+                            FP32 slice sums, int64 recombination), fused
+                            with the band and the scatter; tables, pair
+                            potentials, band and block sums in FP64     */
   DBSRG_FACTOR_FP64 = 2  /* the same factored contraction, all FP64      */
 };
 
