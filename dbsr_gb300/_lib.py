@@ -43,6 +43,7 @@ SIGNATURES = [
     ("dbsrg_release_tables", C.c_int, [_vp]),
     ("dbsrg_timing", C.c_int, [_vp, C.c_int]),
     ("dbsrg_timing_report", C.c_int, [_vp, C.c_char_p, C.c_size_t]),
+    ("dbsrg_backward", C.c_int, [_vp, C.c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     ("dbsrg_exchange_segment_noalloc", C.c_int,
      [C.c_int, C.c_int, _vp, _vp, C.c_int, C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, _vp, _vp]),
 ]

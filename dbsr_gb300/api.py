@@ -125,6 +125,25 @@ class Assembler:
                        np.float64)
         check(self._h, self._L.dbsrg_update_hx(self._h, ich, jch, p, float(c)), "update_hx")
 
+    # -- energy functional and its gradient ------------------------------------
+    def backward(self, k, i1, i2, i3, i4, coef, grad: bool = True):
+        """(E, dE/dpq) of E = sum_e coef[e] R^k[e](i1,i2;i3,i4) over the orbitals
+        set by set_orbitals (1-based, bound); dE/dpq has the shape (ns, 2, nbf)
+        in Fortran order, or is None when grad is False."""
+        n = int(len(coef))
+        ptrs, keep = [], []
+        for a, dt in ((k, np.int32), (i1, np.int32), (i2, np.int32), (i3, np.int32),
+                      (i4, np.int32), (coef, np.float64)):
+            p, kk = _ptr(a, dt)
+            ptrs.append(p)
+            keep.append(kk)
+        e = C.c_double(0.0)
+        g = np.zeros((self.ns, 2, self.nbf), order="F") if grad else None
+        rc = self._L.dbsrg_backward(self._h, n, *ptrs, C.byref(e),
+                                    C.c_void_p(g.ctypes.data) if grad else None)
+        check(self._h, rc, "backward")
+        return e.value, g
+
     # -- results --------------------------------------------------------------
     def get_block(self, ich, jch):
         out = np.zeros((self.ms, self.ms), order="F")

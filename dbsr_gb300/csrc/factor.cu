@@ -767,7 +767,7 @@ static int set_smem(dbsrg_ctx *c, const void *fn, size_t smem) {
 
 // direct pair potentials of (family, type, k, case icv) with density
 // components jp1/jp2: Kd[pair][ns*ncol], cached
-static int get_pairpot_direct(dbsrg_ctx *c, int family, int type, int k, int icv, int jp1,
+int get_pairpot_direct(dbsrg_ctx *c, int family, int type, int k, int icv, int jp1,
                               int jp2, const double **out) {
   const long long key = pairpot_key(0, family, type, k, icv, jp1, jp2);
   auto it = c->ppot.find(key);

@@ -264,6 +264,11 @@ struct SplitExchange {
   const double *cd;
 };
 int split_exchange(dbsrg_ctx *c, const SplitExchange &x);
+// Direct pair potentials of table (family, type, k) for convol case icv with
+// density components jp1/jp2: Kd[pair][ns*ncol] over the ordered bound-orbital
+// pairs (pair = a*nbound + b), cached until release_tables/set_orbitals.
+int get_pairpot_direct(dbsrg_ctx *c, int family, int type, int k, int icv, int jp1, int jp2,
+                       const double **out);
 // pairs[e] = bmap[K2]*nbound + bmap[K3]; sets *derr when an orbital is not bound
 int pair_index(dbsrg_ctx *c, int n, const int *k2, const int *k3, int *pairs, int *derr);
 

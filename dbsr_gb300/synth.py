@@ -340,6 +340,61 @@ def small(ns=60, nch=3, mk=3, n_entries=300, breit=True, seed=99, rmax=20.0, z=8
                   occupancy, breit=breit, o_entries=20)
 
 
+@dataclass
+class EnergyWorkload:
+    """E = sum_e coef[e] R^k[e](i1,i2;i3,i4) over bound orbitals pq(ns,2,nbf)."""
+    name: str
+    t: np.ndarray
+    z: float
+    ks: int
+    ksp: int
+    ksq: int
+    pq: np.ndarray
+    ipbs: np.ndarray
+    k: np.ndarray
+    i1: np.ndarray
+    i2: np.ndarray
+    i3: np.ndarray
+    i4: np.ndarray
+    coef: np.ndarray
+
+    @property
+    def ns(self) -> int:
+        return self.t.size - self.ks
+
+
+def energy_workload(name, seed, ns, rmax, z, norb, kmax, n_entries) -> EnergyWorkload:
+    """Random R^k entries over the first ``norb`` target orbitals: k uniform in
+    0..kmax subject to the parity rule of both pairs (l_a + l_c + k and
+    l_b + l_d + k even, the condition of the angular coefficients),
+    coefficients uniform in [-1, 1]."""
+    rng = np.random.Generator(np.random.Philox(seed))
+    ks, ksp, ksq = 9, 8, 9
+    t = knots(ns, rmax, z, ks)
+    orbitals = TARGET_ORBITALS[:norb]
+    pq = orbital_coefficients(t, ks, ksp, ksq, z, orbitals, rng)
+    ls = np.array([l_kappa(kp) for _, kp in orbitals])
+    out = [[], [], [], [], [], []]
+    while len(out[0]) < n_entries:
+        m = 4 * (n_entries - len(out[0])) + 64
+        k = rng.integers(0, kmax + 1, m)
+        a, b, c, d = (rng.integers(1, norb + 1, m) for _ in range(4))
+        ok = ((ls[a - 1] + ls[c - 1] + k) % 2 == 0) & ((ls[b - 1] + ls[d - 1] + k) % 2 == 0)
+        idx = np.flatnonzero(ok)[: n_entries - len(out[0])]
+        for lst, v in zip(out, (k, a, b, c, d, rng.uniform(-1.0, 1.0, m))):
+            lst.extend(v[idx].tolist())
+    k, i1, i2, i3, i4 = (np.asarray(v, dtype=np.int32) for v in out[:5])
+    return EnergyWorkload(name, t, z, ks, ksp, ksq, pq, np.zeros(norb, dtype=np.int32), k, i1,
+                          i2, i3, i4, np.asarray(out[5], dtype=np.float64))
+
+
+def config4(n_entries: int = 50000) -> EnergyWorkload:
+    """ns=300, Z=18, 30 bound orbitals, k=0..8, 5e4 entries of
+    E = sum c R^k(a,b;c,d)."""
+    return energy_workload(f"config4: ns=300 Z=18 30 orbitals k=0..8 {n_entries} entries", 1238,
+                           300, 30.0, 18.0, 30, 8, n_entries)
+
+
 def algorithmic_flops(w: Workload) -> dict:
     """Reference loop FLOPs of the contraction (2 x multiply-adds):
     T_s^2 per direct 's' convol, T_n^2 per 'n' or exchange convol, one

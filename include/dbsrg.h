@@ -116,6 +116,18 @@ int dbsrg_gen_matrix(dbsrg_ctx *ctx, int icase, int itype, int kpol,
 int dbsrg_update_hx(dbsrg_ctx *ctx, int ich, int jch, const double *d,
                     double c);
 
+/* Energy functional and its gradient (the SCF potentials of DBSR_HF /
+ * DBSR_MCHF, hf_matrix.f90:163-324): E = sum_e coef[e] *
+ * R^k[e](i1[e], i2[e]; i3[e], i4[e]) with R^k as rk (dbsr_lib_dbs.f90:
+ * 3981-4022) over the orbitals of dbsrg_set_orbitals (1-based, bound:
+ * ipbs = 0), and, when grad != NULL, dE/dpq in the layout pq(ns,2,nbf)
+ * (zero for orbitals that appear in no entry).  Host or device arrays;
+ * *energy is written on the host.  No counterpart in DBSR_MAT3 itself: the
+ * backward of the assembly's R^k contraction. */
+int dbsrg_backward(dbsrg_ctx *ctx, int n, const int *k, const int *i1,
+                   const int *i2, const int *i3, const int *i4,
+                   const double *coef, double *energy, double *grad);
+
 /* Copies of results (host or device destination). */
 int dbsrg_get_block(dbsrg_ctx *ctx, int ich, int jch, double *out);
 int dbsrg_get_matrix(dbsrg_ctx *ctx, double *hch);

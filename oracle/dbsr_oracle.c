@@ -1057,6 +1057,74 @@ double orc_rk(const orc_grid *g, const double *f1, const double *f2,
   return r;
 }
 
+/* Symmetric band matrix in 's' storage (a(i,ip) holds A(i,i+ip-1)) times a
+   vector, accumulated: out(m) += s * sum_j A(m,j) f(j) -- the BAV product
+   (used by R_data.f90:181, S_data.f90:205) for the symmetric storage. */
+static void band_sym_mv(int ns, int ks, const double *a, const double *f, double s,
+                        double *out) {
+  for (int m = 1; m <= ns; m++) {
+    double acc = 0.0;
+    for (int j = imax(1, m - ks + 1); j <= imin(ns, m + ks - 1); j++) {
+      int lo = imin(m, j), ip = (m > j ? m - j : j - m) + 1;
+      acc = acc + A2(a, lo, ip, ns) * f[j - 1];
+    }
+    out[m - 1] = out[m - 1] + s * acc;
+  }
+}
+
+/* E = sum_e coef[e] R^k[e](i1,i2;i3,i4), R^k as in rk (dbsr_lib_dbs.f90:
+   3981-4022), and dE/d pq(ns,2,nbf).  R^k is bilinear in the pair densities
+   of the two electrons, so its derivative with respect to a function of one
+   electron is the potential of the other electron's pair density (convol
+   case 1 for electron 1, case 2 for electron 2) applied to the partner
+   function: the direct potentials DBSR_HF builds (hf_matrix.f90:163-324).
+   Orbitals are 1-based indices into pq; R tables are built once per (k,type). */
+double orc_rk_energy_grad(const orc_grid *g, int n, const int *kk, const int *i1,
+                          const int *i2, const int *i3, const int *i4, const double *coef,
+                          const double *pq, int nbf, double *grad) {
+  const int ns = g->ns, ks = g->ks;
+  const size_t nb = (size_t)ns * ks, nt = (size_t)ns * ns * ks * ks;
+  int kmax = 0;
+  for (int e = 0; e < n; e++) kmax = imax(kmax, kk[e]);
+  double **tab = (double **)calloc((size_t)(kmax + 1) * 4, sizeof(double *));
+  double *d1 = (double *)malloc(sizeof(double) * nb), *d2 = (double *)malloc(sizeof(double) * nb);
+  double *a1 = (double *)malloc(sizeof(double) * (size_t)ns * ns);
+  double *a2 = (double *)malloc(sizeof(double) * (size_t)ns * ns);
+  if (grad) memset(grad, 0, sizeof(double) * (size_t)ns * 2 * nbf);
+  /* types in rk's order with the bases of electron 1 (A) and 2 (B): 1 P, 2 Q */
+  static const int types[4] = {0, 1, 3, 2}, ca[4] = {1, 2, 2, 1}, cb[4] = {1, 2, 1, 2};
+  double E = 0.0;
+  for (int e = 0; e < n; e++) {
+    const int k = kk[e];
+    const double *f1 = pq + (size_t)2 * ns * (i1[e] - 1), *f2 = pq + (size_t)2 * ns * (i2[e] - 1);
+    const double *f3 = pq + (size_t)2 * ns * (i3[e] - 1), *f4 = pq + (size_t)2 * ns * (i4[e] - 1);
+    double r = 0.0;
+    for (int q = 0; q < 4; q++) {
+      const int t = types[q], A = ca[q] - 1, B = cb[q] - 1;
+      double **tp = &tab[(size_t)k * 4 + t];
+      if (!*tp) {
+        *tp = (double *)malloc(sizeof(double) * nt);
+        orc_mrk(g, t, k, *tp);
+      }
+      orc_density(ns, ks, d1, f1 + (size_t)ns * A, f3 + (size_t)ns * A, 's');
+      orc_density(ns, ks, d2, f2 + (size_t)ns * B, f4 + (size_t)ns * B, 's');
+      orc_convol(ns, ks, ks, *tp, a2, d1, 2, 's', 's');
+      r = r + orc_sum_amb(ns, ks, a2, d2, 's');
+      if (!grad) continue;
+      orc_convol(ns, ks, ks, *tp, a1, d2, 1, 's', 's');
+      const double c = coef[e];
+      band_sym_mv(ns, ks, a1, f3 + (size_t)ns * A, c, grad + (size_t)2 * ns * (i1[e] - 1) + (size_t)ns * A);
+      band_sym_mv(ns, ks, a1, f1 + (size_t)ns * A, c, grad + (size_t)2 * ns * (i3[e] - 1) + (size_t)ns * A);
+      band_sym_mv(ns, ks, a2, f4 + (size_t)ns * B, c, grad + (size_t)2 * ns * (i2[e] - 1) + (size_t)ns * B);
+      band_sym_mv(ns, ks, a2, f2 + (size_t)ns * B, c, grad + (size_t)2 * ns * (i4[e] - 1) + (size_t)ns * B);
+    }
+    E = E + coef[e] * r;
+  }
+  for (int i = 0; i < (kmax + 1) * 4; i++) free(tab[i]);
+  free(tab); free(d1); free(d2); free(a1); free(a2);
+  return E;
+}
+
 /* ------------------------------------------------------------------ */
 /* DBSR_MAT3 matrix structures */
 orc_mat *orc_mat_new(const orc_grid *g, int nbf, const double *pq,

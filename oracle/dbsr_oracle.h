@@ -79,6 +79,12 @@ double orc_quadr(const orc_grid *g, const double *fi, const double *fj,
                  int m);
 double orc_rk(const orc_grid *g, const double *f1, const double *f2,
               const double *f3, const double *f4, int k);
+/* E = sum_e coef[e] R^k[e](i1,i2;i3,i4) over pq(ns,2,nbf) (1-based orbitals)
+   and, when grad != NULL, dE/dpq(ns,2,nbf) from the potentials of the pair
+   densities */
+double orc_rk_energy_grad(const orc_grid *g, int n, const int *k, const int *i1,
+                          const int *i2, const int *i3, const int *i4,
+                          const double *coef, const double *pq, int nbf, double *grad);
 
 /* ---- level 3: matrix structures and dispatch (DBSR_MAT3) ---- */
 typedef struct orc_mat {

@@ -65,6 +65,9 @@ def lib():
         L.orc_quadr.argtypes = [C.POINTER(_Grid), _dp, _dp, C.c_int]
         L.orc_rk.restype = C.c_double
         L.orc_rk.argtypes = [C.POINTER(_Grid), _dp, _dp, _dp, _dp, C.c_int]
+        L.orc_rk_energy_grad.restype = C.c_double
+        L.orc_rk_energy_grad.argtypes = [C.POINTER(_Grid), C.c_int, _ip, _ip, _ip, _ip, _ip, _dp,
+                                         _dp, C.c_int, _dp]
         L.orc_mat_new.restype = C.c_void_p
         L.orc_mat_new.argtypes = [C.POINTER(_Grid), C.c_int, _dp, _ip, C.c_int, _ip, C.c_int,
                                   _dp, C.c_int, _dp]
@@ -178,6 +181,17 @@ class Grid:
 
     def rk(self, f1, f2, f3, f4, k: int) -> float:
         return lib().orc_rk(self._p, _d(f64(f1)), _d(f64(f2)), _d(f64(f3)), _d(f64(f4)), k)
+
+    def rk_energy_grad(self, k, i1, i2, i3, i4, coef, pq, grad: bool = True):
+        """(E, dE/dpq) of E = sum_e coef[e] R^k[e](i1,i2;i3,i4) (1-based orbitals)."""
+        pq = f64(pq)
+        nbf = pq.size // (2 * self.ns)
+        ints = [np.ascontiguousarray(x, dtype=np.int32) for x in (k, i1, i2, i3, i4)]
+        c = np.ascontiguousarray(coef, dtype=np.float64)
+        g = np.zeros((self.ns, 2, nbf), order="F") if grad else None
+        E = lib().orc_rk_energy_grad(self._p, len(c), *[x.ctypes.data_as(_ip) for x in ints],
+                                     _d(c), _d(pq), nbf, _d(g) if grad else None)
+        return E, g
 
     def v_ch(self, pq_b) -> np.ndarray:
         v = np.zeros(self.ms)
