@@ -19,6 +19,14 @@ STATUS = {0: "OK", -1: "EINVAL", -2: "ECUDA", -3: "ENOMEM", -4: "ERANGE", -5: "E
           -6: "ETIMEOUT"}
 
 # (name, restype, argtypes) for every entry point of include/dbsrg.h
+class ListDesc(C.Structure):
+    """dbsrg_list of include/dbsrg.h"""
+
+    _fields_ = [("icase", C.c_int), ("itype", C.c_int), ("kpol", C.c_int), ("ncdata", C.c_int),
+                ("ipt", C.c_void_p), ("k1", C.c_void_p), ("k2", C.c_void_p),
+                ("k3", C.c_void_p), ("k4", C.c_void_p), ("cdata", C.c_void_p)]
+
+
 SIGNATURES = [
     ("dbsrg_create", C.c_int, [C.POINTER(_vp), _vp]),
     ("dbsrg_destroy", C.c_int, [_vp]),
@@ -43,6 +51,7 @@ SIGNATURES = [
     ("dbsrg_release_tables", C.c_int, [_vp]),
     ("dbsrg_timing", C.c_int, [_vp, C.c_int]),
     ("dbsrg_timing_report", C.c_int, [_vp, C.c_char_p, C.c_size_t]),
+    ("dbsrg_gen_batch", C.c_int, [C.c_int, _vp, _vp, _vp]),
     ("dbsrg_backward", C.c_int, [_vp, C.c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     ("dbsrg_exchange_segment_noalloc", C.c_int,
      [C.c_int, C.c_int, _vp, _vp, C.c_int, C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, _vp, _vp]),

@@ -222,3 +222,33 @@ class Assembler:
 
     def sync(self):
         check(self._h, self._L.dbsrg_sync(self._h), "sync")
+
+
+def gen_batch(assemblers, lists_per_assembler):
+    """dbsrg_gen_batch: every assembler's lists (icase, itype, kpol, k1, k2, k3,
+    k4, cdata[, ipt]) through Gen_matrix, the assemblers concurrently."""
+    L = load()
+    descs, keep, counts = [], [], []
+    for lists in lists_per_assembler:
+        counts.append(len(lists))
+        for item in lists:
+            icase, itype, kpol, k1, k2, k3, k4, cd = item[:8]
+            ipt = item[8] if len(item) > 8 else None
+            ptrs = []
+            for a, dt in ((ipt, np.int32), (k1, np.int32), (k2, np.int32), (k3, np.int32),
+                          (k4, np.int32), (cd, np.float64)):
+                p, kk = _ptr(a, dt)
+                ptrs.append(p.value if p is not None else None)
+                keep.append(kk)
+            descs.append(_lib.ListDesc(icase, itype, kpol, int(len(k1)), *ptrs))
+    n = len(assemblers)
+    arr = (_lib.ListDesc * max(1, len(descs)))(*descs)
+    ctxs = (C.c_void_p * max(1, n))(*[a._h.value for a in assemblers])
+    cnt = (C.c_int * max(1, n))(*counts)
+    rc = L.dbsrg_gen_batch(n, ctxs, cnt, arr)
+    if rc != 0:
+        for a in assemblers:
+            msg = L.dbsrg_last_error(a._h).decode()
+            if msg:
+                check(a._h, rc, "gen_batch")
+        check(None, rc, "gen_batch")

@@ -2,6 +2,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <new>
+#include <thread>
 
 #include "internal.cuh"
 
@@ -390,6 +391,38 @@ int dbsrg_gen_matrix(dbsrg_ctx *c, int icase, int itype, int kpol, int ncdata, c
   if (!k1 || !k2 || !k3 || !cdata) return set_err(c, DBSRG_EINVAL, "null list pointer");
   cudaSetDevice(c->device);
   return gen_matrix_plain(c, icase, itype, kpol, ncdata, ipt, k1, k2, k3, k4, cdata);
+}
+
+int dbsrg_gen_batch(int nctx, dbsrg_ctx *const *ctxs, const int *nlists,
+                    const dbsrg_list *lists) {
+  if (nctx < 0 || (nctx > 0 && (!ctxs || !nlists))) return DBSRG_EINVAL;
+  std::vector<size_t> off((size_t)nctx + 1, 0);
+  for (int i = 0; i < nctx; i++) {
+    if (!ctxs[i] || nlists[i] < 0) return DBSRG_EINVAL;
+    off[i + 1] = off[i] + (size_t)nlists[i];
+  }
+  if (off[nctx] > 0 && !lists) return DBSRG_EINVAL;
+  for (int i = 0; i < nctx; i++)
+    for (int j = i + 1; j < nctx; j++)
+      if (ctxs[i] == ctxs[j]) return set_err(ctxs[i], DBSRG_EINVAL, "gen_batch: context twice");
+  std::vector<int> rc((size_t)nctx, DBSRG_OK);
+  auto work = [&](int i) {
+    dbsrg_ctx *c = ctxs[i];
+    for (size_t l = off[i]; l < off[i + 1] && rc[i] == DBSRG_OK; l++) {
+      const dbsrg_list &L = lists[l];
+      rc[i] = dbsrg_gen_matrix(c, L.icase, L.itype, L.kpol, L.ncdata, L.ipt, L.k1, L.k2, L.k3,
+                               L.k4, L.cdata);
+    }
+  };
+  // one host thread per context (each with its own stream): the host-side
+  // list handling of one block overlaps the kernels of the others
+  std::vector<std::thread> th;
+  for (int i = 1; i < nctx; i++) th.emplace_back(work, i);
+  if (nctx > 0) work(0);
+  for (auto &t : th) t.join();
+  for (int i = 0; i < nctx; i++)
+    if (rc[i] != DBSRG_OK) return rc[i];
+  return DBSRG_OK;
 }
 
 int dbsrg_update_hx(dbsrg_ctx *c, int ich, int jch, const double *d, double cc) {

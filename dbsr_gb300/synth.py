@@ -340,6 +340,28 @@ def small(ns=60, nch=3, mk=3, n_entries=300, breit=True, seed=99, rmax=20.0, z=8
                   occupancy, breit=breit, o_entries=20)
 
 
+def config3(nblocks: int = 64, nch_max: int = 300, rows_entries: float = 1e4,
+            seed: int = 1237) -> list:
+    """Batched form: ``nblocks`` independent J-parity blocks, each with its own
+    grid (ns uniform in 150..450, r_max=40, Z=26), the 20 target orbitals
+    projected on it, channel counts log-uniform in 10..nch_max, k=0..8, and
+    about ``rows_entries`` entries per channel-pair row (nch * rows_entries
+    per block) over 5% of the (channel pair, k) slots.  The full size
+    (nch up to 300) exceeds one GPU's memory in the reference layout; the
+    arguments scale it."""
+    rng = np.random.Generator(np.random.Philox(seed))
+    out = []
+    for b in range(nblocks):
+        ns = int(rng.integers(150, 451))
+        nch = int(round(math.exp(rng.uniform(math.log(10), math.log(nch_max)))))
+        kap = [int(k) * int(s) for k, s in zip(rng.integers(1, 7, nch), rng.choice([-1, 1], nch))]
+        out.append(_build(f"config3 block {b}: ns={ns} nch={nch} k=0..8", seed + 17 * (b + 1), ns,
+                          40.0, 26.0, TARGET_ORBITALS[:20], kap, 8,
+                          max(1, int(rows_entries * nch)), 0.05, breit=True,
+                          o_entries=max(1, nch)))
+    return out
+
+
 @dataclass
 class EnergyWorkload:
     """E = sum_e coef[e] R^k[e](i1,i2;i3,i4) over bound orbitals pq(ns,2,nbf)."""

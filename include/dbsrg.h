@@ -111,6 +111,23 @@ int dbsrg_gen_matrix(dbsrg_ctx *ctx, int icase, int itype, int kpol,
                      const int *k2, const int *k3, const int *k4,
                      const double *cdata);
 
+/* One coefficient list, as for dbsrg_gen_matrix. */
+typedef struct dbsrg_list {
+  int icase, itype, kpol, ncdata;
+  const int *ipt, *k1, *k2, *k3, *k4;
+  const double *cdata;
+} dbsrg_list;
+
+/* A batch of independent symmetry blocks (J-parity partial waves), one
+ * context each with its own grid, orbitals and matrix: context i's lists
+ * are lists[sum(nlists[0..i-1]) ... + nlists[i] - 1], processed in order as
+ * by dbsrg_gen_matrix; the contexts run concurrently (one host thread and
+ * one CUDA stream each).  Returns the first nonzero status by context
+ * index; dbsrg_last_error of that context holds the message.  No
+ * counterpart in DBSR_MAT3, which runs one partial wave per process. */
+int dbsrg_gen_batch(int nctx, dbsrg_ctx *const *ctxs, const int *nlists,
+                    const dbsrg_list *lists);
+
 /* UPDATE_HX(ich,jch,d,C) (updates.f90:79-106): add C*d (d is ms x ms,
  * host or device) to the block of channel pair (ich,jch). */
 int dbsrg_update_hx(dbsrg_ctx *ctx, int ich, int jch, const double *d,
