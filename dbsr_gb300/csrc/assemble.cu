@@ -547,15 +547,6 @@ __global__ void k_update_hx(int ms, int ich, int jch, const double *d, double cc
 }  // namespace
 
 // ---------------------------------------------------------------------------
-static int rd_err(dbsrg_ctx *c, int *derr) {
-  int h = 0;
-  DBSRG_TRY(c, cudaMemcpyAsync(&h, derr, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-  DBSRG_TRY(c, cudaStreamSynchronize(c->stream));
-  if (h == 1) return set_err(c, DBSRG_ERANGE, "channel or orbital index out of range in list");
-  if (h == 2) return set_err(c, DBSRG_ERANGE, "channel pair has no block in icc");
-  return DBSRG_OK;
-}
-
 int update_hx(dbsrg_ctx *c, int ich, int jch, const double *d, double cc) {
   const int ms = c->g.ms;
   if (!c->hch) return set_err(c, DBSRG_ESTATE, "no matrix allocated");
@@ -611,7 +602,7 @@ int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const 
   double *lcd = (double *)take(dbytes);
   int *lpair = (int *)take(ibytes);  // factored path: bound-orbital pair of each entry
   int *seg_start = (int *)take(sizeof(int) * (size_t)(n + 2));
-  int *dscal = (int *)take(64);  // [0]=nseg [1]=err
+  int *dscal = (int *)take(64);  // [0]=nseg [1]=err [2]=blocks touched [3]=pair err
   SegInfo *info = (SegInfo *)take(sizeof(SegInfo) * (size_t)(n + 1));
   int *owners = (int *)take(sizeof(int) * (size_t)(n + 1));
   // per chunk: member segment ids, owner slots and (split exchange) the
@@ -643,10 +634,12 @@ int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const 
               k_group_entries<<<1, 1, 0, st>>>(n, lk1, lk2, lcd, c->ipbs, c->nbf, c->icc, c->nch,
                                                c->iicc, bcount, bstart, order, eblk, tlist,
                                                dscal + 2, dscal + 1));
-    if ((rc = rd_err(c, dscal + 1))) return rc;
-    int ntouched = 0;
-    DBSRG_TRY(c, cudaMemcpyAsync(&ntouched, dscal + 2, sizeof(int), cudaMemcpyDeviceToHost, st));
+    int ho[3] = {0, 0, 0};  // -, error, blocks touched
+    DBSRG_TRY(c, cudaMemcpyAsync(ho, dscal, 3 * sizeof(int), cudaMemcpyDeviceToHost, st));
     DBSRG_TRY(c, cudaStreamSynchronize(st));
+    if (ho[1] == 1) return set_err(c, DBSRG_ERANGE, "channel or orbital index out of range in list");
+    if (ho[1] == 2) return set_err(c, DBSRG_ERANGE, "channel pair has no block in icc");
+    const int ntouched = ho[2];
     if (ntouched < 0 || ntouched > c->iicc) return set_err(c, DBSRG_ECUDA, "inconsistent block list");
     if (ntouched > 0) {
       dim3 grid((unsigned)(((size_t)ms * ms + 255) / 256), (unsigned)ntouched);
@@ -658,16 +651,17 @@ int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const 
     return DBSRG_OK;
   }
 
-  // ---- 2. segments
+  // ---- 2. segments (orbital check and segment count read back together)
   DBSRG_RUN(c, "k_check_orbitals", k_check_orbitals<<<(n + 255) / 256, 256, 0, st>>>(n, lk2, lk3, c->nbf, dscal + 1));
-  if ((rc = rd_err(c, dscal + 1))) return rc;
   DBSRG_RUN(c, "k_segments", k_segments<<<1, 1024, 0, st>>>(n, lk1, seg_start, dscal));
-  int nseg = 0;
-  DBSRG_TRY(c, cudaMemcpyAsync(&nseg, dscal, sizeof(int), cudaMemcpyDeviceToHost, st));
+  int hs[4] = {0, 0, 0, 0};  // nseg, error, -, bound-pair error
+  DBSRG_TRY(c, cudaMemcpyAsync(hs, dscal, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
   DBSRG_TRY(c, cudaStreamSynchronize(st));
+  if (hs[1]) return set_err(c, DBSRG_ERANGE, "channel or orbital index out of range in list");
+  const int nseg = hs[0];
+  if (nseg < 1 || nseg > n) return set_err(c, DBSRG_ECUDA, "inconsistent segment count");
   DBSRG_RUN(c, "k_seg_info", k_seg_info<<<(nseg + 127) / 128, 128, 0, st>>>(nseg, seg_start, lk1, c->nch, c->iicc, c->icc,
                                                  info, dscal + 1));
-  if ((rc = rd_err(c, dscal + 1))) return rc;
 
   // ---- 3. contraction set-up per case
   DensSpec dsp{};
@@ -755,16 +749,17 @@ int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const 
   if (factored) {
     // the factored contraction works with ordered pairs of bound orbitals
     if (c->nbound < 1) return set_err(c, DBSRG_ESTATE, "no bound orbitals (ipbs = 0)");
-    if ((rc = pair_index(c, n, lk2, lk3, lpair, dscal + 1))) return rc;
-    int h = 0;
-    DBSRG_TRY(c, cudaMemcpyAsync(&h, dscal + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
-    DBSRG_TRY(c, cudaStreamSynchronize(st));
-    if (h) return set_err(c, DBSRG_EINVAL, "factored contraction: K2/K3 must be bound orbitals");
+    if ((rc = pair_index(c, n, lk2, lk3, lpair, dscal + 3))) return rc;
   }
+  // segment table, segment errors and bound-pair errors in one read-back
   std::vector<SegInfo> hinfo(nseg);
+  DBSRG_TRY(c, cudaMemcpyAsync(hs, dscal, 4 * sizeof(int), cudaMemcpyDeviceToHost, st));
   DBSRG_TRY(c, cudaMemcpyAsync(hinfo.data(), info, sizeof(SegInfo) * nseg,
                                cudaMemcpyDeviceToHost, st));
   DBSRG_TRY(c, cudaStreamSynchronize(st));
+  if (hs[1] == 1) return set_err(c, DBSRG_ERANGE, "channel or orbital index out of range in list");
+  if (hs[1] == 2) return set_err(c, DBSRG_ERANGE, "channel pair has no block in icc");
+  if (hs[3]) return set_err(c, DBSRG_EINVAL, "factored contraction: K2/K3 must be bound orbitals");
   for (int s = 0; s < nseg; s++) {
     const SegInfo &si = hinfo[s];
     if (si.start < 0 || si.end > n || si.start >= si.end || si.blk < 1 || si.blk > c->iicc ||
@@ -908,5 +903,16 @@ int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const 
     }
   }
   DBSRG_TRY(c, cudaStreamSynchronize(st));
+  if (c->kerr) {  // bounded waits of the tensor-core kernels
+    int h = 0;
+    DBSRG_TRY(c, cudaMemcpyAsync(&h, c->kerr, sizeof(int), cudaMemcpyDeviceToHost, st));
+    DBSRG_TRY(c, cudaStreamSynchronize(st));
+    if (h) {
+      DBSRG_TRY(c, cudaMemsetAsync(c->kerr, 0, sizeof(int), st));
+      DBSRG_TRY(c, cudaStreamSynchronize(st));
+      if (h == 1) return set_err(c, DBSRG_ETIMEOUT, "tensor-core exchange: a wait ran out");
+      return set_err(c, DBSRG_ECUDA, "tensor-core exchange: inconsistent tile terms");
+    }
+  }
   return DBSRG_OK;
 }

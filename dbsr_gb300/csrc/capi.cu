@@ -214,6 +214,7 @@ int dbsrg_destroy(dbsrg_ctx *c) {
   if (c->tcscratch) cudaFree(c->tcscratch);
   if (c->pscratch) cudaFree(c->pscratch);
   if (c->lscratch) cudaFree(c->lscratch);
+  if (c->kerr) cudaFree(c->kerr);
   if (c->bmap) cudaFree(c->bmap);
   if (c->b2o) cudaFree(c->b2o);
   if (c->pinned) cudaFreeHost(c->pinned);

@@ -702,15 +702,17 @@ int split_exchange(dbsrg_ctx *c, const SplitExchange &x) {
   const size_t zex = (size_t)x.na * 2 * x.nm * NR * EXP_PER_ROWTILE;
   const size_t ybn = (size_t)x.na * x.nm * ns * NDB;
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
-  const size_t bytes = al(zel * 2) + al(zex * 4) + al(ybn * 8) + 256;
+  const size_t bytes = al(zel * 2) + al(zex * 4) + al(ybn * 8);
   int rc = ensure_tcscratch(c, bytes);
   if (rc) return rc;
   char *q = (char *)c->tcscratch;
   __nv_bfloat16 *Zd = (__nv_bfloat16 *)q;
   int *ez = (int *)(q + al(zel * 2));
   double *Yb = (double *)(q + al(zel * 2) + al(zex * 4));
-  int *err = (int *)(q + al(zel * 2) + al(zex * 4) + al(ybn * 8));
-  DBSRG_TRY(c, cudaMemsetAsync(err, 0, sizeof(int), st));
+  if (!c->kerr) {  // read and cleared at the end of the Gen_matrix call
+    DBSRG_TRY(c, cudaMalloc((void **)&c->kerr, sizeof(int)));
+    DBSRG_TRY(c, cudaMemsetAsync(c->kerr, 0, sizeof(int), st));
+  }
   ZArgs z{};
   z.ns = ns;
   z.nb = nb;
@@ -753,7 +755,7 @@ int split_exchange(dbsrg_ctx *c, const SplitExchange &x) {
   p.Yb = Yb;
   p.xq = x.xq;
   p.hch = c->hch;
-  p.err = err;
+  p.err = c->kerr;
   const size_t smem = 2 * TS * (size_t)(A_BYTES + B_BYTES) +
                       ((size_t)MAXT * NDB * 128 + 32 * 128) * sizeof(double);
   DBSRG_TRY(c, cudaFuncSetAttribute(k_xfused, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -762,10 +764,5 @@ int split_exchange(dbsrg_ctx *c, const SplitExchange &x) {
   double wbytes = 0.0, wflops = 0.0;
   if (c->timing) xfused_work(x.hxq, x.nxq, ns, x.lower, wbytes, wflops);
   DBSRG_RUN_W(c, "k_xfused", wbytes, wflops, k_xfused<<<(unsigned)nblk, NTHR, smem, st>>>(p));
-  int h = 0;
-  DBSRG_TRY(c, cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, st));
-  DBSRG_TRY(c, cudaStreamSynchronize(st));
-  if (h == 1) return set_err(c, DBSRG_ETIMEOUT, "tensor-core exchange: a completion wait ran out");
-  if (h) return set_err(c, DBSRG_ECUDA, "tensor-core exchange: inconsistent tile terms");
   return DBSRG_OK;
 }

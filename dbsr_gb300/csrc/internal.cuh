@@ -112,6 +112,9 @@ struct dbsrg_ctx {
   size_t pscratch_bytes = 0;
   void *lscratch = nullptr;   // work records derived from one list (split exchange)
   size_t lscratch_bytes = 0;
+  // error word of the tensor-core kernels (bounded waits), read at the end
+  // of each Gen_matrix call
+  int *kerr = nullptr;
   // pinned staging for host lists
   void *pinned = nullptr;
   size_t pinned_bytes = 0;

@@ -586,7 +586,8 @@ int get_band_table(dbsrg_ctx *c, int family, int type, int k, const double **out
 // (QUADR_PQ at R_data.f90:224, which selects the component by atype).
 // First the banded matrix G(i,i+d) = sum over intervals and Gauss points of
 // r^k w B_i B_{i+d} (d = 0..kx-1) per component, then quad(a,b,comp) =
-// sum_{i,j} G(i,j) p_a(i) p_b(j) with one warp per (a,b,comp).
+// sum_{i,j} G(i,j) p_a(i) p_b(j) as W = G P per orbital and the products
+// P^T W of all orbital pairs.
 __global__ void k_rk_gram(int ns, int nv, int ks, int kx, int k, const double *bs,
                           const double *gr, const double *grw, double *G) {
   int q = blockIdx.x * blockDim.x + threadIdx.x;
@@ -610,27 +611,49 @@ __global__ void k_rk_gram(int ns, int nv, int ks, int kx, int k, const double *b
   G[q] = acc;
 }
 
-__global__ void k_quad(int nbf, int ns, int ksp, int ksq, const double *pq, const double *GP,
-                       const double *GQ, double *quad) {
-  int warp = (blockIdx.x * blockDim.x + threadIdx.x) / 32, lane = threadIdx.x % 32;
-  if (warp >= nbf * nbf * 2) return;
-  int a = warp % nbf, b = (warp / nbf) % nbf, comp = warp / (nbf * nbf);
+// W(b, comp)(i) = sum_j G(i,j) p_b(j) over the symmetric band G (d = 0..kx-1
+// stored as G(i, i+d))
+__global__ void k_quad_w(int nbf, int ns, int ksp, int ksq, const double *pq, const double *GP,
+                         const double *GQ, double *W) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= 2 * nbf * ns) return;
+  const int i = q % ns, b = (q / ns) % nbf, comp = q / (ns * nbf);
   const int kx = comp == 0 ? ksp : ksq;
   const double *G = comp == 0 ? GP : GQ;
-  const double *pa = pq + (size_t)ns * comp + (size_t)2 * ns * a;
   const double *pb = pq + (size_t)ns * comp + (size_t)2 * ns * b;
-  double acc = 0.0;
-  for (int i = lane; i < ns; i += 32) {
-    double s = G[i] * pb[i];  // d = 0
-    for (int d = 1; d < kx && i + d < ns; d++) {
-      double g = G[(size_t)i + (size_t)ns * d];
-      s += g * pb[i + d];
-      acc += g * pb[i] * pa[i + d];
-    }
-    acc += pa[i] * s;
+  double s = G[i] * pb[i];
+  for (int d = 1; d < kx; d++) {
+    if (i + d < ns) s += G[(size_t)i + (size_t)ns * d] * pb[i + d];
+    if (i - d >= 0) s += G[(size_t)(i - d) + (size_t)ns * d] * pb[i - d];
   }
-  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-  if (lane == 0) quad[warp] = acc;
+  W[q] = s;
+}
+
+// quad(a, b, comp) = sum_i p_a(i) W(b, comp)(i): 32 x 32 tiles of (a, b)
+__global__ void k_quad_dot(int nbf, int ns, const double *pq, const double *W, double *quad) {
+  __shared__ double sa[32][33], sw[32][33];
+  const int comp = blockIdx.z, a0 = blockIdx.x * 32, b0 = blockIdx.y * 32;
+  const int tx = threadIdx.x % 32, ty = threadIdx.x / 32;  // 256 threads: 8 rows
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int i0 = 0; i0 < ns; i0 += 32) {
+    for (int r = ty; r < 32; r += 8) {
+      const int a = a0 + r, b = b0 + r, i = i0 + tx;
+      sa[r][tx] = (a < nbf && i < ns) ? pq[(size_t)i + (size_t)ns * comp + (size_t)2 * ns * a] : 0.0;
+      sw[r][tx] = (b < nbf && i < ns) ? W[(size_t)i + (size_t)ns * (b + (size_t)nbf * comp)] : 0.0;
+    }
+    __syncthreads();
+    for (int k = 0; k < 4; k++) {
+      const int ar = ty + 8 * k;
+      double s = acc[k];
+      for (int ii = 0; ii < 32; ii++) s += sa[ar][ii] * sw[tx][ii];
+      acc[k] = s;
+    }
+    __syncthreads();
+  }
+  for (int k = 0; k < 4; k++) {
+    const int a = a0 + ty + 8 * k, b = b0 + tx;
+    if (a < nbf && b < nbf) quad[(size_t)a + (size_t)nbf * (b + (size_t)nbf * comp)] = acc[k];
+  }
 }
 
 int get_quad(dbsrg_ctx *c, int k, const double **out) {
@@ -642,16 +665,18 @@ int get_quad(dbsrg_ctx *c, int k, const double **out) {
   const DeviceGrid &g = c->g;
   double *q = nullptr;
   size_t n = (size_t)c->nbf * c->nbf * 2;
-  size_t gp = (size_t)g.ns * g.ksp, gq = (size_t)g.ns * g.ksq;
-  if (cudaMalloc((void **)&q, (n + gp + gq) * sizeof(double)) != cudaSuccess)
+  size_t gp = (size_t)g.ns * g.ksp, gq = (size_t)g.ns * g.ksq, nw = (size_t)2 * c->nbf * g.ns;
+  if (cudaMalloc((void **)&q, (n + gp + gq + nw) * sizeof(double)) != cudaSuccess)
     return set_err(c, DBSRG_ENOMEM, "quad allocation failed");
-  double *GP = q + n, *GQ = GP + gp;
+  double *GP = q + n, *GQ = GP + gp, *W = GQ + gq;
   DBSRG_RUN(c, "k_rk_gram", k_rk_gram<<<(unsigned)((gp + 127) / 128), 128, 0, c->stream>>>(
                                 g.ns, g.nv, g.ks, g.ksp, k, g.pbsp, g.gr, g.grw, GP));
   DBSRG_RUN(c, "k_rk_gram", k_rk_gram<<<(unsigned)((gq + 127) / 128), 128, 0, c->stream>>>(
                                 g.ns, g.nv, g.ks, g.ksq, k, g.qbsp, g.gr, g.grw, GQ));
-  DBSRG_RUN(c, "k_quad", k_quad<<<(unsigned)((n * 32 + 255) / 256), 256, 0, c->stream>>>(
-                             c->nbf, g.ns, g.ksp, g.ksq, c->pq, GP, GQ, q));
+  DBSRG_RUN(c, "k_quad_w", k_quad_w<<<(unsigned)((nw + 255) / 256), 256, 0, c->stream>>>(
+                               c->nbf, g.ns, g.ksp, g.ksq, c->pq, GP, GQ, W));
+  dim3 gd((unsigned)((c->nbf + 31) / 32), (unsigned)((c->nbf + 31) / 32), 2);
+  DBSRG_RUN(c, "k_quad_dot", k_quad_dot<<<gd, 256, 0, c->stream>>>(c->nbf, g.ns, c->pq, W, q));
   c->quad[k] = q;
   *out = q;
   return DBSRG_OK;
