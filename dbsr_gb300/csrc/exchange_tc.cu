@@ -24,9 +24,9 @@
 // Thread 0 loads the next product's operands with 1-D bulk copies
 // (cp.async.bulk completing on an mbarrier), issues its 42 MMAs (21 slice
 // pairs x 2 K-steps of M=128 N=32 K=16) into one of two TMEM accumulator sets
-// and commits them to a second mbarrier, while the eight warps recombine the
+// and commits them to a second mbarrier, while sixteen warps recombine the
 // previous product out of the other set (warp w reads TMEM lanes 32(w%4)..
-// and columns 16(w/4)..).  hch is read and written once per tile; no atomics.
+// and columns 8(w/4)..).  hch is read and written once per tile; no atomics.
 // Every wait is bounded (2 s): on a timeout the kernel records an error word,
 // waits (bounded) for its own copies and MMAs in flight, frees its TMEM and
 // returns.
@@ -210,10 +210,12 @@ __device__ __forceinline__ uint32_t tile_products(const XArgs &p, const Row &r, 
   return codes;
 }
 
-constexpr int NCW = 8;                // consumer (epilogue) warps
+constexpr int NCW = 16;               // consumer (epilogue) warps
+constexpr int CPT = 32 / (NCW / 4);   // tile columns per consumer thread
 constexpr int WPROD = NCW;            // producer warp
 constexpr int WSTAGE = NCW + 1;       // stager warp
 constexpr int NTHR = 32 * (NCW + 2);
+static_assert(TS == 6, "the epilogue pairs the six orders");
 
 __device__ __forceinline__ void consumers_sync() {
   asm volatile("bar.sync 1, %0;\n" ::"n"(32 * NCW) : "memory");
@@ -243,8 +245,10 @@ __device__ __forceinline__ void mbar_arrive(uint32_t mbar) {
 //  * consumers (warps 0..NCW-1): per product read the TMEM set, release it
 //    and add the product into int64 accumulators; per tile convert, add the
 //    band, add hch, store, and release the staging buffers.
-// 10 warps: one SM sub-partition holds 3 of them, so at most 168 registers.
-__global__ void __maxnreg__(168) k_xfused(const XArgs p) {
+// 18 warps: two SM sub-partitions hold 5 of them, and a sub-partition has
+// 16384 registers, so at most 96 registers a thread.  Four consumer warps per
+// sub-partition hide each other's TMEM and integer latencies.
+__global__ void __maxnreg__(96) k_xfused(const XArgs p) {
   extern __shared__ __align__(1024) unsigned char smraw[];
   unsigned char *sA = smraw;                          // [2][TS][A_BYTES]
   unsigned char *sB = sA + 2 * TS * A_BYTES;          // [2][TS][B_BYTES]
@@ -431,18 +435,17 @@ __global__ void __maxnreg__(168) k_xfused(const XArgs p) {
     }
   } else {
     // ------------------------------------------------------------ consumers
-    // Thread (lane group lg, column half hf) owns row x of the tile and 16
+    // Thread (lane group lg, column group cg) owns row x of the tile and CPT
     // columns.  Product p scales element (x, y) by 2^(er_p(x) + ec_p(y)); the
     // thread sums its products exactly in int64 aligned to one exponent, the
-    // largest row + tile-column exponent of the tile's products (right
+    // largest row + column exponent of the products added so far (right
     // shifts drop bits below 2^-56 of the largest scale), and converts each
     // sum to FP64 once.
-    const int lg = warp & 3, hf = warp >> 2, xl = lg * 32 + lane;
-    constexpr uint32_t MAGIC = 0x4B400000u;  // bits of 1.5 * 2^23 (tc::f2i_exact)
+    const int lg = warp & 3, cg = warp >> 2, xl = lg * 32 + lane;
     bool dead = false;
     uint32_t q = 0, ntile = 0;
     Row r;
-    long long Iacc[16];
+    long long Iacc[CPT];
     for (int row = blockIdx.x; row < p.nrows; row += gridDim.x) {
       load_row(p, row, r);
       const int x = r.tx * 128 + xl, x0 = r.tx * 128;
@@ -454,15 +457,15 @@ __global__ void __maxnreg__(168) k_xfused(const XArgs p) {
         bool band;
         const uint32_t codes = tile_products(p, r, ty, np, band);
         if (np == 0 && !band) continue;
-        const int y0 = ty * 32 + hf * 16, ty0 = ty * 32;
+        const int y0 = ty * 32 + cg * CPT, ty0 = ty * 32;
         double *h = const_cast<double *>(hq) + ms * (size_t)y0 + x;
 #pragma unroll
-        for (int c = 0; c < 16; c++) Iacc[c] = 0;
+        for (int c = 0; c < CPT; c++) Iacc[c] = 0;
         if (!bulk) {  // odd ns: the consumers stage hch and the band themselves
 #pragma unroll
-          for (int c = 0; c < 16; c++) {
+          for (int c = 0; c < CPT; c++) {
             const bool ok = row_ok && y0 + c < p.ns;
-            cp_async8(smem_u32(shch + (size_t)(hf * 16 + c) * 128 + xl), ok ? h + ms * c : p.hch,
+            cp_async8(smem_u32(shch + (size_t)(cg * CPT + c) * 128 + xl), ok ? h + ms * c : p.hch,
                       ok);
           }
           if (band) {
@@ -490,9 +493,9 @@ __global__ void __maxnreg__(168) k_xfused(const XArgs p) {
         }
         // per element the exponent the int64 sum is kept at: the largest
         // row + column exponent of the products added so far
-        int cur[16];
+        int cur[CPT];
 #pragma unroll
-        for (int c = 0; c < 16; c++) cur[c] = -100000;
+        for (int c = 0; c < CPT; c++) cur[c] = -100000;
         for (int pc = 0; pc < np; pc++, q++) {
           const int b = q & 1;
           const uint32_t n = q >> 1;
@@ -501,7 +504,12 @@ __global__ void __maxnreg__(168) k_xfused(const XArgs p) {
           const int *eua = p.eu[a] + (size_t)m * EX;
           const int *ezs = p.ez + ((size_t)(a * 2 + m) * p.nm + (tc >> 3)) * EX;
           const int er = tra ? ezs[x] : eua[x];
-          const int *ecol = (tra ? eua : ezs) + y0;
+          // column exponents: 8 ints at a 32-byte aligned offset
+          const int4 *ep = reinterpret_cast<const int4 *>((tra ? eua : ezs) + y0);
+          const int4 e0 = ep[0], e1 = ep[1];
+          const int ec[CPT] = {e0.x, e0.y, e0.z, e0.w, e1.x, e1.y, e1.z, e1.w};
+          // the product's far field: y - x >= FAR (sg = 1) or x - y >= FAR (sg = -1)
+          const int sg = (tra ^ m) ? -1 : 1;
           if (!dead && *abort_flag) dead = true;
           bool ok = !dead && mbar_wait(smem_u32(&bar_mma[b]), n & 1, WAIT_NS);
           ok = __all_sync(0xffffffffu, ok);
@@ -514,54 +522,50 @@ __global__ void __maxnreg__(168) k_xfused(const XArgs p) {
             continue;
           }
           fence_after();
-          // I = sum_g D_g 256^(TS-1-g): pairs of orders combined in int32
-          // (|D_2k 256 + D_2k+1| < 2^31), then I = (P0 2^16 + P1) 2^16 + P2
-          long long I[16];
+          // orders 2k and 2k+1 of the product: bits(D + 1.5 2^23) = D + 1.5 2^23
+          // (as an integer) exactly for |D| < 2^22; wrap-around unsigned
+          // arithmetic leaves P_k = 256 D_2k + D_2k+1
+          int P[3][CPT];
+          const uint32_t col =
+              tbase + ((uint32_t)(lg * 32) << 16) + (uint32_t)(b * 256 + cg * CPT);
 #pragma unroll
-          for (int c = 0; c < 16; c++) I[c] = 0;
-#pragma unroll
-          for (int k = 0; k < TS / 2; k++) {
-            uint32_t v0[16], v1[16];
-            const uint32_t col = tbase + ((uint32_t)(lg * 32) << 16) +
-                                 (uint32_t)(b * 256 + 2 * k * 32 + hf * 16);
-            tmem_ld16(col, v0);
-            tmem_ld16(col + 32, v1);
+          for (int k = 0; k < 3; k++) {
+            uint32_t v0[CPT], v1[CPT];
+            tmem_ld8(col + 64 * k, v0);
+            tmem_ld8(col + 64 * k + 32, v1);
             tmem_wait_ld();
 #pragma unroll
-            for (int c = 0; c < 16; c++) {
-              // bits(D + 1.5 2^23) = D + MAGIC exactly for |D| < 2^22; wrap-around
-              // unsigned arithmetic leaves 256 D_2k + D_2k+1
-              const uint32_t pu =
-                  ((uint32_t)__float_as_uint(__uint_as_float(v0[c]) + 12582912.0f) << 8) +
-                  (uint32_t)__float_as_uint(__uint_as_float(v1[c]) + 12582912.0f) -
-                  257u * MAGIC;
-              I[c] = I[c] * 65536 + (long long)(int)pu;
-            }
+            for (int c = 0; c < CPT; c++)
+              P[k][c] = (int)(((uint32_t)__float_as_uint(__uint_as_float(v0[c]) + 12582912.0f)
+                               << 8) +
+                              (uint32_t)__float_as_uint(__uint_as_float(v1[c]) + 12582912.0f) -
+                              257u * 0x4B400000u);
           }
           fence_before();
           __syncwarp();
           if (lane == 0) mbar_arrive(smem_u32(&bar_free[b]));
 #pragma unroll
-          for (int c = 0; c < 16; c++) {
-            const int d = (y0 + c) - x, se = er + ecol[c];
-            const bool in =
-                tra ? (m == 0 ? d <= -FAR : d >= FAR) : (m == 0 ? d >= FAR : d <= -FAR);
-            if (in) {
+          for (int c = 0; c < CPT; c++) {
+            // I = sum_g D_g 256^(TS-1-g) = P0 2^32 + P1 2^16 + P2
+            const long long I = (long long)P[0][c] * 4294967296LL +
+                                (long long)P[1][c] * 65536LL + (long long)P[2][c];
+            const int d = (y0 + c) - x, se = er + ec[c];
+            if (sg * d >= FAR) {
               if (se > cur[c]) {  // raise the sum to the new exponent
                 const int up = se - cur[c];
                 Iacc[c] = up < 63 ? Iacc[c] >> up : 0;
                 cur[c] = se;
               }
               const int sh = cur[c] - se;
-              if (sh < 63) Iacc[c] += I[c] >> sh;
+              if (sh < 63) Iacc[c] += I >> sh;
             }
           }
         }
         // to FP64 (the factor 1/2 of ich == jch in the exponent), near band,
         // and the write of the tile: one FP64 add per element
-        double val[16];
+        double val[CPT];
 #pragma unroll
-        for (int c = 0; c < 16; c++)
+        for (int c = 0; c < CPT; c++)
           val[c] = cur[c] > -100000 ? i64_to_f64(Iacc[c], cur[c] - 8 * (TS + 1) - r.half) : 0.0;
         if (bulk) {
           const bool ok = dead || mbar_wait(smem_u32(&bar_tile), ntile & 1, WAIT_NS);
@@ -576,7 +580,7 @@ __global__ void __maxnreg__(168) k_xfused(const XArgs p) {
         }
         if (band) {
 #pragma unroll
-          for (int c = 0; c < 16; c++) {
+          for (int c = 0; c < CPT; c++) {
             const int y = y0 + c, d = y - x;
             if (d < -BAND || d > BAND || !row_ok || y >= p.ns) continue;
             for (int t = 0; t < r.nt; t++) {
@@ -589,8 +593,8 @@ __global__ void __maxnreg__(168) k_xfused(const XArgs p) {
         }
         if (row_ok && !dead) {
 #pragma unroll
-          for (int c = 0; c < 16; c++)
-            if (y0 + c < p.ns) h[ms * c] = shch[(size_t)(hf * 16 + c) * 128 + xl] + val[c];
+          for (int c = 0; c < CPT; c++)
+            if (y0 + c < p.ns) h[ms * c] = shch[(size_t)(cg * CPT + c) * 128 + xl] + val[c];
         }
         // release the staging buffers
         if (bulk) {
