@@ -475,11 +475,17 @@ def main():
         dl.append((L.icase, L.itype, L.kpol, *t, c))
     torch.cuda.synchronize()
 
+    # asynchronous mode: the host-side set-up of each list overlaps the
+    # kernels of the previous one; sync() ends every step, so the step's
+    # time covers all of its kernels
+    a.set_async(True)
+
     def step(lists):
         a.zero_matrix()
         a.release_tables()
         for (ic, it, kp, k1, k2, k3, k4, c) in lists:
             a.gen_matrix(ic, it, kp, k1, k2, k3, k4, c)
+        a.sync()
 
     def barrier():
         torch.cuda.synchronize()

@@ -48,6 +48,7 @@ SIGNATURES = [
     ("dbsrg_get_grid_array", C.c_int, [_vp, C.c_char_p, _vp]),
     ("dbsrg_kernel_launches", C.c_longlong, [_vp]),
     ("dbsrg_sync", C.c_int, [_vp]),
+    ("dbsrg_set_async", C.c_int, [_vp, C.c_int]),
     ("dbsrg_release_tables", C.c_int, [_vp]),
     ("dbsrg_timing", C.c_int, [_vp, C.c_int]),
     ("dbsrg_timing_report", C.c_int, [_vp, C.c_char_p, C.c_size_t]),

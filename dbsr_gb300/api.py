@@ -221,7 +221,14 @@ class Assembler:
         return int(self._L.dbsrg_kernel_launches(self._h))
 
     def sync(self):
+        """Wait for the queued kernels; raises on a failure of any of them."""
         check(self._h, self._L.dbsrg_sync(self._h), "sync")
+
+    def set_async(self, enable: bool = True):
+        """Asynchronous mode: gen() returns once the list's kernels are
+        queued, so the set-up of the next list overlaps them; failures surface
+        at the next sync() or read-out."""
+        check(self._h, self._L.dbsrg_set_async(self._h, int(enable)), "set_async")
 
 
 def gen_batch(assemblers, lists_per_assembler):

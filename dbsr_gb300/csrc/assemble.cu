@@ -582,14 +582,22 @@ int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const 
   cudaStream_t st = c->stream;
   int rc;
 
-  // ---- 1. list in IPT order on the device (scratch2 holds the list state)
+  // ---- 1. list in IPT order on the device.  The list state lives in one
+  // of two buffers; with the pipeline on (asynchronous mode, R and S lists)
+  // its set-up runs on the set-up stream once the kernels of the call two
+  // back are done with the buffer, while the previous call's kernels run.
+  const bool pipe = c->async && icase != 0;
+  const int par = c->lpar;
+  c->lpar ^= 1;
+  cudaStream_t ss = pipe ? c->sstream : st;
   const size_t ibytes = sizeof(int) * (size_t)n, dbytes = sizeof(double) * (size_t)n;
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
   size_t tot = 8 * al(ibytes) + 2 * al(dbytes) + al(sizeof(int) * (n + 2)) + al(64) +
                al(sizeof(SegInfo) * (size_t)(n + 1)) + al(sizeof(int) * (size_t)(n + 1)) +
-               al(sizeof(int) * (size_t)(6 * (n + 1)));
-  if ((rc = ensure_scratch2(c, tot))) return rc;
-  char *base = (char *)c->scratch2;
+               al(sizeof(int) * (size_t)(6 * (n + 1))) + al(sizeof(XQuad) * 4 * (size_t)(n + 1));
+  if ((rc = ensure_lstate(c, par, tot))) return rc;
+  if (pipe) DBSRG_TRY(c, cudaStreamWaitEvent(ss, c->lfree[par], 0));
+  char *base = (char *)c->lstate[par];
   auto take = [&](size_t bytes) {
     char *p = base;
     base += al(bytes);
@@ -608,14 +616,16 @@ int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const 
   // per chunk: member segment ids, owner slots and (split exchange) the
   // (owner slot, quadrant) codes -- at most 6 ints per segment
   int *members = (int *)take(sizeof(int) * (size_t)(6 * (n + 1)));
-  if ((rc = copy_in(c, dk1, k1, ibytes))) return rc;
-  if ((rc = copy_in(c, dk2, k2, ibytes))) return rc;
-  if ((rc = copy_in(c, dk3, k3, ibytes))) return rc;
-  if ((rc = copy_in(c, dcd, cdata, dbytes))) return rc;
-  if (ipt && (rc = copy_in(c, dipt, ipt, ibytes))) return rc;
-  DBSRG_TRY(c, cudaMemsetAsync(dscal, 0, 64, st));
-  DBSRG_RUN(c, "k_gather", k_gather<<<(n + 255) / 256, 256, 0, st>>>(n, ipt ? dipt : nullptr, dk1, dk2, dk3, dcd, lk1,
-                                            lk2, lk3, lcd));
+  XQuad *dxq_all = (XQuad *)take(sizeof(XQuad) * 4 * (size_t)(n + 1));
+  if ((rc = copy_in_s(c, dk1, k1, ibytes, ss))) return rc;
+  if ((rc = copy_in_s(c, dk2, k2, ibytes, ss))) return rc;
+  if ((rc = copy_in_s(c, dk3, k3, ibytes, ss))) return rc;
+  if ((rc = copy_in_s(c, dcd, cdata, dbytes, ss))) return rc;
+  if (ipt && (rc = copy_in_s(c, dipt, ipt, ibytes, ss))) return rc;
+  DBSRG_TRY(c, cudaMemsetAsync(dscal, 0, 64, ss));
+  DBSRG_RUN_S(c, ss, "k_gather",
+              k_gather<<<(n + 255) / 256, 256, 0, ss>>>(n, ipt ? dipt : nullptr, dk1, dk2, dk3,
+                                                        dcd, lk1, lk2, lk3, lcd));
 
   // ---- overlaps
   if (icase == 0) {
@@ -652,16 +662,18 @@ int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const 
   }
 
   // ---- 2. segments (orbital check and segment count read back together)
-  DBSRG_RUN(c, "k_check_orbitals", k_check_orbitals<<<(n + 255) / 256, 256, 0, st>>>(n, lk2, lk3, c->nbf, dscal + 1));
-  DBSRG_RUN(c, "k_segments", k_segments<<<1, 1024, 0, st>>>(n, lk1, seg_start, dscal));
+  DBSRG_RUN_S(c, ss, "k_check_orbitals",
+              k_check_orbitals<<<(n + 255) / 256, 256, 0, ss>>>(n, lk2, lk3, c->nbf, dscal + 1));
+  DBSRG_RUN_S(c, ss, "k_segments", k_segments<<<1, 1024, 0, ss>>>(n, lk1, seg_start, dscal));
   int hs[4] = {0, 0, 0, 0};  // nseg, error, -, bound-pair error
-  DBSRG_TRY(c, cudaMemcpyAsync(hs, dscal, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
-  DBSRG_TRY(c, cudaStreamSynchronize(st));
+  DBSRG_TRY(c, cudaMemcpyAsync(hs, dscal, 2 * sizeof(int), cudaMemcpyDeviceToHost, ss));
+  DBSRG_TRY(c, cudaStreamSynchronize(ss));
   if (hs[1]) return set_err(c, DBSRG_ERANGE, "channel or orbital index out of range in list");
   const int nseg = hs[0];
   if (nseg < 1 || nseg > n) return set_err(c, DBSRG_ECUDA, "inconsistent segment count");
-  DBSRG_RUN(c, "k_seg_info", k_seg_info<<<(nseg + 127) / 128, 128, 0, st>>>(nseg, seg_start, lk1, c->nch, c->iicc, c->icc,
-                                                 info, dscal + 1));
+  DBSRG_RUN_S(c, ss, "k_seg_info",
+              k_seg_info<<<(nseg + 127) / 128, 128, 0, ss>>>(nseg, seg_start, lk1, c->nch,
+                                                             c->iicc, c->icc, info, dscal + 1));
 
   // ---- 3. contraction set-up per case
   DensSpec dsp{};
@@ -749,14 +761,14 @@ int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const 
   if (factored) {
     // the factored contraction works with ordered pairs of bound orbitals
     if (c->nbound < 1) return set_err(c, DBSRG_ESTATE, "no bound orbitals (ipbs = 0)");
-    if ((rc = pair_index(c, n, lk2, lk3, lpair, dscal + 3))) return rc;
+    if ((rc = pair_index(c, n, lk2, lk3, lpair, dscal + 3, ss))) return rc;
   }
   // segment table, segment errors and bound-pair errors in one read-back
   std::vector<SegInfo> hinfo(nseg);
-  DBSRG_TRY(c, cudaMemcpyAsync(hs, dscal, 4 * sizeof(int), cudaMemcpyDeviceToHost, st));
+  DBSRG_TRY(c, cudaMemcpyAsync(hs, dscal, 4 * sizeof(int), cudaMemcpyDeviceToHost, ss));
   DBSRG_TRY(c, cudaMemcpyAsync(hinfo.data(), info, sizeof(SegInfo) * nseg,
-                               cudaMemcpyDeviceToHost, st));
-  DBSRG_TRY(c, cudaStreamSynchronize(st));
+                               cudaMemcpyDeviceToHost, ss));
+  DBSRG_TRY(c, cudaStreamSynchronize(ss));
   if (hs[1] == 1) return set_err(c, DBSRG_ERANGE, "channel or orbital index out of range in list");
   if (hs[1] == 2) return set_err(c, DBSRG_ERANGE, "channel pair has no block in icc");
   if (hs[3]) return set_err(c, DBSRG_EINVAL, "factored contraction: K2/K3 must be bound orbitals");
@@ -802,14 +814,28 @@ int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const 
     }
     close();
   }
-  if (!hbuf.empty() && (rc = copy_in(c, members, hbuf.data(), sizeof(int) * hbuf.size())))
-    return rc;
   if (!xq_ok) return set_err(c, DBSRG_ECUDA, "split exchange: a quadrant with more than 4 terms");
+  if (hxq.size() > 4 * (size_t)(n + 1))
+    return set_err(c, DBSRG_ECUDA, "split exchange: quadrant records overflow");
+  // owner segments in list order (asymptotic coefficients of direct R^k)
+  std::vector<int> hown;
+  if (icase == 2 && itype == 3)
+    for (int s = 0; s < nseg; s++)
+      if (hinfo[s].owner) hown.push_back(s);
+  // the host-built work lists go to the list state on the set-up stream;
+  // the contraction waits for the set-up
+  if (!hbuf.empty() && (rc = copy_in_s(c, members, hbuf.data(), sizeof(int) * hbuf.size(), ss)))
+    return rc;
   XQuad *dxq = nullptr;
   if (!hxq.empty()) {
-    if ((rc = ensure_lscratch(c, sizeof(XQuad) * hxq.size()))) return rc;
-    dxq = (XQuad *)c->lscratch;
-    if ((rc = copy_in(c, dxq, hxq.data(), sizeof(XQuad) * hxq.size()))) return rc;
+    dxq = dxq_all;
+    if ((rc = copy_in_s(c, dxq, hxq.data(), sizeof(XQuad) * hxq.size(), ss))) return rc;
+  }
+  if (!hown.empty() && (rc = copy_in_s(c, owners, hown.data(), sizeof(int) * hown.size(), ss)))
+    return rc;
+  if (pipe) {
+    DBSRG_TRY(c, cudaEventRecord(c->lready, ss));
+    DBSRG_TRY(c, cudaStreamWaitEvent(st, c->lready, 0));
   }
   auto run_chunk = [&](const int *mb, int nm, const int *ob, int nown, const XQuad *xq,
                        const XQuad *hxq_chunk, int nxq) -> int {
@@ -888,13 +914,8 @@ int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const 
                         ch.nxq)))
       return rc;
   if (icase == 2 && itype == 3) {
-    // owner segments in list order
-    std::vector<int> hown;
-    for (int s = 0; s < nseg; s++)
-      if (hinfo[s].owner) hown.push_back(s);
     const int nown = (int)hown.size();
     if (nown > 0) {
-      if ((rc = copy_in(c, owners, hown.data(), sizeof(int) * hown.size()))) return rc;
       const double *quad;
       if ((rc = get_quad(c, kpol, &quad))) return rc;
       DBSRG_RUN(c, "k_acf", k_acf<<<(nown + 127) / 128, 128, 0, st>>>(nown, owners, info, kpol,
@@ -902,17 +923,11 @@ int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const 
                                                                     c->acf, c->iicc));
     }
   }
-  DBSRG_TRY(c, cudaStreamSynchronize(st));
-  if (c->kerr) {  // bounded waits of the tensor-core kernels
-    int h = 0;
-    DBSRG_TRY(c, cudaMemcpyAsync(&h, c->kerr, sizeof(int), cudaMemcpyDeviceToHost, st));
-    DBSRG_TRY(c, cudaStreamSynchronize(st));
-    if (h) {
-      DBSRG_TRY(c, cudaMemsetAsync(c->kerr, 0, sizeof(int), st));
-      DBSRG_TRY(c, cudaStreamSynchronize(st));
-      if (h == 1) return set_err(c, DBSRG_ETIMEOUT, "tensor-core exchange: a wait ran out");
-      return set_err(c, DBSRG_ECUDA, "tensor-core exchange: inconsistent tile terms");
-    }
+  // the kernels of this call are done with the list state after this point
+  DBSRG_TRY(c, cudaEventRecord(c->lfree[par], st));
+  if (pipe) {
+    c->pending = true;
+    return DBSRG_OK;
   }
-  return DBSRG_OK;
+  return drain(c);  // synchronous mode: wait, and report the tensor-core error word
 }

@@ -121,13 +121,14 @@ extern "C" int dbsrg_backward(dbsrg_ctx *c, int n, const int *k, const int *i1, 
                               const int *i3, const int *i4, const double *coef, double *energy,
                               double *grad) {
   if (!c) return DBSRG_EINVAL;
+  int rc;
   if (n < 0 || (n > 0 && (!k || !i1 || !i2 || !i3 || !i4 || !coef)) || !energy)
     return set_err(c, DBSRG_EINVAL, "backward: bad arguments");
   if (!c->pq) return set_err(c, DBSRG_ESTATE, "backward: no orbitals set");
   cudaSetDevice(c->device);
+  if (c->pending && (rc = drain(c))) return rc;
   const int ns = c->g.ns, ks = c->g.ks, nbf = c->nbf, nb = c->nbound;
   cudaStream_t st = c->stream;
-  int rc;
   // the entries on the host (small: integer keys and coefficients)
   std::vector<int> hk(n), h1(n), h2(n), h3(n), h4(n);
   std::vector<double> hc(n);

@@ -29,13 +29,45 @@ bool is_device_ptr(const void *p) {
   return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
-int copy_in(dbsrg_ctx *c, void *dst, const void *src, size_t n) {
+int copy_in_s(dbsrg_ctx *c, void *dst, const void *src, size_t n, cudaStream_t s) {
   if (n == 0) return DBSRG_OK;
   if (!src) return set_err(c, DBSRG_EINVAL, "null input pointer");
   cudaMemcpyKind k = is_device_ptr(src) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
-  DBSRG_TRY(c, cudaMemcpyAsync(dst, src, n, k, c->stream));
+  DBSRG_TRY(c, cudaMemcpyAsync(dst, src, n, k, s));
   return DBSRG_OK;
 }
+
+int copy_in(dbsrg_ctx *c, void *dst, const void *src, size_t n) {
+  return copy_in_s(c, dst, src, n, c->stream);
+}
+
+// Waits for both streams, then reads and clears the error word of the
+// tensor-core kernels (a bounded wait that ran out, or inconsistent tile
+// terms).
+int drain(dbsrg_ctx *c) {
+  c->pending = false;
+  if (c->sstream) DBSRG_TRY(c, cudaStreamSynchronize(c->sstream));
+  DBSRG_TRY(c, cudaStreamSynchronize(c->stream));
+  if (!c->kerr) return DBSRG_OK;
+  int h = 0;
+  DBSRG_TRY(c, cudaMemcpyAsync(&h, c->kerr, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  DBSRG_TRY(c, cudaStreamSynchronize(c->stream));
+  if (!h) return DBSRG_OK;
+  DBSRG_TRY(c, cudaMemsetAsync(c->kerr, 0, sizeof(int), c->stream));
+  DBSRG_TRY(c, cudaStreamSynchronize(c->stream));
+  if (h == 1) return set_err(c, DBSRG_ETIMEOUT, "tensor-core exchange: a wait ran out");
+  return set_err(c, DBSRG_ECUDA, "tensor-core exchange: inconsistent tile terms");
+}
+
+// queued work of the asynchronous mode is finished (and its errors read)
+// before any call that reads results or changes state
+#define SETTLE(c)                  \
+  do {                             \
+    if ((c)->pending) {            \
+      int _r = drain(c);           \
+      if (_r) return _r;           \
+    }                              \
+  } while (0)
 
 int copy_out(dbsrg_ctx *c, void *dst, const void *src, size_t n) {
   if (n == 0) return DBSRG_OK;
@@ -84,8 +116,10 @@ int ensure_tcscratch(dbsrg_ctx *c, size_t bytes) {
 int ensure_pscratch(dbsrg_ctx *c, size_t bytes) {
   return grow(c, &c->pscratch, &c->pscratch_bytes, bytes);
 }
-int ensure_lscratch(dbsrg_ctx *c, size_t bytes) {
-  return grow(c, &c->lscratch, &c->lscratch_bytes, bytes);
+int ensure_lstate(dbsrg_ctx *c, int par, size_t bytes) {
+  if (c->lstate_bytes[par] >= bytes) return DBSRG_OK;
+  if (c->lstate[par]) DBSRG_TRY(c, cudaStreamSynchronize(c->sstream));
+  return grow(c, &c->lstate[par], &c->lstate_bytes[par], bytes);
 }
 bool sync_check_enabled() {
   static int v = -1;
@@ -174,6 +208,14 @@ int dbsrg_create(dbsrg_ctx **out, const dbsrg_grid_desc *d) {
     delete c;
     return DBSRG_ECUDA;
   }
+  if (cudaStreamCreateWithFlags(&c->sstream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->lfree[0], cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->lfree[1], cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->lready, cudaEventDisableTiming) != cudaSuccess) {
+    cudaGetLastError();
+    dbsrg_destroy(c);
+    return DBSRG_ECUDA;
+  }
   DeviceGrid &g = c->g;
   g.ns = d->ns;
   g.ks = d->ks;
@@ -195,6 +237,7 @@ int dbsrg_create(dbsrg_ctx **out, const dbsrg_grid_desc *d) {
 int dbsrg_destroy(dbsrg_ctx *c) {
   if (!c) return DBSRG_OK;
   cudaSetDevice(c->device);
+  if (c->sstream) cudaStreamSynchronize(c->sstream);
   if (c->stream) cudaStreamSynchronize(c->stream);
   free_tables(c);
   DeviceGrid &g = c->g;
@@ -213,13 +256,18 @@ int dbsrg_destroy(dbsrg_ctx *c) {
   if (c->fscratch) cudaFree(c->fscratch);
   if (c->tcscratch) cudaFree(c->tcscratch);
   if (c->pscratch) cudaFree(c->pscratch);
-  if (c->lscratch) cudaFree(c->lscratch);
+  for (int i = 0; i < 2; i++) {
+    if (c->lstate[i]) cudaFree(c->lstate[i]);
+    if (c->lfree[i]) cudaEventDestroy(c->lfree[i]);
+  }
+  if (c->lready) cudaEventDestroy(c->lready);
   if (c->kerr) cudaFree(c->kerr);
   if (c->bmap) cudaFree(c->bmap);
   if (c->b2o) cudaFree(c->b2o);
   if (c->pinned) cudaFreeHost(c->pinned);
   timing_clear(c);
   for (cudaEvent_t e : c->evpool) cudaEventDestroy(e);
+  if (c->sstream) cudaStreamDestroy(c->sstream);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return DBSRG_OK;
@@ -228,6 +276,7 @@ int dbsrg_destroy(dbsrg_ctx *c) {
 int dbsrg_release_tables(dbsrg_ctx *c) {
   if (!c) return DBSRG_EINVAL;
   cudaSetDevice(c->device);
+  SETTLE(c);
   DBSRG_TRY(c, cudaStreamSynchronize(c->stream));
   free_tables(c);
   return DBSRG_OK;
@@ -235,6 +284,7 @@ int dbsrg_release_tables(dbsrg_ctx *c) {
 
 int dbsrg_timing(dbsrg_ctx *c, int enable) {
   if (!c) return DBSRG_EINVAL;
+  SETTLE(c);
   DBSRG_TRY(c, cudaStreamSynchronize(c->stream));
   timing_clear(c);
   c->timing = enable != 0;
@@ -243,6 +293,7 @@ int dbsrg_timing(dbsrg_ctx *c, int enable) {
 
 int dbsrg_timing_report(dbsrg_ctx *c, char *buf, size_t len) {
   if (!c || !buf || len < 3) return DBSRG_EINVAL;
+  SETTLE(c);
   DBSRG_TRY(c, cudaStreamSynchronize(c->stream));
   std::vector<std::string> names;
   std::vector<long long> cnt;
@@ -286,13 +337,22 @@ long long dbsrg_kernel_launches(const dbsrg_ctx *c) { return c ? c->launches : 0
 
 int dbsrg_sync(dbsrg_ctx *c) {
   if (!c) return DBSRG_EINVAL;
-  DBSRG_TRY(c, cudaStreamSynchronize(c->stream));
+  cudaSetDevice(c->device);
+  return drain(c);
+}
+
+int dbsrg_set_async(dbsrg_ctx *c, int enable) {
+  if (!c) return DBSRG_EINVAL;
+  cudaSetDevice(c->device);
+  SETTLE(c);
+  c->async = enable != 0;
   return DBSRG_OK;
 }
 
 int dbsrg_set_orbitals(dbsrg_ctx *c, int nbf, const double *pq, const int *ipbs) {
   if (!c || nbf < 1 || !pq || !ipbs) return set_err(c, DBSRG_EINVAL, "bad orbital arguments");
   cudaSetDevice(c->device);
+  SETTLE(c);
   if (c->pq) cudaFree(c->pq);
   if (c->ipbs) cudaFree(c->ipbs);
   c->pq = nullptr;
@@ -340,6 +400,7 @@ int dbsrg_alloc_matrix(dbsrg_ctx *c, int nch, const int *icc, int iicc, int mk) 
   if (!c || nch < 1 || !icc || iicc < 1 || mk < 0)
     return set_err(c, DBSRG_EINVAL, "bad matrix arguments");
   cudaSetDevice(c->device);
+  SETTLE(c);
   if (c->icc) cudaFree(c->icc);
   if (c->hch) cudaFree(c->hch);
   if (c->acf) cudaFree(c->acf);
@@ -368,6 +429,8 @@ int dbsrg_alloc_matrix(dbsrg_ctx *c, int nch, const int *icc, int iicc, int mk) 
 
 int dbsrg_zero_matrix(dbsrg_ctx *c) {
   if (!c || !c->hch) return set_err(c, DBSRG_ESTATE, "no matrix allocated");
+  cudaSetDevice(c->device);
+  SETTLE(c);
   const size_t ms = c->g.ms;
   DBSRG_TRY(c, cudaMemsetAsync(c->hch, 0, sizeof(double) * ms * ms * c->iicc, c->stream));
   DBSRG_TRY(c, cudaMemsetAsync(c->acf, 0, sizeof(double) * (size_t)c->iicc * (c->mk + 1), c->stream));
@@ -379,6 +442,7 @@ int dbsrg_set_precision(dbsrg_ctx *c, int p) {
   if (!c) return DBSRG_EINVAL;
   if (p != DBSRG_PLAIN_FP64 && p != DBSRG_SPLIT_BF16 && p != DBSRG_FACTOR_FP64)
     return set_err(c, DBSRG_EINVAL, "unknown precision");
+  SETTLE(c);
   c->precision = p;
   return DBSRG_OK;
 }
@@ -407,13 +471,21 @@ int dbsrg_gen_batch(int nctx, dbsrg_ctx *const *ctxs, const int *nlists,
     for (int j = i + 1; j < nctx; j++)
       if (ctxs[i] == ctxs[j]) return set_err(ctxs[i], DBSRG_EINVAL, "gen_batch: context twice");
   std::vector<int> rc((size_t)nctx, DBSRG_OK);
+  // every context pipelines its lists (the set-up of one list overlaps the
+  // kernels of the previous one) and is drained at the end
   auto work = [&](int i) {
     dbsrg_ctx *c = ctxs[i];
+    cudaSetDevice(c->device);
+    const bool was = c->async;
+    c->async = true;
     for (size_t l = off[i]; l < off[i + 1] && rc[i] == DBSRG_OK; l++) {
       const dbsrg_list &L = lists[l];
       rc[i] = dbsrg_gen_matrix(c, L.icase, L.itype, L.kpol, L.ncdata, L.ipt, L.k1, L.k2, L.k3,
                                L.k4, L.cdata);
     }
+    const int rd = drain(c);
+    if (rc[i] == DBSRG_OK) rc[i] = rd;
+    c->async = was;
   };
   // one host thread per context (each with its own stream): the host-side
   // list handling of one block overlaps the kernels of the others
@@ -429,11 +501,14 @@ int dbsrg_gen_batch(int nctx, dbsrg_ctx *const *ctxs, const int *nlists,
 int dbsrg_update_hx(dbsrg_ctx *c, int ich, int jch, const double *d, double cc) {
   if (!c || !d) return set_err(c, DBSRG_EINVAL, "bad UPDATE_HX arguments");
   cudaSetDevice(c->device);
+  SETTLE(c);
   return update_hx(c, ich, jch, d, cc);
 }
 
 int dbsrg_get_block(dbsrg_ctx *c, int ich, int jch, double *out) {
   if (!c || !out) return DBSRG_EINVAL;
+  cudaSetDevice(c->device);
+  SETTLE(c);
   if (!c->hch) return set_err(c, DBSRG_ESTATE, "no matrix allocated");
   if (ich < 1 || jch < 1 || ich > c->nch || jch > c->nch)
     return set_err(c, DBSRG_ERANGE, "channel out of range");
@@ -445,6 +520,8 @@ int dbsrg_get_block(dbsrg_ctx *c, int ich, int jch, double *out) {
 
 int dbsrg_get_matrix(dbsrg_ctx *c, double *out) {
   if (!c || !out) return DBSRG_EINVAL;
+  cudaSetDevice(c->device);
+  SETTLE(c);
   if (!c->hch) return set_err(c, DBSRG_ESTATE, "no matrix allocated");
   const size_t ms = c->g.ms;
   return copy_out(c, out, c->hch, sizeof(double) * ms * ms * c->iicc);
@@ -452,12 +529,16 @@ int dbsrg_get_matrix(dbsrg_ctx *c, double *out) {
 
 int dbsrg_get_acf(dbsrg_ctx *c, double *out) {
   if (!c || !out) return DBSRG_EINVAL;
+  cudaSetDevice(c->device);
+  SETTLE(c);
   if (!c->acf) return set_err(c, DBSRG_ESTATE, "no matrix allocated");
   return copy_out(c, out, c->acf, sizeof(double) * (size_t)c->iicc * (c->mk + 1));
 }
 
 int dbsrg_matrix_device_ptr(dbsrg_ctx *c, double **p) {
   if (!c || !p) return DBSRG_EINVAL;
+  cudaSetDevice(c->device);
+  SETTLE(c);
   if (!c->hch) return set_err(c, DBSRG_ESTATE, "no matrix allocated");
   *p = c->hch;
   return DBSRG_OK;
@@ -466,6 +547,7 @@ int dbsrg_matrix_device_ptr(dbsrg_ctx *c, double **p) {
 int dbsrg_get_table(dbsrg_ctx *c, int family, int type, int k, double *out) {
   if (!c || !out || k < 0 || k > 64) return set_err(c, DBSRG_EINVAL, "bad table request");
   cudaSetDevice(c->device);
+  SETTLE(c);
   const double *tab = nullptr;
   int rc;
   size_t n;
@@ -488,6 +570,7 @@ int dbsrg_get_table(dbsrg_ctx *c, int family, int type, int k, double *out) {
 int dbsrg_get_moments(dbsrg_ctx *c, int which, int k, double *out) {
   if (!c || !out || which < 0 || which > 3) return set_err(c, DBSRG_EINVAL, "bad moments request");
   cudaSetDevice(c->device);
+  SETTLE(c);
   const DeviceGrid &g = c->g;
   size_t n = (size_t)g.ks * g.ks * g.nv;
   int rc = ensure_scratch(c, n * sizeof(double));
@@ -499,6 +582,7 @@ int dbsrg_get_moments(dbsrg_ctx *c, int which, int k, double *out) {
 int dbsrg_get_diag_cells(dbsrg_ctx *c, int type, int k, double *out) {
   if (!c || !out || type < 0 || type > 5) return set_err(c, DBSRG_EINVAL, "bad diag-cell request");
   cudaSetDevice(c->device);
+  SETTLE(c);
   const DeviceGrid &g = c->g;
   size_t kk = (size_t)g.ks * g.ks;
   size_t n = kk * kk * g.nv;
@@ -510,6 +594,8 @@ int dbsrg_get_diag_cells(dbsrg_ctx *c, int type, int k, double *out) {
 
 int dbsrg_get_grid_array(dbsrg_ctx *c, const char *name, double *out) {
   if (!c || !name || !out) return DBSRG_EINVAL;
+  cudaSetDevice(c->device);
+  SETTLE(c);
   const DeviceGrid &g = c->g;
   const size_t nv = g.nv, ks = g.ks, ns = g.ns, ms = g.ms;
   const double *src = nullptr;

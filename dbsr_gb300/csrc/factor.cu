@@ -683,13 +683,14 @@ int ensure_fscratch(dbsrg_ctx *c, size_t bytes) {
   return DBSRG_OK;
 }
 
-int pair_index(dbsrg_ctx *c, int n, const int *k2, const int *k3, int *pairs, int *derr) {
+int pair_index(dbsrg_ctx *c, int n, const int *k2, const int *k3, int *pairs, int *derr,
+               cudaStream_t s) {
   if (n <= 0) return DBSRG_OK;
   if (c->nbound < 1 || c->nbound > NB_MAX)
     return set_err(c, DBSRG_EINVAL, "factored contraction: 1..64 bound orbitals (ipbs = 0)");
-  DBSRG_RUN(c, "k_pair_index",
-            k_pair_index<<<(n + 255) / 256, 256, 0, c->stream>>>(n, k2, k3, c->bmap, c->nbound,
-                                                                 pairs, derr));
+  DBSRG_RUN_S(c, s, "k_pair_index",
+              k_pair_index<<<(n + 255) / 256, 256, 0, s>>>(n, k2, k3, c->bmap, c->nbound, pairs,
+                                                           derr));
   return DBSRG_OK;
 }
 

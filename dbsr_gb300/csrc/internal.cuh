@@ -110,10 +110,25 @@ struct dbsrg_ctx {
   size_t tcscratch_bytes = 0;
   void *pscratch = nullptr;   // pair-potential construction (cell sums, cell parts)
   size_t pscratch_bytes = 0;
-  void *lscratch = nullptr;   // work records derived from one list (split exchange)
-  size_t lscratch_bytes = 0;
-  // error word of the tensor-core kernels (bounded waits), read at the end
-  // of each Gen_matrix call
+  // List pipeline.  The state of one Gen_matrix call (the list in IPT order,
+  // segments, chunk members, quadrant records) lives in one of two buffers,
+  // alternating per call.  Its set-up (copies, segment kernels, read-backs)
+  // runs on sstream once the kernels of the call two back have released the
+  // buffer (lfree), and the contraction on stream waits for it (lready), so
+  // the host plans one list while the kernels of the previous one run.
+  cudaStream_t sstream = nullptr;
+  void *lstate[2] = {nullptr, nullptr};
+  size_t lstate_bytes[2] = {0, 0};
+  cudaEvent_t lfree[2] = {nullptr, nullptr};
+  cudaEvent_t lready = nullptr;
+  int lpar = 0;
+  // asynchronous mode (dbsrg_set_async): Gen_matrix returns once its kernels
+  // are queued; failures of queued kernels surface at the next call that
+  // waits (dbsrg_sync, the read-outs, state changes)
+  bool async = false;
+  bool pending = false;
+  // error word of the tensor-core kernels (bounded waits), read whenever the
+  // context waits for its stream
   int *kerr = nullptr;
   // pinned staging for host lists
   void *pinned = nullptr;
@@ -158,26 +173,33 @@ bool sync_check_enabled();
 // Launch a named kernel on the context stream; with timing enabled the
 // launch is bracketed by events (resolved by dbsrg_timing_report) and its
 // algorithmic bytes and FLOPs, where stated, are recorded with it.
-#define DBSRG_RUN_W(ctx, name, wbytes, wflops, ...)               \
+#define DBSRG_RUN_SW(ctx, strm, name, wbytes, wflops, ...)        \
   do {                                                            \
     cudaEvent_t _ea = nullptr;                                    \
     if ((ctx)->timing) {                                          \
       _ea = event_get(ctx);                                       \
-      cudaEventRecord(_ea, (ctx)->stream);                        \
+      cudaEventRecord(_ea, (strm));                               \
     }                                                             \
     __VA_ARGS__;                                                  \
     if ((ctx)->timing) {                                          \
       cudaEvent_t _eb = event_get(ctx);                           \
-      cudaEventRecord(_eb, (ctx)->stream);                        \
+      cudaEventRecord(_eb, (strm));                               \
       (ctx)->tev.push_back({name, _ea, _eb, (double)(wbytes), (double)(wflops)}); \
     }                                                             \
     DBSRG_LAUNCHED(ctx);                                          \
   } while (0)
+#define DBSRG_RUN_W(ctx, name, wbytes, wflops, ...) \
+  DBSRG_RUN_SW(ctx, (ctx)->stream, name, wbytes, wflops, __VA_ARGS__)
 #define DBSRG_RUN(ctx, name, ...) DBSRG_RUN_W(ctx, name, 0, 0, __VA_ARGS__)
+#define DBSRG_RUN_S(ctx, strm, name, ...) DBSRG_RUN_SW(ctx, strm, name, 0, 0, __VA_ARGS__)
 
 bool is_device_ptr(const void *p);
 // copies n bytes from a host-or-device pointer into device memory dst
 int copy_in(dbsrg_ctx *c, void *dst, const void *src, size_t n);
+int copy_in_s(dbsrg_ctx *c, void *dst, const void *src, size_t n, cudaStream_t s);
+// waits for both streams and reports failures of queued kernels
+int drain(dbsrg_ctx *c);
+int ensure_lstate(dbsrg_ctx *c, int par, size_t bytes);
 int copy_out(dbsrg_ctx *c, void *dst, const void *src, size_t n);
 // scratch arenas (device)
 int ensure_scratch(dbsrg_ctx *c, size_t bytes);
@@ -185,7 +207,6 @@ int ensure_scratch2(dbsrg_ctx *c, size_t bytes);
 int ensure_tscratch(dbsrg_ctx *c, size_t bytes);
 int ensure_tcscratch(dbsrg_ctx *c, size_t bytes);
 int ensure_pscratch(dbsrg_ctx *c, size_t bytes);
-int ensure_lscratch(dbsrg_ctx *c, size_t bytes);
 int ensure_pinned(dbsrg_ctx *c, size_t bytes);
 // frees the far-field vectors, pair potentials and bound rows (they depend
 // on the orbitals and the tables)
@@ -273,7 +294,8 @@ int split_exchange(dbsrg_ctx *c, const SplitExchange &x);
 int get_pairpot_direct(dbsrg_ctx *c, int family, int type, int k, int icv, int jp1, int jp2,
                        const double **out);
 // pairs[e] = bmap[K2]*nbound + bmap[K3]; sets *derr when an orbital is not bound
-int pair_index(dbsrg_ctx *c, int n, const int *k2, const int *k3, int *pairs, int *derr);
+int pair_index(dbsrg_ctx *c, int n, const int *k2, const int *k3, int *pairs, int *derr,
+               cudaStream_t s);
 
 // ---- device helpers ---------------------------------------------------------
 // Values of the kx B-splines that are nonzero on the interval starting at

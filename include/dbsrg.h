@@ -173,8 +173,22 @@ int dbsrg_release_tables(dbsrg_ctx *ctx);
 
 /* Number of this library's kernels launched by the context so far. */
 long long dbsrg_kernel_launches(const dbsrg_ctx *ctx);
-/* Synchronise the context's stream. */
+/* Wait for every queued kernel of the context and report a failure of any
+ * of them (DBSRG_ETIMEOUT: a bounded wait of a tensor-core kernel ran out). */
 int dbsrg_sync(dbsrg_ctx *ctx);
+
+/* Asynchronous mode (off by default; no reference counterpart -- Gen_matrix
+ * returns with the matrix updated, gen_matrix.f90:2-17).  When on,
+ * dbsrg_gen_matrix returns once the list's kernels are queued: the host-side
+ * set-up of the next R/S list (segments, chunks, quadrant records) then
+ * overlaps the kernels of this one.  The lists may be reused or freed on
+ * return (they are copied during the call).  A failure of a queued kernel is
+ * reported by the next call that waits: dbsrg_sync, the read-outs
+ * (dbsrg_get_*), dbsrg_matrix_device_ptr and the state changes
+ * (dbsrg_set_orbitals, dbsrg_alloc_matrix, dbsrg_zero_matrix,
+ * dbsrg_set_precision, dbsrg_update_hx, dbsrg_release_tables, dbsrg_backward).
+ * dbsrg_gen_batch pipelines every context this way and waits at its end. */
+int dbsrg_set_async(dbsrg_ctx *ctx, int enable);
 
 /* Per-kernel device timing (no reference counterpart; it replaces the
  * CPU_time counters time_convol/time_density of dbsr_lib_dbs.f90:1106-1116
