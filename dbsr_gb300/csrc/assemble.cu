@@ -22,6 +22,7 @@
 #include "internal.cuh"
 
 #include <algorithm>
+#include <cmath>
 
 namespace {
 
@@ -470,69 +471,49 @@ __global__ void k_vch(int ns, int nbf, const double *fpbs, const double *fqbs,
   vch[q] = s;
 }
 
-// group entries by block, keeping list order (single thread, counting sort)
-__global__ void k_group_entries(int n, const int *k1, const int *k2, const double *cd,
-                                const int *ipbs, int nbf, const int *icc, int nch, int iicc,
-                                int *bcount, int *bstart, int *order, int *eblk, int *tlist,
-                                int *ntouched, int *err) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  for (int b = 0; b <= iicc; b++) bcount[b] = 0;
-  for (int e = 0; e < n; e++) {
-    eblk[e] = 0;
-    if (fabs(cd[e]) < 1.0e-10) continue;  // eps_c, mod_dbsr_mat.f90:56
-    int i1 = k1[e] / DBSRG_IBO, j1 = k2[e] / DBSRG_IBO;
-    if (i1 < 1 || i1 > nbf || j1 < 1 || j1 > nbf) { *err = 1; continue; }
-    int ich = ipbs[i1 - 1], jch = ipbs[j1 - 1];
-    if (ich < 1 || jch < 1 || ich > nch || jch > nch) { *err = 1; continue; }
-    int b = icc[(ich - 1) + (size_t)nch * (jch - 1)];
-    if (b < 1 || b > iicc) { *err = 2; continue; }
-    eblk[e] = b;
-    bcount[b]++;
-  }
-  int acc = 0, nt = 0;
-  for (int b = 0; b <= iicc; b++) {
-    bstart[b] = acc;
-    acc += bcount[b];
-    if (b > 0 && bcount[b] > 0) tlist[nt++] = b;
-    bcount[b] = 0;
-  }
-  *ntouched = nt;
-  bstart[iicc + 1] = acc;
-  for (int e = 0; e < n; e++) {
-    int b = eblk[e];
-    if (b) order[bstart[b] + bcount[b]++] = e;
-  }
-}
-
+// One thread per row r of a touched block and 32 consecutive columns: the
+// entries of the block in list order, each a rank-1 term with the row factor
+// formed once (one FMA per element and entry):
+//   ich > jch: C v(r) w(c);  ich < jch: C w(r) v(c);
+//   ich = jch: C/2 (v(r) w(c) + v(c) w(r))
 __global__ void k_overlap_update(int ns, const int *tlist, const int *bstart, const int *order,
                                  const int *k1, const int *k2, const double *cd,
                                  const int *ipbs, const double *vch, double *hch) {
+  constexpr int NC = 32;
   const int ms = 2 * ns;
-  int b = tlist[blockIdx.y];
-  int e0 = bstart[b], e1 = bstart[b + 1];
-  if (e0 == e1) return;
-  size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= (size_t)ms * ms) return;
-  int r = (int)(q % ms), c = (int)(q / ms);
-  double *h = hch + (size_t)(b - 1) * ms * ms + q;
-  double val = *h;
+  const int b = tlist[blockIdx.z];
+  const int e0 = bstart[b], e1 = bstart[b + 1];
+  const int r = blockIdx.x * blockDim.x + threadIdx.x, c0 = blockIdx.y * NC;
+  if (e0 == e1 || r >= ms) return;
+  const int ncol = min(NC, ms - c0);
+  double *h = hch + (size_t)(b - 1) * ms * ms + r + (size_t)ms * c0;
+  double val[NC];
+#pragma unroll
+  for (int j = 0; j < NC; j++) val[j] = j < ncol ? h[(size_t)ms * j] : 0.0;
   for (int t = e0; t < e1; t++) {
-    int e = order[t];
-    int i1 = k1[e] / DBSRG_IBO, i2 = k1[e] % DBSRG_IBO;
-    int j1 = k2[e] / DBSRG_IBO, j2 = k2[e] % DBSRG_IBO;
-    int ich = ipbs[i1 - 1], jch = ipbs[j1 - 1];
+    const int e = order[t];
+    const int i1 = k1[e] / DBSRG_IBO, i2 = k1[e] % DBSRG_IBO;
+    const int j1 = k2[e] / DBSRG_IBO, j2 = k2[e] % DBSRG_IBO;
+    const int ich = ipbs[i1 - 1], jch = ipbs[j1 - 1];
     const double *v = vch + (size_t)ms * (i2 - 1);
     const double *w = vch + (size_t)ms * (j2 - 1);
-    double C = cd[e], xx;
-    if (ich > jch)
-      xx = C * (v[r] * w[c]);
-    else if (jch > ich)
-      xx = C * (v[c] * w[r]);
-    else
-      xx = (C / 2.0) * (v[r] * w[c] + v[c] * w[r]);
-    val = val + xx;
+    const double C = cd[e];
+    if (ich != jch) {
+      const double *u = ich > jch ? w : v;  // column vector
+      const double a = C * (ich > jch ? v[r] : w[r]);
+#pragma unroll
+      for (int j = 0; j < NC; j++)
+        if (j < ncol) val[j] = fma(a, u[c0 + j], val[j]);
+    } else {
+      const double a1 = 0.5 * C * v[r], a2 = 0.5 * C * w[r];
+#pragma unroll
+      for (int j = 0; j < NC; j++)
+        if (j < ncol) val[j] = fma(a1, w[c0 + j], fma(a2, v[c0 + j], val[j]));
+    }
   }
-  *h = val;
+#pragma unroll
+  for (int j = 0; j < NC; j++)
+    if (j < ncol) h[(size_t)ms * j] = val[j];
 }
 
 // UPDATE_HX (updates.f90:79-106)
@@ -630,32 +611,59 @@ int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const 
   // ---- overlaps
   if (icase == 0) {
     if (itype != 3) return set_err(c, DBSRG_EINVAL, "O_data: only itype 3 is supported");
+    const int iicc = c->iicc;
     size_t vbytes = sizeof(double) * (size_t)ms * c->nbf;
-    rc = ensure_scratch(c, vbytes + sizeof(int) * ((size_t)2 * n + 3 * (c->iicc + 2)) + 1024);
+    rc = ensure_scratch(c, vbytes + sizeof(int) * ((size_t)n + 2 * (iicc + 2)) + 1024);
     if (rc) return rc;
     double *vch = (double *)c->scratch;
-    int *bcount = (int *)(vch + (size_t)ms * c->nbf);
-    int *bstart = bcount + (c->iicc + 2);
-    int *tlist = bstart + (c->iicc + 2);  // blocks with entries
-    int *order = tlist + (c->iicc + 2);
-    int *eblk = order + n;
+    int *bstart = (int *)(vch + (size_t)ms * c->nbf);
+    int *tlist = bstart + (iicc + 2);  // blocks with entries
+    int *order = tlist + (iicc + 2);
     DBSRG_RUN(c, "k_vch", k_vch<<<(2 * ns * c->nbf + 255) / 256, 256, 0, st>>>(ns, c->nbf, g.fpbs, g.fqbs, c->pq, vch));
-    DBSRG_RUN(c, "k_group_entries",
-              k_group_entries<<<1, 1, 0, st>>>(n, lk1, lk2, lcd, c->ipbs, c->nbf, c->icc, c->nch,
-                                               c->iicc, bcount, bstart, order, eblk, tlist,
-                                               dscal + 2, dscal + 1));
-    int ho[3] = {0, 0, 0};  // -, error, blocks touched
-    DBSRG_TRY(c, cudaMemcpyAsync(ho, dscal, 3 * sizeof(int), cudaMemcpyDeviceToHost, st));
+    // entries grouped by block on the host (counting sort, list order kept
+    // within a block); entries below eps_c are dropped (mod_dbsr_mat.f90:56)
+    std::vector<int> hk1(n), hk2(n);
+    std::vector<double> hcd(n);
+    DBSRG_TRY(c, cudaMemcpyAsync(hk1.data(), lk1, ibytes, cudaMemcpyDeviceToHost, st));
+    DBSRG_TRY(c, cudaMemcpyAsync(hk2.data(), lk2, ibytes, cudaMemcpyDeviceToHost, st));
+    DBSRG_TRY(c, cudaMemcpyAsync(hcd.data(), lcd, dbytes, cudaMemcpyDeviceToHost, st));
     DBSRG_TRY(c, cudaStreamSynchronize(st));
-    if (ho[1] == 1) return set_err(c, DBSRG_ERANGE, "channel or orbital index out of range in list");
-    if (ho[1] == 2) return set_err(c, DBSRG_ERANGE, "channel pair has no block in icc");
-    const int ntouched = ho[2];
-    if (ntouched < 0 || ntouched > c->iicc) return set_err(c, DBSRG_ECUDA, "inconsistent block list");
+    std::vector<int> eblk(n, 0), hstart(iicc + 2, 0), hlist, horder(n);
+    for (int e = 0; e < n; e++) {
+      if (std::fabs(hcd[e]) < 1.0e-10) continue;
+      const int i1 = hk1[e] / DBSRG_IBO, j1 = hk2[e] / DBSRG_IBO;
+      if (i1 < 1 || i1 > c->nbf || j1 < 1 || j1 > c->nbf || hk1[e] % DBSRG_IBO < 1 ||
+          hk1[e] % DBSRG_IBO > c->nbf || hk2[e] % DBSRG_IBO < 1 || hk2[e] % DBSRG_IBO > c->nbf)
+        return set_err(c, DBSRG_ERANGE, "channel or orbital index out of range in list");
+      const int ich = c->h_ipbs[i1 - 1], jch = c->h_ipbs[j1 - 1];
+      if (ich < 1 || jch < 1 || ich > c->nch || jch > c->nch)
+        return set_err(c, DBSRG_ERANGE, "channel or orbital index out of range in list");
+      const int b = c->h_icc[(ich - 1) + (size_t)c->nch * (jch - 1)];
+      if (b < 1 || b > iicc) return set_err(c, DBSRG_ERANGE, "channel pair has no block in icc");
+      eblk[e] = b;
+      hstart[b + 1]++;
+    }
+    for (int b = 1; b <= iicc; b++) {
+      if (hstart[b + 1] > 0) hlist.push_back(b);
+      hstart[b + 1] += hstart[b];
+    }
+    {
+      std::vector<int> fill(hstart.begin(), hstart.end());
+      for (int e = 0; e < n; e++)
+        if (eblk[e]) horder[fill[eblk[e]]++] = e;
+    }
+    const int ntouched = (int)hlist.size();
     if (ntouched > 0) {
-      dim3 grid((unsigned)(((size_t)ms * ms + 255) / 256), (unsigned)ntouched);
-      DBSRG_RUN(c, "k_overlap_update",
-                k_overlap_update<<<grid, 256, 0, st>>>(ns, tlist, bstart, order, lk1, lk2, lcd,
-                                                       c->ipbs, vch, c->hch));
+      if ((rc = copy_in(c, bstart, hstart.data(), sizeof(int) * (iicc + 2)))) return rc;
+      if ((rc = copy_in(c, tlist, hlist.data(), sizeof(int) * ntouched))) return rc;
+      if ((rc = copy_in(c, order, horder.data(), sizeof(int) * hstart[iicc + 1]))) return rc;
+      for (int t0 = 0; t0 < ntouched; t0 += 65535) {  // grid z limit
+        dim3 grid((unsigned)((ms + 127) / 128), (unsigned)((ms + 31) / 32),
+                  (unsigned)std::min(65535, ntouched - t0));
+        DBSRG_RUN(c, "k_overlap_update",
+                  k_overlap_update<<<grid, 128, 0, st>>>(ns, tlist + t0, bstart, order, lk1, lk2,
+                                                         lcd, c->ipbs, vch, c->hch));
+      }
     }
     DBSRG_TRY(c, cudaStreamSynchronize(st));
     return DBSRG_OK;

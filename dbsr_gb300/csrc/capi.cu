@@ -242,7 +242,7 @@ int dbsrg_destroy(dbsrg_ctx *c) {
   free_tables(c);
   DeviceGrid &g = c->g;
   double *arrs[] = {g.t, g.tp, g.tq, g.gx, g.gw, g.gr, g.grw, g.grm,
-                    g.pbsp, g.qbsp, g.fpbs, g.fqbs, g.fppqq};
+                    g.pbsp, g.qbsp, g.fpbs, g.fqbs, g.fppqq, g.tri};
   for (double *p : arrs)
     if (p) cudaFree(p);
   if (c->pq) cudaFree(c->pq);

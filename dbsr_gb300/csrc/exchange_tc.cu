@@ -98,18 +98,19 @@ struct ZArgs {
   double *Yb;         // [a][slot][ns*17]
 };
 
-// Per segment slot and atype, one thread per row y:
+// Per segment slot and atype, one thread per row y (ZROWS rows a block):
 //   Z_s(k,y) = sum_{e in s, first orbital k} c_e V(y, second orbital)  (Zl with Vl)
 //   Yb_s(y,d) = sum_e c_e Kb(pair_e; y, d)                             (near band)
 // then the digits of Z (and Zl) and their row exponents.
-__global__ void __launch_bounds__(128) k_zdigits(const ZArgs z) {
-  extern __shared__ double zs[];  // [2][32][128]: per thread one column
-  const int t = threadIdx.x, y = blockIdx.x * 128 + t, slot = blockIdx.y, a = blockIdx.z;
+constexpr int ZROWS = 64;
+__global__ void __launch_bounds__(ZROWS) k_zdigits(const ZArgs z) {
+  extern __shared__ double zs[];  // [2][32][ZROWS]: per thread one column
+  const int t = threadIdx.x, y = blockIdx.x * ZROWS + t, slot = blockIdx.y, a = blockIdx.z;
   const int ns = z.ns, nb = z.nb;
-  double *z0 = zs, *z1 = zs + 32 * 128;
+  double *z0 = zs, *z1 = zs + 32 * ZROWS;
   for (int k = 0; k < 32; k++) {
-    z0[k * 128 + t] = 0.0;
-    z1[k * 128 + t] = 0.0;
+    z0[k * ZROWS + t] = 0.0;
+    z1[k * ZROWS + t] = 0.0;
   }
   const SegInfo si = z.info[z.members[slot]];
   const double *V = z.V[a], *Vl = z.lower ? z.Vl[a] : nullptr, *Kb = z.Kb[a];
@@ -121,8 +122,8 @@ __global__ void __launch_bounds__(128) k_zdigits(const ZArgs z) {
     for (int e = si.start; e < si.end; e++) {
       const int pr = z.pairs[e], oa = pr / nb, ob = pr - oa * nb;
       const double c = z.cd[e];
-      z0[oa * 128 + t] = fma(c, V[(size_t)y + (size_t)ns * ob], z0[oa * 128 + t]);
-      if (Vl) z1[oa * 128 + t] = fma(c, Vl[(size_t)y + (size_t)ns * ob], z1[oa * 128 + t]);
+      z0[oa * ZROWS + t] = fma(c, V[(size_t)y + (size_t)ns * ob], z0[oa * ZROWS + t]);
+      if (Vl) z1[oa * ZROWS + t] = fma(c, Vl[(size_t)y + (size_t)ns * ob], z1[oa * ZROWS + t]);
       const double *kb = Kb + (size_t)pr * kper + y;
 #pragma unroll
       for (int d = 0; d < NDB; d++) band[d] = fma(c, kb[(size_t)ns * d], band[d]);
@@ -138,7 +139,7 @@ __global__ void __launch_bounds__(128) k_zdigits(const ZArgs z) {
     double m = 0.0;
 #pragma unroll
     for (int k = 0; k < 32; k++) {
-      vals[k] = zz[k * 128 + t];
+      vals[k] = zz[k * ZROWS + t];
       m = fmax(m, fabs(vals[k]));
     }
     const int e = scale_exp(m);
@@ -736,11 +737,12 @@ int split_exchange(dbsrg_ctx *c, const SplitExchange &x) {
   z.Zd = Zd;
   z.ez = ez;
   z.Yb = Yb;
-  const size_t zsm = 2 * 32 * 128 * sizeof(double);
+  const size_t zsm = 2 * 32 * ZROWS * sizeof(double);
   DBSRG_TRY(c, cudaFuncSetAttribute(k_zdigits, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)zsm));
   DBSRG_RUN(c, "k_zdigits",
-            k_zdigits<<<dim3((unsigned)ntx, (unsigned)x.nm, (unsigned)x.na), 128, zsm, st>>>(z));
+            k_zdigits<<<dim3((unsigned)(NR * 32 / ZROWS), (unsigned)x.nm, (unsigned)x.na), ZROWS,
+                        zsm, st>>>(z));  // every row of the operand, zeros past ns
   XArgs p{};
   p.ns = ns;
   p.NR = NR;

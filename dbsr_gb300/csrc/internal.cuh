@@ -31,6 +31,10 @@ struct DeviceGrid {
   double *gr = nullptr, *grw = nullptr, *grm = nullptr;
   double *pbsp = nullptr, *qbsp = nullptr;
   double *fpbs = nullptr, *fqbs = nullptr, *fppqq = nullptr;
+  // inner Gauss points of the diagonal cells (they depend on the grid only):
+  // per interval, for the ks x ks points (outer m, inner i): x, weight,
+  // P B-spline values (ksp each), Q B-spline values (ksq each)
+  double *tri = nullptr;
 };
 
 // resident cell moments and diagonal-cell integrals of one table

@@ -115,6 +115,8 @@ __global__ void k_gram(int ns, int nv, int ks, int kx, const double *b, const do
   ym[IDX2(off + i - 1, off + j - 1, ld)] = acc;
 }
 
+static int build_triang_points(dbsrg_ctx *c);
+
 int build_grid(dbsrg_ctx *c, const double *t_in) {
   DeviceGrid &g = c->g;
   const int ns = g.ns, ks = g.ks, nv = g.nv, nw = nv + 1, ms = g.ms;
@@ -151,6 +153,7 @@ int build_grid(dbsrg_ctx *c, const double *t_in) {
   DBSRG_TRY(c, cudaMemsetAsync(g.fppqq, 0, sizeof(double) * (size_t)ms * ms, s));
   DBSRG_RUN(c, "k_gram", k_gram<<<(nn + 255) / 256, 256, 0, s>>>(ns, nv, ks, g.ksp, g.pbsp, g.grw, g.fppqq, ms, 0));
   DBSRG_RUN(c, "k_gram", k_gram<<<(nn + 255) / 256, 256, 0, s>>>(ns, nv, ks, g.ksq, g.qbsp, g.grw, g.fppqq, ms, ns));
+  if ((rc = build_triang_points(c))) return rc;
   DBSRG_TRY(c, cudaStreamSynchronize(s));
   return DBSRG_OK;
 }
@@ -228,15 +231,39 @@ int compute_moments(dbsrg_ctx *c, int which, int k, double *rkm) {
 //   type 3 qpqp: rkd(Q pair, P pair) = the same two sums
 //   type 4 ppqq: rkd(inner (P,Q), outer (P,Q))
 //   type 5 pqqp: rkd(inner (P,Q), outer (Q,P))
-__global__ void k_triang(int nv, int ks, int ksp, int ksq, int type, int k, const double *t,
-                         const double *tp, const double *tq, const double *gx,
-                         const double *gw, const double *gr, const double *grm,
-                         const double *grw, const double *pbsp, const double *qbsp,
-                         double *rkd) {
+// Inner points of the diagonal cells of every interval iv: for outer point
+// r2 = gr(iv,m) the inner Gauss points x = t_iv + (r2 - t_iv) gx(i) on
+// [t_iv, r2], their weights (r2 - t_iv) gw(i) and the P and Q B-splines
+// there (zbsplvd recursion); one thread per (iv, m, i).
+__global__ void k_triang_points(int nv, int ks, int ksp, int ksq, const double *t,
+                                const double *tp, const double *tq, const double *gx,
+                                const double *gw, const double *gr, double *tri) {
+  const int KS2 = ks * ks;
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nv * KS2) return;
+  const int iv = q / KS2, p = q % KS2, m = p / ks, i = p % ks;
+  double *tb = tri + (size_t)iv * KS2 * (2 + ksp + ksq);
+  const double xbase = t[iv + ks - 1];
+  const double r2 = gr[IDX2(iv, m, nv)];
+  const double d = __dsub_rn(r2, xbase);
+  const double x = __dadd_rn(__dmul_rn(d, gx[i]), xbase);
+  tb[p] = x;
+  tb[KS2 + p] = __dmul_rn(d, gw[i]);
+  double v[DBSRG_MAXK];
+  bspline_values(tp, ksp, iv + ksp, x, v);
+  for (int j = 0; j < ksp; j++) tb[2 * KS2 + (size_t)p * ksp + j] = v[j];
+  bspline_values(tq, ksq, iv + ksq, x, v);
+  for (int j = 0; j < ksq; j++) tb[2 * KS2 + (size_t)KS2 * ksp + (size_t)p * ksq + j] = v[j];
+}
+
+__global__ void k_triang(int nv, int ks, int ksp, int ksq, int type, int k, const double *tri,
+                         const double *grm, const double *grw, const double *pbsp,
+                         const double *qbsp, double *rkd) {
   extern __shared__ double sm[];
   const int iv = blockIdx.x;  // 0-based interval
   const int nw = nv + 1, kk = ks * ks;
   const int KS2 = ks * ks;
+  const double *tb = tri + (size_t)iv * KS2 * (2 + ksp + ksq);  // x | w | BP | BQ
   double *wk = sm;                 // (m,i) inner weight * r^k       [ks*ks]
   double *BP = wk + KS2;           // (m,i,j) P values at inner pts  [ks*ks*ksp]
   double *BQ = BP + KS2 * ksp;     // (m,i,j) Q values               [ks*ks*ksq]
@@ -245,27 +272,16 @@ __global__ void k_triang(int nv, int ks, int ksp, int ksq, int type, int k, cons
   double *INTPQ = INTQ + ksq * ksq * ks; // P x Q                    [ksp*ksq*ks]
   double *gxo = INTPQ + ksp * ksq * ks;  // outer weights            [ks]
   double *A = gxo + ks;                  // a(ii,jj) for pppp/qqqq   [kk*kk]
+  // outer products b1(m,i) b2(m,ip) gxo(m) per pair and outer point, formed
+  // once per interval: OB1 for the first pair family, OB2 for the second
+  double *OB1 = A + kk * kk;             //                          [kk*ks]
+  double *OB2 = OB1 + kk * ks;           //                          [kk*ks]
 
-  const bool needP = true, needQ = (type != 0);
-  const double xbase = t[iv + ks - 1];
-  // phase 1: inner points, weights and B-spline values
-  for (int q = threadIdx.x; q < KS2; q += blockDim.x) {
-    int m = q / ks, i = q % ks;
-    double r2 = gr[IDX2(iv, m, nv)];
-    double d = __dsub_rn(r2, xbase);
-    double x = __dadd_rn(__dmul_rn(d, gx[i]), xbase);
-    double w = __dmul_rn(d, gw[i]);
-    wk[q] = __dmul_rn(w, ipow_d(x, k));
-    double v[DBSRG_MAXK];
-    if (needP) {
-      bspline_values(tp, ksp, iv + ksp, x, v);
-      for (int j = 0; j < ksp; j++) BP[(size_t)q * ksp + j] = v[j];
-    }
-    if (needQ || type == 1) {
-      bspline_values(tq, ksq, iv + ksq, x, v);
-      for (int j = 0; j < ksq; j++) BQ[(size_t)q * ksq + j] = v[j];
-    }
-  }
+  // phase 1: inner points, weights and B-spline values (k_triang_points)
+  for (int q = threadIdx.x; q < KS2; q += blockDim.x)
+    wk[q] = __dmul_rn(tb[KS2 + q], ipow_d(tb[q], k));
+  for (int q = threadIdx.x; q < KS2 * (ksp + ksq); q += blockDim.x)
+    BP[q] = tb[2 * KS2 + q];  // BQ follows BP in both layouts
   for (int m = threadIdx.x; m < ks; m += blockDim.x)
     gxo[m] = __dmul_rn(grw[IDX2(iv, m, nv)], ipow_d(grm[IDX2(iv, m, nv)], k + 1));
   __syncthreads();
@@ -304,19 +320,43 @@ __global__ void k_triang(int nv, int ks, int ksp, int ksq, int type, int k, cons
     *i = row;
     *ip = row + r;
   };
+  // triangular pairs (i <= ip) of one basis: OB[ii*ks + m]
+  auto fill_tri = [&](const double *bs, int kx, double *OB) {
+    const int ik = kx * (kx + 1) / 2;
+    for (int q = threadIdx.x; q < ik * ks; q += blockDim.x) {
+      const int ii = q / ks, m = q % ks;
+      int i, ip;
+      pair_of(ii, kx, &i, &ip);
+      OB[q] = ob(bs, i, bs, ip, m);
+    }
+  };
+  if (type == 0) fill_tri(pbsp, ksp, OB1);
+  if (type == 1) fill_tri(qbsp, ksq, OB1);
+  if (type == 2 || type == 3) {
+    fill_tri(pbsp, ksp, OB1);
+    fill_tri(qbsp, ksq, OB2);
+  }
+  if (type == 4 || type == 5) {  // outer (P,Q) pairs ii = i*ksq + ip, or (Q,P) ii = i*ksp + ip
+    const int np = ksp * ksq;
+    for (int q = threadIdx.x; q < np * ks; q += blockDim.x) {
+      const int ii = q / ks, m = q % ks;
+      OB1[q] = type == 4 ? ob(pbsp, ii / ksq, qbsp, ii % ksq, m)
+                         : ob(qbsp, ii / ksp, pbsp, ii % ksp, m);
+    }
+  }
+  __syncthreads();
   if (type == 0 || type == 1) {
     const int kx = type == 0 ? ksp : ksq;
-    const double *bs = type == 0 ? pbsp : qbsp;
     const double *INT = type == 0 ? INTP : INTQ;
     const int ik = kx * (kx + 1) / 2;
     for (int q = threadIdx.x; q < ik * ik; q += blockDim.x) {
       int ii = q % ik, jj = q / ik;
-      int i, ip, j, jp;
-      pair_of(ii, kx, &i, &ip);
+      int j, jp;
       pair_of(jj, kx, &j, &jp);
+      const double *o = OB1 + ii * ks;
       double s = 0.0;
       for (int m = 0; m < ks; m++)
-        s = __dadd_rn(s, __dmul_rn(ob(bs, i, bs, ip, m), INT[j + kx * (jp + kx * m)]));
+        s = __dadd_rn(s, __dmul_rn(o[m], INT[j + kx * (jp + kx * m)]));
       A[q] = s;
     }
     __syncthreads();
@@ -334,11 +374,12 @@ __global__ void k_triang(int nv, int ks, int ksp, int ksq, int type, int k, cons
         int i, ip, j, jp;
         pair_of(pp_, ksp, &i, &ip);
         pair_of(qq_, ksq, &j, &jp);
+        const double *o1 = OB1 + pp_ * ks, *o2 = OB2 + qq_ * ks;
         double s1 = 0.0, s2 = 0.0;
         for (int m = 0; m < ks; m++)
-          s1 = __dadd_rn(s1, __dmul_rn(ob(pbsp, i, pbsp, ip, m), INTQ[j + ksq * (jp + ksq * m)]));
+          s1 = __dadd_rn(s1, __dmul_rn(o1[m], INTQ[j + ksq * (jp + ksq * m)]));
         for (int m = 0; m < ks; m++)
-          s2 = __dadd_rn(s2, __dmul_rn(ob(qbsp, j, qbsp, jp, m), INTP[i + ksp * (ip + ksp * m)]));
+          s2 = __dadd_rn(s2, __dmul_rn(o2[m], INTP[i + ksp * (ip + ksp * m)]));
         v = __dadd_rn(s1, s2);
       }
       out[q] = v;
@@ -350,16 +391,10 @@ __global__ void k_triang(int nv, int ks, int ksp, int ksq, int type, int k, cons
       double v = 0.0;
       if (jj < np && ii < np) {
         int j = jj / ksq, jp = jj % ksq;
-        int i, ip;
-        const double *b1, *b2;
-        if (type == 4) {
-          i = ii / ksq; ip = ii % ksq; b1 = pbsp; b2 = qbsp;
-        } else {
-          i = ii / ksp; ip = ii % ksp; b1 = qbsp; b2 = pbsp;
-        }
+        const double *o = OB1 + ii * ks;
         double s = 0.0;
         for (int m = 0; m < ks; m++)
-          s = __dadd_rn(s, __dmul_rn(ob(b1, i, b2, ip, m), INTPQ[j + ksp * (jp + ksq * m)]));
+          s = __dadd_rn(s, __dmul_rn(o[m], INTPQ[j + ksp * (jp + ksq * m)]));
         v = s;
       }
       out[q] = v;
@@ -367,18 +402,31 @@ __global__ void k_triang(int nv, int ks, int ksp, int ksq, int type, int k, cons
   }
 }
 
+static int build_triang_points(dbsrg_ctx *c) {
+  DeviceGrid &g = c->g;
+  const int KS2 = g.ks * g.ks;
+  const size_t n = (size_t)g.nv * KS2 * (2 + g.ksp + g.ksq);
+  DBSRG_TRY(c, cudaMalloc((void **)&g.tri, n * sizeof(double)));
+  const int nq = g.nv * KS2;
+  DBSRG_RUN(c, "k_triang_points",
+            k_triang_points<<<(nq + 127) / 128, 128, 0, c->stream>>>(
+                g.nv, g.ks, g.ksp, g.ksq, g.t, g.tp, g.tq, g.gx, g.gw, g.gr, g.tri));
+  return DBSRG_OK;
+}
+
 int compute_diag_cells(dbsrg_ctx *c, int type, int k, double *rkd) {
   const DeviceGrid &g = c->g;
   const int ks = g.ks, kk = ks * ks;
   size_t nsm = (size_t)ks * ks + (size_t)ks * ks * g.ksp + (size_t)ks * ks * g.ksq +
                (size_t)g.ksp * g.ksp * ks + (size_t)g.ksq * g.ksq * ks +
-               (size_t)g.ksp * g.ksq * ks + ks + (size_t)kk * kk;
+               (size_t)g.ksp * g.ksq * ks + ks + (size_t)kk * kk + 2 * (size_t)kk * ks;
   size_t bytes = nsm * sizeof(double);
   if (bytes > 48 * 1024)
     DBSRG_TRY(c, cudaFuncSetAttribute(k_triang, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)bytes));
-  DBSRG_RUN(c, "k_triang", k_triang<<<g.nv, 256, bytes, c->stream>>>(g.nv, ks, g.ksp, g.ksq, type, k, g.t, g.tp, g.tq,
-                                            g.gx, g.gw, g.gr, g.grm, g.grw, g.pbsp, g.qbsp, rkd));
+  DBSRG_RUN(c, "k_triang",
+            k_triang<<<g.nv, 256, bytes, c->stream>>>(g.nv, ks, g.ksp, g.ksq, type, k, g.tri,
+                                                      g.grm, g.grw, g.pbsp, g.qbsp, rkd));
   return DBSRG_OK;
 }
 
