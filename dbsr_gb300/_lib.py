@@ -19,6 +19,10 @@ STATUS = {0: "OK", -1: "EINVAL", -2: "ECUDA", -3: "ENOMEM", -4: "ERANGE", -5: "E
           -6: "ETIMEOUT"}
 
 # (name, restype, argtypes) for every entry point of include/dbsrg.h
+# void fn(void *user, int ictx, int blo, int nblocks, const double *window)
+WindowFn = C.CFUNCTYPE(None, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p)
+
+
 class ListDesc(C.Structure):
     """dbsrg_list of include/dbsrg.h"""
 
@@ -49,10 +53,14 @@ SIGNATURES = [
     ("dbsrg_kernel_launches", C.c_longlong, [_vp]),
     ("dbsrg_sync", C.c_int, [_vp]),
     ("dbsrg_set_async", C.c_int, [_vp, C.c_int]),
+    ("dbsrg_alloc_matrix_window", C.c_int, [_vp, C.c_int, _vp, C.c_int, C.c_int, C.c_int]),
+    ("dbsrg_set_window", C.c_int, [_vp, C.c_int]),
+    ("dbsrg_window_blocks", C.c_int, [_vp]),
     ("dbsrg_release_tables", C.c_int, [_vp]),
     ("dbsrg_timing", C.c_int, [_vp, C.c_int]),
     ("dbsrg_timing_report", C.c_int, [_vp, C.c_char_p, C.c_size_t]),
     ("dbsrg_gen_batch", C.c_int, [C.c_int, _vp, _vp, _vp]),
+    ("dbsrg_gen_batch_streamed", C.c_int, [C.c_int, _vp, _vp, _vp, _vp, _vp]),
     ("dbsrg_backward", C.c_int, [_vp, C.c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     ("dbsrg_exchange_segment_noalloc", C.c_int,
      [C.c_int, C.c_int, _vp, _vp, C.c_int, C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, _vp, _vp]),

@@ -95,12 +95,39 @@ class Assembler:
         check(self._h, self._L.dbsrg_set_orbitals(self._h, nbf, p, q), "set_orbitals")
         self.nbf = nbf
 
-    def alloc_matrix(self, nch: int, icc, iicc: int, mk: int):
+    def alloc_matrix(self, nch: int, icc, iicc: int, mk: int, window: int | None = None):
+        """hch(ms,ms,iicc) on the device, or a window of `window` consecutive
+        blocks of it (streamed assembly: set_window, stream)."""
         icc = np.asfortranarray(icc, dtype=np.int32)
         p, keep = _ptr(icc, np.int32)
-        check(self._h, self._L.dbsrg_alloc_matrix(self._h, nch, p, iicc, mk), "alloc_matrix")
+        if window is None:
+            rc = self._L.dbsrg_alloc_matrix(self._h, nch, p, iicc, mk)
+        else:
+            rc = self._L.dbsrg_alloc_matrix_window(self._h, nch, p, iicc, mk, int(window))
+        check(self._h, rc, "alloc_matrix")
         self.nch, self.iicc, self.mk = nch, iicc, mk
+        self.wcap = iicc if window is None else int(window)
         self.icc = icc
+
+    def set_window(self, blo: int):
+        """Hold (and zero) blocks blo .. blo + window - 1."""
+        check(self._h, self._L.dbsrg_set_window(self._h, int(blo)), "set_window")
+
+    @property
+    def window_blocks(self) -> int:
+        return int(self._L.dbsrg_window_blocks(self._h))
+
+    def stream(self, lists):
+        """Assemble the matrix window by window: every list (icase, itype, kpol,
+        k1, k2, k3, k4, cdata) once per window.  Yields (first block, number of
+        blocks) with the window assembled on the device; read it (get_matrix,
+        matrix_device_ptr) before the generator advances."""
+        for blo in range(1, self.iicc + 1, self.wcap):
+            self.set_window(blo)
+            for item in lists:
+                self.gen_matrix(*item[:8])
+            self.sync()
+            yield blo, self.window_blocks
 
     def zero_matrix(self):
         check(self._h, self._L.dbsrg_zero_matrix(self._h), "zero_matrix")
@@ -152,8 +179,9 @@ class Assembler:
         return out
 
     def get_matrix(self, out=None):
+        """The blocks held: all of hch, or the current window's blocks."""
         if out is None:
-            out = np.zeros((self.ms, self.ms, self.iicc), order="F")
+            out = np.zeros((self.ms, self.ms, self.window_blocks), order="F")
         p, keep = _ptr(out, np.float64)
         check(self._h, self._L.dbsrg_get_matrix(self._h, p), "get_matrix")
         return out
@@ -231,10 +259,7 @@ class Assembler:
         check(self._h, self._L.dbsrg_set_async(self._h, int(enable)), "set_async")
 
 
-def gen_batch(assemblers, lists_per_assembler):
-    """dbsrg_gen_batch: every assembler's lists (icase, itype, kpol, k1, k2, k3,
-    k4, cdata[, ipt]) through Gen_matrix, the assemblers concurrently."""
-    L = load()
+def _list_descs(lists_per_assembler):
     descs, keep, counts = [], [], []
     for lists in lists_per_assembler:
         counts.append(len(lists))
@@ -248,8 +273,24 @@ def gen_batch(assemblers, lists_per_assembler):
                 ptrs.append(p.value if p is not None else None)
                 keep.append(kk)
             descs.append(_lib.ListDesc(icase, itype, kpol, int(len(k1)), *ptrs))
-    n = len(assemblers)
     arr = (_lib.ListDesc * max(1, len(descs)))(*descs)
+    return arr, keep, counts
+
+
+def _raise_batch(L, assemblers, rc, what):
+    for a in assemblers:
+        msg = L.dbsrg_last_error(a._h).decode()
+        if msg:
+            check(a._h, rc, what)
+    check(None, rc, what)
+
+
+def gen_batch(assemblers, lists_per_assembler):
+    """dbsrg_gen_batch: every assembler's lists (icase, itype, kpol, k1, k2, k3,
+    k4, cdata[, ipt]) through Gen_matrix, the assemblers concurrently."""
+    L = load()
+    arr, keep, counts = _list_descs(lists_per_assembler)
+    n = len(assemblers)
     ctxs = (C.c_void_p * max(1, n))(*[a._h.value for a in assemblers])
     cnt = (C.c_int * max(1, n))(*counts)
     rc = L.dbsrg_gen_batch(n, ctxs, cnt, arr)
@@ -259,3 +300,33 @@ def gen_batch(assemblers, lists_per_assembler):
             if msg:
                 check(a._h, rc, "gen_batch")
         check(None, rc, "gen_batch")
+
+
+def gen_batch_streamed(assemblers, lists_per_assembler, consumer):
+    """dbsrg_gen_batch_streamed: the assemblers (each allocated with a block
+    window) run their lists once per window, concurrently; after every window
+    consumer(i, blo, nblocks, device_ptr) is called for assembler i (from the
+    assembler's host thread, one call at a time) and may read the window, e.g.
+    with assemblers[i].get_matrix(out=...).  An exception in the consumer is
+    raised once the batch returns."""
+    L = load()
+    arr, keep, counts = _list_descs(lists_per_assembler)
+    n = len(assemblers)
+    ctxs = (C.c_void_p * max(1, n))(*[a._h.value for a in assemblers])
+    cnt = (C.c_int * max(1, n))(*counts)
+    errors = []
+
+    def fn(user, ictx, blo, nblocks, ptr):
+        if errors:
+            return
+        try:
+            consumer(int(ictx), int(blo), int(nblocks), int(ptr or 0))
+        except BaseException as e:  # surfaces after the batch
+            errors.append(e)
+
+    cb = _lib.WindowFn(fn)
+    rc = L.dbsrg_gen_batch_streamed(n, ctxs, cnt, arr, C.cast(cb, C.c_void_p), None)
+    if errors:
+        raise errors[0]
+    if rc != 0:
+        _raise_batch(L, assemblers, rc, "gen_batch_streamed")

@@ -535,6 +535,7 @@ int update_hx(dbsrg_ctx *c, int ich, int jch, const double *d, double cc) {
     return set_err(c, DBSRG_ERANGE, "UPDATE_HX: channel out of range");
   int b = c->h_icc[(ich - 1) + (size_t)c->nch * (jch - 1)];
   if (b < 1 || b > c->iicc) return set_err(c, DBSRG_ERANGE, "UPDATE_HX: i out of range");
+  if (!in_window(c, b)) return DBSRG_OK;  // the block is assembled in another window
   const double *dd = d;
   size_t bytes = sizeof(double) * (size_t)ms * ms;
   if (!is_device_ptr(d)) {
@@ -546,7 +547,7 @@ int update_hx(dbsrg_ctx *c, int ich, int jch, const double *d, double cc) {
   }
   size_t n = (size_t)ms * ms;
   DBSRG_RUN(c, "k_update_hx", k_update_hx<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(
-      ms, ich, jch, dd, cc, c->hch + (size_t)(b - 1) * ms * ms));
+      ms, ich, jch, dd, cc, hch_base(c) + (size_t)(b - 1) * ms * ms));
   DBSRG_TRY(c, cudaStreamSynchronize(c->stream));
   return DBSRG_OK;
 }
@@ -640,6 +641,7 @@ int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const 
         return set_err(c, DBSRG_ERANGE, "channel or orbital index out of range in list");
       const int b = c->h_icc[(ich - 1) + (size_t)c->nch * (jch - 1)];
       if (b < 1 || b > iicc) return set_err(c, DBSRG_ERANGE, "channel pair has no block in icc");
+      if (!in_window(c, b)) continue;
       eblk[e] = b;
       hstart[b + 1]++;
     }
@@ -662,7 +664,7 @@ int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const 
                   (unsigned)std::min(65535, ntouched - t0));
         DBSRG_RUN(c, "k_overlap_update",
                   k_overlap_update<<<grid, 128, 0, st>>>(ns, tlist + t0, bstart, order, lk1, lk2,
-                                                         lcd, c->ipbs, vch, c->hch));
+                                                         lcd, c->ipbs, vch, hch_base(c)));
       }
     }
     DBSRG_TRY(c, cudaStreamSynchronize(st));
@@ -814,7 +816,7 @@ int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const 
       own.clear();
     };
     for (int s = 0; s < nseg; s++) {
-      if (!hinfo[s].owner) continue;
+      if (!hinfo[s].owner || !in_window(c, hinfo[s].blk)) continue;
       own.push_back((int)mem.size());
       mem.push_back(s);
       if (hinfo[s].partner >= 0) mem.push_back(hinfo[s].partner);
@@ -829,7 +831,7 @@ int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const 
   std::vector<int> hown;
   if (icase == 2 && itype == 3)
     for (int s = 0; s < nseg; s++)
-      if (hinfo[s].owner) hown.push_back(s);
+      if (hinfo[s].owner && in_window(c, hinfo[s].blk)) hown.push_back(s);
   // the host-built work lists go to the list state on the set-up stream;
   // the contraction waits for the set-up
   if (!hbuf.empty() && (rc = copy_in_s(c, members, hbuf.data(), sizeof(int) * hbuf.size(), ss)))
@@ -913,7 +915,7 @@ int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const 
     dim3 gs((unsigned)((space + 255) / 256), (unsigned)nown);
     DBSRG_RUN(c, "k_scatter",
               k_scatter<<<gs, 256, 0, st>>>(ns, ks, mode, ssp, nm, mb, ob, info,
-                                            Y, c->hch));
+                                            Y, hch_base(c)));
     return DBSRG_OK;
   };
   for (const Chunk &ch : chunks)

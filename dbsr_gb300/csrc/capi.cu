@@ -59,6 +59,9 @@ int drain(dbsrg_ctx *c) {
   return set_err(c, DBSRG_ECUDA, "tensor-core exchange: inconsistent tile terms");
 }
 
+// blocks of the current window that exist (the last window may run past iicc)
+static int window_blocks(const dbsrg_ctx *c) { return std::min(c->wcap, c->iicc - c->wlo + 1); }
+
 // queued work of the asynchronous mode is finished (and its errors read)
 // before any call that reads results or changes state
 #define SETTLE(c)                  \
@@ -397,7 +400,12 @@ int dbsrg_set_orbitals(dbsrg_ctx *c, int nbf, const double *pq, const int *ipbs)
 }
 
 int dbsrg_alloc_matrix(dbsrg_ctx *c, int nch, const int *icc, int iicc, int mk) {
-  if (!c || nch < 1 || !icc || iicc < 1 || mk < 0)
+  return dbsrg_alloc_matrix_window(c, nch, icc, iicc, mk, iicc);
+}
+
+int dbsrg_alloc_matrix_window(dbsrg_ctx *c, int nch, const int *icc, int iicc, int mk,
+                              int nwin) {
+  if (!c || nch < 1 || !icc || iicc < 1 || mk < 0 || nwin < 1 || nwin > iicc)
     return set_err(c, DBSRG_EINVAL, "bad matrix arguments");
   cudaSetDevice(c->device);
   SETTLE(c);
@@ -417,14 +425,29 @@ int dbsrg_alloc_matrix(dbsrg_ctx *c, int nch, const int *icc, int iicc, int mk) 
     if (v < 0 || v > iicc) return set_err(c, DBSRG_ERANGE, "icc entry out of range");
   const size_t ms = c->g.ms;
   DBSRG_TRY(c, cudaMalloc((void **)&c->icc, sizeof(int) * (size_t)nch * nch));
-  DBSRG_TRY(c, cudaMalloc((void **)&c->hch, sizeof(double) * ms * ms * iicc));
+  DBSRG_TRY(c, cudaMalloc((void **)&c->hch, sizeof(double) * ms * ms * nwin));
   DBSRG_TRY(c, cudaMalloc((void **)&c->acf, sizeof(double) * (size_t)iicc * (mk + 1)));
   int rc = copy_in(c, c->icc, c->h_icc.data(), sizeof(int) * (size_t)nch * nch);
   if (rc) return rc;
   c->nch = nch;
   c->iicc = iicc;
   c->mk = mk;
+  c->wlo = 1;
+  c->wcap = nwin;
   return dbsrg_zero_matrix(c);
+}
+
+int dbsrg_set_window(dbsrg_ctx *c, int blo) {
+  if (!c) return DBSRG_EINVAL;
+  if (!c->hch) return set_err(c, DBSRG_ESTATE, "no matrix allocated");
+  if (blo < 1 || blo > c->iicc) return set_err(c, DBSRG_ERANGE, "window start out of range");
+  cudaSetDevice(c->device);
+  SETTLE(c);
+  c->wlo = blo;
+  const size_t ms = c->g.ms;
+  DBSRG_TRY(c, cudaMemsetAsync(c->hch, 0, sizeof(double) * ms * ms * c->wcap, c->stream));
+  DBSRG_TRY(c, cudaStreamSynchronize(c->stream));
+  return DBSRG_OK;
 }
 
 int dbsrg_zero_matrix(dbsrg_ctx *c) {
@@ -432,7 +455,7 @@ int dbsrg_zero_matrix(dbsrg_ctx *c) {
   cudaSetDevice(c->device);
   SETTLE(c);
   const size_t ms = c->g.ms;
-  DBSRG_TRY(c, cudaMemsetAsync(c->hch, 0, sizeof(double) * ms * ms * c->iicc, c->stream));
+  DBSRG_TRY(c, cudaMemsetAsync(c->hch, 0, sizeof(double) * ms * ms * c->wcap, c->stream));
   DBSRG_TRY(c, cudaMemsetAsync(c->acf, 0, sizeof(double) * (size_t)c->iicc * (c->mk + 1), c->stream));
   DBSRG_TRY(c, cudaStreamSynchronize(c->stream));
   return DBSRG_OK;
@@ -498,6 +521,50 @@ int dbsrg_gen_batch(int nctx, dbsrg_ctx *const *ctxs, const int *nlists,
   return DBSRG_OK;
 }
 
+int dbsrg_gen_batch_streamed(int nctx, dbsrg_ctx *const *ctxs, const int *nlists,
+                             const dbsrg_list *lists, dbsrg_window_fn fn, void *user) {
+  if (nctx < 0 || (nctx > 0 && (!ctxs || !nlists)) || !fn) return DBSRG_EINVAL;
+  std::vector<size_t> off((size_t)nctx + 1, 0);
+  for (int i = 0; i < nctx; i++) {
+    if (!ctxs[i] || nlists[i] < 0) return DBSRG_EINVAL;
+    if (!ctxs[i]->hch) return set_err(ctxs[i], DBSRG_ESTATE, "no matrix allocated");
+    off[i + 1] = off[i] + (size_t)nlists[i];
+  }
+  if (off[nctx] > 0 && !lists) return DBSRG_EINVAL;
+  for (int i = 0; i < nctx; i++)
+    for (int j = i + 1; j < nctx; j++)
+      if (ctxs[i] == ctxs[j]) return set_err(ctxs[i], DBSRG_EINVAL, "gen_batch: context twice");
+  std::vector<int> rc((size_t)nctx, DBSRG_OK);
+  // per context: every window in turn, the lists pipelined within a window,
+  // then the window handed to the consumer
+  auto work = [&](int i) {
+    dbsrg_ctx *c = ctxs[i];
+    cudaSetDevice(c->device);
+    const bool was = c->async;
+    for (int blo = 1; blo <= c->iicc && rc[i] == DBSRG_OK; blo += c->wcap) {
+      if ((rc[i] = dbsrg_set_window(c, blo))) break;
+      c->async = true;
+      for (size_t l = off[i]; l < off[i + 1] && rc[i] == DBSRG_OK; l++) {
+        const dbsrg_list &L = lists[l];
+        rc[i] = dbsrg_gen_matrix(c, L.icase, L.itype, L.kpol, L.ncdata, L.ipt, L.k1, L.k2, L.k3,
+                                 L.k4, L.cdata);
+      }
+      c->async = was;
+      const int rd = drain(c);
+      if (rc[i] == DBSRG_OK) rc[i] = rd;
+      if (rc[i] == DBSRG_OK) fn(user, i, blo, window_blocks(c), c->hch);
+    }
+    c->async = was;
+  };
+  std::vector<std::thread> th;
+  for (int i = 1; i < nctx; i++) th.emplace_back(work, i);
+  if (nctx > 0) work(0);
+  for (auto &t : th) t.join();
+  for (int i = 0; i < nctx; i++)
+    if (rc[i] != DBSRG_OK) return rc[i];
+  return DBSRG_OK;
+}
+
 int dbsrg_update_hx(dbsrg_ctx *c, int ich, int jch, const double *d, double cc) {
   if (!c || !d) return set_err(c, DBSRG_EINVAL, "bad UPDATE_HX arguments");
   cudaSetDevice(c->device);
@@ -514,8 +581,9 @@ int dbsrg_get_block(dbsrg_ctx *c, int ich, int jch, double *out) {
     return set_err(c, DBSRG_ERANGE, "channel out of range");
   int b = c->h_icc[(ich - 1) + (size_t)c->nch * (jch - 1)];
   if (b < 1) return set_err(c, DBSRG_ERANGE, "channel pair has no block");
+  if (!in_window(c, b)) return set_err(c, DBSRG_ESTATE, "block outside the current window");
   const size_t ms = c->g.ms;
-  return copy_out(c, out, c->hch + (size_t)(b - 1) * ms * ms, sizeof(double) * ms * ms);
+  return copy_out(c, out, c->hch + (size_t)(b - c->wlo) * ms * ms, sizeof(double) * ms * ms);
 }
 
 int dbsrg_get_matrix(dbsrg_ctx *c, double *out) {
@@ -524,7 +592,7 @@ int dbsrg_get_matrix(dbsrg_ctx *c, double *out) {
   SETTLE(c);
   if (!c->hch) return set_err(c, DBSRG_ESTATE, "no matrix allocated");
   const size_t ms = c->g.ms;
-  return copy_out(c, out, c->hch, sizeof(double) * ms * ms * c->iicc);
+  return copy_out(c, out, c->hch, sizeof(double) * ms * ms * window_blocks(c));
 }
 
 int dbsrg_get_acf(dbsrg_ctx *c, double *out) {
@@ -534,6 +602,8 @@ int dbsrg_get_acf(dbsrg_ctx *c, double *out) {
   if (!c->acf) return set_err(c, DBSRG_ESTATE, "no matrix allocated");
   return copy_out(c, out, c->acf, sizeof(double) * (size_t)c->iicc * (c->mk + 1));
 }
+
+int dbsrg_window_blocks(const dbsrg_ctx *c) { return c && c->hch ? window_blocks(c) : 0; }
 
 int dbsrg_matrix_device_ptr(dbsrg_ctx *c, double **p) {
   if (!c || !p) return DBSRG_EINVAL;

@@ -760,7 +760,7 @@ int split_exchange(dbsrg_ctx *c, const SplitExchange &x) {
   p.ez = ez;
   p.Yb = Yb;
   p.xq = x.xq;
-  p.hch = c->hch;
+  p.hch = hch_base(c);
   p.err = c->kerr;
   const size_t smem = 2 * TS * (size_t)(A_BYTES + B_BYTES) +
                       ((size_t)MAXT * NDB * 128 + 32 * 128) * sizeof(double);

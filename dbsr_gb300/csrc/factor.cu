@@ -955,7 +955,7 @@ int factored_contract(dbsrg_ctx *c, const FactorJob &j) {
     dim3 gs((unsigned)(4 * nt * nt), (unsigned)j.nown);
     DBSRG_RUN(c, "k_scatter_x",
               k_scatter_x<<<gs, 256, 0, st>>>(ns, qs, j.nm, j.members, j.own, j.info, j.Y,
-                                              j.family == 0 ? 1 : 0, c->hch));
+                                              j.family == 0 ? 1 : 0, hch_base(c)));
     return DBSRG_OK;
   }
   // direct
@@ -969,6 +969,6 @@ int factored_contract(dbsrg_ctx *c, const FactorJob &j) {
   dim3 gs((unsigned)((space + 255) / 256), (unsigned)j.nown);
   DBSRG_RUN(c, "k_scatter_dp",
             k_scatter_dp<<<gs, 256, 0, st>>>(ns, ks, j.sym, qs, kd, j.members, j.own, j.info,
-                                             j.pairs, j.cd, c->hch));
+                                             j.pairs, j.cd, hch_base(c)));
   return DBSRG_OK;
 }

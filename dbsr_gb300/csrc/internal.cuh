@@ -131,6 +131,10 @@ struct dbsrg_ctx {
   // waits (dbsrg_sync, the read-outs, state changes)
   bool async = false;
   bool pending = false;
+  // block window: hch holds blocks wlo .. wlo + wcap - 1 of 1 .. iicc (all
+  // of them unless dbsrg_alloc_matrix_window asked for fewer); Gen_matrix
+  // skips the segments of blocks outside the window
+  int wlo = 1, wcap = 0;
   // error word of the tensor-core kernels (bounded waits), read whenever the
   // context waits for its stream
   int *kerr = nullptr;
@@ -150,6 +154,16 @@ struct dbsrg_ctx {
 };
 
 cudaEvent_t event_get(dbsrg_ctx *c);
+
+// block b (1-based) of the matrix is held by the current window
+inline bool in_window(const dbsrg_ctx *c, int b) { return b >= c->wlo && b < c->wlo + c->wcap; }
+// base the kernels index blocks from, hch + (b - 1) ms^2 for block b: the
+// window's storage shifted by its first block (only blocks inside the window
+// are ever addressed)
+inline double *hch_base(const dbsrg_ctx *c) {
+  const size_t shift = (size_t)(c->wlo - 1) * c->g.ms * c->g.ms * sizeof(double);
+  return reinterpret_cast<double *>(reinterpret_cast<uintptr_t>(c->hch) - shift);
+}
 
 // ---- error helpers -------------------------------------------------------
 int set_err(dbsrg_ctx *c, int code, const std::string &msg);

@@ -340,6 +340,20 @@ def small(ns=60, nch=3, mk=3, n_entries=300, breit=True, seed=99, rmax=20.0, z=8
                   occupancy, breit=breit, o_entries=20)
 
 
+def config3_block(index: int, nch_max: int = 300, rows_entries: float = 1e4,
+                  seed: int = 1237) -> Workload:
+    """Block `index` of config3(nch_max=nch_max, ...), built alone (the draws of
+    the earlier blocks are replayed without building them)."""
+    rng = np.random.Generator(np.random.Philox(seed))
+    for b in range(index + 1):
+        ns = int(rng.integers(150, 451))
+        nch = int(round(math.exp(rng.uniform(math.log(10), math.log(nch_max)))))
+        kap = [int(k) * int(s) for k, s in zip(rng.integers(1, 7, nch), rng.choice([-1, 1], nch))]
+    return _build(f"config3 block {index}: ns={ns} nch={nch} k=0..8", seed + 17 * (index + 1), ns,
+                  40.0, 26.0, TARGET_ORBITALS[:20], kap, 8, max(1, int(rows_entries * nch)), 0.05,
+                  breit=True, o_entries=max(1, nch))
+
+
 def config3(nblocks: int = 64, nch_max: int = 300, rows_entries: float = 1e4,
             seed: int = 1237) -> list:
     """Batched form: ``nblocks`` independent J-parity blocks, each with its own

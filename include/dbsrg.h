@@ -95,6 +95,22 @@ int dbsrg_alloc_matrix(dbsrg_ctx *ctx, int nch, const int *icc, int iicc,
                        int mk);
 int dbsrg_zero_matrix(dbsrg_ctx *ctx);
 
+/* Streamed output for matrices larger than the device memory (no reference
+ * counterpart: Alloc_dbsr_matrix holds all of hch).  The device holds a
+ * window of nwin consecutive blocks, blocks blo .. blo+nwin-1 after
+ * dbsrg_set_window(blo) (blocks 1 .. nwin after the allocation); acf is
+ * held whole.  dbsrg_gen_matrix then adds only the entries of blocks in the
+ * window (the others are skipped, not errors), as do dbsrg_update_hx and
+ * the overlaps, and dbsrg_get_matrix returns the window's blocks (the last
+ * window stops at block iicc).  Running every list once per window and
+ * reading each window out assembles the whole matrix; acf is complete after
+ * the last window.  dbsrg_set_window zeroes the window. */
+int dbsrg_alloc_matrix_window(dbsrg_ctx *ctx, int nch, const int *icc,
+                              int iicc, int mk, int nwin);
+int dbsrg_set_window(dbsrg_ctx *ctx, int blo);
+/* Number of blocks dbsrg_get_matrix returns for the current window. */
+int dbsrg_window_blocks(const dbsrg_ctx *ctx);
+
 int dbsrg_set_precision(dbsrg_ctx *ctx, int precision);
 
 /* Drop-in for Gen_matrix(itype,kpol) (gen_matrix.f90:2-17): processes one
@@ -128,6 +144,21 @@ typedef struct dbsrg_list {
 int dbsrg_gen_batch(int nctx, dbsrg_ctx *const *ctxs, const int *nlists,
                     const dbsrg_list *lists);
 
+/* The batch with streamed output, for symmetry blocks whose matrices do not
+ * fit in device memory together (or alone): every context holds a window
+ * (dbsrg_alloc_matrix_window) and runs its lists once per window, windows
+ * in block order; after each window fn(user, i, blo, nblocks, window) gets
+ * context i's blocks blo .. blo+nblocks-1 on the device (window: the first
+ * of them, ms x ms each, in the hch layout) and may read them (with
+ * dbsrg_get_matrix or its own copies) before it returns, when the window is
+ * reused.  fn runs on the context's host thread, concurrently for different
+ * contexts.  acf is complete at the end.  Returns as dbsrg_gen_batch. */
+typedef void (*dbsrg_window_fn)(void *user, int ictx, int blo, int nblocks,
+                                const double *window);
+int dbsrg_gen_batch_streamed(int nctx, dbsrg_ctx *const *ctxs,
+                             const int *nlists, const dbsrg_list *lists,
+                             dbsrg_window_fn fn, void *user);
+
 /* UPDATE_HX(ich,jch,d,C) (updates.f90:79-106): add C*d (d is ms x ms,
  * host or device) to the block of channel pair (ich,jch). */
 int dbsrg_update_hx(dbsrg_ctx *ctx, int ich, int jch, const double *d,
@@ -145,11 +176,14 @@ int dbsrg_backward(dbsrg_ctx *ctx, int n, const int *k, const int *i1,
                    const int *i2, const int *i3, const int *i4,
                    const double *coef, double *energy, double *grad);
 
-/* Copies of results (host or device destination). */
+/* Copies of results (host or device destination).  With a window, the
+ * block of dbsrg_get_block must lie in it and dbsrg_get_matrix copies the
+ * window's blocks. */
 int dbsrg_get_block(dbsrg_ctx *ctx, int ich, int jch, double *out);
 int dbsrg_get_matrix(dbsrg_ctx *ctx, double *hch);
 int dbsrg_get_acf(dbsrg_ctx *ctx, double *acf);
-/* Device pointer to hch (valid until the next alloc/destroy). */
+/* Device pointer to hch, the window's first block (valid until the next
+ * alloc/destroy). */
 int dbsrg_matrix_device_ptr(dbsrg_ctx *ctx, double **hch_dev);
 
 /* One assembled B-spline integral table, in the reference layout

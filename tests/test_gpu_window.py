@@ -1,0 +1,118 @@
+"""Streamed output: a matrix held as a window of consecutive blocks
+(dbsrg_alloc_matrix_window / dbsrg_set_window) and assembled window by
+window must equal, bit for bit, the matrix assembled whole (every block sums
+the same terms in the same order whatever the window), for every precision
+form, with the overlaps, UPDATE_HX and acf.  At the full size of the largest
+symmetry block of the batched workload (ns=368, 262 channels: 34 453 blocks,
+149 GB in the reference layout) the property is checked through per-block
+checksums taken on the device for two window sizes."""
+import numpy as np
+import pytest
+
+from dbsr_gb300 import FACTOR_FP64, PLAIN_FP64, SPLIT_BF16, Assembler, synth
+from dbsr_gb300.api import gen_batch_streamed
+from dbsr_gb300._lib import DbsrgError
+
+pytestmark = pytest.mark.gpu
+
+
+def items(w):
+    return [(L.icase, L.itype, L.kpol, L.k1, L.k2, L.k3, L.k4, L.c) for L in w.lists]
+
+
+def make(w, precision, window=None):
+    a = Assembler(w.t, w.ks, w.ksp, w.ksq)
+    a.set_orbitals(w.pq, w.ipbs)
+    a.alloc_matrix(w.nch, w.icc, w.iicc, w.mk, window=window)
+    a.set_precision(precision)
+    return a
+
+
+def full(w, precision):
+    a = make(w, precision)
+    for it in items(w):
+        a.gen_matrix(*it)
+    h, acf = a.get_matrix(), a.get_acf()
+    a.close()
+    return h, acf
+
+
+@pytest.mark.parametrize("precision", [PLAIN_FP64, FACTOR_FP64, SPLIT_BF16])
+@pytest.mark.parametrize("window", [1, 4, 7])
+def test_windows_equal_whole_matrix(precision, window):
+    w = synth.small(ns=60, nch=5, mk=3, n_entries=2000, seed=51)
+    h0, acf0 = full(w, precision)
+    a = make(w, precision, window)
+    parts = []
+    for blo, nb in a.stream(items(w)):
+        assert nb == min(window, w.iicc - blo + 1)
+        parts.append(a.get_matrix())
+    acf = a.get_acf()
+    a.close()
+    assert np.array_equal(np.concatenate(parts, axis=2), h0)
+    assert np.array_equal(acf, acf0)
+
+
+def test_window_block_access_and_update_hx():
+    w = synth.small(ns=50, nch=4, mk=2, n_entries=500, seed=52)
+    a = make(w, SPLIT_BF16, 3)
+    a.set_window(4)  # blocks 4..6
+    ich, jch = np.argwhere(w.icc == 1)[0] + 1  # block 1: outside the window
+    with pytest.raises(DbsrgError, match="ESTATE"):
+        a.get_block(ich, jch)
+    d = np.ones((a.ms, a.ms), order="F")
+    a.update_hx(int(ich), int(jch), d, 2.0)  # another window's block: no-op
+    assert not a.get_matrix().any()
+    ich, jch = np.argwhere(w.icc == 5)[0] + 1
+    a.update_hx(int(ich), int(jch), d, 2.0)
+    blk = a.get_block(int(ich), int(jch))
+    assert np.array_equal(blk, 2.0 * (d if ich >= jch else d.T))
+    a.close()
+
+
+def test_streamed_batch_equals_blocks_one_by_one():
+    ws = [synth.small(ns=50 + 10 * i, nch=3 + i, mk=3, n_entries=800, seed=60 + i)
+          for i in range(3)]
+    ref = [full(w, SPLIT_BF16) for w in ws]
+    asm = [make(w, SPLIT_BF16, window=2 + i) for i, w in enumerate(ws)]
+    got = [[] for _ in ws]
+
+    def consume(i, blo, nb, ptr):
+        got[i].append((blo, asm[i].get_matrix()))
+
+    gen_batch_streamed(asm, [items(w) for w in ws], consume)
+    for i, w in enumerate(ws):
+        blos = [b for b, _ in got[i]]
+        assert blos == list(range(1, w.iicc + 1, 2 + i))
+        assert np.array_equal(np.concatenate([m for _, m in got[i]], axis=2), ref[i][0])
+        assert np.array_equal(asm[i].get_acf(), ref[i][1])
+        asm[i].close()
+
+
+def test_largest_batch_block_full_size_window_independent():
+    torch = pytest.importorskip("torch")
+    w = synth.config3_block(44)
+    assert (w.ns, w.nch) == (368, 262)
+    ms = 2 * w.ns
+
+    def checksums(window):
+        a = make(w, SPLIT_BF16, window)
+        a.set_async(True)
+        buf = torch.empty((window, ms, ms), dtype=torch.float64, device="cuda")
+        sums, asums = [], []
+        for blo, nb in a.stream(items(w)):
+            a.get_matrix(out=buf[:nb])
+            sums.append(buf[:nb].sum(dim=(1, 2)).cpu())
+            asums.append(buf[:nb].abs().sum(dim=(1, 2)).cpu())
+        acf = a.get_acf()
+        a.close()
+        del buf
+        torch.cuda.empty_cache()
+        return torch.cat(sums).numpy(), torch.cat(asums).numpy(), acf
+
+    s1, t1, acf1 = checksums(1500)
+    s2, t2, acf2 = checksums(2311)
+    assert s1.shape == (w.iicc,)
+    assert np.isfinite(t1).all() and (t1 > 0).sum() > 0.04 * w.iicc
+    assert np.array_equal(s1, s2) and np.array_equal(t1, t2)
+    assert np.array_equal(acf1, acf2)
