@@ -60,7 +60,9 @@ def parse():
                    help="config1: one 120-channel matrix; batch: independent J-blocks with "
                         "their own grids through dbsrg_gen_batch")
     p.add_argument("--nblocks", type=int, default=64)
-    p.add_argument("--nch-max", type=int, default=32)
+    p.add_argument("--nch-max", type=int, default=300)
+    p.add_argument("--batch-group", type=int, default=8, help="J-blocks run concurrently")
+    p.add_argument("--window-gb", type=float, default=4.0, help="device window per J-block")
     p.add_argument("--rows-entries", type=float, default=1e4)
     return p.parse_args()
 
@@ -343,14 +345,20 @@ def fp64_compare(args, a, w, step, dl, timed, torch, dev, world):
 
 # ---------------------------------------------------------------------------
 def batch_main(args, rank, world, local):
-    """Independent J-parity blocks, each with its own grid, orbitals and
-    matrix, assembled together through dbsrg_gen_batch (one host thread and
-    one stream per block).  Step: every matrix zeroed, every block's tables
-    released and rebuilt, every list of every block."""
+    """The batched form: independent J-parity blocks, each with its own grid,
+    orbitals and matrix, through dbsrg_gen_batch_streamed in groups of
+    --batch-group blocks run concurrently (one host thread and one stream
+    each).  The full batch (about 1.15 TB in the reference layout) exceeds the
+    device, so every block holds a window of at most --window-gb of its
+    matrix and each assembled window is copied to pinned host memory (the
+    streamed output).  Step: per group, the assemblers built (grid, orbitals,
+    window), every list run window by window with each window read out, the
+    assemblers closed -- tables and pair potentials are built inside the
+    step."""
     import torch
 
     from dbsr_gb300 import FACTOR_FP64, PLAIN_FP64, SPLIT_BF16, Assembler, synth
-    from dbsr_gb300.api import gen_batch
+    from dbsr_gb300.api import gen_batch_streamed
 
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
@@ -363,26 +371,42 @@ def batch_main(args, rank, world, local):
     ws = synth.config3(nblocks=args.nblocks, nch_max=args.nch_max, rows_entries=args.rows_entries,
                        seed=1237 + 1000 * rank)
     prec = {"plain": PLAIN_FP64, "split": SPLIT_BF16, "factor": FACTOR_FP64}[args.precision]
-    asm, lists = [], []
-    for w in ws:
-        a = Assembler(w.t, w.ks, w.ksp, w.ksq, device=local)
-        a.set_orbitals(w.pq, w.ipbs)
-        a.alloc_matrix(w.nch, w.icc, w.iicc, w.mk)
-        a.set_precision(prec)
-        asm.append(a)
+    lists = []
+    for w in ws:  # device-resident lists
         dl = []
         for L in w.lists:
             t = [torch.from_numpy(np.ascontiguousarray(x)).to(dev) for x in (L.k1, L.k2, L.k3, L.k4)]
             dl.append((L.icase, L.itype, L.kpol, *t,
                        torch.from_numpy(np.ascontiguousarray(L.c)).to(dev)))
         lists.append(dl)
+    G = max(1, args.batch_group)
+    wbytes = int(args.window_gb * 1e9)
+    host = [torch.empty(wbytes // 8, dtype=torch.float64).pin_memory() for _ in range(G)]
     torch.cuda.synchronize()
+    stats = {"d2h": 0, "windows": 0}
 
     def step():
-        for a in asm:
-            a.zero_matrix()
-            a.release_tables()
-        gen_batch(asm, lists)
+        for g0 in range(0, len(ws), G):
+            gw, gl = ws[g0:g0 + G], lists[g0:g0 + G]
+            asm = []
+            for w in gw:
+                a = Assembler(w.t, w.ks, w.ksp, w.ksq, device=local)
+                a.set_orbitals(w.pq, w.ipbs)
+                blk = (2 * w.ns) ** 2 * 8
+                a.alloc_matrix(w.nch, w.icc, w.iicc, w.mk,
+                               window=max(1, min(w.iicc, wbytes // blk)))
+                a.set_precision(prec)
+                asm.append(a)
+
+            def consume(i, blo, nb, ptr):
+                ms = 2 * gw[i].ns
+                asm[i].get_matrix(out=host[i][: nb * ms * ms])
+                stats["d2h"] += nb * ms * ms * 8
+                stats["windows"] += 1
+
+            gen_batch_streamed(asm, gl, consume)
+            for a in asm:
+                a.close()
 
     for _ in range(args.warmup):
         step()
@@ -391,11 +415,10 @@ def batch_main(args, rank, world, local):
     if pg is not None:
         pg.barrier()
     torch.cuda.synchronize()
+    stats["d2h"] = stats["windows"] = 0
     t0 = time.perf_counter()
     for _ in range(args.steps):
         step()
-    for a in asm:
-        a.sync()
     torch.cuda.synchronize()
     if pg is not None:
         pg.barrier()
@@ -422,13 +445,14 @@ def batch_main(args, rank, world, local):
                        "entries": int(sum(L.n for w in ws for L in w.lists)),
                        "matrix_gb": sum(w.iicc * (2 * w.ns) ** 2 * 8 for w in ws) / 1e9,
                        "algorithmic_tflop": flops / 1e12,
+                       "group": G, "window_gb": args.window_gb,
+                       "output": "every window copied to pinned host memory inside the step",
                        "timing": "host wall clock around the synchronised steps",
                        "parallelism": f"replicas x{world}"},
-            "s_per_batch": dt, "clocks": clocks,
+            "s_per_batch": dt, "d2h_bytes_per_step": stats["d2h"] // max(1, args.steps),
+            "windows_per_step": stats["windows"] // max(1, args.steps), "clocks": clocks,
         }
         print(json.dumps(out), flush=True)
-    for a in asm:
-        a.close()
     if pg is not None:
         pg.destroy_process_group()
 
