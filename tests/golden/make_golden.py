@@ -11,7 +11,10 @@ next to this script:
   DBSR_MAT log;
 * the Dirac-Fock "Coulomb energy" lines of the DBSR_HF logs, together with
   the B-spline orbitals of the matching ``.bsw`` file (gfortran sequential
-  unformatted records, layout written by hf_read_pqbs.f90:110-121).
+  unformatted records, layout written by hf_read_pqbs.f90:110-121);
+* the "Configuration energies" blocks of the DBSR_HF logs (the average
+  energy of every jj configuration with the final orbitals) with the
+  orbitals of the run, for B and the four Fe runs.
 
 Only numbers are stored; no reference source code is copied.
 """
@@ -90,6 +93,23 @@ def parse_bsw(path: str) -> dict:
             "orbitals": orbs}
 
 
+def config_energies(path: str) -> list:
+    """[(subshell occupations {label: q}, energy in au)] of the log's
+    "Configuration energies" block."""
+    lines = open(path).read().split("Configuration energies:")[1].splitlines()
+    out = []
+    for line in lines[1:]:
+        if " au " not in line:
+            if out:
+                break
+            continue
+        head, tail = line.split(" au ")[0].rsplit(None, 1)
+        occ = {m.group(1).strip(): int(m.group(2))
+               for m in re.finditer(r"(\d+[a-z]-?)\s*\(\s*(\d+)\)", head)}
+        out.append((occ, float(tail)))
+    return out
+
+
 def log_value(path: str, pat: str):
     for line in open(path):
         if pat in line:
@@ -120,6 +140,14 @@ def main():
             "bsw": parse_bsw(os.path.join(ex, f"{name}.bsw")),
         }
         g["hf"].append(rec)
+    g["configs"] = []
+    for log, bsw in (("B.log", "B.bsw"), ("Fe/Fe.log", "Fe/Fe.bsw"), ("Fe/2.log", "Fe/2.bsw"),
+                     ("Fe/3.log", "Fe/3.bsw"), ("Fe/4.log", "Fe/4.bsw")):
+        b = parse_bsw(os.path.join(ex, bsw))
+        keep = {"2p-", "2p", "3d-", "3d"}
+        b["orbitals"] = [o for o in b["orbitals"] if o["label"].strip() in keep]
+        g["configs"].append({"log": log, "bsw": bsw, "energies": config_energies(
+            os.path.join(ex, log)), "orbitals": b})
     mline = log_value(os.path.join(REF, "Rb_bound_example/dbsr_cc27/mat_log.005"),
                       "memory of DBS_integrals")
     g["mat_memory"] = {"line": mline.strip() if mline else None, "ns": 109, "ks": 9, "kmax": 7,

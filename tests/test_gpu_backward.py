@@ -78,3 +78,25 @@ def test_autograd_function():
     a.close()
     assert abs(E.item() - Er) == 0.0
     assert np.array_equal(pq.grad.numpy(), np.ascontiguousarray(Gr))
+
+
+def test_rk_on_reference_orbitals_pinned_by_configuration_energies(golden):
+    """The GPU energy functional on the reference's own DHF orbitals (B 2p-/2p
+    and four Fe runs, 3d-/3d) against the second differences of the
+    configuration energies DBSR_HF prints (the pin of config_energy.py)."""
+    import config_energy as CE
+
+    n = 0
+    for rec in golden["configs"]:
+        lm, lp = CE.CASES[rec["log"]]
+        t, pq, labels = CE.bsw_orbitals(rec["orbitals"])
+        b = rec["orbitals"]
+        a = Assembler(t, b["ks"], b["ksp"], b["ksq"])
+        a.set_orbitals(pq, np.zeros(pq.shape[2], dtype=np.int32))
+        ent = CE.second_coefficient_entries(labels.index(lm) + 1, labels.index(lp) + 1, lm, lp)
+        val, _ = a.backward(*ent, grad=False)
+        a.close()
+        for key, r in CE.reference_second_coefficients(rec["energies"], lm, lp):
+            assert abs(val - r) <= 2e-11, (rec["log"], key, val, r)
+            n += 1
+    assert n == 13

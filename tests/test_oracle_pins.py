@@ -171,3 +171,37 @@ def test_oracle_config0_runs_and_is_symmetric():
     for ich in range(1, w.nch + 1):
         b = m.hch[:, :, w.icc[ich - 1, ich - 1] - 1]
         assert np.allclose(b, b.T, rtol=0, atol=1e-15 * np.abs(b).max())
+
+
+def test_threej_against_sympy():
+    sympy = pytest.importorskip("sympy")
+    from sympy.physics.wigner import wigner_3j
+
+    import config_energy as CE
+
+    for j1, k, j2 in ((3, 2, 3), (5, 2, 5), (5, 4, 5), (3, 2, 5), (3, 4, 5), (1, 2, 3)):
+        ref = wigner_3j(sympy.Rational(j1, 2), k, sympy.Rational(j2, 2), sympy.Rational(1, 2), 0,
+                        sympy.Rational(-1, 2)) ** 2
+        assert CE.threej_sq(j1, 2 * k, j2, 1, 0, -1) == sympy.Rational(ref)
+
+
+def test_rk_pinned_by_configuration_energies(golden):
+    """R^k of the reference's own DHF orbitals (B 2p-/2p; Fe 3d-/3d, four
+    runs) against the second differences of the configuration energies the
+    DBSR_HF logs print (27 energies, 13 second differences)."""
+    import config_energy as CE
+
+    n = 0
+    for rec in golden["configs"]:
+        lm, lp = CE.CASES[rec["log"]]
+        t, pq, labels = CE.bsw_orbitals(rec["orbitals"])
+        b = rec["orbitals"]
+        g = O.Grid(t, b["ks"], b["ksp"], b["ksq"])
+        ent = CE.second_coefficient_entries(labels.index(lm) + 1, labels.index(lp) + 1, lm, lp)
+        a, _ = g.rk_energy_grad(*ent, pq, grad=False)
+        refs = CE.reference_second_coefficients(rec["energies"], lm, lp)
+        assert refs, rec["log"]
+        for key, r in refs:
+            assert abs(a - r) <= 2e-11, (rec["log"], key, a, r)
+            n += 1
+    assert n == 13
