@@ -504,9 +504,11 @@ def main():
     # time covers all of its kernels
     a.set_async(True)
 
+    # every step rebuilds the tables, cell data, far fields and pair
+    # potentials (invalidated, rebuilt in the memory they occupied)
     def step(lists):
         a.zero_matrix()
-        a.release_tables()
+        a.invalidate_tables()
         for (ic, it, kp, k1, k2, k3, k4, c) in lists:
             a.gen_matrix(ic, it, kp, k1, k2, k3, k4, c)
         a.sync()
@@ -589,13 +591,6 @@ def main():
                                   "unit": "TFLOP/s", "frac": fl_top / sec / 1e12 / tpk,
                                   "peak_source": f"{peak_kind} bf16_tflops_sustained"}
 
-    # FP64 comparison: the same matrix by the factored FP64 and the plain FP64
-    # assemblies (the plain one is held to the CPU oracle at 1e-12 by the
-    # parity tests), per-block errors of the headline form against plain FP64
-    compare = None
-    if args.precision != "plain" and not args.no_compare:
-        compare = fp64_compare(args, a, w, step, dl, timed, torch, dev, world)
-
     # e2e: lists from pinned host memory, matrix back to pinned host memory
     e2e = None
     if not args.no_e2e:
@@ -608,18 +603,32 @@ def main():
             h2d += sum(x.numel() * 4 for x in t[:3]) + c.numel() * 8
             hl.append((L.icase, L.itype, L.kpol, *[x.numpy() for x in t], c.numpy()))
         hout = torch.empty(w.iicc * a.ms * a.ms, dtype=torch.float64).pin_memory()
-        hout_np = hout.numpy()
+        hacf = torch.empty(w.iicc * (w.mk + 1), dtype=torch.float64).pin_memory()
+        nwin = (w.iicc + 7) // 8
 
         def e2e_step():
-            step(hl)
-            a.get_matrix(out=hout_np)
+            # dbsrg_assemble_to_host: lists from pinned host memory, the matrix
+            # window by window into pinned host memory, each window's copy
+            # overlapped with the next window's assembly
+            a.invalidate_tables()
+            a.assemble_to_host(hl, out=hout, acf=hacf, nwin=nwin)
 
         e2e_step()
-        dte = timed(e2e_step, 1)
+        dte = timed(e2e_step, 2)
+        npass = (w.iicc + nwin - 1) // nwin
         e2e = {"value": world * fl["total"] / dte / 1e9, "unit": "GFLOP/s",
-               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(hout.numel() * 8),
-               "s_per_matrix": dte}
+               "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int((hout.numel() + hacf.numel()) * 8),
+               "s_per_matrix": dte, "api": "dbsrg_assemble_to_host",
+               "windows": npass}
         del hout
+
+    # FP64 comparison: the same matrix by the factored FP64 and the plain FP64
+    # assemblies (the plain one is held to the CPU oracle at 1e-12 by the
+    # parity tests), per-block errors of the headline form against plain FP64
+    compare = None
+    if args.precision != "plain" and not args.no_compare:
+        compare = fp64_compare(args, a, w, step, dl, timed, torch, dev, world)
 
     cpu = None
     if rank == 0 and not args.no_cpu:

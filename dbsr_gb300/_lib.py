@@ -57,10 +57,12 @@ SIGNATURES = [
     ("dbsrg_set_window", C.c_int, [_vp, C.c_int]),
     ("dbsrg_window_blocks", C.c_int, [_vp]),
     ("dbsrg_release_tables", C.c_int, [_vp]),
+    ("dbsrg_invalidate_tables", C.c_int, [_vp]),
     ("dbsrg_timing", C.c_int, [_vp, C.c_int]),
     ("dbsrg_timing_report", C.c_int, [_vp, C.c_char_p, C.c_size_t]),
     ("dbsrg_gen_batch", C.c_int, [C.c_int, _vp, _vp, _vp]),
     ("dbsrg_gen_batch_streamed", C.c_int, [C.c_int, _vp, _vp, _vp, _vp, _vp]),
+    ("dbsrg_assemble_to_host", C.c_int, [_vp, C.c_int, _vp, C.c_int, _vp, _vp]),
     ("dbsrg_backward", C.c_int, [_vp, C.c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     ("dbsrg_exchange_segment_noalloc", C.c_int,
      [C.c_int, C.c_int, _vp, _vp, C.c_int, C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, _vp, _vp]),

@@ -109,6 +109,22 @@ class Assembler:
         self.wcap = iicc if window is None else int(window)
         self.icc = icc
 
+    def assemble_to_host(self, lists, out=None, acf=None, nwin: int = 0):
+        """dbsrg_assemble_to_host: every list (icase, itype, kpol, k1, k2, k3, k4,
+        cdata[, ipt]) into `out` (ms, ms, iicc), window by window, with the copy
+        of each window overlapped with the next one's assembly.  `out` may be
+        host (pinned for the overlap) or device memory; returns (out, acf)."""
+        if out is None:
+            out = np.zeros((self.ms, self.ms, self.iicc), order="F")
+        if acf is None:
+            acf = np.zeros((self.iicc, self.mk + 1), order="F")
+        arr, keep, counts = _list_descs([lists])
+        po, k1 = _ptr(out, np.float64)
+        pa, k2 = _ptr(acf, np.float64)
+        rc = self._L.dbsrg_assemble_to_host(self._h, counts[0], arr, int(nwin), po, pa)
+        check(self._h, rc, "assemble_to_host")
+        return out, acf
+
     def set_window(self, blo: int):
         """Hold (and zero) blocks blo .. blo + window - 1."""
         check(self._h, self._L.dbsrg_set_window(self._h, int(blo)), "set_window")
@@ -228,7 +244,12 @@ class Assembler:
         return out
 
     def release_tables(self):
+        """Free the cached tables and everything derived from them."""
         check(self._h, self._L.dbsrg_release_tables(self._h), "release_tables")
+
+    def invalidate_tables(self):
+        """Mark the cached tables stale; they are rebuilt in their memory."""
+        check(self._h, self._L.dbsrg_invalidate_tables(self._h), "invalidate_tables")
 
     def timing(self, enable: bool = True):
         check(self._h, self._L.dbsrg_timing(self._h, int(enable)), "timing")

@@ -23,6 +23,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <functional>
 
 namespace {
 
@@ -552,53 +553,96 @@ int update_hx(dbsrg_ctx *c, int ich, int jch, const double *d, double cc) {
   return DBSRG_OK;
 }
 
-int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const int *ipt,
-                     const int *k1, const int *k2, const int *k3, const int *k4,
-                     const double *cdata) {
-  (void)k4;
-  if (n <= 0) return DBSRG_OK;
-  if (!c->hch) return set_err(c, DBSRG_ESTATE, "no matrix allocated");
-  if (!c->pq) return set_err(c, DBSRG_ESTATE, "no orbitals set");
+namespace {
+
+// One coefficient list, set up once and executed per block window.
+//  * set-up (plan_list): the list copied in IPT order, its segments and
+//    their blocks read back, the case's structure (PQ types, storage,
+//    convol case), and the work of every window of a partition of the
+//    blocks (windows [blo0 + w*nwin, blo0 + (w+1)*nwin), w < nw): chunks of
+//    owner segments with their partners, quadrant records of the split
+//    exchange, owners for acf, touched blocks of an overlap list.  All work
+//    lists go to the device in one copy.
+//  * execution (exec_list): the window's chunks, acf terms or overlap
+//    updates on the contraction stream, with the tables (cached) fetched
+//    there.
+struct Chunk {
+  int moff, nm, nown, xoff, nxq;
+};
+struct ListPlan {
+  int icase = 0, itype = 0, kpol = 0, n = 0, nseg = 0;
+  bool factored = false, split_x = false;
+  int na = 0, icv = 0, tabfam = 0, ncol = 0, kb = 0;
+  char sym_d = 's';
+  size_t per = 0;
+  DensSpec dsp{};
+  ScatterSpec ssp{};
+  int ttype[4] = {0, 1, 2, 3};
+  int *lk1 = nullptr, *lk2 = nullptr, *lk3 = nullptr, *lpair = nullptr;
+  double *lcd = nullptr;
+  SegInfo *info = nullptr;
+  int *work = nullptr;   // chunk members and owner slots | acf owners
+  XQuad *dxq = nullptr;  // quadrant records
+  double *vch = nullptr;
+  int *bstart = nullptr, *tlist = nullptr, *order = nullptr;  // overlap list
+  std::vector<Chunk> chunks;
+  std::vector<int> wchunk, wown, wtl;  // per window: [w], [w+1] ranges
+  int own_off = 0;                     // acf owners inside `work`
+  std::vector<XQuad> hxq;
+};
+
+size_t al256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+// device bytes of one list's state
+size_t plan_bytes(const dbsrg_ctx *c, int icase, int n) {
+  const size_t ib = sizeof(int) * (size_t)n, db = sizeof(double) * (size_t)n;
+  size_t t = 8 * al256(ib) + 2 * al256(db) + al256(sizeof(int) * (n + 2)) + al256(64) +
+             al256(sizeof(SegInfo) * (size_t)(n + 1)) + al256(sizeof(int) * (size_t)(7 * (n + 1))) +
+             al256(sizeof(XQuad) * 4 * (size_t)(n + 1));
+  if (icase == 0)
+    t += al256(sizeof(double) * (size_t)c->g.ms * c->nbf) +
+         al256(sizeof(int) * (2 * (size_t)(c->iicc + 2) + n));
+  return t;
+}
+
+int plan_list(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const int *ipt,
+              const int *k1, const int *k2, const int *k3, const double *cdata, int blo0,
+              int nwin, int nw, void *dev, cudaStream_t ss, ListPlan &P) {
   const DeviceGrid &g = c->g;
   const int ns = g.ns, ks = g.ks, ms = g.ms;
-  cudaStream_t st = c->stream;
   int rc;
-
-  // ---- 1. list in IPT order on the device.  The list state lives in one
-  // of two buffers; with the pipeline on (asynchronous mode, R and S lists)
-  // its set-up runs on the set-up stream once the kernels of the call two
-  // back are done with the buffer, while the previous call's kernels run.
-  const bool pipe = c->async && icase != 0;
-  const int par = c->lpar;
-  c->lpar ^= 1;
-  cudaStream_t ss = pipe ? c->sstream : st;
+  P.icase = icase;
+  P.itype = itype;
+  P.kpol = kpol;
+  P.n = n;
+  // window of block b in the partition, -1 outside it
+  auto wof = [&](int b) -> int {
+    if (b < blo0) return -1;
+    const int w = (b - blo0) / nwin;
+    return w < nw ? w : -1;
+  };
   const size_t ibytes = sizeof(int) * (size_t)n, dbytes = sizeof(double) * (size_t)n;
-  auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
-  size_t tot = 8 * al(ibytes) + 2 * al(dbytes) + al(sizeof(int) * (n + 2)) + al(64) +
-               al(sizeof(SegInfo) * (size_t)(n + 1)) + al(sizeof(int) * (size_t)(n + 1)) +
-               al(sizeof(int) * (size_t)(6 * (n + 1))) + al(sizeof(XQuad) * 4 * (size_t)(n + 1));
-  if ((rc = ensure_lstate(c, par, tot))) return rc;
-  if (pipe) DBSRG_TRY(c, cudaStreamWaitEvent(ss, c->lfree[par], 0));
-  char *base = (char *)c->lstate[par];
+  char *base = (char *)dev;
   auto take = [&](size_t bytes) {
     char *p = base;
-    base += al(bytes);
+    base += al256(bytes);
     return (void *)p;
   };
   int *dk1 = (int *)take(ibytes), *dk2 = (int *)take(ibytes), *dk3 = (int *)take(ibytes);
   double *dcd = (double *)take(dbytes);
   int *dipt = (int *)take(ibytes);
-  int *lk1 = (int *)take(ibytes), *lk2 = (int *)take(ibytes), *lk3 = (int *)take(ibytes);
-  double *lcd = (double *)take(dbytes);
-  int *lpair = (int *)take(ibytes);  // factored path: bound-orbital pair of each entry
+  P.lk1 = (int *)take(ibytes);
+  P.lk2 = (int *)take(ibytes);
+  P.lk3 = (int *)take(ibytes);
+  P.lcd = (double *)take(dbytes);
+  P.lpair = (int *)take(ibytes);  // factored path: bound-orbital pair of each entry
   int *seg_start = (int *)take(sizeof(int) * (size_t)(n + 2));
-  int *dscal = (int *)take(64);  // [0]=nseg [1]=err [2]=blocks touched [3]=pair err
-  SegInfo *info = (SegInfo *)take(sizeof(SegInfo) * (size_t)(n + 1));
-  int *owners = (int *)take(sizeof(int) * (size_t)(n + 1));
-  // per chunk: member segment ids, owner slots and (split exchange) the
-  // (owner slot, quadrant) codes -- at most 6 ints per segment
-  int *members = (int *)take(sizeof(int) * (size_t)(6 * (n + 1)));
-  XQuad *dxq_all = (XQuad *)take(sizeof(XQuad) * 4 * (size_t)(n + 1));
+  int *dscal = (int *)take(64);  // [0]=nseg [1]=err [2]=- [3]=pair err
+  P.info = (SegInfo *)take(sizeof(SegInfo) * (size_t)(n + 1));
+  // per chunk member segment ids and owner slots (at most 6 ints per
+  // segment), then the acf owners (one per segment)
+  P.work = (int *)take(sizeof(int) * (size_t)(7 * (n + 1)));
+  P.dxq = (XQuad *)take(sizeof(XQuad) * 4 * (size_t)(n + 1));
   if ((rc = copy_in_s(c, dk1, k1, ibytes, ss))) return rc;
   if ((rc = copy_in_s(c, dk2, k2, ibytes, ss))) return rc;
   if ((rc = copy_in_s(c, dk3, k3, ibytes, ss))) return rc;
@@ -607,28 +651,24 @@ int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const 
   DBSRG_TRY(c, cudaMemsetAsync(dscal, 0, 64, ss));
   DBSRG_RUN_S(c, ss, "k_gather",
               k_gather<<<(n + 255) / 256, 256, 0, ss>>>(n, ipt ? dipt : nullptr, dk1, dk2, dk3,
-                                                        dcd, lk1, lk2, lk3, lcd));
+                                                        dcd, P.lk1, P.lk2, P.lk3, P.lcd));
 
-  // ---- overlaps
+  // ---- overlaps: entries grouped by block on the host (counting sort, list
+  // order kept within a block); entries below eps_c are dropped
+  // (mod_dbsr_mat.f90:56)
   if (icase == 0) {
     if (itype != 3) return set_err(c, DBSRG_EINVAL, "O_data: only itype 3 is supported");
     const int iicc = c->iicc;
-    size_t vbytes = sizeof(double) * (size_t)ms * c->nbf;
-    rc = ensure_scratch(c, vbytes + sizeof(int) * ((size_t)n + 2 * (iicc + 2)) + 1024);
-    if (rc) return rc;
-    double *vch = (double *)c->scratch;
-    int *bstart = (int *)(vch + (size_t)ms * c->nbf);
-    int *tlist = bstart + (iicc + 2);  // blocks with entries
-    int *order = tlist + (iicc + 2);
-    DBSRG_RUN(c, "k_vch", k_vch<<<(2 * ns * c->nbf + 255) / 256, 256, 0, st>>>(ns, c->nbf, g.fpbs, g.fqbs, c->pq, vch));
-    // entries grouped by block on the host (counting sort, list order kept
-    // within a block); entries below eps_c are dropped (mod_dbsr_mat.f90:56)
+    P.vch = (double *)take(sizeof(double) * (size_t)ms * c->nbf);
+    P.bstart = (int *)take(sizeof(int) * (2 * (size_t)(iicc + 2) + n));
+    P.tlist = P.bstart + (iicc + 2);  // blocks with entries, ascending
+    P.order = P.tlist + (iicc + 2);
     std::vector<int> hk1(n), hk2(n);
     std::vector<double> hcd(n);
-    DBSRG_TRY(c, cudaMemcpyAsync(hk1.data(), lk1, ibytes, cudaMemcpyDeviceToHost, st));
-    DBSRG_TRY(c, cudaMemcpyAsync(hk2.data(), lk2, ibytes, cudaMemcpyDeviceToHost, st));
-    DBSRG_TRY(c, cudaMemcpyAsync(hcd.data(), lcd, dbytes, cudaMemcpyDeviceToHost, st));
-    DBSRG_TRY(c, cudaStreamSynchronize(st));
+    DBSRG_TRY(c, cudaMemcpyAsync(hk1.data(), P.lk1, ibytes, cudaMemcpyDeviceToHost, ss));
+    DBSRG_TRY(c, cudaMemcpyAsync(hk2.data(), P.lk2, ibytes, cudaMemcpyDeviceToHost, ss));
+    DBSRG_TRY(c, cudaMemcpyAsync(hcd.data(), P.lcd, dbytes, cudaMemcpyDeviceToHost, ss));
+    DBSRG_TRY(c, cudaStreamSynchronize(ss));
     std::vector<int> eblk(n, 0), hstart(iicc + 2, 0), hlist, horder(n);
     for (int e = 0; e < n; e++) {
       if (std::fabs(hcd[e]) < 1.0e-10) continue;
@@ -641,66 +681,59 @@ int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const 
         return set_err(c, DBSRG_ERANGE, "channel or orbital index out of range in list");
       const int b = c->h_icc[(ich - 1) + (size_t)c->nch * (jch - 1)];
       if (b < 1 || b > iicc) return set_err(c, DBSRG_ERANGE, "channel pair has no block in icc");
-      if (!in_window(c, b)) continue;
+      if (wof(b) < 0) continue;
       eblk[e] = b;
       hstart[b + 1]++;
     }
+    P.wtl.assign(nw + 1, 0);
     for (int b = 1; b <= iicc; b++) {
-      if (hstart[b + 1] > 0) hlist.push_back(b);
+      if (hstart[b + 1] > 0) {
+        hlist.push_back(b);
+        P.wtl[wof(b) + 1]++;
+      }
       hstart[b + 1] += hstart[b];
     }
+    for (int w = 0; w < nw; w++) P.wtl[w + 1] += P.wtl[w];
     {
       std::vector<int> fill(hstart.begin(), hstart.end());
       for (int e = 0; e < n; e++)
         if (eblk[e]) horder[fill[eblk[e]]++] = e;
     }
-    const int ntouched = (int)hlist.size();
-    if (ntouched > 0) {
-      if ((rc = copy_in(c, bstart, hstart.data(), sizeof(int) * (iicc + 2)))) return rc;
-      if ((rc = copy_in(c, tlist, hlist.data(), sizeof(int) * ntouched))) return rc;
-      if ((rc = copy_in(c, order, horder.data(), sizeof(int) * hstart[iicc + 1]))) return rc;
-      for (int t0 = 0; t0 < ntouched; t0 += 65535) {  // grid z limit
-        dim3 grid((unsigned)((ms + 127) / 128), (unsigned)((ms + 31) / 32),
-                  (unsigned)std::min(65535, ntouched - t0));
-        DBSRG_RUN(c, "k_overlap_update",
-                  k_overlap_update<<<grid, 128, 0, st>>>(ns, tlist + t0, bstart, order, lk1, lk2,
-                                                         lcd, c->ipbs, vch, hch_base(c)));
-      }
+    if (!hlist.empty()) {
+      if ((rc = copy_in_s(c, P.bstart, hstart.data(), sizeof(int) * (iicc + 2), ss))) return rc;
+      if ((rc = copy_in_s(c, P.tlist, hlist.data(), sizeof(int) * hlist.size(), ss))) return rc;
+      if ((rc = copy_in_s(c, P.order, horder.data(), sizeof(int) * hstart[iicc + 1], ss)))
+        return rc;
     }
-    DBSRG_TRY(c, cudaStreamSynchronize(st));
     return DBSRG_OK;
   }
 
-  // ---- 2. segments (orbital check and segment count read back together)
+  // ---- segments (orbital check and segment count read back together)
   DBSRG_RUN_S(c, ss, "k_check_orbitals",
-              k_check_orbitals<<<(n + 255) / 256, 256, 0, ss>>>(n, lk2, lk3, c->nbf, dscal + 1));
-  DBSRG_RUN_S(c, ss, "k_segments", k_segments<<<1, 1024, 0, ss>>>(n, lk1, seg_start, dscal));
+              k_check_orbitals<<<(n + 255) / 256, 256, 0, ss>>>(n, P.lk2, P.lk3, c->nbf,
+                                                                dscal + 1));
+  DBSRG_RUN_S(c, ss, "k_segments", k_segments<<<1, 1024, 0, ss>>>(n, P.lk1, seg_start, dscal));
   int hs[4] = {0, 0, 0, 0};  // nseg, error, -, bound-pair error
   DBSRG_TRY(c, cudaMemcpyAsync(hs, dscal, 2 * sizeof(int), cudaMemcpyDeviceToHost, ss));
   DBSRG_TRY(c, cudaStreamSynchronize(ss));
   if (hs[1]) return set_err(c, DBSRG_ERANGE, "channel or orbital index out of range in list");
   const int nseg = hs[0];
   if (nseg < 1 || nseg > n) return set_err(c, DBSRG_ECUDA, "inconsistent segment count");
+  P.nseg = nseg;
   DBSRG_RUN_S(c, ss, "k_seg_info",
-              k_seg_info<<<(nseg + 127) / 128, 128, 0, ss>>>(nseg, seg_start, lk1, c->nch,
-                                                             c->iicc, c->icc, info, dscal + 1));
+              k_seg_info<<<(nseg + 127) / 128, 128, 0, ss>>>(nseg, seg_start, P.lk1, c->nch,
+                                                             c->iicc, c->icc, P.info, dscal + 1));
 
-  // ---- 3. contraction set-up per case
-  DensSpec dsp{};
-  ScatterSpec ssp{};
-  int na, icv, tabfam;
-  char sym_d;
-  const double *tabs[4] = {nullptr, nullptr, nullptr, nullptr};
-  int ttype[4] = {0, 1, 2, 3};  // table type of each atype (R: the atype itself)
-  const bool factored = c->precision != DBSRG_PLAIN_FP64;
+  // ---- the case: PQ types, storage and convol case
+  P.factored = c->precision != DBSRG_PLAIN_FP64;
   if (icase == 2) {
     if (itype != 3 && itype != 4)
       return set_err(c, DBSRG_EINVAL, "R_data: only itypes 3 and 4 are supported");
     if (kpol < 0 || kpol > c->mk) return set_err(c, DBSRG_ERANGE, "R_data: kpol out of range");
-    na = 4;
-    tabfam = 0;
-    icv = itype == 3 ? 1 : 3;
-    sym_d = itype == 3 ? 's' : 'x';
+    P.na = 4;
+    P.tabfam = 0;
+    P.icv = itype == 3 ? 1 : 3;
+    P.sym_d = itype == 3 ? 's' : 'x';
     for (int a = 0; a < 4; a++) {
       int ip1, ip2, jp1, jp2;
       switch (a) {  // R_data.f90:73-86
@@ -713,15 +746,8 @@ int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const 
           if (itype == 4) { ip1 = 2; ip2 = 1; jp1 = 2; jp2 = 1; }
           break;
       }
-      dsp.jp1[a] = jp1; dsp.jp2[a] = jp2;
-      ssp.ii[a] = ip1; ssp.jj[a] = ip2;
-      // the factored path reads only the band |j-i| <= 16 of exchange tables
-      // and no table at all for the direct contraction
-      if (!factored)
-        rc = get_rtable(c, a, kpol, &tabs[a]);
-      else if (itype == 4)
-        rc = get_band_table(c, 0, a, kpol, &tabs[a]);
-      if (rc) return rc;
+      P.dsp.jp1[a] = jp1; P.dsp.jp2[a] = jp2;
+      P.ssp.ii[a] = ip1; P.ssp.jj[a] = ip2;
     }
   } else if (icase == 3) {
     int atype = itype / 10, it = itype % 10;
@@ -744,39 +770,33 @@ int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const 
         default: ip1 = 2; ip2 = 2; jp1 = 1; jp2 = 1; in = 4; break;
       }
     }
-    na = 1;
-    tabfam = 1;
-    icv = in;
-    sym_d = in <= 2 ? 'n' : 'x';
-    dsp.jp1[0] = jp1; dsp.jp2[0] = jp2;
-    ssp.ii[0] = ip1; ssp.jj[0] = ip2;
-    if (!factored)
-      rc = get_stable(c, atype, kpol, &tabs[0]);
-    else if (in >= 3)
-      rc = get_band_table(c, 1, atype, kpol, &tabs[0]);
-    if (rc) return rc;
-    ttype[0] = atype;
+    P.na = 1;
+    P.tabfam = 1;
+    P.icv = in;
+    P.sym_d = in <= 2 ? 'n' : 'x';
+    P.dsp.jp1[0] = jp1; P.dsp.jp2[0] = jp2;
+    P.ssp.ii[0] = ip1; P.ssp.jj[0] = ip2;
+    P.ttype[0] = atype;
   } else {
     return set_err(c, DBSRG_EINVAL, "unsupported icase");
   }
-  ssp.na = na;
-  ssp.sym = sym_d;
-  const int ncol = sym_d == 's' ? ks : (sym_d == 'n' ? 2 * ks - 1 : ns);
-  ssp.ncol = ncol;
-  const int kb = tabfam == 0 ? ks : 2 * ks - 1;
+  P.ssp.na = P.na;
+  P.ssp.sym = P.sym_d;
+  P.ncol = P.sym_d == 's' ? ks : (P.sym_d == 'n' ? 2 * ks - 1 : ns);
+  P.ssp.ncol = P.ncol;
+  P.kb = P.tabfam == 0 ? ks : 2 * ks - 1;
+  P.per = (size_t)ns * P.ncol;
+  P.split_x = P.factored && P.icv >= 3 && c->precision == DBSRG_SPLIT_BF16;
 
-  // ---- chunks of owner segments, each with its partner (a channel pair
-  // listed in both orders maps to one block; both lists contribute to that
-  // block in list order within every atype, so they stay in one chunk)
-  if (factored) {
+  if (P.factored) {
     // the factored contraction works with ordered pairs of bound orbitals
     if (c->nbound < 1) return set_err(c, DBSRG_ESTATE, "no bound orbitals (ipbs = 0)");
-    if ((rc = pair_index(c, n, lk2, lk3, lpair, dscal + 3, ss))) return rc;
+    if ((rc = pair_index(c, n, P.lk2, P.lk3, P.lpair, dscal + 3, ss))) return rc;
   }
   // segment table, segment errors and bound-pair errors in one read-back
   std::vector<SegInfo> hinfo(nseg);
   DBSRG_TRY(c, cudaMemcpyAsync(hs, dscal, 4 * sizeof(int), cudaMemcpyDeviceToHost, ss));
-  DBSRG_TRY(c, cudaMemcpyAsync(hinfo.data(), info, sizeof(SegInfo) * nseg,
+  DBSRG_TRY(c, cudaMemcpyAsync(hinfo.data(), P.info, sizeof(SegInfo) * nseg,
                                cudaMemcpyDeviceToHost, ss));
   DBSRG_TRY(c, cudaStreamSynchronize(ss));
   if (hs[1] == 1) return set_err(c, DBSRG_ERANGE, "channel or orbital index out of range in list");
@@ -788,102 +808,148 @@ int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const 
         si.partner < -1 || si.partner >= nseg)
       return set_err(c, DBSRG_ECUDA, "inconsistent segment table");
   }
-  const size_t per = (size_t)ns * ncol;
-  // chunks of owner segments, each with its partner; the member ids and owner
-  // slots of all chunks go to the device in one copy
-  const int chunk = (factored && icv <= 2) ? 16 * kSegChunk : kSegChunk;
-  const bool split_x = factored && icv >= 3 && c->precision == DBSRG_SPLIT_BF16;
-  struct Chunk {
-    int moff, nm, nown, xoff, nxq;
-  };
-  std::vector<Chunk> chunks;
+
+  // ---- chunks of owner segments per window, each owner with its partner (a
+  // channel pair listed in both orders maps to one block; both lists
+  // contribute to that block in list order within every atype, so they stay
+  // in one chunk); owners in list order within a window
+  std::vector<std::vector<int>> wseg(nw);
+  for (int s = 0; s < nseg; s++) {
+    if (!hinfo[s].owner) continue;
+    const int w = wof(hinfo[s].blk);
+    if (w >= 0) wseg[w].push_back(s);
+  }
+  const int chunk = (P.factored && P.icv <= 2) ? 16 * kSegChunk : kSegChunk;
   std::vector<int> hbuf;
-  std::vector<XQuad> hxq;  // split exchange: quadrant records of all chunks
   bool xq_ok = true;
-  {
+  P.wchunk.assign(nw + 1, 0);
+  for (int w = 0; w < nw; w++) {
     std::vector<int> mem, own;  // member segment ids; owner slot positions
     auto close = [&]() {
       if (mem.empty()) return;
-      Chunk ch{(int)hbuf.size(), (int)mem.size(), (int)own.size(), (int)hxq.size(), 0};
+      Chunk ch{(int)hbuf.size(), (int)mem.size(), (int)own.size(), (int)P.hxq.size(), 0};
       hbuf.insert(hbuf.end(), mem.begin(), mem.end());
       hbuf.insert(hbuf.end(), own.begin(), own.end());
-      if (split_x) {
-        xq_ok = xq_ok && build_xquads(na, ssp.ii, ssp.jj, mem, own, hinfo, hxq);
-        ch.nxq = (int)hxq.size() - ch.xoff;
+      if (P.split_x) {
+        xq_ok = xq_ok && build_xquads(P.na, P.ssp.ii, P.ssp.jj, mem, own, hinfo, P.hxq);
+        ch.nxq = (int)P.hxq.size() - ch.xoff;
       }
-      chunks.push_back(ch);
+      P.chunks.push_back(ch);
       mem.clear();
       own.clear();
     };
-    for (int s = 0; s < nseg; s++) {
-      if (!hinfo[s].owner || !in_window(c, hinfo[s].blk)) continue;
+    for (int s : wseg[w]) {
       own.push_back((int)mem.size());
       mem.push_back(s);
       if (hinfo[s].partner >= 0) mem.push_back(hinfo[s].partner);
       if ((int)mem.size() >= chunk - 1) close();
     }
     close();
+    P.wchunk[w + 1] = (int)P.chunks.size();
   }
   if (!xq_ok) return set_err(c, DBSRG_ECUDA, "split exchange: a quadrant with more than 4 terms");
-  if (hxq.size() > 4 * (size_t)(n + 1))
-    return set_err(c, DBSRG_ECUDA, "split exchange: quadrant records overflow");
-  // owner segments in list order (asymptotic coefficients of direct R^k)
-  std::vector<int> hown;
+  if (P.hxq.size() > 4 * (size_t)(n + 1) || hbuf.size() > 6 * (size_t)(n + 1))
+    return set_err(c, DBSRG_ECUDA, "work records overflow");
+  // owners of direct R^k (acf), in list order within a window
+  P.wown.assign(nw + 1, 0);
+  P.own_off = (int)hbuf.size();
   if (icase == 2 && itype == 3)
-    for (int s = 0; s < nseg; s++)
-      if (hinfo[s].owner && in_window(c, hinfo[s].blk)) hown.push_back(s);
-  // the host-built work lists go to the list state on the set-up stream;
-  // the contraction waits for the set-up
-  if (!hbuf.empty() && (rc = copy_in_s(c, members, hbuf.data(), sizeof(int) * hbuf.size(), ss)))
+    for (int w = 0; w < nw; w++) {
+      hbuf.insert(hbuf.end(), wseg[w].begin(), wseg[w].end());
+      P.wown[w + 1] = P.wown[w] + (int)wseg[w].size();
+    }
+  if (!hbuf.empty() && (rc = copy_in_s(c, P.work, hbuf.data(), sizeof(int) * hbuf.size(), ss)))
     return rc;
-  XQuad *dxq = nullptr;
-  if (!hxq.empty()) {
-    dxq = dxq_all;
-    if ((rc = copy_in_s(c, dxq, hxq.data(), sizeof(XQuad) * hxq.size(), ss))) return rc;
-  }
-  if (!hown.empty() && (rc = copy_in_s(c, owners, hown.data(), sizeof(int) * hown.size(), ss)))
+  if (!P.hxq.empty() &&
+      (rc = copy_in_s(c, P.dxq, P.hxq.data(), sizeof(XQuad) * P.hxq.size(), ss)))
     return rc;
-  if (pipe) {
-    DBSRG_TRY(c, cudaEventRecord(c->lready, ss));
-    DBSRG_TRY(c, cudaStreamWaitEvent(st, c->lready, 0));
+  return DBSRG_OK;
+}
+
+// window w of a planned list on the contraction stream; hch_base(c) must
+// address that window's blocks
+int exec_list(dbsrg_ctx *c, const ListPlan &P, int w) {
+  const DeviceGrid &g = c->g;
+  const int ns = g.ns, ks = g.ks, ms = g.ms;
+  cudaStream_t st = c->stream;
+  int rc;
+  if (P.icase == 0) {
+    const int t0 = P.wtl[w], nt = P.wtl[w + 1] - t0;
+    if (nt <= 0) return DBSRG_OK;
+    DBSRG_RUN(c, "k_vch", k_vch<<<(2 * ns * c->nbf + 255) / 256, 256, 0, st>>>(
+                              ns, c->nbf, g.fpbs, g.fqbs, c->pq, P.vch));
+    for (int t = 0; t < nt; t += 65535) {  // grid z limit
+      dim3 grid((unsigned)((ms + 127) / 128), (unsigned)((ms + 31) / 32),
+                (unsigned)std::min(65535, nt - t));
+      DBSRG_RUN(c, "k_overlap_update",
+                k_overlap_update<<<grid, 128, 0, st>>>(ns, P.tlist + t0 + t, P.bstart, P.order,
+                                                       P.lk1, P.lk2, P.lcd, c->ipbs, P.vch,
+                                                       hch_base(c)));
+    }
+    return DBSRG_OK;
   }
-  auto run_chunk = [&](const int *mb, int nm, const int *ob, int nown, const XQuad *xq,
-                       const XQuad *hxq_chunk, int nxq) -> int {
+  const int c0 = P.wchunk[w], c1 = P.wchunk[w + 1];
+  const int o0 = P.wown[w], nown_acf = P.wown[w + 1] - o0;
+  if (c0 == c1 && nown_acf == 0) return DBSRG_OK;
+  // tables of the case (cached after the first use)
+  const double *tabs[4] = {nullptr, nullptr, nullptr, nullptr};
+  for (int a = 0; a < P.na; a++) {
+    rc = DBSRG_OK;
+    if (P.icase == 2) {
+      // the factored path reads only the band |j-i| <= 16 of exchange
+      // tables and no table at all for the direct contraction
+      if (!P.factored)
+        rc = get_rtable(c, a, P.kpol, &tabs[a]);
+      else if (P.itype == 4)
+        rc = get_band_table(c, 0, a, P.kpol, &tabs[a]);
+    } else {
+      if (!P.factored)
+        rc = get_stable(c, P.ttype[0], P.kpol, &tabs[0]);
+      else if (P.icv >= 3)
+        rc = get_band_table(c, 1, P.ttype[0], P.kpol, &tabs[0]);
+    }
+    if (rc) return rc;
+  }
+  const int na = P.na, icv = P.icv;
+  const size_t per = P.per;
+  auto run_chunk = [&](const Chunk &ch) -> int {
+    const int *mb = P.work + ch.moff, *ob = P.work + ch.moff + ch.nm;
+    const int nm = ch.nm, nown = ch.nown;
     int rc2;
-    if (factored) {
+    if (P.factored) {
       double *Y = nullptr;
-      if (icv >= 3 && !split_x) {
+      if (icv >= 3 && !P.split_x) {
         if ((rc2 = ensure_scratch(c, sizeof(double) * per * na * nm))) return rc2;
         Y = (double *)c->scratch;
       }
       FactorJob job{};
-      job.family = tabfam;
-      job.kpol = kpol;
+      job.family = P.tabfam;
+      job.kpol = P.kpol;
       job.icv = icv;
-      job.sym = sym_d;
+      job.sym = P.sym_d;
       job.na = na;
       for (int a = 0; a < na; a++) {
-        job.types[a] = ttype[a];
-        job.jp1[a] = dsp.jp1[a];
-        job.jp2[a] = dsp.jp2[a];
-        job.ii[a] = ssp.ii[a];
-        job.jj[a] = ssp.jj[a];
+        job.types[a] = P.ttype[a];
+        job.jp1[a] = P.dsp.jp1[a];
+        job.jp2[a] = P.dsp.jp2[a];
+        job.ii[a] = P.ssp.ii[a];
+        job.jj[a] = P.ssp.jj[a];
         job.tabs[a] = tabs[a];
       }
       job.nm = nm;
       job.members = mb;
       job.nown = nown;
       job.own = ob;
-      job.info = info;
-      job.k2 = lk2;
-      job.k3 = lk3;
-      job.pairs = lpair;
-      job.cd = lcd;
+      job.info = P.info;
+      job.k2 = P.lk2;
+      job.k3 = P.lk3;
+      job.pairs = P.lpair;
+      job.cd = P.lcd;
       job.Y = Y;
       job.split = c->precision == DBSRG_SPLIT_BF16;
-      job.xq = xq;
-      job.hxq = hxq_chunk;
-      job.nxq = nxq;
+      job.xq = ch.nxq ? P.dxq + ch.xoff : nullptr;
+      job.hxq = ch.nxq ? P.hxq.data() + ch.xoff : nullptr;
+      job.nxq = ch.nxq;
       return factored_contract(c, job);
     }
     if ((rc2 = ensure_scratch(c, 2 * sizeof(double) * per * na * nm))) return rc2;
@@ -892,47 +958,74 @@ int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const 
     {
       dim3 gd((unsigned)((per + 255) / 256), (unsigned)nm, (unsigned)na);
       DBSRG_RUN(c, "k_density_acc",
-                k_density_acc<<<gd, 256, 0, st>>>(ns, ks, sym_d, ncol, na, dsp, nm, mb, info,
-                                                  lk2, lk3, lcd, c->pq, X));
+                k_density_acc<<<gd, 256, 0, st>>>(ns, ks, P.sym_d, P.ncol, na, P.dsp, nm, mb,
+                                                  P.info, P.lk2, P.lk3, P.lcd, c->pq, X));
     }
     for (int a = 0; a < na; a++) {
       const double *Xa = X + (size_t)a * nm * per;
       double *Ya = Y + (size_t)a * nm * per;
       if (icv <= 2) {
         int nrt = (ns + GBM - 1) / GBM;
-        dim3 gg((unsigned)(nrt * kb), (unsigned)((nm + GBN - 1) / GBN));
+        dim3 gg((unsigned)(nrt * P.kb), (unsigned)((nm + GBN - 1) / GBN));
         DBSRG_RUN(c, "k_band_contract",
-                  k_band_contract<<<gg, 256, 0, st>>>(ns, kb, icv, tabs[a], nm, Xa, Ya));
+                  k_band_contract<<<gg, 256, 0, st>>>(ns, P.kb, icv, tabs[a], nm, Xa, Ya));
       } else {
-        int mode = tabfam == 0 ? 0 : (icv == 3 ? 1 : 2);
+        int mode = P.tabfam == 0 ? 0 : (icv == 3 ? 1 : 2);
         dim3 gx((unsigned)(((size_t)ns * ns + 255) / 256), (unsigned)((nm + XNB - 1) / XNB));
         DBSRG_RUN(c, "k_exchange",
                   k_exchange<<<gx, 256, 0, st>>>(ns, ks, mode, nm, tabs[a], Xa, Ya));
       }
     }
-    int mode = sym_d == 'x' ? 0 : 1;
+    int mode = P.sym_d == 'x' ? 0 : 1;
     size_t space = mode == 0 ? (size_t)ms * ms : (size_t)4 * ns * (2 * ks - 1);
     dim3 gs((unsigned)((space + 255) / 256), (unsigned)nown);
     DBSRG_RUN(c, "k_scatter",
-              k_scatter<<<gs, 256, 0, st>>>(ns, ks, mode, ssp, nm, mb, ob, info,
-                                            Y, hch_base(c)));
+              k_scatter<<<gs, 256, 0, st>>>(ns, ks, mode, P.ssp, nm, mb, ob, P.info, Y,
+                                            hch_base(c)));
     return DBSRG_OK;
   };
-  for (const Chunk &ch : chunks)
-    if ((rc = run_chunk(members + ch.moff, ch.nm, members + ch.moff + ch.nm, ch.nown,
-                        dxq ? dxq + ch.xoff : nullptr, dxq ? hxq.data() + ch.xoff : nullptr,
-                        ch.nxq)))
-      return rc;
-  if (icase == 2 && itype == 3) {
-    const int nown = (int)hown.size();
-    if (nown > 0) {
-      const double *quad;
-      if ((rc = get_quad(c, kpol, &quad))) return rc;
-      DBSRG_RUN(c, "k_acf", k_acf<<<(nown + 127) / 128, 128, 0, st>>>(nown, owners, info, kpol,
-                                                                    c->nbf, lk2, lk3, lcd, quad,
-                                                                    c->acf, c->iicc));
-    }
+  for (int k = c0; k < c1; k++)
+    if ((rc = run_chunk(P.chunks[k]))) return rc;
+  if (nown_acf > 0) {
+    const double *quad;
+    if ((rc = get_quad(c, P.kpol, &quad))) return rc;
+    DBSRG_RUN(c, "k_acf",
+              k_acf<<<(nown_acf + 127) / 128, 128, 0, st>>>(
+                  nown_acf, P.work + P.own_off + o0, P.info, P.kpol, c->nbf, P.lk2, P.lk3, P.lcd,
+                  quad, c->acf, c->iicc));
   }
+  return DBSRG_OK;
+}
+
+}  // namespace
+
+int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const int *ipt,
+                     const int *k1, const int *k2, const int *k3, const int *k4,
+                     const double *cdata) {
+  (void)k4;
+  if (n <= 0) return DBSRG_OK;
+  if (!c->hch) return set_err(c, DBSRG_ESTATE, "no matrix allocated");
+  if (!c->pq) return set_err(c, DBSRG_ESTATE, "no orbitals set");
+  cudaStream_t st = c->stream;
+  int rc;
+  // The list state lives in one of two buffers; in the asynchronous mode the
+  // set-up runs on the set-up stream once the kernels of the call two back
+  // are done with the buffer, while the previous call's kernels run.
+  const bool pipe = c->async;
+  const int par = c->lpar;
+  c->lpar ^= 1;
+  cudaStream_t ss = pipe ? c->sstream : st;
+  if ((rc = ensure_lstate(c, par, plan_bytes(c, icase, n)))) return rc;
+  if (pipe) DBSRG_TRY(c, cudaStreamWaitEvent(ss, c->lfree[par], 0));
+  ListPlan P;
+  if ((rc = plan_list(c, icase, itype, kpol, n, ipt, k1, k2, k3, cdata, c->wlo, c->wcap, 1,
+                      c->lstate[par], ss, P)))
+    return rc;
+  if (pipe) {  // the contraction waits for the set-up
+    DBSRG_TRY(c, cudaEventRecord(c->lready, ss));
+    DBSRG_TRY(c, cudaStreamWaitEvent(st, c->lready, 0));
+  }
+  if ((rc = exec_list(c, P, 0))) return rc;
   // the kernels of this call are done with the list state after this point
   DBSRG_TRY(c, cudaEventRecord(c->lfree[par], st));
   if (pipe) {
@@ -940,4 +1033,60 @@ int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const 
     return DBSRG_OK;
   }
   return drain(c);  // synchronous mode: wait, and report the tensor-core error word
+}
+
+int assemble_windows(dbsrg_ctx *c, int nlists, const dbsrg_list *lists, int nwin, int nslot,
+                     const std::function<int(int w, double *slot)> &before,
+                     const std::function<int(int w, int blo, int nb, double *slot)> &after) {
+  const int iicc = c->iicc;
+  const int nw = (iicc + nwin - 1) / nwin;
+  const size_t blk = (size_t)c->g.ms * c->g.ms;
+  std::vector<ListPlan> plans((size_t)nlists);
+  std::vector<void *> mem((size_t)nlists, nullptr);
+  const double *hch0 = c->hch;
+  const int wlo0 = c->wlo, wcap0 = c->wcap;
+  auto slot_of = [&](int w) { return c->hmem + (size_t)(w % nslot) * nwin * blk; };
+  auto enter = [&](int w) {
+    c->hch = slot_of(w);
+    c->wlo = 1 + w * nwin;
+    c->wcap = nwin;
+  };
+  auto body = [&]() -> int {
+    int rc;
+    // window 0 is executed list by list right after each list's set-up, so
+    // the set-up of list l+1 overlaps the kernels of list l
+    enter(0);
+    if ((rc = before(0, c->hch))) return rc;
+    for (int l = 0; l < nlists; l++) {
+      const dbsrg_list &L = lists[l];
+      if (L.ncdata < 0) return set_err(c, DBSRG_EINVAL, "ncdata < 0");
+      if (L.ncdata == 0) continue;
+      if (!L.k1 || !L.k2 || !L.k3 || !L.cdata) return set_err(c, DBSRG_EINVAL, "null list pointer");
+      if (!(mem[l] = cache_alloc(c, plan_bytes(c, L.icase, L.ncdata))))
+        return set_err(c, DBSRG_ENOMEM, "list state allocation failed");
+      if ((rc = plan_list(c, L.icase, L.itype, L.kpol, L.ncdata, L.ipt, L.k1, L.k2, L.k3,
+                          L.cdata, 1, nwin, nw, mem[l], c->sstream, plans[l])))
+        return rc;
+      DBSRG_TRY(c, cudaEventRecord(c->lready, c->sstream));
+      DBSRG_TRY(c, cudaStreamWaitEvent(c->stream, c->lready, 0));
+      if ((rc = exec_list(c, plans[l], 0))) return rc;
+    }
+    if ((rc = after(0, 1, std::min(nwin, iicc), c->hch))) return rc;
+    for (int w = 1; w < nw; w++) {
+      enter(w);
+      if ((rc = before(w, c->hch))) return rc;
+      for (int l = 0; l < nlists; l++)
+        if (lists[l].ncdata > 0 && (rc = exec_list(c, plans[l], w))) return rc;
+      const int blo = 1 + w * nwin;
+      if ((rc = after(w, blo, std::min(nwin, iicc - blo + 1), c->hch))) return rc;
+    }
+    return DBSRG_OK;
+  };
+  int rc = body();
+  const int rd = drain(c);
+  for (void *p : mem) cache_free(c, p);  // pooled for the next assembly
+  c->hch = const_cast<double *>(hch0);
+  c->wlo = wlo0;
+  c->wcap = wcap0;
+  return rc ? rc : rd;
 }

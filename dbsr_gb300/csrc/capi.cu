@@ -1,4 +1,5 @@
 // capi.cu -- the extern "C" entry points declared in include/dbsrg.h.
+#include <algorithm>
 #include <cstdlib>
 #include <cstring>
 #include <new>
@@ -119,6 +120,41 @@ int ensure_tcscratch(dbsrg_ctx *c, size_t bytes) {
 int ensure_pscratch(dbsrg_ctx *c, size_t bytes) {
   return grow(c, &c->pscratch, &c->pscratch_bytes, bytes);
 }
+void *cache_alloc(dbsrg_ctx *c, size_t bytes) {
+  auto it = c->pool.find(bytes);
+  void *p = nullptr;
+  if (it != c->pool.end()) {
+    p = it->second;
+    c->pool.erase(it);
+  } else if (cudaMalloc(&p, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    pool_trim(c);
+    if (cudaMalloc(&p, bytes) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+  }
+  c->psize[p] = bytes;
+  return p;
+}
+
+void cache_free(dbsrg_ctx *c, void *p) {
+  if (!p) return;
+  auto it = c->psize.find(p);
+  if (it == c->psize.end()) {
+    cudaFree(p);
+    return;
+  }
+  c->pool.emplace(it->second, p);
+  c->psize.erase(it);
+}
+
+void pool_trim(dbsrg_ctx *c) {
+  if (!c->pool.empty()) cudaStreamSynchronize(c->stream);
+  for (auto &kv : c->pool) cudaFree(kv.second);
+  c->pool.clear();
+}
+
 int ensure_lstate(dbsrg_ctx *c, int par, size_t bytes) {
   if (c->lstate_bytes[par] >= bytes) return DBSRG_OK;
   if (c->lstate[par]) DBSRG_TRY(c, cudaStreamSynchronize(c->sstream));
@@ -163,21 +199,21 @@ static void timing_clear(dbsrg_ctx *c) {
 
 static void free_tables(dbsrg_ctx *c) {
   for (double *p : c->rtab)
-    if (p) cudaFree(p);
+    cache_free(c, p);
   for (double *p : c->stab)
-    if (p) cudaFree(p);
+    cache_free(c, p);
   for (double *p : c->quad)
-    if (p) cudaFree(p);
+    cache_free(c, p);
   for (double *p : c->rbtab)
-    if (p) cudaFree(p);
+    cache_free(c, p);
   for (double *p : c->sbtab)
-    if (p) cudaFree(p);
+    cache_free(c, p);
   c->rbtab.clear();
   c->sbtab.clear();
   for (auto &cd : c->rcell)
-    if (cd.lo1) cudaFree(cd.lo1);
+    cache_free(c, cd.lo1);
   for (auto &cd : c->scell)
-    if (cd.lo1) cudaFree(cd.lo1);
+    cache_free(c, cd.lo1);
   free_orbital_products(c);
   c->rtab.clear();
   c->stab.clear();
@@ -212,6 +248,10 @@ int dbsrg_create(dbsrg_ctx **out, const dbsrg_grid_desc *d) {
     return DBSRG_ECUDA;
   }
   if (cudaStreamCreateWithFlags(&c->sstream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c->cstream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->cdone[0], cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->cdone[1], cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->wdone, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->lfree[0], cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->lfree[1], cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->lready, cudaEventDisableTiming) != cudaSuccess) {
@@ -241,8 +281,10 @@ int dbsrg_destroy(dbsrg_ctx *c) {
   if (!c) return DBSRG_OK;
   cudaSetDevice(c->device);
   if (c->sstream) cudaStreamSynchronize(c->sstream);
+  if (c->cstream) cudaStreamSynchronize(c->cstream);
   if (c->stream) cudaStreamSynchronize(c->stream);
   free_tables(c);
+  pool_trim(c);
   DeviceGrid &g = c->g;
   double *arrs[] = {g.t, g.tp, g.tq, g.gx, g.gw, g.gr, g.grw, g.grm,
                     g.pbsp, g.qbsp, g.fpbs, g.fqbs, g.fppqq, g.tri};
@@ -251,7 +293,7 @@ int dbsrg_destroy(dbsrg_ctx *c) {
   if (c->pq) cudaFree(c->pq);
   if (c->ipbs) cudaFree(c->ipbs);
   if (c->icc) cudaFree(c->icc);
-  if (c->hch) cudaFree(c->hch);
+  if (c->hmem) cudaFree(c->hmem);
   if (c->acf) cudaFree(c->acf);
   if (c->scratch) cudaFree(c->scratch);
   if (c->scratch2) cudaFree(c->scratch2);
@@ -264,6 +306,8 @@ int dbsrg_destroy(dbsrg_ctx *c) {
     if (c->lfree[i]) cudaEventDestroy(c->lfree[i]);
   }
   if (c->lready) cudaEventDestroy(c->lready);
+  for (cudaEvent_t e : {c->cdone[0], c->cdone[1], c->wdone})
+    if (e) cudaEventDestroy(e);
   if (c->kerr) cudaFree(c->kerr);
   if (c->bmap) cudaFree(c->bmap);
   if (c->b2o) cudaFree(c->b2o);
@@ -271,6 +315,7 @@ int dbsrg_destroy(dbsrg_ctx *c) {
   timing_clear(c);
   for (cudaEvent_t e : c->evpool) cudaEventDestroy(e);
   if (c->sstream) cudaStreamDestroy(c->sstream);
+  if (c->cstream) cudaStreamDestroy(c->cstream);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return DBSRG_OK;
@@ -282,6 +327,16 @@ int dbsrg_release_tables(dbsrg_ctx *c) {
   SETTLE(c);
   DBSRG_TRY(c, cudaStreamSynchronize(c->stream));
   free_tables(c);
+  pool_trim(c);
+  return DBSRG_OK;
+}
+
+int dbsrg_invalidate_tables(dbsrg_ctx *c) {
+  if (!c) return DBSRG_EINVAL;
+  cudaSetDevice(c->device);
+  SETTLE(c);
+  DBSRG_TRY(c, cudaStreamSynchronize(c->stream));
+  free_tables(c);  // the buffers stay in the pool for the rebuild
   return DBSRG_OK;
 }
 
@@ -360,8 +415,7 @@ int dbsrg_set_orbitals(dbsrg_ctx *c, int nbf, const double *pq, const int *ipbs)
   if (c->ipbs) cudaFree(c->ipbs);
   c->pq = nullptr;
   c->ipbs = nullptr;
-  for (double *p : c->quad)
-    if (p) cudaFree(p);
+  for (double *p : c->quad) cache_free(c, p);
   c->quad.clear();
   size_t n = (size_t)2 * c->g.ns * nbf;
   DBSRG_TRY(c, cudaMalloc((void **)&c->pq, n * sizeof(double)));
@@ -410,10 +464,11 @@ int dbsrg_alloc_matrix_window(dbsrg_ctx *c, int nch, const int *icc, int iicc, i
   cudaSetDevice(c->device);
   SETTLE(c);
   if (c->icc) cudaFree(c->icc);
-  if (c->hch) cudaFree(c->hch);
+  if (c->hmem) cudaFree(c->hmem);
   if (c->acf) cudaFree(c->acf);
   c->icc = nullptr;
-  c->hch = nullptr;
+  c->hch = c->hmem = nullptr;
+  c->hcap = 0;
   c->acf = nullptr;
   c->h_icc.assign((size_t)nch * nch, 0);
   if (is_device_ptr(icc)) {
@@ -425,7 +480,9 @@ int dbsrg_alloc_matrix_window(dbsrg_ctx *c, int nch, const int *icc, int iicc, i
     if (v < 0 || v > iicc) return set_err(c, DBSRG_ERANGE, "icc entry out of range");
   const size_t ms = c->g.ms;
   DBSRG_TRY(c, cudaMalloc((void **)&c->icc, sizeof(int) * (size_t)nch * nch));
-  DBSRG_TRY(c, cudaMalloc((void **)&c->hch, sizeof(double) * ms * ms * nwin));
+  DBSRG_TRY(c, cudaMalloc((void **)&c->hmem, sizeof(double) * ms * ms * nwin));
+  c->hch = c->hmem;
+  c->hcap = nwin;
   DBSRG_TRY(c, cudaMalloc((void **)&c->acf, sizeof(double) * (size_t)iicc * (mk + 1)));
   int rc = copy_in(c, c->icc, c->h_icc.data(), sizeof(int) * (size_t)nch * nch);
   if (rc) return rc;
@@ -527,7 +584,7 @@ int dbsrg_gen_batch_streamed(int nctx, dbsrg_ctx *const *ctxs, const int *nlists
   std::vector<size_t> off((size_t)nctx + 1, 0);
   for (int i = 0; i < nctx; i++) {
     if (!ctxs[i] || nlists[i] < 0) return DBSRG_EINVAL;
-    if (!ctxs[i]->hch) return set_err(ctxs[i], DBSRG_ESTATE, "no matrix allocated");
+    if (!ctxs[i]->hmem) return set_err(ctxs[i], DBSRG_ESTATE, "no matrix allocated");
     off[i + 1] = off[i] + (size_t)nlists[i];
   }
   if (off[nctx] > 0 && !lists) return DBSRG_EINVAL;
@@ -535,26 +592,31 @@ int dbsrg_gen_batch_streamed(int nctx, dbsrg_ctx *const *ctxs, const int *nlists
     for (int j = i + 1; j < nctx; j++)
       if (ctxs[i] == ctxs[j]) return set_err(ctxs[i], DBSRG_EINVAL, "gen_batch: context twice");
   std::vector<int> rc((size_t)nctx, DBSRG_OK);
-  // per context: every window in turn, the lists pipelined within a window,
-  // then the window handed to the consumer
+  // per context: every list set up once, the windows in block order, each
+  // window zeroed, assembled, drained and handed to the consumer
   auto work = [&](int i) {
     dbsrg_ctx *c = ctxs[i];
     cudaSetDevice(c->device);
-    const bool was = c->async;
-    for (int blo = 1; blo <= c->iicc && rc[i] == DBSRG_OK; blo += c->wcap) {
-      if ((rc[i] = dbsrg_set_window(c, blo))) break;
-      c->async = true;
-      for (size_t l = off[i]; l < off[i + 1] && rc[i] == DBSRG_OK; l++) {
-        const dbsrg_list &L = lists[l];
-        rc[i] = dbsrg_gen_matrix(c, L.icase, L.itype, L.kpol, L.ncdata, L.ipt, L.k1, L.k2, L.k3,
-                                 L.k4, L.cdata);
-      }
-      c->async = was;
-      const int rd = drain(c);
-      if (rc[i] == DBSRG_OK) rc[i] = rd;
-      if (rc[i] == DBSRG_OK) fn(user, i, blo, window_blocks(c), c->hch);
+    if ((rc[i] = drain(c))) return;
+    const size_t blk = (size_t)c->g.ms * c->g.ms;
+    const int nwin = c->wcap;
+    if (cudaMemsetAsync(c->acf, 0, sizeof(double) * (size_t)c->iicc * (c->mk + 1), c->stream) !=
+        cudaSuccess) {
+      rc[i] = cuda_check(c, cudaGetLastError(), "acf");
+      return;
     }
-    c->async = was;
+    auto before = [&](int, double *slot) -> int {
+      DBSRG_TRY(c, cudaMemsetAsync(slot, 0, sizeof(double) * blk * nwin, c->stream));
+      return DBSRG_OK;
+    };
+    auto after = [&](int, int blo, int nb, double *slot) -> int {
+      int r = drain(c);
+      if (r) return r;
+      fn(user, i, blo, nb, slot);
+      return DBSRG_OK;
+    };
+    rc[i] = assemble_windows(c, nlists[i], lists + off[i], nwin, 1, before, after);
+    c->wlo = 1 + ((c->iicc - 1) / nwin) * nwin;  // the last window stays held
   };
   std::vector<std::thread> th;
   for (int i = 1; i < nctx; i++) th.emplace_back(work, i);
@@ -562,6 +624,48 @@ int dbsrg_gen_batch_streamed(int nctx, dbsrg_ctx *const *ctxs, const int *nlists
   for (auto &t : th) t.join();
   for (int i = 0; i < nctx; i++)
     if (rc[i] != DBSRG_OK) return rc[i];
+  return DBSRG_OK;
+}
+
+int dbsrg_assemble_to_host(dbsrg_ctx *c, int nlists, const dbsrg_list *lists, int nwin,
+                           double *hch_host, double *acf_host) {
+  if (!c) return DBSRG_EINVAL;
+  if (nlists < 0 || (nlists > 0 && !lists) || !hch_host)
+    return set_err(c, DBSRG_EINVAL, "assemble_to_host: bad arguments");
+  if (!c->hmem) return set_err(c, DBSRG_ESTATE, "no matrix allocated");
+  cudaSetDevice(c->device);
+  SETTLE(c);
+  const int iicc = c->iicc;
+  if (nwin <= 0) nwin = std::max(1, (iicc + 7) / 8);
+  nwin = std::min(nwin, iicc);
+  const int nslot = nwin < iicc ? 2 : 1;
+  if (nslot * nwin > c->hcap)
+    return set_err(c, DBSRG_EINVAL, "assemble_to_host: two windows must fit the allocation");
+  const size_t blk = (size_t)c->g.ms * c->g.ms;
+  const cudaMemcpyKind kind =
+      is_device_ptr(hch_host) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  DBSRG_TRY(c, cudaMemsetAsync(c->acf, 0, sizeof(double) * (size_t)iicc * (c->mk + 1), c->stream));
+  // window w (slot w % 2) is assembled on the contraction stream while the
+  // copy stream moves window w-1 out; a slot is zeroed again only after its
+  // copy
+  auto before = [&](int w, double *slot) -> int {
+    DBSRG_TRY(c, cudaStreamWaitEvent(c->stream, c->cdone[w % nslot], 0));
+    DBSRG_TRY(c, cudaMemsetAsync(slot, 0, sizeof(double) * blk * nwin, c->stream));
+    return DBSRG_OK;
+  };
+  auto after = [&](int w, int blo, int nb, double *slot) -> int {
+    DBSRG_TRY(c, cudaEventRecord(c->wdone, c->stream));
+    DBSRG_TRY(c, cudaStreamWaitEvent(c->cstream, c->wdone, 0));
+    DBSRG_TRY(c, cudaMemcpyAsync(hch_host + (size_t)(blo - 1) * blk, slot,
+                                 sizeof(double) * blk * nb, kind, c->cstream));
+    DBSRG_TRY(c, cudaEventRecord(c->cdone[w % nslot], c->cstream));
+    return DBSRG_OK;
+  };
+  const int rc = assemble_windows(c, nlists, lists, nwin, nslot, before, after);
+  const cudaError_t ce = cudaStreamSynchronize(c->cstream);
+  if (rc) return rc;
+  if (ce != cudaSuccess) return cuda_check(c, ce, "assemble_to_host copy");
+  if (acf_host) return copy_out(c, acf_host, c->acf, sizeof(double) * (size_t)iicc * (c->mk + 1));
   return DBSRG_OK;
 }
 

@@ -690,8 +690,7 @@ int split_exchange(dbsrg_ctx *c, const SplitExchange &x) {
     void *d = nullptr;
     const size_t bytes =
         2 * TS * sl * sizeof(__nv_bfloat16) + 2 * (size_t)NR * EXP_PER_ROWTILE * sizeof(int);
-    if (cudaMalloc(&d, bytes) != cudaSuccess) {
-      cudaGetLastError();
+    if (!(d = cache_alloc(c, bytes))) {
       return set_err(c, DBSRG_ENOMEM, "digit allocation failed");
     }
     f->Ud = d;

@@ -710,7 +710,7 @@ static int get_farfield(dbsrg_ctx *c, int family, int type, int k, int cs, const
   const int ns = g.ns, nb = c->nbound, kk = g.ks * g.ks;
   size_t m = (size_t)ns * nb;
   double *base = nullptr;
-  if (cudaMalloc((void **)&base, 4 * m * sizeof(double)) != cudaSuccess)
+  if (!(base = (double *)cache_alloc(c, 4 * m * sizeof(double))))
     return set_err(c, DBSRG_ENOMEM, "far-field allocation failed");
   FarField f;
   f.U = base;
@@ -746,7 +746,8 @@ static int ensure_brows(dbsrg_ctx *c) {
   if (c->brows) return DBSRG_OK;
   const int ns = c->g.ns, nb = c->nbound;
   const size_t m = (size_t)ns * nb;
-  DBSRG_TRY(c, cudaMalloc((void **)&c->brows, 2 * m * sizeof(double)));
+  if (!(c->brows = (double *)cache_alloc(c, 2 * m * sizeof(double))))
+    return set_err(c, DBSRG_ENOMEM, "bound-orbital rows allocation failed");
   for (int comp = 1; comp <= 2; comp++)
     DBSRG_RUN(c, "k_bound_rows",
               k_bound_rows<<<(unsigned)((m + 255) / 256), 256, 0, c->stream>>>(
@@ -796,7 +797,7 @@ int get_pairpot_direct(dbsrg_ctx *c, int family, int type, int k, int icv, int j
   if ((rc = ensure_pscratch(c, sbytes))) return rc;
   double *SA = (double *)c->pscratch, *SB = SA + npair * nv, *Dq = SB + npair * nv;
   double *K = nullptr;
-  if (cudaMalloc((void **)&K, npair * per * sizeof(double)) != cudaSuccess) {
+  if (!(K = (double *)cache_alloc(c, npair * per * sizeof(double)))) {
     cudaGetLastError();
     return set_err(c, DBSRG_ENOMEM, "pair potential allocation failed");
   }
@@ -843,7 +844,7 @@ static int get_pairpot_band(dbsrg_ctx *c, int family, int type, int k, int cs, i
   int rc;
   if ((rc = ensure_brows(c))) return rc;
   double *K = nullptr;
-  if (cudaMalloc((void **)&K, npair * per * sizeof(double)) != cudaSuccess) {
+  if (!(K = (double *)cache_alloc(c, npair * per * sizeof(double)))) {
     cudaGetLastError();
     return set_err(c, DBSRG_ENOMEM, "pair potential allocation failed");
   }
@@ -869,15 +870,15 @@ void free_orbital_products(dbsrg_ctx *c) {
     cudaStreamSynchronize(c->stream);
   for (auto *v : {&c->rfar, &c->sfar})
     for (auto &kv : *v) {
-      if (kv.second.U) cudaFree(kv.second.U);
-      if (kv.second.Ud) cudaFree(kv.second.Ud);
+      cache_free(c, kv.second.U);
+      cache_free(c, kv.second.Ud);
     }
   c->rfar.clear();
   c->sfar.clear();
   for (auto &kv : c->ppot)
-    if (kv.second) cudaFree(kv.second);
+    cache_free(c, kv.second);
   c->ppot.clear();
-  if (c->brows) cudaFree(c->brows);
+  cache_free(c, c->brows);
   c->brows = nullptr;
 }
 

@@ -15,6 +15,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <functional>
 #include <map>
 #include <string>
 #include <vector>
@@ -78,7 +79,9 @@ struct dbsrg_ctx {
   int nch = 0, iicc = 0, mk = -1;
   int *icc = nullptr;
   std::vector<int> h_icc;
-  double *hch = nullptr;
+  double *hch = nullptr;   // the current window's first block
+  double *hmem = nullptr;  // the matrix allocation (hcap blocks)
+  int hcap = 0;
   double *acf = nullptr;
   // table caches, indexed [k*4+type] (R) and [k*2+type] (S)
   std::vector<double *> rtab, stab;
@@ -135,6 +138,17 @@ struct dbsrg_ctx {
   // of them unless dbsrg_alloc_matrix_window asked for fewer); Gen_matrix
   // skips the segments of blocks outside the window
   int wlo = 1, wcap = 0;
+  // assembly straight into host memory (dbsrg_assemble_to_host): windows
+  // alternate between two halves of the allocation while a copy stream
+  // moves the finished one to the host
+  cudaStream_t cstream = nullptr;
+  cudaEvent_t cdone[2] = {nullptr, nullptr}, wdone = nullptr;
+  // pool of released cache buffers (tables, cell data, far fields, digits,
+  // pair potentials), reused by exact size: a rebuild after
+  // dbsrg_invalidate_tables allocates nothing; dbsrg_release_tables and
+  // allocation failures return the pool to the device
+  std::multimap<size_t, void *> pool;
+  std::map<void *, size_t> psize;
   // error word of the tensor-core kernels (bounded waits), read whenever the
   // context waits for its stream
   int *kerr = nullptr;
@@ -218,6 +232,10 @@ int copy_in_s(dbsrg_ctx *c, void *dst, const void *src, size_t n, cudaStream_t s
 // waits for both streams and reports failures of queued kernels
 int drain(dbsrg_ctx *c);
 int ensure_lstate(dbsrg_ctx *c, int par, size_t bytes);
+// cache buffers through the pool (nullptr when the device is out of memory)
+void *cache_alloc(dbsrg_ctx *c, size_t bytes);
+void cache_free(dbsrg_ctx *c, void *p);
+void pool_trim(dbsrg_ctx *c);
 int copy_out(dbsrg_ctx *c, void *dst, const void *src, size_t n);
 // scratch arenas (device)
 int ensure_scratch(dbsrg_ctx *c, size_t bytes);
@@ -248,6 +266,13 @@ int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n,
                      const int *ipt, const int *k1, const int *k2,
                      const int *k3, const int *k4, const double *cdata);
 int update_hx(dbsrg_ctx *c, int ich, int jch, const double *d, double cc);
+// Every list set up once, then executed window by window over the blocks
+// (windows of nwin blocks alternating between nslot slots of the matrix
+// allocation): before(w, slot) prepares a slot (on the contraction stream),
+// after(w, blo, nb, slot) takes the assembled window.  Drains at the end.
+int assemble_windows(dbsrg_ctx *c, int nlists, const dbsrg_list *lists, int nwin, int nslot,
+                     const std::function<int(int w, double *slot)> &before,
+                     const std::function<int(int w, int blo, int nb, double *slot)> &after);
 
 // ---- factor.cu ------------------------------------------------------------
 int ensure_fscratch(dbsrg_ctx *c, size_t bytes);

@@ -552,7 +552,7 @@ int get_celldata(dbsrg_ctx *c, int family, int type, int k, const CellData **out
   const int nv = g.nv, kk = g.ks * g.ks;
   size_t m = (size_t)kk * nv, d = (size_t)kk * kk * nv;
   double *base = nullptr;
-  if (cudaMalloc((void **)&base, (4 * m + d) * sizeof(double)) != cudaSuccess)
+  if (!(base = (double *)cache_alloc(c, (4 * m + d) * sizeof(double))))
     return set_err(c, DBSRG_ENOMEM, "cell data allocation failed");
   CellData cd;
   cd.lo1 = base;
@@ -598,7 +598,7 @@ static int get_table_any(dbsrg_ctx *c, int family, int type, int k, int band,
   int rc = get_celldata(c, family, type, k, &cd);
   if (rc) return rc;
   double *tab = nullptr;
-  if (cudaMalloc((void **)&tab, nt * sizeof(double)) != cudaSuccess)
+  if (!(tab = (double *)cache_alloc(c, nt * sizeof(double))))
     return set_err(c, DBSRG_ENOMEM, "table allocation failed");
   unsigned nb = (unsigned)((nt + 255) / 256);
   if (family == 0) {
@@ -714,7 +714,7 @@ int get_quad(dbsrg_ctx *c, int k, const double **out) {
   double *q = nullptr;
   size_t n = (size_t)c->nbf * c->nbf * 2;
   size_t gp = (size_t)g.ns * g.ksp, gq = (size_t)g.ns * g.ksq, nw = (size_t)2 * c->nbf * g.ns;
-  if (cudaMalloc((void **)&q, (n + gp + gq + nw) * sizeof(double)) != cudaSuccess)
+  if (!(q = (double *)cache_alloc(c, (n + gp + gq + nw) * sizeof(double))))
     return set_err(c, DBSRG_ENOMEM, "quad allocation failed");
   double *GP = q + n, *GQ = GP + gp, *W = GQ + gq;
   DBSRG_RUN(c, "k_rk_gram", k_rk_gram<<<(unsigned)((gp + 127) / 128), 128, 0, c->stream>>>(

@@ -152,12 +152,27 @@ int dbsrg_gen_batch(int nctx, dbsrg_ctx *const *ctxs, const int *nlists,
  * of them, ms x ms each, in the hch layout) and may read them (with
  * dbsrg_get_matrix or its own copies) before it returns, when the window is
  * reused.  fn runs on the context's host thread, concurrently for different
- * contexts.  acf is complete at the end.  Returns as dbsrg_gen_batch. */
+ * contexts.  Every list is set up once (segments, chunks per window) and
+ * executed window by window.  The windows and acf start from zero; acf is
+ * complete at the end.  Returns as dbsrg_gen_batch. */
 typedef void (*dbsrg_window_fn)(void *user, int ictx, int blo, int nblocks,
                                 const double *window);
 int dbsrg_gen_batch_streamed(int nctx, dbsrg_ctx *const *ctxs,
                              const int *nlists, const dbsrg_list *lists,
                              dbsrg_window_fn fn, void *user);
+
+/* The whole assembly of one context straight into a caller's matrix
+ * hch_host(ms,ms,iicc) (host, best pinned, or device) and acf_host
+ * (iicc,0:mk) (may be NULL): the lists run once per window of nwin blocks
+ * (nwin <= 0: iicc/8; every list is set up once, its work split by
+ * window), windows alternating between two halves of the device
+ * allocation, and while one window is assembled the previous one is copied
+ * out on a separate stream, so the copy hides behind the assembly.
+ * The allocation must hold two windows (or nwin >= iicc).  The device
+ * matrix is overwritten; acf is zeroed first.  Lists are as for
+ * dbsrg_gen_batch (one context). */
+int dbsrg_assemble_to_host(dbsrg_ctx *ctx, int nlists, const dbsrg_list *lists,
+                           int nwin, double *hch_host, double *acf_host);
 
 /* UPDATE_HX(ich,jch,d,C) (updates.f90:79-106): add C*d (d is ms x ms,
  * host or device) to the block of channel pair (ich,jch). */
@@ -200,10 +215,14 @@ int dbsrg_get_diag_cells(dbsrg_ctx *ctx, int type, int k, double *out);
  * "qbsd","fpbs","fqbs","fppqq" (reference shapes). */
 int dbsrg_get_grid_array(dbsrg_ctx *ctx, const char *name, double *out);
 
-/* Free the cached R^k/S^k tables (the reference keeps them for the whole
- * run, dbsr_lib_dbs.f90:1595-1624; a caller that wants each assembly to
- * rebuild them, or to reclaim the memory, releases them here). */
+/* Free the cached R^k/S^k tables and everything derived from them (cell
+ * data, far fields, pair potentials), returning the memory to the device
+ * (the reference keeps its tables for the whole run,
+ * dbsr_lib_dbs.f90:1595-1624). */
 int dbsrg_release_tables(dbsrg_ctx *ctx);
+/* Mark the same caches stale: the next assembly rebuilds every table in
+ * the memory they occupied (no reference counterpart). */
+int dbsrg_invalidate_tables(dbsrg_ctx *ctx);
 
 /* Number of this library's kernels launched by the context so far. */
 long long dbsrg_kernel_launches(const dbsrg_ctx *ctx);

@@ -64,3 +64,24 @@ def test_async_setup_errors_raised_by_the_call():
         a.gen_matrix(L.icase, L.itype, L.kpol, bad, L.k2, L.k3, L.k4, L.c)
     a.sync()  # the first list's kernels completed without error
     a.close()
+
+
+def test_invalidated_and_released_tables_rebuild_identically():
+    w = synth.small(ns=70, nch=5, mk=4, n_entries=3000, seed=43)
+    a = Assembler(w.t, w.ks, w.ksp, w.ksq)
+    a.set_orbitals(w.pq, w.ipbs)
+    a.alloc_matrix(w.nch, w.icc, w.iicc, w.mk)
+    a.set_precision(SPLIT_BF16)
+    out = []
+    for how in (None, "invalidate", "invalidate", "release", "invalidate"):
+        if how == "invalidate":
+            a.invalidate_tables()  # rebuilt from the pooled buffers
+        elif how == "release":
+            a.release_tables()
+        a.zero_matrix()
+        for L in w.lists:
+            a.gen_matrix(L.icase, L.itype, L.kpol, L.k1, L.k2, L.k3, L.k4, L.c)
+        out.append(a.get_matrix())
+    a.close()
+    for h in out[1:]:
+        assert np.array_equal(h, out[0])

@@ -116,3 +116,32 @@ def test_largest_batch_block_full_size_window_independent():
     assert np.isfinite(t1).all() and (t1 > 0).sum() > 0.04 * w.iicc
     assert np.array_equal(s1, s2) and np.array_equal(t1, t2)
     assert np.array_equal(acf1, acf2)
+
+
+@pytest.mark.parametrize("nwin", [1, 2, 5, 0, 10 ** 6])
+def test_assemble_to_host_equals_whole_assembly(nwin):
+    torch = pytest.importorskip("torch")
+    w = synth.small(ns=60, nch=5, mk=3, n_entries=2000, seed=53)
+    h0, acf0 = full(w, SPLIT_BF16)
+    a = make(w, SPLIT_BF16)
+    a.gen_matrix(*items(w)[0])  # leftovers in the device matrix must not matter
+    out, acf = a.assemble_to_host(items(w), nwin=nwin)
+    assert np.array_equal(out, h0) and np.array_equal(acf, acf0)
+    # pinned host and device destinations
+    hp = torch.zeros(h0.size, dtype=torch.float64).pin_memory()
+    a.assemble_to_host(items(w), out=hp, nwin=nwin)
+    assert np.array_equal(hp.numpy().reshape(h0.shape, order="F"), h0)
+    hd = torch.zeros(h0.size, dtype=torch.float64, device="cuda")
+    a.assemble_to_host(items(w), out=hd, nwin=nwin)
+    assert np.array_equal(hd.cpu().numpy().reshape(h0.shape, order="F"), h0)
+    a.close()
+
+
+def test_assemble_to_host_needs_two_windows():
+    w = synth.small(ns=50, nch=4, mk=2, n_entries=300, seed=54)
+    a = make(w, SPLIT_BF16, window=4)  # 4 of 10 blocks allocated
+    with pytest.raises(DbsrgError, match="EINVAL"):
+        a.assemble_to_host(items(w), nwin=3)
+    out, _ = a.assemble_to_host(items(w), nwin=2)
+    a.close()
+    assert np.array_equal(out, full(w, SPLIT_BF16)[0])
