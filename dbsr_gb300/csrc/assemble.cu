@@ -20,6 +20,7 @@
 //      (atype-major, then list order), so no atomics are needed and the
 //      result is deterministic.
 #include "internal.cuh"
+#include "ff.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -69,6 +70,12 @@ __global__ void k_segments(int n, const int *k1, int *seg_start, int *nseg_out) 
     seg_start[cnt[tid]] = n;
     *nseg_out = cnt[tid];
   }
+}
+
+// the coefficients as float-float pairs (split form gather-sums)
+__global__ void k_cd_ff(int n, const double *cd, float2 *cdf) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < n) cdf[e] = ffa::split(cd[e]);
 }
 
 // bound-orbital indices of every entry must address pq(:,:,1:nbf)
@@ -580,6 +587,7 @@ struct ListPlan {
   int ttype[4] = {0, 1, 2, 3};
   int *lk1 = nullptr, *lk2 = nullptr, *lk3 = nullptr, *lpair = nullptr;
   double *lcd = nullptr;
+  float2 *lcdf = nullptr;  // the coefficients as float-float pairs
   SegInfo *info = nullptr;
   int *work = nullptr;   // chunk members and owner slots | acf owners
   XQuad *dxq = nullptr;  // quadrant records
@@ -598,7 +606,7 @@ size_t plan_bytes(const dbsrg_ctx *c, int icase, int n) {
   const size_t ib = sizeof(int) * (size_t)n, db = sizeof(double) * (size_t)n;
   size_t t = 8 * al256(ib) + 2 * al256(db) + al256(sizeof(int) * (n + 2)) + al256(64) +
              al256(sizeof(SegInfo) * (size_t)(n + 1)) + al256(sizeof(int) * (size_t)(7 * (n + 1))) +
-             al256(sizeof(XQuad) * 4 * (size_t)(n + 1));
+             al256(sizeof(XQuad) * 4 * (size_t)(n + 1)) + al256(sizeof(float2) * (size_t)n);
   if (icase == 0)
     t += al256(sizeof(double) * (size_t)c->g.ms * c->nbf) +
          al256(sizeof(int) * (2 * (size_t)(c->iicc + 2) + n));
@@ -643,6 +651,7 @@ int plan_list(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const int *ip
   // segment), then the acf owners (one per segment)
   P.work = (int *)take(sizeof(int) * (size_t)(7 * (n + 1)));
   P.dxq = (XQuad *)take(sizeof(XQuad) * 4 * (size_t)(n + 1));
+  P.lcdf = (float2 *)take(sizeof(float2) * (size_t)n);
   if ((rc = copy_in_s(c, dk1, k1, ibytes, ss))) return rc;
   if ((rc = copy_in_s(c, dk2, k2, ibytes, ss))) return rc;
   if ((rc = copy_in_s(c, dk3, k3, ibytes, ss))) return rc;
@@ -652,6 +661,8 @@ int plan_list(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const int *ip
   DBSRG_RUN_S(c, ss, "k_gather",
               k_gather<<<(n + 255) / 256, 256, 0, ss>>>(n, ipt ? dipt : nullptr, dk1, dk2, dk3,
                                                         dcd, P.lk1, P.lk2, P.lk3, P.lcd));
+  DBSRG_RUN_S(c, ss, "k_cd_ff",
+              k_cd_ff<<<(n + 255) / 256, 256, 0, ss>>>(n, P.lcd, P.lcdf));
 
   // ---- overlaps: entries grouped by block on the host (counting sort, list
   // order kept within a block); entries below eps_c are dropped
@@ -945,6 +956,7 @@ int exec_list(dbsrg_ctx *c, const ListPlan &P, int w) {
       job.k3 = P.lk3;
       job.pairs = P.lpair;
       job.cd = P.lcd;
+      job.cdf = P.lcdf;
       job.Y = Y;
       job.split = c->precision == DBSRG_SPLIT_BF16;
       job.xq = ch.nxq ? P.dxq + ch.xoff : nullptr;

@@ -32,6 +32,7 @@
 // returns.
 #include "internal.cuh"
 #include "tc_common.cuh"
+#include "ff.cuh"
 
 namespace {
 
@@ -88,11 +89,11 @@ __global__ void k_udigits(int ns, int nb, int NR, const double *U, __nv_bfloat16
 
 struct ZArgs {
   int ns, nb, NR, nm, lower;
-  const double *V[4], *Vl[4], *Kb[4];
+  const float2 *V[4], *Vl[4], *Kb[4];  // float-float copies
   const int *members;
   const SegInfo *info;
   const int *pairs;
-  const double *cd;
+  const float2 *cd;
   __nv_bfloat16 *Zd;  // [a][mode][slot][slice][NR][TILE]
   int *ez;            // [a][mode][slot][NR*33]
   double *Yb;         // [a][slot][ns*17]
@@ -101,45 +102,55 @@ struct ZArgs {
 // Per segment slot and atype, one thread per row y (ZROWS rows a block):
 //   Z_s(k,y) = sum_{e in s, first orbital k} c_e V(y, second orbital)  (Zl with Vl)
 //   Yb_s(y,d) = sum_e c_e Kb(pair_e; y, d)                             (near band)
-// then the digits of Z (and Zl) and their row exponents.
+// as float-float sums (ff.cuh), then the digits of Z (and Zl) and their row
+// exponents.
 constexpr int ZROWS = 64;
 __global__ void __launch_bounds__(ZROWS) k_zdigits(const ZArgs z) {
-  extern __shared__ double zs[];  // [2][32][ZROWS]: per thread one column
+  extern __shared__ float2 zs[];  // [2][32][ZROWS] float-float: per thread one column
   const int t = threadIdx.x, y = blockIdx.x * ZROWS + t, slot = blockIdx.y, a = blockIdx.z;
   const int ns = z.ns, nb = z.nb;
-  double *z0 = zs, *z1 = zs + 32 * ZROWS;
+  float2 *z0 = zs, *z1 = zs + 32 * ZROWS;
   for (int k = 0; k < 32; k++) {
-    z0[k * ZROWS + t] = 0.0;
-    z1[k * ZROWS + t] = 0.0;
+    z0[k * ZROWS + t] = make_float2(0.0f, 0.0f);
+    z1[k * ZROWS + t] = make_float2(0.0f, 0.0f);
   }
   const SegInfo si = z.info[z.members[slot]];
-  const double *V = z.V[a], *Vl = z.lower ? z.Vl[a] : nullptr, *Kb = z.Kb[a];
+  const float2 *V = z.V[a], *Vl = z.lower ? z.Vl[a] : nullptr, *Kb = z.Kb[a];
   const size_t kper = (size_t)ns * NDB;
-  double band[NDB];
+  float bh[NDB], bl[NDB];
 #pragma unroll
-  for (int d = 0; d < NDB; d++) band[d] = 0.0;
+  for (int d = 0; d < NDB; d++) bh[d] = bl[d] = 0.0f;
   if (y < ns) {
     for (int e = si.start; e < si.end; e++) {
       const int pr = z.pairs[e], oa = pr / nb, ob = pr - oa * nb;
-      const double c = z.cd[e];
-      z0[oa * ZROWS + t] = fma(c, V[(size_t)y + (size_t)ns * ob], z0[oa * ZROWS + t]);
-      if (Vl) z1[oa * ZROWS + t] = fma(c, Vl[(size_t)y + (size_t)ns * ob], z1[oa * ZROWS + t]);
-      const double *kb = Kb + (size_t)pr * kper + y;
+      const float2 c = z.cd[e];
+      {
+        float2 acc = z0[oa * ZROWS + t];
+        ffa::mac(c, V[(size_t)y + (size_t)ns * ob], acc.x, acc.y);
+        z0[oa * ZROWS + t] = acc;
+      }
+      if (Vl) {
+        float2 acc = z1[oa * ZROWS + t];
+        ffa::mac(c, Vl[(size_t)y + (size_t)ns * ob], acc.x, acc.y);
+        z1[oa * ZROWS + t] = acc;
+      }
+      const float2 *kb = Kb + (size_t)pr * kper + y;
 #pragma unroll
-      for (int d = 0; d < NDB; d++) band[d] = fma(c, kb[(size_t)ns * d], band[d]);
+      for (int d = 0; d < NDB; d++) ffa::mac(c, kb[(size_t)ns * d], bh[d], bl[d]);
     }
     double *yb = z.Yb + ((size_t)a * z.nm + slot) * kper + y;
 #pragma unroll
-    for (int d = 0; d < NDB; d++) yb[(size_t)ns * d] = band[d];
+    for (int d = 0; d < NDB; d++) yb[(size_t)ns * d] = ffa::value(bh[d], bl[d]);
   }
   const size_t sl = (size_t)z.NR * TILE;
   for (int mode = 0; mode < (z.lower ? 2 : 1); mode++) {
-    const double *zz = mode ? z1 : z0;
+    const float2 *zz = mode ? z1 : z0;
     double vals[32];
     double m = 0.0;
 #pragma unroll
     for (int k = 0; k < 32; k++) {
-      vals[k] = zz[k * ZROWS + t];
+      const float2 v = zz[k * ZROWS + t];
+      vals[k] = ffa::value(v.x, v.y);
       m = fmax(m, fabs(vals[k]));
     }
     const int e = scale_exp(m);
@@ -723,20 +734,22 @@ int split_exchange(dbsrg_ctx *c, const SplitExchange &x) {
   z.NR = NR;
   z.nm = x.nm;
   z.lower = x.lower;
+  if (!x.cdf) return set_err(c, DBSRG_EINVAL, "split exchange: no float-float coefficients");
+  const size_t mv = (size_t)ns * nb, mk = (size_t)nb * nb * ns * NDB;
   for (int a = 0; a < x.na; a++) {
-    z.V[a] = x.far[a]->V;
-    z.Vl[a] = x.far[a]->Vl;
-    z.Kb[a] = x.Kb[a];
     if (x.lower && !x.far[a]->Vl) return set_err(c, DBSRG_EINVAL, "split exchange: no lower field");
+    if ((rc = ff_of(c, x.far[a]->V, mv, &z.V[a]))) return rc;
+    if (x.lower && (rc = ff_of(c, x.far[a]->Vl, mv, &z.Vl[a]))) return rc;
+    if ((rc = ff_of(c, x.Kb[a], mk, &z.Kb[a]))) return rc;
   }
   z.members = x.members;
   z.info = x.info;
   z.pairs = x.pairs;
-  z.cd = x.cd;
+  z.cd = x.cdf;
   z.Zd = Zd;
   z.ez = ez;
   z.Yb = Yb;
-  const size_t zsm = 2 * 32 * ZROWS * sizeof(double);
+  const size_t zsm = 2 * 32 * ZROWS * sizeof(float2);
   DBSRG_TRY(c, cudaFuncSetAttribute(k_zdigits, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)zsm));
   DBSRG_RUN(c, "k_zdigits",

@@ -36,6 +36,7 @@
 // products on the tensor cores, fused with the near band and the scatter
 // (exchange_tc.cu).
 #include "internal.cuh"
+#include "ff.cuh"
 
 #include <algorithm>
 
@@ -92,9 +93,11 @@ struct QuadSpec {
   int ii[4], jj[4];
 };
 
-// direct pair potentials of the atypes of one list
+// direct pair potentials of the atypes of one list (FP64, or float-float
+// pairs in the split form)
 struct KdSet {
   const double *K[4];
+  const float2 *Kf[4];
 };
 
 // ---------------------------------------------------------------------------
@@ -605,10 +608,12 @@ __device__ __forceinline__ int band_pos(int ns, int ks, char sym, int i, int j) 
 
 // Direct scatter: every band element of the four quadrants of an owner's
 // block; each contribution is formed from the pair potentials and the
-// segment's coefficients where it is added.
+// segment's coefficients where it is added (FF: as a float-float sum).
+template <bool FF>
 __global__ void k_scatter_dp(int ns, int ks, char sym, QuadSpec sp, KdSet kd,
                              const int *members, const int *own_slots, const SegInfo *info,
-                             const int *pairs, const double *cd, double *hch) {
+                             const int *pairs, const double *cd, const float2 *cdf,
+                             double *hch) {
   const int ms = 2 * ns, nd = 2 * ks - 1;
   const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= (size_t)4 * ns * nd) return;
@@ -626,9 +631,17 @@ __global__ void k_scatter_dp(int ns, int ks, char sym, QuadSpec sp, KdSet kd,
               (size_t)ms * ((qc - 1) * ns + lc);
   bool touched = false;
   double val = 0.0;
-  auto ysum = [&](const double *K, const SegInfo &sj, int i, int j) -> double {
+  auto ysum = [&](int a, const SegInfo &sj, int i, int j) -> double {
     const int p = band_pos(ns, ks, sym, i, j);
     if (p < 0) return 0.0;
+    if (FF) {
+      const float2 *K = kd.Kf[a];
+      float sh = 0.0f, sl = 0.0f;
+      for (int e = sj.start; e < sj.end; e++)
+        ffa::mac(cdf[e], K[(size_t)pairs[e] * per + p], sh, sl);
+      return ffa::value(sh, sl);
+    }
+    const double *K = kd.K[a];
     double acc = 0.0;
     for (int e = sj.start; e < sj.end; e++) acc = fma(cd[e], K[(size_t)pairs[e] * per + p], acc);
     return acc;
@@ -642,17 +655,17 @@ __global__ void k_scatter_dp(int ns, int ks, char sym, QuadSpec sp, KdSet kd,
       if (sj.ich != sj.jch) {
         if (qr == ii && qc == jj) {
           if (!touched) { val = *h; touched = true; }
-          val = val + (sj.ich > sj.jch ? ysum(kd.K[a], sj, lr + 1, lc + 1)
-                                       : ysum(kd.K[a], sj, lc + 1, lr + 1));
+          val = val + (sj.ich > sj.jch ? ysum(a, sj, lr + 1, lc + 1)
+                                       : ysum(a, sj, lc + 1, lr + 1));
         }
       } else {
         if (qr == ii && qc == jj) {
           if (!touched) { val = *h; touched = true; }
-          val = val + ysum(kd.K[a], sj, lr + 1, lc + 1) / 2.0;
+          val = val + ysum(a, sj, lr + 1, lc + 1) / 2.0;
         }
         if (qr == jj && qc == ii) {
           if (!touched) { val = *h; touched = true; }
-          val = val + ysum(kd.K[a], sj, lc + 1, lr + 1) / 2.0;
+          val = val + ysum(a, sj, lc + 1, lr + 1) / 2.0;
         }
       }
     }
@@ -866,7 +879,7 @@ static int get_pairpot_band(dbsrg_ctx *c, int family, int type, int k, int cs, i
 }
 
 void free_orbital_products(dbsrg_ctx *c) {
-  if (!c->rfar.empty() || !c->sfar.empty() || !c->ppot.empty() || c->brows)
+  if (!c->rfar.empty() || !c->sfar.empty() || !c->ppot.empty() || c->brows || !c->ffc.empty())
     cudaStreamSynchronize(c->stream);
   for (auto *v : {&c->rfar, &c->sfar})
     for (auto &kv : *v) {
@@ -880,6 +893,30 @@ void free_orbital_products(dbsrg_ctx *c) {
   c->ppot.clear();
   cache_free(c, c->brows);
   c->brows = nullptr;
+  for (auto &kv : c->ffc) cache_free(c, kv.second);
+  c->ffc.clear();
+}
+
+namespace {
+__global__ void k_to_ff(size_t n, const double *src, float2 *dst) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = ffa::split(src[i]);
+}
+}  // namespace
+
+int ff_of(dbsrg_ctx *c, const double *src, size_t n, const float2 **out) {
+  auto it = c->ffc.find(src);
+  if (it != c->ffc.end()) {
+    *out = it->second;
+    return DBSRG_OK;
+  }
+  float2 *d = (float2 *)cache_alloc(c, n * sizeof(float2));
+  if (!d) return set_err(c, DBSRG_ENOMEM, "float-float copy allocation failed");
+  c->ffc[src] = d;
+  DBSRG_RUN(c, "k_to_ff",
+            k_to_ff<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(n, src, d));
+  *out = d;
+  return DBSRG_OK;
 }
 
 int factored_contract(dbsrg_ctx *c, const FactorJob &j) {
@@ -920,6 +957,7 @@ int factored_contract(dbsrg_ctx *c, const FactorJob &j) {
     x.info = j.info;
     x.pairs = j.pairs;
     x.cd = j.cd;
+    x.cdf = j.cdf;
     return split_exchange(c, x);
   }
   if (j.icv >= 3) {
@@ -961,15 +999,24 @@ int factored_contract(dbsrg_ctx *c, const FactorJob &j) {
   }
   // direct
   KdSet kd{};
+  const size_t perd = (size_t)ns * (j.sym == 's' ? ks : 2 * ks - 1);
   for (int a = 0; a < j.na; a++) {
     if ((rc = get_pairpot_direct(c, j.family, j.types[a], j.kpol, j.icv, j.jp1[a], j.jp2[a],
                                  &kd.K[a])))
       return rc;
+    if (j.split && j.cdf &&
+        (rc = ff_of(c, kd.K[a], (size_t)nb * nb * perd, &kd.Kf[a])))
+      return rc;
   }
   const size_t space = (size_t)4 * ns * (2 * ks - 1);
   dim3 gs((unsigned)((space + 255) / 256), (unsigned)j.nown);
-  DBSRG_RUN(c, "k_scatter_dp",
-            k_scatter_dp<<<gs, 256, 0, st>>>(ns, ks, j.sym, qs, kd, j.members, j.own, j.info,
-                                             j.pairs, j.cd, hch_base(c)));
+  if (j.split && j.cdf)
+    DBSRG_RUN(c, "k_scatter_dp",
+              k_scatter_dp<true><<<gs, 256, 0, st>>>(ns, ks, j.sym, qs, kd, j.members, j.own,
+                                                     j.info, j.pairs, j.cd, j.cdf, hch_base(c)));
+  else
+    DBSRG_RUN(c, "k_scatter_dp",
+              k_scatter_dp<false><<<gs, 256, 0, st>>>(ns, ks, j.sym, qs, kd, j.members, j.own,
+                                                      j.info, j.pairs, j.cd, j.cdf, hch_base(c)));
   return DBSRG_OK;
 }

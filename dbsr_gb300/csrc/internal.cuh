@@ -95,6 +95,10 @@ struct dbsrg_ctx {
   // and exchange band results per ordered bound-orbital pair), keyed by
   // pairpot_key(); they depend on the tables and the orbitals
   std::map<long long, double *> ppot;
+  // float-float copies (hi, lo) of orbital products for the split form's
+  // gather-sums, keyed by the FP64 array they copy; dropped with the
+  // orbital products
+  std::map<const void *, float2 *> ffc;
   // bound-orbital rows brows[(comp-1)*nbound*ns + a*ns + x] = pq(x+1, comp, b2o[a])
   double *brows = nullptr;
   // bound-orbital map: bmap[orb-1] = dense bound index or -1; nbound
@@ -247,6 +251,8 @@ int ensure_pinned(dbsrg_ctx *c, size_t bytes);
 // frees the far-field vectors, pair potentials and bound rows (they depend
 // on the orbitals and the tables)
 void free_orbital_products(dbsrg_ctx *c);
+// float-float copy of n doubles at src (cached until the orbital products go)
+int ff_of(dbsrg_ctx *c, const double *src, size_t n, const float2 **out);
 
 // ---- tables.cu ------------------------------------------------------------
 int build_grid(dbsrg_ctx *c, const double *t_host_or_dev);
@@ -296,6 +302,7 @@ struct FactorJob {
   const int *k2, *k3;
   const int *pairs;  // ordered bound-orbital pair index of every entry
   const double *cd;
+  const float2 *cdf;  // split form: the coefficients as float-float pairs
   double *Y;         // exchange results [a][slot][ns*ns] (FP64 far field)
   bool split;        // exchange on the tensor cores (split BF16), fused scatter
   int nxq;           // split exchange: (owner block, quadrant) records of the chunk
@@ -329,6 +336,7 @@ struct SplitExchange {
   const SegInfo *info;
   const int *pairs;
   const double *cd;
+  const float2 *cdf;  // the coefficients as float-float pairs
 };
 int split_exchange(dbsrg_ctx *c, const SplitExchange &x);
 // Direct pair potentials of table (family, type, k) for convol case icv with
