@@ -735,12 +735,12 @@ int split_exchange(dbsrg_ctx *c, const SplitExchange &x) {
   z.nm = x.nm;
   z.lower = x.lower;
   if (!x.cdf) return set_err(c, DBSRG_EINVAL, "split exchange: no float-float coefficients");
-  const size_t mv = (size_t)ns * nb, mk = (size_t)nb * nb * ns * NDB;
+  const size_t mv = (size_t)ns * nb;
   for (int a = 0; a < x.na; a++) {
     if (x.lower && !x.far[a]->Vl) return set_err(c, DBSRG_EINVAL, "split exchange: no lower field");
     if ((rc = ff_of(c, x.far[a]->V, mv, &z.V[a]))) return rc;
     if (x.lower && (rc = ff_of(c, x.far[a]->Vl, mv, &z.Vl[a]))) return rc;
-    if ((rc = ff_of(c, x.Kb[a], mk, &z.Kb[a]))) return rc;
+    z.Kb[a] = x.Kbf[a];
   }
   z.members = x.members;
   z.info = x.info;

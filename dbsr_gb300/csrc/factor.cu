@@ -39,6 +39,7 @@
 #include "ff.cuh"
 
 #include <algorithm>
+#include <type_traits>
 
 namespace {
 
@@ -236,40 +237,48 @@ __global__ void __launch_bounds__(256) k_far_field(int ns, int nb, const double 
 //   Kb(ab; x, y) = sum_i P1(a, i) H(x; i, b)
 // mode 0: R table 's','s' case 3; 1: S 'n','n' case 3; 2: S 'n','n' case 4.
 // Band table layout: rkb(i, j-i+BW+1, ip, jp) for |j - i| <= BW.
+// FF: the windows split once into float-float pairs, both stages as
+// float-float sums (ff.cuh), Kb written as float-float pairs (float2).
+template <bool FF>
 __global__ void __launch_bounds__(256) k_pair_band(int ns, int ks, int nb, int mode,
                                                    const double *__restrict__ rkb,
                                                    const double *__restrict__ P1,
                                                    const double *__restrict__ P2,
-                                                   double *__restrict__ Kb) {
-  extern __shared__ double sm[];
+                                                   void *__restrict__ Kout) {
+  using S = typename std::conditional<FF, float2, double>::type;
+  extern __shared__ double smraw[];
+  S *sm = reinterpret_cast<S *>(smraw);
   const int W = 2 * ks - 1;            // offsets -(ks-1) .. ks-1
   const int WL = PXC + W - 1;          // window of the row vectors
   const int x0 = blockIdx.x * PXC + 1; // first output row (1-based)
   const int d = (int)blockIdx.y - BAND;
-  double *Wm = sm;                     // [PXC][W][W]
-  double *p1w = Wm + PXC * W * W;      // [nb][WL]: P1(a, x0-(ks-1)+t)
-  double *p2w = p1w + nb * WL;         // [nb][WL]: P2(b, x0+d-(ks-1)+t)
-  double *H = p2w + nb * WL;           // [PXC][W][nb]
+  S *Wm = sm;                          // [PXC][W][W]
+  S *p1w = Wm + PXC * W * W;           // [nb][WL]: P1(a, x0-(ks-1)+t)
+  S *p2w = p1w + nb * WL;              // [nb][WL]: P2(b, x0+d-(ks-1)+t)
+  S *H = p2w + nb * WL;                // [PXC][W][nb]
+  auto sv = [](double v) -> S {
+    if constexpr (FF) return ffa::split(v); else return v;
+  };
   const int kb = mode == 0 ? ks : 2 * ks - 1;
   constexpr int BW = DBSRG_TABLE_BAND, NJ = 2 * DBSRG_TABLE_BAND + 1;
   auto TB = [&](int i, int j, int ip, int jp) -> double {
     return rkb[(size_t)(i - 1) + (size_t)ns * ((size_t)(j - i + BW) +
                (size_t)NJ * ((size_t)(ip - 1) + (size_t)kb * (size_t)(jp - 1)))];
   };
-  for (int q = threadIdx.x; q < PXC * W * W; q += blockDim.x) Wm[q] = 0.0;
+  for (int q = threadIdx.x; q < PXC * W * W; q += blockDim.x) Wm[q] = sv(0.0);
   for (int q = threadIdx.x; q < nb * WL; q += blockDim.x) {
     const int a = q / WL, t = q % WL;
     const int xi = x0 - (ks - 1) + t, yi = x0 + d - (ks - 1) + t;
-    p1w[q] = (xi >= 1 && xi <= ns) ? P1[(size_t)a * ns + xi - 1] : 0.0;
-    p2w[q] = (yi >= 1 && yi <= ns) ? P2[(size_t)a * ns + yi - 1] : 0.0;
+    p1w[q] = sv((xi >= 1 && xi <= ns) ? P1[(size_t)a * ns + xi - 1] : 0.0);
+    p2w[q] = sv((yi >= 1 && yi <= ns) ? P2[(size_t)a * ns + yi - 1] : 0.0);
   }
   __syncthreads();
   for (int q = threadIdx.x; q < PXC * kb * kb; q += blockDim.x) {
     const int xl = q / (kb * kb), r = q % (kb * kb), ip = r % kb + 1, jp = r / kb + 1;
     const int x = x0 + xl, y = x + d;
     if (x > ns || y < 1 || y > ns) continue;
-    double *w = Wm + (size_t)xl * W * W;
-    auto put = [&](int i, int j, double v) { w[(i - x + ks - 1) * W + (j - y + ks - 1)] = v; };
+    S *w = Wm + (size_t)xl * W * W;
+    auto put = [&](int i, int j, double v) { w[(i - x + ks - 1) * W + (j - y + ks - 1)] = sv(v); };
     if (mode == 0) {
       if (y - jp + 1 >= 1 && x + ip - 1 <= ns)
         put(x + ip - 1, y - jp + 1, TB(x, y - jp + 1, ip, jp));
@@ -294,11 +303,17 @@ __global__ void __launch_bounds__(256) k_pair_band(int ns, int ks, int nb, int m
   __syncthreads();
   for (int q = threadIdx.x; q < PXC * W * nb; q += blockDim.x) {
     const int b = q % nb, r = q / nb, u = r % W, xl = r / W;
-    const double *w = Wm + ((size_t)xl * W + u) * W;
-    const double *p = p2w + (size_t)b * WL + xl;
-    double s = 0.0;
-    for (int v = 0; v < W; v++) s = fma(w[v], p[v], s);
-    H[q] = s;
+    const S *w = Wm + ((size_t)xl * W + u) * W;
+    const S *p = p2w + (size_t)b * WL + xl;
+    if constexpr (FF) {
+      float sh = 0.0f, sl = 0.0f;
+      for (int v = 0; v < W; v++) ffa::mac(w[v], p[v], sh, sl);
+      H[q] = ffa::norm(sh, sl);
+    } else {
+      double s = 0.0;
+      for (int v = 0; v < W; v++) s = fma(w[v], p[v], s);
+      H[q] = s;
+    }
   }
   __syncthreads();
   const size_t per = (size_t)ns * NDB;
@@ -306,11 +321,18 @@ __global__ void __launch_bounds__(256) k_pair_band(int ns, int ks, int nb, int m
     const int xl = q % PXC, pr = q / PXC, b = pr % nb, a = pr / nb;
     const int x = x0 + xl, y = x + d;
     if (x > ns || y < 1 || y > ns) continue;
-    const double *p = p1w + (size_t)a * WL + xl;
-    const double *h = H + (size_t)xl * W * nb + b;
-    double s = 0.0;
-    for (int u = 0; u < W; u++) s = fma(p[u], h[(size_t)u * nb], s);
-    Kb[(size_t)pr * per + (size_t)(x - 1) + (size_t)ns * (d + BAND)] = s;
+    const S *p = p1w + (size_t)a * WL + xl;
+    const S *h = H + (size_t)xl * W * nb + b;
+    const size_t o = (size_t)pr * per + (size_t)(x - 1) + (size_t)ns * (d + BAND);
+    if constexpr (FF) {
+      float sh = 0.0f, sl = 0.0f;
+      for (int u = 0; u < W; u++) ffa::mac(p[u], h[(size_t)u * nb], sh, sl);
+      static_cast<float2 *>(Kout)[o] = ffa::norm(sh, sl);
+    } else {
+      double s = 0.0;
+      for (int u = 0; u < W; u++) s = fma(p[u], h[(size_t)u * nb], s);
+      static_cast<double *>(Kout)[o] = s;
+    }
   }
 }
 
@@ -403,26 +425,32 @@ __global__ void k_pair_scan(int nv, int npair, double *S, int suffix) {
 // and ph = (cv-1) mod 9: a cell touches outputs with first index in
 // [cv, cv+8], so cells of one phase never share an output.  Two stages:
 // H(po, g1, b) = sum_g2 R P2, then sum_g1 P1 H.
+template <bool FF>
 __global__ void __launch_bounds__(256) k_pair_diag(int ns, int ks, int kk, int nb, int icv,
                                                    char sym, PairSpec eo, PairSpec ed,
                                                    const double *__restrict__ rkd,
                                                    const double *__restrict__ P1,
                                                    const double *__restrict__ P2,
                                                    double *__restrict__ Dq, size_t per) {
-  extern __shared__ double sm[];
+  using S = typename std::conditional<FF, float2, double>::type;
+  extern __shared__ double smraw[];
+  S *sm = reinterpret_cast<S *>(smraw);
+  auto sv = [](double v) -> S {
+    if constexpr (FF) return ffa::split(v); else return v;
+  };
   const int cv = blockIdx.x + 1, k1 = ed.k1, k2 = ed.k2, kd = k1 * k2;
   const int npo = eo.sym ? eo.k1 * (eo.k1 + 1) / 2 : eo.k1 * eo.k2;
   const size_t npair = (size_t)nb * nb;
-  double *w1 = sm, *w2 = w1 + nb * k1, *Rt = w2 + nb * k2;
-  double *H = Rt + (size_t)npo * kd;
+  S *w1 = sm, *w2 = w1 + nb * k1, *Rt = w2 + nb * k2;
+  S *H = Rt + (size_t)npo * kd;
   int *poq = (int *)(H + (size_t)npo * k1 * PBC);
   for (int q = threadIdx.x; q < nb * k1; q += blockDim.x) {
     const int a = q / k1, x = cv + q % k1;
-    w1[q] = x <= ns ? P1[(size_t)a * ns + x - 1] : 0.0;
+    w1[q] = sv(x <= ns ? P1[(size_t)a * ns + x - 1] : 0.0);
   }
   for (int q = threadIdx.x; q < nb * k2; q += blockDim.x) {
     const int b = q / k2, x = cv + q % k2;
-    w2[q] = x <= ns ? P2[(size_t)b * ns + x - 1] : 0.0;
+    w2[q] = sv(x <= ns ? P2[(size_t)b * ns + x - 1] : 0.0);
   }
   for (int po = threadIdx.x; po < npo; po += blockDim.x) {
     int h1, h2;
@@ -446,7 +474,7 @@ __global__ void __launch_bounds__(256) k_pair_diag(int ns, int ks, int kk, int n
   for (int q = threadIdx.x; q < npo * kd; q += blockDim.x) {
     const int po = q / kd, r = q % kd, g1 = r / k2 + 1, g2 = r % k2 + 1;
     const int pd = pidx(ed, g1, g2);
-    Rt[q] = icv == 1 ? rc[(size_t)po + (size_t)kk * pd] : rc[(size_t)pd + (size_t)kk * po];
+    Rt[q] = sv(icv == 1 ? rc[(size_t)po + (size_t)kk * pd] : rc[(size_t)pd + (size_t)kk * po]);
   }
   __syncthreads();
   const int ph = (cv - 1) % FAR;
@@ -454,21 +482,34 @@ __global__ void __launch_bounds__(256) k_pair_diag(int ns, int ks, int kk, int n
     const int bc = min(PBC, nb - b0);
     for (int q = threadIdx.x; q < npo * k1 * bc; q += blockDim.x) {
       const int bb = q % bc, r = q / bc, g1 = r % k1, po = r / k1;
-      const double *rt = Rt + (size_t)po * kd + (size_t)g1 * k2;
-      const double *p = w2 + (size_t)(b0 + bb) * k2;
-      double s = 0.0;
-      for (int g2 = 0; g2 < k2; g2++) s = fma(rt[g2], p[g2], s);
-      H[((size_t)po * k1 + g1) * PBC + bb] = s;
+      const S *rt = Rt + (size_t)po * kd + (size_t)g1 * k2;
+      const S *p = w2 + (size_t)(b0 + bb) * k2;
+      if constexpr (FF) {
+        float sh = 0.0f, sl = 0.0f;
+        for (int g2 = 0; g2 < k2; g2++) ffa::mac(rt[g2], p[g2], sh, sl);
+        H[((size_t)po * k1 + g1) * PBC + bb] = ffa::norm(sh, sl);
+      } else {
+        double s = 0.0;
+        for (int g2 = 0; g2 < k2; g2++) s = fma(rt[g2], p[g2], s);
+        H[((size_t)po * k1 + g1) * PBC + bb] = s;
+      }
     }
     __syncthreads();
     for (int q = threadIdx.x; q < npo * nb * bc; q += blockDim.x) {
       const int bb = q % bc, r = q / bc, a = r % nb, po = r / nb;
       const int qp = poq[po];
       if (qp < 0) continue;
-      const double *p = w1 + (size_t)a * k1;
-      const double *h = H + (size_t)po * k1 * PBC + bb;
-      double s = 0.0;
-      for (int g1 = 0; g1 < k1; g1++) s = fma(p[g1], h[(size_t)g1 * PBC], s);
+      const S *p = w1 + (size_t)a * k1;
+      const S *h = H + (size_t)po * k1 * PBC + bb;
+      double s;
+      if constexpr (FF) {
+        float sh = 0.0f, sl = 0.0f;
+        for (int g1 = 0; g1 < k1; g1++) ffa::mac(p[g1], h[(size_t)g1 * PBC], sh, sl);
+        s = ffa::value(sh, sl);
+      } else {
+        s = 0.0;
+        for (int g1 = 0; g1 < k1; g1++) s = fma(p[g1], h[(size_t)g1 * PBC], s);
+      }
       Dq[((size_t)ph * npair + (size_t)a * nb + b0 + bb) * per + qp] = s;
     }
     __syncthreads();
@@ -477,10 +518,11 @@ __global__ void __launch_bounds__(256) k_pair_diag(int ns, int ks, int kk, int n
 
 // (4) the pair potential: separable terms from the scanned cell sums plus the
 // diagonal-cell parts, cells in order (the output loop of k_direct)
+template <bool FF>
 __global__ void k_pair_direct_final(int ns, int ks, int nv, int kk, int nb, int icv, char sym,
                                     PairSpec eo, const double *lo1, const double *hi1,
                                     const double *hi2, const double *SA, const double *SB,
-                                    const double *Dq, double *K, size_t per) {
+                                    const double *Dq, void *Kout, size_t per) {
   const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= per) return;
   const int pair = blockIdx.y;
@@ -503,7 +545,10 @@ __global__ void k_pair_direct_final(int ns, int ks, int nv, int kk, int nb, int 
       acc += Dq[((size_t)((cv - 1) % FAR) * npair + pair) * per + t];
     }
   }
-  K[(size_t)pair * per + t] = acc;
+  if constexpr (FF)
+    static_cast<float2 *>(Kout)[(size_t)pair * per + t] = ffa::split(acc);
+  else
+    static_cast<double *>(Kout)[(size_t)pair * per + t] = acc;
 }
 
 // ---------------------------------------------------------------------------
@@ -768,9 +813,10 @@ static int ensure_brows(dbsrg_ctx *c) {
   return DBSRG_OK;
 }
 
-static long long pairpot_key(int kind, int family, int type, int k, int icv, int jp1, int jp2) {
+static long long pairpot_key(int kind, int family, int type, int k, int icv, int jp1, int jp2,
+                             bool ff) {
   return (long long)kind | (long long)family << 1 | (long long)type << 2 | (long long)icv << 5 |
-         (long long)jp1 << 8 | (long long)jp2 << 10 | (long long)k << 12;
+         (long long)jp1 << 8 | (long long)jp2 << 10 | (long long)ff << 12 | (long long)k << 13;
 }
 
 static int set_smem(dbsrg_ctx *c, const void *fn, size_t smem) {
@@ -784,7 +830,19 @@ static int set_smem(dbsrg_ctx *c, const void *fn, size_t smem) {
 // components jp1/jp2: Kd[pair][ns*ncol], cached
 int get_pairpot_direct(dbsrg_ctx *c, int family, int type, int k, int icv, int jp1,
                               int jp2, const double **out) {
-  const long long key = pairpot_key(0, family, type, k, icv, jp1, jp2);
+  return get_pairpot_direct_any(c, family, type, k, icv, jp1, jp2, false, (const void **)out);
+}
+
+int get_pairpot_direct_ff(dbsrg_ctx *c, int family, int type, int k, int icv, int jp1, int jp2,
+                          const float2 **out) {
+  return get_pairpot_direct_any(c, family, type, k, icv, jp1, jp2, true, (const void **)out);
+}
+
+// ff: the diagonal-cell contraction in float-float arithmetic and the result
+// stored as float-float pairs (the split form's gather-sums read those)
+int get_pairpot_direct_any(dbsrg_ctx *c, int family, int type, int k, int icv, int jp1,
+                           int jp2, bool ff, const void **out) {
+  const long long key = pairpot_key(0, family, type, k, icv, jp1, jp2, ff);
   auto it = c->ppot.find(key);
   if (it != c->ppot.end()) {
     *out = it->second;
@@ -809,7 +867,7 @@ int get_pairpot_direct(dbsrg_ctx *c, int family, int type, int k, int icv, int j
   const size_t sbytes = (2 * npair * nv + (size_t)FAR * npair * per) * sizeof(double);
   if ((rc = ensure_pscratch(c, sbytes))) return rc;
   double *SA = (double *)c->pscratch, *SB = SA + npair * nv, *Dq = SB + npair * nv;
-  double *K = nullptr;
+  double *K = nullptr;  // doubles, or as many float2 pairs (same bytes)
   if (!(K = (double *)cache_alloc(c, npair * per * sizeof(double)))) {
     cudaGetLastError();
     return set_err(c, DBSRG_ENOMEM, "pair potential allocation failed");
@@ -827,25 +885,39 @@ int get_pairpot_direct(dbsrg_ctx *c, int family, int type, int k, int icv, int j
   const int npo = eo.sym ? eo.k1 * (eo.k1 + 1) / 2 : eo.k1 * eo.k2;
   const size_t sm3 = ((size_t)nb * (ed.k1 + ed.k2) + (size_t)npo * ed.k1 * ed.k2 +
                       (size_t)npo * ed.k1 * PBC) * sizeof(double) + (size_t)npo * sizeof(int);
-  if ((rc = set_smem(c, (const void *)k_pair_diag, sm3))) return rc;
-  DBSRG_RUN(c, "k_pair_diag",
-            k_pair_diag<<<nv, 256, sm3, st>>>(ns, ks, kk, nb, icv, sym, eo, ed, cd->rkd, P1, P2,
-                                              Dq, per));
+  const double *lo1 = icv == 1 ? cd->lo1 : nullptr;
+  const double *hi1 = (icv == 1 && family == 0) ? cd->hi1 : nullptr;
   dim3 gf((unsigned)((per + 255) / 256), (unsigned)npair);
-  DBSRG_RUN(c, "k_pair_direct_final",
-            k_pair_direct_final<<<gf, 256, 0, st>>>(
-                ns, ks, nv, kk, nb, icv, sym, eo, icv == 1 ? cd->lo1 : nullptr,
-                (icv == 1 && family == 0) ? cd->hi1 : nullptr, cd->hi2, SA, M2 ? SB : nullptr, Dq,
-                K, per));
+  if (ff) {
+    if ((rc = set_smem(c, (const void *)k_pair_diag<true>, sm3))) return rc;
+    DBSRG_RUN(c, "k_pair_diag",
+              k_pair_diag<true><<<nv, 256, sm3, st>>>(ns, ks, kk, nb, icv, sym, eo, ed, cd->rkd,
+                                                      P1, P2, Dq, per));
+    DBSRG_RUN(c, "k_pair_direct_final",
+              k_pair_direct_final<true><<<gf, 256, 0, st>>>(ns, ks, nv, kk, nb, icv, sym, eo, lo1,
+                                                            hi1, cd->hi2, SA, M2 ? SB : nullptr,
+                                                            Dq, K, per));
+  } else {
+    if ((rc = set_smem(c, (const void *)k_pair_diag<false>, sm3))) return rc;
+    DBSRG_RUN(c, "k_pair_diag",
+              k_pair_diag<false><<<nv, 256, sm3, st>>>(ns, ks, kk, nb, icv, sym, eo, ed, cd->rkd,
+                                                       P1, P2, Dq, per));
+    DBSRG_RUN(c, "k_pair_direct_final",
+              k_pair_direct_final<false><<<gf, 256, 0, st>>>(ns, ks, nv, kk, nb, icv, sym, eo,
+                                                             lo1, hi1, cd->hi2, SA,
+                                                             M2 ? SB : nullptr, Dq, K, per));
+  }
   *out = K;
   return DBSRG_OK;
 }
 
 // exchange band pair potentials of (family, type, k, case) with density
 // components jp1/jp2: Kb[pair][ns*17], cached
+// ff: both stages in float-float arithmetic, the result stored as
+// float-float pairs (float2, same bytes) for the split form's Z digits
 static int get_pairpot_band(dbsrg_ctx *c, int family, int type, int k, int cs, int jp1, int jp2,
-                            const double *tab, const double **out) {
-  const long long key = pairpot_key(1, family, type, k, cs, jp1, jp2);
+                            const double *tab, bool ff, const void **out) {
+  const long long key = pairpot_key(1, family, type, k, cs, jp1, jp2, ff);
   auto it = c->ppot.find(key);
   if (it != c->ppot.end()) {
     *out = it->second;
@@ -869,11 +941,17 @@ static int get_pairpot_band(dbsrg_ctx *c, int family, int type, int k, int cs, i
   const int W = 2 * ks - 1, WL = PXC + W - 1;
   const size_t smem = ((size_t)PXC * W * W + 2 * (size_t)nb * WL + (size_t)PXC * W * nb) *
                       sizeof(double);
-  if ((rc = set_smem(c, (const void *)k_pair_band, smem))) return rc;
   const int mode = family == 0 ? 0 : (cs == 3 ? 1 : 2);
   dim3 gb((unsigned)((ns + PXC - 1) / PXC), (unsigned)NDB);
-  DBSRG_RUN(c, "k_pair_band",
-            k_pair_band<<<gb, 256, smem, c->stream>>>(ns, ks, nb, mode, tab, P1, P2, K));
+  if (ff) {
+    if ((rc = set_smem(c, (const void *)k_pair_band<true>, smem))) return rc;
+    DBSRG_RUN(c, "k_pair_band",
+              k_pair_band<true><<<gb, 256, smem, c->stream>>>(ns, ks, nb, mode, tab, P1, P2, K));
+  } else {
+    if ((rc = set_smem(c, (const void *)k_pair_band<false>, smem))) return rc;
+    DBSRG_RUN(c, "k_pair_band",
+              k_pair_band<false><<<gb, 256, smem, c->stream>>>(ns, ks, nb, mode, tab, P1, P2, K));
+  }
   *out = K;
   return DBSRG_OK;
 }
@@ -947,7 +1025,7 @@ int factored_contract(dbsrg_ctx *c, const FactorJob &j) {
       if (c1 != j.jp1[a] || c2 != j.jp2[a])
         return set_err(c, DBSRG_EINVAL, "factored exchange: component mismatch");
       if ((rc = get_pairpot_band(c, j.family, j.types[a], j.kpol, cs, j.jp1[a], j.jp2[a],
-                                 j.tabs[a], &x.Kb[a])))
+                                 j.tabs[a], true, (const void **)&x.Kbf[a])))
         return rc;
     }
     x.members = j.members;
@@ -975,7 +1053,7 @@ int factored_contract(dbsrg_ctx *c, const FactorJob &j) {
         return set_err(c, DBSRG_EINVAL, "factored exchange: component mismatch");
       const double *Kb;
       if ((rc = get_pairpot_band(c, j.family, j.types[a], j.kpol, cs, j.jp1[a], j.jp2[a],
-                                 j.tabs[a], &Kb)))
+                                 j.tabs[a], false, (const void **)&Kb)))
         return rc;
       double *Ya = j.Y + (size_t)a * j.nm * per;
       dim3 gz((unsigned)((ns * nb + 127) / 128), (unsigned)j.nm);
@@ -1001,12 +1079,13 @@ int factored_contract(dbsrg_ctx *c, const FactorJob &j) {
   KdSet kd{};
   const size_t perd = (size_t)ns * (j.sym == 's' ? ks : 2 * ks - 1);
   for (int a = 0; a < j.na; a++) {
-    if ((rc = get_pairpot_direct(c, j.family, j.types[a], j.kpol, j.icv, j.jp1[a], j.jp2[a],
-                                 &kd.K[a])))
-      return rc;
-    if (j.split && j.cdf &&
-        (rc = ff_of(c, kd.K[a], (size_t)nb * nb * perd, &kd.Kf[a])))
-      return rc;
+    if (j.split && j.cdf)
+      rc = get_pairpot_direct_ff(c, j.family, j.types[a], j.kpol, j.icv, j.jp1[a], j.jp2[a],
+                                 &kd.Kf[a]);
+    else
+      rc = get_pairpot_direct(c, j.family, j.types[a], j.kpol, j.icv, j.jp1[a], j.jp2[a],
+                              &kd.K[a]);
+    if (rc) return rc;
   }
   const size_t space = (size_t)4 * ns * (2 * ks - 1);
   dim3 gs((unsigned)((space + 255) / 256), (unsigned)j.nown);

@@ -36,4 +36,10 @@ __device__ __forceinline__ void mac(float2 c, float2 k, float &sh, float &sl) {
 
 __device__ __forceinline__ double value(float sh, float sl) { return (double)sh + (double)sl; }
 
+// (hi, lo) renormalised so that lo is below half an ulp of hi (Fast2Sum)
+__device__ __forceinline__ float2 norm(float sh, float sl) {
+  const float s = sh + sl;
+  return make_float2(s, sl - (s - sh));
+}
+
 }  // namespace ffa

@@ -329,7 +329,7 @@ bool build_xquads(int na, const int *ii, const int *jj, const std::vector<int> &
 struct SplitExchange {
   int na, nm, lower;
   const FarField *far[4];  // far-field vectors (and digit caches) per atype
-  const double *Kb[4];     // band pair potentials per atype
+  const float2 *Kbf[4];    // band pair potentials per atype (float-float)
   const int *members;
   const XQuad *xq, *hxq;  // device records and their host copy
   int nxq;
@@ -344,6 +344,12 @@ int split_exchange(dbsrg_ctx *c, const SplitExchange &x);
 // pairs (pair = a*nbound + b), cached until release_tables/set_orbitals.
 int get_pairpot_direct(dbsrg_ctx *c, int family, int type, int k, int icv, int jp1, int jp2,
                        const double **out);
+// the same potentials as float-float pairs, the diagonal cells contracted in
+// float-float arithmetic (the split form's direct sums)
+int get_pairpot_direct_ff(dbsrg_ctx *c, int family, int type, int k, int icv, int jp1, int jp2,
+                          const float2 **out);
+int get_pairpot_direct_any(dbsrg_ctx *c, int family, int type, int k, int icv, int jp1, int jp2,
+                           bool ff, const void **out);
 // pairs[e] = bmap[K2]*nbound + bmap[K3]; sets *derr when an orbital is not bound
 int pair_index(dbsrg_ctx *c, int n, const int *k2, const int *k3, int *pairs, int *derr,
                cudaStream_t s);
