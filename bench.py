@@ -605,14 +605,14 @@ def main():
             hl.append((L.icase, L.itype, L.kpol, *[x.numpy() for x in t], c.numpy()))
         hout = torch.empty(w.iicc * a.ms * a.ms, dtype=torch.float64).pin_memory()
         hacf = torch.empty(w.iicc * (w.mk + 1), dtype=torch.float64).pin_memory()
-        nwin = (w.iicc + 7) // 8
+        nwin = (w.iicc + a.get_tuning("windows") - 1) // a.get_tuning("windows")
 
         def e2e_step():
             # dbsrg_assemble_to_host: lists from pinned host memory, the matrix
             # window by window into pinned host memory, each window's copy
             # overlapped with the next window's assembly
             a.invalidate_tables()
-            a.assemble_to_host(hl, out=hout, acf=hacf, nwin=nwin)
+            a.assemble_to_host(hl, out=hout, acf=hacf)  # windows: the tuned count
 
         e2e_step()
         dte = timed(e2e_step, 2)

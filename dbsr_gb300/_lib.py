@@ -53,6 +53,8 @@ SIGNATURES = [
     ("dbsrg_kernel_launches", C.c_longlong, [_vp]),
     ("dbsrg_sync", C.c_int, [_vp]),
     ("dbsrg_set_async", C.c_int, [_vp, C.c_int]),
+    ("dbsrg_set_tuning", C.c_int, [_vp, C.c_char_p, C.c_int]),
+    ("dbsrg_get_tuning", C.c_int, [_vp, C.c_char_p, _ip]),
     ("dbsrg_alloc_matrix_window", C.c_int, [_vp, C.c_int, _vp, C.c_int, C.c_int, C.c_int]),
     ("dbsrg_set_window", C.c_int, [_vp, C.c_int]),
     ("dbsrg_window_blocks", C.c_int, [_vp]),

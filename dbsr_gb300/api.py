@@ -49,7 +49,11 @@ def _ptr(a, dtype):
 
 
 class Assembler:
-    def __init__(self, t, ks: int = 9, ksp: int = 8, ksq: int = 9, device: int = 0):
+    def __init__(self, t, ks: int = 9, ksp: int = 8, ksq: int = 9, device: int = 0,
+                 tuning: str | dict | None = "auto"):
+        """tuning: "auto" applies the autotuned parameters recorded for this
+        GPU and grid size (dbsr_gb300/tuning.json, written by autotune.py), a
+        dict sets them explicitly, None keeps the library defaults."""
         L = load()
         t = np.ascontiguousarray(t, dtype=np.float64)
         self.ks, self.ksp, self.ksq = ks, ksp, ksq
@@ -66,6 +70,12 @@ class Assembler:
         self.iicc = 0
         self.mk = -1
         self.nbf = 0
+        if tuning == "auto":
+            from . import autotune
+
+            tuning = autotune.lookup(self.ns, device)
+        for name, value in (tuning or {}).items():
+            self.set_tuning(name, int(value))
 
     def close(self):
         if getattr(self, "_h", None):
@@ -272,6 +282,17 @@ class Assembler:
     def sync(self):
         """Wait for the queued kernels; raises on a failure of any of them."""
         check(self._h, self._L.dbsrg_sync(self._h), "sync")
+
+    def set_tuning(self, name: str, value: int):
+        """dbsrg_set_tuning: "xchunk", "dchunk" or "windows"."""
+        check(self._h, self._L.dbsrg_set_tuning(self._h, name.encode(), int(value)),
+              f"set_tuning({name})")
+
+    def get_tuning(self, name: str) -> int:
+        v = C.c_int(0)
+        check(self._h, self._L.dbsrg_get_tuning(self._h, name.encode(), C.byref(v)),
+              f"get_tuning({name})")
+        return int(v.value)
 
     def set_async(self, enable: bool = True):
         """Asynchronous mode: gen() returns once the list's kernels are

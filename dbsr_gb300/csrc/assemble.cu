@@ -28,7 +28,7 @@
 
 namespace {
 
-constexpr int kSegChunk = 256;  // segments per contraction/scatter pass
+constexpr int kSegChunk = 256;  // segments per pass of the plain contraction
 
 
 // ---------------------------------------------------------------------------
@@ -830,7 +830,7 @@ int plan_list(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const int *ip
     const int w = wof(hinfo[s].blk);
     if (w >= 0) wseg[w].push_back(s);
   }
-  const int chunk = (P.factored && P.icv <= 2) ? 16 * kSegChunk : kSegChunk;
+  const int chunk = !P.factored ? kSegChunk : (P.icv <= 2 ? c->tune_dchunk : c->tune_xchunk);
   std::vector<int> hbuf;
   bool xq_ok = true;
   P.wchunk.assign(nw + 1, 0);

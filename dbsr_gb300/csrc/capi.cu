@@ -399,6 +399,33 @@ int dbsrg_sync(dbsrg_ctx *c) {
   return drain(c);
 }
 
+int dbsrg_set_tuning(dbsrg_ctx *c, const char *name, int value) {
+  if (!c || !name) return DBSRG_EINVAL;
+  SETTLE(c);
+  if (!strcmp(name, "xchunk")) {
+    if (value < 2 || value > 4096) return set_err(c, DBSRG_ERANGE, "xchunk: 2..4096");
+    c->tune_xchunk = value;
+  } else if (!strcmp(name, "dchunk")) {
+    if (value < 2 || value > 65535) return set_err(c, DBSRG_ERANGE, "dchunk: 2..65535");
+    c->tune_dchunk = value;
+  } else if (!strcmp(name, "windows")) {
+    if (value < 1 || value > 1024) return set_err(c, DBSRG_ERANGE, "windows: 1..1024");
+    c->tune_windows = value;
+  } else {
+    return set_err(c, DBSRG_EINVAL, "unknown tuning parameter");
+  }
+  return DBSRG_OK;
+}
+
+int dbsrg_get_tuning(const dbsrg_ctx *c, const char *name, int *value) {
+  if (!c || !name || !value) return DBSRG_EINVAL;
+  if (!strcmp(name, "xchunk")) *value = c->tune_xchunk;
+  else if (!strcmp(name, "dchunk")) *value = c->tune_dchunk;
+  else if (!strcmp(name, "windows")) *value = c->tune_windows;
+  else return DBSRG_EINVAL;
+  return DBSRG_OK;
+}
+
 int dbsrg_set_async(dbsrg_ctx *c, int enable) {
   if (!c) return DBSRG_EINVAL;
   cudaSetDevice(c->device);
@@ -636,7 +663,7 @@ int dbsrg_assemble_to_host(dbsrg_ctx *c, int nlists, const dbsrg_list *lists, in
   cudaSetDevice(c->device);
   SETTLE(c);
   const int iicc = c->iicc;
-  if (nwin <= 0) nwin = std::max(1, (iicc + 7) / 8);
+  if (nwin <= 0) nwin = std::max(1, (iicc + c->tune_windows - 1) / c->tune_windows);
   nwin = std::min(nwin, iicc);
   const int nslot = nwin < iicc ? 2 : 1;
   if (nslot * nwin > c->hcap)

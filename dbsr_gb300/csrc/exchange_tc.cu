@@ -45,24 +45,28 @@ constexpr uint32_t B_BYTES = TILE * 2;          // one slice of a 32-row operand
 constexpr int MAXT = 4;                         // terms per tile
 constexpr unsigned long long WAIT_NS = 2000000000ull;
 
-// digits of one 32-wide row (values vals[0..31], row exponent e) into a
-// digit operand laid out [slice][32-row tile][TILE]
+// digits of 8 values (columns 8kg .. 8kg+7 of a 32-wide row, row exponent
+// e) into a digit operand laid out [slice][32-row tile][TILE]
+__device__ __forceinline__ void write_digit_group(__nv_bfloat16 *D, int NR, int row, int kg,
+                                                  const double *vals8, int e) {
+  const int rt = row >> 5, r = row & 31;
+  float d[8][TS];
+#pragma unroll
+  for (int t = 0; t < 8; t++) digits(vals8[t], e, d[t]);
+#pragma unroll
+  for (int i = 0; i < TS; i++) {
+    __align__(16) __nv_bfloat16 h[8];
+#pragma unroll
+    for (int t = 0; t < 8; t++) h[t] = __float2bfloat16_rn(d[t][i]);
+    *(uint4 *)(D + ((size_t)i * NR + rt) * TILE + core_off(r, 8 * kg)) = *(const uint4 *)h;
+  }
+}
+
+// digits of one 32-wide row (values vals[0..31], row exponent e)
 __device__ __forceinline__ void write_digit_row(__nv_bfloat16 *D, int NR, int row,
                                                 const double *vals, int e) {
-  const int rt = row >> 5, r = row & 31;
 #pragma unroll
-  for (int kg = 0; kg < 4; kg++) {
-    float d[8][TS];
-#pragma unroll
-    for (int t = 0; t < 8; t++) digits(vals[8 * kg + t], e, d[t]);
-#pragma unroll
-    for (int i = 0; i < TS; i++) {
-      __align__(16) __nv_bfloat16 h[8];
-#pragma unroll
-      for (int t = 0; t < 8; t++) h[t] = __float2bfloat16_rn(d[t][i]);
-      *(uint4 *)(D + ((size_t)i * NR + rt) * TILE + core_off(r, 8 * kg)) = *(const uint4 *)h;
-    }
-  }
+  for (int kg = 0; kg < 4; kg++) write_digit_group(D, NR, row, kg, vals + 8 * kg, e);
 }
 
 // exponents of one digit operand: NR*32 row exponents, then the NR maxima
@@ -103,7 +107,8 @@ struct ZArgs {
 //   Z_s(k,y) = sum_{e in s, first orbital k} c_e V(y, second orbital)  (Zl with Vl)
 //   Yb_s(y,d) = sum_e c_e Kb(pair_e; y, d)                             (near band)
 // as float-float sums (ff.cuh), then the digits of Z (and Zl) and their row
-// exponents.
+// exponents.  The sums read the pair potentials of every entry: the kernel
+// is bound by those reads (L2 and HBM), not by its arithmetic.
 constexpr int ZROWS = 64;
 __global__ void __launch_bounds__(ZROWS) k_zdigits(const ZArgs z) {
   extern __shared__ float2 zs[];  // [2][32][ZROWS] float-float: per thread one column
@@ -145,20 +150,26 @@ __global__ void __launch_bounds__(ZROWS) k_zdigits(const ZArgs z) {
   const size_t sl = (size_t)z.NR * TILE;
   for (int mode = 0; mode < (z.lower ? 2 : 1); mode++) {
     const float2 *zz = mode ? z1 : z0;
-    double vals[32];
     double m = 0.0;
-#pragma unroll
     for (int k = 0; k < 32; k++) {
       const float2 v = zz[k * ZROWS + t];
-      vals[k] = ffa::value(v.x, v.y);
-      m = fmax(m, fabs(vals[k]));
+      m = fmax(m, fabs(ffa::value(v.x, v.y)));
     }
     const int e = scale_exp(m);
     const size_t op = (size_t)(a * 2 + mode) * z.nm + slot;
     z.ez[op * z.NR * EXP_PER_ROWTILE + y] = e;
     const int et = __reduce_max_sync(0xffffffffu, e);  // a warp is one 32-row tile
     if ((t & 31) == 0) z.ez[op * z.NR * EXP_PER_ROWTILE + z.NR * 32 + y / 32] = et;
-    write_digit_row(z.Zd + op * TS * sl, z.NR, y, vals, e);
+    // the digits 8 columns at a time, re-read from shared memory
+    for (int kg = 0; kg < 4; kg++) {
+      double vals[8];
+#pragma unroll
+      for (int u = 0; u < 8; u++) {
+        const float2 v = zz[(8 * kg + u) * ZROWS + t];
+        vals[u] = ffa::value(v.x, v.y);
+      }
+      write_digit_group(z.Zd + op * TS * sl, z.NR, y, kg, vals, e);
+    }
   }
 }
 

@@ -138,6 +138,9 @@ struct dbsrg_ctx {
   // waits (dbsrg_sync, the read-outs, state changes)
   bool async = false;
   bool pending = false;
+  // tuning (dbsrg_set_tuning): segments per chunk of the factored exchange
+  // and direct contractions, windows of dbsrg_assemble_to_host
+  int tune_xchunk = 256, tune_dchunk = 4096, tune_windows = 8;
   // block window: hch holds blocks wlo .. wlo + wcap - 1 of 1 .. iicc (all
   // of them unless dbsrg_alloc_matrix_window asked for fewer); Gen_matrix
   // skips the segments of blocks outside the window

@@ -230,6 +230,17 @@ long long dbsrg_kernel_launches(const dbsrg_ctx *ctx);
  * of them (DBSRG_ETIMEOUT: a bounded wait of a tensor-core kernel ran out). */
 int dbsrg_sync(dbsrg_ctx *ctx);
 
+/* Tuning parameters (no reference counterpart), picked per device and grid
+ * size by dbsr_gb300/autotune.py:
+ *   "xchunk"  segments per pass of the factored exchange (default 256; the
+ *             batch of the Z-digit and tensor-core exchange kernels)
+ *   "dchunk"  segments per pass of the factored direct contraction (4096)
+ *   "windows" windows of dbsrg_assemble_to_host when nwin <= 0 (8)
+ * Results do not depend on them (every block sums the same terms in the
+ * same order). */
+int dbsrg_set_tuning(dbsrg_ctx *ctx, const char *name, int value);
+int dbsrg_get_tuning(const dbsrg_ctx *ctx, const char *name, int *value);
+
 /* Asynchronous mode (off by default; no reference counterpart -- Gen_matrix
  * returns with the matrix updated, gen_matrix.f90:2-17).  When on,
  * dbsrg_gen_matrix returns once the list's kernels are queued: the host-side

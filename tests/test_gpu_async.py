@@ -85,3 +85,22 @@ def test_invalidated_and_released_tables_rebuild_identically():
     a.close()
     for h in out[1:]:
         assert np.array_equal(h, out[0])
+
+
+def test_tuning_does_not_change_results():
+    w = synth.small(ns=70, nch=6, mk=4, n_entries=4000, seed=44)
+    outs = []
+    for tune in ({}, {"xchunk": 2, "dchunk": 3}, {"xchunk": 1024, "dchunk": 65535}):
+        a = Assembler(w.t, w.ks, w.ksp, w.ksq, tuning=tune)
+        a.set_orbitals(w.pq, w.ipbs)
+        a.alloc_matrix(w.nch, w.icc, w.iicc, w.mk)
+        for prec in (SPLIT_BF16, FACTOR_FP64):
+            a.set_precision(prec)
+            a.zero_matrix()
+            for L in w.lists:
+                a.gen_matrix(L.icase, L.itype, L.kpol, L.k1, L.k2, L.k3, L.k4, L.c)
+            outs.append((tune, prec, a.get_matrix()))
+        a.close()
+    for tune, prec, h in outs[2:]:
+        ref = next(x for t, p, x in outs if p == prec)
+        assert np.array_equal(h, ref), (tune, prec)
