@@ -97,3 +97,47 @@ def test_factored_case4_and_case2_structures():
             h, _ = run(w, prec, [L])
             ref, _ = oracle(w, [L])
             check(h, ref, tol)
+
+
+@pytest.mark.parametrize("ns", [151, 160])
+def test_split_multi_tile_rows_against_plain(ns):
+    """ns above 128: quadrants of several 128-row tiles in the tensor-core
+    exchange (odd ns: the 8-byte staging path, even: bulk copies), every list
+    kind, 12 bound orbitals, per block against the plain FP64 assembly (held
+    to the oracle at 1e-12 by test_gpu_parity)."""
+    w = synth.small(ns=ns, nch=4, mk=3, n_entries=1500, breit=True, seed=70 + ns, norb=12,
+                    rmax=40.0, z=12.0)
+    hp, ap = run(w, PLAIN_FP64)
+    hs, as_ = run(w, SPLIT_BF16)
+    check(hs, hp, 1e-10)
+    assert np.abs(as_ - ap).max() <= 1e-12 * max(np.abs(ap).max(), 1e-300)
+
+
+def test_split_exchange_bound_orbital_limit():
+    """The split exchange holds up to 32 bound orbitals per digit operand
+    (one K tile); more is an EINVAL from the call, and FACTOR_FP64 (up to 64)
+    still assembles the list."""
+    from dbsr_gb300._lib import DbsrgError
+
+    w = synth.small(ns=50, nch=2, mk=2, n_entries=200, breit=False, seed=81)
+    nb0 = int((w.ipbs == 0).sum())
+    extra = 33 - nb0
+    pq = np.concatenate([w.pq[:, :, :nb0]] * (1 + extra // nb0 + 1), axis=2)[:, :, :33]
+    pq = np.concatenate([pq, w.pq[:, :, nb0:]], axis=2)
+    ipbs = np.concatenate([np.zeros(33, np.int32), w.ipbs[nb0:]])
+    # channel orbitals move up by `extra` positions in the O list keys only;
+    # R/S lists address channels by K1 and bound orbitals by K2/K3 (< nb0)
+    L = next(L for L in w.lists if L.icase == 2 and L.itype == 4)
+    a = Assembler(w.t, w.ks, w.ksp, w.ksq)
+    a.set_orbitals(np.asfortranarray(pq), ipbs)
+    a.alloc_matrix(w.nch, w.icc, w.iicc, w.mk)
+    a.set_precision(SPLIT_BF16)
+    with pytest.raises(DbsrgError, match="EINVAL"):
+        a.gen_matrix(L.icase, L.itype, L.kpol, L.k1, L.k2, L.k3, L.k4, L.c)
+    a.set_precision(FACTOR_FP64)
+    a.zero_matrix()
+    a.gen_matrix(L.icase, L.itype, L.kpol, L.k1, L.k2, L.k3, L.k4, L.c)
+    h = a.get_matrix()
+    a.close()
+    ref, _ = oracle(w, [L])
+    check(h, ref, 1e-12)
