@@ -250,12 +250,14 @@ __global__ void __launch_bounds__(256) k_pair_band(int ns, int ks, int nb, int m
   S *sm = reinterpret_cast<S *>(smraw);
   const int W = 2 * ks - 1;            // offsets -(ks-1) .. ks-1
   const int WL = PXC + W - 1;          // window of the row vectors
+  const int WLP = WL | 1;              // its stride (odd: no bank conflicts across orbitals)
+  const int HX = W * nb + 1;           // stride of H per output row (odd)
   const int x0 = blockIdx.x * PXC + 1; // first output row (1-based)
   const int d = (int)blockIdx.y - BAND;
   S *Wm = sm;                          // [PXC][W][W]
-  S *p1w = Wm + PXC * W * W;           // [nb][WL]: P1(a, x0-(ks-1)+t)
-  S *p2w = p1w + nb * WL;              // [nb][WL]: P2(b, x0+d-(ks-1)+t)
-  S *H = p2w + nb * WL;                // [PXC][W][nb]
+  S *p1w = Wm + PXC * W * W;           // [nb][WLP]: P1(a, x0-(ks-1)+t)
+  S *p2w = p1w + nb * WLP;             // [nb][WLP]: P2(b, x0+d-(ks-1)+t)
+  S *H = p2w + nb * WLP;               // [PXC][HX]: H(xl; u, b) at u*nb + b
   auto sv = [](double v) -> S {
     if constexpr (FF) return ffa::split(v); else return v;
   };
@@ -269,8 +271,8 @@ __global__ void __launch_bounds__(256) k_pair_band(int ns, int ks, int nb, int m
   for (int q = threadIdx.x; q < nb * WL; q += blockDim.x) {
     const int a = q / WL, t = q % WL;
     const int xi = x0 - (ks - 1) + t, yi = x0 + d - (ks - 1) + t;
-    p1w[q] = sv((xi >= 1 && xi <= ns) ? P1[(size_t)a * ns + xi - 1] : 0.0);
-    p2w[q] = sv((yi >= 1 && yi <= ns) ? P2[(size_t)a * ns + yi - 1] : 0.0);
+    p1w[a * WLP + t] = sv((xi >= 1 && xi <= ns) ? P1[(size_t)a * ns + xi - 1] : 0.0);
+    p2w[a * WLP + t] = sv((yi >= 1 && yi <= ns) ? P2[(size_t)a * ns + yi - 1] : 0.0);
   }
   __syncthreads();
   for (int q = threadIdx.x; q < PXC * kb * kb; q += blockDim.x) {
@@ -304,15 +306,16 @@ __global__ void __launch_bounds__(256) k_pair_band(int ns, int ks, int nb, int m
   for (int q = threadIdx.x; q < PXC * W * nb; q += blockDim.x) {
     const int b = q % nb, r = q / nb, u = r % W, xl = r / W;
     const S *w = Wm + ((size_t)xl * W + u) * W;
-    const S *p = p2w + (size_t)b * WL + xl;
+    const S *p = p2w + (size_t)b * WLP + xl;
+    S *hq = H + (size_t)xl * HX + (size_t)u * nb + b;
     if constexpr (FF) {
       float sh = 0.0f, sl = 0.0f;
       for (int v = 0; v < W; v++) ffa::mac(w[v], p[v], sh, sl);
-      H[q] = ffa::norm(sh, sl);
+      *hq = ffa::norm(sh, sl);
     } else {
       double s = 0.0;
       for (int v = 0; v < W; v++) s = fma(w[v], p[v], s);
-      H[q] = s;
+      *hq = s;
     }
   }
   __syncthreads();
@@ -321,8 +324,8 @@ __global__ void __launch_bounds__(256) k_pair_band(int ns, int ks, int nb, int m
     const int xl = q % PXC, pr = q / PXC, b = pr % nb, a = pr / nb;
     const int x = x0 + xl, y = x + d;
     if (x > ns || y < 1 || y > ns) continue;
-    const S *p = p1w + (size_t)a * WL + xl;
-    const S *h = H + (size_t)xl * W * nb + b;
+    const S *p = p1w + (size_t)a * WLP + xl;
+    const S *h = H + (size_t)xl * HX + b;
     const size_t o = (size_t)pr * per + (size_t)(x - 1) + (size_t)ns * (d + BAND);
     if constexpr (FF) {
       float sh = 0.0f, sl = 0.0f;
@@ -471,14 +474,25 @@ __global__ void __launch_bounds__(256) k_pair_diag(int ns, int ks, int kk, int n
               : (sym == 's' ? (f - 1) + ns * (s2 - f) : (f - 1) + ns * (s2 - f + ks - 1));
   }
   const double *rc = rkd + (size_t)kk * kk * (cv - 1);  // rkd(e1 pair, e2 pair; cv)
+  // the cell's table slice: consecutive threads read consecutive table
+  // elements (po fastest for case 1, the density pair fastest otherwise)
   for (int q = threadIdx.x; q < npo * kd; q += blockDim.x) {
-    const int po = q / kd, r = q % kd, g1 = r / k2 + 1, g2 = r % k2 + 1;
+    int po, r;
+    if (icv == 1) {
+      po = q % npo;
+      r = q / npo;
+    } else {
+      po = q / kd;
+      r = q % kd;
+    }
+    const int g1 = r / k2 + 1, g2 = r % k2 + 1;
     const int pd = pidx(ed, g1, g2);
-    Rt[q] = sv(icv == 1 ? rc[(size_t)po + (size_t)kk * pd] : rc[(size_t)pd + (size_t)kk * po]);
+    Rt[(size_t)po * kd + r] =
+        sv(icv == 1 ? rc[(size_t)po + (size_t)kk * pd] : rc[(size_t)pd + (size_t)kk * po]);
   }
   __syncthreads();
   const int ph = (cv - 1) % FAR;
-  for (int b0 = 0; b0 < nb; b0 += PBC) {
+  for (int b0 = 0; b0 < nb; b0 += PBC) {  // chunks of second orbitals
     const int bc = min(PBC, nb - b0);
     for (int q = threadIdx.x; q < npo * k1 * bc; q += blockDim.x) {
       const int bb = q % bc, r = q / bc, g1 = r % k1, po = r / k1;
@@ -891,8 +905,8 @@ int get_pairpot_direct_any(dbsrg_ctx *c, int family, int type, int k, int icv, i
   if (ff) {
     if ((rc = set_smem(c, (const void *)k_pair_diag<true>, sm3))) return rc;
     DBSRG_RUN(c, "k_pair_diag",
-              k_pair_diag<true><<<nv, 256, sm3, st>>>(ns, ks, kk, nb, icv, sym, eo, ed, cd->rkd,
-                                                      P1, P2, Dq, per));
+              k_pair_diag<true><<<nv, 256, sm3, st>>>(
+                  ns, ks, kk, nb, icv, sym, eo, ed, cd->rkd, P1, P2, Dq, per));
     DBSRG_RUN(c, "k_pair_direct_final",
               k_pair_direct_final<true><<<gf, 256, 0, st>>>(ns, ks, nv, kk, nb, icv, sym, eo, lo1,
                                                             hi1, cd->hi2, SA, M2 ? SB : nullptr,
@@ -900,8 +914,8 @@ int get_pairpot_direct_any(dbsrg_ctx *c, int family, int type, int k, int icv, i
   } else {
     if ((rc = set_smem(c, (const void *)k_pair_diag<false>, sm3))) return rc;
     DBSRG_RUN(c, "k_pair_diag",
-              k_pair_diag<false><<<nv, 256, sm3, st>>>(ns, ks, kk, nb, icv, sym, eo, ed, cd->rkd,
-                                                       P1, P2, Dq, per));
+              k_pair_diag<false><<<nv, 256, sm3, st>>>(
+                  ns, ks, kk, nb, icv, sym, eo, ed, cd->rkd, P1, P2, Dq, per));
     DBSRG_RUN(c, "k_pair_direct_final",
               k_pair_direct_final<false><<<gf, 256, 0, st>>>(ns, ks, nv, kk, nb, icv, sym, eo,
                                                              lo1, hi1, cd->hi2, SA,
@@ -938,9 +952,9 @@ static int get_pairpot_band(dbsrg_ctx *c, int family, int type, int k, int cs, i
   DBSRG_TRY(c, cudaMemsetAsync(K, 0, npair * per * sizeof(double), c->stream));
   const double *P1 = c->brows + (size_t)(jp1 - 1) * nb * ns;
   const double *P2 = c->brows + (size_t)(jp2 - 1) * nb * ns;
-  const int W = 2 * ks - 1, WL = PXC + W - 1;
-  const size_t smem = ((size_t)PXC * W * W + 2 * (size_t)nb * WL + (size_t)PXC * W * nb) *
-                      sizeof(double);
+  const int W = 2 * ks - 1, WLP = (PXC + W - 1) | 1;
+  const size_t smem =
+      ((size_t)PXC * W * W + 2 * (size_t)nb * WLP + (size_t)PXC * (W * nb + 1)) * sizeof(double);
   const int mode = family == 0 ? 0 : (cs == 3 ? 1 : 2);
   dim3 gb((unsigned)((ns + PXC - 1) / PXC), (unsigned)NDB);
   if (ff) {

@@ -261,6 +261,11 @@ __global__ void k_triang(int nv, int ks, int ksp, int ksq, int type, int k, cons
                          const double *qbsp, double *rkd) {
   extern __shared__ double sm[];
   const int iv = blockIdx.x;  // 0-based interval
+  // this block's share of the interval's kk*kk output cells (blockIdx.y of
+  // gridDim.y, launched with one block per interval: the inner integrals
+  // would be repeated by every block of an interval)
+  const int nq = ks * ks * ks * ks, part = (nq + gridDim.y - 1) / gridDim.y;
+  const int q0 = blockIdx.y * part, q1 = min(nq, q0 + part);
   const int nw = nv + 1, kk = ks * ks;
   const int KS2 = ks * ks;
   const double *tb = tri + (size_t)iv * KS2 * (2 + ksp + ksq);  // x | w | BP | BQ
@@ -360,13 +365,13 @@ __global__ void k_triang(int nv, int ks, int ksp, int ksq, int type, int k, cons
       A[q] = s;
     }
     __syncthreads();
-    for (int q = threadIdx.x; q < kk * kk; q += blockDim.x) {
+    for (int q = q0 + threadIdx.x; q < q1; q += blockDim.x) {
       int ii = q % kk, jj = q / kk;
       out[q] = (ii < ik && jj < ik) ? __dadd_rn(A[ii + ik * jj], A[jj + ik * ii]) : 0.0;
     }
   } else if (type == 2 || type == 3) {
     const int ikp = ksp * (ksp + 1) / 2, ikq = ksq * (ksq + 1) / 2;
-    for (int q = threadIdx.x; q < kk * kk; q += blockDim.x) {
+    for (int q = q0 + threadIdx.x; q < q1; q += blockDim.x) {
       int r = q % kk, cc = q / kk;
       int pp_ = type == 2 ? r : cc, qq_ = type == 2 ? cc : r;  // P pair, Q pair
       double v = 0.0;
@@ -386,7 +391,7 @@ __global__ void k_triang(int nv, int ks, int ksp, int ksq, int type, int k, cons
     }
   } else {
     const int np = ksp * ksq;
-    for (int q = threadIdx.x; q < kk * kk; q += blockDim.x) {
+    for (int q = q0 + threadIdx.x; q < q1; q += blockDim.x) {
       int jj = q % kk, ii = q / kk;  // rkd(jj,ii): jj inner (P,Q), ii outer
       double v = 0.0;
       if (jj < np && ii < np) {
@@ -425,7 +430,7 @@ int compute_diag_cells(dbsrg_ctx *c, int type, int k, double *rkd) {
     DBSRG_TRY(c, cudaFuncSetAttribute(k_triang, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)bytes));
   DBSRG_RUN(c, "k_triang",
-            k_triang<<<g.nv, 256, bytes, c->stream>>>(g.nv, ks, g.ksp, g.ksq, type, k, g.tri,
+            k_triang<<<dim3(g.nv, 1), 256, bytes, c->stream>>>(g.nv, ks, g.ksp, g.ksq, type, k, g.tri,
                                                       g.grm, g.grw, g.pbsp, g.qbsp, rkd));
   return DBSRG_OK;
 }
