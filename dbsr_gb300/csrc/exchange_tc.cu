@@ -126,9 +126,21 @@ __global__ void __launch_bounds__(ZROWS) k_zdigits(const ZArgs z) {
 #pragma unroll
   for (int d = 0; d < NDB; d++) bh[d] = bl[d] = 0.0f;
   if (y < ns) {
+    // the next entry's pair index and coefficient are loaded while this
+    // entry's potentials are summed
+    int pr_n = si.start < si.end ? z.pairs[si.start] : 0;
+    float2 c_n = si.start < si.end ? z.cd[si.start] : make_float2(0.0f, 0.0f);
     for (int e = si.start; e < si.end; e++) {
-      const int pr = z.pairs[e], oa = pr / nb, ob = pr - oa * nb;
-      const float2 c = z.cd[e];
+      const int pr = pr_n, oa = pr / nb, ob = pr - oa * nb;
+      const float2 c = c_n;
+      if (e + 1 < si.end) {
+        pr_n = z.pairs[e + 1];
+        c_n = z.cd[e + 1];
+      }
+      const float2 *kb = Kb + (size_t)pr * kper + y;
+      float2 kv[NDB];
+#pragma unroll
+      for (int d = 0; d < NDB; d++) kv[d] = kb[(size_t)ns * d];
       {
         float2 acc = z0[oa * ZROWS + t];
         ffa::mac(c, V[(size_t)y + (size_t)ns * ob], acc.x, acc.y);
@@ -139,9 +151,8 @@ __global__ void __launch_bounds__(ZROWS) k_zdigits(const ZArgs z) {
         ffa::mac(c, Vl[(size_t)y + (size_t)ns * ob], acc.x, acc.y);
         z1[oa * ZROWS + t] = acc;
       }
-      const float2 *kb = Kb + (size_t)pr * kper + y;
 #pragma unroll
-      for (int d = 0; d < NDB; d++) ffa::mac(c, kb[(size_t)ns * d], bh[d], bl[d]);
+      for (int d = 0; d < NDB; d++) ffa::mac(c, kv[d], bh[d], bl[d]);
     }
     double *yb = z.Yb + ((size_t)a * z.nm + slot) * kper + y;
 #pragma unroll

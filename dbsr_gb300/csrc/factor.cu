@@ -693,16 +693,33 @@ __global__ void k_scatter_dp(int ns, int ks, char sym, QuadSpec sp, KdSet kd,
   auto ysum = [&](int a, const SegInfo &sj, int i, int j) -> double {
     const int p = band_pos(ns, ks, sym, i, j);
     if (p < 0) return 0.0;
+    // entries in batches of EB: the EB potential loads are issued together
+    // (they depend only on the batch's pair indices), then summed in order
+    constexpr int EB = 8;
+    int e = sj.start;
     if (FF) {
       const float2 *K = kd.Kf[a];
       float sh = 0.0f, sl = 0.0f;
-      for (int e = sj.start; e < sj.end; e++)
-        ffa::mac(cdf[e], K[(size_t)pairs[e] * per + p], sh, sl);
+      for (; e + EB <= sj.end; e += EB) {
+        float2 kv[EB];
+#pragma unroll
+        for (int u = 0; u < EB; u++) kv[u] = K[(size_t)pairs[e + u] * per + p];
+#pragma unroll
+        for (int u = 0; u < EB; u++) ffa::mac(cdf[e + u], kv[u], sh, sl);
+      }
+      for (; e < sj.end; e++) ffa::mac(cdf[e], K[(size_t)pairs[e] * per + p], sh, sl);
       return ffa::value(sh, sl);
     }
     const double *K = kd.K[a];
     double acc = 0.0;
-    for (int e = sj.start; e < sj.end; e++) acc = fma(cd[e], K[(size_t)pairs[e] * per + p], acc);
+    for (; e + EB <= sj.end; e += EB) {
+      double kv[EB];
+#pragma unroll
+      for (int u = 0; u < EB; u++) kv[u] = K[(size_t)pairs[e + u] * per + p];
+#pragma unroll
+      for (int u = 0; u < EB; u++) acc = fma(cd[e + u], kv[u], acc);
+    }
+    for (; e < sj.end; e++) acc = fma(cd[e], K[(size_t)pairs[e] * per + p], acc);
     return acc;
   };
   for (int a = 0; a < sp.na; a++) {
