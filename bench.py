@@ -56,7 +56,7 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU sample")
-    p.add_argument("--workload", default="config1", choices=["config1", "batch"],
+    p.add_argument("--workload", default="config1", choices=["config1", "batch", "basis"],
                    help="config1: one 120-channel matrix; batch: independent J-blocks with "
                         "their own grids through dbsrg_gen_batch")
     p.add_argument("--nblocks", type=int, default=64)
@@ -458,6 +458,78 @@ def batch_main(args, rank, world, local):
         pg.destroy_process_group()
 
 
+def basis_main(args, rank, world, local):
+    """The channel basis of the write-out (SURVEY "next" row 2) on the
+    120-channel matrix: the split-form assembly, then dbsrg_diag_channels
+    (one generalized eigenproblem per channel, cuSOLVER sygvd; B = the
+    B-spline overlap fppqq, the first and last B-spline of P and Q removed,
+    every eigenvalue kept) and dbsrg_channel_basis (D_i^T H D_j for the 7140
+    off-diagonal blocks, cuBLAS DGEMM).  Timed once each after a warm-up,
+    host wall clock around synchronised calls."""
+    import torch
+
+    from dbsr_gb300 import SPLIT_BF16, Assembler, synth
+
+    torch.cuda.set_device(local)
+    w = synth.config1(scale=args.scale, nch=args.nch, breit=True)
+    a = Assembler(w.t, w.ks, w.ksp, w.ksq, device=local)
+    a.set_orbitals(w.pq, w.ipbs)
+    a.alloc_matrix(w.nch, w.icc, w.iicc, w.mk)
+    a.set_precision(SPLIT_BF16)
+    ms, ns, nch = a.ms, a.ns, w.nch
+    B = a.grid_array("fppqq").reshape(ms, ms, order="F")
+    bdiag = torch.from_numpy(np.asfortranarray(np.repeat(B[:, :, None], nch, axis=2))
+                             .ravel(order="F")).cuda()
+    iprm = np.ones((ms, nch), dtype=np.int32, order="F")
+    for comp in range(2):
+        iprm[comp * ns, :] = 0
+        iprm[comp * ns + ns - 1, :] = 0
+    sol = torch.empty(ms * ms * nch, dtype=torch.float64, device="cuda")
+
+    def assemble():
+        a.zero_matrix()
+        for L in w.lists:
+            a.gen_matrix(L.icase, L.itype, L.kpol, L.k1, L.k2, L.k3, L.k4, L.c)
+        a.sync()
+
+    out = {}
+    for rep in range(2):  # warm-up, then timed
+        assemble()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        _, ev, nsol = a.diag_channels(bdiag, iprm)  # solutions to `sol` below
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        # the solutions stay on the device: rerun into the device buffer
+        check_nsol = nsol.copy()
+        L = a._L
+        rc = L.dbsrg_diag_channels(a._h, bdiag.data_ptr(), iprm.ctypes.data, -1e30, 1e30, 0.0,
+                                   sol.data_ptr(), ev.ctypes.data, nsol.ctypes.data)
+        assert rc == 0 and np.array_equal(nsol, check_nsol)
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        a.channel_basis(sol, nsol)
+        torch.cuda.synchronize()
+        t3 = time.perf_counter()
+        out = {"diag_channels_s": t1 - t0, "diag_channels_device_out_s": t2 - t1,
+               "channel_basis_s": t3 - t2}
+    fl = 0.0
+    for ich in range(1, nch + 1):
+        for jch in range(1, ich):
+            if w.icc[ich - 1, jch - 1] > 0:
+                ni, nj = int(nsol[ich - 1]), int(nsol[jch - 1])
+                fl += 2.0 * ni * ms * ms + 2.0 * ni * nj * ms
+    out.update({"metric": "channel basis (Diag_channels + Record_matrix transform) s",
+                "unit": "s", "value": out["diag_channels_device_out_s"] + out["channel_basis_s"],
+                "higher_is_better": False, "dtype": "f64",
+                "config": {"workload": f"config1 matrix: ns={ns} nch={nch}", "blocks": w.iicc,
+                           "solutions_per_channel": int(np.median(nsol))},
+                "basis_dgemm_tflop": fl / 1e12,
+                "basis_dgemm_tflops": fl / out["channel_basis_s"] / 1e12})
+    print(json.dumps(out), flush=True)
+    a.close()
+
+
 def main():
     args = parse()
     rank = int(os.environ.get("RANK", "0"))
@@ -468,6 +540,8 @@ def main():
 
     if args.workload == "batch" and args.impl == "ours":
         return batch_main(args, rank, world, local)
+    if args.workload == "basis" and args.impl == "ours":
+        return basis_main(args, rank, world, local)
     w = synth.config1(scale=args.scale, nch=args.nch)
 
     if args.impl == "reference":

@@ -283,6 +283,32 @@ class Assembler:
         """Wait for the queued kernels; raises on a failure of any of them."""
         check(self._h, self._L.dbsrg_sync(self._h), "sync")
 
+    def diag_channels(self, bdiag, iprm, emin=-1.0e30, emax=1.0e30, egap=0.0):
+        """dbsrg_diag_channels: (sol(ms,ms,nch), eval(ms,nch), nsol(nch)) of the
+        generalized channel problems H c = E B c, B = bdiag(:,:,ich) (host or
+        device), on the B-splines with iprm(:,ich) != 0."""
+        sol = np.zeros((self.ms, self.ms, self.nch), order="F")
+        ev = np.zeros((self.ms, self.nch), order="F")
+        ns = np.zeros(self.nch, dtype=np.int32)
+        pb, k1 = _ptr(bdiag, np.float64)
+        pi, k2 = _ptr(np.asfortranarray(iprm, dtype=np.int32), np.int32)
+        rc = self._L.dbsrg_diag_channels(self._h, pb, pi, float(emin), float(emax), float(egap),
+                                         C.c_void_p(sol.ctypes.data), C.c_void_p(ev.ctypes.data),
+                                         C.c_void_p(ns.ctypes.data))
+        check(self._h, rc, "diag_channels")
+        return sol, ev, ns
+
+    def channel_basis(self, sol, nsol, out=None):
+        """dbsrg_channel_basis: every off-diagonal block to D_i^T H D_j in place;
+        returns the transformed matrix when `out` is given or True."""
+        ps, k1 = _ptr(sol, np.float64)
+        pn, k2 = _ptr(np.ascontiguousarray(nsol, dtype=np.int32), np.int32)
+        if out is True:
+            out = np.zeros((self.ms, self.ms, self.iicc), order="F")
+        po, k3 = _ptr(out, np.float64) if out is not None else (None, None)
+        check(self._h, self._L.dbsrg_channel_basis(self._h, ps, pn, po), "channel_basis")
+        return out
+
     def set_tuning(self, name: str, value: int):
         """dbsrg_set_tuning: "xchunk", "dchunk" or "windows"."""
         check(self._h, self._L.dbsrg_set_tuning(self._h, name.encode(), int(value)),

@@ -64,7 +64,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
         objs = list(ex.map(comp, srcs))
     tmp = LIB + ".tmp"
-    cmd = [cc, *ARCH, "-shared", "-cudart=static", "-o", tmp, *objs]
+    cmd = [cc, *ARCH, "-shared", "-cudart=static", "-o", tmp, *objs, "-ldl"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

@@ -283,6 +283,7 @@ int dbsrg_destroy(dbsrg_ctx *c) {
   if (c->sstream) cudaStreamSynchronize(c->sstream);
   if (c->cstream) cudaStreamSynchronize(c->cstream);
   if (c->stream) cudaStreamSynchronize(c->stream);
+  basis_release(c);
   free_tables(c);
   pool_trim(c);
   DeviceGrid &g = c->g;

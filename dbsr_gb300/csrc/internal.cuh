@@ -138,6 +138,8 @@ struct dbsrg_ctx {
   // waits (dbsrg_sync, the read-outs, state changes)
   bool async = false;
   bool pending = false;
+  // cuSOLVER / cuBLAS handles of the channel basis (basis.cu), made on use
+  void *sv_handle = nullptr, *bl_handle = nullptr;
   // tuning (dbsrg_set_tuning): segments per chunk of the factored exchange
   // and direct contractions, windows of dbsrg_assemble_to_host
   int tune_xchunk = 256, tune_dchunk = 4096, tune_windows = 8;
@@ -254,6 +256,8 @@ int ensure_pinned(dbsrg_ctx *c, size_t bytes);
 // frees the far-field vectors, pair potentials and bound rows (they depend
 // on the orbitals and the tables)
 void free_orbital_products(dbsrg_ctx *c);
+// handles of the channel basis (basis.cu)
+void basis_release(dbsrg_ctx *c);
 // float-float copy of n doubles at src (cached until the orbital products go)
 int ff_of(dbsrg_ctx *c, const double *src, size_t n, const float2 **out);
 

@@ -201,6 +201,30 @@ int dbsrg_get_acf(dbsrg_ctx *ctx, double *acf);
  * alloc/destroy). */
 int dbsrg_matrix_device_ptr(dbsrg_ctx *ctx, double **hch_dev);
 
+/* The channel basis of the write-out (SURVEY "next" row 2), on the
+ * device-resident whole matrix (no window).
+ * dbsrg_diag_channels -- Diag_channels (diag.f90:2-81): for every channel
+ * ich with a diagonal block, the generalized problem H c = E B c on the
+ * B-splines kept by the zero conditions (iprm(j,ich) != 0, j = 1..ms,
+ * zero_cond.f90), H the current diagonal block of hch and B = bdiag(:,:,ich)
+ * (the overlap diagonal blocks, ms x ms x nch, host or device); the
+ * solutions with emin <= E <= emax and |E| >= egap, ascending, restored to
+ * the full net with their largest component positive, go to
+ * sol(:, 1:nsol(ich), ich) (ms x ms x nch, host or device; the rest zero),
+ * their energies to eval(1:nsol(ich), ich) (ms x nch).  iprm, eval and nsol
+ * are host arrays.
+ * dbsrg_channel_basis -- the block transformation of Record_matrix
+ * (record_matrix.f90:14-26): every block of a channel pair ich > jch becomes
+ * c = D_ich^T H D_jch (nsol(ich) x nsol(jch) in its top-left corner, zero
+ * elsewhere; D = sol), in place; diagonal blocks stay.  out, when not NULL,
+ * receives a copy of the transformed hch.
+ * Both load cuSOLVER and cuBLAS on first use. */
+int dbsrg_diag_channels(dbsrg_ctx *ctx, const double *bdiag, const int *iprm,
+                        double emin, double emax, double egap, double *sol,
+                        double *eval, int *nsol);
+int dbsrg_channel_basis(dbsrg_ctx *ctx, const double *sol, const int *nsol,
+                        double *out);
+
 /* One assembled B-spline integral table, in the reference layout
  * rkb(ns,ns,ks,ks) for R (type 0 pppp,1 qqqq,2 pqpq,3 qpqp; mrk_*,
  * dbsr_lib_dbs.f90:2898-3492) or rkb(ns,ns,2ks-1,2ks-1) for S (type 0
