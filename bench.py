@@ -63,6 +63,8 @@ def parse():
     p.add_argument("--nch-max", type=int, default=300)
     p.add_argument("--batch-group", type=int, default=8, help="J-blocks run concurrently")
     p.add_argument("--window-gb", type=float, default=4.0, help="device window per J-block")
+    p.add_argument("--tune", default=None,
+                   help="batch: autotune the exchange chunk size first, recording into this table")
     p.add_argument("--rows-entries", type=float, default=1e4)
     return p.parse_args()
 
@@ -385,13 +387,16 @@ def batch_main(args, rank, world, local):
     host = [torch.empty(wbytes // 8, dtype=torch.float64).pin_memory() for _ in range(G)]
     torch.cuda.synchronize()
     stats = {"d2h": 0, "windows": 0}
+    from dbsr_gb300 import autotune
+
+    tuning = autotune.lookup(0, local, mode="batch") or None  # the batch's own entry
 
     def step():
         for g0 in range(0, len(ws), G):
             gw, gl = ws[g0:g0 + G], lists[g0:g0 + G]
             asm = []
             for w in gw:
-                a = Assembler(w.t, w.ks, w.ksp, w.ksq, device=local)
+                a = Assembler(w.t, w.ks, w.ksp, w.ksq, device=local, tuning=tuning)
                 a.set_orbitals(w.pq, w.ipbs)
                 blk = (2 * w.ns) ** 2 * 8
                 a.alloc_matrix(w.nch, w.icc, w.iicc, w.mk,
@@ -409,6 +414,21 @@ def batch_main(args, rank, world, local):
             for a in asm:
                 a.close()
 
+    if args.tune:  # autotune the batch's exchange chunk size, record it, use it
+        def run_batch(t):
+            nonlocal tuning
+            tuning = t
+            step()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            step()
+            torch.cuda.synchronize()
+            return time.perf_counter() - t0
+
+        choice = autotune.tune_batch(run_batch, log=lambda m: print(m, file=sys.stderr))
+        autotune.record(choice, 0, local, note=f"config3 batch nch<={args.nch_max}",
+                        path=args.tune)
+        tuning = {"xchunk": choice["xchunk"]}
     for _ in range(args.warmup):
         step()
     clk = Clocks(local)
@@ -446,7 +466,7 @@ def batch_main(args, rank, world, local):
                        "entries": int(sum(L.n for w in ws for L in w.lists)),
                        "matrix_gb": sum(w.iicc * (2 * w.ns) ** 2 * 8 for w in ws) / 1e9,
                        "algorithmic_tflop": flops / 1e12,
-                       "group": G, "window_gb": args.window_gb,
+                       "group": G, "window_gb": args.window_gb, "tuning": tuning,
                        "output": "every window copied to pinned host memory inside the step",
                        "timing": "host wall clock around the synchronised steps",
                        "parallelism": f"replicas x{world}"},

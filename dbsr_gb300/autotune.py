@@ -15,6 +15,9 @@ coordinate descent (CUDA-event timed steps after a warm-up) and ``record()``
 stores the choice in ``tuning.json`` next to this file, keyed by the device
 name and the number of B-splines; ``lookup()`` (used by Assembler) returns
 the entry of the nearest recorded grid size for the device, or {}.
+``tune_batch()`` times the whole streamed batch (many symmetry blocks at
+once, small windows) for each exchange chunk size, a regime of its own; its
+entry (``"mode": "batch"``) is read by ``lookup(mode="batch")``.
 
     python -m dbsr_gb300.autotune            # the 120-channel workload
 """
@@ -43,13 +46,13 @@ def _device_name(device: int) -> str | None:
     return None
 
 
-def lookup(ns: int, device: int = 0) -> dict:
+def lookup(ns: int, device: int = 0, mode: str = "single") -> dict:
     """Recorded parameters for this GPU and the nearest grid size, or {}."""
     name = _device_name(device)
     if name is None or not os.path.exists(TABLE):
         return {}
     with open(TABLE) as f:
-        entries = json.load(f).get(name, [])
+        entries = [e for e in json.load(f).get(name, []) if e.get("mode", "single") == mode]
     if not entries:
         return {}
     best = min(entries, key=lambda e: abs(e["ns"] - ns))
@@ -118,13 +121,26 @@ def tune(w, reps: int = 3, device: int = 0, log=print) -> dict:
     return choice
 
 
+def tune_batch(run_batch, log=print) -> dict:
+    """Exchange chunk size of the streamed batch: run_batch(tuning) times one
+    whole batch with those parameters (seconds)."""
+    times = {}
+    for v in CANDIDATES["xchunk"][1:]:
+        times[v] = run_batch({"xchunk": v})
+        log(f"batch xchunk={v}: {times[v]:.2f} s")
+    best = min(times, key=times.get)
+    return {"mode": "batch", "xchunk": best, "batch_s": round(times[best], 3)}
+
+
 def record(choice: dict, ns: int, device: int = 0, note: str = "", path: str = TABLE) -> None:
     name = _device_name(device)
     table = {}
     if os.path.exists(path):
         with open(path) as f:
             table = json.load(f)
-    entries = [e for e in table.get(name, []) if e["ns"] != ns]
+    mode = choice.get("mode", "single")
+    entries = [e for e in table.get(name, [])
+               if not (e["ns"] == ns and e.get("mode", "single") == mode)]
     entries.append({"ns": ns, **choice, **({"workload": note} if note else {})})
     table[name] = sorted(entries, key=lambda e: e["ns"])
     with open(path, "w") as f:
@@ -139,17 +155,23 @@ def main():
 
     p = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
     p.add_argument("--nch", type=int, default=120)
+    p.add_argument("--batch-block", type=int, default=None,
+                   help="tune on block N of the batched workload (synth.config3_block) instead")
     p.add_argument("--scale", type=float, default=1.0)
     p.add_argument("--reps", type=int, default=3)
     p.add_argument("--dry", action="store_true", help="print, do not record")
     p.add_argument("--table", default=TABLE, help="tuning table to record into")
     args = p.parse_args()
-    w = synth.config1(scale=args.scale, nch=args.nch)
+    if args.batch_block is not None:
+        w = synth.config3_block(args.batch_block)
+        note = f"config3 block {args.batch_block} (nch={w.nch})"
+    else:
+        w = synth.config1(scale=args.scale, nch=args.nch)
+        note = f"config1 nch={args.nch} scale={args.scale}"
     choice = tune(w, reps=args.reps)
     print(json.dumps(choice))
     if not args.dry:
-        record(choice, int(w.t.size - w.ks), note=f"config1 nch={args.nch} scale={args.scale}",
-               path=args.table)
+        record(choice, int(w.t.size - w.ks), note=note, path=args.table)
 
 
 if __name__ == "__main__":
