@@ -585,13 +585,18 @@ __global__ void __maxnreg__(96) k_xfused(const XArgs p) {
                                 (long long)P[1][c] * 65536LL + (long long)P[2][c];
             const int d = (y0 + c) - x, se = er + ec[c];
             if (sg * d >= FAR) {
-              if (se > cur[c]) {  // raise the sum to the new exponent
-                const int up = se - cur[c];
-                Iacc[c] = up < 63 ? Iacc[c] >> up : 0;
+              if (pc == 0) {  // the tile's first product: the sum starts at its exponent
+                Iacc[c] = I;
                 cur[c] = se;
+              } else {
+                if (se > cur[c]) {  // raise the sum to the new exponent
+                  const int up = se - cur[c];
+                  Iacc[c] = up < 63 ? Iacc[c] >> up : 0;
+                  cur[c] = se;
+                }
+                const int sh = cur[c] - se;
+                if (sh < 63) Iacc[c] += I >> sh;
               }
-              const int sh = cur[c] - se;
-              if (sh < 63) Iacc[c] += I >> sh;
             }
           }
         }

@@ -494,37 +494,74 @@ __global__ void __launch_bounds__(256) k_pair_diag(int ns, int ks, int kk, int n
   const int ph = (cv - 1) % FAR;
   for (int b0 = 0; b0 < nb; b0 += PBC) {  // chunks of second orbitals
     const int bc = min(PBC, nb - b0);
-    for (int q = threadIdx.x; q < npo * k1 * bc; q += blockDim.x) {
-      const int bb = q % bc, r = q / bc, g1 = r % k1, po = r / k1;
+    // stage 1: a thread forms H(po, g1, b) for the bc second orbitals of the
+    // chunk at once (independent sums sharing each table load)
+    for (int q = threadIdx.x; q < npo * k1; q += blockDim.x) {
+      const int g1 = q % k1, po = q / k1;
       const S *rt = Rt + (size_t)po * kd + (size_t)g1 * k2;
-      const S *p = w2 + (size_t)(b0 + bb) * k2;
+      S *hq = H + ((size_t)po * k1 + g1) * PBC;
       if constexpr (FF) {
-        float sh = 0.0f, sl = 0.0f;
-        for (int g2 = 0; g2 < k2; g2++) ffa::mac(rt[g2], p[g2], sh, sl);
-        H[((size_t)po * k1 + g1) * PBC + bb] = ffa::norm(sh, sl);
+        float sh[PBC], sl[PBC];
+#pragma unroll
+        for (int bb = 0; bb < PBC; bb++) sh[bb] = sl[bb] = 0.0f;
+        for (int g2 = 0; g2 < k2; g2++) {
+          const S r = rt[g2];
+#pragma unroll
+          for (int bb = 0; bb < PBC; bb++)
+            if (bb < bc) ffa::mac(r, w2[(size_t)(b0 + bb) * k2 + g2], sh[bb], sl[bb]);
+        }
+#pragma unroll
+        for (int bb = 0; bb < PBC; bb++)
+          if (bb < bc) hq[bb] = ffa::norm(sh[bb], sl[bb]);
       } else {
-        double s = 0.0;
-        for (int g2 = 0; g2 < k2; g2++) s = fma(rt[g2], p[g2], s);
-        H[((size_t)po * k1 + g1) * PBC + bb] = s;
+        double acc[PBC];
+#pragma unroll
+        for (int bb = 0; bb < PBC; bb++) acc[bb] = 0.0;
+        for (int g2 = 0; g2 < k2; g2++) {
+          const S r = rt[g2];
+#pragma unroll
+          for (int bb = 0; bb < PBC; bb++)
+            if (bb < bc) acc[bb] = fma(r, w2[(size_t)(b0 + bb) * k2 + g2], acc[bb]);
+        }
+#pragma unroll
+        for (int bb = 0; bb < PBC; bb++)
+          if (bb < bc) hq[bb] = acc[bb];
       }
     }
     __syncthreads();
-    for (int q = threadIdx.x; q < npo * nb * bc; q += blockDim.x) {
-      const int bb = q % bc, r = q / bc, a = r % nb, po = r / nb;
+    // stage 2: Dq for the bc second orbitals at once
+    for (int q = threadIdx.x; q < npo * nb; q += blockDim.x) {
+      const int a = q % nb, po = q / nb;
       const int qp = poq[po];
       if (qp < 0) continue;
       const S *p = w1 + (size_t)a * k1;
-      const S *h = H + (size_t)po * k1 * PBC + bb;
-      double s;
+      const S *h = H + (size_t)po * k1 * PBC;
+      double s[PBC];
       if constexpr (FF) {
-        float sh = 0.0f, sl = 0.0f;
-        for (int g1 = 0; g1 < k1; g1++) ffa::mac(p[g1], h[(size_t)g1 * PBC], sh, sl);
-        s = ffa::value(sh, sl);
+        float sh[PBC], sl[PBC];
+#pragma unroll
+        for (int bb = 0; bb < PBC; bb++) sh[bb] = sl[bb] = 0.0f;
+        for (int g1 = 0; g1 < k1; g1++) {
+          const S pv = p[g1];
+#pragma unroll
+          for (int bb = 0; bb < PBC; bb++)
+            if (bb < bc) ffa::mac(pv, h[(size_t)g1 * PBC + bb], sh[bb], sl[bb]);
+        }
+#pragma unroll
+        for (int bb = 0; bb < PBC; bb++) s[bb] = ffa::value(sh[bb], sl[bb]);
       } else {
-        s = 0.0;
-        for (int g1 = 0; g1 < k1; g1++) s = fma(p[g1], h[(size_t)g1 * PBC], s);
+#pragma unroll
+        for (int bb = 0; bb < PBC; bb++) s[bb] = 0.0;
+        for (int g1 = 0; g1 < k1; g1++) {
+          const S pv = p[g1];
+#pragma unroll
+          for (int bb = 0; bb < PBC; bb++)
+            if (bb < bc) s[bb] = fma(pv, h[(size_t)g1 * PBC + bb], s[bb]);
+        }
       }
-      Dq[((size_t)ph * npair + (size_t)a * nb + b0 + bb) * per + qp] = s;
+#pragma unroll
+      for (int bb = 0; bb < PBC; bb++)
+        if (bb < bc) Dq[((size_t)ph * npair + (size_t)a * nb + b0 + bb) * per + qp] = s[bb];
     }
     __syncthreads();
   }
