@@ -54,6 +54,8 @@ SIGNATURES = [
     ("dbsrg_sync", C.c_int, [_vp]),
     ("dbsrg_set_async", C.c_int, [_vp, C.c_int]),
     ("dbsrg_set_tuning", C.c_int, [_vp, C.c_char_p, C.c_int]),
+    ("dbsrg_set_wait_limit", C.c_int, [_vp, C.c_longlong]),
+    ("dbsrg_inject_wait_timeout", C.c_int, [_vp, C.c_int]),
     ("dbsrg_diag_channels", C.c_int,
      [_vp, _vp, _vp, C.c_double, C.c_double, C.c_double, _vp, _vp, _vp]),
     ("dbsrg_channel_basis", C.c_int, [_vp, _vp, _vp, _vp]),

@@ -309,6 +309,16 @@ class Assembler:
         check(self._h, self._L.dbsrg_channel_basis(self._h, ps, pn, po), "channel_basis")
         return out
 
+    def set_wait_limit(self, ns: int):
+        """Limit of the tensor-core kernel's pipeline waits (ns)."""
+        check(self._h, self._L.dbsrg_set_wait_limit(self._h, int(ns)), "set_wait_limit")
+
+    def inject_wait_timeout(self, enable: bool = True):
+        """Test switch: the tensor-core kernel's epilogue waits on a barrier
+        nothing completes, so the call must end in DBSRG_ETIMEOUT."""
+        check(self._h, self._L.dbsrg_inject_wait_timeout(self._h, int(enable)),
+              "inject_wait_timeout")
+
     def set_tuning(self, name: str, value: int):
         """dbsrg_set_tuning: "xchunk", "dchunk" or "windows"."""
         check(self._h, self._L.dbsrg_set_tuning(self._h, name.encode(), int(value)),

@@ -78,11 +78,14 @@ __global__ void k_cd_ff(int n, const double *cd, float2 *cdf) {
   if (e < n) cdf[e] = ffa::split(cd[e]);
 }
 
-// bound-orbital indices of every entry must address pq(:,:,1:nbf)
-__global__ void k_check_orbitals(int n, const int *k2, const int *k3, int nbf, int *err) {
+// bound-orbital indices of every entry must address pq(:,:,1:nbf) (err 1),
+// and every coefficient must be finite (err 3)
+__global__ void k_check_orbitals(int n, const int *k2, const int *k3, const double *cd, int nbf,
+                                 int *err) {
   int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= n) return;
   if (k2[e] < 1 || k2[e] > nbf || k3[e] < 1 || k3[e] > nbf) atomicExch(err, 1);
+  if (!isfinite(cd[e])) atomicExch(err, 3);
 }
 
 // decode segments, look up blocks, pair up segments of the same block
@@ -682,6 +685,7 @@ int plan_list(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const int *ip
     DBSRG_TRY(c, cudaStreamSynchronize(ss));
     std::vector<int> eblk(n, 0), hstart(iicc + 2, 0), hlist, horder(n);
     for (int e = 0; e < n; e++) {
+      if (!std::isfinite(hcd[e])) return set_err(c, DBSRG_EINVAL, "non-finite coefficient in list");
       if (std::fabs(hcd[e]) < 1.0e-10) continue;
       const int i1 = hk1[e] / DBSRG_IBO, j1 = hk2[e] / DBSRG_IBO;
       if (i1 < 1 || i1 > c->nbf || j1 < 1 || j1 > c->nbf || hk1[e] % DBSRG_IBO < 1 ||
@@ -721,12 +725,13 @@ int plan_list(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const int *ip
 
   // ---- segments (orbital check and segment count read back together)
   DBSRG_RUN_S(c, ss, "k_check_orbitals",
-              k_check_orbitals<<<(n + 255) / 256, 256, 0, ss>>>(n, P.lk2, P.lk3, c->nbf,
+              k_check_orbitals<<<(n + 255) / 256, 256, 0, ss>>>(n, P.lk2, P.lk3, P.lcd, c->nbf,
                                                                 dscal + 1));
   DBSRG_RUN_S(c, ss, "k_segments", k_segments<<<1, 1024, 0, ss>>>(n, P.lk1, seg_start, dscal));
   int hs[4] = {0, 0, 0, 0};  // nseg, error, -, bound-pair error
   DBSRG_TRY(c, cudaMemcpyAsync(hs, dscal, 2 * sizeof(int), cudaMemcpyDeviceToHost, ss));
   DBSRG_TRY(c, cudaStreamSynchronize(ss));
+  if (hs[1] == 3) return set_err(c, DBSRG_EINVAL, "non-finite coefficient in list");
   if (hs[1]) return set_err(c, DBSRG_ERANGE, "channel or orbital index out of range in list");
   const int nseg = hs[0];
   if (nseg < 1 || nseg > n) return set_err(c, DBSRG_ECUDA, "inconsistent segment count");

@@ -418,6 +418,21 @@ int dbsrg_set_tuning(dbsrg_ctx *c, const char *name, int value) {
   return DBSRG_OK;
 }
 
+int dbsrg_set_wait_limit(dbsrg_ctx *c, long long ns) {
+  if (!c) return DBSRG_EINVAL;
+  if (ns < 1000 || ns > 60000000000LL) return set_err(c, DBSRG_ERANGE, "wait limit: 1 us .. 60 s");
+  SETTLE(c);
+  c->wait_ns = (unsigned long long)ns;
+  return DBSRG_OK;
+}
+
+int dbsrg_inject_wait_timeout(dbsrg_ctx *c, int enable) {
+  if (!c) return DBSRG_EINVAL;
+  SETTLE(c);
+  c->inject_wait = enable != 0;
+  return DBSRG_OK;
+}
+
 int dbsrg_get_tuning(const dbsrg_ctx *c, const char *name, int *value) {
   if (!c || !name || !value) return DBSRG_EINVAL;
   if (!strcmp(name, "xchunk")) *value = c->tune_xchunk;

@@ -43,6 +43,8 @@ constexpr int TILE = 32 * 32;                   // BF16 elements of a 32-row dig
 constexpr uint32_t A_BYTES = 4 * TILE * 2;      // one slice of a 128-row operand
 constexpr uint32_t B_BYTES = TILE * 2;          // one slice of a 32-row operand
 constexpr int MAXT = 4;                         // terms per tile
+// limit of the waits for the kernel's own copies and MMAs before it exits
+// (the pipeline waits use the context's limit, 2 s by default)
 constexpr unsigned long long WAIT_NS = 2000000000ull;
 
 // digits of 8 values (columns 8kg .. 8kg+7 of a 32-wide row, row exponent
@@ -195,6 +197,8 @@ struct XArgs {
   const XQuad *xq;
   double *hch;
   int *err;
+  unsigned long long wait_ns;  // limit of the pipeline waits
+  int inject_wait;             // test: the epilogue first waits on a barrier nobody completes
 };
 
 // one row (quadrant record, x tile): the quadrant's terms, term code
@@ -289,6 +293,7 @@ __global__ void __maxnreg__(96) k_xfused(const XArgs p) {
   double *sband = (double *)(sB + 2 * TS * B_BYTES);  // [MAXT][NDB][128]
   double *shch = sband + (size_t)MAXT * NDB * 128;    // [32 columns][128 rows]
   __shared__ __align__(8) uint64_t bar_ld[2], bar_mma[2], bar_free[2], bar_tile, bar_sfree;
+  __shared__ __align__(8) uint64_t bar_never;  // completed by nobody (the injected timeout)
   __shared__ uint32_t tmem_base;
   __shared__ int s_abort;
   const int tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
@@ -300,6 +305,7 @@ __global__ void __maxnreg__(96) k_xfused(const XArgs p) {
     }
     mbar_init(smem_u32(&bar_tile), 1);
     mbar_init(smem_u32(&bar_sfree), NCW);
+    mbar_init(smem_u32(&bar_never), 1);
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     s_abort = 0;
   }
@@ -342,7 +348,7 @@ __global__ void __maxnreg__(96) k_xfused(const XArgs p) {
             }
             const int b = q & 1;
             const uint32_t n = q >> 1;
-            if (q >= 2 && !mbar_wait(smem_u32(&bar_mma[b]), (n - 1) & 1, WAIT_NS)) {
+            if (q >= 2 && !mbar_wait(smem_u32(&bar_mma[b]), (n - 1) & 1, p.wait_ns)) {
               fail = true;
               break;
             }
@@ -365,12 +371,12 @@ __global__ void __maxnreg__(96) k_xfused(const XArgs p) {
             }
             keyA[b] = akey;
             ld_pend = q;
-            if (!mbar_wait(la, n & 1, WAIT_NS)) {
+            if (!mbar_wait(la, n & 1, p.wait_ns)) {
               fail = true;
               break;
             }
             ld_pend = -1;
-            if (q >= 2 && !mbar_wait(smem_u32(&bar_free[b]), (n - 1) & 1, WAIT_NS)) {
+            if (q >= 2 && !mbar_wait(smem_u32(&bar_free[b]), (n - 1) & 1, p.wait_ns)) {
               fail = true;
               break;
             }
@@ -426,7 +432,7 @@ __global__ void __maxnreg__(96) k_xfused(const XArgs p) {
           const int ty0 = ty * 32, ncol = min(32, p.ns - ty0);
           // the consumers release the buffers of the previous tile
           bool ok = *abort_flag == 0 &&
-                    (nst == 0 || mbar_wait(smem_u32(&bar_sfree), (nst - 1) & 1, WAIT_NS));
+                    (nst == 0 || mbar_wait(smem_u32(&bar_sfree), (nst - 1) & 1, p.wait_ns));
           ok = __all_sync(0xffffffffu, ok);
           if (!ok) {
             fail = true;
@@ -477,6 +483,14 @@ __global__ void __maxnreg__(96) k_xfused(const XArgs p) {
     // sum to FP64 once.
     const int lg = warp & 3, cg = warp >> 2, xl = lg * 32 + lane;
     bool dead = false;
+    if (p.inject_wait) {  // a wait that runs out: the kernel must abort cleanly
+      const bool ok = __all_sync(0xffffffffu, mbar_wait(smem_u32(&bar_never), 0, p.wait_ns));
+      if (!ok) {
+        dead = true;
+        *abort_flag = 1;
+        if (lane == 0) atomicExch(p.err, 1);
+      }
+    }
     uint32_t q = 0, ntile = 0;
     Row r;
     long long Iacc[CPT];
@@ -545,7 +559,7 @@ __global__ void __maxnreg__(96) k_xfused(const XArgs p) {
           // the product's far field: y - x >= FAR (sg = 1) or x - y >= FAR (sg = -1)
           const int sg = (tra ^ m) ? -1 : 1;
           if (!dead && *abort_flag) dead = true;
-          bool ok = !dead && mbar_wait(smem_u32(&bar_mma[b]), n & 1, WAIT_NS);
+          bool ok = !dead && mbar_wait(smem_u32(&bar_mma[b]), n & 1, p.wait_ns);
           ok = __all_sync(0xffffffffu, ok);
           if (!ok) {
             if (!dead) {
@@ -607,7 +621,7 @@ __global__ void __maxnreg__(96) k_xfused(const XArgs p) {
         for (int c = 0; c < CPT; c++)
           val[c] = cur[c] > -100000 ? i64_to_f64(Iacc[c], cur[c] - 8 * (TS + 1) - r.half) : 0.0;
         if (bulk) {
-          const bool ok = dead || mbar_wait(smem_u32(&bar_tile), ntile & 1, WAIT_NS);
+          const bool ok = dead || mbar_wait(smem_u32(&bar_tile), ntile & 1, p.wait_ns);
           if (!ok) {
             dead = true;
             *abort_flag = 1;
@@ -801,6 +815,8 @@ int split_exchange(dbsrg_ctx *c, const SplitExchange &x) {
   p.xq = x.xq;
   p.hch = hch_base(c);
   p.err = c->kerr;
+  p.wait_ns = c->wait_ns;
+  p.inject_wait = c->inject_wait ? 1 : 0;
   const size_t smem = 2 * TS * (size_t)(A_BYTES + B_BYTES) +
                       ((size_t)MAXT * NDB * 128 + 32 * 128) * sizeof(double);
   DBSRG_TRY(c, cudaFuncSetAttribute(k_xfused, cudaFuncAttributeMaxDynamicSharedMemorySize,

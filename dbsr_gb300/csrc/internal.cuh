@@ -138,6 +138,11 @@ struct dbsrg_ctx {
   // waits (dbsrg_sync, the read-outs, state changes)
   bool async = false;
   bool pending = false;
+  // limit of the tensor-core kernels' pipeline waits, and the test switch
+  // that makes one of them run out (dbsrg_set_wait_limit,
+  // dbsrg_inject_wait_timeout)
+  unsigned long long wait_ns = 2000000000ull;
+  bool inject_wait = false;
   // cuSOLVER / cuBLAS handles of the channel basis (basis.cu), made on use
   void *sv_handle = nullptr, *bl_handle = nullptr;
   // tuning (dbsrg_set_tuning): segments per chunk of the factored exchange

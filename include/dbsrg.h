@@ -265,6 +265,16 @@ int dbsrg_sync(dbsrg_ctx *ctx);
 int dbsrg_set_tuning(dbsrg_ctx *ctx, const char *name, int value);
 int dbsrg_get_tuning(const dbsrg_ctx *ctx, const char *name, int *value);
 
+/* Failure detection of the tensor-core exchange: every wait of its
+ * pipeline gives up after a limit (2 s by default; 1 us .. 60 s here), the
+ * kernel then drains its own copies and MMAs, frees its TMEM and returns,
+ * and the call reports DBSRG_ETIMEOUT with the context usable.
+ * dbsrg_inject_wait_timeout(ctx, 1) makes the epilogue warps first wait on a
+ * barrier that nothing completes (a test of that path, no reference
+ * counterpart). */
+int dbsrg_set_wait_limit(dbsrg_ctx *ctx, long long ns);
+int dbsrg_inject_wait_timeout(dbsrg_ctx *ctx, int enable);
+
 /* Asynchronous mode (off by default; no reference counterpart -- Gen_matrix
  * returns with the matrix updated, gen_matrix.f90:2-17).  When on,
  * dbsrg_gen_matrix returns once the list's kernels are queued: the host-side
