@@ -883,13 +883,16 @@ int plan_list(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const int *ip
 }
 
 // window w of a planned list on the contraction stream; hch_base(c) must
-// address that window's blocks
-int exec_list(dbsrg_ctx *c, const ListPlan &P, int w) {
+// address that window's blocks.  prep: build (or find) the tables, pair
+// potentials and digit caches that any window of the list reads, and launch
+// nothing else (every chunk of a list reads the same ones)
+int exec_list(dbsrg_ctx *c, const ListPlan &P, int w, bool prep = false) {
   const DeviceGrid &g = c->g;
   const int ns = g.ns, ks = g.ks, ms = g.ms;
   cudaStream_t st = c->stream;
   int rc;
   if (P.icase == 0) {
+    if (prep) return DBSRG_OK;
     const int t0 = P.wtl[w], nt = P.wtl[w + 1] - t0;
     if (nt <= 0) return DBSRG_OK;
     DBSRG_RUN(c, "k_vch", k_vch<<<(2 * ns * c->nbf + 255) / 256, 256, 0, st>>>(
@@ -904,8 +907,9 @@ int exec_list(dbsrg_ctx *c, const ListPlan &P, int w) {
     }
     return DBSRG_OK;
   }
-  const int c0 = P.wchunk[w], c1 = P.wchunk[w + 1];
-  const int o0 = P.wown[w], nown_acf = P.wown[w + 1] - o0;
+  const int nwp = (int)P.wchunk.size() - 1;
+  const int c0 = prep ? 0 : P.wchunk[w], c1 = prep ? P.wchunk[nwp] : P.wchunk[w + 1];
+  const int o0 = prep ? 0 : P.wown[w], nown_acf = (prep ? P.wown[nwp] : P.wown[w + 1]) - o0;
   if (c0 == c1 && nown_acf == 0) return DBSRG_OK;
   // tables of the case (cached after the first use)
   const double *tabs[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -934,7 +938,7 @@ int exec_list(dbsrg_ctx *c, const ListPlan &P, int w) {
     int rc2;
     if (P.factored) {
       double *Y = nullptr;
-      if (icv >= 3 && !P.split_x) {
+      if (icv >= 3 && !P.split_x && !prep) {
         if ((rc2 = ensure_scratch(c, sizeof(double) * per * na * nm))) return rc2;
         Y = (double *)c->scratch;
       }
@@ -967,8 +971,10 @@ int exec_list(dbsrg_ctx *c, const ListPlan &P, int w) {
       job.xq = ch.nxq ? P.dxq + ch.xoff : nullptr;
       job.hxq = ch.nxq ? P.hxq.data() + ch.xoff : nullptr;
       job.nxq = ch.nxq;
+      job.prep = prep;
       return factored_contract(c, job);
     }
+    if (prep) return DBSRG_OK;
     if ((rc2 = ensure_scratch(c, 2 * sizeof(double) * per * na * nm))) return rc2;
     double *X = (double *)c->scratch;
     double *Y = X + per * na * nm;
@@ -1001,15 +1007,49 @@ int exec_list(dbsrg_ctx *c, const ListPlan &P, int w) {
                                             hch_base(c)));
     return DBSRG_OK;
   };
-  for (int k = c0; k < c1; k++)
+  for (int k = c0; k < (prep ? std::min(c1, c0 + 1) : c1); k++)
     if ((rc = run_chunk(P.chunks[k]))) return rc;
   if (nown_acf > 0) {
     const double *quad;
     if ((rc = get_quad(c, P.kpol, &quad))) return rc;
+    if (prep) return DBSRG_OK;
     DBSRG_RUN(c, "k_acf",
               k_acf<<<(nown_acf + 127) / 128, 128, 0, st>>>(
                   nown_acf, P.work + P.own_off + o0, P.info, P.kpol, c->nbf, P.lk2, P.lk3, P.lcd,
                   quad, c->acf, c->iicc));
+  }
+  return DBSRG_OK;
+}
+
+// The cached inputs of a planned list, built on the table stream of its k;
+// the contraction stream waits for them.  overlap: the contraction stream
+// holds nothing the builds read (only the kernels of earlier lists of this
+// assembly), so they may run beside it.
+int prepare_list(dbsrg_ctx *c, const ListPlan &P, bool overlap) {
+  if (P.icase == 0) return DBSRG_OK;
+  int rc;
+  if (P.factored && !c->brows) {  // shared by the builds of every k
+    if ((rc = ensure_bound_rows(c))) return rc;
+    overlap = false;
+  }
+  if (!overlap || c->stream_built || c->timing) {
+    // timing mode keeps the builds apart from the contraction kernels, so
+    // that each kernel's events time it alone
+    DBSRG_TRY(c, cudaEventRecord(c->sready, c->stream));
+    for (cudaStream_t b : c->bstream) DBSRG_TRY(c, cudaStreamWaitEvent(b, c->sready, 0));
+    c->stream_built = false;
+  }
+  const int bs = P.kpol & 1;
+  const cudaStream_t keep = c->stream;
+  c->stream = c->bstream[bs];
+  rc = exec_list(c, P, 0, true);
+  c->stream = keep;
+  if (rc) return rc;
+  DBSRG_TRY(c, cudaEventRecord(c->tready[bs], c->bstream[bs]));
+  DBSRG_TRY(c, cudaStreamWaitEvent(c->stream, c->tready[bs], 0));
+  if (c->timing) {  // the other table stream joins too (nothing else runs beside)
+    DBSRG_TRY(c, cudaEventRecord(c->tready[bs ^ 1], c->bstream[bs ^ 1]));
+    DBSRG_TRY(c, cudaStreamWaitEvent(c->stream, c->tready[bs ^ 1], 0));
   }
   return DBSRG_OK;
 }
@@ -1042,6 +1082,7 @@ int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const 
     DBSRG_TRY(c, cudaEventRecord(c->lready, ss));
     DBSRG_TRY(c, cudaStreamWaitEvent(st, c->lready, 0));
   }
+  if ((rc = prepare_list(c, P, pipe && c->pending))) return rc;
   if ((rc = exec_list(c, P, 0))) return rc;
   // the kernels of this call are done with the list state after this point
   DBSRG_TRY(c, cudaEventRecord(c->lfree[par], st));
@@ -1074,6 +1115,7 @@ int assemble_windows(dbsrg_ctx *c, int nlists, const dbsrg_list *lists, int nwin
     // the set-up of list l+1 overlaps the kernels of list l
     enter(0);
     if ((rc = before(0, c->hch))) return rc;
+    bool prepared = false;  // the builds of the first list wait for the stream
     for (int l = 0; l < nlists; l++) {
       const dbsrg_list &L = lists[l];
       if (L.ncdata < 0) return set_err(c, DBSRG_EINVAL, "ncdata < 0");
@@ -1086,6 +1128,8 @@ int assemble_windows(dbsrg_ctx *c, int nlists, const dbsrg_list *lists, int nwin
         return rc;
       DBSRG_TRY(c, cudaEventRecord(c->lready, c->sstream));
       DBSRG_TRY(c, cudaStreamWaitEvent(c->stream, c->lready, 0));
+      if ((rc = prepare_list(c, plans[l], prepared))) return rc;
+      prepared = true;
       if ((rc = exec_list(c, plans[l], 0))) return rc;
     }
     if ((rc = after(0, 1, std::min(nwin, iicc), c->hch))) return rc;

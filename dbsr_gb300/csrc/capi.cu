@@ -48,6 +48,8 @@ int copy_in(dbsrg_ctx *c, void *dst, const void *src, size_t n) {
 int drain(dbsrg_ctx *c) {
   c->pending = false;
   if (c->sstream) DBSRG_TRY(c, cudaStreamSynchronize(c->sstream));
+  for (cudaStream_t b : c->bstream)
+    if (b) DBSRG_TRY(c, cudaStreamSynchronize(b));
   DBSRG_TRY(c, cudaStreamSynchronize(c->stream));
   if (!c->kerr) return DBSRG_OK;
   int h = 0;
@@ -117,8 +119,8 @@ int ensure_tscratch(dbsrg_ctx *c, size_t bytes) {
 int ensure_tcscratch(dbsrg_ctx *c, size_t bytes) {
   return grow(c, &c->tcscratch, &c->tcscratch_bytes, bytes);
 }
-int ensure_pscratch(dbsrg_ctx *c, size_t bytes) {
-  return grow(c, &c->pscratch, &c->pscratch_bytes, bytes);
+int ensure_pscratch(dbsrg_ctx *c, int which, size_t bytes) {
+  return grow(c, &c->pscratch[which], &c->pscratch_bytes[which], bytes);
 }
 void *cache_alloc(dbsrg_ctx *c, size_t bytes) {
   auto it = c->pool.find(bytes);
@@ -247,8 +249,15 @@ int dbsrg_create(dbsrg_ctx **out, const dbsrg_grid_desc *d) {
     delete c;
     return DBSRG_ECUDA;
   }
+  int prio_lo = 0, prio_hi = 0;
+  cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
   if (cudaStreamCreateWithFlags(&c->sstream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaStreamCreateWithFlags(&c->cstream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithPriority(&c->bstream[0], cudaStreamNonBlocking, prio_hi) != cudaSuccess ||
+      cudaStreamCreateWithPriority(&c->bstream[1], cudaStreamNonBlocking, prio_hi) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->tready[0], cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->tready[1], cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->sready, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->cdone[0], cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->cdone[1], cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->wdone, cudaEventDisableTiming) != cudaSuccess ||
@@ -282,6 +291,8 @@ int dbsrg_destroy(dbsrg_ctx *c) {
   cudaSetDevice(c->device);
   if (c->sstream) cudaStreamSynchronize(c->sstream);
   if (c->cstream) cudaStreamSynchronize(c->cstream);
+  for (cudaStream_t b : c->bstream)
+    if (b) cudaStreamSynchronize(b);
   if (c->stream) cudaStreamSynchronize(c->stream);
   basis_release(c);
   free_tables(c);
@@ -301,13 +312,14 @@ int dbsrg_destroy(dbsrg_ctx *c) {
   if (c->tscratch) cudaFree(c->tscratch);
   if (c->fscratch) cudaFree(c->fscratch);
   if (c->tcscratch) cudaFree(c->tcscratch);
-  if (c->pscratch) cudaFree(c->pscratch);
+  for (void *p : c->pscratch)
+    if (p) cudaFree(p);
   for (int i = 0; i < 2; i++) {
     if (c->lstate[i]) cudaFree(c->lstate[i]);
     if (c->lfree[i]) cudaEventDestroy(c->lfree[i]);
   }
   if (c->lready) cudaEventDestroy(c->lready);
-  for (cudaEvent_t e : {c->cdone[0], c->cdone[1], c->wdone})
+  for (cudaEvent_t e : {c->cdone[0], c->cdone[1], c->wdone, c->tready[0], c->tready[1], c->sready})
     if (e) cudaEventDestroy(e);
   if (c->kerr) cudaFree(c->kerr);
   if (c->bmap) cudaFree(c->bmap);
@@ -317,6 +329,8 @@ int dbsrg_destroy(dbsrg_ctx *c) {
   for (cudaEvent_t e : c->evpool) cudaEventDestroy(e);
   if (c->sstream) cudaStreamDestroy(c->sstream);
   if (c->cstream) cudaStreamDestroy(c->cstream);
+  for (cudaStream_t b : c->bstream)
+    if (b) cudaStreamDestroy(b);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return DBSRG_OK;

@@ -731,8 +731,9 @@ static void xfused_work(const XQuad *hxq, int nxq, int ns, int lower, double &by
 int split_exchange(dbsrg_ctx *c, const SplitExchange &x) {
   const int ns = c->g.ns, nb = c->nbound;
   if (nb < 1 || nb > 32) return set_err(c, DBSRG_EINVAL, "split exchange: 1..32 bound orbitals");
-  if (x.na < 1 || x.na > 4 || x.nm < 1 || x.nxq < 1) return DBSRG_OK;
+  if (x.na < 1 || x.na > 4 || x.nm < 1 || (x.nxq < 1 && !x.prep)) return DBSRG_OK;
   cudaStream_t st = c->stream;
+  int rc0;
   const int ntx = (ns + 127) / 128, NR = 4 * ntx, nty = (ns + 31) / 32;
   const size_t sl = (size_t)NR * TILE;
   // digits of U (and Ul) per table, cached with the far-field vectors
@@ -752,6 +753,16 @@ int split_exchange(dbsrg_ctx *c, const SplitExchange &x) {
                 k_udigits<<<(unsigned)((NR * 32 + 127) / 128), 128, 0, st>>>(
                     ns, nb, NR, m ? f->Ul : f->U, (__nv_bfloat16 *)f->Ud + (size_t)m * TS * sl,
                     f->eu + (size_t)m * NR * EXP_PER_ROWTILE));
+  }
+  const size_t mv = (size_t)ns * nb;
+  if (x.prep) {  // float-float far-field vectors, then nothing per chunk
+    for (int a = 0; a < x.na; a++) {
+      const float2 *v;
+      if (x.lower && !x.far[a]->Vl) return set_err(c, DBSRG_EINVAL, "split exchange: no lower field");
+      if ((rc0 = ff_of(c, x.far[a]->V, mv, &v))) return rc0;
+      if (x.lower && (rc0 = ff_of(c, x.far[a]->Vl, mv, &v))) return rc0;
+    }
+    return DBSRG_OK;
   }
   // per chunk: Z digits, exponents, band rows, error word
   const size_t zel = (size_t)x.na * 2 * x.nm * TS * sl;
@@ -776,7 +787,6 @@ int split_exchange(dbsrg_ctx *c, const SplitExchange &x) {
   z.nm = x.nm;
   z.lower = x.lower;
   if (!x.cdf) return set_err(c, DBSRG_EINVAL, "split exchange: no float-float coefficients");
-  const size_t mv = (size_t)ns * nb;
   for (int a = 0; a < x.na; a++) {
     if (x.lower && !x.far[a]->Vl) return set_err(c, DBSRG_EINVAL, "split exchange: no lower field");
     if ((rc = ff_of(c, x.far[a]->V, mv, &z.V[a]))) return rc;

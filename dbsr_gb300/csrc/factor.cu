@@ -536,8 +536,8 @@ __global__ void __launch_bounds__(256) k_pair_diag(int ns, int ks, int kk, int n
       if (qp < 0) continue;
       const S *p = w1 + (size_t)a * k1;
       const S *h = H + (size_t)po * k1 * PBC;
-      double s[PBC];
-      if constexpr (FF) {
+      const size_t d0 = ((size_t)ph * npair + (size_t)a * nb + b0) * per + qp;
+      if constexpr (FF) {  // kept as float-float pairs (no FP64 conversion)
         float sh[PBC], sl[PBC];
 #pragma unroll
         for (int bb = 0; bb < PBC; bb++) sh[bb] = sl[bb] = 0.0f;
@@ -547,9 +547,12 @@ __global__ void __launch_bounds__(256) k_pair_diag(int ns, int ks, int kk, int n
           for (int bb = 0; bb < PBC; bb++)
             if (bb < bc) ffa::mac(pv, h[(size_t)g1 * PBC + bb], sh[bb], sl[bb]);
         }
+        float2 *D = reinterpret_cast<float2 *>(Dq);
 #pragma unroll
-        for (int bb = 0; bb < PBC; bb++) s[bb] = ffa::value(sh[bb], sl[bb]);
+        for (int bb = 0; bb < PBC; bb++)
+          if (bb < bc) D[d0 + (size_t)bb * per] = ffa::norm(sh[bb], sl[bb]);
       } else {
+        double s[PBC];
 #pragma unroll
         for (int bb = 0; bb < PBC; bb++) s[bb] = 0.0;
         for (int g1 = 0; g1 < k1; g1++) {
@@ -558,10 +561,10 @@ __global__ void __launch_bounds__(256) k_pair_diag(int ns, int ks, int kk, int n
           for (int bb = 0; bb < PBC; bb++)
             if (bb < bc) s[bb] = fma(pv, h[(size_t)g1 * PBC + bb], s[bb]);
         }
-      }
 #pragma unroll
-      for (int bb = 0; bb < PBC; bb++)
-        if (bb < bc) Dq[((size_t)ph * npair + (size_t)a * nb + b0 + bb) * per + qp] = s[bb];
+        for (int bb = 0; bb < PBC; bb++)
+          if (bb < bc) Dq[d0 + (size_t)bb * per] = s[bb];
+      }
     }
     __syncthreads();
   }
@@ -581,6 +584,7 @@ __global__ void k_pair_direct_final(int ns, int ks, int nv, int kk, int nb, int 
   const int f = (int)(t % ns) + 1, col = (int)(t / ns) + 1;
   const int s2 = sym == 's' ? f + col - 1 : f + col - ks;
   double acc = 0.0;
+  float dh = 0.0f, dl = 0.0f;  // float-float diagonal-cell parts (FF)
   if (s2 >= 1 && s2 <= ns) {
     const int lo = max(max(1, f - eo.k1 + 1), s2 - eo.k2 + 1), hi = min(min(nv, f), s2);
     const double *sa = SA + (size_t)pair * nv;
@@ -593,11 +597,15 @@ __global__ void k_pair_direct_final(int ns, int ks, int nv, int kk, int nb, int 
       } else {
         acc = fma(hi2[o], sa[cv - 1], acc);
       }
-      acc += Dq[((size_t)((cv - 1) % FAR) * npair + pair) * per + t];
+      const size_t dq = ((size_t)((cv - 1) % FAR) * npair + pair) * per + t;
+      if constexpr (FF)
+        ffa::add(reinterpret_cast<const float2 *>(Dq)[dq], dh, dl);
+      else
+        acc += Dq[dq];
     }
   }
   if constexpr (FF)
-    static_cast<float2 *>(Kout)[(size_t)pair * per + t] = ffa::split(acc);
+    static_cast<float2 *>(Kout)[(size_t)pair * per + t] = ffa::split(acc + ffa::value(dh, dl));
   else
     static_cast<double *>(Kout)[(size_t)pair * per + t] = acc;
 }
@@ -881,6 +889,8 @@ static int ensure_brows(dbsrg_ctx *c) {
   return DBSRG_OK;
 }
 
+int ensure_bound_rows(dbsrg_ctx *c) { return ensure_brows(c); }
+
 static long long pairpot_key(int kind, int family, int type, int k, int icv, int jp1, int jp2,
                              bool ff) {
   return (long long)kind | (long long)family << 1 | (long long)type << 2 | (long long)icv << 5 |
@@ -933,8 +943,10 @@ int get_pairpot_direct_any(dbsrg_ctx *c, int family, int type, int k, int icv, i
   const double *M2 = (icv == 1 && family == 0) ? cd->lo2 : nullptr;
   // scratch: SA, SB (npair x nv), Dq (9 x npair x per)
   const size_t sbytes = (2 * npair * nv + (size_t)FAR * npair * per) * sizeof(double);
-  if ((rc = ensure_pscratch(c, sbytes))) return rc;
-  double *SA = (double *)c->pscratch, *SB = SA + npair * nv, *Dq = SB + npair * nv;
+  const int ps = c->stream == c->bstream[1] ? 1 : 0;  // scratch of this stream
+  if (c->stream != c->bstream[0] && c->stream != c->bstream[1]) c->stream_built = true;
+  if ((rc = ensure_pscratch(c, ps, sbytes))) return rc;
+  double *SA = (double *)c->pscratch[ps], *SB = SA + npair * nv, *Dq = SB + npair * nv;
   double *K = nullptr;  // doubles, or as many float2 pairs (same bytes)
   if (!(K = (double *)cache_alloc(c, npair * per * sizeof(double)))) {
     cudaGetLastError();
@@ -1104,7 +1116,19 @@ int factored_contract(dbsrg_ctx *c, const FactorJob &j) {
     x.pairs = j.pairs;
     x.cd = j.cd;
     x.cdf = j.cdf;
+    x.prep = j.prep;
     return split_exchange(c, x);
+  }
+  if (j.icv >= 3 && j.prep) {
+    for (int a = 0; a < j.na; a++) {
+      const FarField *f;
+      const void *Kb;
+      if ((rc = get_farfield(c, j.family, j.types[a], j.kpol, j.icv, &f))) return rc;
+      if ((rc = get_pairpot_band(c, j.family, j.types[a], j.kpol, j.icv, j.jp1[a], j.jp2[a],
+                                 j.tabs[a], false, &Kb)))
+        return rc;
+    }
+    return DBSRG_OK;
   }
   if (j.icv >= 3) {
     const size_t per = (size_t)ns * ns;
@@ -1155,6 +1179,7 @@ int factored_contract(dbsrg_ctx *c, const FactorJob &j) {
                               &kd.K[a]);
     if (rc) return rc;
   }
+  if (j.prep) return DBSRG_OK;
   const size_t space = (size_t)4 * ns * (2 * ks - 1);
   dim3 gs((unsigned)((space + 255) / 256), (unsigned)j.nown);
   if (j.split && j.cdf)

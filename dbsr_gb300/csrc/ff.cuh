@@ -34,6 +34,15 @@ __device__ __forceinline__ void mac(float2 c, float2 k, float &sh, float &sl) {
   sl = sl + (e + x);
 }
 
+// (sh, sl) += v for a float-float v (TwoSum of the high parts)
+__device__ __forceinline__ void add(float2 v, float &sh, float &sl) {
+  const float s = sh + v.x;
+  const float bp = s - sh;
+  const float e = (sh - (s - bp)) + (v.x - bp);
+  sh = s;
+  sl = sl + (e + v.y);
+}
+
 __device__ __forceinline__ double value(float sh, float sl) { return (double)sh + (double)sl; }
 
 // (hi, lo) renormalised so that lo is below half an ulp of hi (Fast2Sum)

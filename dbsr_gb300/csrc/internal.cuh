@@ -119,8 +119,9 @@ struct dbsrg_ctx {
   size_t fscratch_bytes = 0;
   void *tcscratch = nullptr;  // tensor-core far field (digit slices, scales)
   size_t tcscratch_bytes = 0;
-  void *pscratch = nullptr;   // pair-potential construction (cell sums, cell parts)
-  size_t pscratch_bytes = 0;
+  // pair-potential construction (cell sums, cell parts), one per table stream
+  void *pscratch[2] = {nullptr, nullptr};
+  size_t pscratch_bytes[2] = {0, 0};
   // List pipeline.  The state of one Gen_matrix call (the list in IPT order,
   // segments, chunk members, quadrant records) lives in one of two buffers,
   // alternating per call.  Its set-up (copies, segment kernels, read-backs)
@@ -133,6 +134,22 @@ struct dbsrg_ctx {
   cudaEvent_t lfree[2] = {nullptr, nullptr};
   cudaEvent_t lready = nullptr;
   int lpar = 0;
+  // Table streams.  The tables, cell data, far fields, digits and pair
+  // potentials that a list's contraction reads are built on one of two
+  // table streams (the higher priority) before the contraction, which waits
+  // for them (tready).  The stream is chosen by the parity of the list's k:
+  // everything built for one k (cell data, tables, far fields, digits,
+  // quadratures) stays on one stream, and the builds for neighbouring k run
+  // side by side, and beside the kernels of earlier lists.  The bound-orbital
+  // rows (shared by every k) are built on the contraction stream first.
+  // When the contraction stream may hold work the builds read (the first
+  // list after a state change, the timing mode), both table streams first
+  // wait for it (sready).  A pair-potential build made on the contraction
+  // stream itself sets stream_built, with the same effect at the next
+  // preparation, since it shares pscratch[0].
+  cudaStream_t bstream[2] = {nullptr, nullptr};
+  cudaEvent_t tready[2] = {nullptr, nullptr}, sready = nullptr;
+  bool stream_built = false;
   // asynchronous mode (dbsrg_set_async): Gen_matrix returns once its kernels
   // are queued; failures of queued kernels surface at the next call that
   // waits (dbsrg_sync, the read-outs, state changes)
@@ -243,7 +260,8 @@ bool is_device_ptr(const void *p);
 // copies n bytes from a host-or-device pointer into device memory dst
 int copy_in(dbsrg_ctx *c, void *dst, const void *src, size_t n);
 int copy_in_s(dbsrg_ctx *c, void *dst, const void *src, size_t n, cudaStream_t s);
-// waits for both streams and reports failures of queued kernels
+// waits for the set-up, table and contraction streams and reports failures of
+// queued kernels
 int drain(dbsrg_ctx *c);
 int ensure_lstate(dbsrg_ctx *c, int par, size_t bytes);
 // cache buffers through the pool (nullptr when the device is out of memory)
@@ -256,7 +274,9 @@ int ensure_scratch(dbsrg_ctx *c, size_t bytes);
 int ensure_scratch2(dbsrg_ctx *c, size_t bytes);
 int ensure_tscratch(dbsrg_ctx *c, size_t bytes);
 int ensure_tcscratch(dbsrg_ctx *c, size_t bytes);
-int ensure_pscratch(dbsrg_ctx *c, size_t bytes);
+int ensure_pscratch(dbsrg_ctx *c, int which, size_t bytes);
+// the bound-orbital rows of both components (factor.cu), built once per orbital set
+int ensure_bound_rows(dbsrg_ctx *c);
 int ensure_pinned(dbsrg_ctx *c, size_t bytes);
 // frees the far-field vectors, pair potentials and bound rows (they depend
 // on the orbitals and the tables)
@@ -320,6 +340,7 @@ struct FactorJob {
   int nxq;           // split exchange: (owner block, quadrant) records of the chunk
   const struct XQuad *xq;
   const struct XQuad *hxq;  // host copy of the records (work accounting)
+  bool prep;         // build (or find) the cached inputs only, launch no contraction
 };
 int factored_contract(dbsrg_ctx *c, const FactorJob &job);
 // One quadrant of one owner's block in the split exchange and the terms it
@@ -349,6 +370,7 @@ struct SplitExchange {
   const int *pairs;
   const double *cd;
   const float2 *cdf;  // the coefficients as float-float pairs
+  bool prep;          // build the digit and float-float caches only
 };
 int split_exchange(dbsrg_ctx *c, const SplitExchange &x);
 // Direct pair potentials of table (family, type, k) for convol case icv with

@@ -192,8 +192,8 @@ __global__ void k_moments(int nv, int ks, int k1, int k2, int sym, int k, const 
     double w = grw[IDX2(iv, m, nv)];
     if (k > 0) w = __dmul_rn(grw[IDX2(iv, m, nv)], ipow_d(gr[IDX2(iv, m, nv)], k));
     if (k < 0) w = __dmul_rn(grw[IDX2(iv, m, nv)], ipow_d(grm[IDX2(iv, m, nv)], -k));
-    double b2 = __dmul_rn(b2s[IDX3(iv, m, j, nw, ks)], w);
-    s = __dadd_rn(s, __dmul_rn(b1s[IDX3(iv, m, i, nw, ks)], b2));
+    const double b2 = __dmul_rn(b2s[IDX3(iv, m, j, nw, ks)], w);
+    s = fma(b1s[IDX3(iv, m, i, nw, ks)], b2, s);
   }
   rkm[q] = s;
 }
@@ -291,17 +291,22 @@ __global__ void k_triang(int nv, int ks, int ksp, int ksq, int type, int k, cons
     gxo[m] = __dmul_rn(grw[IDX2(iv, m, nv)], ipow_d(grm[IDX2(iv, m, nv)], k + 1));
   __syncthreads();
   // phase 2: INT(j,jp,m) = sum_i (wk*Ba_j)*Bb_jp
+  // (the weighted first factors wk*Ba are formed once per call in A, which
+  // phase 3 fills only after the last call)
   auto inner = [&](const double *Ba, int ka, const double *Bb, int kb, double *INT) {
+    double *WB = A;
+    for (int q = threadIdx.x; q < KS2 * ka; q += blockDim.x) WB[q] = __dmul_rn(wk[q / ka], Ba[q]);
+    __syncthreads();
     for (int q = threadIdx.x; q < ka * kb * ks; q += blockDim.x) {
       int j = q % ka, jp = (q / ka) % kb, m = q / (ka * kb);
       double s = 0.0;
       for (int i = 0; i < ks; i++) {
         int p = m * ks + i;
-        double gwl = __dmul_rn(wk[p], Ba[(size_t)p * ka + j]);
-        s = __dadd_rn(s, __dmul_rn(gwl, Bb[(size_t)p * kb + jp]));
+        s = fma(WB[(size_t)p * ka + j], Bb[(size_t)p * kb + jp], s);
       }
       INT[j + ka * (jp + kb * m)] = s;
     }
+    __syncthreads();
   };
   if (type == 0) inner(BP, ksp, BP, ksp, INTP);
   if (type == 1) inner(BQ, ksq, BQ, ksq, INTQ);
@@ -360,8 +365,7 @@ __global__ void k_triang(int nv, int ks, int ksp, int ksq, int type, int k, cons
       pair_of(jj, kx, &j, &jp);
       const double *o = OB1 + ii * ks;
       double s = 0.0;
-      for (int m = 0; m < ks; m++)
-        s = __dadd_rn(s, __dmul_rn(o[m], INT[j + kx * (jp + kx * m)]));
+      for (int m = 0; m < ks; m++) s = fma(o[m], INT[j + kx * (jp + kx * m)], s);
       A[q] = s;
     }
     __syncthreads();
@@ -381,10 +385,8 @@ __global__ void k_triang(int nv, int ks, int ksp, int ksq, int type, int k, cons
         pair_of(qq_, ksq, &j, &jp);
         const double *o1 = OB1 + pp_ * ks, *o2 = OB2 + qq_ * ks;
         double s1 = 0.0, s2 = 0.0;
-        for (int m = 0; m < ks; m++)
-          s1 = __dadd_rn(s1, __dmul_rn(o1[m], INTQ[j + ksq * (jp + ksq * m)]));
-        for (int m = 0; m < ks; m++)
-          s2 = __dadd_rn(s2, __dmul_rn(o2[m], INTP[i + ksp * (ip + ksp * m)]));
+        for (int m = 0; m < ks; m++) s1 = fma(o1[m], INTQ[j + ksq * (jp + ksq * m)], s1);
+        for (int m = 0; m < ks; m++) s2 = fma(o2[m], INTP[i + ksp * (ip + ksp * m)], s2);
         v = __dadd_rn(s1, s2);
       }
       out[q] = v;
@@ -398,8 +400,7 @@ __global__ void k_triang(int nv, int ks, int ksp, int ksq, int type, int k, cons
         int j = jj / ksq, jp = jj % ksq;
         const double *o = OB1 + ii * ks;
         double s = 0.0;
-        for (int m = 0; m < ks; m++)
-          s = __dadd_rn(s, __dmul_rn(o[m], INTPQ[j + ksp * (jp + ksq * m)]));
+        for (int m = 0; m < ks; m++) s = fma(o[m], INTPQ[j + ksp * (jp + ksq * m)], s);
         v = s;
       }
       out[q] = v;
@@ -472,14 +473,14 @@ __global__ void k_fill_r(int ns, int ks, int nv, int ka, int kb, const double *l
       for (int iv = ivlo; iv <= ivhi; iv++) {
         int ih = i - iv + 1;
         int ii = tri_index(ih, ih + ip - 1, ka);
-        double cc;
         if (iv < jv)
-          cc = __dmul_rn(lowA[(ii - 1) + (size_t)kk * (iv - 1)], highB[(jj - 1) + (size_t)kk * (jv - 1)]);
+          acc = fma(lowA[(ii - 1) + (size_t)kk * (iv - 1)], highB[(jj - 1) + (size_t)kk * (jv - 1)],
+                    acc);
         else if (iv > jv)
-          cc = __dmul_rn(lowB[(jj - 1) + (size_t)kk * (jv - 1)], highA[(ii - 1) + (size_t)kk * (iv - 1)]);
+          acc = fma(lowB[(jj - 1) + (size_t)kk * (jv - 1)], highA[(ii - 1) + (size_t)kk * (iv - 1)],
+                    acc);
         else
-          cc = rkd[(ii - 1) + (size_t)kk * ((jj - 1) + (size_t)kk * (iv - 1))];
-        acc = __dadd_rn(acc, cc);
+          acc += rkd[(ii - 1) + (size_t)kk * ((jj - 1) + (size_t)kk * (iv - 1))];
       }
     }
   }
@@ -523,12 +524,10 @@ __global__ void k_fill_s(int ns, int ks, int nv, int ksp, int ksq, int kj1, int 
       if (iv < 1 || iv > jv) continue;
       int ihp = ip + ih - ks;
       int ii = (ih - 1) * ksq + ihp;
-      double cc;
       if (iv == jv)
-        cc = rkd[(ii - 1) + (size_t)kk * ((jj - 1) + (size_t)kk * (iv - 1))];
+        acc += rkd[(ii - 1) + (size_t)kk * ((jj - 1) + (size_t)kk * (iv - 1))];
       else
-        cc = __dmul_rn(r1[(ii - 1) + (size_t)kk * (iv - 1)], r2[(jj - 1) + (size_t)kk * (jv - 1)]);
-      acc = __dadd_rn(acc, cc);
+        acc = fma(r1[(ii - 1) + (size_t)kk * (iv - 1)], r2[(jj - 1) + (size_t)kk * (jv - 1)], acc);
     }
   }
   rkb[q] = acc;
