@@ -1028,9 +1028,10 @@ int exec_list(dbsrg_ctx *c, const ListPlan &P, int w, bool prep = false) {
 int prepare_list(dbsrg_ctx *c, const ListPlan &P, bool overlap) {
   if (P.icase == 0) return DBSRG_OK;
   int rc;
-  if (P.factored && !c->brows) {  // shared by the builds of every k
-    if ((rc = ensure_bound_rows(c))) return rc;
-    overlap = false;
+  if (P.factored) {  // shared by the builds of every k
+    bool built = false;
+    if ((rc = ensure_bound_rows(c, &built))) return rc;
+    if (built) overlap = false;
   }
   if (!overlap || c->stream_built || c->timing) {
     // timing mode keeps the builds apart from the contraction kernels, so

@@ -128,9 +128,21 @@ __global__ void k_pair_index(int n, const int *k2, const int *k3, const int *bma
 // ---------------------------------------------------------------------------
 // far-field vectors of one electron: Ulo(x,a) = sum_iv sum_xc mlo(pair;iv) p_a(xc)
 // (and Uhi with mhi), x the output function, xc the contracted one.
+// both electrons' vectors in one launch (blockIdx.y)
+struct FarSide {
+  PairSpec e;
+  int out_first, ko, kc, ccomp;
+  const double *mlo, *mhi;
+  double *Ulo, *Uhi;
+};
+
 __global__ void k_far_vectors(int ns, int nv, int kk, int nb, const int *b2o, const double *pq,
-                              PairSpec e, int out_first, int ko, int kc, int ccomp,
-                              const double *mlo, const double *mhi, double *Ulo, double *Uhi) {
+                              const FarSide s0, const FarSide s1) {
+  const FarSide &sd = blockIdx.y ? s1 : s0;
+  const PairSpec e = sd.e;
+  const int out_first = sd.out_first, ko = sd.ko, kc = sd.kc, ccomp = sd.ccomp;
+  const double *mlo = sd.mlo, *mhi = sd.mhi;
+  double *Ulo = sd.Ulo, *Uhi = sd.Uhi;
   int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= ns * nb) return;
   int x = q % ns + 1, a = q / ns;
@@ -390,7 +402,10 @@ __global__ void k_pair_cellsum(int ns, int nv, int kk, int nb, PairSpec ed, cons
 // (2) exclusive suffix (sum over later cells) or prefix sums per pair, one
 // warp per pair: every lane scans a run of cells, the run totals are
 // scanned across the warp by shuffles
-__global__ void k_pair_scan(int nv, int npair, double *S, int suffix) {
+// (blockIdx.y 1: a second array S1 with its own direction, same launch)
+__global__ void k_pair_scan(int nv, int npair, double *S0, int suffix0, double *S1, int suffix1) {
+  double *S = blockIdx.y ? S1 : S0;
+  const int suffix = blockIdx.y ? suffix1 : suffix0;
   const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) / 32), lane = threadIdx.x % 32;
   if (warp >= npair) return;
   double *s = S + (size_t)warp * nv;
@@ -861,15 +876,11 @@ static int get_farfield(dbsrg_ctx *c, int family, int type, int k, int cs, const
   int o2f = cs == 3 ? 0 : 1;
   int ko2 = ord(cs == 3 ? tb.b2 : tb.b1), kc2 = ord(cs == 3 ? tb.b1 : tb.b2);
   int cc2 = cs == 3 ? tb.b1 : tb.b2;
-  unsigned nbk = (unsigned)((m + 127) / 128);
+  const FarSide s1{tb.e1, o1f, ko1, kc1, cc1, cd->lo1, family == 0 ? cd->hi1 : nullptr, f.U, f.Ul};
+  const FarSide s2{tb.e2, o2f, ko2, kc2, cc2, cd->hi2, family == 0 ? cd->lo2 : nullptr, f.V, f.Vl};
+  const dim3 gv((unsigned)((m + 63) / 64), 2);
   DBSRG_RUN(c, "k_far_vectors",
-            k_far_vectors<<<nbk, 128, 0, c->stream>>>(ns, g.nv, kk, nb, c->b2o, c->pq, tb.e1, o1f,
-                                                      ko1, kc1, cc1, cd->lo1,
-                                                      family == 0 ? cd->hi1 : nullptr, f.U, f.Ul));
-  DBSRG_RUN(c, "k_far_vectors",
-            k_far_vectors<<<nbk, 128, 0, c->stream>>>(ns, g.nv, kk, nb, c->b2o, c->pq, tb.e2, o2f,
-                                                      ko2, kc2, cc2, cd->hi2,
-                                                      family == 0 ? cd->lo2 : nullptr, f.V, f.Vl));
+            k_far_vectors<<<gv, 64, 0, c->stream>>>(ns, g.nv, kk, nb, c->b2o, c->pq, s1, s2));
   v[idx] = f;
   *out = &v.at(idx);
   return DBSRG_OK;
@@ -889,7 +900,11 @@ static int ensure_brows(dbsrg_ctx *c) {
   return DBSRG_OK;
 }
 
-int ensure_bound_rows(dbsrg_ctx *c) { return ensure_brows(c); }
+int ensure_bound_rows(dbsrg_ctx *c, bool *built) {
+  if (c->brows) return DBSRG_OK;
+  *built = true;
+  return ensure_brows(c);
+}
 
 static long long pairpot_key(int kind, int family, int type, int k, int icv, int jp1, int jp2,
                              bool ff) {
@@ -960,8 +975,8 @@ int get_pairpot_direct_any(dbsrg_ctx *c, int family, int type, int k, int icv, i
             k_pair_cellsum<<<nv, 256, sm1, st>>>(ns, nv, kk, nb, ed, M1, M2, P1, P2, SA,
                                                  M2 ? SB : nullptr));
   const unsigned gp = (unsigned)((npair * 32 + 255) / 256);
-  DBSRG_RUN(c, "k_pair_scan", k_pair_scan<<<gp, 256, 0, st>>>(nv, (int)npair, SA, icv == 1));
-  if (M2) DBSRG_RUN(c, "k_pair_scan", k_pair_scan<<<gp, 256, 0, st>>>(nv, (int)npair, SB, 0));
+  DBSRG_RUN(c, "k_pair_scan", k_pair_scan<<<dim3(gp, M2 ? 2 : 1), 256, 0, st>>>(
+                                  nv, (int)npair, SA, icv == 1, SB, 0));
   const int npo = eo.sym ? eo.k1 * (eo.k1 + 1) / 2 : eo.k1 * eo.k2;
   const size_t sm3 = ((size_t)nb * (ed.k1 + ed.k2) + (size_t)npo * ed.k1 * ed.k2 +
                       (size_t)npo * ed.k1 * PBC) * sizeof(double) + (size_t)npo * sizeof(int);

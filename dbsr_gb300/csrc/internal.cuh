@@ -140,13 +140,14 @@ struct dbsrg_ctx {
   // for them (tready).  The stream is chosen by the parity of the list's k:
   // everything built for one k (cell data, tables, far fields, digits,
   // quadratures) stays on one stream, and the builds for neighbouring k run
-  // side by side, and beside the kernels of earlier lists.  The bound-orbital
-  // rows (shared by every k) are built on the contraction stream first.
+  // side by side, and beside the kernels of earlier lists.
   // When the contraction stream may hold work the builds read (the first
   // list after a state change, the timing mode), both table streams first
   // wait for it (sready).  A pair-potential build made on the contraction
   // stream itself sets stream_built, with the same effect at the next
-  // preparation, since it shares pscratch[0].
+  // preparation, since it shares pscratch[0].  The bound-orbital rows
+  // (shared by every k) are made on the contraction stream before the first
+  // preparation that needs them.
   cudaStream_t bstream[2] = {nullptr, nullptr};
   cudaEvent_t tready[2] = {nullptr, nullptr}, sready = nullptr;
   bool stream_built = false;
@@ -275,8 +276,9 @@ int ensure_scratch2(dbsrg_ctx *c, size_t bytes);
 int ensure_tscratch(dbsrg_ctx *c, size_t bytes);
 int ensure_tcscratch(dbsrg_ctx *c, size_t bytes);
 int ensure_pscratch(dbsrg_ctx *c, int which, size_t bytes);
-// the bound-orbital rows of both components (factor.cu), built once per orbital set
-int ensure_bound_rows(dbsrg_ctx *c);
+// the bound-orbital rows of both components (factor.cu), built once per
+// orbital set; *built set when they were made now
+int ensure_bound_rows(dbsrg_ctx *c, bool *built);
 int ensure_pinned(dbsrg_ctx *c, size_t bytes);
 // frees the far-field vectors, pair potentials and bound rows (they depend
 // on the orbitals and the tables)

@@ -161,9 +161,20 @@ int build_grid(dbsrg_ctx *c, const double *t_in) {
 // ----------------------------------------------------------------------------
 // Cell moments <B_i|r^k|B_j> per interval: moment_pp/qq/pq/qp,
 // dbsr_lib_dbs.f90:1401-1564.  rkm(ks*ks,nv); pp/qq packed i<=j.
-__global__ void k_moments(int nv, int ks, int k1, int k2, int sym, int k, const double *b1s,
-                          const double *b2s, const double *gr, const double *grm,
-                          const double *grw, double *rkm) {
+// up to four moment arrays per launch (blockIdx.y): the moments of one cell
+// data set
+struct MomentSet {
+  const double *b1s[4], *b2s[4];
+  int k1[4], k2[4], sym[4], k[4];
+  double *rkm[4];
+};
+
+__global__ void k_moments(int nv, int ks, const MomentSet ms, const double *gr,
+                          const double *grm, const double *grw) {
+  const int y = blockIdx.y;
+  const double *b1s = ms.b1s[y], *b2s = ms.b2s[y];
+  const int k1 = ms.k1[y], k2 = ms.k2[y], sym = ms.sym[y], k = ms.k[y];
+  double *rkm = ms.rkm[y];
   int kk = ks * ks;
   int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= kk * nv) return;
@@ -208,15 +219,24 @@ static void basis_of(const DeviceGrid &g, int which, const double **b1, const do
   }
 }
 
-int compute_moments(dbsrg_ctx *c, int which, int k, double *rkm) {
+// n (1..4) moment arrays in one launch: basis pair which[i], power k[i]
+static int compute_moment_set(dbsrg_ctx *c, int n, const int *which, const int *k,
+                              double *const *rkm) {
   const DeviceGrid &g = c->g;
-  const double *b1, *b2;
-  int k1, k2, sym;
-  basis_of(g, which, &b1, &b2, &k1, &k2, &sym);
-  int n = g.ks * g.ks * g.nv;
-  DBSRG_RUN(c, "k_moments", k_moments<<<(n + 127) / 128, 128, 0, c->stream>>>(g.nv, g.ks, k1, k2, sym, k, b1, b2, g.gr,
-                                                   g.grm, g.grw, rkm));
+  MomentSet ms{};
+  for (int i = 0; i < n; i++) {
+    basis_of(g, which[i], &ms.b1s[i], &ms.b2s[i], &ms.k1[i], &ms.k2[i], &ms.sym[i]);
+    ms.k[i] = k[i];
+    ms.rkm[i] = rkm[i];
+  }
+  const int m = g.ks * g.ks * g.nv;
+  DBSRG_RUN(c, "k_moments", k_moments<<<dim3((m + 127) / 128, n), 128, 0, c->stream>>>(
+                                g.nv, g.ks, ms, g.gr, g.grm, g.grw));
   return DBSRG_OK;
+}
+
+int compute_moments(dbsrg_ctx *c, int which, int k, double *rkm) {
+  return compute_moment_set(c, 1, &which, &k, &rkm);
 }
 
 // ----------------------------------------------------------------------------
@@ -567,14 +587,14 @@ int get_celldata(dbsrg_ctx *c, int family, int type, int k, const CellData **out
   int rc;
   if (family == 0) {
     int wa = (type == 0 || type == 2) ? 0 : 1, wb = (type == 0 || type == 3) ? 0 : 1;
-    if ((rc = compute_moments(c, wa, k, cd.lo1))) return rc;
-    if ((rc = compute_moments(c, wa, -(k + 1), cd.hi1))) return rc;
-    if ((rc = compute_moments(c, wb, k, cd.lo2))) return rc;
-    if ((rc = compute_moments(c, wb, -(k + 1), cd.hi2))) return rc;
+    const int wh[4] = {wa, wa, wb, wb}, kp[4] = {k, -(k + 1), k, -(k + 1)};
+    double *const out[4] = {cd.lo1, cd.hi1, cd.lo2, cd.hi2};
+    if ((rc = compute_moment_set(c, 4, wh, kp, out))) return rc;
     if ((rc = compute_diag_cells(c, type, k, cd.rkd))) return rc;
   } else {
-    if ((rc = compute_moments(c, 2, k, cd.lo1))) return rc;
-    if ((rc = compute_moments(c, type == 0 ? 2 : 3, -(k + 1), cd.hi2))) return rc;
+    const int wh[2] = {2, type == 0 ? 2 : 3}, kp[2] = {k, -(k + 1)};
+    double *const out[2] = {cd.lo1, cd.hi2};
+    if ((rc = compute_moment_set(c, 2, wh, kp, out))) return rc;
     if ((rc = compute_diag_cells(c, type == 0 ? 4 : 5, k, cd.rkd))) return rc;
     cd.hi1 = nullptr;
     cd.lo2 = nullptr;
@@ -640,8 +660,13 @@ int get_band_table(dbsrg_ctx *c, int family, int type, int k, const double **out
 // r^k w B_i B_{i+d} (d = 0..kx-1) per component, then quad(a,b,comp) =
 // sum_{i,j} G(i,j) p_a(i) p_b(j) as W = G P per orbital and the products
 // P^T W of all orbital pairs.
-__global__ void k_rk_gram(int ns, int nv, int ks, int kx, int k, const double *bs,
-                          const double *gr, const double *grw, double *G) {
+// blockIdx.y 0: the P basis (order kp, values bp, into Gp); 1: the Q basis
+__global__ void k_rk_gram(int ns, int nv, int ks, int kp, int kq, int k, const double *bp,
+                          const double *bq, const double *gr, const double *grw, double *Gp,
+                          double *Gq) {
+  const int kx = blockIdx.y ? kq : kp;
+  const double *bs = blockIdx.y ? bq : bp;
+  double *G = blockIdx.y ? Gq : Gp;
   int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= ns * kx) return;
   int i = q % ns + 1, d = q / ns, j = i + d;  // 1-based i, j = i + d
@@ -721,10 +746,9 @@ int get_quad(dbsrg_ctx *c, int k, const double **out) {
   if (!(q = (double *)cache_alloc(c, (n + gp + gq + nw) * sizeof(double))))
     return set_err(c, DBSRG_ENOMEM, "quad allocation failed");
   double *GP = q + n, *GQ = GP + gp, *W = GQ + gq;
-  DBSRG_RUN(c, "k_rk_gram", k_rk_gram<<<(unsigned)((gp + 127) / 128), 128, 0, c->stream>>>(
-                                g.ns, g.nv, g.ks, g.ksp, k, g.pbsp, g.gr, g.grw, GP));
-  DBSRG_RUN(c, "k_rk_gram", k_rk_gram<<<(unsigned)((gq + 127) / 128), 128, 0, c->stream>>>(
-                                g.ns, g.nv, g.ks, g.ksq, k, g.qbsp, g.gr, g.grw, GQ));
+  DBSRG_RUN(c, "k_rk_gram",
+            k_rk_gram<<<dim3((unsigned)((std::max(gp, gq) + 63) / 64), 2), 64, 0, c->stream>>>(
+                g.ns, g.nv, g.ks, g.ksp, g.ksq, k, g.pbsp, g.qbsp, g.gr, g.grw, GP, GQ));
   DBSRG_RUN(c, "k_quad_w", k_quad_w<<<(unsigned)((nw + 255) / 256), 256, 0, c->stream>>>(
                                c->nbf, g.ns, g.ksp, g.ksq, c->pq, GP, GQ, W));
   dim3 gd((unsigned)((c->nbf + 31) / 32), (unsigned)((c->nbf + 31) / 32), 2);
