@@ -1,10 +1,10 @@
 // noalloc.cu -- the exchange contraction of one channel-pair segment with
 // no device allocation at all, for callers that cannot call cudaMalloc:
-// code that records its work into a CUDA graph (allocation calls are not
-// allowed while a stream is being captured), and host programs that must
-// fix their GPU memory footprint when they load the library (a partition of
-// device memory agreed between MPI ranks sharing a GPU, or a service that
-// reserves all memory up front).  Every other entry point of this library
+// host programs that must fix their GPU memory footprint when they load the
+// library (a partition of device memory agreed between MPI ranks sharing a
+// GPU, or a service whose own pool reserves all memory up front), and loops
+// that cannot take the device-wide synchronisation an allocation or a free
+// may bring.  Every other entry point of this library
 // grows its own scratch with cudaMalloc on demand; this one uses instead a
 // file-scope device array of fixed size, so its memory is reserved once, on
 // every GPU that loads the library, until the process exits.

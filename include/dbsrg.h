@@ -299,9 +299,11 @@ int dbsrg_timing_report(dbsrg_ctx *ctx, char *buf, size_t len);
 
 /* Allocation-free exchange contraction of one channel-pair segment.  This
  * entry point has no counterpart in the reference; it exists for callers
- * that cannot call cudaMalloc: code recorded into a CUDA graph (allocation
- * is not allowed during stream capture) and programs that must fix their
- * device memory when the library is loaded.  It needs no context.
+ * that cannot call cudaMalloc: MPI ranks that share one GPU under a device
+ * memory split agreed at start-up, host programs whose device memory is
+ * owned by another allocator (a pool reserved up front), and loops that
+ * cannot afford the device-wide synchronisation an allocation or free may
+ * bring.  It needs no context.
  *
  * For the n list entries (k2,k3,cdata) of one segment it forms the 'x'
  * density xx = sum_e cdata(e)*pq(:,jp1,k2(e)) pq(:,jp2,k3(e))^T and writes

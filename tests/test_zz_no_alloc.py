@@ -1,8 +1,9 @@
 """The allocation-free exchange entry point against the regular one.
 
 dbsrg_exchange_segment_noalloc serves callers that cannot allocate device
-memory (work recorded into a CUDA graph, programs with a fixed device
-memory budget): its scratch is a static device array instead of a
+memory (MPI ranks sharing one GPU under a memory split fixed at start-up,
+programs whose device memory is reserved up front by their own pool): its
+scratch is a static device array instead of a
 cudaMalloc'd buffer.  Here the test (not the entry point) allocates the
 inputs and the output, calls the new entry point twice in a row through the
 C ABI and compares each result with the block that Gen_matrix
