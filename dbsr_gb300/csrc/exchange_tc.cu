@@ -21,8 +21,8 @@
 // segment slot, each [slice][32-row tile][32 x 32 BF16, canonical K-major
 // layout], so a 128-row A operand is four consecutive tiles of a slice and a
 // 32-row B operand is one tile.  One CTA per SM walks the tile list.
-// Thread 0 loads the next product's operands with 1-D bulk copies
-// (cp.async.bulk completing on an mbarrier), issues its 42 MMAs (21 slice
+// One producer thread loads the operands two products ahead with 1-D bulk
+// copies (cp.async.bulk completing on an mbarrier), issues each product's 42 MMAs (21 slice
 // pairs x 2 K-steps of M=128 N=32 K=16) into one of two TMEM accumulator sets
 // and commits them to a second mbarrier, while sixteen warps recombine the
 // previous product out of the other set (warp w reads TMEM lanes 32(w%4)..
@@ -43,6 +43,9 @@ constexpr int TILE = 32 * 32;                   // BF16 elements of a 32-row dig
 constexpr uint32_t A_BYTES = 4 * TILE * 2;      // one slice of a 128-row operand
 constexpr uint32_t B_BYTES = TILE * 2;          // one slice of a 32-row operand
 constexpr int MAXT = 4;                         // terms per tile
+// staged band rows per diagonal: a tile's 32 columns meet 32 rows of each
+// diagonal, plus one on each side for the 16-byte alignment of the copies
+constexpr int BR = 34;
 // limit of the waits for the kernel's own copies and MMAs before it exits
 // (the pipeline waits use the context's limit, 2 s by default)
 constexpr unsigned long long WAIT_NS = 2000000000ull;
@@ -248,6 +251,52 @@ __device__ __forceinline__ uint32_t tile_products(const XArgs &p, const Row &r, 
   return codes;
 }
 
+// first staged row of diagonal dd (y - x = dd - BAND) of a direct term's
+// band for the tile at (x0, ty0): rows x = y - (dd - BAND) of the columns
+// y in ty0 .. ty0+31 within the tile's rows, rounded down to even
+__device__ __forceinline__ int band_row0(int x0, int ty0, int dd) {
+  return max(ty0 + BAND - dd, x0) & ~1;
+}
+
+// the producer's walk over the products of its rows (tiles without
+// products skipped): row, tile ty, product pc of np, and the row's terms
+struct ProdIt {
+  int row, ty, pc, np;
+  uint32_t codes;
+  Row r;
+};
+
+// advance to the next product; false when the CTA's rows are done
+__device__ __forceinline__ bool prod_next(const XArgs &p, ProdIt &it) {
+  if (it.row >= p.nrows) return false;
+  it.pc++;
+  while (it.pc >= it.np) {
+    if (++it.ty >= p.nty) {
+      it.row += gridDim.x;
+      if (it.row >= p.nrows) return false;
+      load_row(p, it.row, it.r);
+      it.ty = 0;
+    }
+    bool band;
+    it.codes = tile_products(p, it.r, it.ty, it.np, band);
+    it.pc = 0;
+  }
+  return true;
+}
+
+// digit operands of the current product: A (128 rows of the tile) and B
+// (32 columns), each [slice][32-row tile][TILE] with slices sl apart
+__device__ __forceinline__ void prod_operands(const XArgs &p, const ProdIt &it, size_t sl,
+                                              const __nv_bfloat16 *&As,
+                                              const __nv_bfloat16 *&Bs) {
+  const int pcode = (it.codes >> (3 * it.pc)) & 7, t = pcode & 3, m = pcode >> 2;
+  const int tc = term_code(it.r, t), a = tc & 3, tra = (tc >> 2) & 1, slot = tc >> 3;
+  const __nv_bfloat16 *Ub = p.Ud[a] + (size_t)m * TS * sl;
+  const __nv_bfloat16 *Zb = p.Zd + ((size_t)(a * 2 + m) * p.nm + slot) * TS * sl;
+  As = (tra ? Zb : Ub) + (size_t)4 * it.r.tx * TILE;
+  Bs = (tra ? Ub : Zb) + (size_t)it.ty * TILE;
+}
+
 constexpr int NCW = 16;               // consumer (epilogue) warps
 constexpr int CPT = 32 / (NCW / 4);   // tile columns per consumer thread
 constexpr int WPROD = NCW;            // producer warp
@@ -272,14 +321,15 @@ __device__ __forceinline__ void mbar_arrive(uint32_t mbar) {
 
 // Warp-specialised, one CTA per SM walking rows (quadrant record, x tile)
 // of 128 x ns; every role walks the same tile sequence.
-//  * producer (warp NCW, one lane): per product waits until its operand
-//    stage is free (the MMAs two products back completed), bulk-loads the
-//    operands (the 128-row A operand only when the stage does not hold it
-//    already -- along a row it repeats), waits until the consumers have read
-//    the TMEM set two products back, issues the MMAs and commits them;
+//  * producer (warp NCW, one lane): issues the bulk loads of the next
+//    product (once the MMAs of the previous one completed; the 128-row A
+//    operand only when neither A slot holds it already), then waits for this
+//    product's operands and for the consumers to have read the TMEM set two
+//    products back, issues the MMAs and commits them;
 //  * stager (warp NCW+1, even ns): per tile waits until the consumers are
-//    done with the staging buffers, then bulk-loads the tile's hch columns
-//    and the band rows of its terms (one copy per lane);
+//    done with the tile two back, then bulk-loads the tile's hch columns and
+//    the band rows of its terms (one copy per lane) into the staging buffers
+//    that tile used, so the copies run a tile ahead of the consumers;
 //  * consumers (warps 0..NCW-1): per product read the TMEM set, release it
 //    and add the product into int64 accumulators; per tile convert, add the
 //    band, add hch, store, and release the staging buffers.
@@ -290,9 +340,9 @@ __global__ void __maxnreg__(96) k_xfused(const XArgs p) {
   extern __shared__ __align__(1024) unsigned char smraw[];
   unsigned char *sA = smraw;                          // [2][TS][A_BYTES]
   unsigned char *sB = sA + 2 * TS * A_BYTES;          // [2][TS][B_BYTES]
-  double *sband = (double *)(sB + 2 * TS * B_BYTES);  // [MAXT][NDB][128]
-  double *shch = sband + (size_t)MAXT * NDB * 128;    // [32 columns][128 rows]
-  __shared__ __align__(8) uint64_t bar_ld[2], bar_mma[2], bar_free[2], bar_tile, bar_sfree;
+  double *sband = (double *)(sB + 2 * TS * B_BYTES);  // [2][MAXT][NDB][BR]
+  double *shch = sband + (size_t)2 * MAXT * NDB * BR; // [2][32 columns][128 rows]
+  __shared__ __align__(8) uint64_t bar_ld[2], bar_mma[2], bar_free[2], bar_tile[2], bar_sfree[2];
   __shared__ __align__(8) uint64_t bar_never;  // completed by nobody (the injected timeout)
   __shared__ uint32_t tmem_base;
   __shared__ int s_abort;
@@ -302,9 +352,9 @@ __global__ void __maxnreg__(96) k_xfused(const XArgs p) {
       mbar_init(smem_u32(&bar_ld[b]), 1);
       mbar_init(smem_u32(&bar_mma[b]), 1);
       mbar_init(smem_u32(&bar_free[b]), NCW);
+      mbar_init(smem_u32(&bar_tile[b]), 1);
+      mbar_init(smem_u32(&bar_sfree[b]), NCW);
     }
-    mbar_init(smem_u32(&bar_tile), 1);
-    mbar_init(smem_u32(&bar_sfree), NCW);
     mbar_init(smem_u32(&bar_never), 1);
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     s_abort = 0;
@@ -329,84 +379,107 @@ __global__ void __maxnreg__(96) k_xfused(const XArgs p) {
 
   if (warp == WPROD) {
     // ------------------------------------------------------------ producer
+    // Product q reads B slot q & 1 and one of two A slots, chosen by the A
+    // operand's address (kept while it repeats: U rows of a direct term are
+    // the same for every tile of a row and every row of the CTA).  The loads
+    // of product q + 1 are issued before the MMAs of product q wait for
+    // theirs, so the copies of two products are in flight at once.
     if (lane == 0) {
-      uint32_t q = 0;
-      long long ld_pend = -1, mma_last = -1;
-      long long keyA[2] = {-1, -1};  // (row, term, mode) of the A operand held by each stage
+      ProdIt it;
+      it.row = (int)blockIdx.x - (int)gridDim.x;
+      it.ty = p.nty - 1;
+      it.pc = 0;
+      it.np = 0;
+      it.codes = 0;
+      const __nv_bfloat16 *aKey[2] = {nullptr, nullptr};  // A operand held by each A slot
+      int aslot[2] = {0, 0};                              // A slot of products q & 1
+      long long ld_issued = -1, ld_done = -1, mma_last = -1;
       bool fail = false;
-      Row r;
-      for (int row = blockIdx.x; row < p.nrows && !fail; row += gridDim.x) {
-        load_row(p, row, r);
-        for (int ty = 0; ty < p.nty && !fail; ty++) {
-          int np;
-          bool band;
-          const uint32_t codes = tile_products(p, r, ty, np, band);
-          for (int pc = 0; pc < np; pc++, q++) {
-            if (*abort_flag) {
-              fail = true;
-              break;
-            }
-            const int b = q & 1;
-            const uint32_t n = q >> 1;
-            if (q >= 2 && !mbar_wait(smem_u32(&bar_mma[b]), (n - 1) & 1, p.wait_ns)) {
-              fail = true;
-              break;
-            }
-            const int pcode = (codes >> (3 * pc)) & 7, t = pcode & 3, m = pcode >> 2;
-            const int tc = term_code(r, t), a = tc & 3, tra = (tc >> 2) & 1, slot = tc >> 3;
-            const __nv_bfloat16 *Ub = p.Ud[a] + (size_t)m * TS * sl;
-            const __nv_bfloat16 *Zb = p.Zd + ((size_t)(a * 2 + m) * p.nm + slot) * TS * sl;
-            const __nv_bfloat16 *As = (tra ? Zb : Ub) + (size_t)4 * r.tx * TILE;
-            const __nv_bfloat16 *Bs = (tra ? Ub : Zb) + (size_t)ty * TILE;
-            const long long akey = ((long long)row * MAXT + t) * 2 + m;
-            const bool needA = keyA[b] != akey;
-            const uint32_t la = smem_u32(&bar_ld[b]);
-            mbar_expect_tx(la, TS * (B_BYTES + (needA ? A_BYTES : 0)));
-            for (int i = 0; i < TS; i++) {
-              if (needA)
-                bulk_g2s(smem_u32(sA + (size_t)(b * TS + i) * A_BYTES), As + (size_t)i * sl,
-                         A_BYTES, la);
-              bulk_g2s(smem_u32(sB + (size_t)(b * TS + i) * B_BYTES), Bs + (size_t)i * sl,
-                       B_BYTES, la);
-            }
-            keyA[b] = akey;
-            ld_pend = q;
-            if (!mbar_wait(la, n & 1, p.wait_ns)) {
-              fail = true;
-              break;
-            }
-            ld_pend = -1;
-            if (q >= 2 && !mbar_wait(smem_u32(&bar_free[b]), (n - 1) & 1, p.wait_ns)) {
-              fail = true;
-              break;
-            }
-            fence_after();
-            constexpr uint32_t idesc = make_idesc(128, 32);
-            // descriptors of the stage; operand offsets added to the address
-            // field (shared addresses stay below 2^18 bytes: no carry)
-            const uint64_t ad0 = make_desc(smem_u32(sA + (size_t)b * TS * A_BYTES), 128, 512);
-            const uint64_t bd0 = make_desc(smem_u32(sB + (size_t)b * TS * B_BYTES), 128, 512);
-#pragma unroll
-            for (int g = 0; g < TS; g++) {
-              const uint32_t dt = tbase + (uint32_t)(b * 256 + g * 32);
-#pragma unroll
-              for (int i = 0; i <= g; i++)
-#pragma unroll
-                for (int kk = 0; kk < 2; kk++)
-                  mma_bf16(dt, ad0 + ((i * A_BYTES + kk * 256) >> 4),
-                           bd0 + (((g - i) * B_BYTES + kk * 256) >> 4), idesc,
-                           (i == 0 && kk == 0) ? 0u : 1u);
-            }
-            mma_commit(smem_u32(&bar_mma[b]));
-            mma_last = q;
-          }
+      // bulk loads of product qq into B slot qq & 1 and an A slot
+      auto issue_loads = [&](long long qq) {
+        const __nv_bfloat16 *As, *Bs;
+        prod_operands(p, it, sl, As, Bs);
+        const int bq = (int)(qq & 1);
+        int s;
+        if (aKey[0] == As)
+          s = 0;
+        else if (aKey[1] == As)
+          s = 1;
+        else  // the slot that product qq - 1 (MMAs not yet issued) does not read
+          s = qq == 0 ? 0 : 1 - aslot[(qq - 1) & 1];
+        const bool needA = aKey[s] != As;
+        const uint32_t la = smem_u32(&bar_ld[bq]);
+        mbar_expect_tx(la, TS * (B_BYTES + (needA ? A_BYTES : 0)));
+        for (int i = 0; i < TS; i++) {
+          if (needA)
+            bulk_g2s(smem_u32(sA + (size_t)(s * TS + i) * A_BYTES), As + (size_t)i * sl, A_BYTES,
+                     la);
+          bulk_g2s(smem_u32(sB + (size_t)(bq * TS + i) * B_BYTES), Bs + (size_t)i * sl, B_BYTES,
+                   la);
         }
+        aKey[s] = As;
+        aslot[bq] = s;
+        ld_issued = qq;
+      };
+      bool more = prod_next(p, it);
+      if (more) issue_loads(0);
+      for (long long q = 0; more; q++) {
+        if (*abort_flag) {
+          fail = true;
+          break;
+        }
+        const int b = (int)(q & 1);
+        const uint32_t n = (uint32_t)(q >> 1);
+        // loads of product q + 1: its B slot (and an A slot other than
+        // product q's) were last read by product q - 1 or earlier
+        const bool more1 = prod_next(p, it);
+        if (more1) {
+          if (q >= 1 &&
+              !mbar_wait(smem_u32(&bar_mma[(q - 1) & 1]), (uint32_t)(((q - 1) >> 1) & 1),
+                         p.wait_ns)) {
+            fail = true;
+            break;
+          }
+          issue_loads(q + 1);
+        }
+        // MMAs of product q
+        if (!mbar_wait(smem_u32(&bar_ld[b]), n & 1, p.wait_ns)) {
+          fail = true;
+          break;
+        }
+        ld_done = q;
+        if (q >= 2 && !mbar_wait(smem_u32(&bar_free[b]), (n - 1) & 1, p.wait_ns)) {
+          fail = true;
+          break;
+        }
+        fence_after();
+        constexpr uint32_t idesc = make_idesc(128, 32);
+        // descriptors of the slots; operand offsets added to the address
+        // field (shared addresses stay below 2^18 bytes: no carry)
+        const uint64_t ad0 =
+            make_desc(smem_u32(sA + (size_t)aslot[b] * TS * A_BYTES), 128, 512);
+        const uint64_t bd0 = make_desc(smem_u32(sB + (size_t)b * TS * B_BYTES), 128, 512);
+#pragma unroll
+        for (int g = 0; g < TS; g++) {
+          const uint32_t dt = tbase + (uint32_t)(b * 256 + g * 32);
+#pragma unroll
+          for (int i = 0; i <= g; i++)
+#pragma unroll
+            for (int kk = 0; kk < 2; kk++)
+              mma_bf16(dt, ad0 + ((i * A_BYTES + kk * 256) >> 4),
+                       bd0 + (((g - i) * B_BYTES + kk * 256) >> 4), idesc,
+                       (i == 0 && kk == 0) ? 0u : 1u);
+        }
+        mma_commit(smem_u32(&bar_mma[b]));
+        mma_last = q;
+        more = more1;
       }
       if (fail) {
         *abort_flag = 1;
         atomicExch(p.err, 1);
-        if (ld_pend >= 0)
-          mbar_wait(smem_u32(&bar_ld[ld_pend & 1]), (uint32_t)((ld_pend >> 1) & 1), WAIT_NS);
+        // copies still in flight land before the CTA exits
+        for (long long k = ld_done + 1; k <= ld_issued; k++)
+          mbar_wait(smem_u32(&bar_ld[k & 1]), (uint32_t)((k >> 1) & 1), WAIT_NS);
       }
       // every MMA of this CTA completes before its TMEM is freed
       if (mma_last >= 0)
@@ -415,8 +488,11 @@ __global__ void __maxnreg__(96) k_xfused(const XArgs p) {
   } else if (warp == WSTAGE) {
     // ------------------------------------------------------------ stager
     if (bulk) {
+      // two staging buffers (hch columns and band rows of a tile): tile n
+      // goes to buffer n & 1 once the consumers have released tile n - 2,
+      // so the copies of the next tile overlap the consumers' current one
       uint32_t nst = 0;  // tiles staged
-      long long last_tx = -1;
+      long long last_n[2] = {-1, -1};
       bool fail = false;
       Row r;
       for (int row = blockIdx.x; row < p.nrows && !fail; row += gridDim.x) {
@@ -429,39 +505,58 @@ __global__ void __maxnreg__(96) k_xfused(const XArgs p) {
           bool band;
           tile_products(p, r, ty, np, band);
           if (np == 0 && !band) continue;
-          const int ty0 = ty * 32, ncol = min(32, p.ns - ty0);
-          // the consumers release the buffers of the previous tile
-          bool ok = *abort_flag == 0 &&
-                    (nst == 0 || mbar_wait(smem_u32(&bar_sfree), (nst - 1) & 1, p.wait_ns));
+          const int ty0 = ty * 32, ncol = min(32, p.ns - ty0), s = nst & 1;
+          bool ok = *abort_flag == 0;
+          if (ok && nst >= 2)
+            ok = mbar_wait(smem_u32(&bar_sfree[s]), ((nst >> 1) - 1) & 1, p.wait_ns);
           ok = __all_sync(0xffffffffu, ok);
           if (!ok) {
             fail = true;
             break;
           }
-          const uint32_t tb = smem_u32(&bar_tile);
+          // rows of diagonal dd of a direct term's band: band_row0 .. hi | 1
+          // (both even-aligned ends inside the tile's rows and below ns)
+          const int hib = min(x0 + 127, p.ns - 1);
+          double *sh = shch + (size_t)s * 32 * 128;
+          double *sb = sband + (size_t)s * MAXT * NDB * BR;
+          const uint32_t tb = smem_u32(&bar_tile[s]);
           if (lane == 0) {
             uint32_t bytes = (uint32_t)(ncol * nrow * 8);
             if (band)
-              for (int t = 0; t < r.nt; t++)
-                bytes += NDB * 8 * (((term_code(r, t) >> 2) & 1) ? ncol : nrow);
+              for (int t = 0; t < r.nt; t++) {
+                if ((term_code(r, t) >> 2) & 1) {
+                  bytes += NDB * 8 * ncol;
+                } else {
+                  for (int dd = 0; dd < NDB; dd++) {
+                    const int lo = band_row0(x0, ty0, dd),
+                              hi = min(ty0 + 31 + BAND - dd, hib) | 1;
+                    if (hi > lo) bytes += (uint32_t)(hi - lo + 1) * 8;
+                  }
+                }
+              }
             asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
             mbar_expect_tx(tb, bytes);
           }
           __syncwarp();
           if (lane < ncol)
-            bulk_g2s(smem_u32(shch + (size_t)lane * 128), hq + ms * (size_t)(ty0 + lane) + x0,
+            bulk_g2s(smem_u32(sh + (size_t)lane * 128), hq + ms * (size_t)(ty0 + lane) + x0,
                      (uint32_t)nrow * 8, tb);
           if (band)
             for (int k = lane; k < NDB * r.nt; k += 32) {
               const int t = k / NDB, dd = k % NDB, tc = term_code(r, t);
               const bool tra = (tc >> 2) & 1;
               const double *yb =
-                  p.Yb + ((size_t)(tc & 3) * p.nm + (tc >> 3)) * (size_t)p.ns * NDB;
-              bulk_g2s(smem_u32(sband + (size_t)t * NDB * 128 + dd * (tra ? 32 : 128)),
-                       yb + (tra ? ty0 : x0) + (size_t)p.ns * dd,
-                       (uint32_t)(tra ? ncol : nrow) * 8, tb);
+                  p.Yb + ((size_t)(tc & 3) * p.nm + (tc >> 3)) * (size_t)p.ns * NDB +
+                  (size_t)p.ns * dd;
+              const uint32_t dst = smem_u32(sb + ((size_t)t * NDB + dd) * BR);
+              if (tra) {
+                bulk_g2s(dst, yb + ty0, (uint32_t)ncol * 8, tb);
+              } else {
+                const int lo = band_row0(x0, ty0, dd), hi = min(ty0 + 31 + BAND - dd, hib) | 1;
+                if (hi > lo) bulk_g2s(dst, yb + lo, (uint32_t)(hi - lo + 1) * 8, tb);
+              }
             }
-          last_tx = nst;
+          last_n[s] = nst;
           nst++;
         }
       }
@@ -469,9 +564,11 @@ __global__ void __maxnreg__(96) k_xfused(const XArgs p) {
         *abort_flag = 1;
         atomicExch(p.err, 1);
       }
-      // the copies of the last staged tile land before the CTA exits
-      if (last_tx >= 0 && lane == 0)
-        mbar_wait(smem_u32(&bar_tile), (uint32_t)(last_tx & 1), WAIT_NS);
+      // the copies of the last staged tiles land before the CTA exits
+      if (lane == 0)
+        for (int s = 0; s < 2; s++)
+          if (last_n[s] >= 0)
+            mbar_wait(smem_u32(&bar_tile[s]), (uint32_t)((last_n[s] >> 1) & 1), WAIT_NS);
     }
   } else {
     // ------------------------------------------------------------ consumers
@@ -507,13 +604,17 @@ __global__ void __maxnreg__(96) k_xfused(const XArgs p) {
         if (np == 0 && !band) continue;
         const int y0 = ty * 32 + cg * CPT, ty0 = ty * 32;
         double *h = const_cast<double *>(hq) + ms * (size_t)y0 + x;
+        // this tile's staging buffers (the stager alternates two of them)
+        const int sbuf = bulk ? (int)(ntile & 1) : 0;
+        const double *sh = shch + (size_t)sbuf * 32 * 128;
+        double *sbt = sband + (size_t)sbuf * MAXT * NDB * BR;
 #pragma unroll
         for (int c = 0; c < CPT; c++) Iacc[c] = 0;
         if (!bulk) {  // odd ns: the consumers stage hch and the band themselves
 #pragma unroll
           for (int c = 0; c < CPT; c++) {
             const bool ok = row_ok && y0 + c < p.ns;
-            cp_async8(smem_u32(shch + (size_t)(cg * CPT + c) * 128 + xl), ok ? h + ms * c : p.hch,
+            cp_async8(smem_u32(sh + (size_t)(cg * CPT + c) * 128 + xl), ok ? h + ms * c : p.hch,
                       ok);
           }
           if (band) {
@@ -521,18 +622,20 @@ __global__ void __maxnreg__(96) k_xfused(const XArgs p) {
               const int tc = term_code(r, t);
               const double *yb =
                   p.Yb + ((size_t)(tc & 3) * p.nm + (tc >> 3)) * (size_t)p.ns * NDB;
-              double *sb = sband + (size_t)t * NDB * 128;
-              if (!((tc >> 2) & 1)) {  // rows x of y, diagonals y - x
-                for (int e = tid; e < NDB * 128; e += 32 * NCW) {
-                  const int dd = e / 128, rr = x0 + e % 128, yy = rr + dd - BAND;
-                  const bool ok = rr < p.ns && yy >= 0 && yy < p.ns;
+              double *sb = sbt + (size_t)t * NDB * BR;
+              if (!((tc >> 2) & 1)) {  // rows x of y, diagonals y - x (band_row0 on)
+                for (int e = tid; e < NDB * BR; e += 32 * NCW) {
+                  const int dd = e / BR, rr = band_row0(x0, ty0, dd) + e % BR,
+                            yy = rr + dd - BAND;
+                  const bool ok = rr < p.ns && rr < x0 + 128 && yy >= 0 && yy < p.ns;
                   cp_async8(smem_u32(sb + e), ok ? yb + rr + (size_t)p.ns * dd : yb, ok);
                 }
               } else {  // rows y of y, diagonals x - y
                 for (int e = tid; e < NDB * 32; e += 32 * NCW) {
                   const int dd = e / 32, rr = ty0 + e % 32, xx = rr + dd - BAND;
                   const bool ok = rr < p.ns && xx >= 0 && xx < p.ns;
-                  cp_async8(smem_u32(sb + e), ok ? yb + rr + (size_t)p.ns * dd : yb, ok);
+                  cp_async8(smem_u32(sb + dd * BR + e % 32), ok ? yb + rr + (size_t)p.ns * dd : yb,
+                            ok);
                 }
               }
             }
@@ -621,7 +724,8 @@ __global__ void __maxnreg__(96) k_xfused(const XArgs p) {
         for (int c = 0; c < CPT; c++)
           val[c] = cur[c] > -100000 ? i64_to_f64(Iacc[c], cur[c] - 8 * (TS + 1) - r.half) : 0.0;
         if (bulk) {
-          const bool ok = dead || mbar_wait(smem_u32(&bar_tile), ntile & 1, p.wait_ns);
+          const bool ok =
+              dead || mbar_wait(smem_u32(&bar_tile[sbuf]), (ntile >> 1) & 1, p.wait_ns);
           if (!ok) {
             dead = true;
             *abort_flag = 1;
@@ -637,9 +741,11 @@ __global__ void __maxnreg__(96) k_xfused(const XArgs p) {
             const int y = y0 + c, d = y - x;
             if (d < -BAND || d > BAND || !row_ok || y >= p.ns) continue;
             for (int t = 0; t < r.nt; t++) {
-              const double *sb = sband + (size_t)t * NDB * 128;
-              const double bv = ((term_code(r, t) >> 2) & 1) ? sb[(BAND - d) * 32 + (y - ty0)]
-                                                             : sb[(d + BAND) * 128 + xl];
+              const double *sb = sbt + (size_t)t * NDB * BR;
+              const double bv =
+                  ((term_code(r, t) >> 2) & 1)
+                      ? sb[(BAND - d) * BR + (y - ty0)]
+                      : sb[(d + BAND) * BR + (x - band_row0(x0, ty0, d + BAND))];
               val[c] += r.half ? half_f64(bv) : bv;
             }
           }
@@ -647,12 +753,12 @@ __global__ void __maxnreg__(96) k_xfused(const XArgs p) {
         if (row_ok && !dead) {
 #pragma unroll
           for (int c = 0; c < CPT; c++)
-            if (y0 + c < p.ns) h[ms * c] = shch[(size_t)(cg * CPT + c) * 128 + xl] + val[c];
+            if (y0 + c < p.ns) h[ms * c] = sh[(size_t)(cg * CPT + c) * 128 + xl] + val[c];
         }
         // release the staging buffers
         if (bulk) {
           __syncwarp();
-          if (lane == 0) mbar_arrive(smem_u32(&bar_sfree));
+          if (lane == 0) mbar_arrive(smem_u32(&bar_sfree[sbuf]));
           ntile++;
         } else if (band) {
           consumers_sync();
@@ -828,7 +934,7 @@ int split_exchange(dbsrg_ctx *c, const SplitExchange &x) {
   p.wait_ns = c->wait_ns;
   p.inject_wait = c->inject_wait ? 1 : 0;
   const size_t smem = 2 * TS * (size_t)(A_BYTES + B_BYTES) +
-                      ((size_t)MAXT * NDB * 128 + 32 * 128) * sizeof(double);
+                      ((size_t)2 * MAXT * NDB * BR + 2 * 32 * 128) * sizeof(double);
   DBSRG_TRY(c, cudaFuncSetAttribute(k_xfused, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)smem));
   const int nblk = std::min(p.nrows, std::max(1, c->nsm));
