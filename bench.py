@@ -480,7 +480,9 @@ def batch_main(args, rank, world, local):
 
 def basis_main(args, rank, world, local):
     """The channel basis of the write-out (SURVEY "next" row 2) on the
-    120-channel matrix: the split-form assembly, then dbsrg_diag_channels
+    120-channel matrix: the split-form assembly, dbsrg_orth_channels (DBS_ORTH,
+    "next" row 3: every channel orthogonal to the bound orbitals of its
+    kappa), then dbsrg_diag_channels
     (one generalized eigenproblem per channel, cuSOLVER sygvd; B = the
     B-spline overlap fppqq, the first and last B-spline of P and Q removed,
     every eigenvalue kept) and dbsrg_channel_basis (D_i^T H D_j for the 7140
@@ -512,10 +514,21 @@ def basis_main(args, rank, world, local):
             a.gen_matrix(L.icase, L.itype, L.kpol, L.k1, L.k2, L.k3, L.k4, L.c)
         a.sync()
 
+    # DBS_ORTH (called before Diag_channels, sub1.f90:142-146): every channel
+    # orthogonal to the bound orbitals of its kappa
+    iort = np.zeros((w.nbf, nch), dtype=np.int32, order="F")
+    for ich, kc in enumerate(w.kappa_ch):
+        for j in range(w.nbound):
+            if w.ipbs[j] == 0 and w.kappa_bound[j] == kc:
+                iort[j, ich] = 1
     out = {}
     for rep in range(2):  # warm-up, then timed
         assemble()
         torch.cuda.synchronize()
+        to0 = time.perf_counter()
+        a.orth_channels(iort)
+        torch.cuda.synchronize()
+        to1 = time.perf_counter()
         t0 = time.perf_counter()
         _, ev, nsol = a.diag_channels(bdiag, iprm)  # solutions to `sol` below
         torch.cuda.synchronize()
@@ -531,8 +544,21 @@ def basis_main(args, rank, world, local):
         a.channel_basis(sol, nsol)
         torch.cuda.synchronize()
         t3 = time.perf_counter()
-        out = {"diag_channels_s": t1 - t0, "diag_channels_device_out_s": t2 - t1,
-               "channel_basis_s": t3 - t2}
+        out = {"orth_channels_s": to1 - to0, "diag_channels_s": t1 - t0,
+               "diag_channels_device_out_s": t2 - t1, "channel_basis_s": t3 - t2}
+    # DBS_ORTH work: per block with na (row) and nb (column) orbitals, one
+    # read-modify-write of the block (16 B per element) and 4 (na + nb) ms^2
+    # FP64 operations (T1, T2 and the update)
+    nort = iort[:w.nbound].sum(axis=0)
+    ob = ofl = 0.0
+    for ich in range(nch):
+        for jch in range(ich + 1):
+            if w.icc[ich, jch] > 0 and (nort[ich] or nort[jch]):
+                ob += 16.0 * ms * ms
+                ofl += 4.0 * (nort[ich] + nort[jch]) * ms * ms
+    out.update({"orth_blocks_gb": ob / 1e9, "orth_gbs": ob / out["orth_channels_s"] / 1e9,
+                "orth_fp64_gflops": ofl / out["orth_channels_s"] / 1e9,
+                "orth_orbitals_per_channel": float(nort.mean())})
     fl = 0.0
     for ich in range(1, nch + 1):
         for jch in range(1, ich):

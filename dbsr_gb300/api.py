@@ -309,6 +309,16 @@ class Assembler:
         check(self._h, self._L.dbsrg_channel_basis(self._h, ps, pn, po), "channel_basis")
         return out
 
+    def orth_channels(self, iort):
+        """dbsrg_orth_channels (DBS_ORTH, dbs_orth.f90:2-84): iort(nbf, nch)
+        nonzero where channel ich is made orthogonal to bound orbital j; the
+        whole matrix is transformed in place."""
+        io = np.asfortranarray(iort, dtype=np.int32)
+        if io.shape != (self.nbf, self.nch):
+            raise ValueError(f"iort must be (nbf, nch) = ({self.nbf}, {self.nch})")
+        pi, k = _ptr(io, np.int32)
+        check(self._h, self._L.dbsrg_orth_channels(self._h, pi), "orth_channels")
+
     def set_wait_limit(self, ns: int):
         """Limit of the tensor-core kernel's pipeline waits (ns)."""
         check(self._h, self._L.dbsrg_set_wait_limit(self._h, int(ns)), "set_wait_limit")

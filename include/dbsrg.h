@@ -225,6 +225,21 @@ int dbsrg_diag_channels(dbsrg_ctx *ctx, const double *bdiag, const int *iprm,
 int dbsrg_channel_basis(dbsrg_ctx *ctx, const double *sol, const int *nsol,
                         double *out);
 
+/* Orthogonality of the channels to bound orbitals (SURVEY "next" row 3),
+ * in place on the device-resident whole matrix: DBS_ORTH
+ * (DBSR_MAT3/dbs_orth.f90:2-84), Bentley's projection
+ *     H(ich,jch) -> (1 - A_ich) H(ich,jch) (1 - A_jch^T),
+ *     A_c = sum_{j: iort(j,c) != 0} (B v_j) v_j^T,
+ * v_j = (P_j; Q_j) from the orbitals of dbsrg_set_orbitals and B the
+ * B-spline overlap blockdiag(fpbs, fqbs) (Get_pv/Get_qv, bpq of
+ * read_data.f90:144-145).  iort(nbf,nch) (host, Fortran order): nonzero
+ * where channel ich is made orthogonal to orbital j -- the reference's
+ * selection is ipbs(j) = 0, kbs(j) = kbs(ipch(ich)) and IBORT = 0
+ * (dbs_orth.f90:39-43).  Orbitals with ipbs != 0 give DBSRG_EINVAL, more
+ * than 32 orbitals for one channel DBSRG_ERANGE.  Channel-perturber blocks
+ * (hcp) are not held by this library. */
+int dbsrg_orth_channels(dbsrg_ctx *ctx, const int *iort);
+
 /* One assembled B-spline integral table, in the reference layout
  * rkb(ns,ns,ks,ks) for R (type 0 pppp,1 qqqq,2 pqpq,3 qpqp; mrk_*,
  * dbsr_lib_dbs.f90:2898-3492) or rkb(ns,ns,2ks-1,2ks-1) for S (type 0

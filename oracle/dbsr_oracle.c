@@ -1233,6 +1233,80 @@ void orc_update_hx(orc_mat *m, int ich, int jch, const double *d, double c) {
     }
 }
 
+/* DBS_ORTH: DBSR_MAT3/dbs_orth.f90:28-84 (channel-channel blocks; the
+ * perturber part needs hcp, which is not held).  For each channel ich with
+ * orbitals j selected by iort(j,ich) (the reference's ipbs(j) = 0,
+ * kbs(j) = kbs(i), IBORT(i,j) = 0 filter, :39-43), aa = sum_j w_j v_j^T and
+ * bb = aa^T with v_j = Get_pv = (P_j; Q_j) and w_j = Get_qv = (fpbs P_j;
+ * fqbs Q_j) (bpq, read_data.f90:144-145); then every block of the channel's
+ * row: x - aa x (ich > jch), x - aa x then - x bb (ich = jch), x - x bb
+ * (ich < jch), as full ms x ms products in the order of matmul. */
+void orc_dbs_orth(orc_mat *m, const int *iort) {
+  const orc_grid *g = m->g;
+  const int ns = g->ns, ms = g->ms, nch = m->nch, nbf = m->nbf;
+  double *aa = (double *)malloc(sizeof(double) * (size_t)ms * ms);
+  double *bb = (double *)malloc(sizeof(double) * (size_t)ms * ms);
+  double *cc = (double *)malloc(sizeof(double) * (size_t)ms * ms);
+  double *vv = (double *)malloc(sizeof(double) * ms);
+  double *ww = (double *)malloc(sizeof(double) * ms);
+  for (int ich = 1; ich <= nch; ich++) {
+    int nort = 0;
+    memset(aa, 0, sizeof(double) * (size_t)ms * ms);
+    memset(bb, 0, sizeof(double) * (size_t)ms * ms);
+    for (int j = 1; j <= nbf; j++) {
+      if (!iort[(j - 1) + (size_t)nbf * (ich - 1)]) continue;
+      if (m->ipbs[j - 1] > 0) continue;
+      nort++;
+      const double *p = m->pq + (size_t)2 * ns * (j - 1), *q = p + ns;
+      for (int i = 1; i <= ns; i++) {
+        vv[i - 1] = p[i - 1];
+        vv[ns + i - 1] = q[i - 1];
+      }
+      for (int i = 1; i <= ns; i++) {
+        double sp = 0.0, sq = 0.0;
+        for (int k = 1; k <= ns; k++) {
+          sp = sp + A2(g->fpbs, i, k, ns) * p[k - 1];
+          sq = sq + A2(g->fqbs, i, k, ns) * q[k - 1];
+        }
+        ww[i - 1] = sp;
+        ww[ns + i - 1] = sq;
+      }
+      for (int jj = 1; jj <= ms; jj++)
+        for (int ii = 1; ii <= ms; ii++) {
+          const double S = ww[ii - 1] * vv[jj - 1];
+          A2(aa, ii, jj, ms) = A2(aa, ii, jj, ms) + S;
+          A2(bb, jj, ii, ms) = A2(bb, jj, ii, ms) + S;
+        }
+    }
+    if (nort == 0) continue;
+    for (int jch = 1; jch <= nch; jch++) {
+      const int b = ICC(ich, jch);
+      if (b == 0) continue;
+      for (int pass = 0; pass < 2; pass++) {
+        /* pass 0: x - aa x (ich >= jch); pass 1: x - x bb (ich <= jch) */
+        if (pass == 0 && ich < jch) continue;
+        if (pass == 1 && ich > jch) continue;
+        for (int j = 1; j <= ms; j++)
+          for (int i = 1; i <= ms; i++) {
+            double s = 0.0;
+            if (pass == 0)
+              for (int k = 1; k <= ms; k++) s = s + A2(aa, i, k, ms) * HCH(k, j, b);
+            else
+              for (int k = 1; k <= ms; k++) s = s + HCH(i, k, b) * A2(bb, k, j, ms);
+            A2(cc, i, j, ms) = s;
+          }
+        for (int j = 1; j <= ms; j++)
+          for (int i = 1; i <= ms; i++) HCH(i, j, b) = HCH(i, j, b) - A2(cc, i, j, ms);
+      }
+    }
+  }
+  free(aa);
+  free(bb);
+  free(cc);
+  free(vv);
+  free(ww);
+}
+
 /* UPDATE_HW: updates.f90:183-216 */
 void orc_update_hw(orc_mat *m, int ich, int jch, const double *v,
                    const double *w, double c) {

@@ -112,6 +112,7 @@ void orc_mat_free(orc_mat *m);
 void orc_update_hs(orc_mat *m, int ich, int jch, const double *d, char sym,
                    int ii, int jj);
 void orc_update_hx(orc_mat *m, int ich, int jch, const double *d, double c);
+void orc_dbs_orth(orc_mat *m, const int *iort);
 void orc_update_hw(orc_mat *m, int ich, int jch, const double *v,
                    const double *w, double c);
 

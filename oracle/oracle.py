@@ -58,6 +58,7 @@ def lib():
         L.orc_mrk.argtypes = [C.POINTER(_Grid), C.c_int, C.c_int, _dp]
         L.orc_msk.argtypes = [C.POINTER(_Grid), C.c_int, C.c_int, _dp]
         L.orc_density.argtypes = [C.c_int, C.c_int, _dp, _dp, _dp, C.c_char]
+        L.orc_dbs_orth.argtypes = [C.c_void_p, _ip]
         L.orc_convol.argtypes = [C.c_int, C.c_int, C.c_int, _dp, _dp, _dp, C.c_int, C.c_char, C.c_char]
         L.orc_sum_amb.restype = C.c_double
         L.orc_sum_amb.argtypes = [C.c_int, C.c_int, _dp, _dp, C.c_char]
@@ -254,6 +255,11 @@ class Matrix:
                 self._m = None
         except Exception:
             pass
+
+    def dbs_orth(self, iort):
+        """DBS_ORTH (dbs_orth.f90:28-84) on hch in place; iort(nbf, nch)."""
+        io = np.asfortranarray(iort, dtype=np.int32)
+        lib().orc_dbs_orth(self._m, io.ctypes.data_as(_ip))
 
     def gen_matrix(self, icase, itype, kpol, k1, k2, k3, k4, cdata, ipt=None):
         k1, k2, k3, k4, cdata = i32(k1), i32(k2), i32(k3), i32(k4), f64(cdata)
