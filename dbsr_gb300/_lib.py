@@ -60,6 +60,7 @@ SIGNATURES = [
      [_vp, _vp, _vp, C.c_double, C.c_double, C.c_double, _vp, _vp, _vp]),
     ("dbsrg_channel_basis", C.c_int, [_vp, _vp, _vp, _vp]),
     ("dbsrg_orth_channels", C.c_int, [_vp, _vp]),
+    ("dbsrg_hf_matrix", C.c_int, [_vp, C.c_int, C.c_int, _vp, _vp, C.c_double, _vp, _vp]),
     ("dbsrg_get_tuning", C.c_int, [_vp, C.c_char_p, _ip]),
     ("dbsrg_alloc_matrix_window", C.c_int, [_vp, C.c_int, _vp, C.c_int, C.c_int, C.c_int]),
     ("dbsrg_set_window", C.c_int, [_vp, C.c_int]),

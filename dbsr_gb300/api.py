@@ -319,6 +319,24 @@ class Assembler:
         pi, k = _ptr(io, np.int32)
         check(self._h, self._L.dbsrg_orth_channels(self._h, pi), "orth_channels")
 
+    def hf_matrix(self, iorb: int, a, b, qsum: float, dhl=None, out=None):
+        """dbsrg_hf_matrix (hf_matrix.f90:2-70, Coulomb part): the potential
+        matrix (ms, ms) of orbital iorb (1-based); a, b: (nbf, kmax+1) values
+        of a(iorb,j,k), b(iorb,j,k).  Needs a one-channel matrix
+        (alloc_matrix(1, [[1]], 1, mk))."""
+        A = np.asfortranarray(a, dtype=np.float64)
+        B = np.asfortranarray(b, dtype=np.float64)
+        if A.shape != B.shape or A.shape[0] != self.nbf:
+            raise ValueError("a and b must be (nbf, kmax+1)")
+        if out is None:
+            out = np.zeros((self.ms, self.ms), order="F")
+        po, k1 = _ptr(out, np.float64)
+        pd, k2 = _ptr(dhl, np.float64) if dhl is not None else (None, None)
+        rc = self._L.dbsrg_hf_matrix(self._h, int(iorb), A.shape[1] - 1, A.ctypes.data,
+                                     B.ctypes.data, float(qsum), pd, po)
+        check(self._h, rc, "hf_matrix")
+        return out
+
     def set_wait_limit(self, ns: int):
         """Limit of the tensor-core kernel's pipeline waits (ns)."""
         check(self._h, self._L.dbsrg_set_wait_limit(self._h, int(ns)), "set_wait_limit")

@@ -240,6 +240,24 @@ int dbsrg_channel_basis(dbsrg_ctx *ctx, const double *sol, const int *nsol,
  * (hcp) are not held by this library. */
 int dbsrg_orth_channels(dbsrg_ctx *ctx, const int *iort);
 
+/* SCF potential matrix of one orbital (SURVEY "next" row 4): DBSR_HF's
+ * hf_matrix (hf_matrix.f90:2-70, Coulomb part; the Breit part of
+ * hf_matrix_breit is not included)
+ *   hfm = (qsum dhl + sum_{ii,jj,k} [direct + exchange]) / qsum
+ * for orbital iorb (1-based) of dbsrg_set_orbitals, with a(nbf,0:kmax) and
+ * b(nbf,0:kmax) (host, Fortran order) the values of the energy
+ * expression's a(iorb,j,k) and b(iorb,j,k) (hf_MOD_energy.f90:20-57), dhl
+ * the one-electron matrix (ms x ms, MAT_dhl_pq, host or device) or NULL,
+ * and hfm (ms x ms, host or device) the result.  The context must hold a
+ * one-channel matrix (dbsrg_alloc_matrix with nch = iicc = 1, mk >= kmax);
+ * it is the work area and is overwritten.  Runs in the precision the
+ * context selected.  2 qsum hfm p_iorb (without dhl) is the gradient of the
+ * two-electron energy with respect to p_iorb, the quantity dbsrg_backward
+ * returns for the same energy. */
+int dbsrg_hf_matrix(dbsrg_ctx *ctx, int iorb, int kmax, const double *a,
+                    const double *b, double qsum, const double *dhl,
+                    double *hfm);
+
 /* One assembled B-spline integral table, in the reference layout
  * rkb(ns,ns,ks,ks) for R (type 0 pppp,1 qqqq,2 pqpq,3 qpqp; mrk_*,
  * dbsr_lib_dbs.f90:2898-3492) or rkb(ns,ns,2ks-1,2ks-1) for S (type 0

@@ -1233,6 +1233,99 @@ void orc_update_hx(orc_mat *m, int ich, int jch, const double *d, double c) {
     }
 }
 
+/* hf_matrix: DBSR_HF/hf_matrix.f90:2-70 without the Breit part (mbreit = 2,
+ * :163-324).  The potential matrix of orbital iorb (1-based):
+ *   hfm = (qsum dhl + sum_{ii,jj = 1,2} sum_k [direct + exchange]) / qsum,
+ * direct: convol case 1 ('s','s') of table mrk_aaaa(k,ii,jj) with
+ *   dd = sum_j c_j density_s(p(:,jj,j), p(:,jj,j)), c_j = a(j,k), doubled
+ *   for j = iorb, into quadrant (ii,ii);
+ * exchange: convol case 4 of xx = sum_j b(j,k) density_x(p(:,ii,j),
+ *   p(:,jj,j)) into quadrant (ii,jj);
+ * both through the HF library's Update_hs (dbsr_lib_dbs.f90:4137-4193:
+ * y/2 into (ii,jj), its transpose /2 into (jj,ii)).  a, b: (nbf, 0:kmax),
+ * the values of a(iorb,j,k) and b(iorb,j,k) (hf_MOD_energy.f90:20-57);
+ * dhl: the one-electron matrix (ms x ms) of MAT_dhl_pq, or NULL. */
+static void hf_update(int ns, int ks, int ms, double *hm, int ii, int jj, const double *d,
+                      char sym) {
+  double *y = (double *)calloc((size_t)ns * ns, sizeof(double));
+  if (sym == 's') {
+    for (int jp = 1; jp <= ks; jp++)
+      for (int i = 1; i <= ns - jp + 1; i++) {
+        const int j = i + jp - 1;
+        A2(y, i, j, ns) = A2(d, i, jp, ns);
+        A2(y, j, i, ns) = A2(d, i, jp, ns);
+      }
+  } else {
+    memcpy(y, d, sizeof(double) * (size_t)ns * ns);
+  }
+  const int i1 = 1 + (ii - 1) * ns, j1 = 1 + (jj - 1) * ns;
+  for (size_t q = 0; q < (size_t)ns * ns; q++) y[q] = y[q] / 2.0;
+  for (int j = 1; j <= ns; j++)
+    for (int i = 1; i <= ns; i++)
+      A2(hm, i1 + i - 1, j1 + j - 1, ms) = A2(hm, i1 + i - 1, j1 + j - 1, ms) + A2(y, i, j, ns);
+  for (int j = 1; j <= ns; j++)
+    for (int i = 1; i <= ns; i++)
+      A2(hm, j1 + i - 1, i1 + j - 1, ms) = A2(hm, j1 + i - 1, i1 + j - 1, ms) + A2(y, j, i, ns);
+  free(y);
+}
+
+void orc_hf_matrix(const orc_grid *g, int nbf, const double *pq, int iorb, int kmax,
+                   const double *a, const double *b, double qsum, const double *dhl,
+                   double *hfm) {
+  const int ns = g->ns, ks = g->ks, ms = g->ms;
+  /* table of mrk_aaaa(k,ii,jj): 11 pppp, 12 pqpq, 21 qpqp, 22 qqqq */
+  static const int ttype[2][2] = {{0, 2}, {3, 1}};
+  double *rkb = (double *)malloc(sizeof(double) * (size_t)ns * ns * ks * ks);
+  double *d = (double *)malloc(sizeof(double) * (size_t)ns * ns);
+  double *dd = (double *)malloc(sizeof(double) * (size_t)ns * ns);
+  double *x = (double *)malloc(sizeof(double) * (size_t)ns * ns);
+  double *xx = (double *)malloc(sizeof(double) * (size_t)ns * ns);
+  for (size_t q = 0; q < (size_t)ms * ms; q++) hfm[q] = dhl ? qsum * dhl[q] : 0.0;
+  for (int ii = 1; ii <= 2; ii++)
+    for (int jj = 1; jj <= 2; jj++)
+      for (int k = 0; k <= kmax; k++) {
+        orc_mrk(g, ttype[ii - 1][jj - 1], k, rkb);
+        /* direct */
+        int met = 0;
+        memset(dd, 0, sizeof(double) * (size_t)ns * ks);
+        for (int j = 1; j <= nbf; j++) {
+          double c = a[(j - 1) + (size_t)nbf * k];
+          if (c == 0.0) continue;
+          if (j == iorb) c = c + c;
+          const double *pj = pq + (size_t)2 * ns * (j - 1) + (size_t)ns * (jj - 1);
+          orc_density(ns, ks, d, pj, pj, 's');
+          for (size_t q = 0; q < (size_t)ns * ks; q++) dd[q] = dd[q] + c * d[q];
+          met++;
+        }
+        if (met > 0) {
+          orc_convol(ns, ks, ks, rkb, d, dd, 1, 's', 's');
+          hf_update(ns, ks, ms, hfm, ii, ii, d, 's');
+        }
+        /* exchange */
+        met = 0;
+        memset(xx, 0, sizeof(double) * (size_t)ns * ns);
+        for (int j = 1; j <= nbf; j++) {
+          const double c = b[(j - 1) + (size_t)nbf * k];
+          if (c == 0.0) continue;
+          const double *p1 = pq + (size_t)2 * ns * (j - 1) + (size_t)ns * (ii - 1);
+          const double *p2 = pq + (size_t)2 * ns * (j - 1) + (size_t)ns * (jj - 1);
+          orc_density(ns, ks, x, p1, p2, 'x');
+          for (size_t q = 0; q < (size_t)ns * ns; q++) xx[q] = xx[q] + x[q] * c;
+          met++;
+        }
+        if (met > 0) {
+          orc_convol(ns, ks, ks, rkb, x, xx, 4, 's', 's');
+          hf_update(ns, ks, ms, hfm, ii, jj, x, 'x');
+        }
+      }
+  for (size_t q = 0; q < (size_t)ms * ms; q++) hfm[q] = hfm[q] / qsum;
+  free(rkb);
+  free(d);
+  free(dd);
+  free(x);
+  free(xx);
+}
+
 /* DBS_ORTH: DBSR_MAT3/dbs_orth.f90:28-84 (channel-channel blocks; the
  * perturber part needs hcp, which is not held).  For each channel ich with
  * orbitals j selected by iort(j,ich) (the reference's ipbs(j) = 0,

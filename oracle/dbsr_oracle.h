@@ -113,6 +113,9 @@ void orc_update_hs(orc_mat *m, int ich, int jch, const double *d, char sym,
                    int ii, int jj);
 void orc_update_hx(orc_mat *m, int ich, int jch, const double *d, double c);
 void orc_dbs_orth(orc_mat *m, const int *iort);
+void orc_hf_matrix(const orc_grid *g, int nbf, const double *pq, int iorb, int kmax,
+                   const double *a, const double *b, double qsum, const double *dhl,
+                   double *hfm);
 void orc_update_hw(orc_mat *m, int ich, int jch, const double *v,
                    const double *w, double c);
 

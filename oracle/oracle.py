@@ -59,6 +59,8 @@ def lib():
         L.orc_msk.argtypes = [C.POINTER(_Grid), C.c_int, C.c_int, _dp]
         L.orc_density.argtypes = [C.c_int, C.c_int, _dp, _dp, _dp, C.c_char]
         L.orc_dbs_orth.argtypes = [C.c_void_p, _ip]
+        L.orc_hf_matrix.argtypes = [C.POINTER(_Grid), C.c_int, _dp, C.c_int, C.c_int, _dp, _dp,
+                                    C.c_double, _dp, _dp]
         L.orc_convol.argtypes = [C.c_int, C.c_int, C.c_int, _dp, _dp, _dp, C.c_int, C.c_char, C.c_char]
         L.orc_sum_amb.restype = C.c_double
         L.orc_sum_amb.argtypes = [C.c_int, C.c_int, _dp, _dp, C.c_char]
@@ -193,6 +195,18 @@ class Grid:
         E = lib().orc_rk_energy_grad(self._p, len(c), *[x.ctypes.data_as(_ip) for x in ints],
                                      _d(c), _d(pq), nbf, _d(g) if grad else None)
         return E, g
+
+    def hf_matrix(self, pq, iorb: int, a, b, qsum: float, dhl=None) -> np.ndarray:
+        """hf_matrix (DBSR_HF/hf_matrix.f90:2-70, Coulomb part) of orbital
+        iorb (1-based); a, b: (nbf, kmax+1) coefficient values."""
+        pq = f64(pq)
+        nbf = pq.size // (2 * self.ns)
+        a, b = f64(a), f64(b)
+        kmax = a.shape[1] - 1
+        out = np.zeros((self.ms, self.ms), order="F")
+        lib().orc_hf_matrix(self._p, nbf, _d(pq), iorb, kmax, _d(a), _d(b), float(qsum),
+                            _d(f64(dhl)) if dhl is not None else None, _d(out))
+        return out
 
     def v_ch(self, pq_b) -> np.ndarray:
         v = np.zeros(self.ms)
