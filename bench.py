@@ -56,7 +56,7 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU sample")
-    p.add_argument("--workload", default="config1", choices=["config1", "batch", "basis"],
+    p.add_argument("--workload", default="config1", choices=["config1", "batch", "basis", "hf"],
                    help="config1: one 120-channel matrix; batch: independent J-blocks with "
                         "their own grids through dbsrg_gen_batch")
     p.add_argument("--nblocks", type=int, default=64)
@@ -576,6 +576,85 @@ def basis_main(args, rank, world, local):
     a.close()
 
 
+def hf_main(args, rank, world, local):
+    """The SCF potential matrices (SURVEY "next" row 4): hf_matrix
+    (hf_matrix.f90:2-70, Coulomb part) of all 30 orbitals of the config-4
+    basis (ns=300, Z=18, k=0..8), i.e. one SCF iteration's potentials,
+    through dbsrg_hf_matrix in the split and plain FP64 forms.  Coefficients
+    coef(i,j,k) uniform in [-1,1] where the energy expression's a(i,j,k) and
+    b(i,j,k) allow them (hf_MOD_energy.f90:20-57: k even and
+    k <= (j_i + j_j) for a; i != j, k + l_i + l_j even and
+    |j_i - j_j| <= k <= j_i + j_j for b).  Every iteration sets the orbitals
+    again, so what depends on them is rebuilt.  One warm-up iteration, then
+    `--steps` timed iterations (host wall clock around synchronised calls)."""
+    import torch
+
+    from dbsr_gb300 import PLAIN_FP64, SPLIT_BF16, Assembler, synth
+
+    torch.cuda.set_device(local)
+    w = synth.config4(n_entries=8)
+    norb, kmax = w.pq.shape[2], 8
+    kap = [k for _, k in synth.TARGET_ORBITALS[:norb]]
+    ls = [synth.l_kappa(k) for k in kap]
+    j2 = [synth.j2_kappa(k) for k in kap]
+    rng = np.random.Generator(np.random.Philox(4242))
+    coef = rng.uniform(-1.0, 1.0, (norb, norb, kmax + 1))
+    A = np.zeros((norb, norb, kmax + 1))
+    B = np.zeros((norb, norb, kmax + 1))
+    for i in range(norb):
+        for j in range(norb):
+            for k in range(kmax + 1):
+                if k % 2 == 0 and k <= (j2[i] + j2[j]) // 2:
+                    A[i, j, k] = coef[max(i, j), min(i, j), k]
+                if i != j and (k + ls[i] + ls[j]) % 2 == 0 and \
+                        abs(j2[i] - j2[j]) // 2 <= k <= (j2[i] + j2[j]) // 2:
+                    B[i, j, k] = coef[min(i, j), max(i, j), k]
+    ns, ks = w.ns, w.ks
+    Ts = ks * ns - ks * (ks - 1) // 2
+    # reference loop work per orbital: per table type and k, convol case 1
+    # ('s','s': Ts^2 multiply-adds) when a direct coefficient is nonzero and
+    # case 4 (four updates per table element: 4 Ts^2) when an exchange one is
+    fl = 0.0
+    for i in range(norb):
+        for k in range(kmax + 1):
+            fl += 4 * 2.0 * Ts * Ts * (A[i, :, k] != 0).any()
+            fl += 4 * 2.0 * 4 * Ts * Ts * (B[i, :, k] != 0).any()
+    out = {}
+    dev_out = torch.empty(4 * ns * ns, dtype=torch.float64, device="cuda")
+    for name, prec in (("split", SPLIT_BF16), ("plain", PLAIN_FP64)):
+        a = Assembler(w.t, w.ks, w.ksp, w.ksq, device=local)
+        a.set_orbitals(w.pq, np.zeros(norb, np.int32))
+        a.alloc_matrix(1, np.ones((1, 1), np.int32, order="F"), 1, kmax)
+        a.set_precision(prec)
+
+        def iteration():
+            # new orbitals every SCF iteration: everything derived from them
+            # (pair potentials, far fields) is rebuilt; the tables depend on
+            # the grid only and stay cached, as the reference's do
+            a.set_orbitals(w.pq, np.zeros(norb, np.int32))
+            for i in range(norb):
+                a.hf_matrix(i + 1, A[i], B[i], 1.0, out=dev_out)
+            torch.cuda.synchronize()
+
+        iteration()
+        steps = max(1, args.steps)
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            iteration()
+        dt = (time.perf_counter() - t0) / steps
+        out[name] = {"s_per_iteration": dt, "ms_per_orbital": dt / norb * 1e3,
+                     "gflops": fl / dt / 1e9}
+        a.close()
+    out.update({"metric": "SCF potential matrices (hf_matrix, all orbitals) s per iteration",
+                "unit": "s", "value": out["split"]["s_per_iteration"], "higher_is_better": False,
+                "dtype": "bf16-split/f32-acc/f64",
+                "config": {"workload": f"config4 basis: ns={ns} Z=18 {norb} orbitals k=0..{kmax}",
+                           "direct_terms": int((A != 0).sum()), "exchange_terms": int((B != 0).sum())},
+                "reference_loop_gflop_per_iteration": fl / 1e9,
+                "split_vs_plain": out["plain"]["s_per_iteration"] / out["split"]["s_per_iteration"]})
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
     rank = int(os.environ.get("RANK", "0"))
@@ -588,6 +667,8 @@ def main():
         return batch_main(args, rank, world, local)
     if args.workload == "basis" and args.impl == "ours":
         return basis_main(args, rank, world, local)
+    if args.workload == "hf" and args.impl == "ours":
+        return hf_main(args, rank, world, local)
     w = synth.config1(scale=args.scale, nch=args.nch)
 
     if args.impl == "reference":
