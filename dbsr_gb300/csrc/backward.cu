@@ -1,7 +1,7 @@
 // backward.cu -- the energy functional E = sum_e c_e R^k_e(a,b;c,d) over the
 // bound orbitals and its gradient with respect to their P/Q B-spline
 // coefficients (the direct potentials DBSR_HF and DBSR_MCHF build in their
-// SCF step, hf_matrix.f90:163-324).
+// SCF step, hf_matrix.f90:2-163).
 //
 // R^k(a,b;c,d) (rk, dbsr_lib_dbs.f90:3981-4022) sums four table types t with
 // electron-1 basis A_t and electron-2 basis B_t (0 PP|PP, 1 QQ|QQ,

@@ -180,7 +180,7 @@ int dbsrg_update_hx(dbsrg_ctx *ctx, int ich, int jch, const double *d,
                     double c);
 
 /* Energy functional and its gradient (the SCF potentials of DBSR_HF /
- * DBSR_MCHF, hf_matrix.f90:163-324): E = sum_e coef[e] *
+ * DBSR_MCHF, hf_matrix.f90:2-163): E = sum_e coef[e] *
  * R^k[e](i1[e], i2[e]; i3[e], i4[e]) with R^k as rk (dbsr_lib_dbs.f90:
  * 3981-4022) over the orbitals of dbsrg_set_orbitals (1-based, bound:
  * ipbs = 0), and, when grad != NULL, dE/dpq in the layout pq(ns,2,nbf)

@@ -1077,7 +1077,7 @@ static void band_sym_mv(int ns, int ks, const double *a, const double *f, double
    of the two electrons, so its derivative with respect to a function of one
    electron is the potential of the other electron's pair density (convol
    case 1 for electron 1, case 2 for electron 2) applied to the partner
-   function: the direct potentials DBSR_HF builds (hf_matrix.f90:163-324).
+   function: the direct potentials DBSR_HF builds (hf_matrix.f90:2-163).
    Orbitals are 1-based indices into pq; R tables are built once per (k,type). */
 double orc_rk_energy_grad(const orc_grid *g, int n, const int *kk, const int *i1,
                           const int *i2, const int *i3, const int *i4, const double *coef,
@@ -1234,7 +1234,7 @@ void orc_update_hx(orc_mat *m, int ich, int jch, const double *d, double c) {
 }
 
 /* hf_matrix: DBSR_HF/hf_matrix.f90:2-70 without the Breit part (mbreit = 2,
- * :163-324).  The potential matrix of orbital iorb (1-based):
+ * :91-163).  The potential matrix of orbital iorb (1-based):
  *   hfm = (qsum dhl + sum_{ii,jj = 1,2} sum_k [direct + exchange]) / qsum,
  * direct: convol case 1 ('s','s') of table mrk_aaaa(k,ii,jj) with
  *   dd = sum_j c_j density_s(p(:,jj,j), p(:,jj,j)), c_j = a(j,k), doubled
