@@ -70,21 +70,22 @@ __device__ __forceinline__ int f2i_exact(float f) {
   return __float_as_int(f + 12582912.0f) - 0x4B400000;
 }
 
-// FP64 of I * 2^sh assembled with integer instructions (the FP64 pipe of
-// this GPU is narrow): normalise |I|, keep its leading 53 bits (truncation,
-// relative error below 2^-52) and set sign and exponent.  Results outside
-// the normal range, which the scales here never produce, go through ldexp.
+// I * 2^sh outside the normal range of FP64 (never produced by the scales
+// here); kept out of line so the common path stays short
+__device__ __noinline__ double i64_scale_slow(long long I, int sh) {
+  return ldexp(__ll2double_rn(I), sh);
+}
+
+// FP64 of I * 2^sh: the conversion of I rounded to nearest, then the
+// scale 2^sh added to the exponent field (one conversion on the FP64 pipe
+// and a few integer instructions)
 __device__ __forceinline__ double i64_to_f64(long long I, int sh) {
   if (I == 0) return 0.0;
-  const unsigned long long sgn = (unsigned long long)I & 0x8000000000000000ULL;
-  unsigned long long u = sgn ? 0ULL - (unsigned long long)I : (unsigned long long)I;
-  const int lz = __clzll((long long)u);
-  u <<= lz;                                  // leading bit at position 63
-  const int ex = 63 - lz + sh + 1023;        // biased exponent of the leading bit
-  if (ex <= 0 || ex >= 0x7FF) return ldexp(sgn ? -(double)(u >> 11) : (double)(u >> 11), sh + 11 - lz);
-  const unsigned long long bits =
-      sgn | ((unsigned long long)ex << 52) | ((u >> 11) & 0x000FFFFFFFFFFFFFULL);
-  return __longlong_as_double((long long)bits);
+  const double d = __ll2double_rn(I);
+  const long long bits = __double_as_longlong(d);
+  const int ex = (int)((bits >> 52) & 0x7FF) + sh;
+  if (ex <= 0 || ex >= 0x7FF) return i64_scale_slow(I, sh);
+  return __longlong_as_double(bits + ((long long)sh << 52));
 }
 
 // v / 2 by the exponent field (normal v; zero stays zero)
