@@ -116,13 +116,15 @@ struct ZArgs {
 // is bound by those reads (L2 and HBM), not by its arithmetic.
 constexpr int ZROWS = 64;
 __global__ void __launch_bounds__(ZROWS) k_zdigits(const ZArgs z) {
-  extern __shared__ float2 zs[];  // [2][32][ZROWS] float-float: per thread one column
+  // [mode][nb][ZROWS] float-float: per thread one column; sized by the bound
+  // orbitals (and the modes) in use, which sets how many blocks share an SM
+  extern __shared__ float2 zs[];
   const int t = threadIdx.x, y = blockIdx.x * ZROWS + t, slot = blockIdx.y, a = blockIdx.z;
   const int ns = z.ns, nb = z.nb;
-  float2 *z0 = zs, *z1 = zs + 32 * ZROWS;
-  for (int k = 0; k < 32; k++) {
+  float2 *z0 = zs, *z1 = zs + nb * ZROWS;
+  for (int k = 0; k < nb; k++) {
     z0[k * ZROWS + t] = make_float2(0.0f, 0.0f);
-    z1[k * ZROWS + t] = make_float2(0.0f, 0.0f);
+    if (z.lower) z1[k * ZROWS + t] = make_float2(0.0f, 0.0f);
   }
   const SegInfo si = z.info[z.members[slot]];
   const float2 *V = z.V[a], *Vl = z.lower ? z.Vl[a] : nullptr, *Kb = z.Kb[a];
@@ -167,7 +169,7 @@ __global__ void __launch_bounds__(ZROWS) k_zdigits(const ZArgs z) {
   for (int mode = 0; mode < (z.lower ? 2 : 1); mode++) {
     const float2 *zz = mode ? z1 : z0;
     double m = 0.0;
-    for (int k = 0; k < 32; k++) {
+    for (int k = 0; k < nb; k++) {
       const float2 v = zz[k * ZROWS + t];
       m = fmax(m, fabs(ffa::value(v.x, v.y)));
     }
@@ -181,7 +183,8 @@ __global__ void __launch_bounds__(ZROWS) k_zdigits(const ZArgs z) {
       double vals[8];
 #pragma unroll
       for (int u = 0; u < 8; u++) {
-        const float2 v = zz[(8 * kg + u) * ZROWS + t];
+        const int k = 8 * kg + u;
+        const float2 v = k < nb ? zz[k * ZROWS + t] : make_float2(0.0f, 0.0f);
         vals[u] = ffa::value(v.x, v.y);
       }
       write_digit_group(z.Zd + op * TS * sl, z.NR, y, kg, vals, e);
@@ -906,7 +909,7 @@ int split_exchange(dbsrg_ctx *c, const SplitExchange &x) {
   z.Zd = Zd;
   z.ez = ez;
   z.Yb = Yb;
-  const size_t zsm = 2 * 32 * ZROWS * sizeof(float2);
+  const size_t zsm = (size_t)(x.lower ? 2 : 1) * nb * ZROWS * sizeof(float2);
   DBSRG_TRY(c, cudaFuncSetAttribute(k_zdigits, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)zsm));
   DBSRG_RUN(c, "k_zdigits",
