@@ -1184,7 +1184,6 @@ int factored_contract(dbsrg_ctx *c, const FactorJob &j) {
   }
   // direct
   KdSet kd{};
-  const size_t perd = (size_t)ns * (j.sym == 's' ? ks : 2 * ks - 1);
   for (int a = 0; a < j.na; a++) {
     if (j.split && j.cdf)
       rc = get_pairpot_direct_ff(c, j.family, j.types[a], j.kpol, j.icv, j.jp1[a], j.jp2[a],
