@@ -2,6 +2,8 @@
 #include <algorithm>
 #include <cstdlib>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <new>
 #include <thread>
 
@@ -74,6 +76,17 @@ static int window_blocks(const dbsrg_ctx *c) { return std::min(c->wcap, c->iicc 
       if (_r) return _r;           \
     }                              \
   } while (0)
+
+int raise_smem_limit(dbsrg_ctx *c, const void *fn, size_t bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<int, const void *>, size_t> limit;
+  std::lock_guard<std::mutex> lk(mu);
+  size_t &cur = limit[{c->device, fn}];
+  if (bytes <= cur || bytes <= 48 * 1024) return DBSRG_OK;
+  DBSRG_TRY(c, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  cur = bytes;
+  return DBSRG_OK;
+}
 
 int copy_out(dbsrg_ctx *c, void *dst, const void *src, size_t n) {
   if (n == 0) return DBSRG_OK;

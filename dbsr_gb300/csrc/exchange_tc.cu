@@ -67,6 +67,22 @@ __device__ __forceinline__ void write_digit_group(__nv_bfloat16 *D, int NR, int 
   }
 }
 
+// the same for 8 normalised float-float values (no FP64 arithmetic)
+__device__ __forceinline__ void write_digit_group_ff(__nv_bfloat16 *D, int NR, int row, int kg,
+                                                     const float2 *vals8, int e) {
+  const int rt = row >> 5, r = row & 31;
+  float d[8][TS];
+#pragma unroll
+  for (int t = 0; t < 8; t++) digits_ff(vals8[t].x, vals8[t].y, e, d[t]);
+#pragma unroll
+  for (int i = 0; i < TS; i++) {
+    __align__(16) __nv_bfloat16 h[8];
+#pragma unroll
+    for (int t = 0; t < 8; t++) h[t] = __float2bfloat16_rn(d[t][i]);
+    *(uint4 *)(D + ((size_t)i * NR + rt) * TILE + core_off(r, 8 * kg)) = *(const uint4 *)h;
+  }
+}
+
 // digits of one 32-wide row (values vals[0..31], row exponent e)
 __device__ __forceinline__ void write_digit_row(__nv_bfloat16 *D, int NR, int row,
                                                 const double *vals, int e) {
@@ -167,27 +183,31 @@ __global__ void __launch_bounds__(ZROWS) k_zdigits(const ZArgs z) {
   }
   const size_t sl = (size_t)z.NR * TILE;
   for (int mode = 0; mode < (z.lower ? 2 : 1); mode++) {
-    const float2 *zz = mode ? z1 : z0;
-    double m = 0.0;
+    float2 *zz = mode ? z1 : z0;
+    // each sum renormalised in place (TwoSum: hi + lo unchanged, |lo| at
+    // most half an ulp of hi); the row exponent from the high words
+    float m = 0.0f;
     for (int k = 0; k < nb; k++) {
       const float2 v = zz[k * ZROWS + t];
-      m = fmax(m, fabs(ffa::value(v.x, v.y)));
+      const float s = v.x + v.y, bp = s - v.x;
+      const float2 w = make_float2(s, (v.x - (s - bp)) + (v.y - bp));
+      zz[k * ZROWS + t] = w;
+      m = fmaxf(m, fabsf(w.x));
     }
-    const int e = scale_exp(m);
+    const int e = scale_exp_ff(m);
     const size_t op = (size_t)(a * 2 + mode) * z.nm + slot;
     z.ez[op * z.NR * EXP_PER_ROWTILE + y] = e;
     const int et = __reduce_max_sync(0xffffffffu, e);  // a warp is one 32-row tile
     if ((t & 31) == 0) z.ez[op * z.NR * EXP_PER_ROWTILE + z.NR * 32 + y / 32] = et;
     // the digits 8 columns at a time, re-read from shared memory
     for (int kg = 0; kg < 4; kg++) {
-      double vals[8];
+      float2 vals[8];
 #pragma unroll
       for (int u = 0; u < 8; u++) {
         const int k = 8 * kg + u;
-        const float2 v = k < nb ? zz[k * ZROWS + t] : make_float2(0.0f, 0.0f);
-        vals[u] = ffa::value(v.x, v.y);
+        vals[u] = k < nb ? zz[k * ZROWS + t] : make_float2(0.0f, 0.0f);
       }
-      write_digit_group(z.Zd + op * TS * sl, z.NR, y, kg, vals, e);
+      write_digit_group_ff(z.Zd + op * TS * sl, z.NR, y, kg, vals, e);
     }
   }
 }
@@ -910,8 +930,7 @@ int split_exchange(dbsrg_ctx *c, const SplitExchange &x) {
   z.ez = ez;
   z.Yb = Yb;
   const size_t zsm = (size_t)(x.lower ? 2 : 1) * nb * ZROWS * sizeof(float2);
-  DBSRG_TRY(c, cudaFuncSetAttribute(k_zdigits, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)zsm));
+  if ((rc = raise_smem_limit(c, (const void *)k_zdigits, zsm))) return rc;
   DBSRG_RUN(c, "k_zdigits",
             k_zdigits<<<dim3((unsigned)(NR * 32 / ZROWS), (unsigned)x.nm, (unsigned)x.na), ZROWS,
                         zsm, st>>>(z));  // every row of the operand, zeros past ns
@@ -938,8 +957,7 @@ int split_exchange(dbsrg_ctx *c, const SplitExchange &x) {
   p.inject_wait = c->inject_wait ? 1 : 0;
   const size_t smem = 2 * TS * (size_t)(A_BYTES + B_BYTES) +
                       ((size_t)2 * MAXT * NDB * BR + 2 * 32 * 128) * sizeof(double);
-  DBSRG_TRY(c, cudaFuncSetAttribute(k_xfused, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)smem));
+  if ((rc = raise_smem_limit(c, (const void *)k_xfused, smem))) return rc;
   const int nblk = std::min(p.nrows, std::max(1, c->nsm));
   double wbytes = 0.0, wflops = 0.0;
   if (c->timing) xfused_work(x.hxq, x.nxq, ns, x.lower, wbytes, wflops);

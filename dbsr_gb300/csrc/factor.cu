@@ -914,9 +914,7 @@ static long long pairpot_key(int kind, int family, int type, int k, int icv, int
 
 static int set_smem(dbsrg_ctx *c, const void *fn, size_t smem) {
   if (smem > 220 * 1024) return set_err(c, DBSRG_EINVAL, "pair potentials: too many bound orbitals");
-  if (smem > 48 * 1024)
-    DBSRG_TRY(c, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  return DBSRG_OK;
+  return raise_smem_limit(c, fn, smem);
 }
 
 // direct pair potentials of (family, type, k, case icv) with density

@@ -264,6 +264,10 @@ int copy_in_s(dbsrg_ctx *c, void *dst, const void *src, size_t n, cudaStream_t s
 // waits for the set-up, table and contraction streams and reports failures of
 // queued kernels
 int drain(dbsrg_ctx *c);
+// raises the dynamic shared-memory limit of kernel fn on the context's
+// device to at least bytes; never lowers it (contexts of a batch launch the
+// same kernels concurrently with different sizes), one lock for all
+int raise_smem_limit(dbsrg_ctx *c, const void *fn, size_t bytes);
 int ensure_lstate(dbsrg_ctx *c, int par, size_t bytes);
 // cache buffers through the pool (nullptr when the device is out of memory)
 void *cache_alloc(dbsrg_ctx *c, size_t bytes);

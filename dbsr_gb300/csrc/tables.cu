@@ -447,9 +447,8 @@ int compute_diag_cells(dbsrg_ctx *c, int type, int k, double *rkd) {
                (size_t)g.ksp * g.ksp * ks + (size_t)g.ksq * g.ksq * ks +
                (size_t)g.ksp * g.ksq * ks + ks + (size_t)kk * kk + 2 * (size_t)kk * ks;
   size_t bytes = nsm * sizeof(double);
-  if (bytes > 48 * 1024)
-    DBSRG_TRY(c, cudaFuncSetAttribute(k_triang, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)bytes));
+  int rc = raise_smem_limit(c, (const void *)k_triang, bytes);
+  if (rc) return rc;
   DBSRG_RUN(c, "k_triang",
             k_triang<<<dim3(g.nv, 1), 256, bytes, c->stream>>>(g.nv, ks, g.ksp, g.ksq, type, k, g.tri,
                                                       g.grm, g.grw, g.pbsp, g.qbsp, rkd));

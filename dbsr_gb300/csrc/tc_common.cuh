@@ -35,10 +35,26 @@ __device__ __forceinline__ int scale_exp(double m) {
   return e + 1;
 }
 
-// balanced digits of v / 2^e (|v / 2^e| < 1/2): W = trunc(|v| 2^(8TS-e)) < 2^(8TS-1)
-// in base 256 from the least significant digit, digits >= 128 taking -256
-// and a carry; the leading digit then stays in [0, 128].  Integer
-// instructions on the bit pattern only.
+// the balanced base-256 digits of W < 2^(8TS-1) with sign neg: from the
+// least significant digit, digits >= 128 taking -256 and a carry; the
+// leading digit then stays in [0, 128]
+__device__ __forceinline__ void digits_of(unsigned long long W, bool neg, float *d) {
+  int carry = 0;
+  int q[TS];
+#pragma unroll
+  for (int i = TS - 1; i >= 1; i--) {
+    int t = (int)((W >> (8 * (TS - 1 - i))) & 255ULL) + carry;
+    carry = t >= 128 ? 1 : 0;
+    q[i] = t - 256 * carry;
+  }
+  q[0] = (int)((W >> (8 * (TS - 1))) & 255ULL) + carry;  // W < 2^(8TS-1): in [0, 128]
+  const float sg = neg ? -1.0f : 1.0f;
+#pragma unroll
+  for (int i = 0; i < TS; i++) d[i] = sg * (float)q[i];
+}
+
+// balanced digits of v / 2^e (|v / 2^e| < 1/2): W = trunc(|v| 2^(8TS-e)) < 2^(8TS-1).
+// Integer instructions on the bit pattern only.
 __device__ __forceinline__ void digits(double v, int e, float *d) {
   const long long bits = __double_as_longlong(v);
   const int ev = (int)((bits >> 52) & 0x7FF);
@@ -51,18 +67,41 @@ __device__ __forceinline__ void digits(double v, int e, float *d) {
     else if (-s < 64)
       W = mant >> (-s);
   }
-  int carry = 0;
-  int q[TS];
-#pragma unroll
-  for (int i = TS - 1; i >= 1; i--) {
-    int t = (int)((W >> (8 * (TS - 1 - i))) & 255ULL) + carry;
-    carry = t >= 128 ? 1 : 0;
-    q[i] = t - 256 * carry;
-  }
-  q[0] = (int)((W >> (8 * (TS - 1))) & 255ULL) + carry;  // W < 2^(8TS-1): in [0, 128]
-  const float sg = bits < 0 ? -1.0f : 1.0f;
-#pragma unroll
-  for (int i = 0; i < TS; i++) d[i] = sg * (float)q[i];
+  digits_of(W, bits < 0, d);
+}
+
+// trunc(f 2^sh) toward zero as int64, for |f 2^sh| < 2^62 (zero and
+// subnormal f give 0)
+__device__ __forceinline__ long long f32_fixed(float f, int sh) {
+  const int b = __float_as_int(f);
+  const int ex = (b >> 23) & 0xFF;
+  if (ex == 0) return 0;
+  const long long m = (long long)((b & 0x7FFFFF) | 0x800000);
+  const int s = ex - 150 + sh;  // f 2^sh = m 2^s
+  const long long v = s >= 0 ? (s < 39 ? m << s : 0) : (-s < 63 ? m >> (-s) : 0);
+  return b < 0 ? -v : v;
+}
+
+// the same digits for a float-float value hi + lo (|hi| < 2^(e-1), |lo| at
+// most half an ulp of hi) without FP64 arithmetic: both words to int64 fixed
+// point with 15 bits below the last digit (exact but for the bits of lo
+// beyond them), summed, W the integer part of the magnitude
+constexpr int FFX = 15;
+__device__ __forceinline__ void digits_ff(float hi, float lo, int e, float *d) {
+  const int sh = 8 * TS - e + FFX;
+  const long long X = f32_fixed(hi, sh) + f32_fixed(lo, sh);
+  const bool neg = X < 0;
+  digits_of((unsigned long long)(neg ? -X : X) >> FFX, neg, d);
+}
+
+// exponent e with 2^(e-1) > |hi + lo| from the float-float high words' maximum
+// m: any float below 2^E is at most (1 - 2^-24) 2^E, so hi + lo stays below
+// 2^E too (0 for m == 0)
+__device__ __forceinline__ int scale_exp_ff(float m) {
+  if (m == 0.0f) return 0;
+  int e;
+  frexpf(m, &e);
+  return e + 1;
 }
 
 // exact int32 of an FP32 integer |f| < 2^22
