@@ -484,22 +484,39 @@ __global__ void k_fill_r(int ns, int ks, int nv, int ka, int kb, const double *l
   int jp = (int)(r / ks) + 1;
   double acc = 0.0;
   if (ip <= ka && jp <= kb && j >= 1 && j <= ns) {
-    int ivlo = max(1, i - ka + ip), ivhi = min(nv, i);
-    int jvlo = max(1, j - kb + jp), jvhi = min(nv, j);
-    for (int jv = jvlo; jv <= jvhi; jv++) {
-      int jh = j - jv + 1;
-      int jj = tri_index(jh, jh + jp - 1, kb);
-      for (int iv = ivlo; iv <= ivhi; iv++) {
-        int ih = i - iv + 1;
-        int ii = tri_index(ih, ih + ip - 1, ka);
-        if (iv < jv)
-          acc = fma(lowA[(ii - 1) + (size_t)kk * (iv - 1)], highB[(jj - 1) + (size_t)kk * (jv - 1)],
-                    acc);
-        else if (iv > jv)
-          acc = fma(lowB[(jj - 1) + (size_t)kk * (jv - 1)], highA[(ii - 1) + (size_t)kk * (iv - 1)],
-                    acc);
-        else
-          acc += rkd[(ii - 1) + (size_t)kk * ((jj - 1) + (size_t)kk * (iv - 1))];
+    const int ivlo = max(1, i - ka + ip), ivhi = min(nv, i);
+    const int jvlo = max(1, j - kb + jp), jvhi = min(nv, j);
+    // moment positions of the electron-1 pair in cell iv and the electron-2
+    // pair in cell jv
+    auto ia = [&](int iv) {
+      const int ih = i - iv + 1;
+      return (size_t)(tri_index(ih, ih + ip - 1, ka) - 1) + (size_t)kk * (iv - 1);
+    };
+    auto jb = [&](int jv) {
+      const int jh = j - jv + 1;
+      return (size_t)(tri_index(jh, jh + jp - 1, kb) - 1) + (size_t)kk * (jv - 1);
+    };
+    // the separable cells: iv < jv adds lowA(iv) times the sum of highB over
+    // the cells jv > iv, iv > jv adds highA(iv) times the sum of lowB over
+    // jv < iv.  Both sums are formed by additions only (the moments of
+    // B-spline products are positive), suffix sums with iv descending and
+    // prefix sums with iv ascending, so every element keeps full relative
+    // precision with O(ka + kb) operations instead of O(ka kb).
+    double suf = 0.0;
+    for (int jv = jvhi; jv >= max(jvlo, ivhi + 1); jv--) suf += highB[jb(jv)];
+    for (int iv = ivhi; iv >= ivlo; iv--) {
+      acc = fma(lowA[ia(iv)], suf, acc);
+      if (iv >= jvlo && iv <= jvhi) suf += highB[jb(iv)];
+    }
+    double pre = 0.0;
+    for (int jv = jvlo; jv <= min(jvhi, ivlo - 1); jv++) pre += lowB[jb(jv)];
+    for (int iv = ivlo; iv <= ivhi; iv++) {
+      acc = fma(highA[ia(iv)], pre, acc);
+      if (iv >= jvlo && iv <= jvhi) {  // the diagonal cell, then jv = iv joins the prefix
+        const int ih = i - iv + 1, jh = j - iv + 1;
+        const int ii = tri_index(ih, ih + ip - 1, ka), jj = tri_index(jh, jh + jp - 1, kb);
+        acc += rkd[(ii - 1) + (size_t)kk * ((jj - 1) + (size_t)kk * (iv - 1))];
+        pre += lowB[jb(iv)];
       }
     }
   }
@@ -529,24 +546,28 @@ __global__ void k_fill_s(int ns, int ks, int nv, int ksp, int ksq, int kj1, int 
     return;
   }
   // electron 1: ih in [1,ksp], ihp = ip+ih-ks in [1,ksq], iv = i-ih+1
-  int ihlo = max(1, ks - ip + 1), ihhi = min(ksp, ks - ip + ksq);
+  const int ihlo = max(1, ks - ip + 1), ihhi = min(ksp, ks - ip + ksq);
   // electron 2: jh in [1,kj1], jhp = jp+jh-ks in [1,kj2], jv = j-jh+1
-  int jhlo = max(1, ks - jp + 1), jhhi = min(kj1, ks - jp + kj2);
-  // jv ascending <=> jh descending
-  for (int jh = jhhi; jh >= jhlo; jh--) {
-    int jv = j - jh + 1;
-    if (jv < 1 || jv > nv) continue;
-    int jhp = jp + jh - ks;
-    int jj = (jh - 1) * kj2 + jhp;
-    for (int ih = ihhi; ih >= ihlo; ih--) {
-      int iv = i - ih + 1;
-      if (iv < 1 || iv > jv) continue;
-      int ihp = ip + ih - ks;
-      int ii = (ih - 1) * ksq + ihp;
-      if (iv == jv)
-        acc += rkd[(ii - 1) + (size_t)kk * ((jj - 1) + (size_t)kk * (iv - 1))];
-      else
-        acc = fma(r1[(ii - 1) + (size_t)kk * (iv - 1)], r2[(jj - 1) + (size_t)kk * (jv - 1)], acc);
+  const int jhlo = max(1, ks - jp + 1), jhhi = min(kj1, ks - jp + kj2);
+  const int ivlo = max(1, i - ihhi + 1), ivhi = min(nv, i - ihlo + 1);
+  const int jvlo = max(1, j - jhhi + 1), jvhi = min(nv, j - jhlo + 1);
+  auto ia = [&](int iv) {  // (ii - 1) and the cell offset of electron 1
+    const int ih = i - iv + 1;
+    return (size_t)((ih - 1) * ksq + ip + ih - ks - 1);
+  };
+  auto jb = [&](int jv) {
+    const int jh = j - jv + 1;
+    return (size_t)((jh - 1) * kj2 + jp + jh - ks - 1);
+  };
+  // cells iv < jv: r1(iv) times the suffix sum of r2 over jv > iv (positive
+  // moments, additions only, iv descending); the diagonal cells iv = jv
+  double suf = 0.0;
+  for (int jv = jvhi; jv >= max(jvlo, ivhi + 1); jv--) suf += r2[jb(jv) + (size_t)kk * (jv - 1)];
+  for (int iv = ivhi; iv >= ivlo; iv--) {
+    acc = fma(r1[ia(iv) + (size_t)kk * (iv - 1)], suf, acc);
+    if (iv >= jvlo && iv <= jvhi) {
+      acc += rkd[ia(iv) + (size_t)kk * (jb(iv) + (size_t)kk * (iv - 1))];
+      suf += r2[jb(iv) + (size_t)kk * (iv - 1)];
     }
   }
   rkb[q] = acc;
