@@ -120,6 +120,11 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+# DRAM bytes (read + write) of the 35 k_xfused launches of one 120-channel
+# step, measured by ncu (profiles/k_xfused_traffic_nch120.md)
+XFUSED_DRAM_BYTES_PER_STEP = 49154573568.0 + 32734944768.0
+
+
 def measured_peaks():
     p = os.path.join(HERE, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -787,6 +792,13 @@ def main():
         if by_top > 0:
             roofline["achieved"] = by_top / sec / 1e9
             roofline["frac"] = roofline["achieved"] / peaks["hbm_gbs"]
+        # DRAM traffic of k_xfused at 120 channels, all entries: one ncu
+        # capture (dram__bytes_read.sum + dram__bytes_write.sum, one pass) of
+        # the 35 launches of a step, 49.15 + 32.73 GB
+        # (profiles/k_xfused_traffic_nch120.md); per launch, like achieved
+        if name == "k_xfused" and args.nch == 120 and args.scale == 1.0 and n_top == 35:
+            roofline["traffic"] = XFUSED_DRAM_BYTES_PER_STEP / n_top
+            roofline["traffic_over_algorithmic"] = XFUSED_DRAM_BYTES_PER_STEP / by_top
         if fl_top > 0:
             tpk = peaks.get("bf16_tflops_sustained", peaks["bf16_tflops"])
             roofline["tensor"] = {"achieved": fl_top / sec / 1e12, "peak": tpk,
