@@ -61,6 +61,14 @@ SIGNATURES = [
     ("dbsrg_channel_basis", C.c_int, [_vp, _vp, _vp, _vp]),
     ("dbsrg_orth_channels", C.c_int, [_vp, _vp]),
     ("dbsrg_hf_matrix", C.c_int, [_vp, C.c_int, C.c_int, _vp, _vp, C.c_double, _vp, _vp]),
+    ("dbsrg_lists_create", C.c_int, [C.POINTER(_vp), C.c_int, C.c_int, _vp, _vp, _vp, C.c_int,
+                                     C.c_double, C.c_int]),
+    ("dbsrg_lists_destroy", C.c_int, [_vp]),
+    ("dbsrg_lists_decode", C.c_int, [C.c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    ("dbsrg_lists_add", C.c_int, [_vp, C.c_int] + [_vp] * 10),
+    ("dbsrg_lists_count", C.c_int, [_vp, C.c_int, C.c_int]),
+    ("dbsrg_lists_get", C.c_int, [_vp, C.c_int, C.c_int, _vp, _vp, _vp, _vp, _vp]),
+    ("dbsrg_lists_gen_matrix", C.c_int, [_vp, _vp]),
     ("dbsrg_get_tuning", C.c_int, [_vp, C.c_char_p, _ip]),
     ("dbsrg_alloc_matrix_window", C.c_int, [_vp, C.c_int, _vp, C.c_int, C.c_int, C.c_int]),
     ("dbsrg_set_window", C.c_int, [_vp, C.c_int]),

@@ -436,3 +436,68 @@ def gen_batch_streamed(assemblers, lists_per_assembler, consumer):
         raise errors[0]
     if rc != 0:
         _raise_batch(L, assemblers, rc, "gen_batch_streamed")
+
+
+class Lists:
+    """The list producer between the decoded angular bank and Gen_matrix
+    (dbsrg_lists_*): Add_integral, the Idef_* classification and the sorted,
+    merged (kpol, itype) lists of Add_coef/Add_cdata (add_integral.f90,
+    idef_type.f90, MOD_c_data.f90).  Host code; `gen_matrix(assembler)`
+    hands every list the library assembles to the assembler."""
+
+    def __init__(self, icase: int, ipbs, lbs=None, kbs=None, mk: int = 0, eps_c: float = 1e-10,
+                 check_target: int = 1):
+        self._L = load()
+        self.icase = icase
+        self._keep = [np.ascontiguousarray(x, dtype=np.int32) if x is not None else None
+                      for x in (ipbs, lbs, kbs)]
+        ptrs = [x.ctypes.data if x is not None else None for x in self._keep]
+        h = C.c_void_p()
+        rc = self._L.dbsrg_lists_create(C.byref(h), int(icase), int(self._keep[0].size), *ptrs,
+                                        int(mk), float(eps_c), int(check_target))
+        check(None, rc, "lists_create")
+        self._h = h
+
+    def add(self, kpol, i1, i2, i3, i4, c, ic=None, jc=None, io=None, jo=None):
+        """Add_integral for arrays of decoded coefficients."""
+        n = int(np.asarray(c).size)
+        z = np.zeros(n, dtype=np.int32)
+        arrs = [np.ascontiguousarray(x, dtype=np.int32) for x in (kpol, i1, i2, i3, i4)]
+        cc = np.ascontiguousarray(c, dtype=np.float64)
+        rest = [np.ascontiguousarray(x if x is not None else z, dtype=np.int32)
+                for x in (ic, jc, io, jo)]
+        ptrs = [a.ctypes.data for a in arrs] + [cc.ctypes.data] + [a.ctypes.data for a in rest]
+        check(None, self._L.dbsrg_lists_add(self._h, n, *ptrs), "lists_add")
+
+    def get(self, kpol: int, itype: int):
+        """(k1, k2, k3, k4, cdata) of the merged list, in (K1,K2,K3,K4) order."""
+        n = self._L.dbsrg_lists_count(self._h, int(kpol), int(itype))
+        check(None, min(n, 0), "lists_count")
+        out = [np.zeros(n, dtype=np.int32) for _ in range(4)] + [np.zeros(n)]
+        check(None, self._L.dbsrg_lists_get(self._h, int(kpol), int(itype),
+                                            *[o.ctypes.data for o in out]), "lists_get")
+        return tuple(out)
+
+    def gen_matrix(self, assembler: "Assembler"):
+        check(assembler._h, self._L.dbsrg_lists_gen_matrix(self._h, assembler._h),
+              "lists_gen_matrix")
+
+    @staticmethod
+    def decode(code):
+        """(jcase, kpol, i1, i2, i3, i4) of bank integral codes."""
+        code = np.ascontiguousarray(code, dtype=np.int32)
+        out = [np.zeros(code.size, dtype=np.int32) for _ in range(6)]
+        check(None, load().dbsrg_lists_decode(code.size, code.ctypes.data,
+                                               *[o.ctypes.data for o in out]), "lists_decode")
+        return tuple(out)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.dbsrg_lists_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -258,6 +258,48 @@ int dbsrg_hf_matrix(dbsrg_ctx *ctx, int iorb, int kmax, const double *a,
                     const double *b, double qsum, const double *dhl,
                     double *hfm);
 
+/* List producer between the decoded angular bank and Gen_matrix (SURVEY
+ * "next" row 1, the part after the bank's records are read; the records,
+ * state tables and overlap factors of State_res / Det_fact come from the
+ * caller).  Replaces Add_integral (add_integral.f90:2-57: parity filter,
+ * Breit expansion over v = k-1..k+1 by SMU, hf_energy_BR.f90:58-121), the
+ * classification Idef_Otype/Ltype/Rtype/itype (idef_type.f90:1-437) and the
+ * sorted, merged lists of Add_coef/Add_cdata/Merge_cdata/Add_matrix
+ * (MOD_c_data.f90:117-368): coefficients are appended in arrival order and
+ * each (kpol, itype) list is sorted once by (K1,K2,K3,K4) on host threads,
+ * equal keys summed in arrival order, sums with |c| <= eps_c dropped,
+ * instead of the reference's insertion by binary search and shifting.
+ * icase 0 (O), 1 (L), 2 (R), 3 (S) as DBSR_MAT3's icase; ipbs, lbs (l of each
+ * orbital, icase 2) and kbs (kappa, icase 3) are nbf host arrays; mk the
+ * largest multipole; eps_c and check_target as in mod_dbsr_mat.f90 (1e-10,
+ * 1).  Host code only; no device is needed except by
+ * dbsrg_lists_gen_matrix. */
+typedef struct dbsrg_lists dbsrg_lists;
+int dbsrg_lists_create(dbsrg_lists **lists, int icase, int nbf,
+                       const int *ipbs, const int *lbs, const int *kbs,
+                       int mk, double eps_c, int check_target);
+int dbsrg_lists_destroy(dbsrg_lists *lists);
+/* The integral code of a bank record (state_res.f90:83-96): jcase (2 bits),
+ * kpol (10), and the positions i4, i3, i2, i1 (5 bits each) from the
+ * bottom. */
+int dbsrg_lists_decode(int n, const int *code, int *jcase, int *kpol,
+                       int *i1, int *i2, int *i3, int *i4);
+/* Add_integral for n coefficients: multipole kpol, orbitals i1..i4
+ * (1-based), coefficient c, and the reference's ic, jc, io, jo. */
+int dbsrg_lists_add(dbsrg_lists *lists, int n, const int *kpol, const int *i1,
+                    const int *i2, const int *i3, const int *i4,
+                    const double *c, const int *ic, const int *jc,
+                    const int *io, const int *jo);
+/* Length of the merged list (kpol, itype), and its entries in
+ * (K1,K2,K3,K4) order (host arrays of that length). */
+int dbsrg_lists_count(dbsrg_lists *lists, int kpol, int itype);
+int dbsrg_lists_get(dbsrg_lists *lists, int kpol, int itype, int *k1,
+                    int *k2, int *k3, int *k4, double *cdata);
+/* Add_matrix for every non-empty list this library assembles (O itype 3, R
+ * itypes 3/4, S ktypes 6-9 and 16-19), kpol outer and itype inner as
+ * State_res calls it (state_res.f90:187-191): dbsrg_gen_matrix on ctx. */
+int dbsrg_lists_gen_matrix(dbsrg_lists *lists, dbsrg_ctx *ctx);
+
 /* One assembled B-spline integral table, in the reference layout
  * rkb(ns,ns,ks,ks) for R (type 0 pppp,1 qqqq,2 pqpq,3 qpqp; mrk_*,
  * dbsr_lib_dbs.f90:2898-3492) or rkb(ns,ns,2ks-1,2ks-1) for S (type 0
