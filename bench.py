@@ -485,9 +485,9 @@ def batch_main(args, rank, world, local):
 
 
 def basis_main(args, rank, world, local):
-    """The channel basis of the write-out (SURVEY "next" row 2) on the
-    120-channel matrix: the split-form assembly, dbsrg_orth_channels (DBS_ORTH,
-    "next" row 3: every channel orthogonal to the bound orbitals of its
+    """The channel basis of the write-out on the
+    120-channel matrix: the split-form assembly, dbsrg_orth_channels (DBS_ORTH:
+    every channel orthogonal to the bound orbitals of its
     kappa), then dbsrg_diag_channels
     (one generalized eigenproblem per channel, cuSOLVER sygvd; B = the
     B-spline overlap fppqq, the first and last B-spline of P and Q removed,
@@ -619,7 +619,7 @@ def backward_main(args, rank, world, local):
 
 
 def hf_main(args, rank, world, local):
-    """The SCF potential matrices (SURVEY "next" row 4): hf_matrix
+    """The SCF potential matrices of DBSR_HF: hf_matrix
     (hf_matrix.f90:2-70, Coulomb part) of all 30 orbitals of the config-4
     basis (ns=300, Z=18, k=0..8), i.e. one SCF iteration's potentials,
     through dbsrg_hf_matrix in the split and plain FP64 forms.  Coefficients

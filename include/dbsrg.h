@@ -201,7 +201,7 @@ int dbsrg_get_acf(dbsrg_ctx *ctx, double *acf);
  * alloc/destroy). */
 int dbsrg_matrix_device_ptr(dbsrg_ctx *ctx, double **hch_dev);
 
-/* The channel basis of the write-out (SURVEY "next" row 2), on the
+/* The channel basis of the write-out, on the
  * device-resident whole matrix (no window).
  * dbsrg_diag_channels -- Diag_channels (diag.f90:2-81): for every channel
  * ich with a diagonal block, the generalized problem H c = E B c on the
@@ -225,7 +225,7 @@ int dbsrg_diag_channels(dbsrg_ctx *ctx, const double *bdiag, const int *iprm,
 int dbsrg_channel_basis(dbsrg_ctx *ctx, const double *sol, const int *nsol,
                         double *out);
 
-/* Orthogonality of the channels to bound orbitals (SURVEY "next" row 3),
+/* Orthogonality of the channels to bound orbitals,
  * in place on the device-resident whole matrix: DBS_ORTH
  * (DBSR_MAT3/dbs_orth.f90:2-84), Bentley's projection
  *     H(ich,jch) -> (1 - A_ich) H(ich,jch) (1 - A_jch^T),
@@ -240,7 +240,7 @@ int dbsrg_channel_basis(dbsrg_ctx *ctx, const double *sol, const int *nsol,
  * (hcp) are not held by this library. */
 int dbsrg_orth_channels(dbsrg_ctx *ctx, const int *iort);
 
-/* SCF potential matrix of one orbital (SURVEY "next" row 4): DBSR_HF's
+/* SCF potential matrix of one orbital: DBSR_HF's
  * hf_matrix (hf_matrix.f90:2-70, Coulomb part; the Breit part of
  * hf_matrix_breit is not included)
  *   hfm = (qsum dhl + sum_{ii,jj,k} [direct + exchange]) / qsum
@@ -258,10 +258,9 @@ int dbsrg_hf_matrix(dbsrg_ctx *ctx, int iorb, int kmax, const double *a,
                     const double *b, double qsum, const double *dhl,
                     double *hfm);
 
-/* List producer between the decoded angular bank and Gen_matrix (SURVEY
- * "next" row 1, the part after the bank's records are read; the records,
- * state tables and overlap factors of State_res / Det_fact come from the
- * caller).  Replaces Add_integral (add_integral.f90:2-57: parity filter,
+/* List producer between the decoded angular bank and Gen_matrix (the part
+ * after the bank's records are read; the records, state tables and overlap
+ * factors of State_res / Det_fact come from the caller).  Replaces Add_integral (add_integral.f90:2-57: parity filter,
  * Breit expansion over v = k-1..k+1 by SMU, hf_energy_BR.f90:58-121), the
  * classification Idef_Otype/Ltype/Rtype/itype (idef_type.f90:1-437) and the
  * sorted, merged lists of Add_coef/Add_cdata/Merge_cdata/Add_matrix
