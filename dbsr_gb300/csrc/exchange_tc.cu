@@ -130,7 +130,7 @@ struct ZArgs {
 // as float-float sums (ff.cuh), then the digits of Z (and Zl) and their row
 // exponents.  The sums read the pair potentials of every entry: the kernel
 // is bound by those reads (L2 and HBM), not by its arithmetic.
-constexpr int ZROWS = 64;
+constexpr int ZROWS = 32;  // one warp per block: one 32-row digit tile
 __global__ void __launch_bounds__(ZROWS) k_zdigits(const ZArgs z) {
   // [mode][nb][ZROWS] float-float: per thread one column; sized by the bound
   // orbitals (and the modes) in use, which sets how many blocks share an SM
