@@ -47,7 +47,7 @@ constexpr int NB_MAX = 64;        // bound orbitals handled by the factored path
 constexpr int FAR = 9;            // |y - x| >= FAR is far field (spline orders <= 9)
 constexpr int BAND = FAR - 1;     // near band |y - x| <= 8
 constexpr int NDB = 2 * BAND + 1; // band diagonals
-constexpr int PXC = 8;            // output rows per block of the band pair potentials
+constexpr int PXC = 4;            // output rows per block of the band pair potentials
 constexpr int PBC = 4;            // second-orbital chunk of the diagonal-cell stage
 
 struct PairSpec {
@@ -980,14 +980,14 @@ int get_pairpot_direct_any(dbsrg_ctx *c, int family, int type, int k, int icv, i
                       (size_t)npo * ed.k1 * PBC) * sizeof(double) + (size_t)npo * sizeof(int);
   const double *lo1 = icv == 1 ? cd->lo1 : nullptr;
   const double *hi1 = (icv == 1 && family == 0) ? cd->hi1 : nullptr;
-  dim3 gf((unsigned)((per + 255) / 256), (unsigned)npair);
+  dim3 gf((unsigned)((per + 127) / 128), (unsigned)npair);
   if (ff) {
     if ((rc = set_smem(c, (const void *)k_pair_diag<true>, sm3))) return rc;
     DBSRG_RUN(c, "k_pair_diag",
               k_pair_diag<true><<<nv, 256, sm3, st>>>(
                   ns, ks, kk, nb, icv, sym, eo, ed, cd->rkd, P1, P2, Dq, per));
     DBSRG_RUN(c, "k_pair_direct_final",
-              k_pair_direct_final<true><<<gf, 256, 0, st>>>(ns, ks, nv, kk, nb, icv, sym, eo, lo1,
+              k_pair_direct_final<true><<<gf, 128, 0, st>>>(ns, ks, nv, kk, nb, icv, sym, eo, lo1,
                                                             hi1, cd->hi2, SA, M2 ? SB : nullptr,
                                                             Dq, K, per));
   } else {
@@ -996,7 +996,7 @@ int get_pairpot_direct_any(dbsrg_ctx *c, int family, int type, int k, int icv, i
               k_pair_diag<false><<<nv, 256, sm3, st>>>(
                   ns, ks, kk, nb, icv, sym, eo, ed, cd->rkd, P1, P2, Dq, per));
     DBSRG_RUN(c, "k_pair_direct_final",
-              k_pair_direct_final<false><<<gf, 256, 0, st>>>(ns, ks, nv, kk, nb, icv, sym, eo,
+              k_pair_direct_final<false><<<gf, 128, 0, st>>>(ns, ks, nv, kk, nb, icv, sym, eo,
                                                              lo1, hi1, cd->hi2, SA,
                                                              M2 ? SB : nullptr, Dq, K, per));
   }
@@ -1193,14 +1193,14 @@ int factored_contract(dbsrg_ctx *c, const FactorJob &j) {
   }
   if (j.prep) return DBSRG_OK;
   const size_t space = (size_t)4 * ns * (2 * ks - 1);
-  dim3 gs((unsigned)((space + 255) / 256), (unsigned)j.nown);
+  dim3 gs((unsigned)((space + 127) / 128), (unsigned)j.nown);
   if (j.split && j.cdf)
     DBSRG_RUN(c, "k_scatter_dp",
-              k_scatter_dp<true><<<gs, 256, 0, st>>>(ns, ks, j.sym, qs, kd, j.members, j.own,
+              k_scatter_dp<true><<<gs, 128, 0, st>>>(ns, ks, j.sym, qs, kd, j.members, j.own,
                                                      j.info, j.pairs, j.cd, j.cdf, hch_base(c)));
   else
     DBSRG_RUN(c, "k_scatter_dp",
-              k_scatter_dp<false><<<gs, 256, 0, st>>>(ns, ks, j.sym, qs, kd, j.members, j.own,
+              k_scatter_dp<false><<<gs, 128, 0, st>>>(ns, ks, j.sym, qs, kd, j.members, j.own,
                                                       j.info, j.pairs, j.cd, j.cdf, hch_base(c)));
   return DBSRG_OK;
 }
