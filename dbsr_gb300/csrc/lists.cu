@@ -35,7 +35,6 @@ struct dbsrg_lists {
   std::map<std::pair<int, int>, std::vector<Entry>> raw;     // (kpol, itype) -> arrival order
   std::map<std::pair<int, int>, std::vector<Entry>> merged;  // sorted, summed
   bool dirty = true;
-  std::string err;
 };
 
 namespace {
@@ -314,14 +313,14 @@ int add_integral(dbsrg_lists *L, int kpol, int i1, int i2, int i3, int i4, doubl
       if (!orb(i1) || !orb(i3)) return DBSRG_ERANGE;
       return idef_ltype(L, i1, i3, C, ic, jc, io, jo);
     case 2: {
-      if (!orb(i1) || !orb(i2) || !orb(i3) || !orb(i4)) return DBSRG_ERANGE;
+      if (!orb(i1) || !orb(i2) || !orb(i3) || !orb(i4) || kpol < 0) return DBSRG_ERANGE;
       const int m = (L->lbs[i1 - 1] + L->lbs[i3 - 1] + kpol) % 2 +
                     (L->lbs[i2 - 1] + L->lbs[i4 - 1] + kpol) % 2;
       if (m == 0 && kpol <= L->mk) return idef_rtype(L, kpol, i1, i2, i3, i4, C, ic, jc, io, jo);
       return 0;
     }
     case 3: {
-      if (!orb(i1) || !orb(i2) || !orb(i3) || !orb(i4)) return DBSRG_ERANGE;
+      if (!orb(i1) || !orb(i2) || !orb(i3) || !orb(i4) || kpol < 0) return DBSRG_ERANGE;
       const int ka = L->kbs[i1 - 1], kb = L->kbs[i2 - 1], kc = L->kbs[i3 - 1],
                 kd = L->kbs[i4 - 1];
       for (int v = kpol - 1; v <= kpol + 1; v++) {
