@@ -884,7 +884,7 @@ def main():
         compare = fp64_compare(args, a, w, step, dl, timed, torch, dev, world)
 
     cpu = None
-    if rank == 0 and not args.no_cpu:
+    if rank == 0 and world == 1 and not args.no_cpu:  # the CPU leg at N = 1 only
         gf, full_s, desc = cpu_sample(w, args.cpu_budget)
         cpu = {"value": gf, "unit": "GFLOP/s", "cores": 1, "kind": "port", "sample": desc,
                "s_per_matrix_extrapolated": full_s}
