@@ -22,7 +22,12 @@
  * the orbitals stored in the matching <name>.bsw files.  The matrix-level
  * routines (R_data/S_data/UPDATE_*) have no reference output to compare
  * with: the reference ships no dbsr_mat.nnn; their parity is "unpinned"
- * beyond the restatement itself.
+ * beyond the restatement itself.  The same holds for DBS_ORTH
+ * (orc_dbs_orth, "unpinned", checked against a numpy statement of the same
+ * projection only).  hf_matrix (orc_hf_matrix) is pinned indirectly: its
+ * two-electron part times the orbital reproduces the gradient of the rk
+ * energy functional, whose values are pinned by the configuration
+ * energies above.
  */
 #ifndef DBSR_ORACLE_H
 #define DBSR_ORACLE_H

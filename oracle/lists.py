@@ -5,7 +5,10 @@ Idef_itype (idef_type.f90:1-437) and Add_cdata's sorted insertion with
 binary search (MOD_c_data.f90:177-236), one unbounded block per
 (kpol, itype); Merge_cdata's drop of |c| <= eps_c (MOD_c_data.f90:300) is
 applied when a list is read.  Orbital and channel numbers are 1-based as in
-the reference."""
+the reference.
+
+Parity unpinned: the reference ships no int_bnk bank and no list dump, so
+these lists are checked against this restatement only."""
 from __future__ import annotations
 
 IBO = 2 ** 15
