@@ -189,3 +189,30 @@ def test_produced_lists_assemble_like_the_oracle():
               for b in range(w.iicc))
     assert np.abs(m.hch).max() > 0
     assert err <= 1e-12, err
+
+
+def test_bad_arguments_are_errors_not_faults():
+    import ctypes
+
+    from dbsr_gb300 import DbsrgError, _lib
+
+    L = _lib.load()
+    h = ctypes.c_void_p()
+    ipbs = np.zeros(4, np.int32)
+    lbs = np.zeros(4, np.int32)
+    assert L.dbsrg_lists_create(ctypes.byref(h), 5, 4, ipbs.ctypes.data, lbs.ctypes.data, None,
+                                3, 1e-10, 1) == -1  # unknown icase
+    assert L.dbsrg_lists_create(ctypes.byref(h), 2, 4, ipbs.ctypes.data, None, None, 3, 1e-10,
+                                1) == -1  # R lists need lbs
+    assert L.dbsrg_lists_create(ctypes.byref(h), 3, 4, ipbs.ctypes.data, lbs.ctypes.data, None,
+                                3, 1e-10, 1) == -1  # S lists need kbs
+    lists = Lists(2, ipbs, lbs, None, 3)
+    one = np.ones(1, np.int32)
+    with pytest.raises(DbsrgError):  # orbital 9 of 4
+        lists.add(one * 0, one, one, one * 9, one, np.ones(1))
+    with pytest.raises(DbsrgError):  # negative multipole
+        lists.add(-one, one, one, one, one, np.ones(1))
+    with pytest.raises(DbsrgError):  # jc > 0 with ic = 0: no structure
+        lists.add(one * 0, one, one, one, one, np.ones(1), ic=one * 0, jc=one)
+    assert len(lists.get(0, 1)[0]) == 0
+    lists.close()
