@@ -176,12 +176,13 @@ int ensure_lstate(dbsrg_ctx *c, int par, size_t bytes) {
   return grow(c, &c->lstate[par], &c->lstate_bytes[par], bytes);
 }
 bool sync_check_enabled() {
-  static int v = -1;
-  if (v < 0) {
+  // read once; the initialisation of a function-local static is thread-safe
+  // (the contexts of a batch run on their own host threads)
+  static const bool v = [] {
     const char *e = getenv("DBSRG_SYNC_CHECK");
-    v = (e && e[0] == '1') ? 1 : 0;
-  }
-  return v == 1;
+    return e && e[0] == '1';
+  }();
+  return v;
 }
 int ensure_pinned(dbsrg_ctx *c, size_t bytes) {
   if (c->pinned_bytes >= bytes) return DBSRG_OK;
