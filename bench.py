@@ -121,9 +121,29 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-# DRAM bytes (read + write) of the 35 k_xfused launches of one 120-channel
-# step, measured by ncu (profiles/k_xfused_traffic_nch120.md)
-XFUSED_DRAM_BYTES_PER_STEP = 49154573568.0 + 32734944768.0
+# DRAM traffic of k_xfused per algorithmic byte: ncu (dram__bytes_read.sum +
+# dram__bytes_write.sum, --clock-control none, one kernel, a few launches) on
+# the 40-channel case, divided by the algorithmic bytes the same launches
+# state; the traffic scales with the hch tiles a launch touches, so the
+# ratio carries to the 120-channel launches.  None until such a capture of
+# the current kernel exists: the bench then reports no traffic.
+XFUSED_TRAFFIC_PER_ALGORITHMIC_BYTE = None
+XFUSED_TRAFFIC_SOURCE = None
+
+
+def d2h_gbs(torch, dev, nbytes=4 << 30) -> float:
+    """Device-to-host copy rate of this machine into pinned memory (best of 3)."""
+    src = torch.empty(nbytes // 8, dtype=torch.float64, device=dev)
+    dst = torch.empty(nbytes // 8, dtype=torch.float64).pin_memory()
+    best = 1e9
+    for _ in range(3):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        dst.copy_(src, non_blocking=True)
+        torch.cuda.synchronize()
+        best = min(best, time.perf_counter() - t0)
+    del src, dst
+    return nbytes / best / 1e9
 
 
 def measured_peaks():
@@ -158,136 +178,257 @@ def fp64_peak_tflops(torch, dev) -> float:
 
 
 # ---------------------------------------------------------------------------
-def cpu_sample(w, budget_s: float, threads: int = 1):
-    """Time the CPU restatement on a bounded sample of the workload: the
-    first segments of one direct, one exchange and two S^k lists at k=2
-    (with the tables they need), and extrapolate per algorithmic FLOP.
-    Returns (GFLOP/s, seconds per full matrix, description)."""
-    from dbsr_gb300 import synth
-    from oracle import oracle as O
+# Lists of the CPU sample: R^k direct and exchange at k = 0, 5, 10 and the S^k
+# structures 6 and 8 of both PQ types at v = 5 and 11, so that every
+# contraction kind, the smallest and largest multipoles and the Breit
+# tables of the highest order are in it.
+SAMPLE_SEGS = {}
+for _k in (0, 5, 10):
+    SAMPLE_SEGS[(2, 3, _k)] = 2
+    SAMPLE_SEGS[(2, 4, _k)] = 1
+for _v in (5, 11):
+    for _it in (6, 8, 16, 18):
+        SAMPLE_SEGS[(3, _it, _v)] = 1
 
+
+def convol_flops(w, L, nseg, nent):
+    """Reference loop FLOPs (2 x multiply-adds) of nseg segments holding nent
+    entries of list L: one convol per segment and PQ type plus the density
+    accumulations."""
     ns, ks = w.ns, w.ks
     Ts = ks * ns - ks * (ks - 1) // 2
     Tn = (2 * ks - 1) * ns - ks * (ks - 1)
+    if L.icase == 2:
+        return (4 * nseg * 2 * (Ts * Ts if L.itype == 3 else Tn * Tn) +
+                4 * nent * 2 * ns * (ks if L.itype == 3 else ns))
+    return nseg * 2 * Tn * Tn + nent * 2 * ns * ((2 * ks - 1) if L.itype % 10 <= 7 else ns)
+
+
+def list_kind(L) -> str:
+    """Contraction kind of a list: R^k direct / exchange, S^k direct /
+    exchange.  The reference's loops run at very different rates per kind
+    (the direct 's' convol walks its table with a stride of ns), so CPU
+    times are extrapolated kind by kind."""
+    if L.icase == 2:
+        return "R direct" if L.itype == 3 else "R exchange"
+    return "S direct" if L.itype % 10 <= 7 else "S exchange"
+
+
+def full_flops_by_kind(w) -> dict:
+    out = {}
+    for L in w.lists:
+        if L.icase not in (2, 3) or L.n == 0:
+            continue
+        nseg = int(np.count_nonzero(np.r_[True, L.k1[1:] != L.k1[:-1]]))
+        k = list_kind(L)
+        out[k] = out.get(k, 0.0) + convol_flops(w, L, nseg, L.n)
+    return out
+
+
+def cpu_sample(w, budget_s: float, threads: int = 1):
+    """Time the CPU restatement on a bounded sample of the workload: the
+    first segments of the SAMPLE_SEGS lists (with the tables they need), and
+    extrapolate per algorithmic FLOP.  Each list's first entry runs once
+    untimed before its sample so that its tables are built outside the
+    contraction timing.  Returns (GFLOP/s, seconds per full matrix,
+    description, oracle matrix, the sublists in the order they were added)."""
+    from dbsr_gb300 import synth
+    from oracle import oracle as O
+
     g = O.Grid(w.t, w.ks, w.ksp, w.ksq)
     m = O.Matrix(g, w.pq, w.ipbs, w.nch, w.icc, w.mk)
-    want = {(2, 3, 2): 6, (2, 4, 2): 1, (3, 6, 2): 1, (3, 8, 2): 1}
-    t_tab = 0.0
     t0 = time.perf_counter()
-    # tables first (timed separately; the reference builds each once per run)
-    for typ in range(4):
-        m_t = time.perf_counter()
-        g.mrk(typ, 2)
-        t_tab += time.perf_counter() - m_t
-    n_tab_built = 4
-    for typ in range(2):
-        m_t = time.perf_counter()
-        g.msk(typ, 2)
-        t_tab += time.perf_counter() - m_t
-    n_tab_built += 2
-    flops, t_seg, desc = 0.0, 0.0, []
+    flops, t_seg, t_tab, n_tab, desc, added = 0.0, 0.0, 0.0, 0, [], []
+    kf, kt = {}, {}  # sampled FLOPs and seconds per kind
     for L in w.lists:
         key = (L.icase, L.itype, L.kpol)
-        if key not in want or L.n == 0:
+        if key not in SAMPLE_SEGS or L.n == 0:
             continue
         segs = np.flatnonzero(np.r_[True, L.k1[1:] != L.k1[:-1]])
-        nseg = min(want[key], segs.size)
+        nseg = min(SAMPLE_SEGS[key], segs.size)
         end = segs[nseg] if nseg < segs.size else L.n
-        sub = slice(0, end)
-        # warm the table cache of the Matrix (not timed)
-        m.gen_matrix(L.icase, L.itype, L.kpol, L.k1[:1], L.k2[:1], L.k3[:1], L.k4[:1], L.c[:1])
+        warm = synth.CList(L.icase, L.itype, L.kpol, L.k1[:1], L.k2[:1], L.k3[:1], L.k4[:1],
+                           L.c[:1])
+        sub = synth.CList(L.icase, L.itype, L.kpol, L.k1[:end], L.k2[:end], L.k3[:end],
+                          L.k4[:end], L.c[:end])
+        tw = time.perf_counter()
+        m.gen_matrix(warm.icase, warm.itype, warm.kpol, warm.k1, warm.k2, warm.k3, warm.k4,
+                     warm.c)
+        t_tab += time.perf_counter() - tw  # the table builds (4 R or 1 S) + one entry
+        n_tab += 4 if L.icase == 2 else 1
         ts = time.perf_counter()
-        m.gen_matrix(L.icase, L.itype, L.kpol, L.k1[sub], L.k2[sub], L.k3[sub], L.k4[sub],
-                     L.c[sub])
-        t_seg += time.perf_counter() - ts
-        if L.icase == 2:
-            flops += 4 * nseg * 2 * (Ts * Ts if L.itype == 3 else Tn * Tn)
-            flops += 4 * end * 2 * ns * (ks if L.itype == 3 else ns)
-        else:
-            flops += nseg * 2 * Tn * Tn + end * 2 * ns * ((2 * ks - 1) if L.itype % 10 <= 7 else ns)
+        m.gen_matrix(sub.icase, sub.itype, sub.kpol, sub.k1, sub.k2, sub.k3, sub.k4, sub.c)
+        dts = time.perf_counter() - ts
+        t_seg += dts
+        added += [warm, sub]
+        f = convol_flops(w, L, nseg, end)
+        flops += f
+        kf[list_kind(L)] = kf.get(list_kind(L), 0.0) + f
+        kt[list_kind(L)] = kt.get(list_kind(L), 0.0) + dts
         desc.append(f"{key}:{nseg}seg")
         if time.perf_counter() - t0 > budget_s:
             break
-    rate = flops / t_seg
     fl = synth.algorithmic_flops(w)
     n_tables = 4 * (w.mk + 1) + 2 * (w.mk + 2)
-    full_s = fl["total"] / rate + t_tab / n_tab_built * n_tables
-    return rate / 1e9, full_s, (
-        f"oracle (CPU restatement, -O2, 1 thread) on {', '.join(desc)} at k=2 "
-        f"({t_seg:.1f} s) plus 6 table builds ({t_tab:.1f} s); extrapolated per algorithmic "
-        f"FLOP to the full matrix ({fl['total'] / 1e12:.2f} TFLOP) and {n_tables} tables")
+    full = full_flops_by_kind(w)
+    full_s = sum(F * kt[k] / kf[k] for k, F in full.items()) + t_tab / max(n_tab, 1) * n_tables
+    rates = ", ".join(f"{k} {kf[k] / kt[k] / 1e9:.2f}" for k in sorted(kf))
+    return fl["total"] / full_s / 1e9, full_s, (
+        f"oracle (CPU restatement, -O2, 1 thread) on {', '.join(desc)} ({t_seg:.1f} s; GFLOP/s "
+        f"by kind: {rates}) plus {n_tab} table builds ({t_tab:.1f} s); extrapolated kind by kind "
+        f"to the full matrix ({fl['total'] / 1e12:.2f} TFLOP) and its {n_tables} tables: "
+        f"{full_s:.0f} s per matrix"), m, added
 
 
-def _ref_worker(args):
-    """One reference-arm worker: the oracle on a slice of segments."""
-    ws, key, lo, hi = args
+def oracle_sample_errors(a, m, added, forms):
+    """Per-block max and RMS relative errors, against the oracle's matrix m,
+    of the same sublists assembled on the device in each of `forms`
+    ({name: precision}); the blocks are those the sublists touch."""
+    blocks = [b for b in range(m.iicc) if np.abs(m.hch[:, :, b]).max() > 0]
+    out = {}
+    for name, prec in forms.items():
+        a.set_async(False)
+        a.set_precision(prec)
+        a.zero_matrix()
+        for L in added:
+            a.gen_matrix(L.icase, L.itype, L.kpol, L.k1, L.k2, L.k3, L.k4, L.c)
+        emax, erms = [], []
+        for b in blocks:
+            ich, jch = np.argwhere(np.asarray(a.icc) == b + 1)[0] + 1
+            h = a.get_block(int(ich), int(jch))
+            r = m.hch[:, :, b]
+            d = h - r
+            emax.append(float(np.abs(d).max() / np.abs(r).max()))
+            erms.append(float(np.sqrt((d * d).sum() / (r * r).sum())))
+        out[name] = {"max_rel_err": max(emax), "rms_rel_err": max(erms),
+                     "blocks_within_1e-10": int(sum(e <= 1e-10 for e in emax))}
+    out["blocks"] = len(blocks)
+    out["lists"] = sorted({f"{L.icase}/{L.itype}/k{L.kpol}" for L in added})
+    out["reference"] = ("CPU oracle (the C restatement of the reference loops) on the first "
+                        "segments of the sampled lists, all blocks they touch; max = "
+                        "max|d|/max|ref|, rms = ||d||_2/||ref||_2 per block, worst block")
+    return out
+
+
+def _ref_worker(w, items, conn):
+    """Reference-arm worker: builds the tables of its own work items once
+    (timed), as a serial reference run builds each table once (irka cache,
+    dbsr_lib_dbs.f90:2919-2925), then contracts its items at every "go"."""
     from oracle import oracle as O
 
-    w = ws
     g = O.Grid(w.t, w.ks, w.ksp, w.ksq)
     m = O.Matrix(g, w.pq, w.ipbs, w.nch, w.icc, w.mk)
-    for L in w.lists:
-        if (L.icase, L.itype, L.kpol) == key:
-            sub = slice(lo, hi)
-            m.gen_matrix(L.icase, L.itype, L.kpol, L.k1[sub], L.k2[sub], L.k3[sub], L.k4[sub],
-                         L.c[sub])
-    return 0
+    lists = {(L.icase, L.itype, L.kpol): L for L in w.lists}
+    t0 = time.perf_counter()
+    ntab = 0
+    for key in sorted({it[0] for it in items}):
+        L = lists[key]
+        m.gen_matrix(L.icase, L.itype, L.kpol, L.k1[:1], L.k2[:1], L.k3[:1], L.k4[:1],
+                     L.c[:1] * 0.0)
+        ntab += 4 if L.icase == 2 else 1
+    conn.send((time.perf_counter() - t0, ntab))
+    while conn.recv() == "go":
+        kt = {}
+        for key, lo, hi in items:
+            L = lists[key]
+            s = slice(lo, hi)
+            t1 = time.perf_counter()
+            m.gen_matrix(L.icase, L.itype, L.kpol, L.k1[s], L.k2[s], L.k3[s], L.k4[s], L.c[s])
+            kt[list_kind(L)] = kt.get(list_kind(L), 0.0) + time.perf_counter() - t1
+        conn.send(kt)
 
 
 def reference_arm(args, w):
-    """The reference's CPU path (its restatement: the Fortran reference
-    cannot be built here) on all host cores, each step a bounded sample:
-    the first segments of the k=2 direct and exchange R^k lists, split
-    over worker processes (tables built inside each worker, as a serial
-    reference run does)."""
+    """The reference's CPU path (its C restatement: the Fortran reference
+    cannot be built here) on all host cores.  One worker process per core
+    holds a fixed share of a bounded sample of segments of every kind (R^k
+    direct and exchange, S^k structures 6 and 8 of both PQ types) and builds
+    the tables of its share once; every step runs all shares concurrently.
+    The value is the whole matrix's algorithmic FLOPs over its extrapolated
+    time on these cores: the contraction at the sampled rate (median step)
+    plus the matrix's tables at the measured time per table, shared by the
+    cores."""
     import multiprocessing as mp
 
     from dbsr_gb300 import synth
 
-    ns, ks = w.ns, w.ks
-    Ts = ks * ns - ks * (ks - 1) // 2
-    Tn = (2 * ks - 1) * ns - ks * (ks - 1)
     cores = os.cpu_count() or 1
-    # work items: one exchange segment or four direct segments per worker
-    items, flops = [], 0.0
+    # segments per sampled list, in list order
+    per_list = {2: max(2, cores), 3: max(2, cores // 2)}
+    items, kf = [], {}
     for L in w.lists:
         key = (L.icase, L.itype, L.kpol)
-        if key not in ((2, 3, 2), (2, 4, 2)):
+        if key not in SAMPLE_SEGS or L.n == 0:
             continue
         segs = list(np.flatnonzero(np.r_[True, L.k1[1:] != L.k1[:-1]])) + [L.n]
-        per = 4 if L.itype == 3 else 1
-        take = cores // 2
+        take = min(max(1, per_list[L.icase] // (2 if L.itype == 4 else 1)), len(segs) - 1)
         for i in range(take):
-            a, b = i * per, (i + 1) * per
-            if b >= len(segs):
-                break
-            items.append((w, key, int(segs[a]), int(segs[b])))
-            nseg = per
-            ne = int(segs[b] - segs[a])
-            flops += 4 * nseg * 2 * (Ts * Ts if L.itype == 3 else Tn * Tn)
-            flops += 4 * ne * 2 * ns * (ks if L.itype == 3 else ns)
+            lo, hi = int(segs[i]), int(segs[i + 1])
+            items.append((key, lo, hi, convol_flops(w, L, 1, hi - lo)))
+            kf[list_kind(L)] = kf.get(list_kind(L), 0.0) + items[-1][3]
+    flops = sum(it[3] for it in items)
+    # contiguous shares of about equal FLOPs (few tables per worker)
+    nproc = min(cores, len(items))
+    shares, cur, acc = [], [], 0.0
+    for it in items:
+        cur.append(it[:3])
+        acc += it[3]
+        if acc >= flops * (len(shares) + 1) / nproc and len(shares) < nproc - 1:
+            shares.append(cur)
+            cur = []
+    shares.append(cur)
+    shares = [sh for sh in shares if sh]
     ctx = mp.get_context("spawn")
-    times = []
-    with ctx.Pool(min(cores, len(items))) as pool:
-        for s in range(args.warmup + args.steps):
-            t0 = time.perf_counter()
-            pool.map(_ref_worker, items)
-            dt = time.perf_counter() - t0
-            if s >= args.warmup:
-                times.append(dt)
-    dt = max(times)
-    v = flops / dt / 1e9
-    sample = (f"oracle restatement, {len(items)} worker processes on {cores} cores: first "
-              f"segments of the k=2 R^k direct and exchange lists incl. their table builds, "
-              f"{flops / 1e9:.1f} GFLOP algorithmic per step")
+    procs, conns = [], []
+    for sh in shares:
+        a, b = ctx.Pipe()
+        p = ctx.Process(target=_ref_worker, args=(w, sh, b), daemon=True)
+        p.start()
+        procs.append(p)
+        conns.append(a)
+    tabs = [c.recv() for c in conns]
+    times, kt = [], {}
+    for s in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        for c in conns:
+            c.send("go")
+        got = [c.recv() for c in conns]
+        if s >= args.warmup:
+            times.append(time.perf_counter() - t0)
+            for g in got:
+                for k, v in g.items():
+                    kt[k] = kt.get(k, 0.0) + v / args.steps
+    for c in conns:
+        c.send("stop")
+    for p in procs:
+        p.join(timeout=30)
+    dt = statistics.median(times)
+    nw = len(shares)
+    t_table = sum(t for t, _ in tabs) / max(1, sum(n for _, n in tabs))
+    fl = synth.algorithmic_flops(w)["total"]
+    n_tables = 4 * (w.mk + 1) + 2 * (w.mk + 2)
+    # per kind: core-seconds per sampled FLOP (all workers running together,
+    # so memory contention is in it), the whole matrix's FLOPs of that kind
+    # spread over the workers; plus its tables, spread likewise
+    full = full_flops_by_kind(w)
+    full_s = sum(F * kt[k] / kf[k] for k, F in full.items()) / nw + n_tables * t_table / nw
+    v = fl / full_s / 1e9
+    rates = ", ".join(f"{k} {kf[k] / kt[k] / 1e9:.2f}" for k in sorted(kf))
+    sample = (f"oracle restatement in {nw} worker processes ({cores} cores): per step "
+              f"{len(items)} segments of R^k direct/exchange at k=0,5,10 and S^k 6/8 (both PQ "
+              f"types) at v=5,11, {flops / 1e9:.1f} GFLOP algorithmic, median step "
+              f"{dt:.2f} s (GFLOP/s per core by kind: {rates}); plus {n_tables} table builds at "
+              f"{t_table:.2f} s each shared by the workers; extrapolated kind by kind to the "
+              f"whole matrix ({fl / 1e12:.2f} TFLOP): {full_s:.0f} s per matrix")
     return {
         "metric": METRIC, "value": v, "unit": "GFLOP/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic", "impl": "reference",
-        "config": {"workload": w.name, "sample": "k=2 R^k direct+exchange segments"},
-        "cpu_baseline": {"value": v, "unit": "GFLOP/s", "cores": min(cores, len(items)),
-                         "kind": "port", "sample": sample},
+        "config": {"workload": w.name, "sample": "R^k direct+exchange k=0,5,10; S^k 6/8 v=5,11",
+                   "s_per_matrix_extrapolated": full_s},
+        "cpu_baseline": {"value": v, "unit": "GFLOP/s", "cores": nw, "kind": "port",
+                         "sample": sample},
         "e2e": {"value": v, "unit": "GFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 
@@ -831,13 +972,12 @@ def main():
         if by_top > 0:
             roofline["achieved"] = by_top / sec / 1e9
             roofline["frac"] = roofline["achieved"] / peaks["hbm_gbs"]
-        # DRAM traffic of k_xfused at 120 channels, all entries: one ncu
-        # capture (dram__bytes_read.sum + dram__bytes_write.sum, one pass) of
-        # the 35 launches of a step, 49.15 + 32.73 GB
-        # (profiles/k_xfused_traffic_nch120.md); per launch, like achieved
-        if name == "k_xfused" and args.nch == 120 and args.scale == 1.0 and n_top == 35:
-            roofline["traffic"] = XFUSED_DRAM_BYTES_PER_STEP / n_top
-            roofline["traffic_over_algorithmic"] = XFUSED_DRAM_BYTES_PER_STEP / by_top
+        # DRAM traffic per launch, like achieved: the algorithmic bytes times
+        # the traffic ratio of a small-case capture of the same kernel
+        if name == "k_xfused" and XFUSED_TRAFFIC_PER_ALGORITHMIC_BYTE is not None:
+            roofline["traffic"] = XFUSED_TRAFFIC_PER_ALGORITHMIC_BYTE * by_top / max(n_top, 1)
+            roofline["traffic_over_algorithmic"] = XFUSED_TRAFFIC_PER_ALGORITHMIC_BYTE
+            roofline["traffic_source"] = XFUSED_TRAFFIC_SOURCE
         if fl_top > 0:
             tpk = peaks.get("bf16_tflops_sustained", peaks["bf16_tflops"])
             roofline["tensor"] = {"achieved": fl_top / sec / 1e12, "peak": tpk,
@@ -869,12 +1009,15 @@ def main():
         e2e_step()
         dte = timed(e2e_step, 2)
         npass = (w.iicc + nwin - 1) // nwin
-        e2e = {"value": world * fl["total"] / dte / 1e9, "unit": "GFLOP/s",
-               "h2d_bytes_per_step": int(h2d),
-               "d2h_bytes_per_step": int((hout.numel() + hacf.numel()) * 8),
-               "s_per_matrix": dte, "api": "dbsrg_assemble_to_host",
-               "windows": npass}
+        d2h = int((hout.numel() + hacf.numel()) * 8)
         del hout
+        torch.cuda.empty_cache()
+        link = d2h_gbs(torch, dev)
+        e2e = {"value": world * fl["total"] / dte / 1e9, "unit": "GFLOP/s",
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": d2h,
+               "s_per_matrix": dte, "api": "dbsrg_assemble_to_host",
+               "windows": npass, "d2h_gbs_measured": link,
+               "d2h_copy_floor_s": d2h / link / 1e9}
 
     # FP64 comparison: the same matrix by the factored FP64 and the plain FP64
     # assemblies (the plain one is held to the CPU oracle at 1e-12 by the
@@ -885,9 +1028,17 @@ def main():
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:  # the CPU leg at N = 1 only
-        gf, full_s, desc = cpu_sample(w, args.cpu_budget)
+        gf, full_s, desc, m_or, added = cpu_sample(w, args.cpu_budget)
         cpu = {"value": gf, "unit": "GFLOP/s", "cores": 1, "kind": "port", "sample": desc,
                "s_per_matrix_extrapolated": full_s}
+        # the oracle of that sample is also the checker of the device forms
+        # on the same sublists (untimed)
+        forms = {"plain_fp64": PLAIN_FP64, "factor_fp64": FACTOR_FP64, "split_bf16": SPLIT_BF16}
+        against = oracle_sample_errors(a, m_or, added, forms)
+        del m_or
+        if compare is None:
+            compare = {}
+        compare["against_oracle"] = against
 
     if rank == 0:
         out = {

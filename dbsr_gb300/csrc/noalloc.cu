@@ -18,7 +18,11 @@
 //     by the caller;
 //   * the first call on a device (with that device current) looks up the
 //     device address of the array with cudaGetSymbolAddress; make that
-//     first call before any stream capture begins.
+//     first call before any stream capture begins.  The address belongs to
+//     the device's context of that moment: do not use the entry point after
+//     a cudaDeviceReset of the device in the same process;
+//   * the call is synchronous: it waits on its stream for its own kernels
+//     and for the read-back of its error word before it returns.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -132,10 +136,26 @@ extern "C" int dbsrg_exchange_segment_noalloc(int ns, int ks, const double *rkb,
   if (rc) return rc;
   cudaStream_t st = (cudaStream_t)stream;
   const int nn = ns * ns, nb = (nn + 255) / 256;
-  k_na_clear<<<1, 32, 0, st>>>(err);
-  k_na_density<<<nb, 256, 0, st>>>(ns, nbf, jp1, jp2, n, k2, k3, cdata, pq, scr, err);
-  k_na_exchange<<<nb, 256, 0, st>>>(ns, ks, rkb, scr, out);
-  if (cudaGetLastError() != cudaSuccess) return DBSRG_ECUDA;
+  // each launch reports its own status (cudaLaunchKernel), so an error left
+  // behind by an earlier call of the process is not taken for this one's
+  {
+    void *a[] = {&err};
+    if (cudaLaunchKernel((const void *)k_na_clear, dim3(1), dim3(32), a, 0, st) != cudaSuccess)
+      return DBSRG_ECUDA;
+  }
+  {
+    void *a[] = {(void *)&ns, &nbf, &jp1, &jp2, &n, (void *)&k2, (void *)&k3,
+                 (void *)&cdata, (void *)&pq, &scr, &err};
+    if (cudaLaunchKernel((const void *)k_na_density, dim3(nb), dim3(256), a, 0, st) !=
+        cudaSuccess)
+      return DBSRG_ECUDA;
+  }
+  {
+    void *a[] = {(void *)&ns, (void *)&ks, (void *)&rkb, &scr, &out};
+    if (cudaLaunchKernel((const void *)k_na_exchange, dim3(nb), dim3(256), a, 0, st) !=
+        cudaSuccess)
+      return DBSRG_ECUDA;
+  }
   int h = 0;
   if (cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess)
     return DBSRG_ECUDA;

@@ -328,6 +328,21 @@ def config1(scale: float = 1.0, nch: int = 120, breit: bool = True) -> Workload:
                   o_entries=int(2000 * scale))
 
 
+def config1_shape(nch: int = 4, per_slot: int = 300, seed: int = 1240) -> Workload:
+    """The grid, orbitals and multipoles of config1 (ns=400, r_max=40, Z=26,
+    first knot 0.25/Z, 20 target orbitals, k=0..10 R^k and S^k up to v=11)
+    with a few channels (kappa uniform over +-1..+-6) and every (channel
+    pair, k) slot occupied by about ``per_slot`` entries: the lists the
+    120-channel workload holds, at a size whose blocks the CPU oracle can
+    assemble."""
+    rng = np.random.Generator(np.random.Philox(seed))
+    kap = [int(k) * int(s) for k, s in zip(rng.integers(1, 7, nch), rng.choice([-1, 1], nch))]
+    slots = nch * (nch + 1) // 2 * 11
+    return _build(f"config1 shape: ns=400 Z=26 nch={nch} k=0..10 R^k+S^k", seed, 400, 40.0, 26.0,
+                  TARGET_ORBITALS[:20], kap, 10, per_slot * slots, 1.0, breit=True,
+                  o_entries=4 * nch)
+
+
 def small(ns=60, nch=3, mk=3, n_entries=300, breit=True, seed=99, rmax=20.0, z=8.0,
           occupancy=1.0, norb=4) -> Workload:
     """Reduced workloads for parity tests."""

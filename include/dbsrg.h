@@ -389,7 +389,10 @@ int dbsrg_timing_report(dbsrg_ctx *ctx, char *buf, size_t len);
  * The array is shared by all calls on a device: calls that overlap on the
  * GPU race and must be ordered by the caller.  The first call on a device
  * sets up the array's address (cudaGetSymbolAddress) and must come before
- * any stream capture.  The call waits for its own work to finish. */
+ * any stream capture; that address belongs to the device's context of the
+ * moment, so the entry point must not be used after a cudaDeviceReset of
+ * the device in the same process.  The call is synchronous: it waits on
+ * its stream for its own kernels and the read-back of its error word. */
 int dbsrg_exchange_segment_noalloc(int ns, int ks, const double *rkb,
                                    const double *pq, int nbf, int jp1,
                                    int jp2, int n, const int *k2,

@@ -1,8 +1,8 @@
 """Extract golden vectors from the reference's own example files.
 
-Run in a checkout that has the reference mounted (default path given by
-the DBSR_REFERENCE environment variable).  Writes ``reference_golden.json``
-next to this script:
+Run as ``python make_golden.py <reference root>`` (or with the root in the
+DBSR_REFERENCE environment variable); there is no default location.
+Writes ``reference_golden.json`` next to this script:
 
 * knot sequences printed to 16 digits in ``knot.dat`` / ``<name>.knot``
   files, with the grid parameters that generated them (mkgrid_01);
@@ -28,7 +28,7 @@ import sys
 
 import numpy as np
 
-REF = os.environ.get("DBSR_REFERENCE", "/root/reference")
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("DBSR_REFERENCE", "")
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_golden.json")
 
 
@@ -118,8 +118,8 @@ def log_value(path: str, pat: str):
 
 
 def main():
-    if not os.path.isdir(REF):
-        sys.exit(f"reference not found at {REF}")
+    if not REF or not os.path.isdir(REF):
+        sys.exit("usage: make_golden.py <reference root> (or set DBSR_REFERENCE)")
     g = {"knots": [], "hf": [], "mat_memory": None}
     g["knots"].append(parse_knot(os.path.join(REF, "Rb_bound_example/dbsr_cc27/knot.dat")))
     ex = os.path.join(REF, "DBSR_HF/examples")

@@ -76,6 +76,60 @@ def test_noalloc_exchange_matches_gen_matrix_twice():
         assert err <= 1e-12, (atype, err)
 
 
+def _noalloc(ns, ks, rkb, pq, nbf, jp, k2, k3, c):
+    """One call of the entry point on device copies of the arguments."""
+    import torch
+
+    L_ = _lib.load()
+    dev = torch.device("cuda", 0)
+    t = lambda a, dt: torch.from_numpy(np.ascontiguousarray(a, dtype=dt)).to(dev)  # noqa: E731
+    drkb = t(np.asarray(rkb).ravel(order="F"), np.float64)
+    dpq = t(np.asarray(pq).ravel(order="F"), np.float64)
+    dk2, dk3, dc = t(k2, np.int32), t(k3, np.int32), t(c, np.float64)
+    out = torch.full((ns * ns,), float("nan"), dtype=torch.float64, device=dev)
+    p = lambda x: ctypes.c_void_p(x.data_ptr())  # noqa: E731
+    rc = L_.dbsrg_exchange_segment_noalloc(ns, ks, p(drkb), p(dpq), nbf, jp, jp, len(k2), p(dk2),
+                                           p(dk3), p(dc), p(out), None)
+    return rc, out.cpu().numpy().reshape((ns, ns), order="F")
+
+
+@pytest.mark.parametrize("ns", [60, 512])
+def test_noalloc_exchange_matches_oracle_convol_case3(ns):
+    """Against the oracle's convol case 3 ('s','s'; dbsr_lib_dbs.f90:2344-
+    2356) of the accumulated 'x' density, on a seeded table and orbitals;
+    ns = 512 fills the whole static scratch.  1e-12 of the largest element."""
+    from oracle import oracle as O
+
+    ks, nbf = 9, 3
+    rng = np.random.default_rng(ns)
+    rkb = np.asfortranarray(rng.uniform(-1.0, 1.0, (ns, ns, ks, ks)))
+    pq = np.asfortranarray(rng.uniform(-1.0, 1.0, (ns, 2, nbf)))
+    k2 = np.array([1, 2, 3, 1], np.int32)
+    k3 = np.array([2, 2, 1, 3], np.int32)
+    c = rng.uniform(-1.0, 1.0, 4)
+    for _ in range(2):  # two calls in a row on the shared static scratch
+        rc, got = _noalloc(ns, ks, rkb, pq, nbf, 1, k2, k3, c)
+        assert rc == 0, rc
+        xx = np.zeros((ns, ns), order="F")
+        for a, b, ce in zip(k2, k3, c):
+            xx += ce * np.outer(pq[:, 0, a - 1], pq[:, 0, b - 1])
+        ref = O.convol(ns, ks, rkb, xx, 3, "s", "s")
+        assert np.abs(got - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
+def test_noalloc_orbital_out_of_range_is_erange():
+    ns, ks = 20, 9
+    rkb = np.zeros((ns, ns, ks, ks), order="F")
+    pq = np.zeros((ns, 2, 2), order="F")
+    rc, _ = _noalloc(ns, ks, rkb, pq, 2, 1, np.array([1, 3], np.int32),
+                     np.array([1, 1], np.int32), np.array([1.0, 1.0]))
+    assert rc == -4  # DBSRG_ERANGE
+    # the next call with valid indices succeeds (the error word is cleared)
+    rc, _ = _noalloc(ns, ks, rkb, pq, 2, 1, np.array([1], np.int32), np.array([2], np.int32),
+                     np.array([1.0]))
+    assert rc == 0
+
+
 def test_noalloc_rejects_sizes_beyond_its_scratch():
     L_ = _lib.load()
     one = ctypes.c_void_p(1)
