@@ -81,6 +81,15 @@ SIGNATURES = [
     ("dbsrg_gen_batch_streamed", C.c_int, [C.c_int, _vp, _vp, _vp, _vp, _vp]),
     ("dbsrg_assemble_to_host", C.c_int, [_vp, C.c_int, _vp, C.c_int, _vp, _vp]),
     ("dbsrg_backward", C.c_int, [_vp, C.c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    ("dbsrg_alloc_perturbers", C.c_int, [_vp, C.c_int, _vp, C.c_int, _vp, C.c_int]),
+    ("dbsrg_get_perturbers", C.c_int, [_vp, _vp, _vp]),
+    ("dbsrg_set_targets", C.c_int, [_vp, C.c_int, _vp, C.c_int, C.c_int]),
+    ("dbsrg_get_targets", C.c_int, [_vp, _vp, _vp]),
+    ("dbsrg_set_dhl", C.c_int, [_vp, C.c_int, _vp, _vp, _vp]),
+    ("dbsrg_set_eps_c", C.c_int, [_vp, C.c_double]),
+    ("dbsrg_update_hw", C.c_int, [_vp, C.c_int, C.c_int, _vp, _vp, C.c_double]),
+    ("dbsrg_update_hv", C.c_int, [_vp, C.c_int, C.c_int, _vp, C.c_double]),
+    ("dbsrg_update_hb", C.c_int, [_vp, C.c_int, C.c_int, C.c_double]),
     ("dbsrg_exchange_segment_noalloc", C.c_int,
      [C.c_int, C.c_int, _vp, _vp, C.c_int, C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, _vp, _vp]),
 ]

@@ -178,6 +178,69 @@ class Assembler:
                        np.float64)
         check(self._h, self._L.dbsrg_update_hx(self._h, ich, jch, p, float(c)), "update_hx")
 
+    # -- matrix parts beside hch: perturbers, targets, one-electron data --
+    def alloc_perturbers(self, npert: int, icb, ibb):
+        """hcp(ms,iicb) and hp(iibb) with icb(nch,npert) and ibb(npert,npert)
+        (the perturber part of Alloc_dbsr_matrix, updates.f90:47-72)."""
+        icb = np.asfortranarray(icb, dtype=np.int32)
+        ibb = np.asfortranarray(ibb, dtype=np.int32)
+        self.iicb, self.iibb = int(icb.max(initial=0)), int(ibb.max(initial=0))
+        self.npert = int(npert)
+        check(self._h, self._L.dbsrg_alloc_perturbers(self._h, int(npert), C.c_void_p(icb.ctypes.data),
+                                                      self.iicb, C.c_void_p(ibb.ctypes.data),
+                                                      self.iibb), "alloc_perturbers")
+
+    def get_perturbers(self):
+        """(hcp(ms,iicb), hp(iibb))"""
+        hcp = np.zeros((self.ms, max(self.iicb, 1)), order="F")
+        hp = np.zeros(max(self.iibb, 1))
+        check(self._h, self._L.dbsrg_get_perturbers(self._h, C.c_void_p(hcp.ctypes.data),
+                                                    C.c_void_p(hp.ctypes.data)), "get_perturbers")
+        return hcp, hp
+
+    def set_targets(self, ntarg: int, iptar, iitar: int = 0, check_target: int = 1):
+        """Target_h's matrices htarg/otarg (target_subs.f90:2-31) over ntarg
+        targets, iptar(nch) the target of each channel."""
+        iptar = np.ascontiguousarray(iptar, dtype=np.int32)
+        self.ntarg = int(ntarg)
+        check(self._h, self._L.dbsrg_set_targets(self._h, int(ntarg), C.c_void_p(iptar.ctypes.data),
+                                                 int(iitar), int(check_target)), "set_targets")
+
+    def get_targets(self):
+        n = max(self.ntarg * (self.ntarg + 1) // 2, 1)
+        ht, ot = np.zeros(n), np.zeros(n)
+        check(self._h, self._L.dbsrg_get_targets(self._h, C.c_void_p(ht.ctypes.data),
+                                                 C.c_void_p(ot.ctypes.data)), "get_targets")
+        return ht, ot
+
+    def set_dhl(self, kap_list, hd, kbs):
+        """One-electron Dirac matrices hd(ms,ms,nkap) of the kappas kap_list
+        and the kappa of every orbital kbs(nbf), read by L_data."""
+        kap = np.ascontiguousarray(kap_list, dtype=np.int32)
+        hd = np.asfortranarray(hd, dtype=np.float64)
+        kbs = np.ascontiguousarray(kbs, dtype=np.int32)
+        check(self._h, self._L.dbsrg_set_dhl(self._h, kap.size, C.c_void_p(kap.ctypes.data),
+                                             C.c_void_p(hd.ctypes.data), C.c_void_p(kbs.ctypes.data)),
+              "set_dhl")
+
+    def set_eps_c(self, eps_c: float):
+        check(self._h, self._L.dbsrg_set_eps_c(self._h, float(eps_c)), "set_eps_c")
+
+    def update_hw(self, ich, jch, v, w, c):
+        """UPDATE_HW (updates.f90:183-216): c v w^T into block (ich,jch)."""
+        p, kv = _ptr(v, np.float64)
+        q, kw = _ptr(w, np.float64)
+        check(self._h, self._L.dbsrg_update_hw(self._h, ich, jch, p, q, float(c)), "update_hw")
+
+    def update_hv(self, ich, ip, v, c):
+        """UPDATE_HV (updates.f90:220-242): c v into hcp(:, icb(ich,ip))."""
+        p, kv = _ptr(v, np.float64)
+        check(self._h, self._L.dbsrg_update_hv(self._h, ich, ip, p, float(c)), "update_hv")
+
+    def update_hb(self, ic, jc, c):
+        """UPDATE_HB (updates.f90:245-264): c into hp(ibb(ic,jc))."""
+        check(self._h, self._L.dbsrg_update_hb(self._h, ic, jc, float(c)), "update_hb")
+
     # -- energy functional and its gradient ------------------------------------
     def backward(self, k, i1, i2, i3, i4, coef, grad: bool = True):
         """(E, dE/dpq) of E = sum_e coef[e] R^k[e](i1,i2;i3,i4) over the orbitals

@@ -19,6 +19,8 @@
 //      element and applies the contributions in the reference's order
 //      (atype-major, then list order), so no atomics are needed and the
 //      result is deterministic.
+#include <memory>
+
 #include "internal.cuh"
 #include "ff.cuh"
 
@@ -600,12 +602,15 @@ struct ListPlan {
   std::vector<int> wchunk, wown, wtl;  // per window: [w], [w+1] ranges
   int own_off = 0;                     // acf owners inside `work`
   std::vector<XQuad> hxq;
+  // the structures that are not channel-pair contractions (structures.cu)
+  std::shared_ptr<StructPlan> sp;
 };
 
 size_t al256(size_t b) { return (b + 255) & ~(size_t)255; }
 
 // device bytes of one list's state
-size_t plan_bytes(const dbsrg_ctx *c, int icase, int n) {
+size_t plan_bytes(const dbsrg_ctx *c, int icase, int itype, int n) {
+  if (is_structure_list(icase, itype)) return structure_plan_bytes(c, icase, itype, n);
   const size_t ib = sizeof(int) * (size_t)n, db = sizeof(double) * (size_t)n;
   size_t t = 8 * al256(ib) + 2 * al256(db) + al256(sizeof(int) * (n + 2)) + al256(64) +
              al256(sizeof(SegInfo) * (size_t)(n + 1)) + al256(sizeof(int) * (size_t)(7 * (n + 1))) +
@@ -617,8 +622,8 @@ size_t plan_bytes(const dbsrg_ctx *c, int icase, int n) {
 }
 
 int plan_list(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const int *ipt,
-              const int *k1, const int *k2, const int *k3, const double *cdata, int blo0,
-              int nwin, int nw, void *dev, cudaStream_t ss, ListPlan &P) {
+              const int *k1, const int *k2, const int *k3, const int *k4, const double *cdata,
+              int blo0, int nwin, int nw, void *dev, cudaStream_t ss, ListPlan &P) {
   const DeviceGrid &g = c->g;
   const int ns = g.ns, ks = g.ks, ms = g.ms;
   int rc;
@@ -626,6 +631,14 @@ int plan_list(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const int *ip
   P.itype = itype;
   P.kpol = kpol;
   P.n = n;
+  if (is_structure_list(icase, itype)) {
+    StructPlan *sp = nullptr;
+    rc = plan_structures(c, icase, itype, kpol, n, ipt, k1, k2, k3, k4, cdata, blo0, nwin, nw,
+                         dev, ss, &sp);
+    if (rc) return rc;
+    P.sp.reset(sp, free_structure_plan);
+    return DBSRG_OK;
+  }
   // window of block b in the partition, -1 outside it
   auto wof = [&](int b) -> int {
     if (b < blo0) return -1;
@@ -671,7 +684,7 @@ int plan_list(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const int *ip
   // order kept within a block); entries below eps_c are dropped
   // (mod_dbsr_mat.f90:56)
   if (icase == 0) {
-    if (itype != 3) return set_err(c, DBSRG_EINVAL, "O_data: only itype 3 is supported");
+    if (itype != 3) return set_err(c, DBSRG_EINVAL, "O_data: unknown structure (itype)");
     const int iicc = c->iicc;
     P.vch = (double *)take(sizeof(double) * (size_t)ms * c->nbf);
     P.bstart = (int *)take(sizeof(int) * (2 * (size_t)(iicc + 2) + n));
@@ -686,7 +699,7 @@ int plan_list(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const int *ip
     std::vector<int> eblk(n, 0), hstart(iicc + 2, 0), hlist, horder(n);
     for (int e = 0; e < n; e++) {
       if (!std::isfinite(hcd[e])) return set_err(c, DBSRG_EINVAL, "non-finite coefficient in list");
-      if (std::fabs(hcd[e]) < 1.0e-10) continue;
+      if (std::fabs(hcd[e]) < c->eps_c) continue;
       const int i1 = hk1[e] / DBSRG_IBO, j1 = hk2[e] / DBSRG_IBO;
       if (i1 < 1 || i1 > c->nbf || j1 < 1 || j1 > c->nbf || hk1[e] % DBSRG_IBO < 1 ||
           hk1[e] % DBSRG_IBO > c->nbf || hk2[e] % DBSRG_IBO < 1 || hk2[e] % DBSRG_IBO > c->nbf)
@@ -743,8 +756,7 @@ int plan_list(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const int *ip
   // ---- the case: PQ types, storage and convol case
   P.factored = c->precision != DBSRG_PLAIN_FP64;
   if (icase == 2) {
-    if (itype != 3 && itype != 4)
-      return set_err(c, DBSRG_EINVAL, "R_data: only itypes 3 and 4 are supported");
+    if (itype != 3 && itype != 4) return set_err(c, DBSRG_EINVAL, "R_data: unknown itype");
     if (kpol < 0 || kpol > c->mk) return set_err(c, DBSRG_ERANGE, "R_data: kpol out of range");
     P.na = 4;
     P.tabfam = 0;
@@ -768,7 +780,7 @@ int plan_list(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const int *ip
   } else if (icase == 3) {
     int atype = itype / 10, it = itype % 10;
     if (atype < 0 || atype > 1 || it < 6 || it > 9)
-      return set_err(c, DBSRG_EINVAL, "S_data: only ktypes 6-9 and 16-19 are supported");
+      return set_err(c, DBSRG_EINVAL, "S_data: unknown itype");
     if (kpol < 0 || kpol > c->mk + 1) return set_err(c, DBSRG_ERANGE, "S_data: kpol out of range");
     int ip1, ip2, jp1, jp2, in;  // S_data.f90:74-97
     if (atype == 0) {
@@ -891,6 +903,7 @@ int exec_list(dbsrg_ctx *c, const ListPlan &P, int w, bool prep = false) {
   const int ns = g.ns, ks = g.ks, ms = g.ms;
   cudaStream_t st = c->stream;
   int rc;
+  if (P.sp) return exec_structures(c, *P.sp, w, prep);
   if (P.icase == 0) {
     if (prep) return DBSRG_OK;
     const int t0 = P.wtl[w], nt = P.wtl[w + 1] - t0;
@@ -1021,14 +1034,33 @@ int exec_list(dbsrg_ctx *c, const ListPlan &P, int w, bool prep = false) {
   return DBSRG_OK;
 }
 
+}  // namespace
+
+// convol cases 1/2 of nsg band densities X with one full table (k_band_contract)
+int band_contract(dbsrg_ctx *c, int kb, int icase, const double *rkb, int nsg, const double *X,
+                  double *Y) {
+  const int ns = c->g.ns;
+  const int nrt = (ns + GBM - 1) / GBM;
+  for (int s0 = 0; s0 < nsg; s0 += 65535 * GBN) {
+    const int nn = std::min(nsg - s0, 65535 * GBN);
+    const size_t off = (size_t)s0 * ns * kb;
+    dim3 gg((unsigned)(nrt * kb), (unsigned)((nn + GBN - 1) / GBN));
+    DBSRG_RUN(c, "k_band_contract",
+              k_band_contract<<<gg, 256, 0, c->stream>>>(ns, kb, icase, rkb, nn, X + off, Y + off));
+  }
+  return DBSRG_OK;
+}
+
+namespace {
+
 // The cached inputs of a planned list, built on the table stream of its k;
 // the contraction stream waits for them.  overlap: the contraction stream
 // holds nothing the builds read (only the kernels of earlier lists of this
 // assembly), so they may run beside it.
 int prepare_list(dbsrg_ctx *c, const ListPlan &P, bool overlap) {
-  if (P.icase == 0) return DBSRG_OK;
+  if (P.icase == 0 && !P.sp) return DBSRG_OK;
   int rc;
-  if (P.factored) {  // shared by the builds of every k
+  if (P.factored && !P.sp) {  // shared by the builds of every k
     bool built = false;
     if ((rc = ensure_bound_rows(c, &built))) return rc;
     if (built) overlap = false;
@@ -1060,7 +1092,6 @@ int prepare_list(dbsrg_ctx *c, const ListPlan &P, bool overlap) {
 int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const int *ipt,
                      const int *k1, const int *k2, const int *k3, const int *k4,
                      const double *cdata) {
-  (void)k4;
   if (n <= 0) return DBSRG_OK;
   if (!c->hch) return set_err(c, DBSRG_ESTATE, "no matrix allocated");
   if (!c->pq) return set_err(c, DBSRG_ESTATE, "no orbitals set");
@@ -1073,10 +1104,10 @@ int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const 
   const int par = c->lpar;
   c->lpar ^= 1;
   cudaStream_t ss = pipe ? c->sstream : st;
-  if ((rc = ensure_lstate(c, par, plan_bytes(c, icase, n)))) return rc;
+  if ((rc = ensure_lstate(c, par, plan_bytes(c, icase, itype, n)))) return rc;
   if (pipe) DBSRG_TRY(c, cudaStreamWaitEvent(ss, c->lfree[par], 0));
   ListPlan P;
-  if ((rc = plan_list(c, icase, itype, kpol, n, ipt, k1, k2, k3, cdata, c->wlo, c->wcap, 1,
+  if ((rc = plan_list(c, icase, itype, kpol, n, ipt, k1, k2, k3, k4, cdata, c->wlo, c->wcap, 1,
                       c->lstate[par], ss, P)))
     return rc;
   if (pipe) {  // the contraction waits for the set-up
@@ -1122,9 +1153,9 @@ int assemble_windows(dbsrg_ctx *c, int nlists, const dbsrg_list *lists, int nwin
       if (L.ncdata < 0) return set_err(c, DBSRG_EINVAL, "ncdata < 0");
       if (L.ncdata == 0) continue;
       if (!L.k1 || !L.k2 || !L.k3 || !L.cdata) return set_err(c, DBSRG_EINVAL, "null list pointer");
-      if (!(mem[l] = cache_alloc(c, plan_bytes(c, L.icase, L.ncdata))))
+      if (!(mem[l] = cache_alloc(c, plan_bytes(c, L.icase, L.itype, L.ncdata))))
         return set_err(c, DBSRG_ENOMEM, "list state allocation failed");
-      if ((rc = plan_list(c, L.icase, L.itype, L.kpol, L.ncdata, L.ipt, L.k1, L.k2, L.k3,
+      if ((rc = plan_list(c, L.icase, L.itype, L.kpol, L.ncdata, L.ipt, L.k1, L.k2, L.k3, L.k4,
                           L.cdata, 1, nwin, nw, mem[l], c->sstream, plans[l])))
         return rc;
       DBSRG_TRY(c, cudaEventRecord(c->lready, c->sstream));

@@ -310,6 +310,7 @@ int dbsrg_destroy(dbsrg_ctx *c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   basis_release(c);
   free_tables(c);
+  free_structures(c);
   pool_trim(c);
   DeviceGrid &g = c->g;
   double *arrs[] = {g.t, g.tp, g.tq, g.gx, g.gw, g.gr, g.grw, g.grm,
@@ -519,6 +520,7 @@ int dbsrg_set_orbitals(dbsrg_ctx *c, int nbf, const double *pq, const int *ipbs)
   DBSRG_TRY(c, cudaMalloc((void **)&c->b2o, (b2o.size() + 1) * sizeof(int)));
   if ((rc = copy_in(c, c->bmap, c->h_bmap.data(), nbf * sizeof(int)))) return rc;
   if (!b2o.empty() && (rc = copy_in(c, c->b2o, b2o.data(), b2o.size() * sizeof(int)))) return rc;
+  if (nbf != c->nbf) c->h_kbs.clear();  // the orbital kappas of dbsrg_set_dhl no longer apply
   c->nbf = nbf;
   DBSRG_TRY(c, cudaStreamSynchronize(c->stream));
   return DBSRG_OK;
@@ -537,6 +539,16 @@ int dbsrg_alloc_matrix_window(dbsrg_ctx *c, int nch, const int *icc, int iicc, i
   if (c->icc) cudaFree(c->icc);
   if (c->hmem) cudaFree(c->hmem);
   if (c->acf) cudaFree(c->acf);
+  // the perturber and target parts are laid out over the channels: a new
+  // matrix drops them (dbsrg_alloc_perturbers / dbsrg_set_targets again)
+  for (double **p : {&c->hcp, &c->hp, &c->htarg, &c->otarg}) {
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+  }
+  c->npert = c->iicb = c->iibb = c->ntarg = 0;
+  c->h_icb.clear();
+  c->h_ibb.clear();
+  c->h_iptar.clear();
   c->icc = nullptr;
   c->hch = c->hmem = nullptr;
   c->hcap = 0;
@@ -585,6 +597,8 @@ int dbsrg_zero_matrix(dbsrg_ctx *c) {
   const size_t ms = c->g.ms;
   DBSRG_TRY(c, cudaMemsetAsync(c->hch, 0, sizeof(double) * ms * ms * c->wcap, c->stream));
   DBSRG_TRY(c, cudaMemsetAsync(c->acf, 0, sizeof(double) * (size_t)c->iicc * (c->mk + 1), c->stream));
+  int rc = zero_structures(c);
+  if (rc) return rc;
   DBSRG_TRY(c, cudaStreamSynchronize(c->stream));
   return DBSRG_OK;
 }
@@ -676,6 +690,7 @@ int dbsrg_gen_batch_streamed(int nctx, dbsrg_ctx *const *ctxs, const int *nlists
       rc[i] = cuda_check(c, cudaGetLastError(), "acf");
       return;
     }
+    if ((rc[i] = zero_structures(c))) return;
     auto before = [&](int, double *slot) -> int {
       DBSRG_TRY(c, cudaMemsetAsync(slot, 0, sizeof(double) * blk * nwin, c->stream));
       return DBSRG_OK;
@@ -716,6 +731,8 @@ int dbsrg_assemble_to_host(dbsrg_ctx *c, int nlists, const dbsrg_list *lists, in
   const cudaMemcpyKind kind =
       is_device_ptr(hch_host) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
   DBSRG_TRY(c, cudaMemsetAsync(c->acf, 0, sizeof(double) * (size_t)iicc * (c->mk + 1), c->stream));
+  int rz = zero_structures(c);  // the perturber and target parts start from zero too
+  if (rz) return rz;
   // window w (slot w % 2) is assembled on the contraction stream while the
   // copy stream moves window w-1 out; a slot is zeroed again only after its
   // copy

@@ -197,6 +197,23 @@ struct dbsrg_ctx {
   };
   std::vector<TimedLaunch> tev;
   std::vector<cudaEvent_t> evpool;
+  // Matrix parts outside hch (structures.cu): perturber vectors hcp(ms,iicb)
+  // with icb(nch,npert) and perturber scalars hp(iibb) with ibb(npert,npert)
+  // (Alloc_dbsr_matrix, updates.f90:47-72); target interaction and overlap
+  // matrices htarg/otarg(ntarg(ntarg+1)/2) with iptar(nch) (Target_h,
+  // target_subs.f90:2-31); the one-electron Dirac matrices hd(ms,ms,nkap)
+  // of the kappas h_kap and the kappa of every orbital h_kbs (L_data);
+  // eps_c of the O and L lists (mod_dbsr_mat.f90:50)
+  int npert = 0, iicb = 0, iibb = 0;
+  std::vector<int> h_icb, h_ibb;
+  double *hcp = nullptr, *hp = nullptr;
+  int ntarg = 0, iitar = 0, check_target = 1;
+  std::vector<int> h_iptar;
+  double *htarg = nullptr, *otarg = nullptr;
+  int nkap = 0;
+  std::vector<int> h_kap, h_kbs;
+  double *hd = nullptr;
+  double eps_c = 1.0e-10;
 };
 
 cudaEvent_t event_get(dbsrg_ctx *c);
@@ -310,6 +327,10 @@ int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n,
                      const int *ipt, const int *k1, const int *k2,
                      const int *k3, const int *k4, const double *cdata);
 int update_hx(dbsrg_ctx *c, int ich, int jch, const double *d, double cc);
+// convol cases 1/2 (icase) of nsg band densities X[s][ns*kb] with the full
+// table rkb (kb = ks for R, 2ks-1 for S) into Y[s][ns*kb], on the context stream
+int band_contract(dbsrg_ctx *c, int kb, int icase, const double *rkb, int nsg, const double *X,
+                  double *Y);
 // Every list set up once, then executed window by window over the blocks
 // (windows of nwin blocks alternating between nslot slots of the matrix
 // allocation): before(w, slot) prepares a slot (on the contraction stream),
@@ -317,6 +338,27 @@ int update_hx(dbsrg_ctx *c, int ich, int jch, const double *d, double cc);
 int assemble_windows(dbsrg_ctx *c, int nlists, const dbsrg_list *lists, int nwin, int nslot,
                      const std::function<int(int w, double *slot)> &before,
                      const std::function<int(int w, int blo, int nb, double *slot)> &after);
+
+// ---- structures.cu --------------------------------------------------------
+// The list structures whose terms are not channel-pair contractions: R_data
+// itypes 1/2, S_data itypes 1-5, L_data itypes 1-3, O_data itypes 1/2/4.
+// A list is planned once on the host (entries classified, terms grouped by
+// the block, perturber column or scalar they update) and executed per block
+// window (its potentials, vectors and coefficients computed, the terms of
+// the window's blocks applied; perturber and target terms in the window that
+// holds block 1).
+struct StructPlan;
+bool is_structure_list(int icase, int itype);
+size_t structure_plan_bytes(const dbsrg_ctx *c, int icase, int itype, int n);
+int plan_structures(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const int *ipt,
+                    const int *k1, const int *k2, const int *k3, const int *k4,
+                    const double *cdata, int blo0, int nwin, int nw, void *dev,
+                    cudaStream_t ss, StructPlan **out);
+int exec_structures(dbsrg_ctx *c, const StructPlan &P, int w, bool prep);
+void free_structure_plan(StructPlan *P);
+// zeroes hcp, hp, htarg, otarg (with the matrix); frees them (destroy)
+int zero_structures(dbsrg_ctx *c);
+void free_structures(dbsrg_ctx *c);
 
 // ---- factor.cu ------------------------------------------------------------
 int ensure_fscratch(dbsrg_ctx *c, size_t bytes);

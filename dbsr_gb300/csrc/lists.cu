@@ -478,22 +478,12 @@ extern "C" int dbsrg_lists_gen_matrix(dbsrg_lists *L, dbsrg_ctx *ctx) {
   if (!L || !ctx) return DBSRG_EINVAL;
   finalize(L);
   // Add_matrix per (kpol, itype), kpol outer, itype inner (state_res.f90:187-191),
-  // for the channel-channel structures this library assembles: O itype 3,
-  // R itypes 3/4, S ktypes 6-9 and 16-19 (the others stay with the caller,
-  // dbsrg_lists_get)
-  auto assembled = [&](int itype) {
-    switch (L->icase) {
-      case 0: return itype == 3;
-      case 2: return itype == 3 || itype == 4;
-      case 3: return (itype % IBTYPE) >= 6 && (itype % IBTYPE) <= 9 && itype / IBTYPE <= 1;
-    }
-    return false;
-  };
+  // every non-empty list: Gen_matrix takes every structure of every icase
   std::vector<int> k1, k2, k3, k4;
   std::vector<double> cd;
   for (const auto &kv : L->merged) {
     const auto &v = kv.second;
-    if (v.empty() || !assembled(kv.first.second)) continue;
+    if (v.empty()) continue;
     k1.resize(v.size());
     k2.resize(v.size());
     k3.resize(v.size());

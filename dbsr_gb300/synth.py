@@ -190,6 +190,17 @@ class Workload:
     iicc: int
     mk: int
     lists: list = field(default_factory=list)  # of CList
+    # perturbers (hcp/hp numbering), targets and one-electron matrices, for
+    # the workloads that carry the bound-bound and bound-channel structures
+    npert: int = 0
+    icb: np.ndarray = None    # (nch, npert)
+    ibb: np.ndarray = None    # (npert, npert)
+    ntarg: int = 0
+    iptar: np.ndarray = None  # (nch,)
+    iitar: int = 0
+    kap_list: np.ndarray = None
+    hd: np.ndarray = None     # (ms, ms, nkap)
+    kbs: np.ndarray = None    # (nbf,)
 
     @property
     def ns(self):
@@ -469,3 +480,138 @@ def algorithmic_flops(w: Workload) -> dict:
             fl["density"] += L.n * 2 * ns * ((2 * ks - 1) if it <= 7 else ns)
     fl["total"] = fl["convol"] + fl["density"]
     return fl
+
+
+def perturber_numbering(nch: int, npert: int):
+    """icb(nch,npert) row by row and ibb(npert,npert) over the lower triangle
+    (Alloc_dbsr_matrix with one process, updates.f90:50-70)."""
+    icb = np.zeros((nch, npert), dtype=np.int32, order="F")
+    i = 0
+    for ich in range(nch):
+        for jp in range(npert):
+            i += 1
+            icb[ich, jp] = i
+    ibb = np.zeros((npert, npert), dtype=np.int32, order="F")
+    i = 0
+    for ip in range(npert):
+        for jp in range(ip + 1):
+            i += 1
+            ibb[ip, jp] = i
+            ibb[jp, ip] = i
+    return icb, ibb
+
+
+def structures_case(seed: int = 77, ns: int = 50, nch: int = 3, norb: int = 4, npert: int = 3,
+                    ntarg: int = 2, per_list: int = 24, mk: int = 2, iitar: int = 2,
+                    rmax: float = 20.0, z: float = 8.0) -> Workload:
+    """Lists of every structure that is not a channel-pair contraction --
+    R^k itypes 1 and 2 (R_data.f90:92-211), S^k ktypes 1-5 and 11-15
+    (S_data.f90:115-236), L itypes 1-3 (L_data.f90:46-132), O itypes 1, 2 and
+    4 (O_data.f90:33-78) -- with every routing of their K3/K4 codes
+    (Idef_Rtype / Idef_itype / Idef_Ltype / Idef_Otype, idef_type.f90), on a
+    small grid with perturbers, targets and seeded symmetric one-electron
+    matrices.  Coefficients uniform in [-1, 1]."""
+    w = small(ns=ns, nch=nch, mk=mk, n_entries=8, breit=False, seed=seed, rmax=rmax, z=z,
+              norb=norb)
+    rng = np.random.Generator(np.random.Philox(seed + 500))
+    nb = w.nbound
+    ch_orb = np.arange(nb + 1, nb + nch + 1)  # channel orbitals follow the bound ones
+    kbs = np.array(list(w.kappa_bound) + list(w.kappa_ch), dtype=np.int32)
+    kap_list = np.array(sorted(set(kbs.tolist())), dtype=np.int32)
+    ms = 2 * w.ns
+    hd = np.zeros((ms, ms, kap_list.size), order="F")
+    for k in range(kap_list.size):
+        a = rng.uniform(-1.0, 1.0, (ms, ms))
+        hd[:, :, k] = 0.5 * (a + a.T)
+    icb, ibb = perturber_numbering(nch, npert)
+    iptar = rng.integers(1, ntarg + 1, nch).astype(np.int32)
+
+    def bound():
+        return int(rng.integers(1, nb + 1))
+
+    def pair():
+        a, b = bound(), bound()
+        return min(a, b) * IBO + max(a, b)
+
+    def ovl():  # <channel orbital | bound orbital> code io = io1*ibo + io2
+        return int(ch_orb[rng.integers(0, nch)]) * IBO + bound()
+
+    def tgt():  # <channel orbital | channel orbital> code
+        return int(ch_orb[rng.integers(0, nch)]) * IBO + int(ch_orb[rng.integers(0, nch)])
+
+    def pert():
+        return int(rng.integers(1, npert + 1))
+
+    def chan():
+        return int(rng.integers(1, nch + 1))
+
+    def c():
+        return float(rng.uniform(-1.0, 1.0))
+
+    lists = []
+
+    def add(icase, itype, kpol, rows):
+        if rows:
+            k1, k2, k3, k4, cc = sort_merge(*zip(*rows))
+            lists.append(CList(icase, itype, kpol, k1, k2, k3, k4, cc))
+
+    # R^k / S^k itype 1: K1, K2 bound pairs; K3/K4 = (-ic,-jc), (io,-ic), (io,jo), (io,0)
+    def bound_rows():
+        rows = []
+        for _ in range(per_list):
+            r = int(rng.integers(0, 4))
+            k3, k4 = ((-pert(), -pert()), (ovl(), -pert()), (ovl(), ovl()), (tgt(), 0))[r]
+            rows.append((pair(), pair(), k3, k4, c()))
+        return rows
+
+    # itype 2: K1 bound pair, K2 bound orbital, K3 channel, K4 = io or -ic
+    def channel_rows():
+        rows = []
+        for _ in range(per_list):
+            k4 = ovl() if rng.integers(0, 2) else -pert()
+            rows.append((pair(), bound(), chan(), k4, c()))
+        return rows
+
+    for k in range(mk + 1):
+        add(2, 1, k, bound_rows())
+        add(2, 2, k, channel_rows())
+    for v in (0, mk + 1):
+        for at in (0, 1):
+            add(3, 10 * at + 1, v, bound_rows())
+            for it in (2, 3, 4, 5):
+                add(3, 10 * at + it, v, channel_rows())
+    # L itype 1: K1 <= K2 bound orbitals of one kappa; K3/K4 = (ic,jc), (-io,ic),
+    # (-io,-jo), (-io,0)
+    by_kappa = {}
+    for o in range(1, nb + 1):
+        by_kappa.setdefault(int(kbs[o - 1]), []).append(o)
+    rows = []
+    for _ in range(per_list):
+        grp = list(by_kappa.values())[int(rng.integers(0, len(by_kappa)))]
+        a, b = (int(x) for x in rng.choice(grp, 2))
+        r = int(rng.integers(0, 4))
+        k3, k4 = ((pert(), pert()), (-ovl(), pert()), (-ovl(), -ovl()), (-tgt(), 0))[r]
+        rows.append((min(a, b), max(a, b), k3, k4, c()))
+    add(1, 1, 0, rows)
+    # L itype 2: K1 bound orbital, K2 channel, K3 = ic or -io
+    rows = [(bound(), chan(), (pert() if rng.integers(0, 2) else -ovl()), 0, c())
+            for _ in range(per_list)]
+    add(1, 2, 0, rows)
+    # L itype 3: channel orbitals of one kappa
+    rows = []
+    for _ in range(per_list):
+        i, j = (int(x) for x in rng.integers(0, nch, 2))
+        if kbs[ch_orb[i] - 1] != kbs[ch_orb[j] - 1]:
+            j = i
+        rows.append((int(ch_orb[i]), int(ch_orb[j]), 0, 0, c()))
+    add(1, 3, 0, rows)
+    # O itypes 1, 2, 4
+    add(0, 1, 0, [(pert(), pert(), 0, 0, c()) for _ in range(per_list)])
+    add(0, 2, 0, [(ovl(), pert(), 0, 0, c()) for _ in range(per_list)])
+    add(0, 4, 0, [(tgt(), 0, 0, 0, c()) for _ in range(per_list)])
+    w.name = f"structures ns={w.ns} nch={nch} npert={npert} ntarg={ntarg}"
+    w.lists = lists
+    w.npert, w.icb, w.ibb = npert, icb, ibb
+    w.ntarg, w.iptar, w.iitar = ntarg, iptar, iitar
+    w.kap_list, w.hd, w.kbs = kap_list, hd, kbs
+    return w

@@ -8,9 +8,10 @@
  *   - B-spline grid and Gauss tables      dbsr_lib_dbs.f90:911-1102
  *   - cell moments and R^k/S^k tables    dbsr_lib_dbs.f90:1234-1720,2898-3936
  *   - density / convol / convol_sk       dbsr_lib_dbs.f90:2208-2891
- *   - R_data / S_data / O_data dispatch  DBSR_MAT3/R_data.f90, S_data.f90,
- *                                        O_data.f90
- *   - UPDATE_HS / UPDATE_HW / UPDATE_HX  DBSR_MAT3/updates.f90:79-292
+ *   - R_data / S_data / L_data / O_data DBSR_MAT3/R_data.f90, S_data.f90,
+ *     dispatch                          L_data.f90, O_data.f90
+ *   - UPDATE_HS/HW/HV/HB/HX/ACF,        DBSR_MAT3/updates.f90:79-292,
+ *     Target_h                          target_subs.f90:2-31
  * The Fortran caller keeps its module data; these entry points receive
  * that data explicitly (plain pointers and sizes, Fortran column-major
  * layout, 1-based orbital/channel/block numbers exactly as in the
@@ -117,11 +118,21 @@ int dbsrg_set_precision(dbsrg_ctx *ctx, int precision);
  * coefficient list exactly as Add_matrix leaves it (MOD_c_data.f90:318-
  * 368): entries ipt(1:ncdata) index the arrays k1..k4, cdata, sorted by
  * (K1,K2,K3,K4).  ipt may be NULL for the identity order.
- *   icase 0: overlaps, itype 3 (O_data.f90:50-61)
- *   icase 2: R^k, itype 3 direct / 4 exchange, all four atypes
- *            (R_data.f90:214-277)
- *   icase 3: S^k, ktype = 10*atype + itype, itype 6..9 (S_data.f90:240-274)
- * Adds into hch and acf. */
+ *   icase 0: overlaps O_data (O_data.f90:2-90), itypes 1-4
+ *   icase 1: one-electron L_data (L_data.f90:2-145), itypes 1-3; needs
+ *            dbsrg_set_dhl
+ *   icase 2: R^k R_data (R_data.f90:2-290), itypes 1-4, all four atypes
+ *   icase 3: S^k S_data (S_data.f90:2-287), ktype = 10*atype + itype,
+ *            itypes 1-9
+ * Adds into hch and acf, and into the perturber parts hcp/hp
+ * (dbsrg_alloc_perturbers) and the target matrices htarg/otarg
+ * (dbsrg_set_targets) where the structure updates them.  The perturber
+ * and target terms of a list are added when the current window holds
+ * block 1 (always without windows).  Entries the reference would stop on
+ * (an index out of range, a perturber term without perturbers, an unknown
+ * structure) give DBSRG_ERANGE / DBSRG_EINVAL and nothing of the list is
+ * added.  k4 may be NULL (all zero) except for the structures that read it
+ * (R and S itype 1 and 2, L itype 1). */
 int dbsrg_gen_matrix(dbsrg_ctx *ctx, int icase, int itype, int kpol,
                      int ncdata, const int *ipt, const int *k1,
                      const int *k2, const int *k3, const int *k4,
@@ -169,8 +180,10 @@ int dbsrg_gen_batch_streamed(int nctx, dbsrg_ctx *const *ctxs,
  * allocation, and while one window is assembled the previous one is copied
  * out on a separate stream, so the copy hides behind the assembly.
  * The allocation must hold two windows (or nwin >= iicc).  The device
- * matrix is overwritten; acf is zeroed first.  Lists are as for
- * dbsrg_gen_batch (one context). */
+ * matrix is overwritten; acf, and the perturber and target parts when
+ * held, are zeroed first and hold the list's terms at the end (read them
+ * with dbsrg_get_acf / dbsrg_get_perturbers / dbsrg_get_targets).  Lists
+ * are as for dbsrg_gen_batch (one context). */
 int dbsrg_assemble_to_host(dbsrg_ctx *ctx, int nlists, const dbsrg_list *lists,
                            int nwin, double *hch_host, double *acf_host);
 
@@ -178,6 +191,51 @@ int dbsrg_assemble_to_host(dbsrg_ctx *ctx, int nlists, const dbsrg_list *lists,
  * host or device) to the block of channel pair (ich,jch). */
 int dbsrg_update_hx(dbsrg_ctx *ctx, int ich, int jch, const double *d,
                     double c);
+/* UPDATE_HW(ich,jch,v,w,C) (updates.f90:183-216): the rank-1 term C v w^T
+ * (v, w of length ms, host or device) into the block of (ich,jch),
+ * transposed for ich < jch and symmetrised with C/2 for ich = jch. */
+int dbsrg_update_hw(dbsrg_ctx *ctx, int ich, int jch, const double *v,
+                    const double *w, double c);
+/* UPDATE_HV(ich,ip,v,C) (updates.f90:220-242): C v into the channel-
+ * perturber vector hcp(:,icb(ich,ip)).  UPDATE_HB(ic,jc,C) (:245-264): C
+ * into the perturber scalar hp(ibb(ic,jc)). */
+int dbsrg_update_hv(dbsrg_ctx *ctx, int ich, int ip, const double *v,
+                    double c);
+int dbsrg_update_hb(dbsrg_ctx *ctx, int ic, int jc, double c);
+
+/* Perturber part of the matrix (Alloc_dbsr_matrix, updates.f90:47-72):
+ * hcp(ms,iicb) channel-perturber vectors numbered by icb(nch,npert) and
+ * hp(iibb) perturber-perturber scalars numbered by ibb(npert,npert)
+ * (1-based, 0 = not held; host or device arrays), on the device, zeroed
+ * here and by dbsrg_zero_matrix.  npert = 0 frees them.  A new
+ * dbsrg_alloc_matrix drops them.  dbsrg_get_perturbers copies them out
+ * (either pointer may be NULL). */
+int dbsrg_alloc_perturbers(dbsrg_ctx *ctx, int npert, const int *icb,
+                           int iicb, const int *ibb, int iibb);
+int dbsrg_get_perturbers(dbsrg_ctx *ctx, double *hcp, double *hp);
+
+/* Target interaction and overlap matrices of Target_h (target_subs.f90:
+ * 2-31): htarg and otarg of ntarg(ntarg+1)/2 elements, iptar(nch) the
+ * target of each channel, and the switches iitar (UPDATE_HX of the target
+ * structures for iitar > 0 or > 1, as R/S/L_data and O_data test them) and
+ * check_target (L_data itype 3) of mod_dbsr_mat.f90:72-76 (defaults 0 and
+ * 1).  Zeroed here and by dbsrg_zero_matrix; a new dbsrg_alloc_matrix drops
+ * them.  Without targets (ntarg = 0, the default) Target_h adds nothing. */
+int dbsrg_set_targets(dbsrg_ctx *ctx, int ntarg, const int *iptar, int iitar,
+                      int check_target);
+int dbsrg_get_targets(dbsrg_ctx *ctx, double *htarg, double *otarg);
+
+/* One-electron Dirac matrices for L_data (module dhl_core of the external
+ * library, Gen_dhl_core sub1.f90:23): hd(ms,ms,nkap) for the kappas
+ * kap_list(nkap), and kbs(nbf) the kappa of every orbital of
+ * dbsrg_set_orbitals (call it after that).  L_data's Lval(i,j) is taken as
+ * p_i^T hd(kappa_i) p_j and Gen_Lvec(i) as hd(kappa_i) p_i with p = (P; Q),
+ * and itype 3 adds hd(kappa) itself. */
+int dbsrg_set_dhl(dbsrg_ctx *ctx, int nkap, const int *kap_list,
+                  const double *hd, const int *kbs);
+/* eps_c of the O and L lists (mod_dbsr_mat.f90:50, default 1e-10):
+ * coefficients below it are skipped (O_data.f90:35, L_data.f90:48). */
+int dbsrg_set_eps_c(dbsrg_ctx *ctx, double eps_c);
 
 /* Energy functional and its gradient (the SCF potentials of DBSR_HF /
  * DBSR_MCHF, hf_matrix.f90:2-163): E = sum_e coef[e] *
@@ -294,8 +352,7 @@ int dbsrg_lists_add(dbsrg_lists *lists, int n, const int *kpol, const int *i1,
 int dbsrg_lists_count(dbsrg_lists *lists, int kpol, int itype);
 int dbsrg_lists_get(dbsrg_lists *lists, int kpol, int itype, int *k1,
                     int *k2, int *k3, int *k4, double *cdata);
-/* Add_matrix for every non-empty list this library assembles (O itype 3, R
- * itypes 3/4, S ktypes 6-9 and 16-19), kpol outer and itype inner as
+/* Add_matrix for every non-empty list, kpol outer and itype inner as
  * State_res calls it (state_res.f90:187-191): dbsrg_gen_matrix on ctx. */
 int dbsrg_lists_gen_matrix(dbsrg_lists *lists, dbsrg_ctx *ctx);
 

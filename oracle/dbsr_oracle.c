@@ -1144,8 +1144,41 @@ orc_mat *orc_mat_new(const orc_grid *g, int nbf, const double *pq,
   m->kmax_cache = mk + 2;
   m->rcache = (double **)calloc((size_t)(m->kmax_cache + 1) * 4, sizeof(double *));
   m->scache = (double **)calloc((size_t)(m->kmax_cache + 1) * 2, sizeof(double *));
+  m->eps_c = 1.0e-10;
+  m->check_target = 1;
   return m;
 }
+
+void orc_mat_set_perturbers(orc_mat *m, int npert, const int *icb, int iicb,
+                            const int *ibb, int iibb, double *hcp, double *hp) {
+  m->npert = npert;
+  m->icb = icb;
+  m->iicb = iicb;
+  m->ibb = ibb;
+  m->iibb = iibb;
+  m->hcp = hcp;
+  m->hp = hp;
+}
+
+void orc_mat_set_targets(orc_mat *m, int ntarg, const int *iptar, double *htarg,
+                         double *otarg, int iitar, int check_target) {
+  m->ntarg = ntarg;
+  m->iptar = iptar;
+  m->htarg = htarg;
+  m->otarg = otarg;
+  m->iitar = iitar;
+  m->check_target = check_target;
+}
+
+void orc_mat_set_dhl(orc_mat *m, int nkap, const int *kap_list, const double *hd,
+                     const int *kbs) {
+  m->nkap = nkap;
+  m->kap_list = kap_list;
+  m->hd = hd;
+  m->kbs = kbs;
+}
+
+void orc_mat_set_eps_c(orc_mat *m, double eps_c) { m->eps_c = eps_c; }
 
 void orc_mat_free(orc_mat *m) {
   if (!m) return;
@@ -1441,18 +1474,220 @@ void orc_v_ch(const orc_grid *g, const double *pq_b, double *v) {
 
 #define PQ(orb, comp) (m->pq + (size_t)ns * ((comp)-1) + (size_t)2 * ns * ((orb)-1))
 
+/* KBORT restatement (not in the reference snapshot): the index of the
+ * overlap vector V_ch of channel orbital io1 with bound orbital io2 is io2
+ * (V_ch is the overlap vector of io2, orc_v_ch); 0 when io1 is not a
+ * channel orbital or an index is out of range. */
+static int kbort(const orc_mat *m, int io1, int io2) {
+  if (io1 < 1 || io1 > m->nbf || io2 < 1 || io2 > m->nbf) return 0;
+  const int ich = m->ipbs[io1 - 1];
+  if (ich < 1 || ich > m->nch) return 0;
+  return io2;
+}
+
+/* the UPDATE_* bound checks (updates.f90:91-94,153-159,196-199): -4 */
+static int block_of(const orc_mat *m, int ich, int jch) {
+  if (ich < 1 || jch < 1 || ich > m->nch || jch > m->nch) return 0;
+  int b = ICC(ich, jch);
+  return (b >= 1 && b <= m->iicc) ? b : 0;
+}
+static int update_hw_checked(orc_mat *m, int ich, int jch, const double *v,
+                             const double *w, double c) {
+  if (!block_of(m, ich, jch)) return -4;
+  orc_update_hw(m, ich, jch, v, w, c);
+  return 0;
+}
+static int update_hx_checked(orc_mat *m, int ich, int jch, const double *d, double c) {
+  if (!block_of(m, ich, jch)) return -4;
+  orc_update_hx(m, ich, jch, d, c);
+  return 0;
+}
+
+/* UPDATE_HV: updates.f90:220-242 */
+int orc_update_hv(orc_mat *m, int ich, int ip, const double *v, double c) {
+  const int ms = m->g->ms;
+  if (ich < 1 || ich > m->nch || ip < 1 || ip > m->npert) return -4;
+  int i = A2(m->icb, ich, ip, m->nch);
+  if (i < 1 || i > m->iicb) return -4;
+  for (int r = 1; r <= ms; r++) A2(m->hcp, r, i, ms) = A2(m->hcp, r, i, ms) + c * v[r - 1];
+  return 0;
+}
+
+/* UPDATE_HB: updates.f90:245-264 */
+int orc_update_hb(orc_mat *m, int ic, int jc, double c) {
+  if (ic > m->npert || jc > m->npert || ic <= 0 || jc <= 0) return -4;
+  int i = A2(m->ibb, ic, jc, m->npert);
+  if (i < 1 || i > m->iibb) return -4;
+  m->hp[i - 1] = m->hp[i - 1] + c;
+  return 0;
+}
+
+/* Target_h: target_subs.f90:2-31 (nothing when no targets are given) */
+static int target_h(orc_mat *m, int ich, int jch, double c, double cc) {
+  if (m->ntarg <= 0) return 0;
+  if (ich < 0 || jch < 0 || ich > m->nch || jch > m->nch) return -4;
+  if (ich < 1 || jch < 1 || ICC(ich, jch) == 0) return 0;
+  int it = m->iptar[ich - 1], jt = m->iptar[jch - 1];
+  int i = it > jt ? it : jt, j = it > jt ? jt : it;
+  if (j < 1 || i > m->ntarg) return -4;
+  int ij = (i - 1) * i / 2 + j;
+  m->htarg[ij - 1] = m->htarg[ij - 1] + c;
+  m->otarg[ij - 1] = m->otarg[ij - 1] + cc;
+  return 0;
+}
+
+/* BAV restatement: band matrix (storage sym) times vector, from the right
+ * (dir 'r': v = A b) or the left ('l': v = A^T b); the band entries are
+ * visited column of the band by column (jp outer), rows inner. */
+void orc_bav(int ns, int ks, const double *a, const double *b, double *v,
+             char sym, char dir) {
+  for (int i = 1; i <= ns; i++) v[i - 1] = 0.0;
+  if (sym == 's') {
+    for (int jp = 1; jp <= ks; jp++)
+      for (int i = 1; i <= ns - jp + 1; i++) {
+        int j = i + jp - 1;
+        double x = A2(a, i, jp, ns);
+        v[i - 1] = v[i - 1] + x * b[j - 1];
+        if (jp > 1) v[j - 1] = v[j - 1] + x * b[i - 1];
+      }
+  } else {
+    for (int jp = 1; jp <= 2 * ks - 1; jp++) {
+      int i0 = imax(1, 1 + ks - jp), i1 = imin(ns, ns + ks - jp);
+      for (int i = i0; i <= i1; i++) {
+        int j = i + jp - ks;
+        double x = A2(a, i, jp, ns);
+        if (dir == 'l')
+          v[j - 1] = v[j - 1] + x * b[i - 1];
+        else
+          v[i - 1] = v[i - 1] + x * b[j - 1];
+      }
+    }
+  }
+}
+
+/* Structures 1.x (bound-bound integral times overlap factors) of R_data
+ * (R_data.f90:92-163) and S_data (S_data.f90:115-187): the routing of
+ * C = S * cdata by the signs of ic = -k3, jc = -k4. */
+static int route_bound(orc_mat *m, int k3, int k4, double C, double *vv, double *ww) {
+  const orc_grid *g = m->g;
+  const int ns = g->ns;
+  int ic = -k3, jc = -k4, io = -ic, jo = -jc;
+  if (ic > 0 && jc > 0) return orc_update_hb(m, ic, jc, C);
+  if (ic < 0 && jc > 0) {
+    int o1 = io / ORC_IBO, o2 = io % ORC_IBO;
+    if (!kbort(m, o1, o2)) return -4;
+    orc_v_ch(g, PQ(o2, 1), vv);
+    return orc_update_hv(m, m->ipbs[o1 - 1], jc, vv, C);
+  }
+  if (ic < 0 && jc < 0) {
+    int o1 = io / ORC_IBO, o2 = io % ORC_IBO, p1 = jo / ORC_IBO, p2 = jo % ORC_IBO;
+    if (!kbort(m, o1, o2) || !kbort(m, p1, p2)) return -4;
+    orc_v_ch(g, PQ(o2, 1), vv);
+    orc_v_ch(g, PQ(p2, 1), ww);
+    return update_hw_checked(m, m->ipbs[o1 - 1], m->ipbs[p1 - 1], vv, ww, C);
+  }
+  if (ic < 0 && jc == 0) {
+    int o1 = io / ORC_IBO, o2 = io % ORC_IBO;
+    if (o1 < 1 || o1 > m->nbf || o2 < 1 || o2 > m->nbf) return -4;
+    int ich = m->ipbs[o1 - 1], jch = m->ipbs[o2 - 1];
+    int rc = target_h(m, ich, jch, C, 0.0);
+    if (rc) return rc;
+    if (m->iitar > 0 && ich != jch) return update_hx_checked(m, ich, jch, g->fppqq, C);
+    return 0;
+  }
+  return -1;
+}
+
+/* Structures 2.x (channel orbital in one position of the integral) of
+ * R_data (R_data.f90:167-211) and S_data (S_data.f90:191-236): vv carries
+ * the potential-times-orbital vector in its P or Q half; io = k4 > 0 gives
+ * UPDATE_HW with V_ch, io < 0 UPDATE_HV. */
+static int route_channel(orc_mat *m, int ich, int io, double C, const double *vv, double *ww) {
+  const orc_grid *g = m->g;
+  const int ns = g->ns;
+  if (io > 0) {
+    int o1 = io / ORC_IBO, o2 = io % ORC_IBO;
+    if (!kbort(m, o1, o2)) return -4;
+    orc_v_ch(g, PQ(o2, 1), ww);
+    return update_hw_checked(m, ich, m->ipbs[o1 - 1], vv, ww, C);
+  }
+  if (io < 0) return orc_update_hv(m, ich, -io, vv, C);
+  return -1;
+}
+
+/* itypes 1 and 2 of one table (R or S): density/convol of the bound pair
+ * K1, then SUM_AmB with the density of K2 (itype 1) or BAV with orbital K2
+ * (itype 2, placed into the half of component ipv). */
+static int bound_structures(orc_mat *m, int itype, const double *rkb, int kb, char sym,
+                            int in, int ip1, int ip2, int jp1, int jp2, int ipo, int ipv,
+                            char sym_v, int ncdata, const int *ipt, const int *k1,
+                            const int *k2, const int *k3, const int *k4,
+                            const double *cdata) {
+  const orc_grid *g = m->g;
+  const int ns = g->ns, ks = g->ks, ms = g->ms;
+  size_t nn = (size_t)ns * ns;
+  double *d = (double *)calloc(nn, sizeof(double));
+  double *xx = (double *)calloc(nn, sizeof(double));
+  double *dd = (double *)calloc(nn, sizeof(double));
+  double *v = (double *)calloc(ns, sizeof(double));
+  double *vv = (double *)calloc(ms, sizeof(double));
+  double *ww = (double *)calloc(ms, sizeof(double));
+  int rc = 0, iii = 0, jjj = 0;
+  double S = 0.0;
+  for (int j = 1; j <= ncdata && !rc; j++) {
+    int i = ipt[j - 1];
+    if (itype == 1) {
+      int K1 = k1[i - 1], K2 = k2[i - 1];
+      int i1 = K1 / ORC_IBO, i2 = K1 % ORC_IBO, j1 = K2 / ORC_IBO, j2 = K2 % ORC_IBO;
+      if (i1 < 1 || i1 > m->nbf || i2 < 1 || i2 > m->nbf || j1 < 1 || j1 > m->nbf ||
+          j2 < 1 || j2 > m->nbf) { rc = -4; break; }
+      if (K1 != iii) {
+        orc_density(ns, ks, d, PQ(i1, ip1), PQ(i2, ip2), sym);
+        orc_convol(ns, ks, kb, rkb, xx, d, in, sym, sym);
+      }
+      if (K2 != jjj) orc_density(ns, ks, dd, PQ(j1, jp1), PQ(j2, jp2), sym);
+      if (K1 != iii || K2 != jjj) S = orc_sum_amb(ns, ks, xx, dd, sym);
+      iii = K1;
+      jjj = K2;
+      rc = route_bound(m, k3[i - 1], k4[i - 1], S * cdata[i - 1], vv, ww);
+    } else {
+      int jj = k1[i - 1], ii = k2[i - 1], ich = k3[i - 1], io = k4[i - 1];
+      int j1 = jj / ORC_IBO, j2 = jj % ORC_IBO;
+      if (j1 < 1 || j1 > m->nbf || j2 < 1 || j2 > m->nbf || ii < 1 || ii > m->nbf) {
+        rc = -4;
+        break;
+      }
+      if (jj != jjj || ii != iii) {
+        if (jj != jjj) {
+          orc_density(ns, ks, dd, PQ(j1, jp1), PQ(j2, jp2), sym);
+          orc_convol(ns, ks, kb, rkb, xx, dd, in, sym, sym);
+          jjj = jj;
+        }
+        orc_bav(ns, ks, xx, PQ(ii, ipo), v, sym, sym_v);
+        iii = ii;
+      }
+      for (int r = 0; r < ms; r++) vv[r] = 0.0;
+      for (int r = 0; r < ns; r++) vv[(size_t)ns * (ipv - 1) + r] = v[r];
+      rc = route_channel(m, ich, io, cdata[i - 1], vv, ww);
+    }
+  }
+  free(d); free(xx); free(dd); free(v); free(vv); free(ww);
+  return rc;
+}
+
 /* R_data itype 3 (direct) and 4 (exchange): DBSR_MAT3/R_data.f90:56-86,
  * 214-277.  QUADR_PQ (not in the reference snapshot) is restated as the
  * component of quadr selected by atype (P for atype 0, Q for atype 1). */
 static int r_data(orc_mat *m, int itype, int kpol, int btype, int ncdata,
                   const int *ipt, const int *k1, const int *k2, const int *k3,
-                  const double *cdata) {
+                  const int *k4, const double *cdata) {
   const orc_grid *g = m->g;
   const int ns = g->ns, ks = g->ks;
   int ip1, ip2, jp1, jp2, in;
   char sym_d, sym_r;
   if (itype == 3) { in = 1; sym_d = 's'; sym_r = 's'; }
   else if (itype == 4) { in = 3; sym_d = 'x'; sym_r = 'x'; }
+  else if (itype == 1 || itype == 2) { in = 3 - itype; sym_d = 's'; sym_r = 's'; }
   else return -2;
   int atype = btype;
   switch (atype) {
@@ -1466,6 +1701,10 @@ static int r_data(orc_mat *m, int itype, int kpol, int btype, int ncdata,
       break;
   }
   const double *rkb = rtable(m, atype, kpol);
+  if (itype <= 2)  /* R_data.f90:92-211; BAV with orbital K2 on ip1, into half ip2 */
+    return bound_structures(m, itype, rkb, ks, 's', in, ip1, ip2, jp1, jp2, ip1, ip2, 'r',
+                            ncdata, ipt, k1, k2, k3, k4, cdata);
+  (void)sym_r;
   size_t nn = (size_t)ns * ns;
   double *xx = (double *)calloc(nn, sizeof(double));
   double *dd = (double *)calloc(nn, sizeof(double));
@@ -1498,13 +1737,37 @@ static int r_data(orc_mat *m, int itype, int kpol, int btype, int ncdata,
 /* S_data itypes 6-9: DBSR_MAT3/S_data.f90:67-113, 240-274, with the
  * contraction taken with convol_sk semantics (the S^k table). */
 static int s_data(orc_mat *m, int ktype, int kpol, int ncdata, const int *ipt,
-                  const int *k1, const int *k2, const int *k3,
+                  const int *k1, const int *k2, const int *k3, const int *k4,
                   const double *cdata) {
   const orc_grid *g = m->g;
   const int ns = g->ns, ks = g->ks;
   int atype = ktype / 10, itype = ktype % 10;
   int ip1, ip2, jp1, jp2, in;
-  if (itype < 6 || itype > 9 || atype < 0 || atype > 1) return -2;
+  if (itype < 1 || itype > 9 || atype < 0 || atype > 1) return -2;
+  if (itype <= 5) {  /* S_data.f90:74-97 (itypes 1-5), 115-236 */
+    char sym_v = 'r';
+    if (atype == 0) {
+      switch (itype) {
+        case 1: ip1 = 1; ip2 = 2; jp1 = 1; jp2 = 2; in = 2; break;
+        case 2: ip1 = 1; ip2 = 2; jp1 = 1; jp2 = 2; in = 1; sym_v = 'r'; break;
+        case 3: ip1 = 1; ip2 = 2; jp1 = 1; jp2 = 2; in = 2; sym_v = 'r'; break;
+        case 4: ip1 = 2; ip2 = 1; jp1 = 1; jp2 = 2; in = 1; sym_v = 'l'; break;
+        default: ip1 = 2; ip2 = 1; jp1 = 1; jp2 = 2; in = 2; sym_v = 'l'; break;
+      }
+    } else {
+      switch (itype) {
+        case 1: ip1 = 1; ip2 = 2; jp1 = 2; jp2 = 1; in = 2; break;
+        case 2: ip1 = 1; ip2 = 2; jp1 = 2; jp2 = 1; in = 1; sym_v = 'r'; break;
+        case 3: ip1 = 2; ip2 = 1; jp1 = 1; jp2 = 2; in = 2; sym_v = 'r'; break;
+        case 4: ip1 = 2; ip2 = 1; jp1 = 2; jp2 = 1; in = 1; sym_v = 'l'; break;
+        default: ip1 = 1; ip2 = 2; jp1 = 1; jp2 = 2; in = 2; sym_v = 'l'; break;
+      }
+    }
+    const double *rkb = stable(m, atype, kpol);
+    /* BAV with orbital K2 on component ip2, into half ip2 (S_data.f90:205-211) */
+    return bound_structures(m, itype == 1 ? 1 : 2, rkb, 2 * ks - 1, 'n', in, ip1, ip2, jp1,
+                            jp2, ip2, ip2, sym_v, ncdata, ipt, k1, k2, k3, k4, cdata);
+  }
   if (atype == 0) {
     switch (itype) {
       case 6: ip1 = 1; ip2 = 2; jp1 = 1; jp2 = 2; in = 1; break;
@@ -1544,49 +1807,176 @@ static int s_data(orc_mat *m, int ktype, int kpol, int ncdata, const int *ipt,
   return 0;
 }
 
-/* O_data itype 3 (<i|.><.|j> rank-1 overlaps): O_data.f90:50-61 */
+/* O_data: DBSR_MAT3/O_data.f90:2-90.  itype 1 <ic|jc> (UPDATE_HB), 2
+ * <i|.> jc (UPDATE_HV), 3 <i|.><.|j> (UPDATE_HW), 4 <i|j> (Target_h, and
+ * UPDATE_HX with fppqq for iitar > 1 and ich != jch); coefficients below
+ * eps_c are skipped. */
 static int o_data(orc_mat *m, int itype, int ncdata, const int *ipt,
                   const int *k1, const int *k2, const double *cdata) {
   const orc_grid *g = m->g;
   const int ns = g->ns, ms = g->ms;
-  if (itype != 3) return -2;
+  if (itype < 1 || itype > 4) return -2;
   double *v = (double *)malloc(sizeof(double) * ms);
   double *w = (double *)malloc(sizeof(double) * ms);
-  for (int j = 1; j <= ncdata; j++) {
+  int rc = 0;
+  for (int j = 1; j <= ncdata && !rc; j++) {
     int i = ipt[j - 1];
     double C = cdata[i - 1];
-    if (fabs(C) < 1.0e-10) continue; /* eps_c, mod_dbsr_mat.f90:56 */
-    int io = k1[i - 1], jo = k2[i - 1];
-    int i1 = io / ORC_IBO, i2 = io % ORC_IBO;
-    int j1 = jo / ORC_IBO, j2 = jo % ORC_IBO;
-    orc_v_ch(g, PQ(i2, 1), v);
-    orc_v_ch(g, PQ(j2, 1), w);
-    orc_update_hw(m, m->ipbs[i1 - 1], m->ipbs[j1 - 1], v, w, C);
+    if (fabs(C) < m->eps_c) continue;
+    if (itype == 1) {
+      rc = orc_update_hb(m, k1[i - 1], k2[i - 1], C);
+    } else if (itype == 2) {
+      int io = k1[i - 1], jc = k2[i - 1];
+      int i1 = io / ORC_IBO, i2 = io % ORC_IBO;
+      if (!kbort(m, i1, i2)) { rc = -4; break; }
+      orc_v_ch(g, PQ(i2, 1), v);
+      rc = orc_update_hv(m, m->ipbs[i1 - 1], jc, v, C);
+    } else if (itype == 3) {
+      int io = k1[i - 1], jo = k2[i - 1];
+      int i1 = io / ORC_IBO, i2 = io % ORC_IBO;
+      int j1 = jo / ORC_IBO, j2 = jo % ORC_IBO;
+      if (!kbort(m, i1, i2) || !kbort(m, j1, j2)) { rc = -4; break; }
+      orc_v_ch(g, PQ(i2, 1), v);
+      orc_v_ch(g, PQ(j2, 1), w);
+      rc = update_hw_checked(m, m->ipbs[i1 - 1], m->ipbs[j1 - 1], v, w, C);
+    } else {
+      int io = k1[i - 1], i1 = io / ORC_IBO, i2 = io % ORC_IBO;
+      if (i1 < 1 || i1 > m->nbf || i2 < 1 || i2 > m->nbf) { rc = -4; break; }
+      int ich = m->ipbs[i1 - 1], jch = m->ipbs[i2 - 1];
+      if ((rc = target_h(m, ich, jch, 0.0, C))) break;
+      if (m->iitar > 1 && ich != jch) rc = update_hx_checked(m, ich, jch, g->fppqq, C);
+    }
   }
   free(v);
   free(w);
   (void)ns;
+  return rc;
+}
+
+/* L_data: DBSR_MAT3/L_data.f90:2-145.  Lval and Gen_Lvec (module dhl_core,
+ * not in the reference snapshot) are restated with the caller's one-electron
+ * matrices: Lval(i,j) = p_i^T hd(kappa_i) p_j and Gen_Lvec(i) = hd(kappa_i)
+ * p_i with p = (P; Q) of length ms.  Coefficients below eps_c are skipped. */
+static int kap_index(const orc_mat *m, int kappa) {
+  for (int k = 1; k <= m->nkap; k++)
+    if (m->kap_list[k - 1] == kappa) return k;
   return 0;
+}
+static const double *hd_of(const orc_mat *m, int orb) {
+  if (!m->hd || !m->kbs || orb < 1 || orb > m->nbf) return NULL;
+  int k = kap_index(m, m->kbs[orb - 1]);
+  if (!k) return NULL;
+  const int ms = m->g->ms;
+  return m->hd + (size_t)ms * ms * (k - 1);
+}
+static void gen_lvec(const orc_mat *m, const double *hd, int orb, double *v) {
+  const int ns = m->g->ns, ms = m->g->ms;
+  const double *p = PQ(orb, 1);  /* P then Q: the ms-vector (P; Q) */
+  for (int i = 1; i <= ms; i++) {
+    double s = 0.0;
+    for (int k = 1; k <= ms; k++) s = s + A2(hd, i, k, ms) * p[k - 1];
+    v[i - 1] = s;
+  }
+}
+static int l_data(orc_mat *m, int itype, int ncdata, const int *ipt, const int *k1,
+                  const int *k2, const int *k3, const int *k4, const double *cdata) {
+  const orc_grid *g = m->g;
+  const int ns = g->ns, ms = g->ms;
+  if (itype < 1 || itype > 3) return -2;
+  double *v = (double *)malloc(sizeof(double) * ms);
+  double *w = (double *)malloc(sizeof(double) * ms);
+  int rc = 0;
+  for (int j = 1; j <= ncdata && !rc; j++) {
+    int i = ipt[j - 1];
+    double C = cdata[i - 1];
+    if (fabs(C) < m->eps_c) continue;
+    if (itype == 1) {
+      int i1 = k1[i - 1], i2 = k2[i - 1];
+      const double *hd = hd_of(m, i1);
+      if (!hd || i2 < 1 || i2 > m->nbf) { rc = -4; break; }
+      gen_lvec(m, hd, i2, v);
+      const double *p = PQ(i1, 1);
+      double S = 0.0;
+      for (int k = 1; k <= ms; k++) S = S + p[k - 1] * v[k - 1];
+      C = C * S;
+      int ic = k3[i - 1], jc = k4[i - 1];
+      if (ic > 0 && jc > 0) {
+        rc = orc_update_hb(m, ic, jc, C);
+      } else if (ic < 0 && jc > 0) {
+        int io = -ic, o1 = io / ORC_IBO, o2 = io % ORC_IBO;
+        if (!kbort(m, o1, o2)) { rc = -4; break; }
+        orc_v_ch(g, PQ(o2, 1), v);
+        rc = orc_update_hv(m, m->ipbs[o1 - 1], jc, v, C);
+      } else if (ic < 0 && jc < 0) {
+        int io = -ic, o1 = io / ORC_IBO, o2 = io % ORC_IBO;
+        int jo = -jc, p1 = jo / ORC_IBO, p2 = jo % ORC_IBO;
+        if (!kbort(m, o1, o2) || !kbort(m, p1, p2)) { rc = -4; break; }
+        orc_v_ch(g, PQ(o2, 1), v);
+        orc_v_ch(g, PQ(p2, 1), w);
+        rc = update_hw_checked(m, m->ipbs[o1 - 1], m->ipbs[p1 - 1], v, w, C);
+      } else if (ic < 0 && jc == 0) {
+        int io = -ic, o1 = io / ORC_IBO, o2 = io % ORC_IBO;
+        if (o1 < 1 || o1 > m->nbf || o2 < 1 || o2 > m->nbf) { rc = -4; break; }
+        int ich = m->ipbs[o1 - 1], jch = m->ipbs[o2 - 1];
+        if (m->iitar > 0 && ich != jch && (rc = update_hx_checked(m, ich, jch, g->fppqq, C)))
+          break;
+        rc = target_h(m, ich, jch, C, 0.0);
+      } else {
+        rc = -1;
+      }
+    } else if (itype == 2) {
+      int i1 = k1[i - 1], ich = k2[i - 1], jc = k3[i - 1];
+      const double *hd = hd_of(m, i1);
+      if (!hd) { rc = -4; break; }
+      gen_lvec(m, hd, i1, v);
+      if (jc > 0) {
+        rc = orc_update_hv(m, ich, jc, v, C);
+      } else if (jc < 0) {
+        int jo = -jc, p1 = jo / ORC_IBO, p2 = jo % ORC_IBO;
+        if (!kbort(m, p1, p2)) { rc = -4; break; }
+        orc_v_ch(g, PQ(p2, 1), w);
+        rc = update_hw_checked(m, ich, m->ipbs[p1 - 1], v, w, C);
+      } else {
+        rc = -1;
+      }
+    } else {
+      int i1 = k1[i - 1], j1 = k2[i - 1];
+      if (i1 < 1 || i1 > m->nbf || j1 < 1 || j1 > m->nbf || !m->kbs) { rc = -4; break; }
+      int ich = m->ipbs[i1 - 1], jch = m->ipbs[j1 - 1];
+      if (m->kbs[i1 - 1] != m->kbs[j1 - 1]) { rc = -1; break; }
+      const double *hd = hd_of(m, i1);
+      if (!hd) { rc = -4; break; }
+      if (ich == jch || m->iitar > 1)
+        rc = update_hx_checked(m, ich, jch, hd, C);
+      else if (m->check_target == 1)
+        rc = target_h(m, ich, jch, 0.0, C);
+    }
+  }
+  free(v);
+  free(w);
+  (void)ns;
+  return rc;
 }
 
 /* Gen_matrix: DBSR_MAT3/gen_matrix.f90:2-17 */
 int orc_gen_matrix(orc_mat *m, int icase, int itype, int kpol, int ncdata,
                    const int *ipt, const int *k1, const int *k2,
                    const int *k3, const int *k4, const double *cdata) {
-  (void)k4;
   if (ncdata == 0) return 0;
   if (kpol < 0 || kpol > m->kmax_cache) return -3;
   switch (icase) {
     case 0:
       return o_data(m, itype, ncdata, ipt, k1, k2, cdata);
+    case 1:
+      return l_data(m, itype, ncdata, ipt, k1, k2, k3, k4, cdata);
     case 2:
       for (int bt = 0; bt <= 3; bt++) {
-        int rc = r_data(m, itype, kpol, bt, ncdata, ipt, k1, k2, k3, cdata);
+        int rc = r_data(m, itype, kpol, bt, ncdata, ipt, k1, k2, k3, k4, cdata);
         if (rc) return rc;
       }
       return 0;
     case 3:
-      return s_data(m, itype, kpol, ncdata, ipt, k1, k2, k3, cdata);
+      return s_data(m, itype, kpol, ncdata, ipt, k1, k2, k3, k4, cdata);
     default:
       return -1;
   }

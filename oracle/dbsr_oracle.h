@@ -107,6 +107,22 @@ typedef struct orc_mat {
   int kmax_cache;
   double **rcache;
   double **scache;
+  /* perturbers (Alloc_dbsr_matrix, updates.f90:47-72): hcp(ms,iicb) with
+     icb(nch,npert), hp(iibb) with ibb(npert,npert); npert = 0: none      */
+  int npert, iicb, iibb;
+  const int *icb, *ibb;
+  double *hcp, *hp;
+  /* targets (Target_h, target_subs.f90:2-31): iptar(nch), htarg/otarg of
+     ntarg(ntarg+1)/2; ntarg = 0: Target_h does nothing                   */
+  int ntarg, iitar, check_target;
+  const int *iptar;
+  double *htarg, *otarg;
+  /* one-electron Dirac matrices hd(ms,ms,nkap) of the kappas kap_list and
+     the kappa of every orbital kbs(nbf) (L_data)                         */
+  int nkap;
+  const int *kap_list, *kbs;
+  const double *hd;
+  double eps_c; /* mod_dbsr_mat.f90:50, 1e-10 */
 } orc_mat;
 
 orc_mat *orc_mat_new(const orc_grid *g, int nbf, const double *pq,
@@ -123,9 +139,25 @@ void orc_hf_matrix(const orc_grid *g, int nbf, const double *pq, int iorb, int k
                    double *hfm);
 void orc_update_hw(orc_mat *m, int ich, int jch, const double *v,
                    const double *w, double c);
+/* UPDATE_HV (updates.f90:220-242) and UPDATE_HB (:245-264); 0 or -4 */
+int orc_update_hv(orc_mat *m, int ich, int ip, const double *v, double c);
+int orc_update_hb(orc_mat *m, int ic, int jc, double c);
+void orc_mat_set_perturbers(orc_mat *m, int npert, const int *icb, int iicb,
+                            const int *ibb, int iibb, double *hcp, double *hp);
+void orc_mat_set_targets(orc_mat *m, int ntarg, const int *iptar, double *htarg,
+                         double *otarg, int iitar, int check_target);
+void orc_mat_set_dhl(orc_mat *m, int nkap, const int *kap_list, const double *hd,
+                     const int *kbs);
+void orc_mat_set_eps_c(orc_mat *m, double eps_c);
+/* BAV restatement (band matrix times vector; not in the reference
+ * snapshot): sym 's' a(ns,ks) symmetric upper band, 'n' a(ns,2ks-1) with
+ * A(i,i+jp-ks) = a(i,jp); dir 'r' v = A b, 'l' v = A^T b. */
+void orc_bav(int ns, int ks, const double *a, const double *b, double *v,
+             char sym, char dir);
 
-/* icase 0 O, 2 R, 3 S; lists in Add_matrix order (ipt 1-based). Returns 0
- * or a negative error code. */
+/* icase 0 O, 1 L, 2 R, 3 S; lists in Add_matrix order (ipt 1-based).
+ * Returns 0 or a negative error code (-4 an index out of range, -1 an
+ * unknown structure, -2 an unknown itype, -3 kpol out of range). */
 int orc_gen_matrix(orc_mat *m, int icase, int itype, int kpol, int ncdata,
                    const int *ipt, const int *k1, const int *k2,
                    const int *k3, const int *k4, const double *cdata);

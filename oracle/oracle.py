@@ -79,6 +79,16 @@ def lib():
         L.orc_gen_matrix.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int,
                                      _ip, _ip, _ip, _ip, _ip, _dp]
         L.orc_v_ch.argtypes = [C.POINTER(_Grid), _dp, _dp]
+        L.orc_mat_set_perturbers.argtypes = [C.c_void_p, C.c_int, _ip, C.c_int, _ip, C.c_int,
+                                             _dp, _dp]
+        L.orc_mat_set_targets.argtypes = [C.c_void_p, C.c_int, _ip, _dp, _dp, C.c_int, C.c_int]
+        L.orc_mat_set_dhl.argtypes = [C.c_void_p, C.c_int, _ip, _dp, _ip]
+        L.orc_mat_set_eps_c.argtypes = [C.c_void_p, C.c_double]
+        L.orc_bav.argtypes = [C.c_int, C.c_int, _dp, _dp, _dp, C.c_char, C.c_char]
+        L.orc_update_hv.restype = C.c_int
+        L.orc_update_hv.argtypes = [C.c_void_p, C.c_int, C.c_int, _dp, C.c_double]
+        L.orc_update_hb.restype = C.c_int
+        L.orc_update_hb.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double]
         L.orc_sort_merge.restype = C.c_int
         L.orc_sort_merge.argtypes = [C.c_int, _ip, _ip, _ip, _ip, _dp, _ip, _ip, _ip, _ip, _dp]
         _lib = L
@@ -232,6 +242,15 @@ def convol(ns, ks, rkb, d, icase: int, sym_i: str, sym_j: str) -> np.ndarray:
     return a
 
 
+def bav(ns, ks, a, b, sym: str, direction: str) -> np.ndarray:
+    """BAV restatement: band matrix a ('s' (ns,ks) or 'n' (ns,2ks-1)) times
+    vector b, v = A b ('r') or A^T b ('l')."""
+    a = f64(a)
+    v = np.zeros(ns)
+    lib().orc_bav(ns, ks, _d(a), _d(f64(b)), _d(v), sym.encode(), direction.encode())
+    return v
+
+
 def sort_merge(k1, k2, k3, k4, c):
     """Add_cdata list semantics: sorted unique keys with summed coefficients."""
     k1, k2, k3, k4, c = i32(k1), i32(k2), i32(k3), i32(k4), f64(c)
@@ -269,6 +288,36 @@ class Matrix:
                 self._m = None
         except Exception:
             pass
+
+    def set_perturbers(self, npert: int, icb, ibb):
+        """hcp(ms,iicb) and hp(iibb) with icb(nch,npert), ibb(npert,npert)."""
+        self.icb = np.asfortranarray(icb, dtype=np.int32)
+        self.ibb = np.asfortranarray(ibb, dtype=np.int32)
+        iicb, iibb = int(self.icb.max(initial=0)), int(self.ibb.max(initial=0))
+        self.hcp = np.zeros((self.grid.ms, max(iicb, 1)), order="F")
+        self.hp = np.zeros(max(iibb, 1))
+        lib().orc_mat_set_perturbers(self._m, npert, _i(self.icb), iicb, _i(self.ibb), iibb,
+                                     _d(self.hcp), _d(self.hp))
+
+    def set_targets(self, ntarg: int, iptar, iitar: int = 0, check_target: int = 1):
+        self.iptar = i32(iptar)
+        n = ntarg * (ntarg + 1) // 2
+        self.htarg = np.zeros(max(n, 1))
+        self.otarg = np.zeros(max(n, 1))
+        lib().orc_mat_set_targets(self._m, ntarg, _i(self.iptar), _d(self.htarg),
+                                  _d(self.otarg), iitar, check_target)
+
+    def set_dhl(self, kap_list, hd, kbs):
+        """hd(ms,ms,nkap) one-electron matrices of the kappas in kap_list;
+        kbs(nbf) the kappa of every orbital."""
+        self.kap_list = i32(kap_list)
+        self.hd = f64(hd)
+        self.kbs = i32(kbs)
+        lib().orc_mat_set_dhl(self._m, self.kap_list.size, _i(self.kap_list), _d(self.hd),
+                              _i(self.kbs))
+
+    def set_eps_c(self, eps_c: float):
+        lib().orc_mat_set_eps_c(self._m, float(eps_c))
 
     def dbs_orth(self, iort):
         """DBS_ORTH (dbs_orth.f90:28-84) on hch in place; iort(nbf, nch)."""

@@ -1,0 +1,179 @@
+"""GPU parity of the list structures that are not channel-pair contractions
+against the oracle, through the C ABI: R_data itypes 1/2, S_data ktypes 1-5
+and 11-15, L_data itypes 1-3, O_data itypes 1/2/4, every routing of their
+K3/K4 codes (UPDATE_HB, UPDATE_HV, UPDATE_HW, Target_h and UPDATE_HX of the
+target structures), with perturbers (hcp, hp), targets (htarg, otarg) and
+one-electron matrices.  These run in FP64 in every precision form, so the
+bar is 1e-12 of the largest element of each block, perturber column and
+target matrix.
+"""
+import numpy as np
+import pytest
+
+from dbsr_gb300 import FACTOR_FP64, PLAIN_FP64, SPLIT_BF16, Assembler, DbsrgError, synth
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-12
+
+
+def relmax(a, b):
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+
+
+@pytest.fixture(scope="module")
+def wl():
+    return synth.structures_case()
+
+
+def make_gpu(w, precision=PLAIN_FP64):
+    a = Assembler(w.t, w.ks, w.ksp, w.ksq)
+    a.set_orbitals(w.pq, w.ipbs)
+    a.alloc_matrix(w.nch, w.icc, w.iicc, w.mk)
+    a.alloc_perturbers(w.npert, w.icb, w.ibb)
+    a.set_targets(w.ntarg, w.iptar, w.iitar, 1)
+    a.set_dhl(w.kap_list, w.hd, w.kbs)
+    a.set_precision(precision)
+    return a
+
+
+def make_oracle(w):
+    g = O.Grid(w.t, w.ks, w.ksp, w.ksq)
+    m = O.Matrix(g, w.pq, w.ipbs, w.nch, w.icc, w.mk)
+    m.set_perturbers(w.npert, w.icb, w.ibb)
+    m.set_targets(w.ntarg, w.iptar, w.iitar, 1)
+    m.set_dhl(w.kap_list, w.hd, w.kbs)
+    return g, m
+
+
+def compare(a, m, w):
+    h = a.get_matrix()
+    for b in range(w.iicc):
+        r = m.hch[:, :, b]
+        if np.abs(r).max() == 0:
+            assert np.abs(h[:, :, b]).max() == 0, b
+        else:
+            assert relmax(h[:, :, b], r) <= TOL, b
+    hcp, hp = a.get_perturbers()
+    for col in range(m.hcp.shape[1]):
+        r = m.hcp[:, col]
+        if np.abs(r).max() == 0:
+            assert np.abs(hcp[:, col]).max() == 0, col
+        else:
+            assert relmax(hcp[:, col], r) <= TOL, col
+    assert np.abs(hp - m.hp).max() <= TOL * max(np.abs(m.hp).max(), 1e-300)
+    ht, ot = a.get_targets()
+    assert np.abs(ht - m.htarg).max() <= TOL * max(np.abs(m.htarg).max(), 1e-300)
+    assert np.abs(ot - m.otarg).max() <= TOL * max(np.abs(m.otarg).max(), 1e-300)
+
+
+def run_both(w, lists, precision=PLAIN_FP64):
+    a = make_gpu(w, precision)
+    g, m = make_oracle(w)
+    for L in lists:
+        a.gen_matrix(L.icase, L.itype, L.kpol, L.k1, L.k2, L.k3, L.k4, L.c)
+        m.gen_matrix(L.icase, L.itype, L.kpol, L.k1, L.k2, L.k3, L.k4, L.c)
+    return a, m
+
+
+def test_each_structure_list_against_oracle(wl):
+    seen = set()
+    for L in wl.lists:
+        a, m = run_both(wl, [L])
+        compare(a, m, wl)
+        a.close()
+        seen.add((L.icase, L.itype))
+    assert {(2, 1), (2, 2), (1, 1), (1, 2), (1, 3), (0, 1), (0, 2), (0, 4)} <= seen
+    assert {(3, t) for t in (1, 2, 3, 4, 5, 11, 12, 13, 14, 15)} <= seen
+
+
+@pytest.mark.parametrize("precision", [PLAIN_FP64, FACTOR_FP64, SPLIT_BF16])
+def test_every_list_kind_together_in_every_form(precision):
+    """The drop-in with the whole mix of Gen_matrix lists: the contraction
+    structures (O itype 3, R itypes 3/4, S 6-9) interleaved with all the
+    others, in each precision form."""
+    w = synth.structures_case(seed=91)
+    base = synth.small(ns=w.ns, nch=w.nch, mk=w.mk, n_entries=300, breit=True, seed=91,
+                       rmax=20.0, z=8.0, norb=w.nbound)
+    lists = []
+    for L in base.lists + w.lists:
+        lists.append(L)
+    lists.sort(key=lambda L: (L.icase, L.kpol, L.itype))  # State_res order per icase
+    a, m = run_both(w, lists, precision)
+    h = a.get_matrix()
+    tol = 1e-10 if precision == SPLIT_BF16 else TOL
+    for b in range(w.iicc):
+        r = m.hch[:, :, b]
+        assert relmax(h[:, :, b], r) <= tol, b
+    hcp, hp = a.get_perturbers()
+    assert relmax(hcp, m.hcp) <= TOL and relmax(hp, m.hp) <= TOL
+    ht, ot = a.get_targets()
+    assert relmax(ht, m.htarg) <= TOL and relmax(ot, m.otarg) <= TOL
+    a.close()
+
+
+def test_windowed_assembly_adds_perturber_terms_once(wl):
+    """Through dbsrg_assemble_to_host (lists once per window): the blocks
+    window by window, hcp/hp/htarg/otarg once."""
+    a = make_gpu(wl)
+    a.alloc_matrix(wl.nch, wl.icc, wl.iicc, wl.mk, window=2)
+    a.alloc_perturbers(wl.npert, wl.icb, wl.ibb)
+    a.set_targets(wl.ntarg, wl.iptar, wl.iitar, 1)
+    out = np.zeros((a.ms, a.ms, wl.iicc), order="F")
+    lists = [(L.icase, L.itype, L.kpol, L.k1, L.k2, L.k3, L.k4, L.c) for L in wl.lists]
+    a.assemble_to_host(lists, out=out, nwin=1)
+    g, m = make_oracle(wl)
+    for L in wl.lists:
+        m.gen_matrix(L.icase, L.itype, L.kpol, L.k1, L.k2, L.k3, L.k4, L.c)
+    for b in range(wl.iicc):
+        r = m.hch[:, :, b]
+        if np.abs(r).max() > 0:
+            assert relmax(out[:, :, b], r) <= TOL, b
+    hcp, hp = a.get_perturbers()
+    assert relmax(hcp, m.hcp) <= TOL and relmax(hp, m.hp) <= TOL
+    ht, ot = a.get_targets()
+    assert relmax(ht, m.htarg) <= TOL and relmax(ot, m.otarg) <= TOL
+    a.close()
+
+
+def test_single_term_updates_against_oracle(wl):
+    a = make_gpu(wl)
+    g, m = make_oracle(wl)
+    rng = np.random.default_rng(5)
+    ms = a.ms
+    for ich, jch in ((2, 1), (1, 2), (3, 3)):
+        v, w_ = rng.uniform(-1, 1, ms), rng.uniform(-1, 1, ms)
+        a.update_hw(ich, jch, v, w_, 0.7)
+        O.lib().orc_update_hw(m._m, ich, jch, O._d(v), O._d(w_), 0.7)
+    v = rng.uniform(-1, 1, ms)
+    a.update_hv(2, 3, v, -1.5)
+    assert O.lib().orc_update_hv(m._m, 2, 3, O._d(v), -1.5) == 0
+    a.update_hb(3, 1, 2.5)
+    assert O.lib().orc_update_hb(m._m, 3, 1, 2.5) == 0
+    compare(a, m, wl)
+    with pytest.raises(DbsrgError, match="ERANGE"):
+        a.update_hb(4, 1, 1.0)
+    a.close()
+
+
+def test_errors_leave_the_context_usable(wl):
+    L = next(L for L in wl.lists if (L.icase, L.itype) == (0, 1))
+    a = Assembler(wl.t, wl.ks, wl.ksp, wl.ksq)
+    a.set_orbitals(wl.pq, wl.ipbs)
+    a.alloc_matrix(wl.nch, wl.icc, wl.iicc, wl.mk)
+    with pytest.raises(DbsrgError, match="ERANGE"):  # no perturbers allocated
+        a.gen_matrix(L.icase, L.itype, L.kpol, L.k1, L.k2, L.k3, L.k4, L.c)
+    Ll = next(L for L in wl.lists if (L.icase, L.itype) == (1, 3))
+    with pytest.raises(DbsrgError, match="ESTATE"):  # no one-electron matrices
+        a.gen_matrix(Ll.icase, Ll.itype, Ll.kpol, Ll.k1, Ll.k2, Ll.k3, Ll.k4, Ll.c)
+    Lr = next(L for L in wl.lists if (L.icase, L.itype) == (2, 2))
+    k4 = Lr.k4.copy()
+    k4[:] = 0  # io = 0: unknown structure
+    a.alloc_perturbers(wl.npert, wl.icb, wl.ibb)
+    with pytest.raises(DbsrgError, match="EINVAL"):
+        a.gen_matrix(Lr.icase, Lr.itype, Lr.kpol, Lr.k1, Lr.k2, Lr.k3, k4, Lr.c)
+    assert np.abs(a.get_matrix()).max() == 0  # nothing of a failed list was added
+    a.gen_matrix(Lr.icase, Lr.itype, Lr.kpol, Lr.k1, Lr.k2, Lr.k3, Lr.k4, Lr.c)
+    assert np.abs(a.get_perturbers()[0]).max() > 0
+    a.close()
