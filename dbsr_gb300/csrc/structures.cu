@@ -888,10 +888,13 @@ int exec_structures(dbsrg_ctx *c, const StructPlan &P, int w, bool prep) {
                                    n, P.na, P.lcd, P.Ce));
   if (P.family >= 0 && P.npot > 0) {
     for (int a = 0; a < P.na; a++) {
-      dim3 gd((unsigned)((per + 255) / 256), (unsigned)P.npot);
-      DBSRG_RUN(c, "k_st_density",
-                k_st_density<<<gd, 256, 0, st>>>(ns, ks, P.sym, P.kb, P.npot, P.pots, P.dc1[a],
-                                                 P.dc2[a], c->pq, X));
+      for (int p0 = 0; p0 < P.npot; p0 += 65535) {  // grid y limit
+        const int np = std::min(65535, P.npot - p0);
+        dim3 gd((unsigned)((per + 255) / 256), (unsigned)np);
+        DBSRG_RUN(c, "k_st_density",
+                  k_st_density<<<gd, 256, 0, st>>>(ns, ks, P.sym, P.kb, np, P.pots + p0,
+                                                   P.dc1[a], P.dc2[a], c->pq, X + per * p0));
+      }
       // convol case icv of every pair density with the full table
       if ((rc = band_contract(c, P.kb, P.icv, tabs[a], P.npot, X, Y))) return rc;
       if (P.sum_amb)
@@ -899,20 +902,24 @@ int exec_structures(dbsrg_ctx *c, const StructPlan &P, int w, bool prep) {
                   k_st_sumamb<<<(n + 7) / 8, 256, 0, st>>>(ns, ks, P.sym, P.kb, n, P.epot, P.ej1,
                                                            P.ej2, P.ec1[a], P.ec2[a], c->pq, Y,
                                                            P.lcd, P.Ce + (size_t)a * n));
-      if (P.bav && P.npv > 0) {
-        dim3 gb((unsigned)((ns + 127) / 128), (unsigned)P.npv);
+      for (int q0 = 0; P.bav && q0 < P.npv; q0 += 65535) {
+        const int nq = std::min(65535, P.npv - q0);
+        dim3 gb((unsigned)((ns + 127) / 128), (unsigned)nq);
         DBSRG_RUN(c, "k_st_bav",
-                  k_st_bav<<<gb, 128, 0, st>>>(ns, ks, P.sym, P.dir, P.kb, P.npv, P.vjobs,
-                                               P.ipo[a], P.ipv[a], c->pq, Y,
-                                               pool + (size_t)ms * (nbf + (size_t)a * P.npv)));
+                  k_st_bav<<<gb, 128, 0, st>>>(
+                      ns, ks, P.sym, P.dir, P.kb, nq, P.vjobs + q0, P.ipo[a], P.ipv[a], c->pq, Y,
+                      pool + (size_t)ms * (nbf + (size_t)a * P.npv + q0)));
       }
     }
   }
   if (P.nlv > 0) {
     double *lpool = pool + (size_t)ms * (nbf + (size_t)P.na * P.npv);
-    dim3 gl((unsigned)((ms + 127) / 128), (unsigned)P.nlv);
-    DBSRG_RUN(c, "k_st_lvec",
-              k_st_lvec<<<gl, 128, 0, st>>>(ms, P.nlv, P.ljobs, c->hd, c->pq, lpool));
+    for (int l0 = 0; l0 < P.nlv; l0 += 65535) {
+      const int nl = std::min(65535, P.nlv - l0);
+      dim3 gl((unsigned)((ms + 127) / 128), (unsigned)nl);
+      DBSRG_RUN(c, "k_st_lvec", k_st_lvec<<<gl, 128, 0, st>>>(ms, nl, P.ljobs + l0, c->hd, c->pq,
+                                                              lpool + (size_t)ms * l0));
+    }
     if (P.lval)
       DBSRG_RUN(c, "k_st_lval", k_st_lval<<<(n + 7) / 8, 256, 0, st>>>(
                                     ms, n, P.ej1, P.elv, c->pq, lpool, P.lcd, P.Ce));
@@ -934,7 +941,7 @@ int exec_structures(dbsrg_ctx *c, const StructPlan &P, int w, bool prep) {
                                                     P.Ce, pool, c->hcp));
     }
   }
-  if (first && P.nsc > 0)
+  if (first && P.nsc > 0)  // one thread per scalar: a 1-D grid of ceil(nsc/128) blocks
     DBSRG_RUN(c, "k_st_scalar_terms",
               k_st_scalar_terms<<<(P.nsc + 127) / 128, 128, 0, st>>>(
                   P.nsc, P.scstart, P.scterms, P.Ce, c->hp, c->htarg, c->otarg));
