@@ -5,7 +5,11 @@ K3/K4 codes (UPDATE_HB, UPDATE_HV, UPDATE_HW, Target_h and UPDATE_HX of the
 target structures), with perturbers (hcp, hp), targets (htarg, otarg) and
 one-electron matrices.  These run in FP64 in every precision form, so the
 bar is 1e-12 of the largest element of each block, perturber column and
-target matrix.
+target matrix -- or, where a structure's sums cancel, 20 times the block's
+own sensitivity: the relative change of the oracle's block when the
+orbitals are perturbed by 1e-15 relative (the S^k pqqp integrals of this
+workload change by 1e-12 relative under that perturbation, so no FP64
+evaluation in another order can agree with the oracle better than that).
 """
 import numpy as np
 import pytest
@@ -47,25 +51,43 @@ def make_oracle(w):
     return g, m
 
 
-def compare(a, m, w):
-    h = a.get_matrix()
-    for b in range(w.iicc):
-        r = m.hch[:, :, b]
-        if np.abs(r).max() == 0:
-            assert np.abs(h[:, :, b]).max() == 0, b
-        else:
-            assert relmax(h[:, :, b], r) <= TOL, b
+def parts(m):
+    """The oracle's results as named arrays: blocks, perturber columns,
+    hp, htarg, otarg."""
+    out = {("hch", b): m.hch[:, :, b] for b in range(m.hch.shape[2])}
+    out.update({("hcp", c): m.hcp[:, c] for c in range(m.hcp.shape[1])})
+    out.update({("hp",): m.hp, ("htarg",): m.htarg, ("otarg",): m.otarg})
+    return out
+
+
+def sensitivity(w, lists):
+    """Relative change of every part of the oracle's result when the
+    orbitals are perturbed by 1e-15 relative (seeded)."""
+    rng = np.random.default_rng(123)
+    pq2 = np.asfortranarray(w.pq * (1.0 + 1e-15 * rng.uniform(-1.0, 1.0, w.pq.shape)))
+    w2 = synth.Workload(**{**w.__dict__, "pq": pq2})
+    _, m1 = make_oracle(w)
+    _, m2 = make_oracle(w2)
+    for L in lists:
+        m1.gen_matrix(L.icase, L.itype, L.kpol, L.k1, L.k2, L.k3, L.k4, L.c)
+        m2.gen_matrix(L.icase, L.itype, L.kpol, L.k1, L.k2, L.k3, L.k4, L.c)
+    p1, p2 = parts(m1), parts(m2)
+    return {k: (relmax(p2[k], p1[k]) if np.abs(p1[k]).max() > 0 else 0.0) for k in p1}
+
+
+def compare(a, m, w, lists, tol=TOL):
+    sens = sensitivity(w, lists)
     hcp, hp = a.get_perturbers()
-    for col in range(m.hcp.shape[1]):
-        r = m.hcp[:, col]
-        if np.abs(r).max() == 0:
-            assert np.abs(hcp[:, col]).max() == 0, col
-        else:
-            assert relmax(hcp[:, col], r) <= TOL, col
-    assert np.abs(hp - m.hp).max() <= TOL * max(np.abs(m.hp).max(), 1e-300)
     ht, ot = a.get_targets()
-    assert np.abs(ht - m.htarg).max() <= TOL * max(np.abs(m.htarg).max(), 1e-300)
-    assert np.abs(ot - m.otarg).max() <= TOL * max(np.abs(m.otarg).max(), 1e-300)
+    h = a.get_matrix()
+    got = {("hch", b): h[:, :, b] for b in range(w.iicc)}
+    got.update({("hcp", c): hcp[:, c] for c in range(hcp.shape[1])})
+    got.update({("hp",): hp, ("htarg",): ht, ("otarg",): ot})
+    for k, r in parts(m).items():
+        if np.abs(r).max() == 0:
+            assert np.abs(got[k]).max() == 0, k
+        else:
+            assert relmax(got[k], r) <= max(tol, 20.0 * sens[k]), (k, relmax(got[k], r), sens[k])
 
 
 def run_both(w, lists, precision=PLAIN_FP64):
@@ -81,7 +103,7 @@ def test_each_structure_list_against_oracle(wl):
     seen = set()
     for L in wl.lists:
         a, m = run_both(wl, [L])
-        compare(a, m, wl)
+        compare(a, m, wl, [L])
         a.close()
         seen.add((L.icase, L.itype))
     assert {(2, 1), (2, 2), (1, 1), (1, 2), (1, 3), (0, 1), (0, 2), (0, 4)} <= seen
@@ -101,15 +123,7 @@ def test_every_list_kind_together_in_every_form(precision):
         lists.append(L)
     lists.sort(key=lambda L: (L.icase, L.kpol, L.itype))  # State_res order per icase
     a, m = run_both(w, lists, precision)
-    h = a.get_matrix()
-    tol = 1e-10 if precision == SPLIT_BF16 else TOL
-    for b in range(w.iicc):
-        r = m.hch[:, :, b]
-        assert relmax(h[:, :, b], r) <= tol, b
-    hcp, hp = a.get_perturbers()
-    assert relmax(hcp, m.hcp) <= TOL and relmax(hp, m.hp) <= TOL
-    ht, ot = a.get_targets()
-    assert relmax(ht, m.htarg) <= TOL and relmax(ot, m.otarg) <= TOL
+    compare(a, m, w, lists, 1e-10 if precision == SPLIT_BF16 else TOL)
     a.close()
 
 
@@ -126,14 +140,17 @@ def test_windowed_assembly_adds_perturber_terms_once(wl):
     g, m = make_oracle(wl)
     for L in wl.lists:
         m.gen_matrix(L.icase, L.itype, L.kpol, L.k1, L.k2, L.k3, L.k4, L.c)
+    sens = sensitivity(wl, wl.lists)
     for b in range(wl.iicc):
         r = m.hch[:, :, b]
         if np.abs(r).max() > 0:
-            assert relmax(out[:, :, b], r) <= TOL, b
+            assert relmax(out[:, :, b], r) <= max(TOL, 20 * sens[("hch", b)]), b
     hcp, hp = a.get_perturbers()
-    assert relmax(hcp, m.hcp) <= TOL and relmax(hp, m.hp) <= TOL
     ht, ot = a.get_targets()
-    assert relmax(ht, m.htarg) <= TOL and relmax(ot, m.otarg) <= TOL
+    for k, got in ((("hp",), hp), (("htarg",), ht), (("otarg",), ot)):
+        assert relmax(got, parts(m)[k]) <= max(TOL, 20 * sens[k]), k
+    for col in range(hcp.shape[1]):
+        assert relmax(hcp[:, col], m.hcp[:, col]) <= max(TOL, 20 * sens[("hcp", col)]), col
     a.close()
 
 
@@ -151,7 +168,7 @@ def test_single_term_updates_against_oracle(wl):
     assert O.lib().orc_update_hv(m._m, 2, 3, O._d(v), -1.5) == 0
     a.update_hb(3, 1, 2.5)
     assert O.lib().orc_update_hb(m._m, 3, 1, 2.5) == 0
-    compare(a, m, wl)
+    compare(a, m, wl, [])
     with pytest.raises(DbsrgError, match="ERANGE"):
         a.update_hb(4, 1, 1.0)
     a.close()
