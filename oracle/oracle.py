@@ -85,6 +85,7 @@ def lib():
         L.orc_mat_set_dhl.argtypes = [C.c_void_p, C.c_int, _ip, _dp, _ip]
         L.orc_mat_set_eps_c.argtypes = [C.c_void_p, C.c_double]
         L.orc_bav.argtypes = [C.c_int, C.c_int, _dp, _dp, _dp, C.c_char, C.c_char]
+        L.orc_update_hw.argtypes = [C.c_void_p, C.c_int, C.c_int, _dp, _dp, C.c_double]
         L.orc_update_hv.restype = C.c_int
         L.orc_update_hv.argtypes = [C.c_void_p, C.c_int, C.c_int, _dp, C.c_double]
         L.orc_update_hb.restype = C.c_int

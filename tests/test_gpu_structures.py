@@ -194,3 +194,113 @@ def test_errors_leave_the_context_usable(wl):
     a.gen_matrix(Lr.icase, Lr.itype, Lr.kpol, Lr.k1, Lr.k2, Lr.k3, Lr.k4, Lr.c)
     assert np.abs(a.get_perturbers()[0]).max() > 0
     a.close()
+
+
+def _records(rng, w, icase, n, npert):
+    """Decoded coefficients (k, i1..i4, c, ic, jc, io, jo) of every structure
+    Idef_Otype / Idef_Ltype / Idef_Rtype / Idef_itype route (idef_type.f90),
+    with overlap codes io = (channel orbital, bound orbital) and target codes
+    (channel orbital, channel orbital) as Det_fact_new hands them over."""
+    nb, nch = w.nbound, w.nch
+    IBO = synth.IBO
+    b = lambda: int(rng.integers(1, nb + 1))  # noqa: E731
+    ch = lambda: nb + int(rng.integers(1, nch + 1))  # noqa: E731
+    ovl = lambda: ch() * IBO + b()  # noqa: E731
+    tgt = lambda: ch() * IBO + ch()  # noqa: E731
+    pert = lambda: sorted((int(x) for x in rng.integers(1, npert + 1, 2)), reverse=True)  # noqa
+    out = []
+    for _ in range(n):
+        k = int(rng.integers(0, w.mk + 1))
+        o = [b(), b(), b(), b()]
+        ic = jc = io = jo = 0
+        if icase in (2, 3):
+            kind = int(rng.integers(0, 7))
+            if kind == 0:  # channel-channel
+                a, bb = ((0, 2), (1, 3), (0, 3), (1, 2))[int(rng.integers(0, 4))]
+                o[a], o[bb] = ch(), ch()
+            elif kind == 1:
+                ic, jc = pert()
+            elif kind == 2:
+                o[int(rng.integers(0, 4))] = ch()
+                ic = pert()[0]
+            elif kind == 3:
+                o[int(rng.integers(0, 4))] = ch()
+                io = ovl()
+            elif kind == 4:
+                io, jo = ovl(), ovl()
+            elif kind == 5:
+                ic, io = pert()[0], ovl()
+            else:
+                io = tgt()
+        elif icase == 1:
+            kind = int(rng.integers(0, 6))
+            if kind == 0:
+                ic, jc = pert()
+            elif kind == 1:
+                ic, io = pert()[0], ovl()
+            elif kind == 2:
+                io, jo = ovl(), ovl()
+            elif kind == 3:
+                o[0] = ch()
+                io = ovl()
+            elif kind == 4:  # L(i j): two channel orbitals of one kappa
+                i = ch()
+                same = [q for q in range(w.nbound + 1, w.nbf + 1) if w.kbs[q - 1] == w.kbs[i - 1]]
+                o[0], o[2] = i, int(rng.choice(same))
+            else:
+                ic, io = 0, tgt()
+            if kind in (0, 1, 2, 5):  # L(. .): two bound orbitals of one kappa
+                same = [q for q in range(1, nb + 1) if w.kbs[q - 1] == w.kbs[o[0] - 1]]
+                o[2] = int(rng.choice(same))
+        else:
+            kind = int(rng.integers(0, 4))
+            if kind == 0:
+                ic, jc = pert()
+            elif kind == 1:
+                ic, io = pert()[0], ovl()
+            elif kind == 2:
+                io, jo = ovl(), ovl()
+            else:
+                io = tgt()
+        out.append((k, *o, float(rng.uniform(-1, 1)), ic, jc, io, jo))
+    return [np.array([r[q] for r in out], dtype=np.float64 if q == 5 else np.int64)
+            for q in range(10)]
+
+
+def test_produced_lists_of_every_structure_assemble_like_the_oracle():
+    """The whole hand-off of State_res (Add_integral, the Idef_* routing,
+    Add_cdata merging, Add_matrix -> Gen_matrix) for O, L, R and S
+    coefficients of every structure, through dbsrg_lists_* and
+    dbsrg_gen_matrix, against the oracle's lists assembled by the oracle."""
+    from dbsr_gb300.api import Lists
+    from oracle import lists as OL
+
+    w = synth.structures_case(seed=93, npert=4)
+    kap = np.asarray(w.kbs, dtype=np.int32)
+    lbs = np.array([synth.l_kappa(int(k)) for k in kap], dtype=np.int32)
+    ipbs = np.asarray(w.ipbs, dtype=np.int32)
+    rng = np.random.default_rng(44)
+    a = make_gpu(w)
+    g, m = make_oracle(w)
+    used = []
+    for icase in (0, 1, 2, 3):
+        recs = _records(rng, w, icase, 300, w.npert)
+        prod = Lists(icase, ipbs, lbs, kap, w.mk)
+        prod.add(*recs)
+        prod.gen_matrix(a)
+        prod.close()
+        ol = OL.Lists(icase, ipbs, lbs, kap, w.mk)
+        for e in range(len(recs[5])):
+            ol.add_integral(*[x[e].item() for x in recs])
+        for kp, it in ol.keys():
+            ref = ol.get(kp, it)
+            L = synth.CList(icase, it, kp, *[np.array([e[j] for e in ref], dtype=np.int32)
+                                             for j in range(4)],
+                            np.array([e[4] for e in ref]))
+            m.gen_matrix(L.icase, L.itype, L.kpol, L.k1, L.k2, L.k3, L.k4, L.c)
+            used.append(L)
+    kinds = {(L.icase, L.itype % 10) for L in used}
+    assert {(0, 1), (0, 2), (0, 3), (0, 4), (1, 1), (1, 2), (1, 3), (2, 1), (2, 2), (2, 3),
+            (2, 4), (3, 1), (3, 2), (3, 6), (3, 8)} <= kinds, kinds
+    compare(a, m, w, used)
+    a.close()
