@@ -223,6 +223,10 @@ class Assembler:
                                              C.c_void_p(hd.ctypes.data), C.c_void_p(kbs.ctypes.data)),
               "set_dhl")
 
+    def scale_matrix(self, s: float):
+        """hch, hcp and hp times s (SUB1's core-energy shifts, sub1.f90:96,222)."""
+        check(self._h, self._L.dbsrg_scale_matrix(self._h, float(s)), "scale_matrix")
+
     def set_eps_c(self, eps_c: float):
         check(self._h, self._L.dbsrg_set_eps_c(self._h, float(eps_c)), "set_eps_c")
 

@@ -304,6 +304,11 @@ __global__ void k_st_hv1(int ms, double C, const double *v, double *col) {
 __global__ void k_st_hb1(double C, double *dst) {
   if (threadIdx.x == 0 && blockIdx.x == 0) *dst = __dadd_rn(*dst, C);
 }
+__global__ void k_st_scale(size_t n, double s, double *x) {
+  for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < n;
+       q += (size_t)gridDim.x * blockDim.x)
+    x[q] = __dmul_rn(x[q], s);
+}
 
 }  // namespace
 
@@ -1155,6 +1160,26 @@ int dbsrg_update_hb(dbsrg_ctx *c, int ic, int jc, double cc) {
   const int i = c->h_ibb[(ic - 1) + (size_t)c->npert * (jc - 1)];
   if (i < 1 || i > c->iibb) return set_err(c, DBSRG_ERANGE, "UPDATE_HB: ic, jc out of range");
   DBSRG_RUN(c, "k_st_hb1", k_st_hb1<<<1, 32, 0, c->stream>>>(cc, c->hp + (i - 1)));
+  DBSRG_TRY(c, cudaStreamSynchronize(c->stream));
+  return DBSRG_OK;
+}
+
+int dbsrg_scale_matrix(dbsrg_ctx *c, double s) {
+  if (!c) return DBSRG_EINVAL;
+  if (!c->hch) return set_err(c, DBSRG_ESTATE, "no matrix allocated");
+  cudaSetDevice(c->device);
+  ST_SETTLE(c);
+  const size_t ms = c->g.ms;
+  struct {
+    double *p;
+    size_t n;
+  } parts[] = {{c->hch, ms * ms * (size_t)c->wcap}, {c->hcp, ms * (size_t)c->iicb},
+               {c->hp, (size_t)c->iibb}};
+  for (auto &q : parts) {
+    if (!q.p || q.n == 0) continue;
+    const unsigned nb = (unsigned)std::min<size_t>((q.n + 255) / 256, (size_t)c->nsm * 8);
+    DBSRG_RUN(c, "k_st_scale", k_st_scale<<<nb, 256, 0, c->stream>>>(q.n, s, q.p));
+  }
   DBSRG_TRY(c, cudaStreamSynchronize(c->stream));
   return DBSRG_OK;
 }

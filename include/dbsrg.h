@@ -233,6 +233,10 @@ int dbsrg_get_targets(dbsrg_ctx *ctx, double *htarg, double *otarg);
  * and itype 3 adds hd(kappa) itself. */
 int dbsrg_set_dhl(dbsrg_ctx *ctx, int nkap, const int *kap_list,
                   const double *hd, const int *kbs);
+/* hch (the current window), hcp and hp multiplied by s: the core-energy
+ * shifts of SUB1 between the overlap and the Hamiltonian passes
+ * (sub1.f90:96, 222-223, hch = hch * Ecore and the same for hcp, hp). */
+int dbsrg_scale_matrix(dbsrg_ctx *ctx, double s);
 /* eps_c of the O and L lists (mod_dbsr_mat.f90:50, default 1e-10):
  * coefficients below it are skipped (O_data.f90:35, L_data.f90:48). */
 int dbsrg_set_eps_c(dbsrg_ctx *ctx, double eps_c);

@@ -304,3 +304,24 @@ def test_produced_lists_of_every_structure_assemble_like_the_oracle():
             (2, 4), (3, 1), (3, 2), (3, 6), (3, 8)} <= kinds, kinds
     compare(a, m, w, used)
     a.close()
+
+
+def test_core_energy_shift_scales_hch_hcp_hp(wl):
+    """SUB1's shifts between the overlap and Hamiltonian passes
+    (sub1.f90:96, 222-223) on the device: hch, hcp, hp times Ecore, then more
+    lists on top."""
+    lists = [L for L in wl.lists if L.icase == 0] + [L for L in wl.lists if L.icase == 2][:2]
+    a = make_gpu(wl)
+    g, m = make_oracle(wl)
+    for L in lists[:3]:
+        a.gen_matrix(L.icase, L.itype, L.kpol, L.k1, L.k2, L.k3, L.k4, L.c)
+        m.gen_matrix(L.icase, L.itype, L.kpol, L.k1, L.k2, L.k3, L.k4, L.c)
+    a.scale_matrix(-1.75)
+    m.hch *= -1.75
+    m.hcp *= -1.75
+    m.hp *= -1.75
+    for L in lists[3:]:
+        a.gen_matrix(L.icase, L.itype, L.kpol, L.k1, L.k2, L.k3, L.k4, L.c)
+        m.gen_matrix(L.icase, L.itype, L.kpol, L.k1, L.k2, L.k3, L.k4, L.c)
+    compare(a, m, wl, lists)
+    a.close()
