@@ -941,6 +941,24 @@ def main():
     tot_ms = sum(v[1] for v in rep.values())
 
     peaks, peak_kind = measured_peaks()
+    # executed work of the kernels that state it (bytes and FLOPs, FP64 or
+    # float-float counted as FP64-equivalent multiply-adds x 2) over their
+    # measured time: what the factored step actually executes, beside the
+    # reference-loop count of the metric
+    kernel_work = {}
+    for name, (n_l, ms_l, by_l, fl_l) in sorted(rep.items(), key=lambda kv: -kv[1][1]):
+        if by_l <= 0 and fl_l <= 0:
+            continue
+        sec_l = ms_l / 1e3
+        kernel_work[name] = {"ms": round(ms_l, 3), "launches": n_l, "gflop": fl_l / 1e9,
+                             "gb": by_l / 1e9, "gflops": fl_l / sec_l / 1e9 if sec_l else None,
+                             "gbs": by_l / sec_l / 1e9 if sec_l else None}
+    executed = {"tflop_stated": sum(v["gflop"] for v in kernel_work.values()) / 1e3,
+                "gb_stated": sum(v["gb"] for v in kernel_work.values()),
+                "kernels_stated": sorted(kernel_work),
+                "note": ("the kernels above state their executed work (the rest, table "
+                         "construction and list bookkeeping, do not); k_xfused counts its "
+                         "tensor-core MMA FLOPs, the others FP64-equivalent multiply-adds")}
     if args.precision == "plain":
         p64 = fp64_peak_tflops(torch, dev)
         # algorithmic FLOPs of the contraction kernels (convol) over their time
@@ -1062,6 +1080,8 @@ def main():
             "clocks": clocks,
             "gpu_launches": int(launches),
             "kernel_ms": {k: round(v[1], 3) for k, v in sorted(rep.items(), key=lambda kv: -kv[1][1])},
+            "kernel_work": kernel_work,
+            "executed": executed,
             "peaks": {"source": peak_kind, "bf16_tflops": peaks.get("bf16_tflops"),
                       "hbm_gbs": peaks.get("hbm_gbs")},
         }

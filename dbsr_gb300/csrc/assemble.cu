@@ -580,6 +580,7 @@ namespace {
 //    there.
 struct Chunk {
   int moff, nm, nown, xoff, nxq;
+  long long nent;  // entries of the member segments (executed-work statements)
 };
 struct ListPlan {
   int icase = 0, itype = 0, kpol = 0, n = 0, nseg = 0;
@@ -600,6 +601,7 @@ struct ListPlan {
   int *bstart = nullptr, *tlist = nullptr, *order = nullptr;  // overlap list
   std::vector<Chunk> chunks;
   std::vector<int> wchunk, wown, wtl;  // per window: [w], [w+1] ranges
+  std::vector<double> wovl;            // overlap list: executed FLOPs per window
   int own_off = 0;                     // acf owners inside `work`
   std::vector<XQuad> hxq;
   // the structures that are not channel-pair contractions (structures.cu)
@@ -714,10 +716,13 @@ int plan_list(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const int *ip
       hstart[b + 1]++;
     }
     P.wtl.assign(nw + 1, 0);
+    P.wovl.assign(nw, 0.0);
     for (int b = 1; b <= iicc; b++) {
       if (hstart[b + 1] > 0) {
         hlist.push_back(b);
         P.wtl[wof(b) + 1]++;
+        // one multiply-add per element and entry (two on diagonal blocks)
+        P.wovl[wof(b)] += 2.0 * (double)ms * ms * hstart[b + 1];
       }
       hstart[b + 1] += hstart[b];
     }
@@ -855,7 +860,8 @@ int plan_list(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const int *ip
     std::vector<int> mem, own;  // member segment ids; owner slot positions
     auto close = [&]() {
       if (mem.empty()) return;
-      Chunk ch{(int)hbuf.size(), (int)mem.size(), (int)own.size(), (int)P.hxq.size(), 0};
+      Chunk ch{(int)hbuf.size(), (int)mem.size(), (int)own.size(), (int)P.hxq.size(), 0, 0};
+      for (int m : mem) ch.nent += hinfo[m].end - hinfo[m].start;
       hbuf.insert(hbuf.end(), mem.begin(), mem.end());
       hbuf.insert(hbuf.end(), own.begin(), own.end());
       if (P.split_x) {
@@ -911,12 +917,16 @@ int exec_list(dbsrg_ctx *c, const ListPlan &P, int w, bool prep = false) {
     DBSRG_RUN(c, "k_vch", k_vch<<<(2 * ns * c->nbf + 255) / 256, 256, 0, st>>>(
                               ns, c->nbf, g.fpbs, g.fqbs, c->pq, P.vch));
     for (int t = 0; t < nt; t += 65535) {  // grid z limit
-      dim3 grid((unsigned)((ms + 127) / 128), (unsigned)((ms + 31) / 32),
-                (unsigned)std::min(65535, nt - t));
-      DBSRG_RUN(c, "k_overlap_update",
-                k_overlap_update<<<grid, 128, 0, st>>>(ns, P.tlist + t0 + t, P.bstart, P.order,
-                                                       P.lk1, P.lk2, P.lcd, c->ipbs, P.vch,
-                                                       hch_base(c)));
+      const int nz = std::min(65535, nt - t);
+      dim3 grid((unsigned)((ms + 127) / 128), (unsigned)((ms + 31) / 32), (unsigned)nz);
+      // executed work: the window's multiply-adds, one read-modify-write of
+      // every touched block (16 bytes an element)
+      const double ob = 16.0 * (double)ms * ms * nz;
+      const double of = t == 0 ? P.wovl[w] : 0.0;
+      DBSRG_RUN_W(c, "k_overlap_update", ob, of,
+                  k_overlap_update<<<grid, 128, 0, st>>>(ns, P.tlist + t0 + t, P.bstart, P.order,
+                                                         P.lk1, P.lk2, P.lcd, c->ipbs, P.vch,
+                                                         hch_base(c)));
     }
     return DBSRG_OK;
   }
@@ -984,6 +994,7 @@ int exec_list(dbsrg_ctx *c, const ListPlan &P, int w, bool prep = false) {
       job.xq = ch.nxq ? P.dxq + ch.xoff : nullptr;
       job.hxq = ch.nxq ? P.hxq.data() + ch.xoff : nullptr;
       job.nxq = ch.nxq;
+      job.nent = ch.nent;
       job.prep = prep;
       return factored_contract(c, job);
     }

@@ -931,9 +931,17 @@ int split_exchange(dbsrg_ctx *c, const SplitExchange &x) {
   z.Yb = Yb;
   const size_t zsm = (size_t)(x.lower ? 2 : 1) * nb * ZROWS * sizeof(float2);
   if ((rc = raise_smem_limit(c, (const void *)k_zdigits, zsm))) return rc;
-  DBSRG_RUN(c, "k_zdigits",
-            k_zdigits<<<dim3((unsigned)(NR * 32 / ZROWS), (unsigned)x.nm, (unsigned)x.na), ZROWS,
-                        zsm, st>>>(z));  // every row of the operand, zeros past ns
+  // executed work: per PQ type, row and entry one multiply-add per field
+  // (Z, and Zl for R^k) and per band diagonal (17), float-float; the entry's
+  // band potential values (17 float-float pairs a row) read, the digits and
+  // band rows written
+  const double zf = 2.0 * x.na * ns * (1.0 + x.lower + NDB) * (double)x.nent;
+  const double zb = 8.0 * x.na * ns * ((1.0 + x.lower + NDB) * (double)x.nent +
+                                       NDB * (double)x.nm) +
+                    2.0 * TS * (double)x.na * (1 + x.lower) * x.nm * NR * TILE;
+  DBSRG_RUN_W(c, "k_zdigits", zb, zf,
+              k_zdigits<<<dim3((unsigned)(NR * 32 / ZROWS), (unsigned)x.nm, (unsigned)x.na),
+                          ZROWS, zsm, st>>>(z));  // every row of the operand, zeros past ns
   XArgs p{};
   p.ns = ns;
   p.NR = NR;

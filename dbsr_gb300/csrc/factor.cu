@@ -981,24 +981,33 @@ int get_pairpot_direct_any(dbsrg_ctx *c, int family, int type, int k, int icv, i
   const double *lo1 = icv == 1 ? cd->lo1 : nullptr;
   const double *hi1 = (icv == 1 && family == 0) ? cd->hi1 : nullptr;
   dim3 gf((unsigned)((per + 127) / 128), (unsigned)npair);
+  // executed work of the diagonal cells: per cell, stage 1 npo k1 k2 nb and
+  // stage 2 npo nb k1 nb multiply-adds; the cell's table slice read and its
+  // npo nb^2 outputs written.  The final potentials: per output element and
+  // pair a few separable terms (about 4 multiply-adds) and the nine
+  // diagonal-cell phases read, the potential written.
+  const double dflops = 2.0 * nv * npo * ed.k1 * ((double)ed.k2 * nb + (double)nb * nb);
+  const double dbytes = 8.0 * nv * ((double)npo * ed.k1 * ed.k2 + (double)npo * nb * nb);
+  const double fflops = 8.0 * (double)per * npair;
+  const double fbytes = 8.0 * (double)per * npair * (FAR + 1);
   if (ff) {
     if ((rc = set_smem(c, (const void *)k_pair_diag<true>, sm3))) return rc;
-    DBSRG_RUN(c, "k_pair_diag",
-              k_pair_diag<true><<<nv, 256, sm3, st>>>(
-                  ns, ks, kk, nb, icv, sym, eo, ed, cd->rkd, P1, P2, Dq, per));
-    DBSRG_RUN(c, "k_pair_direct_final",
-              k_pair_direct_final<true><<<gf, 128, 0, st>>>(ns, ks, nv, kk, nb, icv, sym, eo, lo1,
-                                                            hi1, cd->hi2, SA, M2 ? SB : nullptr,
-                                                            Dq, K, per));
+    DBSRG_RUN_W(c, "k_pair_diag", dbytes, dflops,
+                k_pair_diag<true><<<nv, 256, sm3, st>>>(
+                    ns, ks, kk, nb, icv, sym, eo, ed, cd->rkd, P1, P2, Dq, per));
+    DBSRG_RUN_W(c, "k_pair_direct_final", fbytes, fflops,
+                k_pair_direct_final<true><<<gf, 128, 0, st>>>(ns, ks, nv, kk, nb, icv, sym, eo,
+                                                              lo1, hi1, cd->hi2, SA,
+                                                              M2 ? SB : nullptr, Dq, K, per));
   } else {
     if ((rc = set_smem(c, (const void *)k_pair_diag<false>, sm3))) return rc;
-    DBSRG_RUN(c, "k_pair_diag",
-              k_pair_diag<false><<<nv, 256, sm3, st>>>(
-                  ns, ks, kk, nb, icv, sym, eo, ed, cd->rkd, P1, P2, Dq, per));
-    DBSRG_RUN(c, "k_pair_direct_final",
-              k_pair_direct_final<false><<<gf, 128, 0, st>>>(ns, ks, nv, kk, nb, icv, sym, eo,
-                                                             lo1, hi1, cd->hi2, SA,
-                                                             M2 ? SB : nullptr, Dq, K, per));
+    DBSRG_RUN_W(c, "k_pair_diag", dbytes, dflops,
+                k_pair_diag<false><<<nv, 256, sm3, st>>>(
+                    ns, ks, kk, nb, icv, sym, eo, ed, cd->rkd, P1, P2, Dq, per));
+    DBSRG_RUN_W(c, "k_pair_direct_final", fbytes, fflops,
+                k_pair_direct_final<false><<<gf, 128, 0, st>>>(ns, ks, nv, kk, nb, icv, sym, eo,
+                                                               lo1, hi1, cd->hi2, SA,
+                                                               M2 ? SB : nullptr, Dq, K, per));
   }
   *out = K;
   return DBSRG_OK;
@@ -1036,14 +1045,22 @@ static int get_pairpot_band(dbsrg_ctx *c, int family, int type, int k, int cs, i
       ((size_t)PXC * W * W + 2 * (size_t)nb * WLP + (size_t)PXC * (W * nb + 1)) * sizeof(double);
   const int mode = family == 0 ? 0 : (cs == 3 ? 1 : 2);
   dim3 gb((unsigned)((ns + PXC - 1) / PXC), (unsigned)NDB);
+  // executed work: per output row and band diagonal W^2 nb (stage 1) and
+  // W nb^2 (stage 2) multiply-adds; the band table read, the potentials
+  // written
+  const double kb = family == 0 ? ks : W;
+  const double bflops = 2.0 * ns * NDB * ((double)W * W * nb + (double)W * nb * nb);
+  const double bbytes = 8.0 * ns * NDB * (kb * kb + (double)npair);
   if (ff) {
     if ((rc = set_smem(c, (const void *)k_pair_band<true>, smem))) return rc;
-    DBSRG_RUN(c, "k_pair_band",
-              k_pair_band<true><<<gb, 256, smem, c->stream>>>(ns, ks, nb, mode, tab, P1, P2, K));
+    DBSRG_RUN_W(c, "k_pair_band", bbytes, bflops,
+                k_pair_band<true><<<gb, 256, smem, c->stream>>>(ns, ks, nb, mode, tab, P1, P2,
+                                                                K));
   } else {
     if ((rc = set_smem(c, (const void *)k_pair_band<false>, smem))) return rc;
-    DBSRG_RUN(c, "k_pair_band",
-              k_pair_band<false><<<gb, 256, smem, c->stream>>>(ns, ks, nb, mode, tab, P1, P2, K));
+    DBSRG_RUN_W(c, "k_pair_band", bbytes, bflops,
+                k_pair_band<false><<<gb, 256, smem, c->stream>>>(ns, ks, nb, mode, tab, P1, P2,
+                                                                 K));
   }
   *out = K;
   return DBSRG_OK;
@@ -1130,6 +1147,7 @@ int factored_contract(dbsrg_ctx *c, const FactorJob &j) {
     x.cd = j.cd;
     x.cdf = j.cdf;
     x.prep = j.prep;
+    x.nent = j.nent;
     return split_exchange(c, x);
   }
   if (j.icv >= 3 && j.prep) {
@@ -1194,13 +1212,21 @@ int factored_contract(dbsrg_ctx *c, const FactorJob &j) {
   if (j.prep) return DBSRG_OK;
   const size_t space = (size_t)4 * ns * (2 * ks - 1);
   dim3 gs((unsigned)((space + 127) / 128), (unsigned)j.nown);
+  // executed work: per PQ type every band element of its quadrant (about
+  // ns (2ks-1)) sums one pair-potential value per entry of the owner and
+  // partner segments (one multiply-add, float-float in the split form), and
+  // is read and written once in hch; the potentials are read per entry
+  const double nd = 2.0 * ks - 1.0, band = ns * nd;
+  const double wflops = 2.0 * j.na * band * (double)j.nent;
+  const double wbytes = 16.0 * j.na * band * j.nown + 8.0 * j.na * band * (double)j.nent;
   if (j.split && j.cdf)
-    DBSRG_RUN(c, "k_scatter_dp",
-              k_scatter_dp<true><<<gs, 128, 0, st>>>(ns, ks, j.sym, qs, kd, j.members, j.own,
-                                                     j.info, j.pairs, j.cd, j.cdf, hch_base(c)));
+    DBSRG_RUN_W(c, "k_scatter_dp", wbytes, wflops,
+                k_scatter_dp<true><<<gs, 128, 0, st>>>(ns, ks, j.sym, qs, kd, j.members, j.own,
+                                                       j.info, j.pairs, j.cd, j.cdf, hch_base(c)));
   else
-    DBSRG_RUN(c, "k_scatter_dp",
-              k_scatter_dp<false><<<gs, 128, 0, st>>>(ns, ks, j.sym, qs, kd, j.members, j.own,
-                                                      j.info, j.pairs, j.cd, j.cdf, hch_base(c)));
+    DBSRG_RUN_W(c, "k_scatter_dp", wbytes, wflops,
+                k_scatter_dp<false><<<gs, 128, 0, st>>>(ns, ks, j.sym, qs, kd, j.members, j.own,
+                                                        j.info, j.pairs, j.cd, j.cdf,
+                                                        hch_base(c)));
   return DBSRG_OK;
 }

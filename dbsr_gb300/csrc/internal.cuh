@@ -389,6 +389,7 @@ struct FactorJob {
   const struct XQuad *xq;
   const struct XQuad *hxq;  // host copy of the records (work accounting)
   bool prep;         // build (or find) the cached inputs only, launch no contraction
+  long long nent;    // entries of the member segments (executed-work statements)
 };
 int factored_contract(dbsrg_ctx *c, const FactorJob &job);
 // One quadrant of one owner's block in the split exchange and the terms it
@@ -419,6 +420,7 @@ struct SplitExchange {
   const double *cd;
   const float2 *cdf;  // the coefficients as float-float pairs
   bool prep;          // build the digit and float-float caches only
+  long long nent;     // entries of the member segments (executed-work statements)
 };
 int split_exchange(dbsrg_ctx *c, const SplitExchange &x);
 // Direct pair potentials of table (family, type, k) for convol case icv with

@@ -64,6 +64,48 @@ def test_backward_finite_differences_config4():
     assert worst <= 1e-7 * np.abs(G).max(), worst / np.abs(G).max()
 
 
+def test_backward_finite_differences_config4_wide():
+    """Central differences on 220 gradient entries of the config-4 size
+    (300 splines, 30 orbitals, Z = 18, k = 0..8, 5e4 entries): the 80
+    largest P and the 60 largest Q components, 40 of middle magnitude and
+    40 random ones.  Every entry within 1e-7 of max|G|; entries with
+    |G| >= 1e-3 max|G| also within 1e-6 of their own value."""
+    w = synth.config4()
+    a = assembler(w)
+    E, G = a.backward(w.k, w.i1, w.i2, w.i3, w.i4, w.coef)
+    gmax = np.abs(G).max()
+    rng = np.random.default_rng(11)
+    ns, _, nb = G.shape
+    order = np.argsort(-np.abs(G).ravel(order="F"))
+    comp = np.unravel_index(order, G.shape, order="F")[1]
+    pick = order[comp == 0][:80].tolist() + order[comp == 1][:60].tolist()
+    mid = order[(np.abs(G).ravel(order="F")[order] < 1e-2 * gmax) &
+                (np.abs(G).ravel(order="F")[order] > 1e-5 * gmax)]
+    pick += rng.choice(mid, min(40, mid.size), replace=False).tolist()
+    pick += rng.integers(0, G.size, 40).tolist()
+    assert len(pick) >= 200
+    scale = np.abs(w.pq).max()
+    h = 1e-6 * scale
+    worst_abs, worst_rel, nq = 0.0, 0.0, 0
+    for f in pick:
+        idx = np.unravel_index(f, G.shape, order="F")
+        nq += idx[1] == 1
+        vals = []
+        for sgn in (+1, -1):
+            p = w.pq.copy(order="F")
+            p[idx] += sgn * h
+            a.set_orbitals(p, w.ipbs)
+            vals.append(a.backward(w.k, w.i1, w.i2, w.i3, w.i4, w.coef, grad=False)[0])
+        fd = (vals[0] - vals[1]) / (2 * h)
+        worst_abs = max(worst_abs, abs(fd - G[idx]) / gmax)
+        if abs(G[idx]) >= 1e-3 * gmax:
+            worst_rel = max(worst_rel, abs(fd - G[idx]) / abs(G[idx]))
+    a.close()
+    assert nq >= 60
+    assert worst_abs <= 1e-7, worst_abs
+    assert worst_rel <= 1e-6, worst_rel
+
+
 def test_autograd_function():
     torch = pytest.importorskip("torch")
     from dbsr_gb300.autograd import RkEnergy
