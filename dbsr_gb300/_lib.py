@@ -91,6 +91,7 @@ SIGNATURES = [
     ("dbsrg_update_hv", C.c_int, [_vp, C.c_int, C.c_int, _vp, C.c_double]),
     ("dbsrg_update_hb", C.c_int, [_vp, C.c_int, C.c_int, C.c_double]),
     ("dbsrg_scale_matrix", C.c_int, [_vp, C.c_double]),
+    ("dbsrg_hf_breit_list", C.c_int, [_vp, C.c_int, _vp, _vp, _vp, _vp, _vp]),
     ("dbsrg_exchange_segment_noalloc", C.c_int,
      [C.c_int, C.c_int, _vp, _vp, C.c_int, C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, _vp, _vp]),
 ]

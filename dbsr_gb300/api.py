@@ -386,6 +386,15 @@ class Assembler:
         pi, k = _ptr(io, np.int32)
         check(self._h, self._L.dbsrg_orth_channels(self._h, pi), "orth_channels")
 
+    def hf_breit_list(self, kr1, kr2, kr3, kr4, crk):
+        """rk4 entries of the Breit energy for the Breit part of hf_matrix
+        (hf_matrix_breit, DBSR_HF/hf_matrix.f90:91-163)."""
+        arrs = [np.ascontiguousarray(x, dtype=np.int32) for x in (kr1, kr2, kr3, kr4)]
+        c = np.ascontiguousarray(crk, dtype=np.float64)
+        check(self._h, self._L.dbsrg_hf_breit_list(self._h, int(c.size),
+                                                   *[C.c_void_p(x.ctypes.data) for x in arrs],
+                                                   C.c_void_p(c.ctypes.data)), "hf_breit_list")
+
     def hf_matrix(self, iorb: int, a, b, qsum: float, dhl=None, out=None):
         """dbsrg_hf_matrix (hf_matrix.f90:2-70, Coulomb part): the potential
         matrix (ms, ms) of orbital iorb (1-based); a, b: (nbf, kmax+1) values

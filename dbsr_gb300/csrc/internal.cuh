@@ -214,6 +214,10 @@ struct dbsrg_ctx {
   std::vector<int> h_kap, h_kbs;
   double *hd = nullptr;
   double eps_c = 1.0e-10;
+  // rk4 entries of DBSR_HF's Breit energy (dbsrg_hf_breit_list), read by
+  // dbsrg_hf_matrix for its Breit part (hf_matrix_breit)
+  std::vector<int> hf_kr1, hf_kr2, hf_kr3, hf_kr4;
+  std::vector<double> hf_crk;
 };
 
 cudaEvent_t event_get(dbsrg_ctx *c);

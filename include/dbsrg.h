@@ -303,8 +303,8 @@ int dbsrg_channel_basis(dbsrg_ctx *ctx, const double *sol, const int *nsol,
 int dbsrg_orth_channels(dbsrg_ctx *ctx, const int *iort);
 
 /* SCF potential matrix of one orbital: DBSR_HF's
- * hf_matrix (hf_matrix.f90:2-70, Coulomb part; the Breit part of
- * hf_matrix_breit is not included)
+ * hf_matrix (hf_matrix.f90:2-70; the Breit part of hf_matrix_breit when
+ * dbsrg_hf_breit_list holds entries)
  *   hfm = (qsum dhl + sum_{ii,jj,k} [direct + exchange]) / qsum
  * for orbital iorb (1-based) of dbsrg_set_orbitals, with a(nbf,0:kmax) and
  * b(nbf,0:kmax) (host, Fortran order) the values of the energy
@@ -319,6 +319,20 @@ int dbsrg_orth_channels(dbsrg_ctx *ctx, const int *iort);
 int dbsrg_hf_matrix(dbsrg_ctx *ctx, int iorb, int kmax, const double *a,
                     const double *b, double qsum, const double *dhl,
                     double *hfm);
+/* The Breit part of dbsrg_hf_matrix (hf_matrix_breit, hf_matrix.f90:91-163,
+ * DBSR_HF's mbreit = 2): the rk4 entries of the Breit energy (module
+ * rk4_data, dbsr_lib_zcom.f90:2984-3003) -- kr1 = k + 1000*itype (itype 0
+ * S^k ppqq, 1 pqqp), kr2 = int 1..4, kr3, kr4 orbitals (1-based), crk the
+ * coefficient; host arrays, copied.  Every later dbsrg_hf_matrix adds, per
+ * itype, k <= kmax and int, convol_sk case int of the coefficient-weighted
+ * densities of the orbital's partners into its quadrant, before the
+ * division by qsum.  As in the reference, the exchange forms int 3 and 4
+ * add nothing: hf_matrix_breit hands convol_sk the storage 'x','x', which
+ * convol_sk does not contract (dbsr_lib_dbs.f90:2610-2700).  nrk = 0
+ * removes the Breit part. */
+int dbsrg_hf_breit_list(dbsrg_ctx *ctx, int nrk, const int *kr1,
+                        const int *kr2, const int *kr3, const int *kr4,
+                        const double *crk);
 
 /* List producer between the decoded angular bank and Gen_matrix (the part
  * after the bank's records are read; the records, state tables and overlap

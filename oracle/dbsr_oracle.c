@@ -1288,6 +1288,11 @@ static void hf_update(int ns, int ks, int ms, double *hm, int ii, int jj, const 
         A2(y, i, j, ns) = A2(d, i, jp, ns);
         A2(y, j, i, ns) = A2(d, i, jp, ns);
       }
+  } else if (sym == 'n') {
+    for (int jp = 1; jp <= ks + ks - 1; jp++) {
+      const int i0 = imax(1, 1 + ks - jp), i1 = imin(ns, ns + ks - jp);
+      for (int i = i0; i <= i1; i++) A2(y, i, i + jp - ks, ns) = A2(d, i, jp, ns);
+    }
   } else {
     memcpy(y, d, sizeof(double) * (size_t)ns * ns);
   }
@@ -2033,4 +2038,69 @@ int orc_sort_merge(int n, const int *k1, const int *k2, const int *k3,
   free(a);
   free(tmp);
   return u + 1;
+}
+
+
+/* hf_matrix_breit: DBSR_HF/hf_matrix.f90:91-163, the Breit part of the
+ * potential matrix of orbital iorb, added into hfm (hf_matrix adds it
+ * before the division by qsum, :64-66).  For itype 0 (S^k ppqq) and 1
+ * (pqqp), k = 0..kmax and int = 1..4 (storage 'n','n','x','x'):
+ *   xx = sum over the rk4 entries ik with kr1 = k + 1000 itype and
+ *        i = kr3 (jnt = kr2, j = kr4) or i = kr4 (jnt = kint(kr2), j = kr3,
+ *        kint = 2,1,4,3), jnt = int, of crk(ik) density(p(jp1,j), p(jp2,j))
+ *   convol_sk case int of xx with the S^k table, into quadrant (ip1,ip2)
+ *   through the HF library's Update_hs (half and half transposed),
+ * with ip1,ip2,jp1,jp2 of :123-138. */
+void orc_hf_matrix_breit(const orc_grid *g, int nbf, const double *pq, int iorb, int kmax,
+                         int nrk, const int *kr1, const int *kr2, const int *kr3,
+                         const int *kr4, const double *crk, double *hfm) {
+  const int ns = g->ns, ks = g->ks, ms = g->ms, kb = 2 * ks - 1;
+  static const char sym_int[4] = {'n', 'n', 'x', 'x'};
+  static const int kint[4] = {2, 1, 4, 3};
+  static const int ipt[2][4][4] = {
+      {{1, 2, 1, 2}, {1, 2, 1, 2}, {1, 2, 2, 1}, {2, 1, 1, 2}},
+      {{1, 2, 2, 1}, {2, 1, 1, 2}, {1, 1, 2, 2}, {2, 2, 1, 1}}};
+  double *rkb = (double *)malloc(sizeof(double) * (size_t)ns * ns * kb * kb);
+  double *x = (double *)calloc((size_t)ns * ns, sizeof(double));
+  double *xx = (double *)calloc((size_t)ns * ns, sizeof(double));
+  (void)nbf;
+  for (int itype = 0; itype <= 1; itype++)
+    for (int k = 0; k <= kmax; k++) {
+      const int kk = k + 1000 * itype;
+      orc_msk(g, itype, k, rkb);
+      for (int in = 1; in <= 4; in++) {
+        const char sym = sym_int[in - 1];
+        const int ip1 = ipt[itype][in - 1][0], ip2 = ipt[itype][in - 1][1];
+        const int jp1 = ipt[itype][in - 1][2], jp2 = ipt[itype][in - 1][3];
+        memset(xx, 0, sizeof(double) * (size_t)ns * ns);
+        int met = 0;
+        for (int ik = 0; ik < nrk; ik++) {
+          if (kk != kr1[ik]) continue;
+          int jnt, j;
+          if (iorb == kr3[ik]) {
+            jnt = kr2[ik];
+            j = kr4[ik];
+          } else if (iorb == kr4[ik]) {
+            jnt = kint[kr2[ik] - 1];
+            j = kr3[ik];
+          } else {
+            continue;
+          }
+          if (jnt != in) continue;
+          const double *p1 = pq + (size_t)2 * ns * (j - 1) + (size_t)ns * (jp1 - 1);
+          const double *p2 = pq + (size_t)2 * ns * (j - 1) + (size_t)ns * (jp2 - 1);
+          orc_density(ns, ks, x, p1, p2, sym);
+          const size_t nn = (size_t)ns * (sym == 'n' ? kb : ns);
+          for (size_t q = 0; q < nn; q++) xx[q] = xx[q] + crk[ik] * x[q];
+          met++;
+        }
+        if (met > 0) {
+          orc_convol(ns, ks, kb, rkb, x, xx, in, sym, sym);
+          hf_update(ns, ks, ms, hfm, ip1, ip2, x, sym);
+        }
+      }
+    }
+  free(rkb);
+  free(x);
+  free(xx);
 }

@@ -137,6 +137,13 @@ void orc_dbs_orth(orc_mat *m, const int *iort);
 void orc_hf_matrix(const orc_grid *g, int nbf, const double *pq, int iorb, int kmax,
                    const double *a, const double *b, double qsum, const double *dhl,
                    double *hfm);
+/* hf_matrix_breit (DBSR_HF/hf_matrix.f90:91-163): the Breit part of the
+ * potential matrix of orbital iorb from the rk4 entries (kr1 = k + 1000
+ * itype, kr2 = int 1..4, kr3, kr4 orbitals, crk coefficients), added into
+ * hfm (ms x ms) before any division by qsum */
+void orc_hf_matrix_breit(const orc_grid *g, int nbf, const double *pq, int iorb, int kmax,
+                         int nrk, const int *kr1, const int *kr2, const int *kr3,
+                         const int *kr4, const double *crk, double *hfm);
 void orc_update_hw(orc_mat *m, int ich, int jch, const double *v,
                    const double *w, double c);
 /* UPDATE_HV (updates.f90:220-242) and UPDATE_HB (:245-264); 0 or -4 */

@@ -61,6 +61,8 @@ def lib():
         L.orc_dbs_orth.argtypes = [C.c_void_p, _ip]
         L.orc_hf_matrix.argtypes = [C.POINTER(_Grid), C.c_int, _dp, C.c_int, C.c_int, _dp, _dp,
                                     C.c_double, _dp, _dp]
+        L.orc_hf_matrix_breit.argtypes = [C.POINTER(_Grid), C.c_int, _dp, C.c_int, C.c_int,
+                                          C.c_int, _ip, _ip, _ip, _ip, _dp, _dp]
         L.orc_convol.argtypes = [C.c_int, C.c_int, C.c_int, _dp, _dp, _dp, C.c_int, C.c_char, C.c_char]
         L.orc_sum_amb.restype = C.c_double
         L.orc_sum_amb.argtypes = [C.c_int, C.c_int, _dp, _dp, C.c_char]
@@ -217,6 +219,18 @@ class Grid:
         out = np.zeros((self.ms, self.ms), order="F")
         lib().orc_hf_matrix(self._p, nbf, _d(pq), iorb, kmax, _d(a), _d(b), float(qsum),
                             _d(f64(dhl)) if dhl is not None else None, _d(out))
+        return out
+
+    def hf_matrix_breit(self, pq, iorb: int, kmax: int, kr1, kr2, kr3, kr4, crk,
+                        hfm=None) -> np.ndarray:
+        """hf_matrix_breit (DBSR_HF/hf_matrix.f90:91-163) of orbital iorb added
+        into hfm (a zero matrix when None)."""
+        pq = f64(pq)
+        nbf = pq.size // (2 * self.ns)
+        out = np.zeros((self.ms, self.ms), order="F") if hfm is None else f64(hfm).copy(order="F")
+        ints = [i32(x) for x in (kr1, kr2, kr3, kr4)]
+        lib().orc_hf_matrix_breit(self._p, nbf, _d(pq), iorb, kmax, len(crk), *[_i(x) for x in ints],
+                                  _d(f64(crk)), _d(out))
         return out
 
     def v_ch(self, pq_b) -> np.ndarray:
