@@ -20,7 +20,11 @@
 // Operands are digit tiles in HBM (tc_common.cuh): U per table, Z per
 // segment slot, each [slice][32-row tile][32 x 32 BF16, canonical K-major
 // layout], so a 128-row A operand is four consecutive tiles of a slice and a
-// 32-row B operand is one tile.  One CTA per SM walks the tile list.
+// 32-row B operand is one tile.  The K dimension of a tile is 32 bound
+// orbitals; with more, the orbitals are cut into chunks of 32 (nbk of them),
+// every chunk its own digit operand with its own row/column exponents, and
+// a term's product is taken once per chunk (the chunks' products summed
+// exactly in the int64 accumulators like the products of different terms).  One CTA per SM walks the tile list.
 // One producer thread loads the operands two products ahead with 1-D bulk
 // copies (cp.async.bulk completing on an mbarrier), issues each product's 42 MMAs (21 slice
 // pairs x 2 K-steps of M=128 N=32 K=16) into one of two TMEM accumulator sets
@@ -43,6 +47,7 @@ constexpr int TILE = 32 * 32;                   // BF16 elements of a 32-row dig
 constexpr uint32_t A_BYTES = 4 * TILE * 2;      // one slice of a 128-row operand
 constexpr uint32_t B_BYTES = TILE * 2;          // one slice of a 32-row operand
 constexpr int MAXT = 4;                         // terms per tile
+constexpr int MAX_NBK = 4;                      // chunks of 32 bound orbitals (128 in all)
 // staged band rows per diagonal: a tile's 32 columns meet 32 rows of each
 // diagonal, plus one on each side for the 16-byte alignment of the copies
 constexpr int BR = 34;
@@ -94,15 +99,22 @@ __device__ __forceinline__ void write_digit_row(__nv_bfloat16 *D, int NR, int ro
 // over its 32-row tiles
 constexpr int EXP_PER_ROWTILE = 33;
 
-// U (ns x nb, column-major) -> digit operand [slice][NR][TILE] and exponents
-__global__ void k_udigits(int ns, int nb, int NR, const double *U, __nv_bfloat16 *D, int *eu) {
+// U (ns x nb, column-major), orbital chunk blockIdx.y (orbitals 32c ..
+// 32c+31) -> digit operand [chunk][slice][NR][TILE] and exponents
+// [chunk][NR*33]
+__global__ void k_udigits(int ns, int nb, int NR, const double *U, __nv_bfloat16 *Dall,
+                          int *euall) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int ck = blockIdx.y;
   if (x >= NR * 32) return;
+  __nv_bfloat16 *D = Dall + (size_t)ck * TS * NR * TILE;
+  int *eu = euall + (size_t)ck * NR * EXP_PER_ROWTILE;
   double vals[32];
   double m = 0.0;
 #pragma unroll
   for (int k = 0; k < 32; k++) {
-    vals[k] = (x < ns && k < nb) ? U[(size_t)x + (size_t)ns * k] : 0.0;
+    const int o = 32 * ck + k;
+    vals[k] = (x < ns && o < nb) ? U[(size_t)x + (size_t)ns * o] : 0.0;
     m = fmax(m, fabs(vals[k]));
   }
   const int e = scale_exp(m);
@@ -113,14 +125,14 @@ __global__ void k_udigits(int ns, int nb, int NR, const double *U, __nv_bfloat16
 }
 
 struct ZArgs {
-  int ns, nb, NR, nm, lower;
+  int ns, nb, nbk, NR, nm, lower;
   const float2 *V[4], *Vl[4], *Kb[4];  // float-float copies
   const int *members;
   const SegInfo *info;
   const int *pairs;
   const float2 *cd;
-  __nv_bfloat16 *Zd;  // [a][mode][slot][slice][NR][TILE]
-  int *ez;            // [a][mode][slot][NR*33]
+  __nv_bfloat16 *Zd;  // [a][mode][slot][chunk][slice][NR][TILE]
+  int *ez;            // [a][mode][slot][chunk][NR*33]
   double *Yb;         // [a][slot][ns*17]
 };
 
@@ -185,40 +197,43 @@ __global__ void __launch_bounds__(ZROWS) k_zdigits(const ZArgs z) {
   for (int mode = 0; mode < (z.lower ? 2 : 1); mode++) {
     float2 *zz = mode ? z1 : z0;
     // each sum renormalised in place (TwoSum: hi + lo unchanged, |lo| at
-    // most half an ulp of hi); the row exponent from the high words
-    float m = 0.0f;
+    // most half an ulp of hi)
     for (int k = 0; k < nb; k++) {
       const float2 v = zz[k * ZROWS + t];
       const float s = v.x + v.y, bp = s - v.x;
-      const float2 w = make_float2(s, (v.x - (s - bp)) + (v.y - bp));
-      zz[k * ZROWS + t] = w;
-      m = fmaxf(m, fabsf(w.x));
+      zz[k * ZROWS + t] = make_float2(s, (v.x - (s - bp)) + (v.y - bp));
     }
-    const int e = scale_exp_ff(m);
-    const size_t op = (size_t)(a * 2 + mode) * z.nm + slot;
-    z.ez[op * z.NR * EXP_PER_ROWTILE + y] = e;
-    const int et = __reduce_max_sync(0xffffffffu, e);  // a warp is one 32-row tile
-    if ((t & 31) == 0) z.ez[op * z.NR * EXP_PER_ROWTILE + z.NR * 32 + y / 32] = et;
-    // the digits 8 columns at a time, re-read from shared memory
-    for (int kg = 0; kg < 4; kg++) {
-      float2 vals[8];
+    // per chunk of 32 orbitals: the row exponent from the high words, the
+    // digits 8 columns at a time
+    for (int ck = 0; ck < z.nbk; ck++) {
+      float m = 0.0f;
+      for (int k = 32 * ck; k < min(nb, 32 * ck + 32); k++) m = fmaxf(m, fabsf(zz[k * ZROWS + t].x));
+      const int e = scale_exp_ff(m);
+      const size_t op = ((size_t)(a * 2 + mode) * z.nm + slot) * z.nbk + ck;
+      z.ez[op * z.NR * EXP_PER_ROWTILE + y] = e;
+      const int et = __reduce_max_sync(0xffffffffu, e);  // a warp is one 32-row tile
+      if ((t & 31) == 0) z.ez[op * z.NR * EXP_PER_ROWTILE + z.NR * 32 + y / 32] = et;
+      for (int kg = 0; kg < 4; kg++) {
+        float2 vals[8];
 #pragma unroll
-      for (int u = 0; u < 8; u++) {
-        const int k = 8 * kg + u;
-        vals[u] = k < nb ? zz[k * ZROWS + t] : make_float2(0.0f, 0.0f);
+        for (int u = 0; u < 8; u++) {
+          const int k = 32 * ck + 8 * kg + u;
+          vals[u] = k < nb ? zz[k * ZROWS + t] : make_float2(0.0f, 0.0f);
+        }
+        write_digit_group_ff(z.Zd + op * TS * sl, z.NR, y, kg, vals, e);
       }
-      write_digit_group_ff(z.Zd + op * TS * sl, z.NR, y, kg, vals, e);
     }
   }
 }
 
 struct XArgs {
   int ns, NR, ntx, nty, nm, na, lower;
+  int nbk;                     // chunks of 32 bound orbitals (products per term and field)
   int nrows;                   // (quadrant record, x tile) rows of 128 x ns
-  const __nv_bfloat16 *Ud[4];  // per atype: [mode][slice][NR][TILE]
-  const int *eu[4];            // per atype: [mode][NR*33]
-  const __nv_bfloat16 *Zd;     // [a][mode][slot][slice][NR][TILE]
-  const int *ez;               // [a][mode][slot][NR*33]
+  const __nv_bfloat16 *Ud[4];  // per atype: [mode][chunk][slice][NR][TILE]
+  const int *eu[4];            // per atype: [mode][chunk][NR*33]
+  const __nv_bfloat16 *Zd;     // [a][mode][slot][chunk][slice][NR][TILE]
+  const int *ez;               // [a][mode][slot][chunk][NR*33]
   const double *Yb;            // [a][slot][ns*17]
   const XQuad *xq;
   double *hch;
@@ -289,11 +304,12 @@ struct ProdIt {
   Row r;
 };
 
-// advance to the next product; false when the CTA's rows are done
+// advance to the next product (product pc of a tile: field product pc / nbk
+// of the codes, orbital chunk pc % nbk); false when the CTA's rows are done
 __device__ __forceinline__ bool prod_next(const XArgs &p, ProdIt &it) {
   if (it.row >= p.nrows) return false;
   it.pc++;
-  while (it.pc >= it.np) {
+  while (it.pc >= it.np * p.nbk) {
     if (++it.ty >= p.nty) {
       it.row += gridDim.x;
       if (it.row >= p.nrows) return false;
@@ -312,10 +328,12 @@ __device__ __forceinline__ bool prod_next(const XArgs &p, ProdIt &it) {
 __device__ __forceinline__ void prod_operands(const XArgs &p, const ProdIt &it, size_t sl,
                                               const __nv_bfloat16 *&As,
                                               const __nv_bfloat16 *&Bs) {
-  const int pcode = (it.codes >> (3 * it.pc)) & 7, t = pcode & 3, m = pcode >> 2;
+  const int fp = it.pc / p.nbk, ck = it.pc - fp * p.nbk;
+  const int pcode = (it.codes >> (3 * fp)) & 7, t = pcode & 3, m = pcode >> 2;
   const int tc = term_code(it.r, t), a = tc & 3, tra = (tc >> 2) & 1, slot = tc >> 3;
-  const __nv_bfloat16 *Ub = p.Ud[a] + (size_t)m * TS * sl;
-  const __nv_bfloat16 *Zb = p.Zd + ((size_t)(a * 2 + m) * p.nm + slot) * TS * sl;
+  const __nv_bfloat16 *Ub = p.Ud[a] + ((size_t)m * p.nbk + ck) * TS * sl;
+  const __nv_bfloat16 *Zb =
+      p.Zd + (((size_t)(a * 2 + m) * p.nm + slot) * p.nbk + ck) * TS * sl;
   As = (tra ? Zb : Ub) + (size_t)4 * it.r.tx * TILE;
   Bs = (tra ? Ub : Zb) + (size_t)it.ty * TILE;
 }
@@ -670,13 +688,14 @@ __global__ void __maxnreg__(96) k_xfused(const XArgs p) {
         int cur[CPT];
 #pragma unroll
         for (int c = 0; c < CPT; c++) cur[c] = -100000;
-        for (int pc = 0; pc < np; pc++, q++) {
+        for (int pc = 0; pc < np * p.nbk; pc++, q++) {
           const int b = q & 1;
           const uint32_t n = q >> 1;
-          const int pcode = (codes >> (3 * pc)) & 7, m = pcode >> 2;
+          const int fp = pc / p.nbk, ck = pc - fp * p.nbk;
+          const int pcode = (codes >> (3 * fp)) & 7, m = pcode >> 2;
           const int tc = term_code(r, pcode & 3), a = tc & 3, tra = (tc >> 2) & 1;
-          const int *eua = p.eu[a] + (size_t)m * EX;
-          const int *ezs = p.ez + ((size_t)(a * 2 + m) * p.nm + (tc >> 3)) * EX;
+          const int *eua = p.eu[a] + ((size_t)m * p.nbk + ck) * EX;
+          const int *ezs = p.ez + (((size_t)(a * 2 + m) * p.nm + (tc >> 3)) * p.nbk + ck) * EX;
           const int er = tra ? ezs[x] : eua[x];
           // column exponents: 8 ints at a 32-byte aligned offset
           const int4 *ep = reinterpret_cast<const int4 *>((tra ? eua : ezs) + y0);
@@ -833,7 +852,7 @@ bool build_xquads(int na, const int *ii, const int *jj, const std::vector<int> &
 // algorithmic work of one k_xfused launch: the read-modify-write of hch over
 // every tile that receives a product or a band term (16 bytes per element),
 // and the tensor-core FLOPs of its products (42 MMAs of 128 x 32 x 16)
-static void xfused_work(const XQuad *hxq, int nxq, int ns, int lower, double &bytes,
+static void xfused_work(const XQuad *hxq, int nxq, int ns, int lower, int nbk, double &bytes,
                         double &flops) {
   bytes = flops = 0.0;
   if (!hxq) return;
@@ -852,14 +871,16 @@ static void xfused_work(const XQuad *hxq, int nxq, int ns, int lower, double &by
         const bool band = (y0 + 31) - x0 >= -BAND && y0 - (x0 + 127) <= BAND;
         if (np == 0 && !band) continue;
         bytes += 16.0 * std::min(128, ns - x0) * std::min(32, ns - y0);
-        flops += np * (TS * (TS + 1)) * 2.0 * 128 * 32 * 16;
+        flops += (double)np * nbk * (TS * (TS + 1)) * 2.0 * 128 * 32 * 16;
       }
   }
 }
 
 int split_exchange(dbsrg_ctx *c, const SplitExchange &x) {
   const int ns = c->g.ns, nb = c->nbound;
-  if (nb < 1 || nb > 32) return set_err(c, DBSRG_EINVAL, "split exchange: 1..32 bound orbitals");
+  if (nb < 1 || nb > 32 * MAX_NBK)
+    return set_err(c, DBSRG_EINVAL, "split exchange: 1..128 bound orbitals");
+  const int nbk = (nb + 31) / 32;  // chunks of 32 bound orbitals
   if (x.na < 1 || x.na > 4 || x.nm < 1 || (x.nxq < 1 && !x.prep)) return DBSRG_OK;
   cudaStream_t st = c->stream;
   int rc0;
@@ -870,18 +891,19 @@ int split_exchange(dbsrg_ctx *c, const SplitExchange &x) {
     FarField *f = const_cast<FarField *>(x.far[a]);
     if (f->Ud) continue;
     void *d = nullptr;
-    const size_t bytes =
-        2 * TS * sl * sizeof(__nv_bfloat16) + 2 * (size_t)NR * EXP_PER_ROWTILE * sizeof(int);
+    const size_t bytes = 2 * (size_t)nbk * TS * sl * sizeof(__nv_bfloat16) +
+                         2 * (size_t)nbk * NR * EXP_PER_ROWTILE * sizeof(int);
     if (!(d = cache_alloc(c, bytes))) {
       return set_err(c, DBSRG_ENOMEM, "digit allocation failed");
     }
     f->Ud = d;
-    f->eu = (int *)((char *)d + 2 * TS * sl * sizeof(__nv_bfloat16));
+    f->eu = (int *)((char *)d + 2 * (size_t)nbk * TS * sl * sizeof(__nv_bfloat16));
     for (int m = 0; m < (f->Ul ? 2 : 1); m++)
       DBSRG_RUN(c, "k_udigits",
-                k_udigits<<<(unsigned)((NR * 32 + 127) / 128), 128, 0, st>>>(
-                    ns, nb, NR, m ? f->Ul : f->U, (__nv_bfloat16 *)f->Ud + (size_t)m * TS * sl,
-                    f->eu + (size_t)m * NR * EXP_PER_ROWTILE));
+                k_udigits<<<dim3((unsigned)((NR * 32 + 127) / 128), (unsigned)nbk), 128, 0, st>>>(
+                    ns, nb, NR, m ? f->Ul : f->U,
+                    (__nv_bfloat16 *)f->Ud + (size_t)m * nbk * TS * sl,
+                    f->eu + (size_t)m * nbk * NR * EXP_PER_ROWTILE));
   }
   const size_t mv = (size_t)ns * nb;
   if (x.prep) {  // float-float far-field vectors, then nothing per chunk
@@ -894,8 +916,8 @@ int split_exchange(dbsrg_ctx *c, const SplitExchange &x) {
     return DBSRG_OK;
   }
   // per chunk: Z digits, exponents, band rows, error word
-  const size_t zel = (size_t)x.na * 2 * x.nm * TS * sl;
-  const size_t zex = (size_t)x.na * 2 * x.nm * NR * EXP_PER_ROWTILE;
+  const size_t zel = (size_t)x.na * 2 * x.nm * nbk * TS * sl;
+  const size_t zex = (size_t)x.na * 2 * x.nm * nbk * NR * EXP_PER_ROWTILE;
   const size_t ybn = (size_t)x.na * x.nm * ns * NDB;
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
   const size_t bytes = al(zel * 2) + al(zex * 4) + al(ybn * 8);
@@ -912,6 +934,7 @@ int split_exchange(dbsrg_ctx *c, const SplitExchange &x) {
   ZArgs z{};
   z.ns = ns;
   z.nb = nb;
+  z.nbk = nbk;
   z.NR = NR;
   z.nm = x.nm;
   z.lower = x.lower;
@@ -938,7 +961,7 @@ int split_exchange(dbsrg_ctx *c, const SplitExchange &x) {
   const double zf = 2.0 * x.na * ns * (1.0 + x.lower + NDB) * (double)x.nent;
   const double zb = 8.0 * x.na * ns * ((1.0 + x.lower + NDB) * (double)x.nent +
                                        NDB * (double)x.nm) +
-                    2.0 * TS * (double)x.na * (1 + x.lower) * x.nm * NR * TILE;
+                    2.0 * TS * (double)x.na * (1 + x.lower) * x.nm * nbk * NR * TILE;
   DBSRG_RUN_W(c, "k_zdigits", zb, zf,
               k_zdigits<<<dim3((unsigned)(NR * 32 / ZROWS), (unsigned)x.nm, (unsigned)x.na),
                           ZROWS, zsm, st>>>(z));  // every row of the operand, zeros past ns
@@ -950,6 +973,7 @@ int split_exchange(dbsrg_ctx *c, const SplitExchange &x) {
   p.nm = x.nm;
   p.na = x.na;
   p.lower = x.lower;
+  p.nbk = nbk;
   p.nrows = x.nxq * ntx;
   for (int a = 0; a < x.na; a++) {
     p.Ud[a] = (const __nv_bfloat16 *)x.far[a]->Ud;
@@ -968,7 +992,7 @@ int split_exchange(dbsrg_ctx *c, const SplitExchange &x) {
   if ((rc = raise_smem_limit(c, (const void *)k_xfused, smem))) return rc;
   const int nblk = std::min(p.nrows, std::max(1, c->nsm));
   double wbytes = 0.0, wflops = 0.0;
-  if (c->timing) xfused_work(x.hxq, x.nxq, ns, x.lower, wbytes, wflops);
+  if (c->timing) xfused_work(x.hxq, x.nxq, ns, x.lower, nbk, wbytes, wflops);
   DBSRG_RUN_W(c, "k_xfused", wbytes, wflops, k_xfused<<<(unsigned)nblk, NTHR, smem, st>>>(p));
   return DBSRG_OK;
 }

@@ -43,7 +43,7 @@
 
 namespace {
 
-constexpr int NB_MAX = 64;        // bound orbitals handled by the factored path
+constexpr int NB_MAX = 128;       // bound orbitals handled by the factored path
 constexpr int FAR = 9;            // |y - x| >= FAR is far field (spline orders <= 9)
 constexpr int BAND = FAR - 1;     // near band |y - x| <= 8
 constexpr int NDB = 2 * BAND + 1; // band diagonals
@@ -836,7 +836,7 @@ int pair_index(dbsrg_ctx *c, int n, const int *k2, const int *k3, int *pairs, in
                cudaStream_t s) {
   if (n <= 0) return DBSRG_OK;
   if (c->nbound < 1 || c->nbound > NB_MAX)
-    return set_err(c, DBSRG_EINVAL, "factored contraction: 1..64 bound orbitals (ipbs = 0)");
+    return set_err(c, DBSRG_EINVAL, "factored contraction: 1..128 bound orbitals (ipbs = 0)");
   DBSRG_RUN_S(c, s, "k_pair_index",
               k_pair_index<<<(n + 255) / 256, 256, 0, s>>>(n, k2, k3, c->bmap, c->nbound, pairs,
                                                            derr));
@@ -1113,7 +1113,7 @@ int factored_contract(dbsrg_ctx *c, const FactorJob &j) {
   cudaStream_t st = c->stream;
   int rc;
   if (nb < 1 || nb > NB_MAX)
-    return set_err(c, DBSRG_EINVAL, "factored contraction: 1..64 bound orbitals (ipbs = 0)");
+    return set_err(c, DBSRG_EINVAL, "factored contraction: 1..128 bound orbitals (ipbs = 0)");
   if (ks > FAR) return set_err(c, DBSRG_EINVAL, "factored contraction: spline order above 9");
   if (j.nown < 1) return DBSRG_OK;
   QuadSpec qs{};

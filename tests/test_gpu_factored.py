@@ -113,31 +113,49 @@ def test_split_multi_tile_rows_against_plain(ns):
     assert np.abs(as_ - ap).max() <= 1e-12 * max(np.abs(ap).max(), 1e-300)
 
 
-def test_split_exchange_bound_orbital_limit():
-    """The split exchange holds up to 32 bound orbitals per digit operand
-    (one K tile); more is an EINVAL from the call, and FACTOR_FP64 (up to 64)
-    still assembles the list."""
+def _many_orbitals(nb, seed):
+    """A small grid with nb bound orbitals (hydrogenic shapes with n up to 12
+    over the kappas of the target list) and two channels; R^k and S^k lists
+    whose entries draw bound orbitals from all of them."""
+    base = synth.TARGET_ORBITALS
+    orbitals = [(n + 1 + i // len(base), k) for i, (n, k) in enumerate(base * 5)][:nb]
+    return synth._build(f"{nb} bound orbitals", seed, 60, 20.0, 8.0, orbitals, [-1, 2], 2,
+                        900, 1.0, breit=True, o_entries=6)
+
+
+@pytest.mark.parametrize("nb", [48, 96])
+@pytest.mark.parametrize("precision,tol", [(FACTOR_FP64, 1e-12), (SPLIT_BF16, 1e-10)])
+def test_factored_forms_with_many_bound_orbitals(nb, precision, tol):
+    """More than 32 bound orbitals: the split exchange takes one product per
+    chunk of 32 orbitals (48: two chunks, 96: three), the factored FP64 path
+    any number up to 128; every block against the oracle."""
+    w = _many_orbitals(nb, 300 + nb)
+    used = set()
+    for L in w.lists:
+        if L.icase in (2, 3):
+            used |= set(L.k2.tolist()) | set(L.k3.tolist())
+    assert max(used) > 64 if nb > 64 else max(used) > 32
+    h, acf = run(w, precision)
+    ref, racf = oracle(w)
+    check(h, ref, tol)
+    assert relmax(acf, racf) <= 1e-12
+
+
+def test_bound_orbital_limit_of_the_factored_forms():
+    """129 bound orbitals are beyond the factored forms (EINVAL from the
+    call); the plain form still assembles the list."""
     from dbsr_gb300._lib import DbsrgError
 
-    w = synth.small(ns=50, nch=2, mk=2, n_entries=200, breit=False, seed=81)
-    nb0 = int((w.ipbs == 0).sum())
-    extra = 33 - nb0
-    pq = np.concatenate([w.pq[:, :, :nb0]] * (1 + extra // nb0 + 1), axis=2)[:, :, :33]
-    pq = np.concatenate([pq, w.pq[:, :, nb0:]], axis=2)
-    ipbs = np.concatenate([np.zeros(33, np.int32), w.ipbs[nb0:]])
-    # channel orbitals move up by `extra` positions in the O list keys only;
-    # R/S lists address channels by K1 and bound orbitals by K2/K3 (< nb0)
+    w = _many_orbitals(129, 81)
     L = next(L for L in w.lists if L.icase == 2 and L.itype == 4)
-    a = Assembler(w.t, w.ks, w.ksp, w.ksq)
-    a.set_orbitals(np.asfortranarray(pq), ipbs)
-    a.alloc_matrix(w.nch, w.icc, w.iicc, w.mk)
-    a.set_precision(SPLIT_BF16)
-    with pytest.raises(DbsrgError, match="EINVAL"):
-        a.gen_matrix(L.icase, L.itype, L.kpol, L.k1, L.k2, L.k3, L.k4, L.c)
-    a.set_precision(FACTOR_FP64)
-    a.zero_matrix()
-    a.gen_matrix(L.icase, L.itype, L.kpol, L.k1, L.k2, L.k3, L.k4, L.c)
-    h = a.get_matrix()
-    a.close()
+    for prec in (SPLIT_BF16, FACTOR_FP64):
+        a = Assembler(w.t, w.ks, w.ksp, w.ksq)
+        a.set_orbitals(w.pq, w.ipbs)
+        a.alloc_matrix(w.nch, w.icc, w.iicc, w.mk)
+        a.set_precision(prec)
+        with pytest.raises(DbsrgError, match="EINVAL"):
+            a.gen_matrix(L.icase, L.itype, L.kpol, L.k1, L.k2, L.k3, L.k4, L.c)
+        a.close()
+    h, _ = run(w, PLAIN_FP64, [L])
     ref, _ = oracle(w, [L])
     check(h, ref, 1e-12)
