@@ -124,22 +124,6 @@ __global__ void k_udigits(int ns, int nb, int NR, const double *U, __nv_bfloat16
   write_digit_row(D, NR, x, vals, e);
 }
 
-// Per segment slot and atype, one thread per row y, in two kernels:
-// k_zsums forms
-//   Z_s(k,y) = sum_{e in s, first orbital k} c_e V(y, second orbital)  (Zl with Vl)
-//   Yb_s(y,d) = sum_e c_e Kb(pair_e; y, d)                             (near band)
-// as float-float sums (ff.cuh), walking the segment's entries once: the Z
-// sum of the current first orbital stays in registers and goes to Zs when
-// the first orbital changes (a list sorted by (K1,K2,K3) meets each first
-// orbital in one run, so every Z(k,y) is written once; a later run of the
-// same orbital is added to it); k_zdigits then forms the digits of Z (and
-// Zl) and their row exponents, per chunk of 32 bound orbitals.  The sums
-// read the pair potentials of every entry: that kernel is bound by those
-// reads (L2 and HBM), and keeps no per-orbital arrays in shared memory so
-// that many warps share an SM to hide them.
-constexpr int ZROWS = 128;  // rows of a k_zsums block (4 warps)
-constexpr int DROWS = 32;   // rows of a k_zdigits block (one warp: one 32-row tile)
-
 struct ZArgs {
   int ns, nb, nbk, NR, nm, lower;
   const float2 *V[4], *Vl[4], *Kb[4];  // float-float copies
@@ -147,53 +131,36 @@ struct ZArgs {
   const SegInfo *info;
   const int *pairs;
   const float2 *cd;
-  float2 *Zs;         // [a][mode][slot][nb][NR*32] the sums (hi, lo), unnormalised
   __nv_bfloat16 *Zd;  // [a][mode][slot][chunk][slice][NR][TILE]
   int *ez;            // [a][mode][slot][chunk][NR*33]
   double *Yb;         // [a][slot][ns*17]
 };
 
-__global__ void __launch_bounds__(ZROWS, 6) k_zsums(const ZArgs z) {
+// Per segment slot and atype, one thread per row y (ZROWS rows a block):
+//   Z_s(k,y) = sum_{e in s, first orbital k} c_e V(y, second orbital)  (Zl with Vl)
+//   Yb_s(y,d) = sum_e c_e Kb(pair_e; y, d)                             (near band)
+// as float-float sums (ff.cuh), then the digits of Z (and Zl) and their row
+// exponents.  The sums read the pair potentials of every entry: the kernel
+// is bound by those reads (L2 and HBM), not by its arithmetic.
+constexpr int ZROWS = 32;  // one warp per block: one 32-row digit tile
+__global__ void __launch_bounds__(ZROWS) k_zdigits(const ZArgs z) {
+  // [mode][nb][ZROWS] float-float: per thread one column; sized by the bound
+  // orbitals (and the modes) in use, which sets how many blocks share an SM
+  extern __shared__ float2 zs[];
   const int t = threadIdx.x, y = blockIdx.x * ZROWS + t, slot = blockIdx.y, a = blockIdx.z;
-  const int ns = z.ns, nb = z.nb, NRR = z.NR * 32;
-  if (y >= NRR) return;
-  float2 *Z0 = z.Zs + ((size_t)(a * 2 + 0) * z.nm + slot) * nb * NRR + y;
-  float2 *Z1 = z.Zs + ((size_t)(a * 2 + 1) * z.nm + slot) * nb * NRR + y;
+  const int ns = z.ns, nb = z.nb;
+  float2 *z0 = zs, *z1 = zs + nb * ZROWS;
+  for (int k = 0; k < nb; k++) {
+    z0[k * ZROWS + t] = make_float2(0.0f, 0.0f);
+    if (z.lower) z1[k * ZROWS + t] = make_float2(0.0f, 0.0f);
+  }
   const SegInfo si = z.info[z.members[slot]];
   const float2 *V = z.V[a], *Vl = z.lower ? z.Vl[a] : nullptr, *Kb = z.Kb[a];
   const size_t kper = (size_t)ns * NDB;
-  // first orbitals already written (bit k), to add a later run instead of
-  // storing over it; 128 orbitals at most
-  uint32_t done[4] = {0u, 0u, 0u, 0u};
-  int cur = -1;
-  float zh = 0.0f, zl = 0.0f, wh = 0.0f, wl = 0.0f;  // Z and Zl of orbital cur
-  auto flush = [&]() {
-    if (cur < 0) return;
-    const uint32_t bit = 1u << (cur & 31);
-    float2 *d0 = Z0 + (size_t)cur * NRR, *d1 = Z1 + (size_t)cur * NRR;
-    if (done[cur >> 5] & bit) {  // a second run of the same orbital: add
-      float2 o = *d0;
-      ffa::add(make_float2(zh, zl), o.x, o.y);
-      *d0 = o;
-      if (Vl) {
-        float2 p = *d1;
-        ffa::add(make_float2(wh, wl), p.x, p.y);
-        *d1 = p;
-      }
-    } else {
-      *d0 = make_float2(zh, zl);
-      if (Vl) *d1 = make_float2(wh, wl);
-      done[cur >> 5] |= bit;
-    }
-  };
-  // two passes over the entries: the Z sums and band diagonals 0..8, then
-  // diagonals 9..16 (half the band registers, so more warps share an SM)
-  constexpr int HB = (NDB + 1) / 2;
-  for (int pass = 0; pass < 2 && y < ns; pass++) {
-    const int d0 = pass * HB;
-    float bh[HB], bl[HB];
+  float bh[NDB], bl[NDB];
 #pragma unroll
-    for (int u = 0; u < HB; u++) bh[u] = bl[u] = 0.0f;
+  for (int d = 0; d < NDB; d++) bh[d] = bl[d] = 0.0f;
+  if (y < ns) {
     // the next entry's pair index and coefficient are loaded while this
     // entry's potentials are summed
     int pr_n = si.start < si.end ? z.pairs[si.start] : 0;
@@ -205,69 +172,56 @@ __global__ void __launch_bounds__(ZROWS, 6) k_zsums(const ZArgs z) {
         pr_n = z.pairs[e + 1];
         c_n = z.cd[e + 1];
       }
-      const float2 *kb = Kb + (size_t)pr * kper + (size_t)ns * d0 + y;
-      float2 kv[HB];
+      const float2 *kb = Kb + (size_t)pr * kper + y;
+      float2 kv[NDB];
 #pragma unroll
-      for (int u = 0; u < HB; u++)
-        if (d0 + u < NDB) kv[u] = kb[(size_t)ns * u];
-      if (pass == 0) {
-        const float2 vv = V[(size_t)y + (size_t)ns * ob];
-        const float2 vl = Vl ? Vl[(size_t)y + (size_t)ns * ob] : make_float2(0.0f, 0.0f);
-        if (oa != cur) {
-          flush();
-          cur = oa;
-          zh = zl = wh = wl = 0.0f;
-        }
-        ffa::mac(c, vv, zh, zl);
-        if (Vl) ffa::mac(c, vl, wh, wl);
+      for (int d = 0; d < NDB; d++) kv[d] = kb[(size_t)ns * d];
+      {
+        float2 acc = z0[oa * ZROWS + t];
+        ffa::mac(c, V[(size_t)y + (size_t)ns * ob], acc.x, acc.y);
+        z0[oa * ZROWS + t] = acc;
+      }
+      if (Vl) {
+        float2 acc = z1[oa * ZROWS + t];
+        ffa::mac(c, Vl[(size_t)y + (size_t)ns * ob], acc.x, acc.y);
+        z1[oa * ZROWS + t] = acc;
       }
 #pragma unroll
-      for (int u = 0; u < HB; u++)
-        if (d0 + u < NDB) ffa::mac(c, kv[u], bh[u], bl[u]);
+      for (int d = 0; d < NDB; d++) ffa::mac(c, kv[d], bh[d], bl[d]);
     }
-    if (pass == 0) flush();
-    double *yb = z.Yb + ((size_t)a * z.nm + slot) * kper + (size_t)ns * d0 + y;
+    double *yb = z.Yb + ((size_t)a * z.nm + slot) * kper + y;
 #pragma unroll
-    for (int u = 0; u < HB; u++)
-      if (d0 + u < NDB) yb[(size_t)ns * u] = ffa::value(bh[u], bl[u]);
+    for (int d = 0; d < NDB; d++) yb[(size_t)ns * d] = ffa::value(bh[d], bl[d]);
   }
-  // orbitals with no entries (and every row past ns) hold zeros
-  for (int k = 0; k < nb; k++)
-    if (!(done[k >> 5] & (1u << (k & 31)))) {
-      Z0[(size_t)k * NRR] = make_float2(0.0f, 0.0f);
-      if (z.lower) Z1[(size_t)k * NRR] = make_float2(0.0f, 0.0f);
-    }
-}
-
-// the digits of the sums: per slot, atype and field one thread per row y,
-// each sum renormalised (TwoSum: hi + lo unchanged, |lo| at most half an ulp
-// of hi), the row exponent per chunk of 32 orbitals from the high words
-__global__ void __launch_bounds__(DROWS) k_zdigits(const ZArgs z) {
-  const int t = threadIdx.x, y = blockIdx.x * DROWS + t, slot = blockIdx.y;
-  const int a = blockIdx.z >> 1, mode = blockIdx.z & 1;
-  if (mode == 1 && !z.lower) return;
-  const int nb = z.nb, NRR = z.NR * 32;
-  const float2 *Zr = z.Zs + ((size_t)(a * 2 + mode) * z.nm + slot) * nb * NRR + y;
   const size_t sl = (size_t)z.NR * TILE;
-  auto zval = [&](int k) -> float2 {
-    if (k >= nb) return make_float2(0.0f, 0.0f);
-    const float2 v = Zr[(size_t)k * NRR];
-    const float s = v.x + v.y, bp = s - v.x;
-    return make_float2(s, (v.x - (s - bp)) + (v.y - bp));
-  };
-  for (int ck = 0; ck < z.nbk; ck++) {
-    float m = 0.0f;
-    for (int k = 32 * ck; k < min(nb, 32 * ck + 32); k++) m = fmaxf(m, fabsf(zval(k).x));
-    const int e = scale_exp_ff(m);
-    const size_t op = ((size_t)(a * 2 + mode) * z.nm + slot) * z.nbk + ck;
-    z.ez[op * z.NR * EXP_PER_ROWTILE + y] = e;
-    const int et = __reduce_max_sync(0xffffffffu, e);  // a warp is one 32-row tile
-    if ((t & 31) == 0) z.ez[op * z.NR * EXP_PER_ROWTILE + z.NR * 32 + y / 32] = et;
-    for (int kg = 0; kg < 4; kg++) {
-      float2 vals[8];
+  for (int mode = 0; mode < (z.lower ? 2 : 1); mode++) {
+    float2 *zz = mode ? z1 : z0;
+    // each sum renormalised in place (TwoSum: hi + lo unchanged, |lo| at
+    // most half an ulp of hi)
+    for (int k = 0; k < nb; k++) {
+      const float2 v = zz[k * ZROWS + t];
+      const float s = v.x + v.y, bp = s - v.x;
+      zz[k * ZROWS + t] = make_float2(s, (v.x - (s - bp)) + (v.y - bp));
+    }
+    // per chunk of 32 orbitals: the row exponent from the high words, the
+    // digits 8 columns at a time
+    for (int ck = 0; ck < z.nbk; ck++) {
+      float m = 0.0f;
+      for (int k = 32 * ck; k < min(nb, 32 * ck + 32); k++) m = fmaxf(m, fabsf(zz[k * ZROWS + t].x));
+      const int e = scale_exp_ff(m);
+      const size_t op = ((size_t)(a * 2 + mode) * z.nm + slot) * z.nbk + ck;
+      z.ez[op * z.NR * EXP_PER_ROWTILE + y] = e;
+      const int et = __reduce_max_sync(0xffffffffu, e);  // a warp is one 32-row tile
+      if ((t & 31) == 0) z.ez[op * z.NR * EXP_PER_ROWTILE + z.NR * 32 + y / 32] = et;
+      for (int kg = 0; kg < 4; kg++) {
+        float2 vals[8];
 #pragma unroll
-      for (int u = 0; u < 8; u++) vals[u] = zval(32 * ck + 8 * kg + u);
-      write_digit_group_ff(z.Zd + op * TS * sl, z.NR, y, kg, vals, e);
+        for (int u = 0; u < 8; u++) {
+          const int k = 32 * ck + 8 * kg + u;
+          vals[u] = k < nb ? zz[k * ZROWS + t] : make_float2(0.0f, 0.0f);
+        }
+        write_digit_group_ff(z.Zd + op * TS * sl, z.NR, y, kg, vals, e);
+      }
     }
   }
 }
@@ -343,19 +297,22 @@ __device__ __forceinline__ int band_row0(int x0, int ty0, int dd) {
 }
 
 // the producer's walk over the products of its rows (tiles without
-// products skipped): row, tile ty, product pc of np, and the row's terms
+// products skipped): row, tile ty, field product pc of np (the codes) and
+// orbital chunk ck of nbk, and the row's terms
 struct ProdIt {
-  int row, ty, pc, np;
+  int row, ty, pc, np, ck;
   uint32_t codes;
   Row r;
 };
 
-// advance to the next product (product pc of a tile: field product pc / nbk
-// of the codes, orbital chunk pc % nbk); false when the CTA's rows are done
+// advance to the next product (orbital chunks innermost); false when the
+// CTA's rows are done
 __device__ __forceinline__ bool prod_next(const XArgs &p, ProdIt &it) {
   if (it.row >= p.nrows) return false;
+  if (++it.ck < p.nbk) return true;
+  it.ck = 0;
   it.pc++;
-  while (it.pc >= it.np * p.nbk) {
+  while (it.pc >= it.np) {
     if (++it.ty >= p.nty) {
       it.row += gridDim.x;
       if (it.row >= p.nrows) return false;
@@ -374,8 +331,8 @@ __device__ __forceinline__ bool prod_next(const XArgs &p, ProdIt &it) {
 __device__ __forceinline__ void prod_operands(const XArgs &p, const ProdIt &it, size_t sl,
                                               const __nv_bfloat16 *&As,
                                               const __nv_bfloat16 *&Bs) {
-  const int fp = it.pc / p.nbk, ck = it.pc - fp * p.nbk;
-  const int pcode = (it.codes >> (3 * fp)) & 7, t = pcode & 3, m = pcode >> 2;
+  const int ck = it.ck;
+  const int pcode = (it.codes >> (3 * it.pc)) & 7, t = pcode & 3, m = pcode >> 2;
   const int tc = term_code(it.r, t), a = tc & 3, tra = (tc >> 2) & 1, slot = tc >> 3;
   const __nv_bfloat16 *Ub = p.Ud[a] + ((size_t)m * p.nbk + ck) * TS * sl;
   const __nv_bfloat16 *Zb =
@@ -477,6 +434,7 @@ __global__ void __maxnreg__(96) k_xfused(const XArgs p) {
       it.ty = p.nty - 1;
       it.pc = 0;
       it.np = 0;
+      it.ck = p.nbk - 1;  // the first prod_next moves to the first product
       it.codes = 0;
       const __nv_bfloat16 *aKey[2] = {nullptr, nullptr};  // A operand held by each A slot
       int aslot[2] = {0, 0};                              // A slot of products q & 1
@@ -734,10 +692,12 @@ __global__ void __maxnreg__(96) k_xfused(const XArgs p) {
         int cur[CPT];
 #pragma unroll
         for (int c = 0; c < CPT; c++) cur[c] = -100000;
-        for (int pc = 0; pc < np * p.nbk; pc++, q++) {
+        // products of the tile: field product fp of the codes, orbital chunk
+        // ck (innermost)
+        for (int pc = 0, fp = 0, ck = 0; fp < np;
+             pc++, q++, (++ck == p.nbk ? (ck = 0, fp++) : 0)) {
           const int b = q & 1;
           const uint32_t n = q >> 1;
-          const int fp = pc / p.nbk, ck = pc - fp * p.nbk;
           const int pcode = (codes >> (3 * fp)) & 7, m = pcode >> 2;
           const int tc = term_code(r, pcode & 3), a = tc & 3, tra = (tc >> 2) & 1;
           const int *eua = p.eu[a] + ((size_t)m * p.nbk + ck) * EX;
@@ -961,20 +921,18 @@ int split_exchange(dbsrg_ctx *c, const SplitExchange &x) {
     }
     return DBSRG_OK;
   }
-  // per chunk: Z digits, exponents, band rows, Z sums, error word
+  // per chunk: Z digits, exponents, band rows, error word
   const size_t zel = (size_t)x.na * 2 * x.nm * nbk * TS * sl;
   const size_t zex = (size_t)x.na * 2 * x.nm * nbk * NR * EXP_PER_ROWTILE;
   const size_t ybn = (size_t)x.na * x.nm * ns * NDB;
-  const size_t zsn = (size_t)x.na * 2 * x.nm * nb * NR * 32;
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
-  const size_t bytes = al(zel * 2) + al(zex * 4) + al(ybn * 8) + al(zsn * 8);
+  const size_t bytes = al(zel * 2) + al(zex * 4) + al(ybn * 8);
   int rc = ensure_tcscratch(c, bytes);
   if (rc) return rc;
   char *q = (char *)c->tcscratch;
   __nv_bfloat16 *Zd = (__nv_bfloat16 *)q;
   int *ez = (int *)(q + al(zel * 2));
   double *Yb = (double *)(q + al(zel * 2) + al(zex * 4));
-  float2 *Zs = (float2 *)(q + al(zel * 2) + al(zex * 4) + al(ybn * 8));
   if (!c->kerr) {  // read and cleared at the end of the Gen_matrix call
     DBSRG_TRY(c, cudaMalloc((void **)&c->kerr, sizeof(int)));
     DBSRG_TRY(c, cudaMemsetAsync(c->kerr, 0, sizeof(int), st));
@@ -997,28 +955,22 @@ int split_exchange(dbsrg_ctx *c, const SplitExchange &x) {
   z.info = x.info;
   z.pairs = x.pairs;
   z.cd = x.cdf;
-  z.Zs = Zs;
   z.Zd = Zd;
   z.ez = ez;
   z.Yb = Yb;
+  const size_t zsm = (size_t)(x.lower ? 2 : 1) * nb * ZROWS * sizeof(float2);
+  if ((rc = raise_smem_limit(c, (const void *)k_zdigits, zsm))) return rc;
   // executed work: per PQ type, row and entry one multiply-add per field
   // (Z, and Zl for R^k) and per band diagonal (17), float-float; the entry's
-  // potential values (17 band and 1-2 field float-float pairs a row) read,
-  // the band rows and the sums written; then the sums read and the digits
-  // written
+  // band potential values (17 float-float pairs a row) read, the digits and
+  // band rows written
   const double zf = 2.0 * x.na * ns * (1.0 + x.lower + NDB) * (double)x.nent;
-  const double zsb = 8.0 * x.na * ns * ((1.0 + x.lower + NDB) * (double)x.nent +
-                                        NDB * (double)x.nm) +
-                     8.0 * x.na * (1 + x.lower) * x.nm * (double)nb * NR * 32;
-  const double zdb = 8.0 * x.na * (1 + x.lower) * x.nm * (double)nb * NR * 32 +
-                     2.0 * TS * (double)x.na * (1 + x.lower) * x.nm * nbk * NR * TILE;
-  DBSRG_RUN_W(c, "k_zsums", zsb, zf,
-              k_zsums<<<dim3((unsigned)(NR * 32 / ZROWS), (unsigned)x.nm, (unsigned)x.na),
-                        ZROWS, 0, st>>>(z));  // every row of the operand, zeros past ns
-  DBSRG_RUN_W(c, "k_zdigits", zdb, 0.0,
-              k_zdigits<<<dim3((unsigned)(NR * 32 / DROWS), (unsigned)x.nm,
-                               (unsigned)(2 * x.na)),
-                          DROWS, 0, st>>>(z));
+  const double zb = 8.0 * x.na * ns * ((1.0 + x.lower + NDB) * (double)x.nent +
+                                       NDB * (double)x.nm) +
+                    2.0 * TS * (double)x.na * (1 + x.lower) * x.nm * nbk * NR * TILE;
+  DBSRG_RUN_W(c, "k_zdigits", zb, zf,
+              k_zdigits<<<dim3((unsigned)(NR * 32 / ZROWS), (unsigned)x.nm, (unsigned)x.na),
+                          ZROWS, zsm, st>>>(z));  // every row of the operand, zeros past ns
   XArgs p{};
   p.ns = ns;
   p.NR = NR;

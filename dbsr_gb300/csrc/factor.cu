@@ -507,10 +507,7 @@ __global__ void __launch_bounds__(256) k_pair_diag(int ns, int ks, int kk, int n
   }
   __syncthreads();
   const int ph = (cv - 1) % FAR;
-  // the chunk of PBC second orbitals of this block (blockIdx.y): the chunks
-  // of a cell run in separate blocks, which keeps more warps on an SM
-  {
-    const int b0 = blockIdx.y * PBC;
+  for (int b0 = 0; b0 < nb; b0 += PBC) {  // chunks of second orbitals
     const int bc = min(PBC, nb - b0);
     // stage 1: a thread forms H(po, g1, b) for the bc second orbitals of the
     // chunk at once (independent sums sharing each table load)
@@ -584,6 +581,7 @@ __global__ void __launch_bounds__(256) k_pair_diag(int ns, int ks, int kk, int n
           if (bb < bc) Dq[d0 + (size_t)bb * per] = s[bb];
       }
     }
+    __syncthreads();
   }
 }
 
@@ -983,7 +981,6 @@ int get_pairpot_direct_any(dbsrg_ctx *c, int family, int type, int k, int icv, i
   const double *lo1 = icv == 1 ? cd->lo1 : nullptr;
   const double *hi1 = (icv == 1 && family == 0) ? cd->hi1 : nullptr;
   dim3 gf((unsigned)((per + 127) / 128), (unsigned)npair);
-  const dim3 gd((unsigned)nv, (unsigned)((nb + PBC - 1) / PBC));  // cells x orbital chunks
   // executed work of the diagonal cells: per cell, stage 1 npo k1 k2 nb and
   // stage 2 npo nb k1 nb multiply-adds; the cell's table slice read and its
   // npo nb^2 outputs written.  The final potentials: per output element and
@@ -996,7 +993,7 @@ int get_pairpot_direct_any(dbsrg_ctx *c, int family, int type, int k, int icv, i
   if (ff) {
     if ((rc = set_smem(c, (const void *)k_pair_diag<true>, sm3))) return rc;
     DBSRG_RUN_W(c, "k_pair_diag", dbytes, dflops,
-                k_pair_diag<true><<<gd, 256, sm3, st>>>(
+                k_pair_diag<true><<<nv, 256, sm3, st>>>(
                     ns, ks, kk, nb, icv, sym, eo, ed, cd->rkd, P1, P2, Dq, per));
     DBSRG_RUN_W(c, "k_pair_direct_final", fbytes, fflops,
                 k_pair_direct_final<true><<<gf, 128, 0, st>>>(ns, ks, nv, kk, nb, icv, sym, eo,
@@ -1005,7 +1002,7 @@ int get_pairpot_direct_any(dbsrg_ctx *c, int family, int type, int k, int icv, i
   } else {
     if ((rc = set_smem(c, (const void *)k_pair_diag<false>, sm3))) return rc;
     DBSRG_RUN_W(c, "k_pair_diag", dbytes, dflops,
-                k_pair_diag<false><<<gd, 256, sm3, st>>>(
+                k_pair_diag<false><<<nv, 256, sm3, st>>>(
                     ns, ks, kk, nb, icv, sym, eo, ed, cd->rkd, P1, P2, Dq, per));
     DBSRG_RUN_W(c, "k_pair_direct_final", fbytes, fflops,
                 k_pair_direct_final<false><<<gf, 128, 0, st>>>(ns, ks, nv, kk, nb, icv, sym, eo,
