@@ -16,7 +16,7 @@ _ip = C.POINTER(C.c_int)
 _vp = C.c_void_p
 
 STATUS = {0: "OK", -1: "EINVAL", -2: "ECUDA", -3: "ENOMEM", -4: "ERANGE", -5: "ESTATE",
-          -6: "ETIMEOUT"}
+          -6: "ETIMEOUT", -7: "EIO"}
 
 # (name, restype, argtypes) for every entry point of include/dbsrg.h
 # void fn(void *user, int ictx, int blo, int nblocks, const double *window)
@@ -59,6 +59,9 @@ SIGNATURES = [
     ("dbsrg_diag_channels", C.c_int,
      [_vp, _vp, _vp, C.c_double, C.c_double, C.c_double, _vp, _vp, _vp]),
     ("dbsrg_channel_basis", C.c_int, [_vp, _vp, _vp, _vp]),
+    ("dbsrg_record_header", C.c_int, [_vp, C.c_char_p, C.c_int, C.c_int, _vp, _vp, _vp]),
+    ("dbsrg_record_matrix", C.c_int, [_vp, _vp, _vp, C.c_int, C.c_char_p, _vp]),
+    ("dbsrg_record_acf", C.c_int, [_vp, C.c_char_p, _vp]),
     ("dbsrg_orth_channels", C.c_int, [_vp, _vp]),
     ("dbsrg_hf_matrix", C.c_int, [_vp, C.c_int, C.c_int, _vp, _vp, C.c_double, _vp, _vp]),
     ("dbsrg_lists_create", C.c_int, [C.POINTER(_vp), C.c_int, C.c_int, _vp, _vp, _vp, C.c_int,

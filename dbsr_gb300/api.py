@@ -18,6 +18,7 @@ reference would stop.
 from __future__ import annotations
 
 import ctypes as C
+import os
 
 import numpy as np
 
@@ -70,6 +71,7 @@ class Assembler:
         self.iicc = 0
         self.mk = -1
         self.nbf = 0
+        self.npert = 0
         if tuning == "auto":
             from . import autotune
 
@@ -375,6 +377,41 @@ class Assembler:
         po, k3 = _ptr(out, np.float64) if out is not None else (None, None)
         check(self._h, self._L.dbsrg_channel_basis(self._h, ps, pn, po), "channel_basis")
         return out
+
+    def record_header(self, path, sol, ev, nsol, nsp=None, nsq=None):
+        """dbsrg_record_header: SUB1's records after Diag_channels
+        (sub1.f90:164-168) to a new file at `path`."""
+        ps, k1 = _ptr(sol, np.float64)
+        e = np.asfortranarray(ev, dtype=np.float64)
+        n = np.ascontiguousarray(nsol, dtype=np.int32)
+        nsp = self.ns if nsp is None else nsp
+        nsq = self.ns if nsq is None else nsq
+        rc = self._L.dbsrg_record_header(self._h, os.fsencode(path), int(nsp), int(nsq), ps,
+                                         C.c_void_p(e.ctypes.data), C.c_void_p(n.ctypes.data))
+        check(self._h, rc, "record_header")
+
+    def record_matrix(self, path, sol, nsol, icase=2, overlaps=None):
+        """dbsrg_record_matrix: Record_matrix (record_matrix.f90:2-60)
+        appended to `path`; with icase 0 fills and returns `overlaps`
+        ((nch+npert)^2, created zero when None).  hch is left transformed."""
+        ps, k1 = _ptr(sol, np.float64)
+        n = np.ascontiguousarray(nsol, dtype=np.int32)
+        if icase == 0 and overlaps is None:
+            no = self.nch + self.npert
+            overlaps = np.zeros((no, no), order="F")
+        po = C.c_void_p(overlaps.ctypes.data) if overlaps is not None else None
+        rc = self._L.dbsrg_record_matrix(self._h, ps, C.c_void_p(n.ctypes.data), int(icase),
+                                         os.fsencode(path), po)
+        check(self._h, rc, "record_matrix")
+        return overlaps
+
+    def record_acf(self, path, bcf):
+        """dbsrg_record_acf: the records (mk) and (bcf(nch,nch,0:mk))."""
+        b = np.asfortranarray(bcf, dtype=np.float64)
+        if b.shape != (self.nch, self.nch, self.mk + 1):
+            raise ValueError("bcf must be (nch, nch, mk+1)")
+        rc = self._L.dbsrg_record_acf(self._h, os.fsencode(path), C.c_void_p(b.ctypes.data))
+        check(self._h, rc, "record_acf")
 
     def orth_channels(self, iort):
         """dbsrg_orth_channels (DBS_ORTH, dbs_orth.f90:2-84): iort(nbf, nch)

@@ -47,7 +47,8 @@ enum dbsrg_status {
   DBSRG_ENOMEM = -3,   /* device allocation failed                        */
   DBSRG_ERANGE = -4,   /* index out of range in a list (UPDATE_* checks)  */
   DBSRG_ESTATE = -5,   /* call order violated (e.g. no matrix allocated)  */
-  DBSRG_ETIMEOUT = -6  /* a device-side bounded wait ran out              */
+  DBSRG_ETIMEOUT = -6, /* a device-side bounded wait ran out              */
+  DBSRG_EIO = -7       /* a file of the write-out could not be written     */
 };
 
 /* precision / algorithm of the contraction */
@@ -286,6 +287,35 @@ int dbsrg_diag_channels(dbsrg_ctx *ctx, const double *bdiag, const int *iprm,
                         double *eval, int *nsol);
 int dbsrg_channel_basis(dbsrg_ctx *ctx, const double *sol, const int *nsol,
                         double *out);
+
+/* The dbsr_mat.nnn write-out, as Fortran sequential unformatted records
+ * (gfortran's layout: a 4-byte record length before and after each record,
+ * machine byte order).
+ * dbsrg_record_header -- SUB1's records after Diag_channels
+ * (sub1.f90:164-168), written to a new file at path (truncated, as the
+ * rewind of nui does): (ns, nch, npert, nsp, nsq), (nsol), (jpsol(0:nch)),
+ * (eval(1:nsol)), (diag(1:ms, 1:ipsol(ich), ich) of every channel); sol,
+ * eval and nsol as dbsrg_diag_channels returns them (eval, nsol host).
+ * dbsrg_record_matrix -- Record_matrix (record_matrix.f90:2-60), appended
+ * to path: (ich, jch) and c = D_ich^T H D_jch (nsol(ich) x nsol(jch)) for
+ * every channel pair ich > jch whose block has an element of at least
+ * 1e-20 (the test on the block before the transformation), (nch+ip, ich)
+ * and D_ich^T hcp(:,k) for every such channel-perturber vector,
+ * (nch+ip, nch+jp) and hp(k) for every nonzero perturber element, then
+ * (0, 0).  With icase = 0 and overlaps != NULL (host, (nch+npert)^2,
+ * column-major) the largest modulus of each written record goes to
+ * overlaps(ich, jch), overlaps(nch+ip, ich), overlaps(nch+ip, nch+jp)
+ * (the input of Check_mat); other elements are left as they are.  The
+ * blocks are transformed in place on the device (dbsrg_channel_basis):
+ * hch holds the transformed blocks afterwards.
+ * dbsrg_record_acf -- the closing records (mk) and (bcf(nch,nch,0:mk))
+ * (sub1.f90:286-287), appended; bcf (host) as SUB1 collects it.
+ * A file that cannot be opened or written gives DBSRG_EIO. */
+int dbsrg_record_header(dbsrg_ctx *ctx, const char *path, int nsp, int nsq,
+                        const double *sol, const double *eval, const int *nsol);
+int dbsrg_record_matrix(dbsrg_ctx *ctx, const double *sol, const int *nsol,
+                        int icase, const char *path, double *overlaps);
+int dbsrg_record_acf(dbsrg_ctx *ctx, const char *path, const double *bcf);
 
 /* Orthogonality of the channels to bound orbitals,
  * in place on the device-resident whole matrix: DBS_ORTH

@@ -2104,3 +2104,241 @@ void orc_hf_matrix_breit(const orc_grid *g, int nbf, const double *pq, int iorb,
   free(x);
   free(xx);
 }
+
+/* ======================================================================
+ * Write-out of DBSR_MAT3: Diag_channels (diag.f90:2-81) and the block
+ * transformation of Record_matrix (record_matrix.f90:14-26).
+ *
+ * Diag_channels solves, per channel with a diagonal block, H c = E B c on
+ * the B-splines the zero conditions keep (iprm != 0) with LAPACK DSYGV
+ * (itype 1, 'V', 'L').  LAPACK is a third-party library absent from the
+ * reference tree; its published algorithm is restated here: the Cholesky
+ * factor B = L L^T of the lower triangle, the standard problem
+ * C = L^-1 A L^-T (A from its lower triangle), C y = E y by the cyclic
+ * Jacobi method (rotations that zero one off-diagonal element at a time,
+ * sweeps until the off-diagonal part vanishes to rounding), x = L^-T y
+ * (so x^T B x = 1), eigenvalues ascending.  The eigenvectors agree with
+ * LAPACK's up to sign for distinct eigenvalues; the reference fixes the
+ * sign (largest component positive), so the comparison is sign-free.
+ * Parity unpinned: the reference ships no dbsr_mat.nnn.
+ * ====================================================================== */
+
+/* lower Cholesky factor in place (a: n x n, leading dimension lda);
+ * returns 0, or the order of the first non-positive pivot */
+static int chol_lower(int n, double *a, int lda) {
+  for (int j = 0; j < n; j++) {
+    double d = a[j + (size_t)lda * j];
+    for (int k = 0; k < j; k++) d -= a[j + (size_t)lda * k] * a[j + (size_t)lda * k];
+    if (!(d > 0.0)) return j + 1;
+    d = sqrt(d);
+    a[j + (size_t)lda * j] = d;
+    for (int i = j + 1; i < n; i++) {
+      double s = a[i + (size_t)lda * j];
+      for (int k = 0; k < j; k++) s -= a[i + (size_t)lda * k] * a[j + (size_t)lda * k];
+      a[i + (size_t)lda * j] = s / d;
+    }
+  }
+  return 0;
+}
+
+/* cyclic Jacobi: symmetric c (n x n, full storage) -> eigenvalues w and
+ * eigenvectors v (columns), ascending */
+static void jacobi_eig(int n, double *c, double *w, double *v) {
+  for (int j = 0; j < n; j++)
+    for (int i = 0; i < n; i++) v[i + (size_t)n * j] = i == j ? 1.0 : 0.0;
+  for (int sweep = 0; sweep < 100; sweep++) {
+    double off = 0.0, tot = 0.0;
+    for (int j = 0; j < n; j++)
+      for (int i = 0; i < n; i++) {
+        const double x = c[i + (size_t)n * j] * c[i + (size_t)n * j];
+        tot += x;
+        if (i != j) off += x;
+      }
+    if (off <= 1e-30 * tot || off == 0.0) break;
+    for (int p = 0; p < n - 1; p++)
+      for (int q = p + 1; q < n; q++) {
+        const double apq = c[p + (size_t)n * q];
+        if (apq == 0.0) continue;
+        const double app = c[p + (size_t)n * p], aqq = c[q + (size_t)n * q];
+        /* rotation angle: t = tan(phi) of the smaller root (Rutishauser) */
+        const double th = (aqq - app) / (2.0 * apq);
+        const double t = (th >= 0.0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
+        const double cs = 1.0 / sqrt(t * t + 1.0), sn = t * cs;
+        for (int k = 0; k < n; k++) { /* columns p, q */
+          const double akp = c[k + (size_t)n * p], akq = c[k + (size_t)n * q];
+          c[k + (size_t)n * p] = cs * akp - sn * akq;
+          c[k + (size_t)n * q] = sn * akp + cs * akq;
+        }
+        for (int k = 0; k < n; k++) { /* rows p, q */
+          const double apk = c[p + (size_t)n * k], aqk = c[q + (size_t)n * k];
+          c[p + (size_t)n * k] = cs * apk - sn * aqk;
+          c[q + (size_t)n * k] = sn * apk + cs * aqk;
+        }
+        for (int k = 0; k < n; k++) {
+          const double vkp = v[k + (size_t)n * p], vkq = v[k + (size_t)n * q];
+          v[k + (size_t)n * p] = cs * vkp - sn * vkq;
+          v[k + (size_t)n * q] = sn * vkp + cs * vkq;
+        }
+      }
+  }
+  for (int i = 0; i < n; i++) w[i] = c[i + (size_t)n * i];
+  /* ascending order (selection sort of eigenpairs) */
+  for (int i = 0; i < n - 1; i++) {
+    int m = i;
+    for (int j = i + 1; j < n; j++)
+      if (w[j] < w[m]) m = j;
+    if (m == i) continue;
+    const double t = w[i];
+    w[i] = w[m];
+    w[m] = t;
+    for (int k = 0; k < n; k++) {
+      const double x = v[k + (size_t)n * i];
+      v[k + (size_t)n * i] = v[k + (size_t)n * m];
+      v[k + (size_t)n * m] = x;
+    }
+  }
+}
+
+/* Generalised symmetric-definite problem A x = E B x on the lower
+ * triangles of a and b (n x n, lda); eigenvalues w ascending, eigenvectors
+ * in the columns of x (n x n) with x^T B x = 1.  Returns 0 or the order of
+ * the failed Cholesky pivot. */
+int orc_sygv(int n, const double *a, const double *b, int lda, double *w, double *x) {
+  double *L = (double *)malloc(sizeof(double) * (size_t)n * n);
+  double *C = (double *)malloc(sizeof(double) * (size_t)n * n);
+  double *Y = (double *)malloc(sizeof(double) * (size_t)n * n);
+  for (int j = 0; j < n; j++)
+    for (int i = 0; i < n; i++) L[i + (size_t)n * j] = i >= j ? b[i + (size_t)lda * j] : 0.0;
+  int rc = chol_lower(n, L, n);
+  if (rc == 0) {
+    /* C = L^-1 A L^-T with A symmetric from its lower triangle: first
+     * Y = L^-1 A (forward substitution per column), then C = L^-1 Y^T */
+    for (int j = 0; j < n; j++)
+      for (int i = 0; i < n; i++)
+        Y[i + (size_t)n * j] = i >= j ? a[i + (size_t)lda * j] : a[j + (size_t)lda * i];
+    for (int pass = 0; pass < 2; pass++) {
+      for (int j = 0; j < n; j++)
+        for (int i = 0; i < n; i++) {
+          double s = Y[i + (size_t)n * j];
+          for (int k = 0; k < i; k++) s -= L[i + (size_t)n * k] * Y[k + (size_t)n * j];
+          Y[i + (size_t)n * j] = s / L[i + (size_t)n * i];
+        }
+      /* transpose: pass 0 leaves L^-1 A, its transpose is A L^-T */
+      for (int j = 0; j < n; j++)
+        for (int i = 0; i < n; i++) C[i + (size_t)n * j] = Y[j + (size_t)n * i];
+      memcpy(Y, C, sizeof(double) * (size_t)n * n);
+    }
+    /* symmetrise against rounding, then the standard problem */
+    for (int j = 0; j < n; j++)
+      for (int i = j + 1; i < n; i++) {
+        const double s = 0.5 * (C[i + (size_t)n * j] + C[j + (size_t)n * i]);
+        C[i + (size_t)n * j] = C[j + (size_t)n * i] = s;
+      }
+    jacobi_eig(n, C, w, Y);
+    /* x = L^-T y (back substitution per column) */
+    for (int j = 0; j < n; j++)
+      for (int i = n - 1; i >= 0; i--) {
+        double s = Y[i + (size_t)n * j];
+        for (int k = i + 1; k < n; k++) s -= L[k + (size_t)n * i] * x[k + (size_t)n * j];
+        x[i + (size_t)n * j] = s / L[i + (size_t)n * i];
+      }
+  }
+  free(L);
+  free(C);
+  free(Y);
+  return rc;
+}
+
+/* Diag_channels (diag.f90:2-81) without its printing: for every channel
+ * ich with a diagonal block k = icc(ich,ich), the kept B-splines
+ * (iprm(j,ich) != 0, j = 1..ms), the problem hch(:,:,k) c = E bdiag(:,:,ich)
+ * c on them, the solutions with emin <= E <= emax and |E| >= egap in
+ * ascending order, restored to the full net (zeros on the dropped
+ * B-splines) with their largest component positive (maxloc: the first of
+ * equal maxima), into sol(:,ksol,ich) (ms x ms x nch), their energies into
+ * eval(ksol,ich) (ms x nch) and their count into nsol(ich).  Returns 0 or
+ * -(ich) of a channel whose overlap block is not positive definite
+ * ('channel diagonalization failed'). */
+int orc_diag_channels(orc_mat *m, const double *bdiag, const int *iprm, double emin, double emax,
+                      double egap, double *sol, double *eval, int *nsol) {
+  const int ms = m->g->ms, nch = m->nch;
+  double *a = (double *)malloc(sizeof(double) * (size_t)ms * ms);
+  double *b = (double *)malloc(sizeof(double) * (size_t)ms * ms);
+  double *x = (double *)malloc(sizeof(double) * (size_t)ms * ms);
+  double *w = (double *)malloc(sizeof(double) * ms);
+  double *v = (double *)malloc(sizeof(double) * ms);
+  int rc = 0;
+  memset(sol, 0, sizeof(double) * (size_t)ms * ms * nch);
+  memset(eval, 0, sizeof(double) * (size_t)ms * nch);
+  for (int ich = 1; ich <= nch && rc == 0; ich++) {
+    nsol[ich - 1] = 0;
+    const int k = ICC(ich, ich);
+    if (k == 0) continue;
+    const int *ip = iprm + (size_t)ms * (ich - 1);
+    const double *bc = bdiag + (size_t)ms * ms * (ich - 1);
+    int jj = 0, ii = 0;
+    for (int j = 1; j <= ms; j++) {
+      if (ip[j - 1] == 0) continue;
+      jj++;
+      ii = 0;
+      for (int i = 1; i <= ms; i++) {
+        if (ip[i - 1] == 0) continue;
+        ii++;
+        a[(ii - 1) + (size_t)ms * (jj - 1)] = HCH(i, j, k);
+        b[(ii - 1) + (size_t)ms * (jj - 1)] = bc[(i - 1) + (size_t)ms * (j - 1)];
+      }
+    }
+    if (orc_sygv(ii, a, b, ms, w, x)) {
+      rc = -ich;
+      break;
+    }
+    int ksol = 0;
+    for (int i = 1; i <= ii; i++) {
+      const double e = w[i - 1];
+      if (e < emin || e > emax || fabs(e) < egap) continue;
+      ksol++;
+      int q = 0;
+      for (int j = 1; j <= ms; j++) {
+        v[j - 1] = 0.0;
+        if (ip[j - 1] == 0) continue;
+        q++;
+        v[j - 1] = x[(q - 1) + (size_t)ii * (i - 1)];
+      }
+      int pos = 0;
+      for (int j = 1; j < ms; j++)
+        if (fabs(v[j]) > fabs(v[pos])) pos = j;
+      const double sg = v[pos] < 0.0 ? -1.0 : 1.0;
+      for (int j = 0; j < ms; j++) sol[j + (size_t)ms * (ksol - 1) + (size_t)ms * ms * (ich - 1)] = sg * v[j];
+      eval[(ksol - 1) + (size_t)ms * (ich - 1)] = e;
+    }
+    nsol[ich - 1] = ksol;
+  }
+  free(a);
+  free(b);
+  free(x);
+  free(w);
+  free(v);
+  return rc;
+}
+
+/* The block transformation of Record_matrix (record_matrix.f90:14-26) for
+ * one block: c(i,j) = sum_l w(l) dj(l,j) with w(l) = sum_m di(m,i) h(m,l),
+ * i = 1..ni, j = 1..nj (h ms x ms, di/dj ms x ni/nj, c ni x nj). */
+void orc_record_block(int ms, const double *h, const double *di, int ni, const double *dj,
+                      int nj, double *c) {
+  double *w = (double *)malloc(sizeof(double) * ms);
+  for (int i = 1; i <= ni; i++) {
+    for (int l = 1; l <= ms; l++) {
+      double s = 0.0;
+      for (int mm = 1; mm <= ms; mm++)
+        s = s + di[(mm - 1) + (size_t)ms * (i - 1)] * h[(mm - 1) + (size_t)ms * (l - 1)];
+      w[l - 1] = s;
+    }
+    for (int j = 1; j <= nj; j++) {
+      double s = 0.0;
+      for (int l = 1; l <= ms; l++) s = s + w[l - 1] * dj[(l - 1) + (size_t)ms * (j - 1)];
+      c[(i - 1) + (size_t)ni * (j - 1)] = s;
+    }
+  }
+  free(w);
+}

@@ -180,6 +180,15 @@ int orc_sort_merge(int n, const int *k1, const int *k2, const int *k3,
                    const int *k4, const double *c, int *o1, int *o2,
                    int *o3, int *o4, double *oc);
 
+/* ---- write-out: Diag_channels and Record_matrix (diag.f90,
+ * record_matrix.f90); the generalised eigenproblem restates LAPACK DSYGV
+ * (Cholesky + cyclic Jacobi) ---- */
+int orc_sygv(int n, const double *a, const double *b, int lda, double *w, double *x);
+int orc_diag_channels(orc_mat *m, const double *bdiag, const int *iprm, double emin, double emax,
+                      double egap, double *sol, double *eval, int *nsol);
+void orc_record_block(int ms, const double *h, const double *di, int ni, const double *dj,
+                      int nj, double *c);
+
 #ifdef __cplusplus
 }
 #endif

@@ -94,6 +94,12 @@ def lib():
         L.orc_update_hb.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double]
         L.orc_sort_merge.restype = C.c_int
         L.orc_sort_merge.argtypes = [C.c_int, _ip, _ip, _ip, _ip, _dp, _ip, _ip, _ip, _ip, _dp]
+        L.orc_sygv.restype = C.c_int
+        L.orc_sygv.argtypes = [C.c_int, _dp, _dp, C.c_int, _dp, _dp]
+        L.orc_diag_channels.restype = C.c_int
+        L.orc_diag_channels.argtypes = [C.c_void_p, _dp, _ip, C.c_double, C.c_double, C.c_double,
+                                        _dp, _dp, _ip]
+        L.orc_record_block.argtypes = [C.c_int, _dp, _dp, C.c_int, _dp, C.c_int, _dp]
         _lib = L
     return _lib
 
@@ -334,6 +340,21 @@ class Matrix:
     def set_eps_c(self, eps_c: float):
         lib().orc_mat_set_eps_c(self._m, float(eps_c))
 
+    def diag_channels(self, bdiag, iprm, emin: float, emax: float, egap: float):
+        """Diag_channels (diag.f90:2-81) on the diagonal blocks of hch:
+        bdiag(ms, ms, nch) overlap blocks, iprm(ms, nch) kept B-splines.
+        Returns sol(ms, ms, nch), eval(ms, nch), nsol(nch)."""
+        ms, nch = self.grid.ms, self.nch
+        bd, ip = f64(bdiag), np.asfortranarray(iprm, dtype=np.int32)
+        sol = np.zeros((ms, ms, nch), order="F")
+        ev = np.zeros((ms, nch), order="F")
+        ns_ = np.zeros(nch, dtype=np.int32)
+        rc = lib().orc_diag_channels(self._m, _d(bd), _i(ip), float(emin), float(emax),
+                                     float(egap), _d(sol), _d(ev), _i(ns_))
+        if rc != 0:
+            raise RuntimeError(f"channel diagonalization failed (channel {-rc})")
+        return sol, ev, ns_
+
     def dbs_orth(self, iort):
         """DBS_ORTH (dbs_orth.f90:28-84) on hch in place; iort(nbf, nch)."""
         io = np.asfortranarray(iort, dtype=np.int32)
@@ -347,3 +368,25 @@ class Matrix:
                                   _i(k3), _i(k4), _d(cdata))
         if rc != 0:
             raise RuntimeError(f"orc_gen_matrix failed: {rc}")
+
+
+def sygv(a, b):
+    """A x = E B x from the lower triangles (restated DSYGV itype 1):
+    eigenvalues ascending, eigenvectors with x^T B x = 1."""
+    a, b = f64(a), f64(b)
+    n = a.shape[0]
+    w = np.zeros(n)
+    x = np.zeros((n, n), order="F")
+    if lib().orc_sygv(n, _d(a), _d(b), n, _d(w), _d(x)) != 0:
+        raise RuntimeError("overlap matrix not positive definite")
+    return w, x
+
+
+def record_block(h, di, dj):
+    """Record_matrix's c = D_i^T H D_j (record_matrix.f90:21-24)."""
+    h, di, dj = f64(h), f64(di), f64(dj)
+    ms, ni, nj = h.shape[0], di.shape[1], dj.shape[1]
+    c = np.zeros((ni, nj), order="F")
+    if ni and nj:
+        lib().orc_record_block(ms, _d(h), _d(di), ni, _d(dj), nj, _d(c))
+    return c
