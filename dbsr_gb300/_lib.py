@@ -64,6 +64,10 @@ SIGNATURES = [
     ("dbsrg_record_acf", C.c_int, [_vp, C.c_char_p, _vp]),
     ("dbsrg_orth_channels", C.c_int, [_vp, _vp]),
     ("dbsrg_hf_matrix", C.c_int, [_vp, C.c_int, C.c_int, _vp, _vp, C.c_double, _vp, _vp]),
+    ("dbsrg_mchf_matrix", C.c_int, [_vp, C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, C.c_int, _vp,
+                                    _vp, _vp, _vp, _vp, _vp, _vp, C.c_int, C.c_int, C.c_double,
+                                    _vp, _vp, _vp, _vp, _vp]),
+    ("dbsrg_mchf_core", C.c_int, [_vp, C.c_int, C.c_int, _vp, _vp, _vp, _vp, C.c_int, _vp, _vp]),
     ("dbsrg_lists_create", C.c_int, [C.POINTER(_vp), C.c_int, C.c_int, _vp, _vp, _vp, C.c_int,
                                      C.c_double, C.c_int]),
     ("dbsrg_lists_destroy", C.c_int, [_vp]),

@@ -450,6 +450,48 @@ class Assembler:
         check(self._h, rc, "hf_matrix")
         return out
 
+    def mchf_matrix(self, iorb: int, kmax: int, lint, rint, dhl, irhs=1, newton=0, eps_c=1e-10):
+        """dbsrg_mchf_matrix (DBSR_MCHF/mchf_matrix.f90:2-251) of orbital iorb
+        outside the core: lint = (i1, i2, c), rint = (k, i1, i2, i3, i4, c)
+        with the expansion weights applied; dhl (ms, ms).  Needs a
+        one-channel matrix.  Returns (hfm, rhs, hx, e, qsum)."""
+        li = [np.ascontiguousarray(x, dtype=np.int32) for x in lint[:2]]
+        lc = np.ascontiguousarray(lint[2], dtype=np.float64)
+        ri = [np.ascontiguousarray(x, dtype=np.int32) for x in rint[:5]]
+        rc = np.ascontiguousarray(rint[5], dtype=np.float64)
+        D = np.asfortranarray(dhl, dtype=np.float64)
+        ms = self.ms
+        hfm = np.zeros((ms, ms), order="F")
+        hx = np.zeros((ms, ms), order="F")
+        rhs = np.zeros(ms)
+        e = np.zeros(1)
+        q = np.zeros(1)
+        ptr = lambda a: C.c_void_p(a.ctypes.data)  # noqa: E731
+        rcode = self._L.dbsrg_mchf_matrix(
+            self._h, int(iorb), int(kmax), lc.size, ptr(li[0]), ptr(li[1]), ptr(lc), rc.size,
+            *[ptr(x) for x in ri], ptr(rc), ptr(D), int(irhs), int(newton), float(eps_c),
+            ptr(hfm), ptr(rhs), ptr(hx), ptr(e), ptr(q))
+        check(self._h, rcode, "mchf_matrix")
+        return hfm, rhs, hx, float(e[0]), float(q[0])
+
+    def mchf_core(self, iorb: int, a, b, qsum, hd, newton=0):
+        """dbsrg_mchf_core (core_matrix, mchf_matrix.f90:255-346): a, b
+        (nbf, kmax+1), qsum (nbf), hd (ms, ms).  Returns (hfm, hx)."""
+        A = np.asfortranarray(a, dtype=np.float64)
+        B = np.asfortranarray(b, dtype=np.float64)
+        if A.shape != B.shape or A.shape[0] != self.nbf:
+            raise ValueError("a and b must be (nbf, kmax+1)")
+        Q = np.ascontiguousarray(qsum, dtype=np.float64)
+        H = np.asfortranarray(hd, dtype=np.float64)
+        ms = self.ms
+        hfm = np.zeros((ms, ms), order="F")
+        hx = np.zeros((ms, ms), order="F")
+        ptr = lambda x: C.c_void_p(x.ctypes.data)  # noqa: E731
+        rc = self._L.dbsrg_mchf_core(self._h, int(iorb), A.shape[1] - 1, ptr(A), ptr(B), ptr(Q),
+                                     ptr(H), int(newton), ptr(hfm), ptr(hx))
+        check(self._h, rc, "mchf_core")
+        return hfm, hx
+
     def set_wait_limit(self, ns: int):
         """Limit of the tensor-core kernel's pipeline waits (ns)."""
         check(self._h, self._L.dbsrg_set_wait_limit(self._h, int(ns)), "set_wait_limit")

@@ -1062,6 +1062,16 @@ int band_contract(dbsrg_ctx *c, int kb, int icase, const double *rkb, int nsg, c
   return DBSRG_OK;
 }
 
+// convol case 3 of nsg full ('x') densities X with one full R^k table
+// (k_exchange, 's','s' storage); for these tables case 4 adds the same
+// products (dbsr_lib_dbs.f90:2344-2470)
+int exchange_contract(dbsrg_ctx *c, const double *rkb, int nsg, const double *X, double *Y) {
+  const int ns = c->g.ns, ks = c->g.ks;
+  dim3 gx((unsigned)(((size_t)ns * ns + 255) / 256), (unsigned)((nsg + XNB - 1) / XNB));
+  DBSRG_RUN(c, "k_exchange", k_exchange<<<gx, 256, 0, c->stream>>>(ns, ks, 0, nsg, rkb, X, Y));
+  return DBSRG_OK;
+}
+
 namespace {
 
 // The cached inputs of a planned list, built on the table stream of its k;

@@ -335,6 +335,8 @@ int update_hx(dbsrg_ctx *c, int ich, int jch, const double *d, double cc);
 // table rkb (kb = ks for R, 2ks-1 for S) into Y[s][ns*kb], on the context stream
 int band_contract(dbsrg_ctx *c, int kb, int icase, const double *rkb, int nsg, const double *X,
                   double *Y);
+// convol case 3 (= 4) of nsg full densities with one full R^k table
+int exchange_contract(dbsrg_ctx *c, const double *rkb, int nsg, const double *X, double *Y);
 // Every list set up once, then executed window by window over the blocks
 // (windows of nwin blocks alternating between nslot slots of the matrix
 // allocation): before(w, slot) prepares a slot (on the contraction stream),

@@ -364,6 +364,34 @@ int dbsrg_hf_breit_list(dbsrg_ctx *ctx, int nrk, const int *kr1,
                         const int *kr2, const int *kr3, const int *kr4,
                         const double *crk);
 
+/* DBSR_MCHF's SCF potential matrices on a one-channel matrix (as for
+ * dbsrg_hf_matrix), in the precision form selected.
+ * dbsrg_mchf_matrix -- mchf_matrix (DBSR_MCHF/mchf_matrix.f90:2-251) of
+ * orbital iorb outside the core: the one-electron entries (li1, li2, lc;
+ * nl of them) and the R^k entries (rk, ri1..ri4, rcoef; nr) with the
+ * expansion weights already applied (WW(ic,jc) L_coef and WW(ic,jc)
+ * Rk_coef, mchf_matrix.f90:65, 95), k ascending; dhl (ms x ms) the
+ * one-electron matrix of Get_hd_core; irhs, newton and eps_c as in the
+ * reference.  Out: hfm (ms x ms), rhs (ms), hx (ms x ms, written when
+ * newton != 0), e = e(i) and qsum = qsum(i) (host scalars).  The
+ * Add_id4_data classification (mchf_matrix.f90:98-135) is applied with
+ * entries appended in order; the Newton term convolves the last -3 density
+ * of each k unweighted, as the reference's Convol(ns,ks,xx,x,4,..) does.
+ * dbsrg_mchf_core -- core_matrix (mchf_matrix.f90:255-346) of a core
+ * orbital: a, b (nbf x (kmax+1), host) the angular coefficients a(i,j,k),
+ * b(i,j,k), qsum (nbf, host), hd (ms x ms) of Get_hd; out hfm and, when
+ * newton != 0, hx.
+ * Lists, e and qsum are host arrays; dhl/hd and the outputs host or device. */
+int dbsrg_mchf_matrix(dbsrg_ctx *ctx, int iorb, int kmax, int nl, const int *li1,
+                      const int *li2, const double *lc, int nr, const int *rk,
+                      const int *ri1, const int *ri2, const int *ri3, const int *ri4,
+                      const double *rcoef, const double *dhl, int irhs, int newton,
+                      double eps_c, double *hfm, double *rhs, double *hx, double *e,
+                      double *qsum);
+int dbsrg_mchf_core(dbsrg_ctx *ctx, int iorb, int kmax, const double *a, const double *b,
+                    const double *qsum, const double *hd, int newton, double *hfm,
+                    double *hx);
+
 /* List producer between the decoded angular bank and Gen_matrix (the part
  * after the bank's records are read; the records, state tables and overlap
  * factors of State_res / Det_fact come from the caller).  Replaces Add_integral (add_integral.f90:2-57: parity filter,

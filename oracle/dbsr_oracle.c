@@ -2342,3 +2342,326 @@ void orc_record_block(int ms, const double *h, const double *di, int ni, const d
   }
   free(w);
 }
+
+/* ======================================================================
+ * DBSR_MCHF's SCF potential matrices (mchf_matrix.f90).
+ *
+ * orc_mchf_matrix restates mchf_matrix (mchf_matrix.f90:2-251) for an
+ * orbital outside the core.  The caller passes the expansion-weighted
+ * coefficients that mchf_matrix forms with WW (mchf_matrix.f90:65, 95):
+ * L entries (li1, li2, lc = WW L_coef) and R^k entries (rk, ri1..ri4,
+ * rc = WW Rk_coef) in the order of the integral lists (k ascending), the
+ * one-electron matrix dhl of Get_hd_core (ms x ms), and the flags irhs and
+ * newton.  Add_id4_data (module id4_data, absent from the reference tree)
+ * is restated as appending (k, id2, id3, id4, C) to the list of its k.
+ * The loop over id4 entries of the newton term convolves the density left
+ * in x by the last entry it visits, unweighted (mchf_matrix.f90:211-216:
+ * Convol(ns,ks,xx,x,4,...) writes its result over the weighted sum xx), and
+ * this restatement does the same.  Outputs: hfm, rhs, hx (ms x ms, ms,
+ * ms x ms), the energy e(i) and qsum(i).
+ *
+ * orc_mchf_core restates core_matrix (mchf_matrix.f90:255-346) with the
+ * angular coefficients a(i,j,k), b(i,j,k) given as arrays (nbf, kmax+1),
+ * qsum(nbf) and the one-electron matrix hd of Get_hd (ms x ms).
+ * Parity unpinned (the reference ships no potential matrices).
+ * ====================================================================== */
+
+typedef struct {
+  int id2, id3, id4;
+  double c;
+} id4_entry;
+
+static void id4_add(id4_entry **v, int *n, int *cap, int id2, int id3, int id4, double c) {
+  if (*n == *cap) {
+    *cap = *cap ? 2 * *cap : 64;
+    *v = (id4_entry *)realloc(*v, sizeof(id4_entry) * (size_t)*cap);
+  }
+  (*v)[*n].id2 = id2;
+  (*v)[*n].id3 = id3;
+  (*v)[*n].id4 = id4;
+  (*v)[*n].c = c;
+  (*n)++;
+}
+
+void orc_mchf_matrix(const orc_grid *g, int nbf, const double *pq, int iorb, int kmax, int nl,
+                     const int *li1, const int *li2, const double *lc, int nr, const int *rk,
+                     const int *ri1, const int *ri2, const int *ri3, const int *ri4,
+                     const double *rc, const double *dhl, int irhs, int newton, double eps_c,
+                     double *hfm, double *rhs, double *hx, double *e_out, double *qsum_out) {
+  const int ns = g->ns, ks = g->ks, ms = g->ms, i = iorb;
+  static const int ttype[2][2] = {{0, 2}, {3, 1}};
+  const double qsum_min = 1e-8; /* MOD_dbsr_mchf.f90:55 */
+  double *rkb = (double *)malloc(sizeof(double) * (size_t)ns * ns * ks * ks);
+  double *d = (double *)malloc(sizeof(double) * (size_t)ns * ns);
+  double *dd = (double *)malloc(sizeof(double) * (size_t)ns * ns);
+  double *x = (double *)malloc(sizeof(double) * (size_t)ns * ns);
+  double *xx = (double *)malloc(sizeof(double) * (size_t)ns * ns);
+  double *aa = (double *)malloc(sizeof(double) * (size_t)ns * ks * nbf);
+  int *iaa = (int *)malloc(sizeof(int) * nbf);
+  double *v = (double *)malloc(sizeof(double) * ms);
+  double *vv = (double *)malloc(sizeof(double) * ms);
+  double *v1 = (double *)malloc(sizeof(double) * ns);
+  double *CI = (double *)calloc(nbf, sizeof(double));
+  id4_entry *ent = NULL;
+  int cap = 0;
+#define GETPV(io, vec)                                                     \
+  do {                                                                     \
+    const double *pp_ = pq + (size_t)2 * ns * ((io) - 1);                  \
+    for (int q_ = 0; q_ < ns; q_++) {                                      \
+      (vec)[q_] = pp_[q_];                                                 \
+      (vec)[ns + q_] = pp_[ns + q_];                                       \
+    }                                                                      \
+  } while (0)
+  for (size_t q = 0; q < (size_t)ms * ms; q++) hfm[q] = hx[q] = 0.0;
+  for (int q = 0; q < ms; q++) rhs[q] = 0.0;
+  /* one-electron integrals (:59-84) */
+  double S = 0.0;
+  for (int m = 0; m < nl; m++) {
+    const int i1 = li1[m], i2 = li2[m];
+    const double C = lc[m];
+    if (i1 == i && i2 == i)
+      S = S + C;
+    else if (i1 == i && i2 != i)
+      CI[i2 - 1] = CI[i2 - 1] + C;
+    else if (i1 != i && i2 == i)
+      CI[i1 - 1] = CI[i1 - 1] + C;
+  }
+  if (fabs(S) < qsum_min) S = qsum_min;
+  *qsum_out = S;
+  double sci = 0.0;
+  for (int io = 0; io < nbf; io++) sci += fabs(CI[io]);
+  if (sci != 0.0) {
+    for (int q = 0; q < ms; q++) vv[q] = 0.0;
+    for (int io = 1; io <= nbf; io++) {
+      if (CI[io - 1] == 0.0) continue;
+      GETPV(io, v);
+      for (int q = 0; q < ms; q++) vv[q] = vv[q] + v[q] * CI[io - 1] / S / 2.0;
+    }
+    for (int r = 1; r <= ms; r++) { /* rhs + matmul(dhl, vv) */
+      double s = 0.0;
+      for (int q = 1; q <= ms; q++) s = s + A2(dhl, r, q, ms) * vv[q - 1];
+      rhs[r - 1] = rhs[r - 1] + s;
+    }
+  }
+  for (int k = 0; k <= kmax; k++) {
+    int nid = 0;
+    for (int m = 0; m < nr; m++) {
+      if (rk[m] != k) continue;
+      const int i1 = ri1[m], i2 = ri2[m], i3 = ri3[m], i4 = ri4[m];
+      const double C = rc[m] / S;
+      if (fabs(C) < eps_c) continue;
+      const int ii = (i == i1) * 1000 + (i == i2) * 100 + (i == i3) * 10 + (i == i4);
+      switch (ii) {
+        case 1111: id4_add(&ent, &nid, &cap, -1, i1, i3, 2 * C);
+                   id4_add(&ent, &nid, &cap, -3, i1, i3, 4 * C); break;
+        case 1010: id4_add(&ent, &nid, &cap, -1, i2, i4, C); break;
+        case 101:  id4_add(&ent, &nid, &cap, -1, i1, i3, C); break;
+        case 1001: id4_add(&ent, &nid, &cap, -2, i2, i3, C); break;
+        case 1100: id4_add(&ent, &nid, &cap, -2, i3, i4, C); break;
+        case 110:  id4_add(&ent, &nid, &cap, -2, i1, i4, C); break;
+        case 11:   id4_add(&ent, &nid, &cap, -2, i1, i2, C); break;
+        case 111:  id4_add(&ent, &nid, &cap, -1, i1, i3, C);
+                   id4_add(&ent, &nid, &cap, -2, i1, i3, C / 2);
+                   id4_add(&ent, &nid, &cap, -3, i1, i3, 3 * C / 2); break;
+        case 1011: id4_add(&ent, &nid, &cap, -1, i2, i4, C);
+                   id4_add(&ent, &nid, &cap, -2, i2, i4, C / 2);
+                   id4_add(&ent, &nid, &cap, -3, i2, i4, 3 * C / 2); break;
+        case 1101: id4_add(&ent, &nid, &cap, -1, i1, i3, C);
+                   id4_add(&ent, &nid, &cap, -2, i1, i3, C / 2);
+                   id4_add(&ent, &nid, &cap, -3, i1, i3, 3 * C / 2); break;
+        case 1110: id4_add(&ent, &nid, &cap, -1, i2, i4, C);
+                   id4_add(&ent, &nid, &cap, -2, i2, i4, C / 2);
+                   id4_add(&ent, &nid, &cap, -3, i2, i4, 3 * C / 2); break;
+        case 1000: id4_add(&ent, &nid, &cap, i3, i2, i4, C / 2); break;
+        case 100:  id4_add(&ent, &nid, &cap, i4, i1, i3, C / 2); break;
+        case 10:   id4_add(&ent, &nid, &cap, i1, i2, i4, C / 2); break;
+        case 1:    id4_add(&ent, &nid, &cap, i2, i1, i3, C / 2); break;
+        default: break;
+      }
+    }
+    if (nid == 0) continue;
+    for (int ii = 1; ii <= 2; ii++)
+      for (int jj = 1; jj <= 2; jj++) {
+        orc_mrk(g, ttype[ii - 1][jj - 1], k, rkb);
+#define PCOMP(io, comp) (pq + (size_t)2 * ns * ((io) - 1) + (size_t)ns * ((comp) - 1))
+        /* direct (:155-169) */
+        int met = 0;
+        memset(dd, 0, sizeof(double) * (size_t)ns * ks);
+        for (int j = 0; j < nid; j++) {
+          if (ent[j].id2 != -1 || ent[j].c == 0.0) continue;
+          orc_density(ns, ks, d, PCOMP(ent[j].id3, jj), PCOMP(ent[j].id4, jj), 's');
+          for (size_t q = 0; q < (size_t)ns * ks; q++) dd[q] = dd[q] + ent[j].c * d[q];
+          met = 1;
+        }
+        if (met) {
+          orc_convol(ns, ks, ks, rkb, d, dd, 1, 's', 's');
+          hf_update(ns, ks, ms, hfm, ii, ii, d, 's');
+        }
+        /* exchange (:171-185) */
+        met = 0;
+        memset(xx, 0, sizeof(double) * (size_t)ns * ns);
+        for (int j = 0; j < nid; j++) {
+          if (ent[j].id2 != -2 || ent[j].c == 0.0) continue;
+          orc_density(ns, ks, x, PCOMP(ent[j].id3, ii), PCOMP(ent[j].id4, jj), 'x');
+          for (size_t q = 0; q < (size_t)ns * ns; q++) xx[q] = xx[q] + ent[j].c * x[q];
+          met = 1;
+        }
+        if (met) {
+          orc_convol(ns, ks, ks, rkb, x, xx, 4, 's', 's');
+          hf_update(ns, ks, ms, hfm, ii, jj, x, 'x');
+        }
+        /* rhs (:187-205) */
+        memset(aa, 0, sizeof(double) * (size_t)ns * ks * nbf);
+        memset(iaa, 0, sizeof(int) * nbf);
+        for (int j = 0; j < nid; j++) {
+          if (ent[j].id2 <= 0) continue;
+          orc_density(ns, ks, d, PCOMP(ent[j].id3, jj), PCOMP(ent[j].id4, jj), 's');
+          double *a_ = aa + (size_t)ns * ks * (ent[j].id2 - 1);
+          for (size_t q = 0; q < (size_t)ns * ks; q++) a_[q] = a_[q] + d[q] * ent[j].c;
+          iaa[ent[j].id2 - 1]++;
+        }
+        for (int j = 1; j <= nbf; j++) {
+          if (iaa[j - 1] == 0) continue;
+          memcpy(d, aa + (size_t)ns * ks * (j - 1), sizeof(double) * (size_t)ns * ks);
+          orc_convol(ns, ks, ks, rkb, dd, d, 1, 's', 's');
+          /* Full_mat_sym 's' (dbsr_lib_zcom.f90:1263-1268) into xx */
+          memset(xx, 0, sizeof(double) * (size_t)ns * ns);
+          for (int jp = 1; jp <= ks; jp++)
+            for (int r = 1; r <= ns - jp + 1; r++) {
+              const int cidx = r + jp - 1;
+              A2(xx, r, cidx, ns) = A2(dd, r, jp, ns);
+              A2(xx, cidx, r, ns) = A2(dd, r, jp, ns);
+            }
+          const double *pj = PCOMP(j, ii);
+          for (int r = 1; r <= ns; r++) {
+            double s = 0.0;
+            for (int q = 1; q <= ns; q++) s = s + A2(xx, r, q, ns) * pj[q - 1];
+            v1[r - 1] = s;
+          }
+          for (int r = 0; r < ns; r++) rhs[(ii - 1) * ns + r] = rhs[(ii - 1) * ns + r] + v1[r];
+        }
+        /* hx for the Newton-Raphson method (:209-221) */
+        if (newton != 0) {
+          met = 0;
+          memset(xx, 0, sizeof(double) * (size_t)ns * ns);
+          for (int j = 0; j < nid; j++) {
+            if (ent[j].id2 != -3 || ent[j].c == 0.0) continue;
+            orc_density(ns, ks, x, PCOMP(ent[j].id3, jj), PCOMP(ent[j].id4, jj), 'x');
+            for (size_t q = 0; q < (size_t)ns * ns; q++) xx[q] = xx[q] + ent[j].c * x[q];
+            met = 1;
+          }
+          if (met) {
+            orc_convol(ns, ks, ks, rkb, xx, x, 4, 's', 's');
+            hf_update(ns, ks, ms, hx, ii, jj, xx, 'x');
+          }
+        }
+#undef PCOMP
+      }
+  }
+  /* rhs into hfm (:223-241) */
+  double srhs = 0.0;
+  for (int q = 0; q < ms; q++) srhs += fabs(rhs[q]);
+  if (srhs < 1e-8) {
+    for (int q = 0; q < ms; q++) rhs[q] = 0.0;
+    srhs = 0.0;
+  }
+  if (irhs > 0 && srhs > 0.0) {
+    GETPV(i, v);
+    double SS = 0.0;
+    for (int q = 0; q < ms; q++) SS += rhs[q] * v[q];
+    SS = -SS;
+    for (size_t q = 0; q < (size_t)ms * ms; q++) hfm[q] = hfm[q] + SS * g->fppqq[q];
+    for (int r = 1; r <= ms; r++) {
+      double s = 0.0;
+      for (int q = 1; q <= ms; q++) s = s + A2(g->fppqq, r, q, ms) * v[q - 1];
+      vv[r - 1] = s;
+    }
+    for (int a_ = 1; a_ <= ms; a_++)
+      for (int b_ = 1; b_ <= ms; b_++)
+        A2(hfm, a_, b_, ms) = A2(hfm, a_, b_, ms) + rhs[a_ - 1] * vv[b_ - 1] + rhs[b_ - 1] * vv[a_ - 1];
+    for (int q = 0; q < ms; q++) rhs[q] = 0.0;
+  }
+  /* final matrix and energy (:243-249) */
+  for (size_t q = 0; q < (size_t)ms * ms; q++) hfm[q] = dhl[q] + hfm[q];
+  for (int q = 0; q < ms; q++) rhs[q] = -rhs[q];
+  GETPV(i, v);
+  double e = 0.0;
+  for (int r = 1; r <= ms; r++) {
+    double s = 0.0;
+    for (int q = 1; q <= ms; q++) s = s + A2(hfm, r, q, ms) * v[q - 1];
+    e += v[r - 1] * (s - rhs[r - 1]);
+  }
+  *e_out = e;
+#undef GETPV
+  free(ent);
+  free(rkb); free(d); free(dd); free(x); free(xx); free(aa); free(iaa);
+  free(v); free(vv); free(v1); free(CI);
+}
+
+void orc_mchf_core(const orc_grid *g, int nbf, const double *pq, int iorb, int kmax,
+                   const double *a, const double *b, const double *qsum, const double *hd,
+                   int newton, double *hfm, double *hx) {
+  const int ns = g->ns, ks = g->ks, ms = g->ms, i = iorb;
+  static const int ttype[2][2] = {{0, 2}, {3, 1}};
+  double *rkb = (double *)malloc(sizeof(double) * (size_t)ns * ns * ks * ks);
+  double *d = (double *)malloc(sizeof(double) * (size_t)ns * ns);
+  double *dd = (double *)malloc(sizeof(double) * (size_t)ns * ns);
+  double *x = (double *)malloc(sizeof(double) * (size_t)ns * ns);
+  double *xx = (double *)malloc(sizeof(double) * (size_t)ns * ns);
+  const double qi = qsum[i - 1];
+  for (size_t q = 0; q < (size_t)ms * ms; q++) {
+    hfm[q] = qi * hd[q];
+    hx[q] = 0.0;
+  }
+#define PCOMP(io, comp) (pq + (size_t)2 * ns * ((io) - 1) + (size_t)ns * ((comp) - 1))
+  for (int ii = 1; ii <= 2; ii++)
+    for (int jj = 1; jj <= 2; jj++)
+      for (int k = 0; k <= kmax; k++) {
+        orc_mrk(g, ttype[ii - 1][jj - 1], k, rkb);
+        int met = 0;
+        memset(dd, 0, sizeof(double) * (size_t)ns * ks);
+        for (int j = 1; j <= nbf; j++) {
+          double c = a[(j - 1) + (size_t)nbf * k];
+          if (i != j) c = c * qi * qsum[j - 1];
+          if (i == j) c = c * qi * (qi - 1);
+          if (c == 0.0) continue;
+          orc_density(ns, ks, d, PCOMP(j, jj), PCOMP(j, jj), 's');
+          for (size_t q = 0; q < (size_t)ns * ks; q++) dd[q] = dd[q] + c * d[q];
+          met = 1;
+        }
+        if (met) {
+          orc_convol(ns, ks, ks, rkb, d, dd, 1, 's', 's');
+          hf_update(ns, ks, ms, hfm, ii, ii, d, 's');
+        }
+        met = 0;
+        memset(xx, 0, sizeof(double) * (size_t)ns * ns);
+        for (int j = 1; j <= nbf; j++) {
+          double c = b[(j - 1) + (size_t)nbf * k];
+          if (i != j) c = c * qi * qsum[j - 1];
+          if (i == j) c = c * qi * (qi - 1);
+          if (c == 0.0) continue;
+          orc_density(ns, ks, x, PCOMP(j, ii), PCOMP(j, jj), 'x');
+          for (size_t q = 0; q < (size_t)ns * ns; q++) xx[q] = xx[q] + x[q] * c;
+          met = 1;
+        }
+        if (met) {
+          orc_convol(ns, ks, ks, rkb, x, xx, 4, 's', 's');
+          hf_update(ns, ks, ms, hfm, ii, jj, x, 'x');
+        }
+        if (newton != 0) {
+          double c = 2.0 * a[(i - 1) + (size_t)nbf * k];
+          if (c == 0.0) continue;
+          c = c * qi * (qi - 1);
+          orc_density(ns, ks, x, PCOMP(i, ii), PCOMP(i, jj), 'x');
+          for (size_t q = 0; q < (size_t)ns * ns; q++) xx[q] = c * x[q];
+          orc_convol(ns, ks, ks, rkb, x, xx, 4, 's', 's');
+          hf_update(ns, ks, ms, hx, ii, jj, x, 'x');
+        }
+      }
+#undef PCOMP
+  for (size_t q = 0; q < (size_t)ms * ms; q++) {
+    hfm[q] = hfm[q] / qi;
+    hx[q] = hx[q] / qi;
+  }
+  free(rkb); free(d); free(dd); free(x); free(xx);
+}

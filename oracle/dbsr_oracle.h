@@ -189,6 +189,16 @@ int orc_diag_channels(orc_mat *m, const double *bdiag, const int *iprm, double e
 void orc_record_block(int ms, const double *h, const double *di, int ni, const double *dj,
                       int nj, double *c);
 
+/* ---- DBSR_MCHF potentials (mchf_matrix.f90): mchf_matrix and core_matrix ---- */
+void orc_mchf_matrix(const orc_grid *g, int nbf, const double *pq, int iorb, int kmax, int nl,
+                     const int *li1, const int *li2, const double *lc, int nr, const int *rk,
+                     const int *ri1, const int *ri2, const int *ri3, const int *ri4,
+                     const double *rc, const double *dhl, int irhs, int newton, double eps_c,
+                     double *hfm, double *rhs, double *hx, double *e_out, double *qsum_out);
+void orc_mchf_core(const orc_grid *g, int nbf, const double *pq, int iorb, int kmax,
+                   const double *a, const double *b, const double *qsum, const double *hd,
+                   int newton, double *hfm, double *hx);
+
 #ifdef __cplusplus
 }
 #endif

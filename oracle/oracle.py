@@ -100,6 +100,11 @@ def lib():
         L.orc_diag_channels.argtypes = [C.c_void_p, _dp, _ip, C.c_double, C.c_double, C.c_double,
                                         _dp, _dp, _ip]
         L.orc_record_block.argtypes = [C.c_int, _dp, _dp, C.c_int, _dp, C.c_int, _dp]
+        L.orc_mchf_matrix.argtypes = [C.POINTER(_Grid), C.c_int, _dp, C.c_int, C.c_int, C.c_int,
+                                      _ip, _ip, _dp, C.c_int, _ip, _ip, _ip, _ip, _ip, _dp, _dp,
+                                      C.c_int, C.c_int, C.c_double, _dp, _dp, _dp, _dp, _dp]
+        L.orc_mchf_core.argtypes = [C.POINTER(_Grid), C.c_int, _dp, C.c_int, C.c_int, _dp, _dp,
+                                    _dp, _dp, C.c_int, _dp, _dp]
         _lib = L
     return _lib
 
@@ -226,6 +231,43 @@ class Grid:
         lib().orc_hf_matrix(self._p, nbf, _d(pq), iorb, kmax, _d(a), _d(b), float(qsum),
                             _d(f64(dhl)) if dhl is not None else None, _d(out))
         return out
+
+    def mchf_matrix(self, pq, iorb: int, kmax: int, lint, rint, dhl, irhs=1, newton=0,
+                    eps_c=1e-10):
+        """mchf_matrix (DBSR_MCHF/mchf_matrix.f90:2-251) of orbital iorb outside
+        the core.  lint = (i1, i2, c) one-electron entries, rint = (k, i1, i2,
+        i3, i4, c) R^k entries, both with the expansion weights applied.
+        Returns (hfm, rhs, hx, e, qsum)."""
+        pq = f64(pq)
+        nbf = pq.size // (2 * self.ns)
+        li1, li2 = i32(lint[0]), i32(lint[1])
+        lc = f64(lint[2])
+        rk, r1, r2, r3, r4 = (i32(x) for x in rint[:5])
+        rc = f64(rint[5])
+        ms = self.ms
+        hfm = np.zeros((ms, ms), order="F")
+        hx = np.zeros((ms, ms), order="F")
+        rhs = np.zeros(ms)
+        e = np.zeros(1)
+        q = np.zeros(1)
+        lib().orc_mchf_matrix(self._p, nbf, _d(pq), iorb, kmax, li1.size, _i(li1), _i(li2),
+                              _d(lc), rk.size, _i(rk), _i(r1), _i(r2), _i(r3), _i(r4), _d(rc),
+                              _d(f64(dhl)), int(irhs), int(newton), float(eps_c), _d(hfm),
+                              _d(rhs), _d(hx), _d(e), _d(q))
+        return hfm, rhs, hx, float(e[0]), float(q[0])
+
+    def mchf_core(self, pq, iorb: int, a, b, qsum, hd, newton=0):
+        """core_matrix (DBSR_MCHF/mchf_matrix.f90:255-346); a, b: (nbf,
+        kmax+1), qsum(nbf).  Returns (hfm, hx)."""
+        pq = f64(pq)
+        nbf = pq.size // (2 * self.ns)
+        a, b = f64(a), f64(b)
+        ms = self.ms
+        hfm = np.zeros((ms, ms), order="F")
+        hx = np.zeros((ms, ms), order="F")
+        lib().orc_mchf_core(self._p, nbf, _d(pq), iorb, a.shape[1] - 1, _d(a), _d(b),
+                            _d(f64(qsum)), _d(f64(hd)), int(newton), _d(hfm), _d(hx))
+        return hfm, hx
 
     def hf_matrix_breit(self, pq, iorb: int, kmax: int, kr1, kr2, kr3, kr4, crk,
                         hfm=None) -> np.ndarray:
