@@ -7,7 +7,8 @@
 //    with Edmin <= E <= Edmax and |E| >= Egap, restored to the full B-spline
 //    net and signed so that their largest component is positive;
 //  * Record_matrix (record_matrix.f90:14-26): every off-diagonal block
-//    replaced by c = D_ich^T H D_jch (two DGEMMs through cuBLAS).
+//    replaced by c = D_ich^T H D_jch: in the split form as split-BF16
+//    tcgen05 products (sgemm.cu), otherwise two DGEMMs through cuBLAS.
 // cuSOLVER and cuBLAS are loaded on first use (dlopen), so the assembly
 // library itself does not depend on them.
 #include <cublas_v2.h>
@@ -300,6 +301,15 @@ extern "C" int dbsrg_channel_basis(dbsrg_ctx *c, const double *sol, const int *n
     cudaGetLastError();
     if (dD) cudaFree(dD);
     return set_err(c, DBSRG_ENOMEM, "channel_basis: allocation failed");
+  }
+  if (c->precision == DBSRG_SPLIT_BF16) {  // split-BF16 tensor-core products (sgemm.cu)
+    rc = split_channel_basis(c, D, nsol);
+    cudaStreamSynchronize(st);
+    cudaFree(dWt);
+    if (dD) cudaFree(dD);
+    if (rc) return rc;
+    if (out) return copy_out(c, out, c->hch, blk * c->iicc * 8);
+    return DBSRG_OK;
   }
   const double one = 1.0, zero = 0.0;
   int bad = 0;

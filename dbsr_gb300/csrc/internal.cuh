@@ -337,6 +337,9 @@ int band_contract(dbsrg_ctx *c, int kb, int icase, const double *rkb, int nsg, c
                   double *Y);
 // convol case 3 (= 4) of nsg full densities with one full R^k table
 int exchange_contract(dbsrg_ctx *c, const double *rkb, int nsg, const double *X, double *Y);
+// Record_matrix's c = D_ich^T H D_jch for all blocks ich > jch as split-BF16
+// tensor-core products (sgemm.cu); D on the device
+int split_channel_basis(dbsrg_ctx *c, const double *D, const int *nsol);
 // Every list set up once, then executed window by window over the blocks
 // (windows of nwin blocks alternating between nslot slots of the matrix
 // allocation): before(w, slot) prepares a slot (on the contraction stream),

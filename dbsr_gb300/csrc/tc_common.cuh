@@ -111,7 +111,7 @@ __device__ __forceinline__ int f2i_exact(float f) {
 
 // I * 2^sh outside the normal range of FP64 (never produced by the scales
 // here); kept out of line so the common path stays short
-__device__ __noinline__ double i64_scale_slow(long long I, int sh) {
+static __device__ __noinline__ double i64_scale_slow(long long I, int sh) {
   return ldexp(__ll2double_rn(I), sh);
 }
 

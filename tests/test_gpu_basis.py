@@ -9,7 +9,8 @@ of Record_matrix and SUB1 (record_matrix.f90:2-60, sub1.f90:164-168,
 Tolerances: eigenvalues 1e-10 of the largest modulus; eigenvectors 1e-8
 (a vector moves by about eps ||A|| / gap, and the generic test matrices
 have gaps near 1e-3 of their scale); transformed blocks and records 1e-12
-of each record's largest element when both sides use the same solutions.
+of each record's largest element when both sides use the same solutions
+(1e-10 for the split form's tensor-core products).
 """
 import os
 
@@ -55,9 +56,13 @@ def _oracle_matrix(w, H):
     return g, m
 
 
-def test_channel_basis_against_oracle():
+@pytest.mark.parametrize("precision,tol", [(PLAIN_FP64, 1e-12), (SPLIT_BF16, 1e-10)])
+def test_channel_basis_against_oracle(precision, tol):
+    """The plain form transforms the blocks with cuBLAS DGEMM (1e-12 of each
+    block's largest element); the split form with the split-BF16 tcgen05
+    products (1e-10)."""
     w = synth.small(ns=40, nch=4, mk=2, n_entries=500, breit=True, seed=91)
-    a = _assembler(w, SPLIT_BF16)
+    a = _assembler(w, precision)
     for L in w.lists:
         a.gen_matrix(L.icase, L.itype, L.kpol, L.k1, L.k2, L.k3, L.k4, L.c)
     _generic_diagonal(a, w, 3)
@@ -91,7 +96,7 @@ def test_channel_basis_against_oracle():
                 ni, nj = rnsol[ich - 1], rnsol[jch - 1]
                 ref = O.record_block(H[:, :, k - 1], rsol[:, :ni, ich - 1], rsol[:, :nj, jch - 1])
                 got = out[:, :, k - 1]
-                assert np.abs(got[:ni, :nj] - ref).max() <= 1e-12 * max(np.abs(ref).max(), 1e-300)
+                assert np.abs(got[:ni, :nj] - ref).max() <= tol * max(np.abs(ref).max(), 1e-300)
                 assert not got[ni:, :].any() and not got[:, nj:].any()
     a.close()
 
@@ -174,3 +179,39 @@ def test_write_out_against_oracle(tmp_path):
     assert np.abs(ov - rov).max() <= 1e-12 * np.abs(rov).max()
     assert rov[w.nch:, :w.nch].any() and rov[w.nch:, w.nch:].any()
     assert os.path.getsize(path) == len(got)
+
+
+@pytest.mark.parametrize("ns,nch", [(70, 3), (150, 2)])
+def test_split_transform_sizes(ns, nch):
+    """The split-BF16 transform at sizes with several 128-row tiles and K
+    chunks (ms = 140, 300) and uneven solution counts, against the oracle's
+    loops, two calls in a row on the same solutions."""
+    w = synth.small(ns=ns, nch=nch, mk=1, n_entries=60 * nch, breit=False, seed=ns + nch,
+                    rmax=30.0)
+    a = _assembler(w, SPLIT_BF16)
+    for L in w.lists:
+        a.gen_matrix(L.icase, L.itype, L.kpol, L.k1, L.k2, L.k3, L.k4, L.c)
+    ms = a.ms
+    rng = np.random.default_rng(ns)
+    for ich in range(1, nch + 1):
+        for jch in range(1, ich + 1):
+            X = rng.standard_normal((ms, ms)) * 10.0 ** rng.uniform(-3, 3)
+            a.update_hx(ich, jch, np.asfortranarray(X if ich != jch else X + X.T), 1.0)
+    H = a.get_matrix()
+    sol = np.zeros((ms, ms, nch), order="F")
+    nsol = np.array([ms - 5 - 17 * i for i in range(nch)], dtype=np.int32)
+    for ich in range(nch):
+        sol[:, :nsol[ich], ich] = rng.standard_normal((ms, nsol[ich]))
+    for rep in range(2):
+        out = a.channel_basis(sol, nsol, out=True)
+        for ich in range(2, nch + 1):
+            for jch in range(1, ich):
+                k = w.icc[ich - 1, jch - 1]
+                ni, nj = nsol[ich - 1], nsol[jch - 1]
+                src = H if rep == 0 else prev
+                ref = O.record_block(src[:, :, k - 1], sol[:, :ni, ich - 1], sol[:, :nj, jch - 1])
+                got = out[:, :, k - 1]
+                assert np.abs(got[:ni, :nj] - ref).max() <= 1e-10 * np.abs(ref).max(), (rep, ich, jch)
+                assert not got[ni:, :].any() and not got[:, nj:].any()
+        prev = out.copy()
+    a.close()
