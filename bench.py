@@ -122,13 +122,17 @@ class Clocks:
 
 
 # DRAM traffic of k_xfused per algorithmic byte: ncu (dram__bytes_read.sum +
-# dram__bytes_write.sum, --clock-control none, one kernel, a few launches) on
-# the 40-channel case, divided by the algorithmic bytes the same launches
-# state; the traffic scales with the hch tiles a launch touches, so the
-# ratio carries to the 120-channel launches.  None until such a capture of
-# the current kernel exists: the bench then reports no traffic.
-XFUSED_TRAFFIC_PER_ALGORITHMIC_BYTE = None
-XFUSED_TRAFFIC_SOURCE = None
+# dram__bytes_write.sum, --clock-control none, k_xfused launches only) on the
+# 40-channel case, divided by the algorithmic bytes the same launches state;
+# the traffic scales with the hch tiles a launch touches, so the ratio is
+# carried to the 120-channel launches.  At 40 channels the 129 MB L2 holds a
+# larger share of a launch's tiles than at 120, so the carried figure is a
+# lower estimate of the full-size traffic.  None: no traffic reported.
+XFUSED_TRAFFIC_PER_ALGORITHMIC_BYTE = 0.891
+XFUSED_TRAFFIC_SOURCE = ("ncu over the 35 k_xfused launches of one 40-channel step "
+                         "(ns=400, 4.2 GB matrix): 5.105 GB read + 1.997 GB written "
+                         "against 7.967 GB stated algorithmic bytes; ratio carried "
+                         "to the 120-channel launches (a lower estimate)")
 
 
 def d2h_gbs(torch, dev, nbytes=4 << 30) -> float:
@@ -633,11 +637,12 @@ def basis_main(args, rank, world, local):
     (one generalized eigenproblem per channel, cuSOLVER sygvd; B = the
     B-spline overlap fppqq, the first and last B-spline of P and Q removed,
     every eigenvalue kept) and dbsrg_channel_basis (D_i^T H D_j for the 7140
-    off-diagonal blocks, cuBLAS DGEMM).  Timed once each after a warm-up,
-    host wall clock around synchronised calls."""
+    off-diagonal blocks: split-BF16 tcgen05 products, then again with cuBLAS
+    DGEMM on the same matrix for comparison).  Timed once each after a
+    warm-up, host wall clock around synchronised calls."""
     import torch
 
-    from dbsr_gb300 import SPLIT_BF16, Assembler, synth
+    from dbsr_gb300 import PLAIN_FP64, SPLIT_BF16, Assembler, synth
 
     torch.cuda.set_device(local)
     w = synth.config1(scale=args.scale, nch=args.nch, breit=True)
@@ -693,6 +698,29 @@ def basis_main(args, rank, world, local):
         t3 = time.perf_counter()
         out = {"orth_channels_s": to1 - to0, "diag_channels_s": t1 - t0,
                "diag_channels_device_out_s": t2 - t1, "channel_basis_s": t3 - t2}
+    # the same transformation by cuBLAS DGEMM (the FP64 forms' path) on the
+    # same assembled matrix and solutions, and the split products' error
+    # against it on a sample of blocks (max over each block's elements,
+    # relative to the block's largest element)
+    rng = np.random.default_rng(5)
+    pairs = [(i, j) for i in range(2, nch + 1) for j in range(1, i) if w.icc[i - 1, j - 1] > 0]
+    sample = [pairs[q] for q in rng.choice(len(pairs), min(48, len(pairs)), replace=False)]
+    split_blocks = [a.get_block(i, j) for i, j in sample]
+    assemble()
+    a.orth_channels(iort)
+    a.set_precision(PLAIN_FP64)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    a.channel_basis(sol, nsol)
+    torch.cuda.synchronize()
+    out["channel_basis_dgemm_s"] = time.perf_counter() - t0
+    a.set_precision(SPLIT_BF16)
+    worst = 0.0
+    for (i, j), sb in zip(sample, split_blocks):
+        db = a.get_block(i, j)
+        worst = max(worst, float(np.abs(sb - db).max() / max(np.abs(db).max(), 1e-300)))
+    out["split_vs_dgemm_max_rel"] = worst
+    out["split_vs_dgemm_blocks"] = len(sample)
     # DBS_ORTH work: per block with na (row) and nb (column) orbitals, one
     # read-modify-write of the block (16 B per element) and 4 (na + nb) ms^2
     # FP64 operations (T1, T2 and the update)
@@ -717,8 +745,9 @@ def basis_main(args, rank, world, local):
                 "higher_is_better": False, "dtype": "f64",
                 "config": {"workload": f"config1 matrix: ns={ns} nch={nch}", "blocks": w.iicc,
                            "solutions_per_channel": int(np.median(nsol))},
-                "basis_dgemm_tflop": fl / 1e12,
-                "basis_dgemm_tflops": fl / out["channel_basis_s"] / 1e12})
+                "basis_fp64_tflop": fl / 1e12,
+                "basis_split_tflops": fl / out["channel_basis_s"] / 1e12,
+                "basis_dgemm_tflops": fl / out["channel_basis_dgemm_s"] / 1e12})
     print(json.dumps(out), flush=True)
     a.close()
 

@@ -280,8 +280,10 @@ int dbsrg_matrix_device_ptr(dbsrg_ctx *ctx, double **hch_dev);
  * (record_matrix.f90:14-26): every block of a channel pair ich > jch becomes
  * c = D_ich^T H D_jch (nsol(ich) x nsol(jch) in its top-left corner, zero
  * elsewhere; D = sol), in place; diagonal blocks stay.  out, when not NULL,
- * receives a copy of the transformed hch.
- * Both load cuSOLVER and cuBLAS on first use. */
+ * receives a copy of the transformed hch.  In the split form
+ * (DBSRG_SPLIT_BF16) the products are split-BF16 tensor-core products
+ * (within 1e-10 of each block's largest element), in the FP64 forms cuBLAS
+ * DGEMM.  Both load cuSOLVER and cuBLAS on first use. */
 int dbsrg_diag_channels(dbsrg_ctx *ctx, const double *bdiag, const int *iprm,
                         double emin, double emax, double egap, double *sol,
                         double *eval, int *nsol);
