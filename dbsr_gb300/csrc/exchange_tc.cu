@@ -143,6 +143,8 @@ struct ZArgs {
 // exponents.  The sums read the pair potentials of every entry: the kernel
 // is bound by those reads (L2 and HBM), not by its arithmetic.
 constexpr int ZROWS = 32;  // one warp per block: one 32-row digit tile
+// ONE: at most 32 bound orbitals (one chunk)
+template <bool ONE>
 __global__ void __launch_bounds__(ZROWS) k_zdigits(const ZArgs z) {
   // [mode][nb][ZROWS] float-float: per thread one column; sized by the bound
   // orbitals (and the modes) in use, which sets how many blocks share an SM
@@ -196,20 +198,19 @@ __global__ void __launch_bounds__(ZROWS) k_zdigits(const ZArgs z) {
   const size_t sl = (size_t)z.NR * TILE;
   for (int mode = 0; mode < (z.lower ? 2 : 1); mode++) {
     float2 *zz = mode ? z1 : z0;
-    // each sum renormalised in place (TwoSum: hi + lo unchanged, |lo| at
-    // most half an ulp of hi)
-    for (int k = 0; k < nb; k++) {
-      const float2 v = zz[k * ZROWS + t];
-      const float s = v.x + v.y, bp = s - v.x;
-      zz[k * ZROWS + t] = make_float2(s, (v.x - (s - bp)) + (v.y - bp));
-    }
-    // per chunk of 32 orbitals: the row exponent from the high words, the
-    // digits 8 columns at a time
-    for (int ck = 0; ck < z.nbk; ck++) {
+    // per chunk of 32 orbitals: each sum renormalised in place (TwoSum:
+    // hi + lo unchanged, |lo| at most half an ulp of hi), the row exponent
+    // from the high words, the digits 8 columns at a time
+    for (int ck = 0; ck < (ONE ? 1 : z.nbk); ck++) {
       float m = 0.0f;
-      for (int k = 32 * ck; k < min(nb, 32 * ck + 32); k++) m = fmaxf(m, fabsf(zz[k * ZROWS + t].x));
+      for (int k = 32 * ck; k < (ONE ? nb : min(nb, 32 * ck + 32)); k++) {
+        const float2 v = zz[k * ZROWS + t];
+        const float s = v.x + v.y, bp = s - v.x;
+        zz[k * ZROWS + t] = make_float2(s, (v.x - (s - bp)) + (v.y - bp));
+        m = fmaxf(m, fabsf(s));
+      }
       const int e = scale_exp_ff(m);
-      const size_t op = ((size_t)(a * 2 + mode) * z.nm + slot) * z.nbk + ck;
+      const size_t op = ((size_t)(a * 2 + mode) * z.nm + slot) * (ONE ? 1 : z.nbk) + ck;
       z.ez[op * z.NR * EXP_PER_ROWTILE + y] = e;
       const int et = __reduce_max_sync(0xffffffffu, e);  // a warp is one 32-row tile
       if ((t & 31) == 0) z.ez[op * z.NR * EXP_PER_ROWTILE + z.NR * 32 + y / 32] = et;
@@ -307,9 +308,9 @@ struct ProdIt {
 
 // advance to the next product (orbital chunks innermost); false when the
 // CTA's rows are done
-__device__ __forceinline__ bool prod_next(const XArgs &p, ProdIt &it) {
+__device__ __forceinline__ bool prod_next(const XArgs &p, int nbk, ProdIt &it) {
   if (it.row >= p.nrows) return false;
-  if (++it.ck < p.nbk) return true;
+  if (++it.ck < nbk) return true;
   it.ck = 0;
   it.pc++;
   while (it.pc >= it.np) {
@@ -328,15 +329,15 @@ __device__ __forceinline__ bool prod_next(const XArgs &p, ProdIt &it) {
 
 // digit operands of the current product: A (128 rows of the tile) and B
 // (32 columns), each [slice][32-row tile][TILE] with slices sl apart
-__device__ __forceinline__ void prod_operands(const XArgs &p, const ProdIt &it, size_t sl,
+__device__ __forceinline__ void prod_operands(const XArgs &p, int nbk, const ProdIt &it, size_t sl,
                                               const __nv_bfloat16 *&As,
                                               const __nv_bfloat16 *&Bs) {
   const int ck = it.ck;
   const int pcode = (it.codes >> (3 * it.pc)) & 7, t = pcode & 3, m = pcode >> 2;
   const int tc = term_code(it.r, t), a = tc & 3, tra = (tc >> 2) & 1, slot = tc >> 3;
-  const __nv_bfloat16 *Ub = p.Ud[a] + ((size_t)m * p.nbk + ck) * TS * sl;
+  const __nv_bfloat16 *Ub = p.Ud[a] + ((size_t)m * nbk + ck) * TS * sl;
   const __nv_bfloat16 *Zb =
-      p.Zd + (((size_t)(a * 2 + m) * p.nm + slot) * p.nbk + ck) * TS * sl;
+      p.Zd + (((size_t)(a * 2 + m) * p.nm + slot) * nbk + ck) * TS * sl;
   As = (tra ? Zb : Ub) + (size_t)4 * it.r.tx * TILE;
   Bs = (tra ? Ub : Zb) + (size_t)it.ty * TILE;
 }
@@ -380,6 +381,9 @@ __device__ __forceinline__ void mbar_arrive(uint32_t mbar) {
 // 18 warps: two SM sub-partitions hold 5 of them, and a sub-partition has
 // 16384 registers, so at most 96 registers a thread.  Four consumer warps per
 // sub-partition hide each other's TMEM and integer latencies.
+//
+// ONE: at most 32 bound orbitals (one orbital chunk, nbk = 1).
+template <bool ONE>
 __global__ void __maxnreg__(96) k_xfused(const XArgs p) {
   extern __shared__ __align__(1024) unsigned char smraw[];
   unsigned char *sA = smraw;                          // [2][TS][A_BYTES]
@@ -416,6 +420,7 @@ __global__ void __maxnreg__(96) k_xfused(const XArgs p) {
   const size_t sl = (size_t)p.NR * TILE;  // elements per slice of a digit operand
   const size_t ms = 2 * (size_t)p.ns;
   const int EX = p.NR * EXP_PER_ROWTILE;  // exponents per digit operand
+  const int nbk = ONE ? 1 : p.nbk;
   // even ns: every hch column and band row of a tile starts on a 16-byte
   // boundary and is staged by 1-D bulk copies; odd ns: 8-byte cp.async
   const bool bulk = (p.ns % 2) == 0;
@@ -434,7 +439,7 @@ __global__ void __maxnreg__(96) k_xfused(const XArgs p) {
       it.ty = p.nty - 1;
       it.pc = 0;
       it.np = 0;
-      it.ck = p.nbk - 1;  // the first prod_next moves to the first product
+      it.ck = nbk - 1;  // the first prod_next moves to the first product
       it.codes = 0;
       const __nv_bfloat16 *aKey[2] = {nullptr, nullptr};  // A operand held by each A slot
       int aslot[2] = {0, 0};                              // A slot of products q & 1
@@ -443,7 +448,7 @@ __global__ void __maxnreg__(96) k_xfused(const XArgs p) {
       // bulk loads of product qq into B slot qq & 1 and an A slot
       auto issue_loads = [&](long long qq) {
         const __nv_bfloat16 *As, *Bs;
-        prod_operands(p, it, sl, As, Bs);
+        prod_operands(p, nbk, it, sl, As, Bs);
         const int bq = (int)(qq & 1);
         int s;
         if (aKey[0] == As)
@@ -466,7 +471,7 @@ __global__ void __maxnreg__(96) k_xfused(const XArgs p) {
         aslot[bq] = s;
         ld_issued = qq;
       };
-      bool more = prod_next(p, it);
+      bool more = prod_next(p, nbk, it);
       if (more) issue_loads(0);
       for (long long q = 0; more; q++) {
         if (*abort_flag) {
@@ -477,7 +482,7 @@ __global__ void __maxnreg__(96) k_xfused(const XArgs p) {
         const uint32_t n = (uint32_t)(q >> 1);
         // loads of product q + 1: its B slot (and an A slot other than
         // product q's) were last read by product q - 1 or earlier
-        const bool more1 = prod_next(p, it);
+        const bool more1 = prod_next(p, nbk, it);
         if (more1) {
           if (q >= 1 &&
               !mbar_wait(smem_u32(&bar_mma[(q - 1) & 1]), (uint32_t)(((q - 1) >> 1) & 1),
@@ -695,13 +700,13 @@ __global__ void __maxnreg__(96) k_xfused(const XArgs p) {
         // products of the tile: field product fp of the codes, orbital chunk
         // ck (innermost)
         for (int pc = 0, fp = 0, ck = 0; fp < np;
-             pc++, q++, (++ck == p.nbk ? (ck = 0, fp++) : 0)) {
+             pc++, q++, (++ck == nbk ? (ck = 0, fp++) : 0)) {
           const int b = q & 1;
           const uint32_t n = q >> 1;
           const int pcode = (codes >> (3 * fp)) & 7, m = pcode >> 2;
           const int tc = term_code(r, pcode & 3), a = tc & 3, tra = (tc >> 2) & 1;
-          const int *eua = p.eu[a] + ((size_t)m * p.nbk + ck) * EX;
-          const int *ezs = p.ez + (((size_t)(a * 2 + m) * p.nm + (tc >> 3)) * p.nbk + ck) * EX;
+          const int *eua = p.eu[a] + ((size_t)m * nbk + ck) * EX;
+          const int *ezs = p.ez + (((size_t)(a * 2 + m) * p.nm + (tc >> 3)) * nbk + ck) * EX;
           const int er = tra ? ezs[x] : eua[x];
           // column exponents: 8 ints at a 32-byte aligned offset
           const int4 *ep = reinterpret_cast<const int4 *>((tra ? eua : ezs) + y0);
@@ -727,18 +732,21 @@ __global__ void __maxnreg__(96) k_xfused(const XArgs p) {
           int P[3][CPT];
           const uint32_t col =
               tbase + ((uint32_t)(lg * 32) << 16) + (uint32_t)(b * 256 + cg * CPT);
+          {
+            // the six orders' columns loaded together, one wait
+            uint32_t v[TS][CPT];
 #pragma unroll
-          for (int k = 0; k < 3; k++) {
-            uint32_t v0[CPT], v1[CPT];
-            tmem_ld8(col + 64 * k, v0);
-            tmem_ld8(col + 64 * k + 32, v1);
+            for (int g = 0; g < TS; g++) tmem_ld8(col + 32 * g, v[g]);
             tmem_wait_ld();
 #pragma unroll
-            for (int c = 0; c < CPT; c++)
-              P[k][c] = (int)(((uint32_t)__float_as_uint(__uint_as_float(v0[c]) + 12582912.0f)
-                               << 8) +
-                              (uint32_t)__float_as_uint(__uint_as_float(v1[c]) + 12582912.0f) -
-                              257u * 0x4B400000u);
+            for (int k = 0; k < 3; k++)
+#pragma unroll
+              for (int c = 0; c < CPT; c++)
+                P[k][c] =
+                    (int)(((uint32_t)__float_as_uint(__uint_as_float(v[2 * k][c]) + 12582912.0f)
+                           << 8) +
+                          (uint32_t)__float_as_uint(__uint_as_float(v[2 * k + 1][c]) + 12582912.0f) -
+                          257u * 0x4B400000u);
           }
           fence_before();
           __syncwarp();
@@ -959,7 +967,8 @@ int split_exchange(dbsrg_ctx *c, const SplitExchange &x) {
   z.ez = ez;
   z.Yb = Yb;
   const size_t zsm = (size_t)(x.lower ? 2 : 1) * nb * ZROWS * sizeof(float2);
-  if ((rc = raise_smem_limit(c, (const void *)k_zdigits, zsm))) return rc;
+  const void *zk = nbk == 1 ? (const void *)k_zdigits<true> : (const void *)k_zdigits<false>;
+  if ((rc = raise_smem_limit(c, zk, zsm))) return rc;
   // executed work: per PQ type, row and entry one multiply-add per field
   // (Z, and Zl for R^k) and per band diagonal (17), float-float; the entry's
   // band potential values (17 float-float pairs a row) read, the digits and
@@ -968,9 +977,12 @@ int split_exchange(dbsrg_ctx *c, const SplitExchange &x) {
   const double zb = 8.0 * x.na * ns * ((1.0 + x.lower + NDB) * (double)x.nent +
                                        NDB * (double)x.nm) +
                     2.0 * TS * (double)x.na * (1 + x.lower) * x.nm * nbk * NR * TILE;
-  DBSRG_RUN_W(c, "k_zdigits", zb, zf,
-              k_zdigits<<<dim3((unsigned)(NR * 32 / ZROWS), (unsigned)x.nm, (unsigned)x.na),
-                          ZROWS, zsm, st>>>(z));  // every row of the operand, zeros past ns
+  // every row of the operand, zeros past ns
+  const dim3 gz((unsigned)(NR * 32 / ZROWS), (unsigned)x.nm, (unsigned)x.na);
+  if (nbk == 1)
+    DBSRG_RUN_W(c, "k_zdigits", zb, zf, k_zdigits<true><<<gz, ZROWS, zsm, st>>>(z));
+  else
+    DBSRG_RUN_W(c, "k_zdigits", zb, zf, k_zdigits<false><<<gz, ZROWS, zsm, st>>>(z));
   XArgs p{};
   p.ns = ns;
   p.NR = NR;
@@ -995,10 +1007,16 @@ int split_exchange(dbsrg_ctx *c, const SplitExchange &x) {
   p.inject_wait = c->inject_wait ? 1 : 0;
   const size_t smem = 2 * TS * (size_t)(A_BYTES + B_BYTES) +
                       ((size_t)2 * MAXT * NDB * BR + 2 * 32 * 128) * sizeof(double);
-  if ((rc = raise_smem_limit(c, (const void *)k_xfused, smem))) return rc;
+  const void *xk = nbk == 1 ? (const void *)k_xfused<true> : (const void *)k_xfused<false>;
+  if ((rc = raise_smem_limit(c, xk, smem))) return rc;
   const int nblk = std::min(p.nrows, std::max(1, c->nsm));
   double wbytes = 0.0, wflops = 0.0;
   if (c->timing) xfused_work(x.hxq, x.nxq, ns, x.lower, nbk, wbytes, wflops);
-  DBSRG_RUN_W(c, "k_xfused", wbytes, wflops, k_xfused<<<(unsigned)nblk, NTHR, smem, st>>>(p));
+  if (nbk == 1)
+    DBSRG_RUN_W(c, "k_xfused", wbytes, wflops,
+                k_xfused<true><<<(unsigned)nblk, NTHR, smem, st>>>(p));
+  else
+    DBSRG_RUN_W(c, "k_xfused", wbytes, wflops,
+                k_xfused<false><<<(unsigned)nblk, NTHR, smem, st>>>(p));
   return DBSRG_OK;
 }

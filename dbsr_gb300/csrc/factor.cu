@@ -444,7 +444,7 @@ __global__ void k_pair_scan(int nv, int npair, double *S0, int suffix0, double *
 // [cv, cv+8], so cells of one phase never share an output.  Two stages:
 // H(po, g1, b) = sum_g2 R P2, then sum_g1 P1 H.
 template <bool FF>
-__global__ void __launch_bounds__(256) k_pair_diag(int ns, int ks, int kk, int nb, int icv,
+__global__ void __launch_bounds__(512) k_pair_diag(int ns, int ks, int kk, int nb, int icv,
                                                    char sym, PairSpec eo, PairSpec ed,
                                                    const double *__restrict__ rkd,
                                                    const double *__restrict__ P1,
@@ -993,7 +993,7 @@ int get_pairpot_direct_any(dbsrg_ctx *c, int family, int type, int k, int icv, i
   if (ff) {
     if ((rc = set_smem(c, (const void *)k_pair_diag<true>, sm3))) return rc;
     DBSRG_RUN_W(c, "k_pair_diag", dbytes, dflops,
-                k_pair_diag<true><<<nv, 256, sm3, st>>>(
+                k_pair_diag<true><<<nv, 512, sm3, st>>>(
                     ns, ks, kk, nb, icv, sym, eo, ed, cd->rkd, P1, P2, Dq, per));
     DBSRG_RUN_W(c, "k_pair_direct_final", fbytes, fflops,
                 k_pair_direct_final<true><<<gf, 128, 0, st>>>(ns, ks, nv, kk, nb, icv, sym, eo,
@@ -1002,7 +1002,7 @@ int get_pairpot_direct_any(dbsrg_ctx *c, int family, int type, int k, int icv, i
   } else {
     if ((rc = set_smem(c, (const void *)k_pair_diag<false>, sm3))) return rc;
     DBSRG_RUN_W(c, "k_pair_diag", dbytes, dflops,
-                k_pair_diag<false><<<nv, 256, sm3, st>>>(
+                k_pair_diag<false><<<nv, 512, sm3, st>>>(
                     ns, ks, kk, nb, icv, sym, eo, ed, cd->rkd, P1, P2, Dq, per));
     DBSRG_RUN_W(c, "k_pair_direct_final", fbytes, fflops,
                 k_pair_direct_final<false><<<gf, 128, 0, st>>>(ns, ks, nv, kk, nb, icv, sym, eo,

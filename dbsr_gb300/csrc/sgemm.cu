@@ -5,12 +5,13 @@
 //
 // Operands.  Both GEMMs are C(r, c) = sum_k A(r, k) B(k, c) with the rows of
 // A and the columns of B given as vectors contiguous in k ("vectors": the
-// columns of D, of H and of W^T).  Every vector v gets one exponent e with
-// 2^(e-1) > max |v| and six balanced base-256 digits per element
-// (tc_common.cuh), stored as K chunks of 32: [chunk][slice][32-vector tile]
-// [32 x 32 BF16, canonical K-major layout].  The digits of D_ch serve as A
-// of the first product (its columns are the rows of D_ch^T) and as B of the
-// second (the columns of D_ch).
+// columns of D, of H and of W^T).  Every vector is cut into K chunks of 32;
+// every chunk gets its own exponent e with 2^(e-1) > its largest modulus
+// and six balanced base-256 digits per element (tc_common.cuh), stored as
+// [chunk][slice][32-vector tile][32 x 32 BF16, canonical K-major layout],
+// the exponents as [chunk][vector].  The digits of D_ch serve as A of the
+// first product (its columns are the rows of D_ch^T) and as B of the second
+// (the columns of D_ch).
 //
 // Products.  One CTA per 128 x 32 output tile walks the K chunks: a producer
 // thread bulk-copies the six A slices (128 x 32) and B slices (32 x 32) of a
@@ -18,11 +19,12 @@
 // (21 slice pairs of order i + j <= 5, two K steps of 16) into one of two
 // TMEM accumulator sets; eight epilogue warps read the six orders of the
 // set (exact integers below 2^22), recombine them into int64
-// I = sum_g D_g 256^(5-g), and add I >> 5 into their int64 sums (every
-// chunk of a row has the same scale, so no alignment; |sum| <= K/4 2^56
-// before the shift, so the shift keeps it inside int64 for K up to 16384
-// and drops bits below 2^-51 of the scale).  The result is 2^(e_r + e_c - 51) times the sum, converted once.
-// Error: about K 2^-48 of max|A row| max|B column| per element.
+// I = sum_g D_g 256^(5-g) at the chunk's scale 2^(e_r + e_c - 56), and add
+// I >> 5 into an int64 sum kept at the largest scale met so far (smaller
+// scales shifted right: bits below 2^-51 of the largest one dropped; with
+// |I| < 2^59 a chunk, the sum of up to 256 chunks stays inside int64).  The
+// sum is converted to FP64 once.  Error: about 32 2^-48 of max|A| max|B|
+// over each chunk, summed over the chunks.
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -43,32 +45,40 @@ constexpr int NCW = 8;                      // epilogue warps
 constexpr int NTHR = 32 * (NCW + 1);        // + one producer warp
 constexpr unsigned long long WAIT_NS = 2000000000ull;
 
+constexpr int ZERO_EXP = -20000;  // exponent of an all-zero chunk
+constexpr int NO_EXP = -100000;   // the empty sum
+
 // digits of R vectors of K elements (vector r at X + r ldx, contiguous),
 // rows padded to NR*32 and K to nk*32 with zeros: out [nk][TS][NR][TILE],
-// exponents ex[NR*32].  One warp per vector.
+// chunk exponents ex[nk][NR*32].  One warp per vector; lanes 4q..4q+3 hold
+// the four groups of 8 elements of one chunk.
 __global__ void k_vec_digits(int R, int K, const double *X, size_t ldx, int NR, int nk,
                              __nv_bfloat16 *out, int *ex) {
   const int r = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32, lane = threadIdx.x % 32;
-  if (r >= NR * 32) return;
+  if (r >= NR * 32) return;  // whole warps
   const double *x = X + (size_t)r * ldx;
   const bool live = r < R;
-  double m = 0.0;
-  if (live)
-    for (int k = lane; k < K; k += 32) m = fmax(m, fabs(x[k]));
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-  const int e = scale_exp(m);
-  if (lane == 0) ex[r] = e;
   const int rt = r >> 5, rr = r & 31;
   const size_t sl = (size_t)NR * TILE;
-  for (int g = lane; g < nk * 4; g += 32) {  // groups of 8 elements
-    const int kc = g >> 2, kg = g & 3;
-    float d[8][TS];
+  for (int g0 = 0; g0 < nk * 4; g0 += 32) {
+    const int g = g0 + lane, kc = g >> 2, kg = g & 3;
+    const bool gv = g < nk * 4;
+    double v[8];
+    double m = 0.0;
 #pragma unroll
     for (int t = 0; t < 8; t++) {
       const int k = 32 * kc + 8 * kg + t;
-      digits(live && k < K ? x[k] : 0.0, e, d[t]);
+      v[t] = live && gv && k < K ? x[k] : 0.0;
+      m = fmax(m, fabs(v[t]));
     }
+    m = fmax(m, __shfl_xor_sync(0xffffffffu, m, 1));
+    m = fmax(m, __shfl_xor_sync(0xffffffffu, m, 2));
+    const int e = m == 0.0 ? ZERO_EXP : scale_exp(m);
+    if (!gv) continue;
+    if (kg == 0) ex[(size_t)kc * NR * 32 + r] = e;
+    float d[8][TS];
+#pragma unroll
+    for (int t = 0; t < 8; t++) digits(v[t], e, d[t]);
     __nv_bfloat16 *base = out + (size_t)kc * TS * sl + (size_t)rt * TILE + core_off(rr, 8 * kg);
 #pragma unroll
     for (int i = 0; i < TS; i++) {
@@ -82,7 +92,7 @@ __global__ void k_vec_digits(int R, int K, const double *X, size_t ldx, int NR, 
 
 struct GemmJob {
   const __nv_bfloat16 *A, *B;  // digits, [nk][TS][NRa|NRb][TILE]
-  const int *ea, *eb;          // vector exponents
+  const int *ea, *eb;          // chunk exponents, [nk][NRa*32] and [nk][NRb*32]
   double *C;                   // C(r, c) at C[r*sr + c*sc]
   long long sr, sc;
   int M, N, NRa, NRb;
@@ -196,14 +206,22 @@ __global__ void __launch_bounds__(NTHR) k_sgemm(const GemmJob *jobs, int nk, int
     // ---------------------------------------------------------- epilogue
     // warp w reads TMEM lanes 32 (w & 3) .. +31 (rows) and columns 16 (w >> 2)
     const int lg = warp & 3, ch = warp >> 2;
-    const int r = mt * 128 + lg * 32 + lane;
+    const int r = mt * 128 + lg * 32 + lane;  // < NRa*32: A rows are padded to 128
     long long acc[16];
+    int cur[16];
 #pragma unroll
-    for (int c = 0; c < 16; c++) acc[c] = 0;
+    for (int c = 0; c < 16; c++) acc[c] = 0, cur[c] = NO_EXP;
     bool dead = false;
     for (int kc = 0; kc < nk; kc++) {
       const int s = kc & 1;
       const uint32_t n = (uint32_t)(kc >> 1);
+      // the chunk's row exponent and the 16 column exponents (64-byte aligned)
+      const int er = jb.ea[(size_t)kc * jb.NRa * 32 + r];
+      const int4 *ep =
+          reinterpret_cast<const int4 *>(jb.eb + (size_t)kc * jb.NRb * 32 + nt * 32 + ch * 16);
+      const int4 e0 = ep[0], e1 = ep[1], e2 = ep[2], e3 = ep[3];
+      const int ec[16] = {e0.x, e0.y, e0.z, e0.w, e1.x, e1.y, e1.z, e1.w,
+                          e2.x, e2.y, e2.z, e2.w, e3.x, e3.y, e3.z, e3.w};
       if (!dead && *abort_flag) dead = true;
       bool ok = !dead && mbar_wait(smem_u32(&bar_mma[s]), n & 1, WAIT_NS);
       ok = __all_sync(0xffffffffu, ok);
@@ -240,19 +258,25 @@ __global__ void __launch_bounds__(NTHR) k_sgemm(const GemmJob *jobs, int nk, int
       if (lane == 0) mbar_arrive1(smem_u32(&bar_free[s]));
 #pragma unroll
       for (int c = 0; c < 16; c++) {
-        const long long I = (long long)P[0][c] * 4294967296LL + (long long)P[1][c] * 65536LL +
-                            (long long)P[2][c];
-        acc[c] += I >> SHIFT;
+        const long long I = ((long long)P[0][c] * 4294967296LL + (long long)P[1][c] * 65536LL +
+                             (long long)P[2][c]) >> SHIFT;
+        const int se = er + ec[c];
+        if (se > cur[c]) {  // the sum raised to the larger scale
+          const int up = se - cur[c];
+          acc[c] = up < 63 ? acc[c] >> up : 0;
+          cur[c] = se;
+        }
+        const int sh = cur[c] - se;
+        if (sh < 63) acc[c] += I >> sh;
       }
     }
     if (!dead && r < jb.M) {
-      const int er = jb.ea[r];
 #pragma unroll
       for (int c = 0; c < 16; c++) {
         const int cc = nt * 32 + ch * 16 + c;
         if (cc < jb.N)
           jb.C[(long long)r * jb.sr + (long long)cc * jb.sc] =
-              i64_to_f64(acc[c], er + jb.eb[cc] - 8 * (TS + 1) + SHIFT);
+              i64_to_f64(acc[c], cur[c] - 8 * (TS + 1) + SHIFT);
       }
     }
   }
@@ -285,7 +309,7 @@ int split_channel_basis(dbsrg_ctx *c, const double *D, const int *nsol) {
   const int ms = c->g.ms, nch = c->nch;
   // vectors padded to whole 128-row A tiles, K to whole chunks of 32
   const int NR = 4 * ((ms + 127) / 128), nk = (ms + 31) / 32;
-  if (nk * 32 > 16384) return set_err(c, DBSRG_EINVAL, "channel_basis: ms above 16384");
+  if (nk > 256) return set_err(c, DBSRG_EINVAL, "channel_basis: ms above 8192");
   const size_t blk = (size_t)ms * ms;
   const size_t dsz = (size_t)nk * TS * NR * TILE;  // BF16 elements of one digit operand
   cudaStream_t st = c->stream;
@@ -302,7 +326,8 @@ int split_channel_basis(dbsrg_ctx *c, const double *D, const int *nsol) {
   if (bk.empty()) return DBSRG_OK;
   // digits of every channel's solutions (columns of D_ch)
   Buf dD, eD, err;
-  if (!dD.alloc(dsz * 2 * nch) || !eD.alloc(sizeof(int) * NR * 32 * nch) || !err.alloc(4))
+  const size_t esz = (size_t)nk * NR * 32;  // chunk exponents of one operand
+  if (!dD.alloc(dsz * 2 * nch) || !eD.alloc(sizeof(int) * esz * nch) || !err.alloc(4))
     return set_err(c, DBSRG_ENOMEM, "channel_basis: digit allocation failed");
   __nv_bfloat16 *Dd = (__nv_bfloat16 *)dD.p;
   int *De = (int *)eD.p;
@@ -312,16 +337,16 @@ int split_channel_basis(dbsrg_ctx *c, const double *D, const int *nsol) {
     DBSRG_RUN(c, "k_vec_digits",
               k_vec_digits<<<gv, 256, 0, st>>>(nsol[ch - 1], ms, D + (size_t)(ch - 1) * blk, ms,
                                                 NR, nk, Dd + dsz * (ch - 1),
-                                                De + (size_t)NR * 32 * (ch - 1)));
+                                                De + esz * (ch - 1)));
   // blocks in batches: digits of H's columns, W^T (ms x ni), digits of W's rows
-  const size_t per_blk = 2 * dsz * 2 + blk * 8 + 2 * sizeof(int) * NR * 32;
+  const size_t per_blk = 2 * dsz * 2 + blk * 8 + 2 * sizeof(int) * esz;
   size_t freeb = 0, totb = 0;
   cudaMemGetInfo(&freeb, &totb);
   int nb = (int)std::max<size_t>(1, std::min<size_t>(256, (freeb / 4) / per_blk));
   nb = std::min<int>(nb, (int)bk.size());
   Buf dH, dW, dWd, eH, eW, dJ;
   if (!dH.alloc(dsz * 2 * nb) || !dW.alloc(blk * 8 * nb) || !dWd.alloc(dsz * 2 * nb) ||
-      !eH.alloc(sizeof(int) * NR * 32 * nb) || !eW.alloc(sizeof(int) * NR * 32 * nb) ||
+      !eH.alloc(sizeof(int) * esz * nb) || !eW.alloc(sizeof(int) * esz * nb) ||
       !dJ.alloc(sizeof(GemmJob) * nb))
     return set_err(c, DBSRG_ENOMEM, "channel_basis: product allocation failed");
   const size_t smem = 2 * TS * (A_BYTES + B_BYTES);
@@ -337,7 +362,7 @@ int split_channel_basis(dbsrg_ctx *c, const double *D, const int *nsol) {
       DBSRG_RUN(c, "k_vec_digits",
                 k_vec_digits<<<gv, 256, 0, st>>>(ms, ms, H, ms, NR, nk,
                                                   (__nv_bfloat16 *)dH.p + dsz * q,
-                                                  (int *)eH.p + (size_t)NR * 32 * q));
+                                                  (int *)eH.p + esz * q));
     }
     // W^T(k, r) = sum_m H(m, k) D_ich(m, r): A = D_ich^T (rows r), B = H (columns k),
     // stored transposed: element (r, k) at Wt[k + ms r]
@@ -347,9 +372,9 @@ int split_channel_basis(dbsrg_ctx *c, const double *D, const int *nsol) {
       if (ni == 0) continue;
       GemmJob &j = jobs[jn++];
       j.A = Dd + dsz * (ich - 1);
-      j.ea = De + (size_t)NR * 32 * (ich - 1);
+      j.ea = De + esz * (ich - 1);
       j.B = (__nv_bfloat16 *)dH.p + dsz * q;
-      j.eb = (int *)eH.p + (size_t)NR * 32 * q;
+      j.eb = (int *)eH.p + esz * q;
       j.C = (double *)dW.p + blk * q;
       j.sr = ms;
       j.sc = 1;
@@ -370,7 +395,7 @@ int split_channel_basis(dbsrg_ctx *c, const double *D, const int *nsol) {
       DBSRG_RUN(c, "k_vec_digits",
                 k_vec_digits<<<gv, 256, 0, st>>>(ni, ms, (double *)dW.p + blk * q, ms, NR, nk,
                                                   (__nv_bfloat16 *)dWd.p + dsz * q,
-                                                  (int *)eW.p + (size_t)NR * 32 * q));
+                                                  (int *)eW.p + esz * q));
     }
     // c = W D_jch into the zeroed block (column-major, ld ms)
     jn = 0;
@@ -381,9 +406,9 @@ int split_channel_basis(dbsrg_ctx *c, const double *D, const int *nsol) {
       if (ni == 0 || nj == 0) continue;
       GemmJob &j = jobs[jn++];
       j.A = (__nv_bfloat16 *)dWd.p + dsz * q;
-      j.ea = (int *)eW.p + (size_t)NR * 32 * q;
+      j.ea = (int *)eW.p + esz * q;
       j.B = Dd + dsz * (jch - 1);
-      j.eb = De + (size_t)NR * 32 * (jch - 1);
+      j.eb = De + esz * (jch - 1);
       j.C = H;
       j.sr = 1;
       j.sc = ms;
