@@ -135,10 +135,12 @@ XFUSED_TRAFFIC_SOURCE = ("ncu over the 35 k_xfused launches of one 40-channel st
                          "to the 120-channel launches (a lower estimate)")
 
 
-def d2h_gbs(torch, dev, nbytes=4 << 30) -> float:
-    """Device-to-host copy rate of this machine into pinned memory (best of 3)."""
+def d2h_gbs(torch, dev, nbytes=4 << 30, dst=None) -> float:
+    """Device-to-host copy rate of this machine into pinned memory (best of 3):
+    into a new buffer, or into the first nbytes of `dst` (a pinned tensor)."""
     src = torch.empty(nbytes // 8, dtype=torch.float64, device=dev)
-    dst = torch.empty(nbytes // 8, dtype=torch.float64).pin_memory()
+    dst = (torch.empty(nbytes // 8, dtype=torch.float64).pin_memory() if dst is None
+           else dst[: nbytes // 8])
     best = 1e9
     for _ in range(3):
         torch.cuda.synchronize()
@@ -1055,15 +1057,27 @@ def main():
 
         e2e_step()
         dte = timed(e2e_step, 2)
-        npass = (w.iicc + nwin - 1) // nwin
+        # the library's partition: windows of nwin blocks, the first and the
+        # last max(1, nwin // 8) blocks (when there are more than two)
+        edge = max(1, nwin // 8)
+        if w.iicc > 2 * nwin:
+            npass, rest = 2, w.iicc - 2 * edge
+            npass += -(-rest // nwin)
+        else:
+            npass = -(-w.iicc // nwin)
         d2h = int((hout.numel() + hacf.numel()) * 8)
+        # the copy rate into the output buffer itself, its first and last
+        # 4 GB (a buffer partly in far host memory copies slower)
+        q = hout.numel() - (4 << 30) // 8
+        into = [d2h_gbs(torch, dev, dst=hout), d2h_gbs(torch, dev, dst=hout[q:])]
         del hout
         torch.cuda.empty_cache()
         link = d2h_gbs(torch, dev)
         e2e = {"value": world * fl["total"] / dte / 1e9, "unit": "GFLOP/s",
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": d2h,
                "s_per_matrix": dte, "api": "dbsrg_assemble_to_host",
-               "windows": npass, "d2h_gbs_measured": link,
+               "windows": npass, "window_blocks": nwin, "d2h_gbs_measured": link,
+               "d2h_gbs_into_output_first_last": into,
                "d2h_copy_floor_s": d2h / link / 1e9}
 
     # FP64 comparison: the same matrix by the factored FP64 and the plain FP64

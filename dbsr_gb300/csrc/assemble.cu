@@ -625,7 +625,8 @@ size_t plan_bytes(const dbsrg_ctx *c, int icase, int itype, int n) {
 
 int plan_list(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const int *ipt,
               const int *k1, const int *k2, const int *k3, const int *k4, const double *cdata,
-              int blo0, int nwin, int nw, void *dev, cudaStream_t ss, ListPlan &P) {
+              int blo0, int nwin, int nw, void *dev, cudaStream_t ss, ListPlan &P,
+              const int *wstart = nullptr) {
   const DeviceGrid &g = c->g;
   const int ns = g.ns, ks = g.ks, ms = g.ms;
   int rc;
@@ -636,13 +637,17 @@ int plan_list(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const int *ip
   if (is_structure_list(icase, itype)) {
     StructPlan *sp = nullptr;
     rc = plan_structures(c, icase, itype, kpol, n, ipt, k1, k2, k3, k4, cdata, blo0, nwin, nw,
-                         dev, ss, &sp);
+                         dev, ss, &sp, wstart);
     if (rc) return rc;
     P.sp.reset(sp, free_structure_plan);
     return DBSRG_OK;
   }
   // window of block b in the partition, -1 outside it
   auto wof = [&](int b) -> int {
+    if (wstart) {
+      if (b < wstart[0] || b >= wstart[nw]) return -1;
+      return (int)(std::upper_bound(wstart, wstart + nw + 1, b) - wstart) - 1;
+    }
     if (b < blo0) return -1;
     const int w = (b - blo0) / nwin;
     return w < nw ? w : -1;
@@ -1148,9 +1153,22 @@ int gen_matrix_plain(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const 
 
 int assemble_windows(dbsrg_ctx *c, int nlists, const dbsrg_list *lists, int nwin, int nslot,
                      const std::function<int(int w, double *slot)> &before,
-                     const std::function<int(int w, int blo, int nb, double *slot)> &after) {
+                     const std::function<int(int w, int blo, int nb, double *slot)> &after,
+                     const std::vector<int> *wstart) {
   const int iicc = c->iicc;
-  const int nw = (iicc + nwin - 1) / nwin;
+  const int nw = wstart ? (int)wstart->size() - 1 : (iicc + nwin - 1) / nwin;
+  if (wstart) {
+    const std::vector<int> &ws = *wstart;
+    if (nw < 1 || ws[0] != 1 || ws[nw] != iicc + 1)
+      return set_err(c, DBSRG_EINVAL, "window partition must cover blocks 1..iicc");
+    for (int w = 0; w < nw; w++)
+      if (ws[w + 1] <= ws[w] || ws[w + 1] - ws[w] > nwin)
+        return set_err(c, DBSRG_EINVAL, "window partition: empty or oversized window");
+  }
+  auto wlo_of = [&](int w) { return wstart ? (*wstart)[w] : 1 + w * nwin; };
+  auto wsize = [&](int w) {
+    return wstart ? (*wstart)[w + 1] - (*wstart)[w] : std::min(nwin, iicc - w * nwin);
+  };
   const size_t blk = (size_t)c->g.ms * c->g.ms;
   std::vector<ListPlan> plans((size_t)nlists);
   std::vector<void *> mem((size_t)nlists, nullptr);
@@ -1159,8 +1177,8 @@ int assemble_windows(dbsrg_ctx *c, int nlists, const dbsrg_list *lists, int nwin
   auto slot_of = [&](int w) { return c->hmem + (size_t)(w % nslot) * nwin * blk; };
   auto enter = [&](int w) {
     c->hch = slot_of(w);
-    c->wlo = 1 + w * nwin;
-    c->wcap = nwin;
+    c->wlo = wlo_of(w);
+    c->wcap = wstart ? wsize(w) : nwin;
   };
   auto body = [&]() -> int {
     int rc;
@@ -1177,7 +1195,8 @@ int assemble_windows(dbsrg_ctx *c, int nlists, const dbsrg_list *lists, int nwin
       if (!(mem[l] = cache_alloc(c, plan_bytes(c, L.icase, L.itype, L.ncdata))))
         return set_err(c, DBSRG_ENOMEM, "list state allocation failed");
       if ((rc = plan_list(c, L.icase, L.itype, L.kpol, L.ncdata, L.ipt, L.k1, L.k2, L.k3, L.k4,
-                          L.cdata, 1, nwin, nw, mem[l], c->sstream, plans[l])))
+                          L.cdata, 1, nwin, nw, mem[l], c->sstream, plans[l],
+                          wstart ? wstart->data() : nullptr)))
         return rc;
       DBSRG_TRY(c, cudaEventRecord(c->lready, c->sstream));
       DBSRG_TRY(c, cudaStreamWaitEvent(c->stream, c->lready, 0));
@@ -1185,14 +1204,13 @@ int assemble_windows(dbsrg_ctx *c, int nlists, const dbsrg_list *lists, int nwin
       prepared = true;
       if ((rc = exec_list(c, plans[l], 0))) return rc;
     }
-    if ((rc = after(0, 1, std::min(nwin, iicc), c->hch))) return rc;
+    if ((rc = after(0, 1, wsize(0), c->hch))) return rc;
     for (int w = 1; w < nw; w++) {
       enter(w);
       if ((rc = before(w, c->hch))) return rc;
       for (int l = 0; l < nlists; l++)
         if (lists[l].ncdata > 0 && (rc = exec_list(c, plans[l], w))) return rc;
-      const int blo = 1 + w * nwin;
-      if ((rc = after(w, blo, std::min(nwin, iicc - blo + 1), c->hch))) return rc;
+      if ((rc = after(w, wlo_of(w), wsize(w), c->hch))) return rc;
     }
     return DBSRG_OK;
   };

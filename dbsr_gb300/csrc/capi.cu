@@ -749,7 +749,20 @@ int dbsrg_assemble_to_host(dbsrg_ctx *c, int nlists, const dbsrg_list *lists, in
     DBSRG_TRY(c, cudaEventRecord(c->cdone[w % nslot], c->cstream));
     return DBSRG_OK;
   };
-  const int rc = assemble_windows(c, nlists, lists, nwin, nslot, before, after);
+  // windows of nwin blocks, the first and the last an eighth of that: the
+  // first window's assembly and the last window's copy are the parts that
+  // nothing overlaps
+  std::vector<int> ws;
+  const int edge = std::max(1, nwin / 8);
+  if (nslot == 2 && iicc > 2 * nwin) {
+    ws.push_back(1);
+    ws.push_back(1 + edge);
+    while (iicc + 1 - ws.back() > nwin + edge) ws.push_back(ws.back() + nwin);
+    ws.push_back(iicc + 1 - edge);
+    ws.push_back(iicc + 1);
+  }
+  const int rc =
+      assemble_windows(c, nlists, lists, nwin, nslot, before, after, ws.empty() ? nullptr : &ws);
   const cudaError_t ce = cudaStreamSynchronize(c->cstream);
   if (rc) return rc;
   if (ce != cudaSuccess) return cuda_check(c, ce, "assemble_to_host copy");

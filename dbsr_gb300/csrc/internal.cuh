@@ -342,11 +342,14 @@ int exchange_contract(dbsrg_ctx *c, const double *rkb, int nsg, const double *X,
 int split_channel_basis(dbsrg_ctx *c, const double *D, const int *nsol);
 // Every list set up once, then executed window by window over the blocks
 // (windows of nwin blocks alternating between nslot slots of the matrix
-// allocation): before(w, slot) prepares a slot (on the contraction stream),
-// after(w, blo, nb, slot) takes the assembled window.  Drains at the end.
+// allocation; or, with wstart, the windows [wstart[w], wstart[w+1]) of at
+// most nwin blocks, wstart[0] = 1 and wstart[nw] = iicc + 1): before(w,
+// slot) prepares a slot (on the contraction stream), after(w, blo, nb, slot)
+// takes the assembled window.  Drains at the end.
 int assemble_windows(dbsrg_ctx *c, int nlists, const dbsrg_list *lists, int nwin, int nslot,
                      const std::function<int(int w, double *slot)> &before,
-                     const std::function<int(int w, int blo, int nb, double *slot)> &after);
+                     const std::function<int(int w, int blo, int nb, double *slot)> &after,
+                     const std::vector<int> *wstart = nullptr);
 
 // ---- structures.cu --------------------------------------------------------
 // The list structures whose terms are not channel-pair contractions: R_data
@@ -362,7 +365,7 @@ size_t structure_plan_bytes(const dbsrg_ctx *c, int icase, int itype, int n);
 int plan_structures(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const int *ipt,
                     const int *k1, const int *k2, const int *k3, const int *k4,
                     const double *cdata, int blo0, int nwin, int nw, void *dev,
-                    cudaStream_t ss, StructPlan **out);
+                    cudaStream_t ss, StructPlan **out, const int *wstart = nullptr);
 int exec_structures(dbsrg_ctx *c, const StructPlan &P, int w, bool prep);
 void free_structure_plan(StructPlan *P);
 // zeroes hcp, hp, htarg, otarg (with the matrix); frees them (destroy)

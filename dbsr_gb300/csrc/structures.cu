@@ -374,10 +374,15 @@ namespace {
 struct Builder {
   dbsrg_ctx *c;
   int blo0, nwin, nw;
+  const int *wstart;  // explicit window starts (nw + 1), or null
   std::vector<std::pair<int, StTerm>> bterms;  // (block, term)
   std::vector<std::pair<int, StTerm>> hvterms; // (hcp column, term)
   std::vector<std::pair<long long, StTerm>> scterms;  // (array*2^40 + index, term)
   int wof(int b) const {
+    if (wstart) {
+      if (b < wstart[0] || b >= wstart[nw]) return -1;
+      return (int)(std::upper_bound(wstart, wstart + nw + 1, b) - wstart) - 1;
+    }
     if (b < blo0) return -1;
     const int w = (b - blo0) / nwin;
     return w < nw ? w : -1;
@@ -470,7 +475,7 @@ int fetch(dbsrg_ctx *c, std::vector<T> &out, const T *src, int n) {
 int plan_structures(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const int *ipt,
                     const int *k1, const int *k2, const int *k3, const int *k4,
                     const double *cdata, int blo0, int nwin, int nw, void *dev,
-                    cudaStream_t ss, StructPlan **out) {
+                    cudaStream_t ss, StructPlan **out, const int *wstart) {
   const int ns = c->g.ns, ks = c->g.ks, nbf = c->nbf;
   int rc;
   auto P = std::unique_ptr<StructPlan>(new StructPlan());
@@ -499,7 +504,7 @@ int plan_structures(dbsrg_ctx *c, int icase, int itype, int kpol, int n, const i
   }
   for (int e = 0; e < n; e++)
     if (!std::isfinite(hc[e])) return set_err(c, DBSRG_EINVAL, "non-finite coefficient in list");
-  Builder B{c, blo0, nwin, nw, {}, {}, {}};
+  Builder B{c, blo0, nwin, nw, wstart, {}, {}, {}};
   auto orb_ok = [&](int o) { return o >= 1 && o <= nbf; };
   std::vector<int2> pots, vjobs, ljobs;
   std::vector<int> epot(n, -1), ej1(n, 0), ej2(n, 0), elv(n, -1);

@@ -175,11 +175,14 @@ int dbsrg_gen_batch_streamed(int nctx, dbsrg_ctx *const *ctxs,
 
 /* The whole assembly of one context straight into a caller's matrix
  * hch_host(ms,ms,iicc) (host, best pinned, or device) and acf_host
- * (iicc,0:mk) (may be NULL): the lists run once per window of nwin blocks
- * (nwin <= 0: iicc/8; every list is set up once, its work split by
- * window), windows alternating between two halves of the device
- * allocation, and while one window is assembled the previous one is copied
- * out on a separate stream, so the copy hides behind the assembly.
+ * (iicc,0:mk) (may be NULL): the lists run once per window of at most
+ * nwin blocks (nwin <= 0: from the tuned window count; every list is set up
+ * once, its work split by window), windows alternating between two halves
+ * of the device allocation, and while one window is assembled the previous
+ * one is copied out on a separate stream, so the copy hides behind the
+ * assembly.  With more than two windows' worth of blocks the first and the
+ * last window hold max(1, nwin/8) blocks: the first window's assembly and
+ * the last window's copy are what nothing overlaps.
  * The allocation must hold two windows (or nwin >= iicc).  The device
  * matrix is overwritten; acf, and the perturber and target parts when
  * held, are zeroed first and hold the list's terms at the end (read them
