@@ -212,16 +212,25 @@ __global__ void __launch_bounds__(NTHR) k_sgemm(const GemmJob *jobs, int nk, int
 #pragma unroll
     for (int c = 0; c < 16; c++) acc[c] = 0, cur[c] = NO_EXP;
     bool dead = false;
+    // the chunk's row exponent and its 16 column exponents (64-byte aligned),
+    // loaded one chunk ahead of their use
+    int er_n;
+    int4 en[4];
+    auto exps = [&](int kc) {
+      er_n = jb.ea[(size_t)kc * jb.NRa * 32 + r];
+      const int4 *ep =
+          reinterpret_cast<const int4 *>(jb.eb + (size_t)kc * jb.NRb * 32 + nt * 32 + ch * 16);
+#pragma unroll
+      for (int u = 0; u < 4; u++) en[u] = ep[u];
+    };
+    exps(0);
     for (int kc = 0; kc < nk; kc++) {
       const int s = kc & 1;
       const uint32_t n = (uint32_t)(kc >> 1);
-      // the chunk's row exponent and the 16 column exponents (64-byte aligned)
-      const int er = jb.ea[(size_t)kc * jb.NRa * 32 + r];
-      const int4 *ep =
-          reinterpret_cast<const int4 *>(jb.eb + (size_t)kc * jb.NRb * 32 + nt * 32 + ch * 16);
-      const int4 e0 = ep[0], e1 = ep[1], e2 = ep[2], e3 = ep[3];
-      const int ec[16] = {e0.x, e0.y, e0.z, e0.w, e1.x, e1.y, e1.z, e1.w,
-                          e2.x, e2.y, e2.z, e2.w, e3.x, e3.y, e3.z, e3.w};
+      const int er = er_n;
+      const int ec[16] = {en[0].x, en[0].y, en[0].z, en[0].w, en[1].x, en[1].y, en[1].z, en[1].w,
+                          en[2].x, en[2].y, en[2].z, en[2].w, en[3].x, en[3].y, en[3].z, en[3].w};
+      if (kc + 1 < nk) exps(kc + 1);
       if (!dead && *abort_flag) dead = true;
       bool ok = !dead && mbar_wait(smem_u32(&bar_mma[s]), n & 1, WAIT_NS);
       ok = __all_sync(0xffffffffu, ok);
