@@ -360,6 +360,15 @@ __device__ __forceinline__ void cp_async8(uint32_t dst, const void *src, bool va
                : "memory");
 }
 
+// hch[dst .. dst + bytes) += smem[src ..] as one asynchronous bulk
+// reduction (FP64 add in L2, one add per element: the same rounding as an
+// FP64 add on the SM); 16-byte aligned addresses, bytes a multiple of 16
+__device__ __forceinline__ void bulk_reduce_add_f64(double *dst, uint32_t src, uint32_t bytes) {
+  asm volatile("cp.reduce.async.bulk.global.shared::cta.bulk_group.add.f64 [%0], [%1], %2;\n" ::"l"(dst),
+               "r"(src), "r"(bytes)
+               : "memory");
+}
+
 __device__ __forceinline__ void mbar_arrive(uint32_t mbar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(mbar) : "memory");
 }
@@ -372,12 +381,17 @@ __device__ __forceinline__ void mbar_arrive(uint32_t mbar) {
 //    product's operands and for the consumers to have read the TMEM set two
 //    products back, issues the MMAs and commits them;
 //  * stager (warp NCW+1, even ns): per tile waits until the consumers are
-//    done with the tile two back, then bulk-loads the tile's hch columns and
-//    the band rows of its terms (one copy per lane) into the staging buffers
-//    that tile used, so the copies run a tile ahead of the consumers;
+//    done with the tile two back, adds that tile's results into hch with
+//    one asynchronous bulk reduction per column (cp.reduce.async.bulk
+//    .add.f64: the FP64 add happens in L2, so hch is neither loaded into the
+//    SM nor added there), waits until the reduction has read the buffer,
+//    then bulk-loads the band rows of the new tile's terms (one copy per
+//    lane) into the buffers that tile used, a tile ahead of the consumers;
 //  * consumers (warps 0..NCW-1): per product read the TMEM set, release it
 //    and add the product into int64 accumulators; per tile convert, add the
-//    band, add hch, store, and release the staging buffers.
+//    band, write the results into the tile's result buffer and release it.
+//    (Odd ns: the consumers stage hch and the band themselves with 8-byte
+//    copies and write hch + result to global memory.)
 // 18 warps: two SM sub-partitions hold 5 of them, and a sub-partition has
 // 16384 registers, so at most 96 registers a thread.  Four consumer warps per
 // sub-partition hide each other's TMEM and integer latencies.
@@ -538,12 +552,31 @@ __global__ void __maxnreg__(96) k_xfused(const XArgs p) {
   } else if (warp == WSTAGE) {
     // ------------------------------------------------------------ stager
     if (bulk) {
-      // two staging buffers (hch columns and band rows of a tile): tile n
-      // goes to buffer n & 1 once the consumers have released tile n - 2,
-      // so the copies of the next tile overlap the consumers' current one
+      // two buffer pairs (the results and the band rows of a tile): tile n
+      // takes pair n & 1 once the consumers have released tile n - 2 and
+      // its results have been reduced into hch, so the band copies of the
+      // next tile overlap the consumers' current one
       uint32_t nst = 0;  // tiles staged
       long long last_n[2] = {-1, -1};
       bool fail = false;
+      // the hch columns of the tile each buffer holds the results of: the
+      // tile's first column in hch, its rows and columns
+      double *pdst[2] = {nullptr, nullptr};
+      int prow[2] = {0, 0}, pcol[2] = {0, 0};
+      // add buffer s's results into hch once the consumers have written them
+      // (waited before), and wait until the reduction has read the buffer
+      auto reduce = [&](int s) {
+        if (pdst[s] && *abort_flag == 0) {
+          if (lane < pcol[s])
+            bulk_reduce_add_f64(pdst[s] + ms * (size_t)lane,
+                                smem_u32(shch + (size_t)s * 32 * 128 + (size_t)lane * 128),
+                                (uint32_t)prow[s] * 8);
+          asm volatile("cp.async.bulk.commit_group;\n" ::: "memory");
+          asm volatile("cp.async.bulk.wait_group.read 0;\n" ::: "memory");
+        }
+        pdst[s] = nullptr;
+        __syncwarp();
+      };
       Row r;
       for (int row = blockIdx.x; row < p.nrows && !fail; row += gridDim.x) {
         load_row(p, row, r);
@@ -564,14 +597,14 @@ __global__ void __maxnreg__(96) k_xfused(const XArgs p) {
             fail = true;
             break;
           }
+          reduce(s);  // tile nst - 2's results, before the buffer is reused
           // rows of diagonal dd of a direct term's band: band_row0 .. hi | 1
           // (both even-aligned ends inside the tile's rows and below ns)
           const int hib = min(x0 + 127, p.ns - 1);
-          double *sh = shch + (size_t)s * 32 * 128;
           double *sb = sband + (size_t)s * MAXT * NDB * BR;
           const uint32_t tb = smem_u32(&bar_tile[s]);
           if (lane == 0) {
-            uint32_t bytes = (uint32_t)(ncol * nrow * 8);
+            uint32_t bytes = 0;  // the band rows (hch is added by a bulk reduction)
             if (band)
               for (int t = 0; t < r.nt; t++) {
                 if ((term_code(r, t) >> 2) & 1) {
@@ -588,9 +621,9 @@ __global__ void __maxnreg__(96) k_xfused(const XArgs p) {
             mbar_expect_tx(tb, bytes);
           }
           __syncwarp();
-          if (lane < ncol)
-            bulk_g2s(smem_u32(sh + (size_t)lane * 128), hq + ms * (size_t)(ty0 + lane) + x0,
-                     (uint32_t)nrow * 8, tb);
+          pdst[s] = const_cast<double *>(hq) + ms * (size_t)ty0 + x0;
+          prow[s] = nrow;
+          pcol[s] = ncol;
           if (band)
             for (int k = lane; k < NDB * r.nt; k += 32) {
               const int t = k / NDB, dd = k % NDB, tc = term_code(r, t);
@@ -610,11 +643,25 @@ __global__ void __maxnreg__(96) k_xfused(const XArgs p) {
           nst++;
         }
       }
+      // the results of the last two staged tiles, once their consumers are done
+      for (long long k = (long long)nst - 2; !fail && k < (long long)nst; k++) {
+        if (k < 0) continue;
+        const int s = (int)(k & 1);
+        bool ok = mbar_wait(smem_u32(&bar_sfree[s]), (uint32_t)((k >> 1) & 1), p.wait_ns);
+        ok = __all_sync(0xffffffffu, ok);
+        if (!ok) {
+          fail = true;
+          break;
+        }
+        reduce(s);
+      }
       if (fail && lane == 0) {
         *abort_flag = 1;
         atomicExch(p.err, 1);
       }
-      // the copies of the last staged tiles land before the CTA exits
+      // the reductions complete, and the copies of the last staged tiles
+      // land, before the CTA exits
+      asm volatile("cp.async.bulk.wait_group 0;\n" ::: "memory");
       if (lane == 0)
         for (int s = 0; s < 2; s++)
           if (last_n[s] >= 0)
@@ -806,18 +853,25 @@ __global__ void __maxnreg__(96) k_xfused(const XArgs p) {
             }
           }
         }
-        if (row_ok && !dead) {
-#pragma unroll
-          for (int c = 0; c < CPT; c++)
-            if (y0 + c < p.ns) h[ms * c] = sh[(size_t)(cg * CPT + c) * 128 + xl] + val[c];
-        }
-        // release the staging buffers
         if (bulk) {
+          // the results into the buffer; the stager adds the buffer into hch
+          // (one bulk reduction per column) before the buffer is reused
+          if (!dead) {
+            double *so = const_cast<double *>(sh);
+#pragma unroll
+            for (int c = 0; c < CPT; c++) so[(size_t)(cg * CPT + c) * 128 + xl] = val[c];
+          }
+          asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
           __syncwarp();
           if (lane == 0) mbar_arrive(smem_u32(&bar_sfree[sbuf]));
           ntile++;
-        } else if (band) {
-          consumers_sync();
+        } else {
+          if (row_ok && !dead) {
+#pragma unroll
+            for (int c = 0; c < CPT; c++)
+              if (y0 + c < p.ns) h[ms * c] = sh[(size_t)(cg * CPT + c) * 128 + xl] + val[c];
+          }
+          if (band) consumers_sync();
         }
       }
     }
