@@ -128,9 +128,9 @@ class Clocks:
 # carried to the 120-channel launches.  At 40 channels the 129 MB L2 holds a
 # larger share of a launch's tiles than at 120, so the carried figure is a
 # lower estimate of the full-size traffic.  None: no traffic reported.
-XFUSED_TRAFFIC_PER_ALGORITHMIC_BYTE = 0.891
+XFUSED_TRAFFIC_PER_ALGORITHMIC_BYTE = 0.882
 XFUSED_TRAFFIC_SOURCE = ("ncu over the 35 k_xfused launches of one 40-channel step "
-                         "(ns=400, 4.2 GB matrix): 5.105 GB read + 1.997 GB written "
+                         "(ns=400, 4.2 GB matrix): 5.087 GB read + 1.938 GB written "
                          "against 7.967 GB stated algorithmic bytes; ratio carried "
                          "to the 120-channel launches (a lower estimate)")
 
