@@ -17,10 +17,9 @@
 //     (different streams, or host threads) race on it and must be ordered
 //     by the caller;
 //   * the first call on a device (with that device current) looks up the
-//     device address of the array with cudaGetSymbolAddress; make that
-//     first call before any stream capture begins.  The address belongs to
-//     the device's context of that moment: do not use the entry point after
-//     a cudaDeviceReset of the device in the same process;
+//     device address of the array with cudaGetSymbolAddress.  The address
+//     belongs to the device's context of that moment: do not use the entry
+//     point after a cudaDeviceReset of the device in the same process;
 //   * the call is synchronous: it waits on its stream for its own kernels
 //     and for the read-back of its error word before it returns.
 #include <cuda_runtime.h>
