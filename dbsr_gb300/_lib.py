@@ -87,6 +87,7 @@ SIGNATURES = [
     ("dbsrg_gen_batch", C.c_int, [C.c_int, _vp, _vp, _vp]),
     ("dbsrg_gen_batch_streamed", C.c_int, [C.c_int, _vp, _vp, _vp, _vp, _vp]),
     ("dbsrg_assemble_to_host", C.c_int, [_vp, C.c_int, _vp, C.c_int, _vp, _vp]),
+    ("dbsrg_assemble_streamed_host", C.c_int, [_vp, C.c_int, _vp, C.c_int, _vp, _vp, _vp, _vp]),
     ("dbsrg_backward", C.c_int, [_vp, C.c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     ("dbsrg_alloc_perturbers", C.c_int, [_vp, C.c_int, _vp, C.c_int, _vp, C.c_int]),
     ("dbsrg_get_perturbers", C.c_int, [_vp, _vp, _vp]),

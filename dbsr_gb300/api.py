@@ -137,6 +137,49 @@ class Assembler:
         check(self._h, rc, "assemble_to_host")
         return out, acf
 
+    def assemble_streamed(self, lists, stage, consumer, acf=None, nwin: int = 0):
+        """dbsrg_assemble_streamed_host: every list, window by window of at most
+        `nwin` blocks, each window copied into one half of `stage` (room for
+        2*nwin blocks of ms x ms; numpy or torch, host -- pinned for the
+        overlap -- or device) while the next window is assembled.
+        consumer(blo, nblocks, view) runs on this thread for every window, in
+        block order, once its copy is complete; `view` is the window's part of
+        `stage` as (ms, ms, nblocks), valid until the consumer returns.  An
+        exception in the consumer is raised when the call returns.  Returns
+        acf (iicc, 0:mk)."""
+        if acf is None:
+            acf = np.zeros((self.iicc, self.mk + 1), order="F")
+        arr, keep, counts = _list_descs([lists])
+        ps, hold = _ptr(stage, np.float64)
+        pa, k2 = _ptr(acf, np.float64)
+        if hasattr(hold, "data_ptr"):
+            flat, base = hold.view(-1), int(hold.data_ptr())
+        else:
+            flat, base = hold.ravel(order="K"), int(hold.ctypes.data)
+        ms = self.ms
+        errors = []
+
+        def fn(user, ictx, blo, nblocks, ptr):
+            if errors:
+                return
+            try:
+                off = (int(ptr) - base) // 8
+                n = int(nblocks) * ms * ms
+                view = flat[off:off + n]
+                view = view.reshape(int(nblocks), ms, ms).permute(2, 1, 0) if hasattr(
+                    view, "permute") else view.reshape((ms, ms, int(nblocks)), order="F")
+                consumer(int(blo), int(nblocks), view)
+            except BaseException as e:  # surfaces after the call
+                errors.append(e)
+
+        cb = _lib.WindowFn(fn)
+        rc = self._L.dbsrg_assemble_streamed_host(self._h, counts[0], arr, int(nwin), ps,
+                                                  C.cast(cb, C.c_void_p), None, pa)
+        if errors:
+            raise errors[0]
+        check(self._h, rc, "assemble_streamed")
+        return acf
+
     def set_window(self, blo: int):
         """Hold (and zero) blocks blo .. blo + window - 1."""
         check(self._h, self._L.dbsrg_set_window(self._h, int(blo)), "set_window")

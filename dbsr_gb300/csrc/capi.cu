@@ -713,6 +713,25 @@ int dbsrg_gen_batch_streamed(int nctx, dbsrg_ctx *const *ctxs, const int *nlists
   return DBSRG_OK;
 }
 
+// The window partition of the assemblies that copy windows out while the
+// next one is assembled: windows of nwin blocks, the first and the last
+// max(1, nwin/8) blocks when two device slots alternate over more than two
+// windows' worth of blocks -- the first window's assembly and the last
+// window's copy are the parts that nothing overlaps.  Empty: plain windows
+// of nwin blocks.
+static std::vector<int> host_windows(int iicc, int nwin, int nslot) {
+  std::vector<int> ws;
+  const int edge = std::max(1, nwin / 8);
+  if (nslot == 2 && iicc > 2 * nwin) {
+    ws.push_back(1);
+    ws.push_back(1 + edge);
+    while (iicc + 1 - ws.back() > nwin + edge) ws.push_back(ws.back() + nwin);
+    ws.push_back(iicc + 1 - edge);
+    ws.push_back(iicc + 1);
+  }
+  return ws;
+}
+
 int dbsrg_assemble_to_host(dbsrg_ctx *c, int nlists, const dbsrg_list *lists, int nwin,
                            double *hch_host, double *acf_host) {
   if (!c) return DBSRG_EINVAL;
@@ -749,23 +768,76 @@ int dbsrg_assemble_to_host(dbsrg_ctx *c, int nlists, const dbsrg_list *lists, in
     DBSRG_TRY(c, cudaEventRecord(c->cdone[w % nslot], c->cstream));
     return DBSRG_OK;
   };
-  // windows of nwin blocks, the first and the last an eighth of that: the
-  // first window's assembly and the last window's copy are the parts that
-  // nothing overlaps
-  std::vector<int> ws;
-  const int edge = std::max(1, nwin / 8);
-  if (nslot == 2 && iicc > 2 * nwin) {
-    ws.push_back(1);
-    ws.push_back(1 + edge);
-    while (iicc + 1 - ws.back() > nwin + edge) ws.push_back(ws.back() + nwin);
-    ws.push_back(iicc + 1 - edge);
-    ws.push_back(iicc + 1);
-  }
+  const std::vector<int> ws = host_windows(iicc, nwin, nslot);
   const int rc =
       assemble_windows(c, nlists, lists, nwin, nslot, before, after, ws.empty() ? nullptr : &ws);
   const cudaError_t ce = cudaStreamSynchronize(c->cstream);
   if (rc) return rc;
   if (ce != cudaSuccess) return cuda_check(c, ce, "assemble_to_host copy");
+  if (acf_host) return copy_out(c, acf_host, c->acf, sizeof(double) * (size_t)iicc * (c->mk + 1));
+  return DBSRG_OK;
+}
+
+int dbsrg_assemble_streamed_host(dbsrg_ctx *c, int nlists, const dbsrg_list *lists, int nwin,
+                                 double *stage, dbsrg_window_fn fn, void *user,
+                                 double *acf_host) {
+  if (!c) return DBSRG_EINVAL;
+  if (nlists < 0 || (nlists > 0 && !lists) || !stage || !fn)
+    return set_err(c, DBSRG_EINVAL, "assemble_streamed_host: bad arguments");
+  if (!c->hmem) return set_err(c, DBSRG_ESTATE, "no matrix allocated");
+  cudaSetDevice(c->device);
+  SETTLE(c);
+  const int iicc = c->iicc;
+  if (nwin <= 0) nwin = std::max(1, (iicc + c->tune_windows - 1) / c->tune_windows);
+  nwin = std::min(nwin, iicc);
+  const int nslot = nwin < iicc ? 2 : 1;
+  if (nslot * nwin > c->hcap)
+    return set_err(c, DBSRG_EINVAL, "assemble_streamed_host: two windows must fit the allocation");
+  const size_t blk = (size_t)c->g.ms * c->g.ms;
+  const cudaMemcpyKind kind =
+      is_device_ptr(stage) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  DBSRG_TRY(c, cudaMemsetAsync(c->acf, 0, sizeof(double) * (size_t)iicc * (c->mk + 1), c->stream));
+  int rz = zero_structures(c);
+  if (rz) return rz;
+  // window w: assembled in device slot w % 2 on the contraction stream,
+  // copied into stage half w % 2 on the copy stream; handed to fn once its
+  // copy is complete, which the host waits for right after it has queued
+  // window w + 1 (so the device assembles w + 1 meanwhile).  Half w % 2 is
+  // written again by window w + 2, queued only after that hand-over.
+  int pend = -1, pend_blo = 0, pend_nb = 0;  // copied or in flight, not handed over
+  auto hand = [&]() -> int {
+    if (pend < 0) return DBSRG_OK;
+    DBSRG_TRY(c, cudaEventSynchronize(c->cdone[pend % nslot]));
+    fn(user, 0, pend_blo, pend_nb, stage + (size_t)(pend % nslot) * nwin * blk);
+    pend = -1;
+    return DBSRG_OK;
+  };
+  auto before = [&](int w, double *slot) -> int {
+    DBSRG_TRY(c, cudaStreamWaitEvent(c->stream, c->cdone[w % nslot], 0));
+    DBSRG_TRY(c, cudaMemsetAsync(slot, 0, sizeof(double) * blk * nwin, c->stream));
+    return DBSRG_OK;
+  };
+  auto after = [&](int w, int blo, int nb, double *slot) -> int {
+    DBSRG_TRY(c, cudaEventRecord(c->wdone, c->stream));
+    DBSRG_TRY(c, cudaStreamWaitEvent(c->cstream, c->wdone, 0));
+    DBSRG_TRY(c, cudaMemcpyAsync(stage + (size_t)(w % nslot) * nwin * blk, slot,
+                                 sizeof(double) * blk * nb, kind, c->cstream));
+    DBSRG_TRY(c, cudaEventRecord(c->cdone[w % nslot], c->cstream));
+    const int r = hand();  // window w - 1
+    if (r) return r;
+    pend = w;
+    pend_blo = blo;
+    pend_nb = nb;
+    return DBSRG_OK;
+  };
+  const std::vector<int> ws = host_windows(iicc, nwin, nslot);
+  const int rc =
+      assemble_windows(c, nlists, lists, nwin, nslot, before, after, ws.empty() ? nullptr : &ws);
+  const cudaError_t ce = cudaStreamSynchronize(c->cstream);
+  if (rc) return rc;
+  if (ce != cudaSuccess) return cuda_check(c, ce, "assemble_streamed_host copy");
+  const int rh = hand();  // the last window
+  if (rh) return rh;
   if (acf_host) return copy_out(c, acf_host, c->acf, sizeof(double) * (size_t)iicc * (c->mk + 1));
   return DBSRG_OK;
 }

@@ -191,6 +191,24 @@ int dbsrg_gen_batch_streamed(int nctx, dbsrg_ctx *const *ctxs,
 int dbsrg_assemble_to_host(dbsrg_ctx *ctx, int nlists, const dbsrg_list *lists,
                            int nwin, double *hch_host, double *acf_host);
 
+/* The same assembly streamed through a caller's staging area instead of a
+ * whole host matrix, for matrices larger than the host memory set aside
+ * for them: stage holds two windows (2*nwin blocks of ms x ms; one window
+ * when nwin >= iicc), host memory (pinned, for the overlap) or device
+ * memory.  Window w is copied into half w % 2 of stage while window w+1 is
+ * assembled; once that copy is complete, fn(user, 0, blo, nblocks, half)
+ * runs on the calling thread with the window's blocks blo .. blo+nblocks-1
+ * (hch layout) and may read them until it returns, the device meanwhile
+ * assembling the next window.  Windows, their sizes (first and last
+ * window short), nwin <= 0, the allocation rule, acf_host and the zeroed
+ * parts are as for dbsrg_assemble_to_host.  No counterpart in DBSR_MAT3,
+ * which holds the whole matrix (updates.f90:2-76) and writes it with
+ * Record_matrix. */
+int dbsrg_assemble_streamed_host(dbsrg_ctx *ctx, int nlists,
+                                 const dbsrg_list *lists, int nwin,
+                                 double *stage, dbsrg_window_fn fn,
+                                 void *user, double *acf_host);
+
 /* UPDATE_HX(ich,jch,d,C) (updates.f90:79-106): add C*d (d is ms x ms,
  * host or device) to the block of channel pair (ich,jch). */
 int dbsrg_update_hx(dbsrg_ctx *ctx, int ich, int jch, const double *d,
@@ -526,10 +544,9 @@ int dbsrg_timing_report(dbsrg_ctx *ctx, char *buf, size_t len);
  * (larger ns returns DBSRG_ERANGE, as do orbital indices outside 1..nbf).
  * The array is shared by all calls on a device: calls that overlap on the
  * GPU race and must be ordered by the caller.  The first call on a device
- * sets up the array's address (cudaGetSymbolAddress) and must come before
- * any stream capture; that address belongs to the device's context of the
- * moment, so the entry point must not be used after a cudaDeviceReset of
- * the device in the same process.  The call is synchronous: it waits on
+ * sets up the array's address (cudaGetSymbolAddress); that address belongs
+ * to the device's context of the moment, so the entry point must not be
+ * used after a cudaDeviceReset of the device in the same process.  The call is synchronous: it waits on
  * its stream for its own kernels and the read-back of its error word. */
 int dbsrg_exchange_segment_noalloc(int ns, int ks, const double *rkb,
                                    const double *pq, int nbf, int jp1,

@@ -145,3 +145,71 @@ def test_assemble_to_host_needs_two_windows():
     out, _ = a.assemble_to_host(items(w), nwin=2)
     a.close()
     assert np.array_equal(out, full(w, SPLIT_BF16)[0])
+
+
+@pytest.mark.parametrize("nwin", [1, 3, 6, 0, 10 ** 6])
+@pytest.mark.parametrize("where", ["pinned", "pageable", "device"])
+def test_assemble_streamed_equals_whole_assembly(nwin, where):
+    """dbsrg_assemble_streamed_host: the windows handed to the consumer, in
+    block order and each at most nwin blocks, put together equal the whole
+    assembly bit for bit (acf too), from a staging area of two windows."""
+    torch = pytest.importorskip("torch")
+    w = synth.small(ns=60, nch=5, mk=3, n_entries=2000, seed=55)
+    h0, acf0 = full(w, SPLIT_BF16)
+    a = make(w, SPLIT_BF16)
+    ms = a.ms
+    eff = nwin if nwin > 0 else -(-w.iicc // a.get_tuning("windows"))
+    eff = min(eff, w.iicc)
+    nstage = (2 if eff < w.iicc else 1) * eff * ms * ms
+    if where == "device":
+        stage = torch.zeros(nstage, dtype=torch.float64, device="cuda")
+    elif where == "pinned":
+        stage = torch.zeros(nstage, dtype=torch.float64).pin_memory()
+    else:
+        stage = np.zeros(nstage)
+    a.gen_matrix(*items(w)[0])  # leftovers in the device matrix must not matter
+    got, nxt = [], [1]
+
+    def consume(blo, nb, view):
+        assert blo == nxt[0] and 1 <= nb <= eff
+        nxt[0] = blo + nb
+        v = view.cpu().numpy() if hasattr(view, "cpu") else view
+        assert v.shape == (ms, ms, nb)
+        got.append(np.array(v))
+
+    acf = a.assemble_streamed(items(w), stage, consume, nwin=nwin)
+    assert nxt[0] == w.iicc + 1
+    assert np.array_equal(np.concatenate(got, axis=2), h0)
+    assert np.array_equal(acf, acf0)
+    a.close()
+
+
+def test_assemble_streamed_consumer_error_and_reuse():
+    """An exception in the consumer is raised when the call returns; the
+    context stays usable and a second call delivers the matrix again."""
+    w = synth.small(ns=50, nch=4, mk=2, n_entries=600, seed=56)
+    h0, _ = full(w, SPLIT_BF16)
+    a = make(w, SPLIT_BF16)
+    stage = np.zeros(2 * 3 * a.ms * a.ms)
+
+    def bad(blo, nb, view):
+        raise RuntimeError("consumer failed")
+
+    with pytest.raises(RuntimeError, match="consumer failed"):
+        a.assemble_streamed(items(w), stage, bad, nwin=3)
+    parts = []
+    a.assemble_streamed(items(w), stage, lambda blo, nb, v: parts.append(np.array(v)), nwin=3)
+    assert np.array_equal(np.concatenate(parts, axis=2), h0)
+    a.close()
+
+
+def test_assemble_streamed_needs_two_windows():
+    w = synth.small(ns=50, nch=4, mk=2, n_entries=300, seed=57)
+    a = make(w, SPLIT_BF16, window=4)  # 4 of 10 blocks allocated
+    stage = np.zeros(2 * 3 * a.ms * a.ms)
+    with pytest.raises(DbsrgError, match="EINVAL"):
+        a.assemble_streamed(items(w), stage, lambda *x: None, nwin=3)
+    parts = []
+    a.assemble_streamed(items(w), stage, lambda blo, nb, v: parts.append(np.array(v)), nwin=2)
+    a.close()
+    assert np.array_equal(np.concatenate(parts, axis=2), full(w, SPLIT_BF16)[0])
