@@ -440,28 +440,35 @@ __global__ void k_scatter(int ns, int ks, int mode, ScatterSpec sp, int nm, cons
   if (touched) *h = val;
 }
 
-// asymptotic coefficients (UPDATE_ACF, R_data.f90:223-240): one thread per
-// owner segment, atypes 0 and 1, list order.
+// asymptotic coefficients (UPDATE_ACF, R_data.f90:223-240): one warp per
+// owner segment (owners have distinct blocks); per atype 0, 1 and per
+// segment (the owner, then its partner) the lanes sum every 32nd entry and
+// a butterfly combines the lanes, and the sum is added to acf in that order.
+constexpr int ACF_WARPS = 4;  // warps per block
 __global__ void k_acf(int nseg_owner, const int *owners, const SegInfo *info, int kpol,
                       int nbf, const int *k2, const int *k3, const double *cd,
                       const double *quad, double *acf, int iicc) {
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const int t = blockIdx.x * ACF_WARPS + threadIdx.x / 32;
   if (t >= nseg_owner) return;
-  int s = owners[t];
-  SegInfo si = info[s];
+  const int s = owners[t];
+  const SegInfo si = info[s];
   if (si.blk < 1) return;
   double *dst = acf + (size_t)(si.blk - 1) + (size_t)iicc * kpol;
   for (int a = 0; a < 2; a++) {
     for (int pass = 0; pass < 2; pass++) {
-      int ss = pass == 0 ? s : si.partner;
+      const int ss = pass == 0 ? s : si.partner;
       if (pass == 1 && ss < 0) break;
-      SegInfo sj = info[ss];
+      const SegInfo sj = info[ss];
       double CA = 0.0;
-      for (int e = sj.start; e < sj.end; e++) {
-        double S = quad[(size_t)(k2[e] - 1) + (size_t)nbf * ((k3[e] - 1) + (size_t)nbf * a)];
+      for (int e = sj.start + lane; e < sj.end; e += 32) {
+        const double S =
+            quad[(size_t)(k2[e] - 1) + (size_t)nbf * ((k3[e] - 1) + (size_t)nbf * a)];
         CA = CA + cd[e] * S;
       }
-      *dst = *dst + CA;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) CA += __shfl_xor_sync(0xffffffffu, CA, o);
+      if (lane == 0) *dst = *dst + CA;
     }
   }
 }
@@ -919,8 +926,11 @@ int exec_list(dbsrg_ctx *c, const ListPlan &P, int w, bool prep = false) {
     if (prep) return DBSRG_OK;
     const int t0 = P.wtl[w], nt = P.wtl[w + 1] - t0;
     if (nt <= 0) return DBSRG_OK;
-    DBSRG_RUN(c, "k_vch", k_vch<<<(2 * ns * c->nbf + 255) / 256, 256, 0, st>>>(
-                              ns, c->nbf, g.fpbs, g.fqbs, c->pq, P.vch));
+    // the overlap vectors depend on the orbitals only: built by the first
+    // window with blocks of this list, kept by the plan for the later ones
+    if (t0 == P.wtl[0])
+      DBSRG_RUN(c, "k_vch", k_vch<<<(2 * ns * c->nbf + 255) / 256, 256, 0, st>>>(
+                                ns, c->nbf, g.fpbs, g.fqbs, c->pq, P.vch));
     for (int t = 0; t < nt; t += 65535) {  // grid z limit
       const int nz = std::min(65535, nt - t);
       dim3 grid((unsigned)((ms + 127) / 128), (unsigned)((ms + 31) / 32), (unsigned)nz);
@@ -1043,7 +1053,7 @@ int exec_list(dbsrg_ctx *c, const ListPlan &P, int w, bool prep = false) {
     if ((rc = get_quad(c, P.kpol, &quad))) return rc;
     if (prep) return DBSRG_OK;
     DBSRG_RUN(c, "k_acf",
-              k_acf<<<(nown_acf + 127) / 128, 128, 0, st>>>(
+              k_acf<<<(nown_acf + ACF_WARPS - 1) / ACF_WARPS, 32 * ACF_WARPS, 0, st>>>(
                   nown_acf, P.work + P.own_off + o0, P.info, P.kpol, c->nbf, P.lk2, P.lk3, P.lcd,
                   quad, c->acf, c->iicc));
   }
