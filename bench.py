@@ -63,7 +63,7 @@ def parse():
     p.add_argument("--nblocks", type=int, default=64)
     p.add_argument("--nch-max", type=int, default=300)
     p.add_argument("--batch-group", type=int, default=8, help="J-blocks run concurrently")
-    p.add_argument("--window-gb", type=float, default=4.0, help="device window per J-block")
+    p.add_argument("--window-gb", type=float, default=2.0, help="device window per J-block")
     p.add_argument("--tune", default=None,
                    help="batch: autotune the exchange chunk size first, recording into this table")
     p.add_argument("--rows-entries", type=float, default=1e4)
@@ -511,6 +511,10 @@ def batch_main(args, rank, world, local):
     window), every list run window by window with each window read out, the
     assemblers closed -- tables and pair potentials are built inside the
     step."""
+    # eight contexts of four or five streams each: the default of eight
+    # hardware work queues would make unrelated streams wait behind one
+    # another (set before the process's first CUDA call)
+    os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
     import torch
 
     from dbsr_gb300 import FACTOR_FP64, PLAIN_FP64, SPLIT_BF16, Assembler, synth
@@ -621,6 +625,7 @@ def batch_main(args, rank, world, local):
                        "algorithmic_tflop": flops / 1e12,
                        "group": G, "window_gb": args.window_gb, "tuning": tuning,
                        "output": "every window copied to pinned host memory inside the step",
+                       "cuda_device_max_connections": os.environ.get("CUDA_DEVICE_MAX_CONNECTIONS"),
                        "timing": "host wall clock around the synchronised steps",
                        "parallelism": f"replicas x{world}"},
             "s_per_batch": dt, "d2h_bytes_per_step": stats["d2h"] // max(1, args.steps),
@@ -1044,7 +1049,11 @@ def main():
             c = torch.from_numpy(np.ascontiguousarray(L.c)).pin_memory()
             h2d += sum(x.numel() * 4 for x in t[:3]) + c.numel() * 8
             hl.append((L.icase, L.itype, L.kpol, *[x.numpy() for x in t], c.numpy()))
-        hout = torch.empty(w.iicc * a.ms * a.ms, dtype=torch.float64).pin_memory()
+        # the output in page-locked huge pages (dbsrg_host_alloc)
+        from dbsr_gb300.api import HostMatrix
+
+        hbuf = HostMatrix(w.iicc * a.ms * a.ms)
+        hout = torch.from_numpy(hbuf.array)
         hacf = torch.empty(w.iicc * (w.mk + 1), dtype=torch.float64).pin_memory()
         nwin = (w.iicc + a.get_tuning("windows") - 1) // a.get_tuning("windows")
 
@@ -1074,12 +1083,14 @@ def main():
         q = hout.numel() - (4 << 30) // 8
         into = [d2h_gbs(torch, dev, dst=hout), d2h_gbs(torch, dev, dst=hout[q:])]
         del hout
+        hbuf.close()
         torch.cuda.empty_cache()
         link = d2h_gbs(torch, dev)
         e2e = {"value": world * fl["total"] / dte / 1e9, "unit": "GFLOP/s",
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": d2h,
                "s_per_matrix": dte, "s_per_matrix_samples": e2e_samples,
                "statistic": "median of 5 single-step samples",
+               "host_output": "dbsrg_host_alloc: page-locked, transparent huge pages",
                "api": "dbsrg_assemble_to_host",
                "windows": npass, "window_blocks": nwin, "d2h_gbs_measured": link,
                "d2h_gbs_into_output_first_last": into,

@@ -606,6 +606,35 @@ def gen_batch(assemblers, lists_per_assembler):
         check(None, rc, "gen_batch")
 
 
+class HostMatrix:
+    """dbsrg_host_alloc: n float64 values of page-locked host memory in huge
+    pages, zeroed, for a matrix the device writes (the `out` of
+    Assembler.assemble_to_host, the `stage` of assemble_streamed).  `array`
+    is the numpy view; the memory is returned by close() or when the object
+    is collected, so keep the object while the array is in use."""
+
+    def __init__(self, n: int):
+        self._L = load()
+        self.nbytes = int(n) * 8
+        p = C.c_void_p()
+        check(None, self._L.dbsrg_host_alloc(C.c_size_t(self.nbytes), C.byref(p)), "host_alloc")
+        self._p = p
+        buf = (C.c_char * self.nbytes).from_address(p.value)
+        self.array = np.frombuffer(buf, dtype=np.float64, count=int(n))
+
+    def close(self):
+        if self._p is not None:
+            self.array = None
+            self._L.dbsrg_host_free(self._p)
+            self._p = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def gen_batch_streamed(assemblers, lists_per_assembler, consumer):
     """dbsrg_gen_batch_streamed: the assemblers (each allocated with a block
     window) run their lists once per window, concurrently; after every window

@@ -6,6 +6,10 @@
 #include <mutex>
 #include <new>
 #include <thread>
+#include <vector>
+
+#include <sys/mman.h>
+#include <unistd.h>
 
 #include "internal.cuh"
 
@@ -236,6 +240,16 @@ static void free_tables(dbsrg_ctx *c) {
   c->quad.clear();
   c->rcell.clear();
   c->scell.clear();
+}
+
+// the mappings of dbsrg_host_alloc and their lengths
+static std::mutex &host_mu() {
+  static std::mutex m;
+  return m;
+}
+static std::map<void *, size_t> &host_sizes() {
+  static std::map<void *, size_t> m;
+  return m;
 }
 
 extern "C" {
@@ -839,6 +853,70 @@ int dbsrg_assemble_streamed_host(dbsrg_ctx *c, int nlists, const dbsrg_list *lis
   const int rh = hand();  // the last window
   if (rh) return rh;
   if (acf_host) return copy_out(c, acf_host, c->acf, sizeof(double) * (size_t)iicc * (c->mk + 1));
+  return DBSRG_OK;
+}
+
+int dbsrg_host_alloc(size_t bytes, void **out) {
+  if (!out || bytes == 0) return DBSRG_EINVAL;
+  *out = nullptr;
+  // the transparent huge page size of the kernel (2 MB with 4 KB pages,
+  // 512 MB with 64 KB pages); the mapping is over-allocated by one huge
+  // page and trimmed so that it starts on a huge-page boundary
+  size_t hp = 2u << 20;
+  if (FILE *f = fopen("/sys/kernel/mm/transparent_hugepage/hpage_pmd_size", "r")) {
+    unsigned long long v = 0;
+    if (fscanf(f, "%llu", &v) == 1 && v >= 4096 && (v & (v - 1)) == 0) hp = (size_t)v;
+    fclose(f);
+  }
+  const size_t page = (size_t)sysconf(_SC_PAGESIZE);
+  const size_t len = (bytes + page - 1) / page * page;
+  char *raw = (char *)mmap(nullptr, len + hp, PROT_READ | PROT_WRITE,
+                           MAP_PRIVATE | MAP_ANONYMOUS, -1, 0);
+  if (raw == MAP_FAILED) return DBSRG_ENOMEM;
+  char *p = (char *)(((uintptr_t)raw + hp - 1) / hp * hp);
+  if (p > raw) munmap(raw, (size_t)(p - raw));
+  const size_t tail = (size_t)(raw + len + hp - (p + len));
+  if (tail) munmap(p + len, tail);
+#ifdef MADV_HUGEPAGE
+  madvise(p, len, MADV_HUGEPAGE);  // advisory: small pages if refused
+#endif
+  // touch (zero) the pages from several threads, in huge-page pieces
+  const unsigned nth = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  const size_t npiece = (len + hp - 1) / hp;
+  std::vector<std::thread> th;
+  for (unsigned t = 0; t < nth; t++)
+    th.emplace_back([=]() {
+      for (size_t q = t; q < npiece; q += nth) {
+        const size_t a = q * hp, b = std::min(len, a + hp);
+        std::memset(p + a, 0, b - a);
+      }
+    });
+  for (auto &x : th) x.join();
+  if (cudaHostRegister(p, len, cudaHostRegisterDefault) != cudaSuccess) {
+    cudaGetLastError();
+    munmap(p, len);
+    return DBSRG_ENOMEM;
+  }
+  {
+    std::lock_guard<std::mutex> lk(host_mu());
+    host_sizes()[p] = len;
+  }
+  *out = p;
+  return DBSRG_OK;
+}
+
+int dbsrg_host_free(void *p) {
+  if (!p) return DBSRG_OK;
+  size_t len = 0;
+  {
+    std::lock_guard<std::mutex> lk(host_mu());
+    auto it = host_sizes().find(p);
+    if (it == host_sizes().end()) return DBSRG_EINVAL;
+    len = it->second;
+    host_sizes().erase(it);
+  }
+  cudaHostUnregister(p);
+  munmap(p, len);
   return DBSRG_OK;
 }
 

@@ -209,6 +209,18 @@ int dbsrg_assemble_streamed_host(dbsrg_ctx *ctx, int nlists,
                                  double *stage, dbsrg_window_fn fn,
                                  void *user, double *acf_host);
 
+/* Page-locked host memory for a matrix that the device writes (the hch_host
+ * of dbsrg_assemble_to_host, the stage of dbsrg_assemble_streamed_host):
+ * an anonymous mapping aligned to the kernel's transparent huge page size
+ * with huge pages requested, zeroed by several host threads and registered
+ * with the CUDA driver.  Copies from the device into 64 KB pages of a
+ * matrix of tens of GB ran at two speeds from one run to the next; into
+ * huge pages they run at the link's rate.  *out receives the address;
+ * DBSRG_ENOMEM when the mapping or the registration fails.  Free with
+ * dbsrg_host_free.  No counterpart in DBSR_MAT3. */
+int dbsrg_host_alloc(size_t bytes, void **out);
+int dbsrg_host_free(void *p);
+
 /* UPDATE_HX(ich,jch,d,C) (updates.f90:79-106): add C*d (d is ms x ms,
  * host or device) to the block of channel pair (ich,jch). */
 int dbsrg_update_hx(dbsrg_ctx *ctx, int ich, int jch, const double *d,

@@ -213,3 +213,27 @@ def test_assemble_streamed_needs_two_windows():
     a.assemble_streamed(items(w), stage, lambda blo, nb, v: parts.append(np.array(v)), nwin=2)
     a.close()
     assert np.array_equal(np.concatenate(parts, axis=2), full(w, SPLIT_BF16)[0])
+
+
+def test_host_matrix_destination():
+    """dbsrg_host_alloc memory (page-locked, huge pages, zeroed) as the
+    destination of dbsrg_assemble_to_host; dbsrg_host_free of an address it
+    did not allocate is refused."""
+    import ctypes as C
+
+    from dbsr_gb300._lib import load
+    from dbsr_gb300.api import HostMatrix
+
+    w = synth.small(ns=60, nch=5, mk=3, n_entries=2000, seed=58)
+    h0, acf0 = full(w, SPLIT_BF16)
+    a = make(w, SPLIT_BF16)
+    hm = HostMatrix(h0.size)
+    assert hm.array.shape == (h0.size,) and not hm.array.any()
+    out, acf = a.assemble_to_host(items(w), out=hm.array, nwin=3)
+    assert np.array_equal(hm.array.reshape(h0.shape, order="F"), h0)
+    assert np.array_equal(acf, acf0)
+    a.close()
+    hm.close()
+    hm.close()
+    x = np.zeros(16)
+    assert load().dbsrg_host_free(C.c_void_p(x.ctypes.data)) == -1
