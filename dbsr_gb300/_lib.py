@@ -89,6 +89,9 @@ SIGNATURES = [
     ("dbsrg_assemble_to_host", C.c_int, [_vp, C.c_int, _vp, C.c_int, _vp, _vp]),
     ("dbsrg_assemble_streamed_host", C.c_int, [_vp, C.c_int, _vp, C.c_int, _vp, _vp, _vp, _vp]),
     ("dbsrg_host_alloc", C.c_int, [C.c_size_t, _vp]),
+    ("dbsrg_graph_capture", C.c_int, [_vp, C.c_int, _vp]),
+    ("dbsrg_graph_launch", C.c_int, [_vp, _vp]),
+    ("dbsrg_graph_release", C.c_int, [_vp]),
     ("dbsrg_host_free", C.c_int, [_vp]),
     ("dbsrg_backward", C.c_int, [_vp, C.c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     ("dbsrg_alloc_perturbers", C.c_int, [_vp, C.c_int, _vp, C.c_int, _vp, C.c_int]),

@@ -180,6 +180,23 @@ class Assembler:
         check(self._h, rc, "assemble_streamed")
         return acf
 
+    def graph_capture(self, lists):
+        """dbsrg_graph_capture: every list (icase, itype, kpol, k1, k2, k3, k4,
+        cdata[, ipt]) planned, the whole assembly (table builds included)
+        captured as one CUDA graph and run once."""
+        arr, keep, counts = _list_descs([lists])
+        check(self._h, self._L.dbsrg_graph_capture(self._h, counts[0], arr), "graph_capture")
+
+    def graph_launch(self, pq=None):
+        """dbsrg_graph_launch: the captured assembly again, from new orbitals
+        pq(ns,2,nbf) (same count and channels) or the orbitals held."""
+        p, keep = (None, None) if pq is None else _ptr(
+            pq if hasattr(pq, "data_ptr") else np.asfortranarray(pq, dtype=np.float64), np.float64)
+        check(self._h, self._L.dbsrg_graph_launch(self._h, p), "graph_launch")
+
+    def graph_release(self):
+        check(self._h, self._L.dbsrg_graph_release(self._h), "graph_release")
+
     def set_window(self, blo: int):
         """Hold (and zero) blocks blo .. blo + window - 1."""
         check(self._h, self._L.dbsrg_set_window(self._h, int(blo)), "set_window")

@@ -1232,3 +1232,137 @@ int assemble_windows(dbsrg_ctx *c, int nlists, const dbsrg_list *lists, int nwin
   c->wcap = wcap0;
   return rc ? rc : rd;
 }
+
+// ---------------------------------------------------------------------------
+// A whole assembly captured as one CUDA graph (dbsrg_graph_capture): every
+// list is planned first (segments and chunks need the list read back, which
+// a graph cannot do), the cached tables and orbital products are dropped,
+// and then the zeroing of the matrix, the builds of every table, pair
+// potential and digit operand the lists read, and every contraction and
+// scatter are captured from the contraction stream (the table streams join
+// through the events of prepare_list).  A replay repeats all of that from
+// the orbitals in the context's orbital buffer.
+struct GraphState {
+  std::vector<ListPlan> plans;
+  std::vector<void *> mem;
+  cudaGraphExec_t exec = nullptr;
+  long long launches = 0;
+};
+
+void graph_drop(dbsrg_ctx *c) {
+  GraphState *g = c->graph;
+  if (!g) return;
+  c->graph = nullptr;
+  // a replay may be running: its plan memory goes back to the pool only
+  // once the stream is idle
+  cudaStreamSynchronize(c->stream);
+  if (g->exec) cudaGraphExecDestroy(g->exec);
+  for (void *p : g->mem) cache_free(c, p);
+  delete g;
+}
+
+int graph_capture(dbsrg_ctx *c, int nlists, const dbsrg_list *lists) {
+  graph_drop(c);
+  if (!c->hch) return set_err(c, DBSRG_ESTATE, "no matrix allocated");
+  if (!c->pq) return set_err(c, DBSRG_ESTATE, "no orbitals set");
+  if (c->hcap < c->iicc) return set_err(c, DBSRG_ESTATE, "graph capture needs the whole matrix");
+  if (c->timing) return set_err(c, DBSRG_ESTATE, "graph capture with timing on");
+  int rc = drain(c);
+  if (rc) return rc;
+  free_tables(c);  // rebuilt inside the graph (the buffers stay pooled)
+  GraphState *g = new (std::nothrow) GraphState();
+  if (!g) return set_err(c, DBSRG_ENOMEM, "graph state");
+  g->plans.resize((size_t)nlists);
+  g->mem.assign((size_t)nlists, nullptr);
+  const double *hch0 = c->hch;
+  c->hch = c->hmem;
+  c->wlo = 1;
+  auto fail = [&](int r) {
+    for (void *p : g->mem) cache_free(c, p);
+    delete g;
+    c->hch = const_cast<double *>(hch0);
+    return r;
+  };
+  for (int l = 0; l < nlists; l++) {
+    const dbsrg_list &L = lists[l];
+    if (L.ncdata < 0) return fail(set_err(c, DBSRG_EINVAL, "ncdata < 0"));
+    if (L.ncdata == 0) continue;
+    if (!L.k1 || !L.k2 || !L.k3 || !L.cdata)
+      return fail(set_err(c, DBSRG_EINVAL, "null list pointer"));
+    if (!(g->mem[l] = cache_alloc(c, plan_bytes(c, L.icase, L.itype, L.ncdata))))
+      return fail(set_err(c, DBSRG_ENOMEM, "list state allocation failed"));
+    if ((rc = plan_list(c, L.icase, L.itype, L.kpol, L.ncdata, L.ipt, L.k1, L.k2, L.k3, L.k4,
+                        L.cdata, 1, c->iicc, 1, g->mem[l], c->sstream, g->plans[l])))
+      return fail(rc);
+  }
+  DBSRG_TRY(c, cudaStreamSynchronize(c->sstream));
+  const long long l0 = c->launches;
+  DBSRG_TRY(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed));
+  rc = DBSRG_OK;
+  {
+    const size_t blk = (size_t)c->g.ms * c->g.ms;
+    cudaError_t e = cudaMemsetAsync(c->hmem, 0, sizeof(double) * blk * c->iicc, c->stream);
+    if (e == cudaSuccess)
+      e = cudaMemsetAsync(c->acf, 0, sizeof(double) * (size_t)c->iicc * (c->mk + 1), c->stream);
+    if (e != cudaSuccess) rc = cuda_check(c, e, "graph zeroing");
+  }
+  if (!rc) rc = zero_structures(c);
+  // both table streams join the capture here (a list without table builds,
+  // such as an overlap list first, would leave them outside it)
+  for (int b = 0; b < 2 && !rc; b++) {
+    cudaError_t e = cudaEventRecord(c->sready, c->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(c->bstream[b], c->sready, 0);
+    if (e != cudaSuccess) rc = cuda_check(c, e, "graph fork");
+  }
+  bool prepared = false;
+  for (int l = 0; l < nlists && !rc; l++) {
+    if (lists[l].ncdata <= 0) continue;
+    if ((rc = prepare_list(c, g->plans[l], prepared))) break;
+    prepared = true;
+    rc = exec_list(c, g->plans[l], 0);
+  }
+  // both table streams back into the contraction stream (one of them may
+  // have joined the capture without work after its last join)
+  for (int b = 0; b < 2 && !rc; b++) {
+    cudaError_t e = cudaEventRecord(c->tready[b], c->bstream[b]);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(c->stream, c->tready[b], 0);
+    if (e != cudaSuccess) rc = cuda_check(c, e, "graph join");
+  }
+  cudaGraph_t graph = nullptr;
+  const cudaError_t ee = cudaStreamEndCapture(c->stream, &graph);
+  if (!rc && ee != cudaSuccess) rc = cuda_check(c, ee, "graph capture");
+  if (!rc) {
+    const cudaError_t ei = cudaGraphInstantiate(&g->exec, graph, 0);
+    if (ei != cudaSuccess) rc = cuda_check(c, ei, "graph instantiate");
+  }
+  if (graph) cudaGraphDestroy(graph);
+  c->stream_built = false;
+  if (rc) {
+    cudaGetLastError();
+    if (g->exec) cudaGraphExecDestroy(g->exec);
+    g->exec = nullptr;
+    free_tables(c);  // whatever the capture cached was never computed
+    return fail(rc);
+  }
+  g->launches = c->launches - l0;
+  c->launches = l0;
+  c->hch = const_cast<double *>(hch0);
+  c->graph = g;
+  return DBSRG_OK;
+}
+
+int graph_launch(dbsrg_ctx *c, const double *pq) {
+  GraphState *g = c->graph;
+  if (!g) return set_err(c, DBSRG_ESTATE, "no captured assembly");
+  if (pq) {
+    int rc = copy_in(c, c->pq, pq, sizeof(double) * 2 * (size_t)c->g.ns * c->nbf);
+    if (rc) return rc;
+  }
+  DBSRG_TRY(c, cudaGraphLaunch(g->exec, c->stream));
+  c->launches += g->launches;
+  if (c->async) {
+    c->pending = true;
+    return DBSRG_OK;
+  }
+  return drain(c);
+}

@@ -101,15 +101,20 @@ int copy_out(dbsrg_ctx *c, void *dst, const void *src, size_t n) {
   return DBSRG_OK;
 }
 
-static int grow(dbsrg_ctx *c, void **p, size_t *have, size_t bytes) {
+// A scratch buffer that must grow: queued work may still read the old one,
+// so it is retired (freed when the context is destroyed or its memory
+// trimmed) rather than freed -- growing waits for nothing, neither the
+// context's streams nor (through cudaFree) the whole device -- and the new
+// one is at least twice the old one, which bounds the retired memory by
+// the final size.
+int grow_buffer(dbsrg_ctx *c, void **p, size_t *have, size_t bytes) {
   if (*have >= bytes) return DBSRG_OK;
+  size_t want = std::max(bytes + bytes / 4, 2 * *have);
   if (*p) {
-    cudaStreamSynchronize(c->stream);
-    cudaFree(*p);
+    c->retired.push_back(*p);
     *p = nullptr;
     *have = 0;
   }
-  size_t want = bytes + bytes / 4;
   cudaError_t e = cudaMalloc(p, want);
   if (e != cudaSuccess) {
     cudaGetLastError();
@@ -125,19 +130,19 @@ static int grow(dbsrg_ctx *c, void **p, size_t *have, size_t bytes) {
 }
 
 int ensure_scratch(dbsrg_ctx *c, size_t bytes) {
-  return grow(c, &c->scratch, &c->scratch_bytes, bytes);
+  return grow_buffer(c, &c->scratch, &c->scratch_bytes, bytes);
 }
 int ensure_scratch2(dbsrg_ctx *c, size_t bytes) {
-  return grow(c, &c->scratch2, &c->scratch2_bytes, bytes);
+  return grow_buffer(c, &c->scratch2, &c->scratch2_bytes, bytes);
 }
 int ensure_tscratch(dbsrg_ctx *c, size_t bytes) {
-  return grow(c, &c->tscratch, &c->tscratch_bytes, bytes);
+  return grow_buffer(c, &c->tscratch, &c->tscratch_bytes, bytes);
 }
 int ensure_tcscratch(dbsrg_ctx *c, size_t bytes) {
-  return grow(c, &c->tcscratch, &c->tcscratch_bytes, bytes);
+  return grow_buffer(c, &c->tcscratch, &c->tcscratch_bytes, bytes);
 }
 int ensure_pscratch(dbsrg_ctx *c, int which, size_t bytes) {
-  return grow(c, &c->pscratch[which], &c->pscratch_bytes[which], bytes);
+  return grow_buffer(c, &c->pscratch[which], &c->pscratch_bytes[which], bytes);
 }
 void *cache_alloc(dbsrg_ctx *c, size_t bytes) {
   auto it = c->pool.find(bytes);
@@ -169,15 +174,23 @@ void cache_free(dbsrg_ctx *c, void *p) {
 }
 
 void pool_trim(dbsrg_ctx *c) {
-  if (!c->pool.empty()) cudaStreamSynchronize(c->stream);
+  graph_drop(c);
+  if (!c->pool.empty() || !c->retired.empty()) {
+    // the pooled and retired buffers may be named by queued work on any of
+    // the context's streams
+    if (c->sstream) cudaStreamSynchronize(c->sstream);
+    for (cudaStream_t b : c->bstream)
+      if (b) cudaStreamSynchronize(b);
+    cudaStreamSynchronize(c->stream);
+  }
   for (auto &kv : c->pool) cudaFree(kv.second);
   c->pool.clear();
+  for (void *p : c->retired) cudaFree(p);
+  c->retired.clear();
 }
 
 int ensure_lstate(dbsrg_ctx *c, int par, size_t bytes) {
-  if (c->lstate_bytes[par] >= bytes) return DBSRG_OK;
-  if (c->lstate[par]) DBSRG_TRY(c, cudaStreamSynchronize(c->sstream));
-  return grow(c, &c->lstate[par], &c->lstate_bytes[par], bytes);
+  return grow_buffer(c, &c->lstate[par], &c->lstate_bytes[par], bytes);
 }
 bool sync_check_enabled() {
   // read once; the initialisation of a function-local static is thread-safe
@@ -217,7 +230,8 @@ static void timing_clear(dbsrg_ctx *c) {
   c->tev.clear();
 }
 
-static void free_tables(dbsrg_ctx *c) {
+void free_tables(dbsrg_ctx *c) {
+  graph_drop(c);
   for (double *p : c->rtab)
     cache_free(c, p);
   for (double *p : c->stab)
@@ -497,6 +511,7 @@ int dbsrg_set_orbitals(dbsrg_ctx *c, int nbf, const double *pq, const int *ipbs)
   if (!c || nbf < 1 || !pq || !ipbs) return set_err(c, DBSRG_EINVAL, "bad orbital arguments");
   cudaSetDevice(c->device);
   SETTLE(c);
+  graph_drop(c);
   if (c->pq) cudaFree(c->pq);
   if (c->ipbs) cudaFree(c->ipbs);
   c->pq = nullptr;
@@ -550,6 +565,7 @@ int dbsrg_alloc_matrix_window(dbsrg_ctx *c, int nch, const int *icc, int iicc, i
     return set_err(c, DBSRG_EINVAL, "bad matrix arguments");
   cudaSetDevice(c->device);
   SETTLE(c);
+  graph_drop(c);
   if (c->icc) cudaFree(c->icc);
   if (c->hmem) cudaFree(c->hmem);
   if (c->acf) cudaFree(c->acf);
@@ -917,6 +933,38 @@ int dbsrg_host_free(void *p) {
   }
   cudaHostUnregister(p);
   munmap(p, len);
+  return DBSRG_OK;
+}
+
+int dbsrg_graph_capture(dbsrg_ctx *c, int nlists, const dbsrg_list *lists) {
+  if (!c) return DBSRG_EINVAL;
+  if (nlists < 0 || (nlists > 0 && !lists))
+    return set_err(c, DBSRG_EINVAL, "graph_capture: bad arguments");
+  cudaSetDevice(c->device);
+  SETTLE(c);
+  const bool async = c->async;
+  int rc = graph_capture(c, nlists, lists);
+  if (rc) return rc;
+  // the first replay: the cached tables the capture set up hold values only
+  // once the graph has run
+  c->async = false;
+  rc = graph_launch(c, nullptr);
+  c->async = async;
+  return rc;
+}
+
+int dbsrg_graph_launch(dbsrg_ctx *c, const double *pq) {
+  if (!c) return DBSRG_EINVAL;
+  cudaSetDevice(c->device);
+  SETTLE(c);
+  return graph_launch(c, pq);
+}
+
+int dbsrg_graph_release(dbsrg_ctx *c) {
+  if (!c) return DBSRG_EINVAL;
+  cudaSetDevice(c->device);
+  SETTLE(c);
+  graph_drop(c);
   return DBSRG_OK;
 }
 

@@ -812,24 +812,7 @@ __global__ void k_scatter_dp(int ns, int ks, char sym, QuadSpec sp, KdSet kd,
 }  // namespace
 
 int ensure_fscratch(dbsrg_ctx *c, size_t bytes) {
-  if (c->fscratch_bytes >= bytes) return DBSRG_OK;
-  if (c->fscratch) {
-    cudaStreamSynchronize(c->stream);
-    cudaFree(c->fscratch);
-    c->fscratch = nullptr;
-    c->fscratch_bytes = 0;
-  }
-  size_t want = bytes + bytes / 4;
-  if (cudaMalloc(&c->fscratch, want) != cudaSuccess) {
-    cudaGetLastError();
-    if (cudaMalloc(&c->fscratch, bytes) != cudaSuccess) {
-      c->fscratch = nullptr;
-      return set_err(c, DBSRG_ENOMEM, "factor scratch allocation failed");
-    }
-    want = bytes;
-  }
-  c->fscratch_bytes = want;
-  return DBSRG_OK;
+  return grow_buffer(c, &c->fscratch, &c->fscratch_bytes, bytes);
 }
 
 int pair_index(dbsrg_ctx *c, int n, const int *k2, const int *k3, int *pairs, int *derr,
@@ -1067,6 +1050,7 @@ static int get_pairpot_band(dbsrg_ctx *c, int family, int type, int k, int cs, i
 }
 
 void free_orbital_products(dbsrg_ctx *c) {
+  graph_drop(c);
   if (!c->rfar.empty() || !c->sfar.empty() || !c->ppot.empty() || c->brows || !c->ffc.empty())
     cudaStreamSynchronize(c->stream);
   for (auto *v : {&c->rfar, &c->sfar})

@@ -181,6 +181,13 @@ struct dbsrg_ctx {
   // allocation failures return the pool to the device
   std::multimap<size_t, void *> pool;
   std::map<void *, size_t> psize;
+  // scratch buffers replaced by larger ones while queued work could still
+  // read them (grow_buffer); freed with the pool
+  std::vector<void *> retired;
+  // a captured whole assembly (dbsrg_graph_capture), replayed by
+  // dbsrg_graph_launch; dropped by every call that frees or replaces memory
+  // it names
+  struct GraphState *graph = nullptr;
   // error word of the tensor-core kernels (bounded waits), read whenever the
   // context waits for its stream
   int *kerr = nullptr;
@@ -296,6 +303,9 @@ void cache_free(dbsrg_ctx *c, void *p);
 void pool_trim(dbsrg_ctx *c);
 int copy_out(dbsrg_ctx *c, void *dst, const void *src, size_t n);
 // scratch arenas (device)
+// grows a scratch buffer to at least bytes; the old one is retired, not
+// freed (queued work may still use it)
+int grow_buffer(dbsrg_ctx *c, void **p, size_t *have, size_t bytes);
 int ensure_scratch(dbsrg_ctx *c, size_t bytes);
 int ensure_scratch2(dbsrg_ctx *c, size_t bytes);
 int ensure_tscratch(dbsrg_ctx *c, size_t bytes);
@@ -308,6 +318,14 @@ int ensure_pinned(dbsrg_ctx *c, size_t bytes);
 // frees the far-field vectors, pair potentials and bound rows (they depend
 // on the orbitals and the tables)
 void free_orbital_products(dbsrg_ctx *c);
+// the cached tables and orbital products back to the pool (capi.cu)
+void free_tables(dbsrg_ctx *c);
+// captured whole assembly (assemble.cu): capture (plans every list, then
+// captures the table builds and contractions from the contraction stream),
+// replay with the orbitals optionally replaced (same size), drop
+int graph_capture(dbsrg_ctx *c, int nlists, const dbsrg_list *lists);
+int graph_launch(dbsrg_ctx *c, const double *pq);
+void graph_drop(dbsrg_ctx *c);
 // handles of the channel basis (basis.cu)
 void basis_release(dbsrg_ctx *c);
 // float-float copy of n doubles at src (cached until the orbital products go)

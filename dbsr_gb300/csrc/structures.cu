@@ -995,6 +995,7 @@ int dbsrg_alloc_perturbers(dbsrg_ctx *c, int npert, const int *icb, int iicb, co
     return set_err(c, DBSRG_EINVAL, "bad perturber arguments");
   cudaSetDevice(c->device);
   ST_SETTLE(c);
+  graph_drop(c);  // frees memory a captured assembly names
   for (double **p : {&c->hcp, &c->hp}) {
     if (*p) cudaFree(*p);
     *p = nullptr;
@@ -1040,6 +1041,7 @@ int dbsrg_set_targets(dbsrg_ctx *c, int ntarg, const int *iptar, int iitar, int 
   if (ntarg < 0 || (ntarg > 0 && !iptar)) return set_err(c, DBSRG_EINVAL, "bad target arguments");
   cudaSetDevice(c->device);
   ST_SETTLE(c);
+  graph_drop(c);  // frees memory a captured assembly names
   for (double **p : {&c->htarg, &c->otarg}) {
     if (*p) cudaFree(*p);
     *p = nullptr;
@@ -1083,6 +1085,7 @@ int dbsrg_set_dhl(dbsrg_ctx *c, int nkap, const int *kap_list, const double *hd,
     return set_err(c, DBSRG_EINVAL, "bad one-electron arguments");
   cudaSetDevice(c->device);
   ST_SETTLE(c);
+  graph_drop(c);  // frees memory a captured assembly names
   if (c->hd) cudaFree(c->hd);
   c->hd = nullptr;
   c->nkap = 0;

@@ -209,6 +209,31 @@ int dbsrg_assemble_streamed_host(dbsrg_ctx *ctx, int nlists,
                                  double *stage, dbsrg_window_fn fn,
                                  void *user, double *acf_host);
 
+/* A whole assembly captured as one CUDA graph, for matrices rebuilt many
+ * times from the same lists with new orbitals (SCF iterations, scans over
+ * orbital parameters).  dbsrg_graph_capture plans every list (segments and
+ * chunks, which read the lists back to the host), drops the cached tables,
+ * captures the zeroing of the matrix, acf and the perturber and target
+ * parts, every table, pair-potential and digit build and every
+ * contraction and scatter into one graph, and runs it once: the matrix
+ * then equals the one dbsrg_gen_matrix gives for the same lists.  The
+ * lists' arrays are read during the call only.  dbsrg_graph_launch(ctx,
+ * pq) runs the graph again, after copying pq(ns,2,nbf) (host or device,
+ * the orbitals' count and ipbs unchanged; NULL: the orbitals held) into
+ * the context: every table and orbital product is rebuilt and the matrix
+ * assembled anew, equal to what dbsrg_set_orbitals and dbsrg_gen_matrix
+ * would give.  A replay repeats the capture's precision, tuning and
+ * matrix parts.  The whole matrix must be allocated (no window).  The
+ * graph is dropped by dbsrg_graph_release and by every call that frees
+ * or replaces memory it names: dbsrg_set_orbitals, dbsrg_alloc_matrix*,
+ * dbsrg_alloc_perturbers, dbsrg_set_targets, dbsrg_set_dhl,
+ * dbsrg_invalidate_tables, dbsrg_release_tables, dbsrg_destroy; after
+ * that dbsrg_graph_launch returns DBSRG_ESTATE.  No counterpart in
+ * DBSR_MAT3, which builds each matrix once. */
+int dbsrg_graph_capture(dbsrg_ctx *ctx, int nlists, const dbsrg_list *lists);
+int dbsrg_graph_launch(dbsrg_ctx *ctx, const double *pq);
+int dbsrg_graph_release(dbsrg_ctx *ctx);
+
 /* Page-locked host memory for a matrix that the device writes (the hch_host
  * of dbsrg_assemble_to_host, the stage of dbsrg_assemble_streamed_host):
  * an anonymous mapping aligned to the kernel's transparent huge page size
