@@ -54,6 +54,7 @@ def parse():
     p.add_argument("--scale", type=float, default=1.0, help="fraction of the 2e6 entries")
     p.add_argument("--nch", type=int, default=120)
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-graph", action="store_true", help="skip the captured-graph replays")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU sample")
     p.add_argument("--workload", default="config1",
@@ -968,6 +969,25 @@ def main():
     fl = synth.algorithmic_flops(w)
     value = world * fl["total"] / dt / 1e9
 
+    # the same assembly captured as one CUDA graph (dbsrg_graph_capture) and
+    # replayed: every table and orbital product rebuilt, the matrix zeroed
+    # and assembled; the lists' planning happens once, in the capture
+    graph = None
+    if not args.no_graph and args.precision != "plain":
+        a.set_async(False)
+        t0 = time.perf_counter()
+        a.graph_capture(dl)
+        cap_s = time.perf_counter() - t0
+        a.graph_launch()
+        g0 = a.launches
+        dtg = timed(a.graph_launch, max(3, args.steps))
+        graph = {"s_per_matrix": dtg, "value": world * fl["total"] / dtg / 1e9,
+                 "unit": "GFLOP/s", "capture_and_first_run_s": cap_s,
+                 "launches_per_replay": (a.launches - g0) // max(3, args.steps),
+                 "api": "dbsrg_graph_capture + dbsrg_graph_launch"}
+        a.graph_release()
+        a.set_async(True)
+
     # per-kernel device time of one instrumented step (outside the timed region)
     a.timing(True)
     step(dl)
@@ -1136,6 +1156,7 @@ def main():
             "roofline": roofline,
             "cpu_baseline": cpu,
             "e2e": e2e,
+            "graph_replay": graph,
             "clocks": clocks,
             "gpu_launches": int(launches),
             "kernel_ms": {k: round(v[1], 3) for k, v in sorted(rep.items(), key=lambda kv: -kv[1][1])},
