@@ -1275,12 +1275,17 @@ int graph_capture(dbsrg_ctx *c, int nlists, const dbsrg_list *lists) {
   g->plans.resize((size_t)nlists);
   g->mem.assign((size_t)nlists, nullptr);
   const double *hch0 = c->hch;
+  const int wlo0 = c->wlo;
   c->hch = c->hmem;
   c->wlo = 1;
+  auto restore = [&]() {
+    c->hch = const_cast<double *>(hch0);
+    c->wlo = wlo0;
+  };
   auto fail = [&](int r) {
     for (void *p : g->mem) cache_free(c, p);
     delete g;
-    c->hch = const_cast<double *>(hch0);
+    restore();
     return r;
   };
   for (int l = 0; l < nlists; l++) {
@@ -1346,7 +1351,7 @@ int graph_capture(dbsrg_ctx *c, int nlists, const dbsrg_list *lists) {
   }
   g->launches = c->launches - l0;
   c->launches = l0;
-  c->hch = const_cast<double *>(hch0);
+  restore();
   c->graph = g;
   return DBSRG_OK;
 }
